@@ -1,0 +1,512 @@
+// C harness over the reference PhysX immediate-mode API, compiled together with
+// the reference's own sources by oracle/ref/Makefile into oracle/_ref/libpxref.so.
+//
+// Test infrastructure only: Python loads it with ctypes to produce golden
+// fixtures and to pin the CPU restatement in oracle/port.  Every entry point
+// is a thin adapter: plain arrays in, the reference function called exactly as
+// its canonical caller (the immediate-mode snippet) calls it, plain arrays out.
+//
+// Layout conventions shared with the rest of the repository:
+//   pose    = 7 floats  (qx, qy, qz, qw, px, py, pz)          -- PxTransform
+//   geom    = type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box) +
+//             4 floats (sphere: r; capsule: r, halfHeight; box: hx, hy, hz)
+//   contact = 8 floats  (nx, ny, nz, separation, px, py, pz, 0)
+#include "PxImmediateMode.h"
+#include "PxBroadPhase.h"
+#include "foundation/PxFoundation.h"
+#include "foundation/PxPhysicsVersion.h"
+#include "foundation/PxAllocatorCallback.h"
+#include "foundation/PxErrorCallback.h"
+#include "geometry/PxSphereGeometry.h"
+#include "geometry/PxPlaneGeometry.h"
+#include "geometry/PxCapsuleGeometry.h"
+#include "geometry/PxBoxGeometry.h"
+#include "geomutils/PxContactPoint.h"
+#include "collision/PxCollisionDefs.h"
+#include "solver/PxSolverDefs.h"
+
+#include <cstdlib>
+#include <cstring>
+#include <cstdio>
+#include <vector>
+#include <map>
+#include <utility>
+
+using namespace physx;
+using namespace physx::immediate;
+
+#define HX extern "C" __attribute__((visibility("default")))
+
+namespace
+{
+struct HAlloc : PxAllocatorCallback
+{
+	void* allocate(size_t size, const char*, const char*, int) override
+	{
+		void* p = nullptr;
+		if(posix_memalign(&p, 16, size ? size : 16)) return nullptr;
+		return p;
+	}
+	void deallocate(void* ptr) override { free(ptr); }
+};
+struct HErr : PxErrorCallback
+{
+	void reportError(PxErrorCode::Enum code, const char* message, const char* file, int line) override
+	{
+		fprintf(stderr, "[pxref] error %d: %s (%s:%d)\n", int(code), message, file, line);
+	}
+};
+HAlloc gAlloc;
+HErr gErr;
+PxFoundation* gFoundation = nullptr;
+
+void ensureFoundation()
+{
+	if(!gFoundation)
+		gFoundation = PxCreateFoundation(PX_PHYSICS_VERSION, gAlloc, gErr);
+}
+
+// Bump arena with 16-byte alignment; reset wholesale.
+struct Arena
+{
+	std::vector<PxU8*> blocks;
+	PxU8* cur = nullptr;
+	size_t used = 0, cap = 0;
+	PxU8* alloc(size_t n)
+	{
+		n = (n + 15) & ~size_t(15);
+		if(!cur || used + n > cap)
+		{
+			size_t sz = n > (1u << 20) ? n : (1u << 20);
+			void* p = nullptr;
+			if(posix_memalign(&p, 16, sz)) return nullptr;
+			memset(p, 0, sz);
+			blocks.push_back(static_cast<PxU8*>(p));
+			cur = static_cast<PxU8*>(p);
+			used = 0;
+			cap = sz;
+		}
+		PxU8* r = cur + used;
+		used += n;
+		return r;
+	}
+	void reset()
+	{
+		for(PxU8* b : blocks) free(b);
+		blocks.clear();
+		cur = nullptr;
+		used = cap = 0;
+	}
+	~Arena() { reset(); }
+};
+
+// Cache memory lives two frames, as the PxCacheAllocator contract asks.
+struct FrameCacheAllocator : PxCacheAllocator
+{
+	Arena arenas[2];
+	int frame = 0;
+	PxU8* allocateCacheData(const PxU32 byteSize) override { return arenas[frame & 1].alloc(byteSize); }
+	void nextFrame() { frame++; arenas[frame & 1].reset(); }
+	void resetAll() { arenas[0].reset(); arenas[1].reset(); }
+};
+
+// Constraint rows live until the solve ends; friction data lives two frames.
+struct FrameConstraintAllocator : PxConstraintAllocator
+{
+	Arena rows;
+	Arena friction[2];
+	int frame = 0;
+	PxU8* reserveConstraintData(const PxU32 byteSize) override { return rows.alloc(byteSize); }
+	PxU8* reserveFrictionData(const PxU32 byteSize) override { return friction[frame & 1].alloc(byteSize); }
+	void nextFrame() { rows.reset(); frame++; friction[frame & 1].reset(); }
+};
+
+struct GeomHolder
+{
+	PxSphereGeometry sphere;
+	PxPlaneGeometry plane;
+	PxCapsuleGeometry capsule;
+	PxBoxGeometry box;
+	const PxGeometry* set(int type, const float* p)
+	{
+		switch(type)
+		{
+		case 0: sphere = PxSphereGeometry(p[0]); return &sphere;
+		case 1: plane = PxPlaneGeometry(); return &plane;
+		case 2: capsule = PxCapsuleGeometry(p[0], p[1]); return &capsule;
+		case 3: box = PxBoxGeometry(p[0], p[1], p[2]); return &box;
+		default: return nullptr;
+		}
+	}
+};
+
+PxTransform loadPose(const float* p)
+{
+	return PxTransform(PxVec3(p[4], p[5], p[6]), PxQuat(p[0], p[1], p[2], p[3]));
+}
+
+void storePose(float* o, const PxTransform& t)
+{
+	o[0] = t.q.x; o[1] = t.q.y; o[2] = t.q.z; o[3] = t.q.w;
+	o[4] = t.p.x; o[5] = t.p.y; o[6] = t.p.z;
+}
+
+struct BufferRecorder : PxContactRecorder
+{
+	float* out;
+	PxU32* counts;
+	PxU32 maxPerPair;
+	bool recordContacts(const PxContactPoint* c, PxU32 n, PxU32 index) override
+	{
+		counts[index] = n;
+		for(PxU32 i = 0; i < n && i < maxPerPair; i++)
+		{
+			float* o = out + (size_t(index) * maxPerPair + i) * 8;
+			o[0] = c[i].normal.x; o[1] = c[i].normal.y; o[2] = c[i].normal.z;
+			o[3] = c[i].separation;
+			o[4] = c[i].point.x; o[5] = c[i].point.y; o[6] = c[i].point.z;
+			o[7] = 0.0f;
+		}
+		return true;
+	}
+};
+} // namespace
+
+//////////////////////////////////////////////////////////////////////////////
+// Sizes of the public structures (checked against the GB300 build's mirrors).
+HX int pxref_sizeof(int which)
+{
+	switch(which)
+	{
+	case 0: return int(sizeof(PxRigidBodyData));
+	case 1: return int(sizeof(PxTGSSolverBodyVel));
+	case 2: return int(sizeof(PxTGSSolverBodyTxInertia));
+	case 3: return int(sizeof(PxTGSSolverBodyData));
+	case 4: return int(sizeof(PxSolverConstraintDesc));
+	case 5: return int(sizeof(PxConstraintBatchHeader));
+	case 6: return int(sizeof(PxTGSSolverContactDesc));
+	case 7: return int(sizeof(PxContactPoint));
+	case 8: return int(sizeof(PxCache));
+	case 9: return int(sizeof(PxBounds3));
+	case 10: return int(sizeof(PxBroadPhasePair));
+	case 11: return int(sizeof(PxTransform));
+	default: return -1;
+	}
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// Broadphase: PxCreateBroadPhase(eABP) + update/fetchResults.
+HX void* pxref_bp_create(int discardStaticVsKinematic, int discardKinematicVsKinematic)
+{
+	ensureFoundation();
+	PxBroadPhaseDesc desc(PxBroadPhaseType::eABP);
+	desc.mDiscardStaticVsKinematic = discardStaticVsKinematic != 0;
+	desc.mDiscardKinematicVsKinematic = discardKinematicVsKinematic != 0;
+	return PxCreateBroadPhase(desc);
+}
+
+HX void pxref_bp_release(void* bp)
+{
+	if(bp) static_cast<PxBroadPhase*>(bp)->release();
+}
+
+HX PxU32 pxref_bp_filter_group(int kind, PxU32 id)
+{
+	ensureFoundation();
+	if(kind == 0) return PxGetBroadPhaseStaticFilterGroup();
+	if(kind == 1) return PxGetBroadPhaseKinematicFilterGroup(id);
+	return PxGetBroadPhaseDynamicFilterGroup(id);
+}
+
+// bounds: 6 floats per object (minx miny minz maxx maxy maxz), capacity+1 entries
+// (the reference may read 4 bytes past the last one).
+HX int pxref_bp_update(void* bpv, const PxU32* created, PxU32 nbCreated, const PxU32* updated, PxU32 nbUpdated,
+	const PxU32* removed, PxU32 nbRemoved, const float* bounds, const PxU32* groups, const float* distances, PxU32 capacity,
+	PxU32* outCreated, PxU32 maxCreated, PxU32* nbOutCreated, PxU32* outLost, PxU32 maxLost, PxU32* nbOutLost)
+{
+	PxBroadPhase* bp = static_cast<PxBroadPhase*>(bpv);
+	const PxBroadPhaseUpdateData data(created, nbCreated, updated, nbUpdated, removed, nbRemoved,
+		reinterpret_cast<const PxBounds3*>(bounds), groups, distances, capacity);
+	PxBroadPhaseResults results;
+	bp->update(results, data);
+	*nbOutCreated = results.mNbCreatedPairs;
+	*nbOutLost = results.mNbDeletedPairs;
+	for(PxU32 i = 0; i < results.mNbCreatedPairs && i < maxCreated; i++)
+	{
+		outCreated[2 * i] = results.mCreatedPairs[i].mID0;
+		outCreated[2 * i + 1] = results.mCreatedPairs[i].mID1;
+	}
+	for(PxU32 i = 0; i < results.mNbDeletedPairs && i < maxLost; i++)
+	{
+		outLost[2 * i] = results.mDeletedPairs[i].mID0;
+		outLost[2 * i + 1] = results.mDeletedPairs[i].mID1;
+	}
+	return (results.mNbCreatedPairs <= maxCreated && results.mNbDeletedPairs <= maxLost) ? 0 : 1;
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// Narrowphase: PxGenerateContacts, one pair per call as the snippet does, with
+// a persistent PxCache per pair slot.
+namespace
+{
+struct NpContext
+{
+	std::vector<PxCache> caches;
+	FrameCacheAllocator alloc;
+};
+}
+
+HX void* pxref_np_create(PxU32 nbPairs)
+{
+	ensureFoundation();
+	NpContext* c = new NpContext;
+	c->caches.resize(nbPairs);
+	return c;
+}
+
+HX void pxref_np_release(void* c) { delete static_cast<NpContext*>(c); }
+
+HX void pxref_np_reset(void* cv)
+{
+	NpContext* c = static_cast<NpContext*>(cv);
+	for(PxCache& k : c->caches) k = PxCache();
+	c->alloc.resetAll();
+}
+
+HX int pxref_np_run(void* cv, const int* type0, const float* geom0, const int* type1, const float* geom1,
+	const float* pose0, const float* pose1, PxU32 nbPairs, float contactDistance, float meshContactMargin,
+	float toleranceLength, int freshCaches, float* outContacts, PxU32 maxPerPair, PxU32* outCounts)
+{
+	NpContext* c = static_cast<NpContext*>(cv);
+	if(nbPairs > c->caches.size()) c->caches.resize(nbPairs);
+	c->alloc.nextFrame();
+	BufferRecorder rec;
+	rec.out = outContacts;
+	rec.counts = outCounts;
+	rec.maxPerPair = maxPerPair;
+	int overflow = 0;
+	for(PxU32 i = 0; i < nbPairs; i++)
+	{
+		outCounts[i] = 0;
+		GeomHolder h0, h1;
+		const PxGeometry* g0 = h0.set(type0[i], geom0 + 4 * i);
+		const PxGeometry* g1 = h1.set(type1[i], geom1 + 4 * i);
+		if(!g0 || !g1) return -1;
+		const PxTransform t0 = loadPose(pose0 + 7 * i);
+		const PxTransform t1 = loadPose(pose1 + 7 * i);
+		if(freshCaches) c->caches[i] = PxCache();
+		// The recorder indexes by the pair index passed here: rebase to slot i.
+		struct Rebase : PxContactRecorder
+		{
+			BufferRecorder* r; PxU32 slot;
+			bool recordContacts(const PxContactPoint* p, PxU32 n, PxU32) override { return r->recordContacts(p, n, slot); }
+		} rb;
+		rb.r = &rec;
+		rb.slot = i;
+		PxGenerateContacts(&g0, &g1, &t0, &t1, &c->caches[i], 1, rb, contactDistance, meshContactMargin, toleranceLength, c->alloc);
+		if(outCounts[i] > maxPerPair) overflow = 1;
+	}
+	return overflow;
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// TGS bodies: PxConstructSolverBodiesTGS / PxConstructStaticSolverBodyTGS.
+// rigid: nb x 96-byte PxRigidBodyData; outputs raw 64/64/48-byte records.
+HX void pxref_construct_bodies_tgs(const void* rigid, PxU32 nb, const float* gravity, float dt,
+	void* outVel, void* outTxI, void* outData)
+{
+	ensureFoundation();
+	PxConstructSolverBodiesTGS(static_cast<const PxRigidBodyData*>(rigid), static_cast<PxTGSSolverBodyVel*>(outVel),
+		static_cast<PxTGSSolverBodyTxInertia*>(outTxI), static_cast<PxTGSSolverBodyData*>(outData), nb,
+		PxVec3(gravity[0], gravity[1], gravity[2]), dt, false);
+}
+
+HX void pxref_construct_static_body_tgs(const float* pose, void* outVel, void* outTxI, void* outData)
+{
+	ensureFoundation();
+	PxConstructStaticSolverBodyTGS(loadPose(pose), *static_cast<PxTGSSolverBodyVel*>(outVel),
+		*static_cast<PxTGSSolverBodyTxInertia*>(outTxI), *static_cast<PxTGSSolverBodyData*>(outData));
+}
+
+// Batching: constraint i joins body pairA[i], pairB[i]; indices >= nbDyn are
+// static/kinematic (placed after the dynamic bodies in one array, as the
+// snippet does).  Outputs headers (start, stride) and the order of the
+// original constraint indices.
+HX PxU32 pxref_batch_constraints_tgs(const PxU32* bodyA, const PxU32* bodyB, PxU32 nbConstraints, PxU32 nbDyn, PxU32 nbStatic,
+	PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outOrder)
+{
+	ensureFoundation();
+	std::vector<PxTGSSolverBodyVel> bodies(nbDyn + nbStatic);
+	memset(bodies.data(), 0, sizeof(PxTGSSolverBodyVel) * bodies.size());
+	std::vector<PxSolverConstraintDesc> descs(nbConstraints), ordered(nbConstraints);
+	std::vector<PxU32> ids(nbConstraints);
+	for(PxU32 i = 0; i < nbConstraints; i++)
+	{
+		PxSolverConstraintDesc& d = descs[i];
+		memset(&d, 0, sizeof(d));
+		d.tgsBodyA = &bodies[bodyA[i]];
+		d.tgsBodyB = &bodies[bodyB[i]];
+		d.bodyADataIndex = bodyA[i];
+		d.bodyBDataIndex = bodyB[i];
+		d.linkIndexA = PxSolverConstraintDesc::RIGID_BODY;
+		d.linkIndexB = PxSolverConstraintDesc::RIGID_BODY;
+		ids[i] = i;
+		d.constraint = reinterpret_cast<PxU8*>(&ids[i]);
+		d.constraintType = PxSolverConstraintDesc::eCONTACT_CONSTRAINT;
+	}
+	std::vector<PxConstraintBatchHeader> headers(nbConstraints ? nbConstraints : 1);
+	const PxU32 nbHeaders = PxBatchConstraintsTGS(descs.data(), nbConstraints, bodies.data(), nbDyn, headers.data(), ordered.data());
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		outHeaderStart[h] = headers[h].startIndex;
+		outHeaderStride[h] = headers[h].stride;
+	}
+	for(PxU32 i = 0; i < nbConstraints; i++)
+		outOrder[i] = *reinterpret_cast<const PxU32*>(ordered[i].constraint);
+	return nbHeaders;
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// One TGS solve from given contacts, in the order the reference batches them:
+// construct bodies, batch, create contact constraints, solve, integrate.
+//
+// rigid       nbDyn x PxRigidBodyData (96 B)
+// staticPose  nbStatic x 7 floats
+// pairA/B     body indices (>= nbDyn: static nbDyn+s)
+// contactStart/contactCount per constraint into contacts (8 floats each)
+// friction    per-constraint static/dynamic friction and restitution (3 floats)
+// out*        velocities after solve (lin, ang: 6 floats per dynamic body, the
+//             angular one in world space after PxIntegrateSolverBodiesTGS),
+//             poses after integration (7 floats per dynamic body),
+//             headers and order as pxref_batch_constraints_tgs.
+HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
+	const PxU32* pairA, const PxU32* pairB, PxU32 nbConstraints, const PxU32* contactStart, const PxU32* contactCount,
+	const float* contacts, const float* material, const float* gravity, float dt, PxU32 nbPos, PxU32 nbVel,
+	float bounceThreshold, float frictionOffsetThreshold, float correlationDistance,
+	float* outVel, float* outPose, PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outOrder,
+	void* outBodyVelRaw, void* outTxIRaw)
+{
+	ensureFoundation();
+	const PxU32 nbTotal = nbDyn + nbStatic;
+	std::vector<PxTGSSolverBodyVel> bodies(nbTotal);
+	std::vector<PxTGSSolverBodyTxInertia> txI(nbTotal);
+	std::vector<PxTGSSolverBodyData> bodyData(nbTotal);
+	std::vector<PxTransform> poses(nbTotal);
+	const PxRigidBodyData* rb = static_cast<const PxRigidBodyData*>(rigid);
+	const PxVec3 g(gravity[0], gravity[1], gravity[2]);
+	for(PxU32 a = 0; a < nbDyn; a++)
+	{
+		PxConstructSolverBodiesTGS(&rb[a], &bodies[a], &txI[a], &bodyData[a], 1, g, dt, false);
+		poses[a] = rb[a].body2World;
+	}
+	for(PxU32 s = 0; s < nbStatic; s++)
+	{
+		poses[nbDyn + s] = loadPose(staticPose + 7 * s);
+		PxConstructStaticSolverBodyTGS(poses[nbDyn + s], bodies[nbDyn + s], txI[nbDyn + s], bodyData[nbDyn + s]);
+	}
+
+	// Contact points with the material fields the snippet's recorder fills in.
+	PxU32 nbContactsTotal = 0;
+	for(PxU32 i = 0; i < nbConstraints; i++)
+		nbContactsTotal = PxMax(nbContactsTotal, contactStart[i] + contactCount[i]);
+	std::vector<PxContactPoint> points(nbContactsTotal ? nbContactsTotal : 1);
+	for(PxU32 i = 0; i < nbConstraints; i++)
+	{
+		for(PxU32 c = 0; c < contactCount[i]; c++)
+		{
+			const float* s = contacts + 8 * (contactStart[i] + c);
+			PxContactPoint& p = points[contactStart[i] + c];
+			memset(&p, 0, sizeof(p));
+			p.normal = PxVec3(s[0], s[1], s[2]);
+			p.separation = s[3];
+			p.point = PxVec3(s[4], s[5], s[6]);
+			p.maxImpulse = PX_MAX_F32;
+			p.targetVel = PxVec3(0.0f);
+			p.staticFriction = material[3 * i + 0];
+			p.dynamicFriction = material[3 * i + 1];
+			p.restitution = material[3 * i + 2];
+			p.damping = 0.0f;
+			p.materialFlags = 0;
+		}
+	}
+	std::vector<PxReal> forces(nbContactsTotal ? nbContactsTotal : 1, 0.0f);
+
+	std::vector<PxSolverConstraintDesc> descs(nbConstraints), ordered(nbConstraints);
+	std::vector<PxU32> ids(nbConstraints);
+	for(PxU32 i = 0; i < nbConstraints; i++)
+	{
+		PxSolverConstraintDesc& d = descs[i];
+		memset(&d, 0, sizeof(d));
+		d.tgsBodyA = &bodies[pairA[i]];
+		d.tgsBodyB = &bodies[pairB[i]];
+		d.bodyADataIndex = pairA[i];
+		d.bodyBDataIndex = pairB[i];
+		d.linkIndexA = PxSolverConstraintDesc::RIGID_BODY;
+		d.linkIndexB = PxSolverConstraintDesc::RIGID_BODY;
+		ids[i] = i;
+		d.constraint = reinterpret_cast<PxU8*>(&ids[i]);
+		d.constraintType = PxSolverConstraintDesc::eCONTACT_CONSTRAINT;
+	}
+	std::vector<PxConstraintBatchHeader> headers(nbConstraints ? nbConstraints : 1);
+	const PxU32 nbHeaders = PxBatchConstraintsTGS(descs.data(), nbConstraints, bodies.data(), nbDyn, headers.data(), ordered.data());
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		outHeaderStart[h] = headers[h].startIndex;
+		outHeaderStride[h] = headers[h].stride;
+	}
+	for(PxU32 i = 0; i < nbConstraints; i++)
+		outOrder[i] = *reinterpret_cast<const PxU32*>(ordered[i].constraint);
+
+	const PxReal invDt = 1.0f / dt;
+	const PxReal stepDt = dt / PxReal(nbPos);
+	const PxReal invStepDt = invDt * PxReal(nbPos);
+	FrameConstraintAllocator alloc;
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		PxConstraintBatchHeader& header = headers[h];
+		PxTGSSolverContactDesc cd[4];
+		for(PxU32 a = 0; a < header.stride; a++)
+		{
+			PxSolverConstraintDesc& desc = ordered[header.startIndex + a];
+			const PxU32 ci = *reinterpret_cast<const PxU32*>(desc.constraint);
+			PxTGSSolverContactDesc& c = cd[a];
+			memset(&c, 0, sizeof(c));
+			c.body0 = desc.tgsBodyA;
+			c.body1 = desc.tgsBodyB;
+			c.bodyData0 = &bodyData[desc.bodyADataIndex];
+			c.bodyData1 = &bodyData[desc.bodyBDataIndex];
+			c.body0TxI = &txI[desc.bodyADataIndex];
+			c.body1TxI = &txI[desc.bodyBDataIndex];
+			c.bodyFrame0 = poses[desc.bodyADataIndex];
+			c.bodyFrame1 = poses[desc.bodyBDataIndex];
+			c.contactForces = &forces[contactStart[ci]];
+			c.contacts = &points[contactStart[ci]];
+			c.numContacts = contactCount[ci];
+			c.frictionPtr = NULL;
+			c.frictionCount = 0;
+			c.shapeInteraction = NULL;
+			c.maxCCDSeparation = PX_MAX_F32;
+			c.bodyState0 = desc.bodyADataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
+			c.bodyState1 = desc.bodyBDataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
+			c.desc = &desc;
+			c.invMassScales.angular0 = c.invMassScales.angular1 = c.invMassScales.linear0 = c.invMassScales.linear1 = 1.0f;
+		}
+		PxCreateContactConstraintsTGS(&header, 1, cd, alloc, invStepDt, invDt, bounceThreshold, frictionOffsetThreshold, correlationDistance);
+	}
+
+	PxSolveConstraintsTGS(headers.data(), nbHeaders, ordered.data(), bodies.data(), txI.data(), nbDyn, nbPos, nbVel, stepDt, invStepDt);
+	if(outBodyVelRaw) memcpy(outBodyVelRaw, bodies.data(), sizeof(PxTGSSolverBodyVel) * nbDyn);
+	if(outTxIRaw) memcpy(outTxIRaw, txI.data(), sizeof(PxTGSSolverBodyTxInertia) * nbDyn);
+	PxIntegrateSolverBodiesTGS(bodies.data(), txI.data(), poses.data(), nbDyn, dt);
+	for(PxU32 a = 0; a < nbDyn; a++)
+	{
+		outVel[6 * a + 0] = bodies[a].linearVelocity.x;
+		outVel[6 * a + 1] = bodies[a].linearVelocity.y;
+		outVel[6 * a + 2] = bodies[a].linearVelocity.z;
+		outVel[6 * a + 3] = bodies[a].angularVelocity.x;
+		outVel[6 * a + 4] = bodies[a].angularVelocity.y;
+		outVel[6 * a + 5] = bodies[a].angularVelocity.z;
+		storePose(outPose + 7 * a, poses[a]);
+	}
+	return nbHeaders;
+}
