@@ -1,0 +1,731 @@
+// Broadphase for the GB300 rigid-body step: a drop-in for PhysX's ABP
+// PxBroadPhase (PxCreateBroadPhase(eABP) + update/fetchResults).
+//
+// Semantics follow the reference ABP (physx/source/lowlevelaabb/src/BpBroadPhaseABP.cpp):
+//  * bounds are inflated by the per-object distance in float (BoxManager::prepareData,
+//    :1712-1729), X extents are compared as order-preserving integer keys
+//    (BpBroadPhaseIntegerAABB.h:44 encodeFloat), Y/Z as closed float intervals
+//    (the SIMD test at :2216-2235);
+//  * a pair is (re)tested only when at least one object was added/updated/removed
+//    this frame; boxes that were not updated keep the bounds stored at their last
+//    add/update (the reference's "sleeping" array);
+//  * filtering is BpFiltering.h:90 groupFiltering with the LUT of BpFiltering.cpp:34;
+//  * created/lost reporting follows ABP_PairManager::computeCreatedDeletedPairs (:3714):
+//    new pairs are created, re-found pairs persist, pairs with an updated endpoint
+//    that were not re-found are lost (reported unless an endpoint was removed), and
+//    pairs between two non-updated objects persist silently.
+//
+// GB300 design: all object state lives in HBM indexed by handle; each update
+// sorts the live boxes by their encoded min-X key with a hand-written radix
+// sort, sweeps updated boxes warp-cooperatively (one ballot per 32
+// candidates), and maintains the active pair set as a sorted array of 64-bit
+// keys (id0 << 32 | id1, id0 < id1), so created/lost lists come out sorted and
+// deterministic.
+#include "common.cuh"
+#include "radix_sort.cuh"
+#include <vector>
+#include <algorithm>
+
+namespace gbpx
+{
+namespace bp
+{
+enum : uint8_t { F_UPDATED = 1, F_REMOVED = 2 };
+
+// Packed add/update record staged on the host: id, group, distance, bounds.
+struct UpdateRec
+{
+	uint32_t id;
+	uint32_t group;
+	float dist;
+	float mn[3];
+	float mx[3];
+	uint32_t isCreate;
+};
+static_assert(sizeof(UpdateRec) == 40, "UpdateRec layout");
+
+__device__ __forceinline__ bool lutAllows(uint32_t t0, uint32_t t1, uint32_t lutBits)
+{
+	return (lutBits >> (t0 * 7 + t1)) & 1u;
+}
+
+__device__ __forceinline__ bool groupFilter(uint32_t g0, uint32_t g1, uint32_t lutLo, uint32_t lutHi)
+{
+	if(g0 == g1) return false;
+	const uint32_t t0 = g0 & 7u, t1 = g1 & 7u;
+	if(t0 >= 7u || t1 >= 7u) return false;
+	const uint32_t bit = t0 * 7u + t1;
+	return bit < 32u ? ((lutLo >> bit) & 1u) : ((lutHi >> (bit - 32u)) & 1u);
+}
+
+__global__ void applyRemovedKernel(const uint32_t* __restrict__ ids, uint32_t n, uint8_t* __restrict__ live, uint8_t* __restrict__ flags)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const uint32_t id = ids[i];
+	live[id] = 0;
+	flags[id] = F_UPDATED | F_REMOVED;
+}
+
+__global__ void applyUpdatesKernel(const UpdateRec* __restrict__ recs, uint32_t n, uint2* __restrict__ bx, float4* __restrict__ byz,
+                                   uint32_t* __restrict__ groups, uint8_t* __restrict__ live, uint8_t* __restrict__ flags)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const UpdateRec r = recs[i];
+	const float d = r.dist;
+	// Inflate exactly as the reference: min - d, max + d in FP32.
+	const float minX = __fsub_rn(r.mn[0], d), minY = __fsub_rn(r.mn[1], d), minZ = __fsub_rn(r.mn[2], d);
+	const float maxX = __fadd_rn(r.mx[0], d), maxY = __fadd_rn(r.mx[1], d), maxZ = __fadd_rn(r.mx[2], d);
+	bx[r.id] = make_uint2(encodeFloatBits(__float_as_uint(minX)), encodeFloatBits(__float_as_uint(maxX)));
+	byz[r.id] = make_float4(-minY, -minZ, maxY, maxZ);
+	if(r.isCreate) groups[r.id] = r.group;
+	live[r.id] = 1;
+	flags[r.id] |= F_UPDATED;
+}
+
+// Stable compaction of live handles into (key = encoded min X, value = handle).
+__global__ void countLiveKernel(const uint8_t* __restrict__ live, uint32_t cap, uint32_t* __restrict__ blockCounts)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool v = i < cap && live[i];
+	const uint32_t b = __syncthreads_count(v);
+	if(threadIdx.x == 0) blockCounts[blockIdx.x] = b;
+}
+
+__global__ void emitLiveKernel(const uint8_t* __restrict__ live, const uint2* __restrict__ bx, uint32_t cap,
+                               const uint32_t* __restrict__ blockOffsets, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+	__shared__ uint32_t warpCounts[32];
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool v = i < cap && live[i];
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t ballot = __ballot_sync(0xffffffffu, v);
+	if(lane == 0) warpCounts[warp] = __popc(ballot);
+	__syncthreads();
+	if(warp == 0)
+	{
+		const uint32_t nw = blockDim.x >> 5;
+		uint32_t c = lane < nw ? warpCounts[lane] : 0u;
+		uint32_t incl = c;
+		for(int o = 1; o < 32; o <<= 1)
+		{
+			const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+			if(lane >= uint32_t(o)) incl += t;
+		}
+		if(lane < nw) warpCounts[lane] = incl - c;
+	}
+	__syncthreads();
+	if(v)
+	{
+		const uint32_t dst = blockOffsets[blockIdx.x] + warpCounts[warp] + __popc(ballot & laneMaskLt());
+		keys[dst] = bx[i].x;
+		vals[dst] = i;
+	}
+}
+
+// Gathers the sorted SoA arrays and marks which sorted positions were updated.
+__global__ void gatherSortedKernel(const uint32_t* __restrict__ sortedIds, uint32_t n, const uint2* __restrict__ bx,
+                                   const float4* __restrict__ byz, const uint32_t* __restrict__ groups, const uint8_t* __restrict__ flags,
+                                   uint2* __restrict__ sx, float4* __restrict__ syz, uint32_t* __restrict__ sgrp, uint32_t* __restrict__ supd)
+{
+	const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= n) return;
+	const uint32_t id = sortedIds[p];
+	sx[p] = bx[id];
+	syz[p] = byz[id];
+	sgrp[p] = groups[id];
+	supd[p] = (flags[id] & F_UPDATED) ? 1u : 0u;
+}
+
+// Stable compaction of sorted positions that were / were not updated.
+__global__ void countFlagKernel(const uint32_t* __restrict__ flag, uint32_t n, uint32_t want, uint32_t* __restrict__ blockCounts)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool v = i < n && flag[i] == want;
+	const uint32_t b = __syncthreads_count(v);
+	if(threadIdx.x == 0) blockCounts[blockIdx.x] = b;
+}
+
+__global__ void emitFlagKernel(const uint32_t* __restrict__ flag, uint32_t n, uint32_t want, const uint32_t* __restrict__ blockOffsets,
+                               uint32_t* __restrict__ out)
+{
+	__shared__ uint32_t warpCounts[32];
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool v = i < n && flag[i] == want;
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t ballot = __ballot_sync(0xffffffffu, v);
+	if(lane == 0) warpCounts[warp] = __popc(ballot);
+	__syncthreads();
+	if(warp == 0)
+	{
+		const uint32_t nw = blockDim.x >> 5;
+		uint32_t c = lane < nw ? warpCounts[lane] : 0u;
+		uint32_t incl = c;
+		for(int o = 1; o < 32; o <<= 1)
+		{
+			const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+			if(lane >= uint32_t(o)) incl += t;
+		}
+		if(lane < nw) warpCounts[lane] = incl - c;
+	}
+	__syncthreads();
+	if(v) out[blockOffsets[blockIdx.x] + warpCounts[warp] + __popc(ballot & laneMaskLt())] = i;
+}
+
+__device__ __forceinline__ bool overlapYZ(const float4 a, const float4 b)
+{
+	// a, b hold (-minY, -minZ, maxY, maxZ): closed-interval overlap in Y and Z.
+	return (b.x >= -a.z) & (b.y >= -a.w) & (b.z >= -a.x) & (b.w >= -a.y);
+}
+
+__device__ __forceinline__ void emitPairs(uint32_t hitMask, uint32_t idA, uint32_t idB, unsigned long long* __restrict__ out,
+                                          uint32_t cap, uint32_t* __restrict__ counter)
+{
+	// Warp-aggregated append: one atomic per warp per batch of hits.
+	const uint32_t lane = threadIdx.x & 31;
+	if(!hitMask) return;
+	uint32_t base = 0;
+	if(lane == __ffs(hitMask) - 1) base = atomicAdd(counter, __popc(hitMask));
+	base = __shfl_sync(0xffffffffu, base, __ffs(hitMask) - 1);
+	if(hitMask & (1u << lane))
+	{
+		const uint32_t slot = base + __popc(hitMask & laneMaskLt());
+		const uint32_t lo = min(idA, idB), hi = max(idA, idB);
+		if(slot < cap) out[slot] = (static_cast<unsigned long long>(lo) << 32) | hi;
+	}
+}
+
+// Pass 1: one warp per updated box; scans every later box in sorted order whose
+// min X does not exceed this box's max X.
+__global__ void sweepUpdatedKernel(const uint32_t* __restrict__ updPos, uint32_t nbUpd, uint32_t n, const uint2* __restrict__ sx,
+                                   const float4* __restrict__ syz, const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds,
+                                   uint32_t lutLo, uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
+	for(uint32_t k = warpId; k < nbUpd; k += nWarps)
+	{
+		const uint32_t p = updPos[k];
+		const uint2 x0 = sx[p];
+		const float4 yz0 = syz[p];
+		const uint32_t g0 = sgrp[p];
+		const uint32_t id0 = sortedIds[p];
+		for(uint32_t q0 = p + 1; q0 < n; q0 += 32)
+		{
+			const uint32_t q = q0 + lane;
+			bool inRange = false, hit = false;
+			if(q < n)
+			{
+				inRange = sx[q].x <= x0.y;
+				if(inRange) hit = overlapYZ(yz0, syz[q]) && groupFilter(g0, sgrp[q], lutLo, lutHi);
+			}
+			const uint32_t hitMask = __ballot_sync(0xffffffffu, hit);
+			emitPairs(hitMask, id0, q < n ? sortedIds[q] : 0u, out, cap, counter);
+			if(__ballot_sync(0xffffffffu, inRange) != 0xffffffffu) break;
+		}
+	}
+}
+
+// Pass 2: one thread per non-updated box; scans the updated boxes that come
+// later in sorted order (pairs whose first box in sorted order did not move).
+__global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint32_t nbSleep, const uint32_t* __restrict__ updPos,
+                                    uint32_t nbUpd, const uint2* __restrict__ sx, const float4* __restrict__ syz,
+                                    const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds, uint32_t lutLo,
+                                    uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
+{
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t lane = threadIdx.x & 31;
+	uint32_t p = 0, lo = nbUpd;
+	uint2 x0 = make_uint2(1u, 0u);
+	float4 yz0 = make_float4(0, 0, 0, 0);
+	uint32_t g0 = 0, id0 = 0;
+	const bool active = k < nbSleep;
+	if(active)
+	{
+		p = sleepPos[k];
+		x0 = sx[p];
+		yz0 = syz[p];
+		g0 = sgrp[p];
+		id0 = sortedIds[p];
+		// first updated position > p
+		uint32_t a = 0, b = nbUpd;
+		while(a < b)
+		{
+			const uint32_t m = (a + b) >> 1;
+			if(updPos[m] <= p) a = m + 1; else b = m;
+		}
+		lo = a;
+	}
+	bool more = active && lo < nbUpd;
+	uint32_t j = lo;
+	while(__any_sync(0xffffffffu, more))
+	{
+		bool hit = false;
+		uint32_t idq = 0;
+		if(more)
+		{
+			const uint32_t q = updPos[j];
+			if(sx[q].x <= x0.y)
+			{
+				idq = sortedIds[q];
+				hit = overlapYZ(yz0, syz[q]) && groupFilter(g0, sgrp[q], lutLo, lutHi);
+				j++;
+				more = j < nbUpd;
+			}
+			else more = false;
+		}
+		// Emission is per lane here (divergent scans); aggregate the lanes that hit.
+		const uint32_t hitMask = __ballot_sync(0xffffffffu, hit);
+		if(hitMask)
+		{
+			uint32_t base = 0;
+			const uint32_t leader = __ffs(hitMask) - 1;
+			if(lane == leader) base = atomicAdd(counter, __popc(hitMask));
+			base = __shfl_sync(0xffffffffu, base, leader);
+			if(hit)
+			{
+				const uint32_t slot = base + __popc(hitMask & laneMaskLt());
+				const uint32_t a = min(id0, idq), b = max(id0, idq);
+				if(slot < cap) out[slot] = (static_cast<unsigned long long>(a) << 32) | b;
+			}
+		}
+	}
+}
+
+__device__ __forceinline__ bool containsKey(const unsigned long long* __restrict__ arr, uint32_t n, unsigned long long key)
+{
+	uint32_t a = 0, b = n;
+	while(a < b)
+	{
+		const uint32_t m = (a + b) >> 1;
+		if(arr[m] < key) a = m + 1; else b = m;
+	}
+	return a < n && arr[a] == key;
+}
+
+__device__ __forceinline__ uint32_t lowerBound(const unsigned long long* __restrict__ arr, uint32_t n, unsigned long long key)
+{
+	uint32_t a = 0, b = n;
+	while(a < b)
+	{
+		const uint32_t m = (a + b) >> 1;
+		if(arr[m] < key) a = m + 1; else b = m;
+	}
+	return a;
+}
+
+// Classifies found pairs: flag 1 = created (absent from the previous set).
+__global__ void classifyFoundKernel(const unsigned long long* __restrict__ found, uint32_t nFound, const unsigned long long* __restrict__ prev,
+                                    uint32_t nPrev, uint32_t* __restrict__ isCreated)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= nFound) return;
+	isCreated[i] = containsKey(prev, nPrev, found[i]) ? 0u : 1u;
+}
+
+// Classifies previous pairs: 0 = persists via the found set, 1 = kept (both
+// endpoints sleeping), 2 = lost and reported, 3 = dropped silently (removed endpoint).
+__global__ void classifyPrevKernel(const unsigned long long* __restrict__ prev, uint32_t nPrev, const unsigned long long* __restrict__ found,
+                                   uint32_t nFound, const uint8_t* __restrict__ flags, uint32_t* __restrict__ cls)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= nPrev) return;
+	const unsigned long long k = prev[i];
+	const uint32_t id0 = uint32_t(k >> 32), id1 = uint32_t(k);
+	const uint8_t f0 = flags[id0], f1 = flags[id1];
+	uint32_t c;
+	if(!((f0 | f1) & F_UPDATED)) c = 1;
+	else if(containsKey(found, nFound, k)) c = 0;
+	else if((f0 | f1) & F_REMOVED) c = 3;
+	else c = 2;
+	cls[i] = c;
+}
+
+__global__ void flagEqualsKernel(const uint32_t* __restrict__ cls, uint32_t n, uint32_t want, uint32_t* __restrict__ out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) out[i] = cls[i] == want ? 1u : 0u;
+}
+
+__global__ void scatterSelectedKernel(const unsigned long long* __restrict__ src, const uint32_t* __restrict__ sel,
+                                      const uint32_t* __restrict__ pos, uint32_t n, unsigned long long* __restrict__ dst)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n && sel[i]) dst[pos[i]] = src[i];
+}
+
+// Merge of two sorted, disjoint key arrays by co-ranking.
+__global__ void mergeKernel(const unsigned long long* __restrict__ a, uint32_t na, const unsigned long long* __restrict__ b, uint32_t nb,
+                            unsigned long long* __restrict__ out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < na) out[i + lowerBound(b, nb, a[i])] = a[i];
+	else if(i < na + nb)
+	{
+		const uint32_t j = i - na;
+		out[j + lowerBound(a, na, b[j])] = b[j];
+	}
+}
+
+__global__ void keysToPairsKernel(const unsigned long long* __restrict__ keys, uint32_t n, uint2* __restrict__ out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) out[i] = make_uint2(uint32_t(keys[i] >> 32), uint32_t(keys[i]));
+}
+
+} // namespace bp
+
+// One ABP-compatible broadphase instance.
+struct BroadPhase
+{
+	cudaStream_t stream = 0;
+	uint32_t lutLo = 0, lutHi = 0;
+	uint32_t capacity = 0;  // handle capacity on device
+
+	DevBuf<uint2> bx;
+	DevBuf<float4> byz;
+	DevBuf<uint32_t> groups;
+	DevBuf<uint8_t> live, flags;
+
+	// per-update scratch
+	DevBuf<bp::UpdateRec> dRecs;
+	DevBuf<uint32_t> dRemoved;
+	HostBuf<bp::UpdateRec> hRecs;
+	DevBuf<uint32_t> blockCounts, keysA, valsA, keysB, valsB, hist;
+	DevBuf<uint2> sx;
+	DevBuf<float4> syz;
+	DevBuf<uint32_t> sgrp, supd, updPos, sleepPos;
+	DevBuf<unsigned long long> found, foundAlt, prev, next, created, lost;
+	DevBuf<uint32_t> counter, cls, sel, pos;
+	DevBuf<uint2> createdPairs, lostPairs;
+	HostBuf<uint32_t> hCounts;
+	HostBuf<uint2> hCreated, hLost;
+	uint32_t nPrev = 0;
+	uint32_t nbCreatedOut = 0, nbLostOut = 0;
+	bool pending = false;
+	uint64_t stats[4] = {0, 0, 0, 0};  // live boxes, updated boxes, found pairs, active pairs (last update)
+
+	int init(bool discardStaticKinematic, bool discardKinematicKinematic)
+	{
+		// LUT of BpFiltering.cpp:34 (7 filter types), flattened type0*7+type1.
+		bool lut[7][7] = {};
+		const int S = 0, K = 1, D = 2, A = 3, DS = 4, DV = 5, PS = 6;
+		auto set = [&](int a, int b, bool v) { lut[a][b] = lut[b][a] = v; };
+		set(S, D, true);
+		set(S, K, !discardStaticKinematic);
+		set(D, K, true);
+		set(D, D, true);
+		set(K, K, !discardKinematicKinematic);
+		set(S, A, true); set(K, A, true); set(D, A, true); set(A, A, true);
+		set(DS, D, true); set(DS, S, true); set(DS, K, true); set(DS, DS, true);
+		set(DV, D, true); set(DV, S, true); set(DV, K, true); set(DV, DS, true); set(DV, DV, true);
+		set(PS, D, true); set(PS, S, true); set(PS, K, true); set(PS, DS, true); set(PS, DV, true); set(PS, PS, true);
+		uint64_t bits = 0;
+		for(int a = 0; a < 7; a++)
+			for(int b = 0; b < 7; b++)
+				if(lut[a][b]) bits |= 1ull << (a * 7 + b);
+		lutLo = uint32_t(bits);
+		lutHi = uint32_t(bits >> 32);
+		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		if(counter.reserve(4)) return GBPX_ERR_NOMEM;
+		if(hCounts.reserve(8)) return GBPX_ERR_NOMEM;
+		return GBPX_OK;
+	}
+
+	void release()
+	{
+		if(stream) cudaStreamSynchronize(stream);
+		bx.release(); byz.release(); groups.release(); live.release(); flags.release();
+		dRecs.release(); dRemoved.release(); hRecs.release();
+		blockCounts.release(); keysA.release(); valsA.release(); keysB.release(); valsB.release(); hist.release();
+		sx.release(); syz.release(); sgrp.release(); supd.release(); updPos.release(); sleepPos.release();
+		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
+		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release();
+		hCounts.release(); hCreated.release(); hLost.release();
+		if(stream) cudaStreamDestroy(stream);
+		stream = 0;
+	}
+
+	int growCapacity(uint32_t need)
+	{
+		if(need <= capacity) return GBPX_OK;
+		uint32_t nc = capacity ? capacity : 1024;
+		while(nc < need) nc *= 2;
+		DevBuf<uint2> nbx; DevBuf<float4> nbyz; DevBuf<uint32_t> ng; DevBuf<uint8_t> nl, nf;
+		if(nbx.reserve(nc) || nbyz.reserve(nc) || ng.reserve(nc) || nl.reserve(nc) || nf.reserve(nc)) return GBPX_ERR_NOMEM;
+		GBPX_CUDA_TRY(cudaMemsetAsync(nl.ptr, 0, nc, stream));
+		GBPX_CUDA_TRY(cudaMemsetAsync(nf.ptr, 0, nc, stream));
+		GBPX_CUDA_TRY(cudaMemsetAsync(ng.ptr, 0xff, size_t(nc) * 4, stream));
+		if(capacity)
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(nbx.ptr, bx.ptr, size_t(capacity) * sizeof(uint2), cudaMemcpyDeviceToDevice, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(nbyz.ptr, byz.ptr, size_t(capacity) * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(ng.ptr, groups.ptr, size_t(capacity) * 4, cudaMemcpyDeviceToDevice, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(nl.ptr, live.ptr, capacity, cudaMemcpyDeviceToDevice, stream));
+		}
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		bx.release(); byz.release(); groups.release(); live.release(); flags.release();
+		bx = nbx; byz = nbyz; groups = ng; live = nl; flags = nf;
+		capacity = nc;
+		return GBPX_OK;
+	}
+
+	// Compacts sorted positions p with flag[p] == want into out (stable).
+	int compactFlag(const uint32_t* flag, uint32_t n, uint32_t want, uint32_t* out)
+	{
+		const uint32_t nb = divUp(n, 256);
+		if(blockCounts.reserve(nb + 1)) return GBPX_ERR_NOMEM;
+		bp::countFlagKernel<<<nb, 256, 0, stream>>>(flag, n, want, blockCounts.ptr);
+		if(cudaMemsetAsync(blockCounts.ptr + nb, 0, 4, stream) != cudaSuccess) return GBPX_ERR_CUDA;
+		rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nb + 1);
+		bp::emitFlagKernel<<<nb, 256, 0, stream>>>(flag, n, want, blockCounts.ptr, out);
+		return GBPX_OK;
+	}
+
+	// Exclusive scan of sel[0..n) into pos; total read back to *total (synchronous).
+	int scanSelect(const uint32_t* selIn, uint32_t n, uint32_t* posOut, uint32_t* total)
+	{
+		if(!n) { *total = 0; return GBPX_OK; }
+		GBPX_CUDA_TRY(cudaMemcpyAsync(posOut, selIn, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream));
+		GBPX_CUDA_TRY(cudaMemsetAsync(posOut + n, 0, 4, stream));
+		rs::scanKernel<<<1, 1024, 0, stream>>>(posOut, n + 1);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, posOut + n, 4, cudaMemcpyDeviceToHost, stream));
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		*total = hCounts.ptr[0];
+		return GBPX_OK;
+	}
+
+	int update(const uint32_t* createdIds, uint32_t nbCreated, const uint32_t* updatedIds, uint32_t nbUpdated,
+	           const uint32_t* removedIds, uint32_t nbRemoved, const float* bounds, const uint32_t* groupsIn,
+	           const float* distances, uint32_t cap)
+	{
+		if(pending) return GBPX_ERR_STATE;
+		if((nbCreated && !createdIds) || (nbUpdated && !updatedIds) || (nbRemoved && !removedIds)) return GBPX_ERR_INVALID;
+		if((nbCreated || nbUpdated) && (!bounds || !distances)) return GBPX_ERR_INVALID;
+		if(nbCreated && !groupsIn) return GBPX_ERR_INVALID;
+		for(uint32_t i = 0; i < nbCreated; i++) if(createdIds[i] >= cap) return GBPX_ERR_INVALID;
+		for(uint32_t i = 0; i < nbUpdated; i++) if(updatedIds[i] >= cap) return GBPX_ERR_INVALID;
+		for(uint32_t i = 0; i < nbRemoved; i++) if(removedIds[i] >= capacity) return GBPX_ERR_INVALID;
+		int rc = growCapacity(cap);
+		if(rc) return rc;
+
+		// 1. Stage add/update records (host gather of the user-owned arrays) and upload.
+		const uint32_t nbRec = nbCreated + nbUpdated;
+		if(hRecs.reserve(nbRec ? nbRec : 1) || dRecs.reserve(nbRec ? nbRec : 1) || dRemoved.reserve(nbRemoved ? nbRemoved : 1))
+			return GBPX_ERR_NOMEM;
+		for(uint32_t i = 0; i < nbRec; i++)
+		{
+			const bool isC = i < nbCreated;
+			const uint32_t id = isC ? createdIds[i] : updatedIds[i - nbCreated];
+			bp::UpdateRec& r = hRecs.ptr[i];
+			r.id = id;
+			r.group = isC ? groupsIn[id] : 0u;
+			r.dist = distances[id];
+			memcpy(r.mn, bounds + 6 * size_t(id), 12);
+			memcpy(r.mx, bounds + 6 * size_t(id) + 3, 12);
+			r.isCreate = isC ? 1u : 0u;
+		}
+		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
+		if(nbRemoved)
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(dRemoved.ptr, removedIds, size_t(nbRemoved) * 4, cudaMemcpyHostToDevice, stream));
+			bp::applyRemovedKernel<<<divUp(nbRemoved, 256), 256, 0, stream>>>(dRemoved.ptr, nbRemoved, live.ptr, flags.ptr);
+		}
+		if(nbRec)
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(dRecs.ptr, hRecs.ptr, size_t(nbRec) * sizeof(bp::UpdateRec), cudaMemcpyHostToDevice, stream));
+			bp::applyUpdatesKernel<<<divUp(nbRec, 256), 256, 0, stream>>>(dRecs.ptr, nbRec, bx.ptr, byz.ptr, groups.ptr, live.ptr, flags.ptr);
+		}
+		return runFrame(nbRec + nbRemoved);
+	}
+
+	// Everything after the object state is current on the device.
+	int runFrame(uint32_t nbTouched)
+	{
+		// 2. Live boxes sorted by encoded min X.
+		const uint32_t nbBlk = divUp(capacity, 256);
+		if(blockCounts.reserve(nbBlk + 1)) return GBPX_ERR_NOMEM;
+		bp::countLiveKernel<<<nbBlk, 256, 0, stream>>>(live.ptr, capacity, blockCounts.ptr);
+		GBPX_CUDA_TRY(cudaMemsetAsync(blockCounts.ptr + nbBlk, 0, 4, stream));
+		rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nbBlk + 1);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + nbBlk, 4, cudaMemcpyDeviceToHost, stream));
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		const uint32_t n = hCounts.ptr[0];
+		if(keysA.reserve(n + 1) || valsA.reserve(n + 1) || keysB.reserve(n + 1) || valsB.reserve(n + 1) ||
+		   hist.reserve(radixSortHistEntries(n) + 1) || sx.reserve(n + 1) || syz.reserve(n + 1) || sgrp.reserve(n + 1) ||
+		   supd.reserve(n + 1) || updPos.reserve(n + 1) || sleepPos.reserve(n + 1))
+			return GBPX_ERR_NOMEM;
+		bp::emitLiveKernel<<<nbBlk, 256, 0, stream>>>(live.ptr, bx.ptr, capacity, blockCounts.ptr, keysA.ptr, valsA.ptr);
+		const bool alt = radixSort<uint32_t, true>(keysA.ptr, valsA.ptr, keysB.ptr, valsB.ptr, n, 0, 32, hist.ptr, stream);
+		const uint32_t* sortedIds = alt ? valsB.ptr : valsA.ptr;
+		if(n)
+			bp::gatherSortedKernel<<<divUp(n, 256), 256, 0, stream>>>(sortedIds, n, bx.ptr, byz.ptr, groups.ptr, flags.ptr, sx.ptr, syz.ptr,
+			                                                        sgrp.ptr, supd.ptr);
+
+		// 3. Split sorted positions into updated / sleeping lists.
+		uint32_t nbUpd = 0;
+		if(n)
+		{
+			if(compactFlag(supd.ptr, n, 1u, updPos.ptr)) return GBPX_ERR_NOMEM;
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + divUp(n, 256), 4, cudaMemcpyDeviceToHost, stream));
+			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+			nbUpd = hCounts.ptr[0];
+			if(compactFlag(supd.ptr, n, 0u, sleepPos.ptr)) return GBPX_ERR_NOMEM;
+		}
+		const uint32_t nbSleep = n - nbUpd;
+
+		// 4. Sweep.  The found buffer grows and the sweep reruns if it overflowed.
+		uint32_t nFound = 0;
+		if(found.reserve(1024) || foundAlt.reserve(1024)) return GBPX_ERR_NOMEM;
+		for(int attempt = 0; attempt < 3; attempt++)
+		{
+			GBPX_CUDA_TRY(cudaMemsetAsync(counter.ptr, 0, 4, stream));
+			const uint32_t capF = uint32_t(std::min<size_t>(found.cap, 0xffffffffu));
+			if(nbUpd)
+			{
+				const uint32_t warps = nbUpd;
+				const uint32_t blocks = std::min<uint32_t>(divUp(uint64_t(warps) * 32, 256), 152u * 64u);
+				bp::sweepUpdatedKernel<<<blocks, 256, 0, stream>>>(updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
+				                                                  found.ptr, capF, counter.ptr);
+				if(nbSleep)
+					bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
+					                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
+					                                                                 counter.ptr);
+			}
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, counter.ptr, 4, cudaMemcpyDeviceToHost, stream));
+			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+			nFound = hCounts.ptr[0];
+			if(nFound <= capF) break;
+			if(found.reserve(size_t(nFound) + 1024) || foundAlt.reserve(size_t(nFound) + 1024)) return GBPX_ERR_NOMEM;
+			if(attempt == 2) return GBPX_ERR_CAPACITY;
+		}
+
+		// 5. Deterministic order: sort the found keys.
+		if(hist.reserve(radixSortHistEntries(nFound) + 1)) return GBPX_ERR_NOMEM;
+		unsigned long long* F = found.ptr;
+		if(nFound > 1)
+		{
+			const bool a2 = radixSort<unsigned long long, false>(found.ptr, nullptr, foundAlt.ptr, nullptr, nFound, 0, 64, hist.ptr, stream);
+			F = a2 ? foundAlt.ptr : found.ptr;
+		}
+
+		// 6. Created / lost / next active set.
+		const uint32_t m = std::max(nFound, nPrev) + 1;
+		if(cls.reserve(m) || sel.reserve(m) || pos.reserve(m + 1) || created.reserve(m) || lost.reserve(m) || next.reserve(size_t(nFound) + nPrev + 1) ||
+		   prev.reserve(1) || createdPairs.reserve(m) || lostPairs.reserve(m))
+			return GBPX_ERR_NOMEM;
+		uint32_t nCreated = 0, nLost = 0, nKeep = 0;
+		if(nFound)
+		{
+			bp::classifyFoundKernel<<<divUp(nFound, 256), 256, 0, stream>>>(F, nFound, prev.ptr, nPrev, sel.ptr);
+			int r2 = scanSelect(sel.ptr, nFound, pos.ptr, &nCreated);
+			if(r2) return r2;
+			bp::scatterSelectedKernel<<<divUp(nFound, 256), 256, 0, stream>>>(F, sel.ptr, pos.ptr, nFound, created.ptr);
+		}
+		unsigned long long* keep = lost.ptr + 0;  // placeholder, reassigned below
+		DevBuf<unsigned long long>& keepBuf = foundAlt.ptr == F ? found : foundAlt;  // the sort buffer not holding F
+		if(keepBuf.reserve(size_t(nPrev) + 1)) return GBPX_ERR_NOMEM;
+		keep = keepBuf.ptr;
+		if(nPrev)
+		{
+			bp::classifyPrevKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, nPrev, F, nFound, flags.ptr, cls.ptr);
+			bp::flagEqualsKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(cls.ptr, nPrev, 2u, sel.ptr);
+			int r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nLost);
+			if(r2) return r2;
+			bp::scatterSelectedKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, sel.ptr, pos.ptr, nPrev, lost.ptr);
+			bp::flagEqualsKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(cls.ptr, nPrev, 1u, sel.ptr);
+			r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nKeep);
+			if(r2) return r2;
+			bp::scatterSelectedKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, sel.ptr, pos.ptr, nPrev, keep);
+		}
+		const uint32_t nNext = nKeep + nFound;
+		if(nNext)
+			bp::mergeKernel<<<divUp(nNext, 256), 256, 0, stream>>>(keep, nKeep, F, nFound, next.ptr);
+		std::swap(prev, next);
+		nPrev = nNext;
+
+		// 7. Results to the host (owned by the broadphase until the next update).
+		if(hCreated.reserve(nCreated + 1) || hLost.reserve(nLost + 1)) return GBPX_ERR_NOMEM;
+		if(nCreated)
+		{
+			bp::keysToPairsKernel<<<divUp(nCreated, 256), 256, 0, stream>>>(created.ptr, nCreated, createdPairs.ptr);
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hCreated.ptr, createdPairs.ptr, size_t(nCreated) * 8, cudaMemcpyDeviceToHost, stream));
+		}
+		if(nLost)
+		{
+			bp::keysToPairsKernel<<<divUp(nLost, 256), 256, 0, stream>>>(lost.ptr, nLost, lostPairs.ptr);
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hLost.ptr, lostPairs.ptr, size_t(nLost) * 8, cudaMemcpyDeviceToHost, stream));
+		}
+		nbCreatedOut = nCreated;
+		nbLostOut = nLost;
+		stats[0] = n; stats[1] = nbUpd; stats[2] = nFound; stats[3] = nPrev;
+		(void)nbTouched;
+		pending = true;
+		return GBPX_OK;
+	}
+
+	int fetchResults(const uint2** outCreated, uint32_t* nbCreated, const uint2** outLost, uint32_t* nbLost)
+	{
+		if(!pending) return GBPX_ERR_STATE;
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		GBPX_CUDA_TRY(cudaGetLastError());
+		pending = false;
+		*outCreated = hCreated.ptr;
+		*nbCreated = nbCreatedOut;
+		*outLost = hLost.ptr;
+		*nbLost = nbLostOut;
+		return GBPX_OK;
+	}
+};
+} // namespace gbpx
+
+using gbpx::BroadPhase;
+
+GBPX_API int gbpx_bp_create(int discardStaticVsKinematic, int discardKinematicVsKinematic, void** outBp)
+{
+	if(!outBp) return GBPX_ERR_INVALID;
+	BroadPhase* bp = new BroadPhase;
+	const int rc = bp->init(discardStaticVsKinematic != 0, discardKinematicVsKinematic != 0);
+	if(rc) { bp->release(); delete bp; return rc; }
+	*outBp = bp;
+	return GBPX_OK;
+}
+
+GBPX_API void gbpx_bp_release(void* bp)
+{
+	if(!bp) return;
+	static_cast<BroadPhase*>(bp)->release();
+	delete static_cast<BroadPhase*>(bp);
+}
+
+GBPX_API uint32_t gbpx_bp_static_filter_group(void) { return 0u; }
+GBPX_API uint32_t gbpx_bp_dynamic_filter_group(uint32_t id) { return ((id + 1u) << 3) | 2u; }
+GBPX_API uint32_t gbpx_bp_kinematic_filter_group(uint32_t id) { return ((id + 1u) << 3) | 1u; }
+
+GBPX_API int gbpx_bp_update(void* bp, const uint32_t* created, uint32_t nbCreated, const uint32_t* updated, uint32_t nbUpdated,
+                            const uint32_t* removed, uint32_t nbRemoved, const float* bounds, const uint32_t* groups,
+                            const float* distances, uint32_t capacity)
+{
+	if(!bp) return GBPX_ERR_INVALID;
+	return static_cast<BroadPhase*>(bp)->update(created, nbCreated, updated, nbUpdated, removed, nbRemoved, bounds, groups, distances,
+	                                            capacity);
+}
+
+GBPX_API int gbpx_bp_fetch_results(void* bp, const uint32_t** created, uint32_t* nbCreated, const uint32_t** lost, uint32_t* nbLost)
+{
+	if(!bp || !created || !nbCreated || !lost || !nbLost) return GBPX_ERR_INVALID;
+	const uint2 *c = nullptr, *l = nullptr;
+	const int rc = static_cast<BroadPhase*>(bp)->fetchResults(&c, nbCreated, &l, nbLost);
+	*created = reinterpret_cast<const uint32_t*>(c);
+	*lost = reinterpret_cast<const uint32_t*>(l);
+	return rc;
+}
+
+GBPX_API int gbpx_bp_stats(void* bp, uint64_t* out4)
+{
+	if(!bp || !out4) return GBPX_ERR_INVALID;
+	memcpy(out4, static_cast<BroadPhase*>(bp)->stats, sizeof(uint64_t) * 4);
+	return GBPX_OK;
+}

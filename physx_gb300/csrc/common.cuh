@@ -1,0 +1,94 @@
+// Shared device/host helpers for the GB300 rigid-body step.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#define GBPX_API extern "C" __attribute__((visibility("default")))
+
+// Status codes returned through the C ABI (include/gbpx.h mirrors them).
+enum GbpxStatus
+{
+	GBPX_OK = 0,
+	GBPX_ERR_INVALID = -1,      // bad argument (null pointer, size out of range)
+	GBPX_ERR_CUDA = -2,         // a CUDA runtime call failed
+	GBPX_ERR_CAPACITY = -3,     // a device buffer overflowed; retried once then reported
+	GBPX_ERR_NOMEM = -4,        // device allocation failed
+	GBPX_ERR_STATE = -5,        // call sequence violated (e.g. fetch without update)
+	GBPX_ERR_BUDGET = -6,       // memory budget exceeded (serving admission)
+	GBPX_ERR_TIMEOUT = -7,      // a bounded device wait gave up
+};
+
+#define GBPX_CUDA_TRY(expr)                                                                   \
+	do {                                                                                      \
+		cudaError_t _e = (expr);                                                              \
+		if(_e != cudaSuccess) {                                                               \
+			fprintf(stderr, "[gbpx] CUDA error %s at %s:%d: %s\n", cudaGetErrorName(_e),     \
+			        __FILE__, __LINE__, cudaGetErrorString(_e));                              \
+			return GBPX_ERR_CUDA;                                                             \
+		}                                                                                     \
+	} while(0)
+
+namespace gbpx
+{
+static inline uint32_t divUp(uint64_t a, uint32_t b) { return uint32_t((a + b - 1) / b); }
+
+// Device buffer that only grows; contents are not preserved across growth unless asked.
+template <typename T>
+struct DevBuf
+{
+	T* ptr = nullptr;
+	size_t cap = 0;
+	int reserve(size_t n, cudaStream_t s = 0, bool keep = false, size_t keepCount = 0)
+	{
+		if(n <= cap) return GBPX_OK;
+		size_t nc = cap ? cap : 256;
+		while(nc < n) nc *= 2;
+		T* np = nullptr;
+		if(cudaMalloc(&np, nc * sizeof(T)) != cudaSuccess) return GBPX_ERR_NOMEM;
+		if(keep && ptr && keepCount)
+			if(cudaMemcpyAsync(np, ptr, keepCount * sizeof(T), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return GBPX_ERR_CUDA;
+		if(ptr) { cudaStreamSynchronize(s); cudaFree(ptr); }
+		ptr = np;
+		cap = nc;
+		return GBPX_OK;
+	}
+	void release() { if(ptr) cudaFree(ptr); ptr = nullptr; cap = 0; }
+};
+
+template <typename T>
+struct HostBuf
+{
+	T* ptr = nullptr;
+	size_t cap = 0;
+	int reserve(size_t n, bool keep = false)
+	{
+		if(n <= cap) return GBPX_OK;
+		size_t nc = cap ? cap : 256;
+		while(nc < n) nc *= 2;
+		T* np = nullptr;
+		if(cudaMallocHost(&np, nc * sizeof(T)) != cudaSuccess) return GBPX_ERR_NOMEM;
+		if(keep && ptr) memcpy(np, ptr, cap * sizeof(T));
+		if(ptr) cudaFreeHost(ptr);
+		ptr = np;
+		cap = nc;
+		return GBPX_OK;
+	}
+	void release() { if(ptr) cudaFreeHost(ptr); ptr = nullptr; cap = 0; }
+};
+
+// IEEE-754 float bits -> order-preserving unsigned key (negatives reversed,
+// positives shifted above them).  -0.0 maps just below +0.0.
+__host__ __device__ __forceinline__ uint32_t encodeFloatBits(uint32_t ir)
+{
+	return (ir & 0x80000000u) ? ~ir : (ir | 0x80000000u);
+}
+
+__device__ __forceinline__ uint32_t laneMaskLt()
+{
+	uint32_t m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
+} // namespace gbpx

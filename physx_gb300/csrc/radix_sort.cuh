@@ -1,0 +1,184 @@
+// Stable LSD radix sort (8-bit digits) for 32- and 64-bit keys with optional
+// 32-bit values.  Hand-written for sm_103a: per-tile digit histograms, one
+// scan over the (digit-major) histogram table, then a stable scatter where
+// each warp ranks its keys with __match_any_sync and a per-warp counter row
+// in shared memory.
+//
+// Tiles are 256 threads x 8 keys.  Warp w of a tile owns the contiguous key
+// range [w*256, w*256+256) of the tile, which keeps the scatter stable.
+#pragma once
+#include "common.cuh"
+
+namespace gbpx
+{
+namespace rs
+{
+constexpr int THREADS = 256;
+constexpr int ITEMS = 8;
+constexpr int TILE = THREADS * ITEMS;
+constexpr int WARPS = THREADS / 32;
+constexpr int WARP_SPAN = 32 * ITEMS;
+
+template <typename K>
+__global__ void __launch_bounds__(THREADS) histogramKernel(const K* __restrict__ keys, uint32_t n, int shift, uint32_t numTiles,
+                                                           uint32_t* __restrict__ hist)
+{
+	__shared__ uint32_t h[256];
+	h[threadIdx.x] = 0;
+	__syncthreads();
+	const uint64_t base = uint64_t(blockIdx.x) * TILE;
+#pragma unroll
+	for(int i = 0; i < ITEMS; i++)
+	{
+		const uint64_t idx = base + uint64_t(i) * THREADS + threadIdx.x;
+		if(idx < n)
+		{
+			const uint32_t d = uint32_t(keys[idx] >> shift) & 0xffu;
+			atomicAdd(&h[d], 1u);
+		}
+	}
+	__syncthreads();
+	hist[uint64_t(threadIdx.x) * numTiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of `count` u32 values in place by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) scanKernel(uint32_t* __restrict__ data, uint32_t count)
+{
+	__shared__ uint32_t warpSums[32];
+	__shared__ uint32_t carry;
+	if(threadIdx.x == 0) carry = 0;
+	__syncthreads();
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for(uint32_t start = 0; start < count; start += 1024 * 4)
+	{
+		uint32_t v[4];
+		uint32_t local = 0;
+		const uint32_t b = start + threadIdx.x * 4;
+#pragma unroll
+		for(int k = 0; k < 4; k++)
+		{
+			v[k] = (b + k < count) ? data[b + k] : 0u;
+			local += v[k];
+		}
+		uint32_t incl = local;
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1)
+		{
+			const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+			if(lane >= uint32_t(o)) incl += t;
+		}
+		if(lane == 31) warpSums[warp] = incl;
+		__syncthreads();
+		if(warp == 0)
+		{
+			uint32_t ws = warpSums[lane];
+			uint32_t wi = ws;
+#pragma unroll
+			for(int o = 1; o < 32; o <<= 1)
+			{
+				const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+				if(lane >= uint32_t(o)) wi += t;
+			}
+			warpSums[lane] = wi - ws;
+		}
+		__syncthreads();
+		uint32_t run = carry + warpSums[warp] + incl - local;
+#pragma unroll
+		for(int k = 0; k < 4; k++)
+		{
+			if(b + k < count) data[b + k] = run;
+			run += v[k];
+		}
+		__syncthreads();
+		if(threadIdx.x == 1023) carry = run;
+		__syncthreads();
+	}
+}
+
+template <typename K, bool HAS_VAL>
+__global__ void __launch_bounds__(THREADS) scatterKernel(const K* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+                                                         K* __restrict__ keysOut, uint32_t* __restrict__ valsOut, uint32_t n,
+                                                         int shift, uint32_t numTiles, const uint32_t* __restrict__ offsets)
+{
+	__shared__ uint32_t cnt[WARPS][256];
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for(int d = threadIdx.x; d < WARPS * 256; d += THREADS) (&cnt[0][0])[d] = 0;
+	__syncthreads();
+
+	const uint64_t base = uint64_t(blockIdx.x) * TILE + uint64_t(warp) * WARP_SPAN;
+	K key[ITEMS];
+	uint32_t val[ITEMS];
+	uint32_t rank[ITEMS];
+	const uint32_t lt = laneMaskLt();
+#pragma unroll
+	for(int i = 0; i < ITEMS; i++)
+	{
+		const uint64_t idx = base + uint64_t(i) * 32 + lane;
+		const bool valid = idx < n;
+		key[i] = valid ? keysIn[idx] : K(0);
+		if(HAS_VAL) val[i] = valid ? valsIn[idx] : 0u;
+		const uint32_t d = valid ? (uint32_t(key[i] >> shift) & 0xffu) : 0x100u;
+		const uint32_t peers = __match_any_sync(0xffffffffu, d);
+		uint32_t c = 0;
+		if(valid) c = cnt[warp][d];
+		__syncwarp();
+		rank[i] = c + __popc(peers & lt);
+		const bool leader = (peers & lt) == 0;
+		if(valid && leader) cnt[warp][d] = c + __popc(peers);
+		__syncwarp();
+	}
+	__syncthreads();
+	{
+		const uint32_t d = threadIdx.x;  // THREADS == 256 digits
+		uint32_t run = offsets[uint64_t(d) * numTiles + blockIdx.x];
+#pragma unroll
+		for(int w = 0; w < WARPS; w++)
+		{
+			const uint32_t t = cnt[w][d];
+			cnt[w][d] = run;
+			run += t;
+		}
+	}
+	__syncthreads();
+#pragma unroll
+	for(int i = 0; i < ITEMS; i++)
+	{
+		const uint64_t idx = base + uint64_t(i) * 32 + lane;
+		if(idx < n)
+		{
+			const uint32_t d = uint32_t(key[i] >> shift) & 0xffu;
+			const uint32_t dst = cnt[warp][d] + rank[i];
+			keysOut[dst] = key[i];
+			if(HAS_VAL) valsOut[dst] = val[i];
+		}
+	}
+}
+} // namespace rs
+
+// Scratch needed by radixSort for n keys (histogram table, u32 entries).
+static inline size_t radixSortHistEntries(uint32_t n) { return size_t(256) * (divUp(n ? n : 1, rs::TILE)); }
+
+// Sorts keys[0..n) (and vals) on bits [beginBit, endBit).  Ping-pongs between
+// (keys, vals) and (keysAlt, valsAlt); returns true if the result ended in the
+// Alt buffers.
+template <typename K, bool HAS_VAL>
+static bool radixSort(K* keys, uint32_t* vals, K* keysAlt, uint32_t* valsAlt, uint32_t n, int beginBit, int endBit,
+                      uint32_t* hist, cudaStream_t s)
+{
+	if(n <= 1) return false;
+	const uint32_t numTiles = divUp(n, rs::TILE);
+	bool inAlt = false;
+	for(int shift = beginBit; shift < endBit; shift += 8)
+	{
+		const K* kin = inAlt ? keysAlt : keys;
+		const uint32_t* vin = inAlt ? valsAlt : vals;
+		K* kout = inAlt ? keys : keysAlt;
+		uint32_t* vout = inAlt ? vals : valsAlt;
+		rs::histogramKernel<K><<<numTiles, rs::THREADS, 0, s>>>(kin, n, shift, numTiles, hist);
+		rs::scanKernel<<<1, 1024, 0, s>>>(hist, 256u * numTiles);
+		rs::scatterKernel<K, HAS_VAL><<<numTiles, rs::THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, numTiles, hist);
+		inAlt = !inAlt;
+	}
+	return inAlt;
+}
+} // namespace gbpx

@@ -1,0 +1,28 @@
+// Device discovery and small runtime helpers exported through the C ABI.
+#include "common.cuh"
+
+GBPX_API int gbpx_device_count(int* out)
+{
+	if(!out) return GBPX_ERR_INVALID;
+	int n = 0;
+	if(cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); n = 0; }
+	*out = n;
+	return GBPX_OK;
+}
+
+// name (up to 256 bytes), SM count, compute capability major*10+minor.
+GBPX_API int gbpx_device_info(int device, char* name, int nameBytes, int* smCount, int* cc)
+{
+	cudaDeviceProp p;
+	GBPX_CUDA_TRY(cudaGetDeviceProperties(&p, device));
+	if(name && nameBytes > 0) { strncpy(name, p.name, size_t(nameBytes) - 1); name[nameBytes - 1] = 0; }
+	if(smCount) *smCount = p.multiProcessorCount;
+	if(cc) *cc = p.major * 10 + p.minor;
+	return GBPX_OK;
+}
+
+GBPX_API int gbpx_device_synchronize(void)
+{
+	GBPX_CUDA_TRY(cudaDeviceSynchronize());
+	return GBPX_OK;
+}

@@ -1,0 +1,35 @@
+"""The C-ABI library builds, loads and exports every symbol include/*.h declares.
+Runs without a GPU (no compute calls)."""
+import ctypes
+import glob
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names.update(re.findall(r"\b(gbpx_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "gbpx_bp_update" in syms and len(syms) >= 8
+
+
+def test_library_exports_every_declared_symbol(gbpx_built):
+    lib = ctypes.CDLL(gbpx_built)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_no_visible_internal_symbols(gbpx_built):
+    # Only the C ABI is exported (hidden visibility for everything else).
+    out = os.popen("nm -D --defined-only %s" % gbpx_built).read()
+    exported = [l.split()[-1] for l in out.splitlines() if " T " in l]
+    assert exported and all(s.startswith("gbpx_") for s in exported), [s for s in exported if not s.startswith("gbpx_")][:10]
