@@ -60,6 +60,18 @@ uint32_t gbpx_bp_static_filter_group(void);
 uint32_t gbpx_bp_dynamic_filter_group(uint32_t id);
 uint32_t gbpx_bp_kinematic_filter_group(uint32_t id);
 
+/* -------------------------------------------------------------- narrowphase
+ * immediate::PxGenerateContacts (physx/include/PxImmediateMode.h:267) for
+ * sphere / plane / capsule / box pairs with a fresh PxCache per pair.
+ * type: PxGeometryType (0 sphere, 1 plane, 2 capsule, 3 box); geom: 4 floats
+ * (sphere r | capsule r, halfHeight | box hx, hy, hz); pose: PxTransform.
+ * outContacts: nbPairs x maxPerPair x 8 floats (normal xyz, separation,
+ * point xyz, 0); outCounts: contacts per pair.  The normal points along the
+ * direction shape0 must move, as PxContactPoint (geomutils/PxContactPoint.h:39). */
+int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                           const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
+                           float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts);
+
 #ifdef __cplusplus
 }
 #endif

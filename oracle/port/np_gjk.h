@@ -44,11 +44,4 @@ struct GjkResult
 	float penDep;
 };
 
-struct MatTr;
-
-// Box-box edge-edge fallback (GJK/EPA between the boxes) and the capsule-box
-// full manifold: not restated yet, so these pairs report no contact.  The
-// tests mark the affected configurations and skip them.
-static inline bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
-static inline bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, void*, int&, V3&) { return false; }
 } // namespace orc

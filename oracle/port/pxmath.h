@@ -169,6 +169,18 @@ static inline M33 m33FromQuatS(Q q)
 	m.c2 = v3(xz + yw, yz - xw, 1.0f - xx - yy);
 	return m;
 }
+// QuatGetMat33V, column-output SSE form (PxVecMathSSE.h:54), used by
+// PxMatTransformV and PxMat33Padded: columns are v*2q_i + (2w*w - 1 / +-2w*q_j)
+static inline M33 m33FromQuatCol(Q q)
+{
+	const float x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z, w2 = q.w + q.w;
+	const float qx = x2 * q.w, qy = y2 * q.w, qz = z2 * q.w, qw = w2 * q.w + (-1.0f);
+	M33 m;
+	m.c0 = v3(q.x * x2 + qw, q.y * x2 + qz, q.z * x2 + (-qy));
+	m.c1 = v3(q.x * y2 + (-qz), q.y * y2 + qw, q.z * y2 + qx);
+	m.c2 = v3(q.x * z2 + qy, q.y * z2 + (-qx), q.z * z2 + qw);
+	return m;
+}
 // PxMat33 * PxVec3 (scalar): c0*x + c1*y + c2*z
 static inline V3 m33MulVS(const M33& m, V3 v)
 {

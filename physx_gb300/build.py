@@ -15,7 +15,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbpx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+# --fmad=false: no fused multiply-add, so contact and solver arithmetic rounds
+# like the reference (whose SSE2 build has no FMA).  IEEE division and square
+# root stay on (no fast-math flags).
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                      "-I" + os.path.join(os.path.dirname(HERE), "include")]
 
 
@@ -41,6 +44,14 @@ def _compile(nvcc, src):
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(NVCC_FLAGS)
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for f in os.listdir(BUILD):
+            if f.endswith(".o"):
+                os.remove(os.path.join(BUILD, f))
+        with open(stamp, "w") as fh:
+            fh.write(flags)
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s), srcs))

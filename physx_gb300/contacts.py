@@ -1,0 +1,41 @@
+"""immediate::PxGenerateContacts mirror over the GB300 narrowphase.
+
+Mirrors physx/include/PxImmediateMode.h:267 for sphere / plane / capsule / box
+geometries with a fresh PxCache per pair.  Pairs are given as arrays:
+type0/type1 (PxGeometryType), geom0/geom1 (4 floats), pose0/pose1 (7 floats
+qx qy qz qw px py pz).  Contacts come back as (counts, contacts[n, max, 8]).
+"""
+import ctypes
+
+import numpy as np
+
+from . import GbpxError, check, lib
+
+_ARG_KEYS = ("type0", "geom0", "type1", "geom1", "pose0", "pose1")
+_DTYPES = (np.int32, np.float32, np.int32, np.float32, np.float32, np.float32)
+
+
+def _setup():
+    L = lib()
+    if not getattr(L, "_np_ready", False):
+        L.gbpx_generate_contacts.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                                                     ctypes.c_float, ctypes.c_void_p, ctypes.c_uint32,
+                                                                     ctypes.c_void_p]
+        L._np_ready = True
+    return L
+
+
+def generate_contacts(pairs, contact_distance=0.04, mesh_contact_margin=0.01, tolerance_length=1.0, max_per_pair=4):
+    L = _setup()
+    arrs = [np.ascontiguousarray(pairs[k], dtype=d) for k, d in zip(_ARG_KEYS, _DTYPES)]
+    n = len(arrs[0])
+    out = np.zeros((n, max_per_pair, 8), np.float32)
+    cnt = np.zeros(n, np.uint32)
+    rc = L.gbpx_generate_contacts(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], n, contact_distance, mesh_contact_margin,
+                                  tolerance_length, out.ctypes.data_as(ctypes.c_void_p), max_per_pair,
+                                  cnt.ctypes.data_as(ctypes.c_void_p))
+    if rc not in (0, -3):
+        check(rc, "PxGenerateContacts")
+    if rc == -3:
+        raise GbpxError(rc, "PxGenerateContacts (more contacts than max_per_pair)")
+    return cnt, out

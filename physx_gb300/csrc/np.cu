@@ -1,0 +1,175 @@
+// Narrowphase for the GB300 rigid-body step: immediate::PxGenerateContacts
+// (physx/include/PxImmediateMode.h:267, physx/source/immediatemode/src/NpImmediateMode.cpp:732)
+// over a batch of sphere / plane / capsule / box pairs, with fresh-cache
+// semantics (the persistent manifold is regenerated for every call).
+//
+// GB300 layout: the batch is bucketed by (type0, type1) with a 16-bin counting
+// pass so every warp runs a single generator (no divergence between pair
+// types); each lane runs one pair and writes its <= 4 contacts as float4 pairs
+// (normal|separation, point|0) into a fixed 4-slot record, so no compaction is
+// needed and the host reads counts + records in one copy.
+#include "common.cuh"
+#include "contacts.cuh"
+
+namespace gbpx
+{
+namespace np
+{
+struct PairRef   // one pair of the caller's batch (AoS arrays of the C ABI)
+{
+	const int* type0; const float* geom0; const int* type1; const float* geom1; const float* pose0; const float* pose1;
+};
+
+__device__ __forceinline__ Tr loadPose7(const float* p)
+{
+	Tr t;
+	t.q.x = p[0]; t.q.y = p[1]; t.q.z = p[2]; t.q.w = p[3];
+	t.p = v3(p[4], p[5], p[6]);
+	return t;
+}
+
+__device__ __forceinline__ uint32_t pairKey(int t0, int t1)
+{
+	const int a = t0 < t1 ? t0 : t1, b = t0 < t1 ? t1 : t0;
+	return uint32_t(((a & 3) << 2) | (b & 3));
+}
+
+__global__ void bucketCountKernel(PairRef pr, uint32_t n, uint32_t* __restrict__ hist)
+{
+	__shared__ uint32_t h[16];
+	if(threadIdx.x < 16) h[threadIdx.x] = 0;
+	__syncthreads();
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n) atomicAdd(&h[pairKey(pr.type0[i], pr.type1[i])], 1u);
+	__syncthreads();
+	if(threadIdx.x < 16 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void bucketOffsetsKernel(uint32_t* __restrict__ hist)
+{
+	if(threadIdx.x == 0)
+	{
+		uint32_t run = 0;
+		for(int k = 0; k < 16; k++) { const uint32_t c = hist[k]; hist[k] = run; hist[16 + k] = run; run += c; }
+	}
+}
+
+__global__ void bucketScatterKernel(PairRef pr, uint32_t n, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const uint32_t slot = atomicAdd(&cursor[pairKey(pr.type0[i], pr.type1[i])], 1u);
+	perm[slot] = i;
+}
+
+// One lane per pair (in bucket order).  out: n x 4 contacts x 2 float4.
+__global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t* __restrict__ perm, uint32_t n, float contactDistance,
+                                                      float toleranceLength, float4* __restrict__ out, uint32_t* __restrict__ counts)
+{
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= n) return;
+	const uint32_t i = perm[k];
+	int ta = pr.type0[i], tb = pr.type1[i];
+	float ga[4], gb[4];
+#pragma unroll
+	for(int c = 0; c < 4; c++) { ga[c] = pr.geom0[4 * size_t(i) + c]; gb[c] = pr.geom1[4 * size_t(i) + c]; }
+	Tr pa = loadPose7(pr.pose0 + 7 * size_t(i)), pb = loadPose7(pr.pose1 + 7 * size_t(i));
+	const bool swap = ta > tb;
+	if(swap)
+	{
+		const int t = ta; ta = tb; tb = t;
+		for(int c = 0; c < 4; c++) { const float x = ga[c]; ga[c] = gb[c]; gb[c] = x; }
+		const Tr t2 = pa; pa = pb; pb = t2;
+	}
+	Buffer buf;
+	generate(ta, ga, tb, gb, pa, pb, contactDistance, toleranceLength, buf);
+	counts[i] = uint32_t(buf.count);
+	float4* o = out + size_t(i) * 8;
+	for(int c = 0; c < buf.count; c++)
+	{
+		V3 nn = buf.c[c].n;
+		if(swap) nn = neg(nn);
+		o[2 * c] = make_float4(nn.x, nn.y, nn.z, buf.c[c].sep);
+		o[2 * c + 1] = make_float4(buf.c[c].p.x, buf.c[c].p.y, buf.c[c].p.z, 0.0f);
+	}
+}
+} // namespace np
+
+// Per-call device workspace of the immediate-mode narrowphase entry point.
+struct NpWorkspace
+{
+	cudaStream_t stream = 0;
+	DevBuf<int> t0, t1;
+	DevBuf<float> g0, g1, p0, p1;
+	DevBuf<uint32_t> hist, perm, counts;
+	DevBuf<float4> out;
+	HostBuf<float4> hOut;
+	HostBuf<uint32_t> hCounts;
+	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
+};
+
+static NpWorkspace* npWorkspace()
+{
+	static NpWorkspace* ws = nullptr;
+	if(!ws)
+	{
+		ws = new NpWorkspace;
+		if(ws->init()) { delete ws; ws = nullptr; }
+	}
+	return ws;
+}
+} // namespace gbpx
+
+using namespace gbpx;
+
+// PxGenerateContacts over nbPairs pairs (host arrays, fresh caches).  Layout:
+// geometry type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box) and 4
+// floats per shape, poses 7 floats, contacts 8 floats (normal, separation,
+// point, 0) with maxPerPair slots per pair.  Returns GBPX_ERR_CAPACITY if a
+// pair produced more than maxPerPair contacts (counts are still exact).
+GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                                    const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
+                                    float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts)
+{
+	(void)meshContactMargin;
+	if(!nbPairs) return GBPX_OK;
+	if(!type0 || !geom0 || !type1 || !geom1 || !pose0 || !pose1 || !outContacts || !outCounts || !maxPerPair) return GBPX_ERR_INVALID;
+	if(!(contactDistance > 0.0f) || !(toleranceLength > 0.0f)) return GBPX_ERR_INVALID;
+	for(uint32_t i = 0; i < nbPairs; i++)
+		if(uint32_t(type0[i]) > 3u || uint32_t(type1[i]) > 3u) return GBPX_ERR_INVALID;
+	NpWorkspace* ws = npWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	const size_t n = nbPairs;
+	if(ws->t0.reserve(n) || ws->t1.reserve(n) || ws->g0.reserve(4 * n) || ws->g1.reserve(4 * n) || ws->p0.reserve(7 * n) ||
+	   ws->p1.reserve(7 * n) || ws->hist.reserve(32) || ws->perm.reserve(n) || ws->counts.reserve(n) || ws->out.reserve(8 * n) ||
+	   ws->hOut.reserve(8 * n) || ws->hCounts.reserve(n))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->t0.ptr, type0, n * 4, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->t1.ptr, type1, n * 4, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->g0.ptr, geom0, n * 16, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->g1.ptr, geom1, n * 16, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->p0.ptr, pose0, n * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->p1.ptr, pose1, n * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemsetAsync(ws->hist.ptr, 0, 32 * 4, s));
+	np::PairRef pr = {ws->t0.ptr, ws->g0.ptr, ws->t1.ptr, ws->g1.ptr, ws->p0.ptr, ws->p1.ptr};
+	const uint32_t blocks = divUp(n, 256);
+	np::bucketCountKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr);
+	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(ws->hist.ptr);
+	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr + 16, ws->perm.ptr);
+	np::generateKernel<<<divUp(n, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPairs, contactDistance, toleranceLength, ws->out.ptr, ws->counts.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->hCounts.ptr, ws->counts.ptr, n * 4, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->hOut.ptr, ws->out.ptr, n * 8 * sizeof(float4), cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	int rc = GBPX_OK;
+	for(size_t i = 0; i < n; i++)
+	{
+		const uint32_t c = ws->hCounts.ptr[i];
+		outCounts[i] = c;
+		if(c > maxPerPair) rc = GBPX_ERR_CAPACITY;
+		const uint32_t m = c < maxPerPair ? c : maxPerPair;
+		memcpy(outContacts + i * maxPerPair * 8, ws->hOut.ptr + i * 8, size_t(m) * 8 * sizeof(float));
+	}
+	return rc;
+}

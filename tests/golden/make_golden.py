@@ -17,8 +17,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_libs import CpuBroadPhase, reference  # noqa: E402
-from scenarios import bp_frames  # noqa: E402
+from oracle_libs import CpuBroadPhase, reference, run_contacts  # noqa: E402
+from scenarios import bp_frames, np_pairs  # noqa: E402
 
 BP_CASES = [
     # name, seed, boxes, frames, extent
@@ -44,9 +44,27 @@ def make_bp():
         print("wrote", name)
 
 
+NP_CASES = [
+    # name, seed, pairs: near-contact pairs of every sphere/plane/capsule/box combination
+    ("np_mixed", 17, 3000),
+]
+
+
+def make_np():
+    for name, seed, n in NP_CASES:
+        pairs = np_pairs(seed, n)
+        cnt, out = run_contacts("pxref", pairs, max_per_pair=8)
+        packed = np.concatenate([out[i, :cnt[i]] for i in range(n) if cnt[i]]) if cnt.sum() else np.zeros((0, 8), np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), counts=cnt, contacts=packed.astype(np.float32),
+                            contact_distance=np.float32(0.04), tolerance_length=np.float32(1.0), **pairs)
+        print("wrote", name)
+
+
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp"]
+    which = sys.argv[1:] or ["bp", "np"]
     if "bp" in which:
         make_bp()
+    if "np" in which:
+        make_np()

@@ -70,3 +70,95 @@ class CpuBroadPhase:
         if self.h:
             getattr(self.L, self.pre + "_bp_release")(self.h)
             self.h = None
+
+
+def run_contacts(which, pairs, contact_distance=0.04, mesh_margin=0.01, tolerance_length=1.0, max_per_pair=16):
+    """PxGenerateContacts with fresh caches: returns (counts, contacts[n, max, 8])."""
+    n = len(pairs["type0"])
+    out = np.zeros((n, max_per_pair, 8), np.float32)
+    cnt = np.zeros(n, np.uint32)
+    args = [_p(np.ascontiguousarray(pairs[k])) for k in ("type0", "geom0", "type1", "geom1", "pose0", "pose1")]
+    if which == "orc":
+        L = oracle()
+        rc = L.orc_np_run(*args, ctypes.c_uint32(n), ctypes.c_float(contact_distance), ctypes.c_float(mesh_margin),
+                          ctypes.c_float(tolerance_length), _p(out), ctypes.c_uint32(max_per_pair), _p(cnt))
+    else:
+        L = reference()
+        L.pxref_np_create.restype = ctypes.c_void_p
+        ctx = ctypes.c_void_p(L.pxref_np_create(ctypes.c_uint32(n)))
+        rc = L.pxref_np_run(ctx, *args, ctypes.c_uint32(n), ctypes.c_float(contact_distance), ctypes.c_float(mesh_margin),
+                            ctypes.c_float(tolerance_length), 1, _p(out), ctypes.c_uint32(max_per_pair), _p(cnt))
+        L.pxref_np_release(ctx)
+    assert rc == 0, "contact buffer overflow"
+    return cnt, out
+
+
+def scene_pairs(scene):
+    """All dynamic-dynamic pairs (i < j) and every dynamic body against every static
+    shape, in that order: (bodyA, bodyB) with statics indexed after the dynamics."""
+    n = len(scene["types"])
+    m = len(scene["static_poses"])
+    A, B = [], []
+    for i in range(n):
+        for j in range(i + 1, n):
+            A.append(i)
+            B.append(j)
+        for s in range(m):
+            A.append(i)
+            B.append(n + s)
+    return np.array(A, np.uint32), np.array(B, np.uint32)
+
+
+def scene_contacts(which, scene, A, B, contact_distance=0.04):
+    """Fresh-cache contacts for the given pairs (through `which` narrowphase);
+    returns per-pair (start, count) into a packed contact array plus the pair materials."""
+    n = len(scene["types"])
+    rb = scene["rigid"]
+
+    def pose_of(k):
+        if k < n:
+            return np.concatenate([rb[k]["q"], rb[k]["p"]]).astype(np.float32)
+        return scene["static_poses"][k - n]
+
+    def geom_of(k):
+        return (scene["types"][k], scene["geoms"][k]) if k < n else (scene["static_types"][k - n], scene["static_geoms"][k - n])
+
+    pairs = dict(type0=np.array([geom_of(a)[0] for a in A], np.int32), geom0=np.array([geom_of(a)[1] for a in A], np.float32),
+                 type1=np.array([geom_of(b)[0] for b in B], np.int32), geom1=np.array([geom_of(b)[1] for b in B], np.float32),
+                 pose0=np.array([pose_of(a) for a in A], np.float32), pose1=np.array([pose_of(b) for b in B], np.float32))
+    cnt, out = run_contacts(which, pairs, contact_distance=contact_distance)
+    keep = np.flatnonzero(cnt > 0)
+    start = np.zeros(len(keep), np.uint32)
+    count = cnt[keep].astype(np.uint32)
+    start[1:] = np.cumsum(count)[:-1]
+    packed = np.concatenate([out[k, :cnt[k]] for k in keep]) if len(keep) else np.zeros((0, 8), np.float32)
+    fr = scene["friction"]
+    mat = np.zeros((len(keep), 3), np.float32)
+    for r, k in enumerate(keep):
+        fa = fr[A[k]]
+        fb = fr[B[k]] if B[k] < n else np.float32(0.5)
+        mat[r, 0] = mat[r, 1] = np.float32((fa + fb) * np.float32(0.5))
+    return A[keep], B[keep], start, count, np.ascontiguousarray(packed, np.float32), mat
+
+
+def run_tgs(which, scene, A, B, start, count, contacts, mat, dt=1.0 / 60.0, nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0),
+            bounce=-2.0, friction_offset=0.04, correlation=0.025):
+    """One TGS solve (construct, batch, prep, solve, integrate): returns velocities (n,6),
+    poses (n,7), headers (start, stride) and the constraint order."""
+    n = len(scene["types"])
+    m = len(scene["static_poses"])
+    nc = len(A)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nc, 1) * 2, np.uint32)
+    hst = np.zeros(max(nc, 1) * 2, np.uint32)
+    order = np.zeros(max(nc, 1), np.uint32)
+    g = np.array(gravity, np.float32)
+    L = oracle() if which == "orc" else reference()
+    fn = L.orc_tgs_solve if which == "orc" else L.pxref_tgs_solve
+    fn.restype = ctypes.c_uint32
+    nh = fn(_p(scene["rigid"]), ctypes.c_uint32(n), _p(np.ascontiguousarray(scene["static_poses"], np.float32)), ctypes.c_uint32(m),
+            _p(A), _p(B), ctypes.c_uint32(nc), _p(start), _p(count), _p(contacts), _p(mat), _p(g), ctypes.c_float(dt),
+            ctypes.c_uint32(nb_pos), ctypes.c_uint32(nb_vel), ctypes.c_float(bounce), ctypes.c_float(friction_offset),
+            ctypes.c_float(correlation), _p(vel), _p(pose), _p(hs), _p(hst), _p(order), None, None)
+    return vel, pose, hs[:nh].copy(), hst[:nh].copy(), order[:nc].copy()

@@ -53,3 +53,25 @@ def test_oracle_bp_matches_reference_live(seed, n, frames, extent):
         oc, ol = orc.update(fr)
         assert np.array_equal(sorted_pairs(rc), sorted_pairs(oc))
         assert np.array_equal(sorted_pairs(rl), sorted_pairs(ol))
+
+
+NP_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "np_*.npz")))
+
+
+def load_np_fixture(path):
+    z = np.load(path)
+    pairs = {k: z[k] for k in ("type0", "geom0", "type1", "geom1", "pose0", "pose1")}
+    return pairs, z["counts"], z["contacts"], float(z["contact_distance"]), float(z["tolerance_length"])
+
+
+@pytest.mark.parametrize("path", NP_FIXTURES, ids=[os.path.basename(p) for p in NP_FIXTURES])
+def test_oracle_contacts_match_reference_golden(path):
+    from contact_compare import assert_report, compare, unpack
+    from oracle_libs import run_contacts
+    pairs, rc, rpacked, cd, tl = load_np_fixture(path)
+    oc, oo = run_contacts("orc", pairs, contact_distance=cd, tolerance_length=tl, max_per_pair=8)
+    rep = compare(pairs, rc, unpack(rc, rpacked), oc, [oo[i, :oc[i]] for i in range(len(oc))])
+    assert_report(rep)
+    # the analytic pairs are reproduced bit for bit
+    for k in ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule"):
+        assert rep[k]["maxdiff"] == 0.0, (k, rep[k])
