@@ -1,0 +1,293 @@
+"""Benchmark of the batched rigid-body step on GB300.
+
+Workload: 4096 independent scenes, body counts log-uniform in [8, 512] (sphere /
+box / capsule mix), dropped from U(1, 20) m onto a per-scene ground plane; TGS
+4 position / 1 velocity iterations, dt = 1/60 s, FP32 (synthetic, seeded).
+A step is one frame of every scene: bounds, ABP broadphase, contacts, TGS
+batching / rows / solve / integration, all in one persistent launch.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput in
+body-steps/s; `e2e` re-measures it through the public world API with the
+bodies uploaded from and downloaded to pinned host memory every step.
+`--impl reference` times the CPU restatement of the reference path (the
+oracle) on all host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s batched+served vs plain GPU step at 1e-5 tol; p50/p99 latency"
+UNIT = "body-steps/s"
+WORKLOAD = ("batched: 4096 scenes, bodies log-uniform [8,512] sphere/box/capsule, drop U(1,20) m onto per-scene plane, "
+            "ABP + contacts + TGS 4/1, dt 1/60, FP32")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbpx", choices=["gbpx", "reference"])
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--preroll", type=int, default=120, help="untimed steps first, so bodies have landed (contact-rich state)")
+    ap.add_argument("--cpu-scenes", type=int, default=1024, help="scenes in the bounded CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--plain-scenes", type=int, default=256, help="scenes timed one-per-launch for the plain comparison")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle restatement, all cores)
+def _cpu_worker(payload):
+    import ctypes
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import _p, oracle
+    scenes, pv, it, steps = payload
+    L = oracle()
+    keep = [np.ascontiguousarray(scenes[k], d) for k, d in (("body_count", np.uint32), ("static_count", np.uint32), ("types", np.int32),
+                                                              ("geoms", np.float32), ("friction", np.float32), ("static_poses", np.float32),
+                                                              ("static_types", np.int32), ("static_geoms", np.float32))]
+    rb = np.ascontiguousarray(scenes["rigid"]).copy()
+    t = time.perf_counter()
+    for _ in range(steps):
+        L.orc_scene_step(ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]),
+                         _p(keep[5]), _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
+    return time.perf_counter() - t, int(keep[0].sum())
+
+
+def split_scenes(scenes, idx):
+    import numpy as np
+    counts = scenes["body_count"]
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    sel = np.concatenate([np.arange(starts[i], starts[i] + counts[i]) for i in idx]) if len(idx) else np.zeros(0, np.int64)
+    return dict(body_count=counts[idx], static_count=scenes["static_count"][idx], rigid=scenes["rigid"][sel], types=scenes["types"][sel],
+                geoms=scenes["geoms"][sel], friction=scenes["friction"][sel], static_poses=scenes["static_poses"][idx],
+                static_types=scenes["static_types"][idx], static_geoms=scenes["static_geoms"][idx])
+
+
+def cpu_baseline(scenes, params, nb_scenes, steps, pool, cores):
+    """Oracle restatement of the reference step on a bounded sample, scenes split across `cores` processes."""
+    import numpy as np
+    from physx_gb300.world import param_vector
+    pv, it = param_vector(params)
+    # an even spread of scene sizes: every k-th scene
+    S = len(scenes["body_count"])
+    idx = np.linspace(0, S - 1, min(nb_scenes, S)).astype(np.int64)
+    chunks = [idx[i::cores] for i in range(cores)]
+    payloads = [(split_scenes(scenes, c), pv, it, steps) for c in chunks if len(c)]
+    t = time.perf_counter()
+    res = list(pool.map(_cpu_worker, payloads))
+    wall = time.perf_counter() - t
+    bodies = sum(r[1] for r in res)
+    return dict(value=bodies * steps / wall, unit=UNIT, cores=cores, kind="port",
+                sample="%d of %d scenes (%d bodies) x %d steps, oracle restatement, %d processes" % (len(idx), S, bodies, steps, cores),
+                seconds=wall)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                                          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                                          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = sorted(float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit())
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 3 + k and s[3 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per step-kernel launch from the committed ncu summary, scaled to the workload, if present."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_batched.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_body_step:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def dist_setup(n):
+    if n <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist.init_process_group("gloo", init_method="env://")
+    return rank, world, dist
+
+
+def main():
+    a = parse()
+    import numpy as np
+    rank, world, dist = dist_setup(a.gpus)
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import DEFAULT_PARAMS
+    cores = os.cpu_count() or 1
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        scenes = batched_scenes(a.seed, a.scenes)
+        with ctx.Pool(cores) as pool:
+            # warm-up (builds the oracle library, pages code in)
+            for _ in range(max(1, min(a.warmup, 1))):
+                cpu_baseline(scenes, DEFAULT_PARAMS, min(a.cpu_scenes, 32), 1, pool, cores)
+            per_step = []
+            for _ in range(a.steps):
+                r = cpu_baseline(scenes, DEFAULT_PARAMS, a.cpu_scenes, 1, pool, cores)
+                per_step.append(r)
+        value = sum(r["value"] for r in per_step) / len(per_step)
+        ms = 1000.0 * sum(r["seconds"] for r in per_step) / len(per_step)
+        line = dict(impl="reference", metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
+                    ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
+                    config=dict(workload=WORKLOAD, scenes=a.scenes, sample_scenes=a.cpu_scenes, l2="n/a (CPU)"),
+                    cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind="port", sample=per_step[0]["sample"]),
+                    e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line))
+        return
+
+    # CPU baseline pool is spawned before any CUDA call
+    pool = None
+    if rank == 0:
+        import multiprocessing as mp
+        pool = mp.get_context("spawn").Pool(cores)
+    import physx_gb300
+    physx_gb300.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from physx_gb300.world import World
+    scenes = batched_scenes(a.seed + 1000 * rank, a.scenes)
+    w = World(scenes)
+    info = w.info()
+    bodies = info["bodies"]
+    # pre-roll to a contact-rich state, then warm up (builds the graph)
+    w.step(a.preroll, graph=True)
+    w.step(a.warmup, graph=True)
+    w.synchronize()
+    state = w.get_bodies()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    ms = w.time_steps(a.steps, graph=True)
+    clk = clocks.stop()
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        bt = torch.tensor([bodies], dtype=torch.float64)
+        dist.all_reduce(bt)
+        total_bodies = int(bt.item())
+    else:
+        total_bodies = bodies
+    status = w.status()
+    st = w.stats()
+    value = total_bodies * a.steps / (ms / 1000.0)
+
+    # end to end through host memory: upload bodies, step, download, every step
+    host_in = w.pinned_bodies()
+    host_out = w.pinned_bodies()
+    host_out[:] = state
+    e2e_ms = 0.0
+    for _ in range(a.steps):
+        host_in[:] = host_out
+        e2e_ms += w.step_host(host_in, host_out, 1, graph=True)
+    e2e_value = bodies * a.steps / (e2e_ms / 1000.0)
+
+    # plain comparison: the same scenes, one scene per launch
+    counts = scenes["body_count"]
+    idx = np.linspace(0, len(counts) - 1, min(a.plain_scenes, len(counts))).astype(np.int64)
+    plain_ms = 0.0
+    plain_bodies = 0
+    for i in idx:
+        plain_ms += w.time_plain(int(i), 1)
+        plain_bodies += int(counts[i])
+    plain_value = plain_bodies / (plain_ms / 1000.0)
+
+    # roofline of the step kernel: compulsory HBM bytes per step (bodies read+written,
+    # pair records, contacts written and read) over the event-timed step
+    bytes_step = bodies * (96 + 52) + st["pairs"] * 108 + st["contacts"] * 64
+    achieved = bytes_step / (ms / a.steps / 1000.0) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic_per_body = profiled_traffic()
+    roofline = dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                    traffic=(traffic_per_body * bodies if traffic_per_body else None), peak_source=peak_kind,
+                    algorithmic_bytes_per_step=bytes_step)
+    cpu = None
+    if rank == 0:
+        cpu = cpu_baseline(dict(scenes, rigid=state), DEFAULT_PARAMS, a.cpu_scenes, a.cpu_steps, pool, cores)
+        cpu.pop("seconds", None)
+        pool.close()
+    if rank != 0:
+        return
+    line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
+                config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
+                            constraints_per_step=st["constraints"], contacts_per_step=st["contacts"], graph=True,
+                            l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
+                            parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),
+                e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=bodies * 96, d2h_bytes_per_step=bodies * 96),
+                plain_gpu=dict(value=plain_value, unit=UNIT, sample="%d scenes (%d bodies), one scene per launch" % (len(idx), plain_bodies),
+                               batched_over_plain=value / plain_value),
+                roofline=roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps,
+                contacts_per_s=st["contacts"] * a.steps / (ms / 1000.0), pairs_per_s=st["pairs"] * a.steps / (ms / 1000.0),
+                status_nonzero_scenes=int((status != 0).sum()))
+    print(json.dumps(line))
+    w.release()
+
+
+if __name__ == "__main__":
+    main()

@@ -33,6 +33,7 @@ extern "C" {
 int gbpx_device_count(int* out);
 int gbpx_device_info(int device, char* name, int nameBytes, int* smCount, int* computeCapability);
 int gbpx_device_synchronize(void);
+int gbpx_set_device(int device);
 
 /* ---------------------------------------------------------------- broadphase
  * ABP-compatible broadphase.  Replaces:
@@ -71,6 +72,64 @@ uint32_t gbpx_bp_kinematic_filter_group(uint32_t id);
 int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
                            const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
                            float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts);
+
+/* ---------------------------------------------------------------------- TGS
+ * Rigid bodies use PxRigidBodyData (physx/include/PxImmediateMode.h:68, 96 B).
+ *
+ * PxConstructSolverBodiesTGS (physx/include/PxImmediateMode.h:592): writes
+ * PxTGSSolverBodyVel (64 B), PxTGSSolverBodyTxInertia (64 B) and
+ * PxTGSSolverBodyData (48 B) records per body. */
+int gbpx_construct_solver_bodies_tgs(const void* rigidBodies, uint32_t nbBodies, const float* gravity, float dt, void* outBodyVel,
+                                     void* outTxInertia, void* outBodyData);
+/* PxBatchConstraintsTGS (physx/include/PxImmediateMode.h:620): constraint i
+ * joins bodies bodyA[i], bodyB[i]; indices >= nbDynamic are static/kinematic.
+ * Returns the header count; headers are (start, stride), outOrder lists the
+ * caller's constraint indices in solve order. */
+uint32_t gbpx_batch_constraints_tgs(const uint32_t* bodyA, const uint32_t* bodyB, uint32_t nbConstraints, uint32_t nbDynamic,
+                                    uint32_t nbStatic, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder);
+/* One TGS step from given contacts: PxConstructSolverBodiesTGS,
+ * PxBatchConstraintsTGS, PxCreateContactConstraintsTGS (:642),
+ * PxSolveConstraintsTGS (:716) and PxIntegrateSolverBodiesTGS (:729) with
+ * the immediate-mode settings (fresh friction data, unit mass scales).
+ * contacts: 8 floats each (normal, separation, point, 0), <= 4 per constraint;
+ * material: (static friction, dynamic friction, restitution) per constraint.
+ * outVelocity: linear + world angular (6 floats) per dynamic body; outPose:
+ * PxTransform per dynamic body. */
+int gbpx_tgs_solve(const void* rigidBodies, uint32_t nbDynamic, const float* staticPoses, uint32_t nbStatic, const uint32_t* bodyA,
+                   const uint32_t* bodyB, uint32_t nbConstraints, const uint32_t* contactStart, const uint32_t* contactCount,
+                   const float* contacts, const float* material, const float* gravity, float dt, uint32_t nbPositionIterations,
+                   uint32_t nbVelocityIterations, float bounceThreshold, float frictionOffsetThreshold, float correlationDistance,
+                   float* outVelocity, float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder,
+                   uint32_t* outNbHeaders);
+
+/* -------------------------------------------------------- batched world
+ * Many independent scenes advanced together: one persistent launch per step
+ * (optionally a CUDA graph), all state resident on the device.  Each scene's
+ * frame is the reference immediate-mode loop (physx/snippets/
+ * snippetimmediatemode/SnippetImmediateMode.cpp:473) with a fresh broadphase,
+ * PxCache and friction data per frame.  No single reference function is
+ * replaced: this is the multi-scene driver of the functions above.
+ * params (11 floats): dt, gravity xyz, contactDistance, toleranceLength,
+ * boundsMargin, bounceThreshold, frictionOffsetThreshold, correlationDistance,
+ * staticFriction; iterations: position, velocity. */
+int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, const void* rigidBodies,
+                      const int* types, const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes,
+                      const float* staticGeoms, const float* params, const uint32_t* iterations, uint32_t pairsPerBody, void** outWorld);
+void gbpx_world_release(void* world);
+int gbpx_world_step(void* world, uint32_t nbSteps, int useGraph);
+int gbpx_world_synchronize(void* world);
+int gbpx_world_get_bodies(void* world, void* outRigidBodies);
+int gbpx_world_set_bodies(void* world, const void* rigidBodies);
+int gbpx_world_status(void* world, uint32_t* outStatus);
+int gbpx_world_info(void* world, uint64_t* out6);
+int gbpx_world_scene_pairs(void* world, uint32_t scene, uint32_t* outKeys, uint32_t* outContactCounts, uint32_t capacity,
+                           uint32_t* outCount);
+int gbpx_world_time_steps(void* world, uint32_t nbSteps, int useGraph, float* outMs);
+int gbpx_world_time_plain(void* world, uint32_t firstScene, uint32_t nbScenes, float* outMs);
+int gbpx_world_stats(void* world, uint64_t* out3);
+int gbpx_world_step_host(void* world, const void* rigidIn, void* rigidOut, uint32_t nbSteps, int useGraph, float* outMs);
+int gbpx_host_alloc(size_t bytes, void** out);
+void gbpx_host_free(void* p);
 
 #ifdef __cplusplus
 }

@@ -31,6 +31,8 @@
 #include <vector>
 #include <map>
 #include <utility>
+#include <algorithm>
+#include <cmath>
 
 using namespace physx;
 using namespace physx::immediate;
@@ -509,4 +511,143 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 		storePose(outPose + 7 * a, poses[a]);
 	}
 	return nbHeaders;
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// One frame of the immediate-mode loop for many independent scenes, through
+// the reference: bounds (shape AABB + margin, same arithmetic as the GB300
+// build and the oracle) -> PxBroadPhase(eABP) with every object created (a
+// fresh broadphase per frame) -> pairs sorted by (id0, id1) ->
+// PxGenerateContacts (fresh caches) -> pxref_tgs_solve -> write-back.
+namespace
+{
+void sceneShapeBounds(int type, const float* g, const float* pose7, float margin, float* out)
+{
+	const float qx = pose7[0], qy = pose7[1], qz = pose7[2], qw = pose7[3];
+	float e[3];
+	if(type == 0) { e[0] = e[1] = e[2] = g[0]; }
+	else if(type == 2)
+	{
+		// QuatGetBasisVector0 (aos order)
+		const float x2 = qx * 2.0f, w2 = qw * 2.0f;
+		const float ax = (qw * w2 + qx * x2) - 1.0f, ay = qz * w2 + qy * x2, az = (-qy) * w2 + qz * x2;
+		e[0] = fabsf(ax) * g[1] + g[0]; e[1] = fabsf(ay) * g[1] + g[0]; e[2] = fabsf(az) * g[1] + g[0];
+	}
+	else if(type == 3)
+	{
+		// QuatGetMat33V column form (PxVecMathSSE.h)
+		const float x2 = qx + qx, y2 = qy + qy, z2 = qz + qz, w2 = qw + qw;
+		const float cx = x2 * qw, cy = y2 * qw, cz = z2 * qw, cw = w2 * qw + (-1.0f);
+		const float c0[3] = {qx * x2 + cw, qy * x2 + cz, qz * x2 + (-cy)};
+		const float c1[3] = {qx * y2 + (-cz), qy * y2 + cw, qz * y2 + cx};
+		const float c2[3] = {qx * z2 + cy, qy * z2 + (-cx), qz * z2 + cw};
+		for(int k = 0; k < 3; k++) e[k] = (fabsf(c0[k]) * g[0] + fabsf(c1[k]) * g[1]) + fabsf(c2[k]) * g[2];
+	}
+	else
+	{
+		for(int k = 0; k < 3; k++) { out[k] = -1e30f - margin; out[3 + k] = 1e30f + margin; }
+		return;
+	}
+	for(int k = 0; k < 3; k++) { out[k] = (pose7[4 + k] - e[k]) - margin; out[3 + k] = (pose7[4 + k] + e[k]) + margin; }
+}
+}
+
+HX int pxref_scene_step(PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32* sceneStaticCount, void* rigidIO, const int* types,
+	const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+	const float* params, const PxU32* iterations)
+{
+	ensureFoundation();
+	PxRigidBodyData* rigid = static_cast<PxRigidBodyData*>(rigidIO);
+	const float dt = params[0];
+	const float cDist = params[4], tolLen = params[5], margin = params[6];
+	PxU32 b0 = 0, s0 = 0;
+	for(PxU32 s = 0; s < nbScenes; s++)
+	{
+		const PxU32 n = sceneBodyCount[s], m = sceneStaticCount[s];
+		std::vector<float> bounds(6 * size_t(n + m + 1), 0.0f), pose(7 * size_t(n + m)), geom(4 * size_t(n + m));
+		std::vector<int> type(n + m);
+		std::vector<PxU32> handles(n + m), groups(n + m);
+		std::vector<float> dist(n + m, 0.0f);
+		for(PxU32 i = 0; i < n + m; i++)
+		{
+			if(i < n)
+			{
+				const PxRigidBodyData& r = rigid[b0 + i];
+				const float p7[7] = {r.body2World.q.x, r.body2World.q.y, r.body2World.q.z, r.body2World.q.w, r.body2World.p.x, r.body2World.p.y, r.body2World.p.z};
+				memcpy(&pose[7 * i], p7, 28);
+				type[i] = types[b0 + i];
+				memcpy(&geom[4 * i], geoms + 4 * size_t(b0 + i), 16);
+				groups[i] = PxGetBroadPhaseDynamicFilterGroup(i);
+			}
+			else
+			{
+				memcpy(&pose[7 * i], staticPoses + 7 * size_t(s0 + i - n), 28);
+				type[i] = staticTypes[s0 + i - n];
+				memcpy(&geom[4 * i], staticGeoms + 4 * size_t(s0 + i - n), 16);
+				groups[i] = PxGetBroadPhaseStaticFilterGroup();
+			}
+			sceneShapeBounds(type[i], &geom[4 * i], &pose[7 * i], margin, &bounds[6 * i]);
+			handles[i] = i;
+		}
+		PxBroadPhaseDesc bpDesc(PxBroadPhaseType::eABP);
+		PxBroadPhase* bp = PxCreateBroadPhase(bpDesc);
+		const PxBroadPhaseUpdateData ud(handles.data(), n + m, NULL, 0, NULL, 0, reinterpret_cast<const PxBounds3*>(bounds.data()), groups.data(),
+			dist.data(), n + m);
+		PxBroadPhaseResults res;
+		bp->update(res, ud);
+		std::vector<std::pair<PxU32, PxU32>> pairs;
+		for(PxU32 k = 0; k < res.mNbCreatedPairs; k++)
+		{
+			PxU32 a = res.mCreatedPairs[k].mID0, b = res.mCreatedPairs[k].mID1;
+			if(a > b) std::swap(a, b);
+			pairs.push_back(std::make_pair(a, b));
+		}
+		bp->release();
+		std::sort(pairs.begin(), pairs.end());
+		const size_t np = pairs.size();
+		std::vector<int> t0(np), t1(np);
+		std::vector<float> g0(4 * np), g1(4 * np), p0(7 * np), p1(7 * np);
+		for(size_t k = 0; k < np; k++)
+		{
+			const PxU32 a = pairs[k].first, b = pairs[k].second;
+			t0[k] = type[a]; t1[k] = type[b];
+			memcpy(&g0[4 * k], &geom[4 * a], 16); memcpy(&g1[4 * k], &geom[4 * b], 16);
+			memcpy(&p0[7 * k], &pose[7 * a], 28); memcpy(&p1[7 * k], &pose[7 * b], 28);
+		}
+		std::vector<float> cts(np * 8 * 8 + 8);
+		std::vector<PxU32> cnt(np + 1);
+		void* np_ = pxref_np_create(PxU32(np));
+		if(np) pxref_np_run(np_, t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), PxU32(np), cDist, 0.01f, tolLen, 1, cts.data(), 8, cnt.data());
+		pxref_np_release(np_);
+		std::vector<PxU32> ca, cb, cs, cc;
+		std::vector<float> packed, mat;
+		for(size_t k = 0; k < np; k++)
+		{
+			if(!cnt[k]) continue;
+			ca.push_back(pairs[k].first); cb.push_back(pairs[k].second);
+			cs.push_back(PxU32(packed.size() / 8)); cc.push_back(cnt[k]);
+			packed.insert(packed.end(), &cts[k * 64], &cts[k * 64] + 8 * cnt[k]);
+			const float fa = friction[b0 + pairs[k].first];
+			const float fb = pairs[k].second < n ? friction[b0 + pairs[k].second] : params[10];
+			const float mu = (fa + fb) * 0.5f;
+			mat.push_back(mu); mat.push_back(mu); mat.push_back(0.0f);
+		}
+		std::vector<float> vel(6 * size_t(n)), outPose(7 * size_t(n)), statics(7 * size_t(m) + 7);
+		std::vector<PxU32> hs(2 * ca.size() + 2), hst(2 * ca.size() + 2), ord(ca.size() + 1);
+		for(PxU32 k = 0; k < m; k++) memcpy(&statics[7 * k], staticPoses + 7 * size_t(s0 + k), 28);
+		const float g[3] = {params[1], params[2], params[3]};
+		pxref_tgs_solve(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), PxU32(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(), g,
+			dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(), ord.data(), NULL, NULL);
+		for(PxU32 i = 0; i < n; i++)
+		{
+			PxRigidBodyData& r = rigid[b0 + i];
+			r.linearVelocity = PxVec3(vel[6 * i], vel[6 * i + 1], vel[6 * i + 2]);
+			r.angularVelocity = PxVec3(vel[6 * i + 3], vel[6 * i + 4], vel[6 * i + 5]);
+			r.body2World = PxTransform(PxVec3(outPose[7 * i + 4], outPose[7 * i + 5], outPose[7 * i + 6]),
+				PxQuat(outPose[7 * i], outPose[7 * i + 1], outPose[7 * i + 2], outPose[7 * i + 3]));
+		}
+		b0 += n;
+		s0 += m;
+	}
+	return 0;
 }

@@ -46,3 +46,10 @@ def check(rc, what=""):
     if rc != GBPX_OK:
         raise GbpxError(rc, what)
     return rc
+
+
+def set_device(device):
+    """Selects the CUDA device used by subsequently created objects (one process per GPU)."""
+    L = lib()
+    L.gbpx_set_device.argtypes = [ctypes.c_int]
+    check(L.gbpx_set_device(int(device)), "gbpx_set_device")

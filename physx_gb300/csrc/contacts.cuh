@@ -78,7 +78,7 @@ struct Manifold
 	int num = 0;
 };
 
-__device__ float distPointSegSq(V3 a, V3 b, V3 p)
+static __device__ float distPointSegSq(V3 a, V3 b, V3 p)
 {
 	const V3 ap = sub(p, a), ab = sub(b, a);
 	const float nom = dotA(ap, ab), denom = dotA(ab, ab);
@@ -89,7 +89,7 @@ __device__ float distPointSegSq(V3 a, V3 b, V3 p)
 }
 
 // ----------------------------------------------------------------- sphere
-__device__ bool sphereSphere(float r0, float r1, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
+static __device__ bool sphereSphere(float r0, float r1, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
 {
 	const V3 d = sub(t0.p, t1.p);
 	const float distSq = dotA(d, d);
@@ -105,7 +105,7 @@ __device__ bool sphereSphere(float r0, float r1, const Tr& t0, const Tr& t1, flo
 	return false;
 }
 
-__device__ bool spherePlane(float r, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
+static __device__ bool spherePlane(float r, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
 {
 	const V3 c = trTransformInv(t1, t0.p);
 	const float sep = c.x - r;
@@ -119,7 +119,7 @@ __device__ bool spherePlane(float r, const Tr& t0, const Tr& t1, float cDist, Bu
 	return false;
 }
 
-__device__ bool sphereCapsule(float sr, float cr, float hh, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
+static __device__ bool sphereCapsule(float sr, float cr, float hh, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
 {
 	const V3 b0 = qBasis0(t1.q);
 	const V3 tmp = scale(b0, hh);
@@ -145,7 +145,7 @@ __device__ bool sphereCapsule(float sr, float cr, float hh, const Tr& t0, const 
 	return false;
 }
 
-__device__ bool sphereBox(float r, V3 ext, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
+static __device__ bool sphereBox(float r, V3 ext, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
 {
 	const V3 c = trTransformInv(t1, t0.p);
 	const float infl = r + cDist;
@@ -183,7 +183,7 @@ __device__ bool sphereBox(float r, V3 ext, const Tr& t0, const Tr& t1, float cDi
 }
 
 // ----------------------------------------------------------------- manifold helpers
-__device__ bool replacePoint(Manifold& m, const PC& c, float thr)
+static __device__ bool replacePoint(Manifold& m, const PC& c, float thr)
 {
 	const float sd = thr * thr;
 	for(int i = 0; i < m.num; i++)
@@ -195,7 +195,7 @@ __device__ bool replacePoint(Manifold& m, const PC& c, float thr)
 	return false;
 }
 
-__device__ void addPoint2(Manifold& m, const PC& c, float thr)
+static __device__ void addPoint2(Manifold& m, const PC& c, float thr)
 {
 	if(replacePoint(m, c, thr)) return;
 	if(m.num < 2) { m.pts[m.num++] = c; return; }
@@ -205,7 +205,7 @@ __device__ void addPoint2(Manifold& m, const PC& c, float thr)
 }
 
 // addManifoldContactsToContactBuffer for sphere/capsule vs primitive (GuPersistentContactManifold.cpp:783)
-__device__ void outputCapsuleLike(const Manifold& m, V3 normal, V3 projN, const Tr& tA, float radius, float cDist, Buffer& out)
+static __device__ void outputCapsuleLike(const Manifold& m, V3 normal, V3 projN, const Tr& tA, float radius, float cDist, Buffer& out)
 {
 	for(int i = 0; i < m.num; i++)
 	{
@@ -215,7 +215,7 @@ __device__ void outputCapsuleLike(const Manifold& m, V3 normal, V3 projN, const 
 }
 
 // addManifoldContactsToContactBuffer(normal, transf1, contactOffset) (GuPersistentContactManifold.cpp:739)
-__device__ void outputWithOffset(const Manifold& m, V3 normal, const Tr& tB, float cDist, Buffer& out)
+static __device__ void outputWithOffset(const Manifold& m, V3 normal, const Tr& tB, float cDist, Buffer& out)
 {
 	for(int i = 0; i < m.num; i++)
 	{
@@ -225,7 +225,7 @@ __device__ void outputWithOffset(const Manifold& m, V3 normal, const Tr& tB, flo
 }
 
 // reduceBatchContactsCluster (GuPersistentContactManifold.cpp:859)
-__device__ void reduceCluster(Manifold& m, const PC* pts, int n)
+static __device__ void reduceCluster(Manifold& m, const PC* pts, int n)
 {
 	bool chosen[MAXC] = {};
 	const float FMAX = FLT_MAX;
@@ -291,7 +291,7 @@ __device__ void reduceCluster(Manifold& m, const PC* pts, int n)
 }
 
 // reduceBatchContacts (GuPersistentContactManifold.cpp:1008)
-__device__ void reduceBatch(Manifold& m, const PC* pts, int n, float tolLen)
+static __device__ void reduceBatch(Manifold& m, const PC* pts, int n, float tolLen)
 {
 	int chosenIdx[4];
 	int cand[MAXC];
@@ -378,7 +378,7 @@ __device__ void reduceBatch(Manifold& m, const PC* pts, int n, float tolLen)
 }
 
 // reduceBatchContacts2 (GuPersistentContactManifold.cpp:1177)
-__device__ void reduceBatch2(Manifold& m, const PC* pts, int n)
+static __device__ void reduceBatch2(Manifold& m, const PC* pts, int n)
 {
 	bool chosen[MAXC] = {};
 	float maxDis = pts[0].pen;
@@ -407,32 +407,32 @@ __device__ void reduceBatch2(Manifold& m, const PC* pts, int n)
 	if(second != index) m.pts[1] = pts[second];
 }
 
-__device__ void addBatch(Manifold& m, const PC* pts, int n, float tolLen)
+static __device__ void addBatch(Manifold& m, const PC* pts, int n, float tolLen)
 {
 	if(n <= 4) { for(int i = 0; i < n; i++) m.pts[i] = pts[i]; m.num = n; }
 	else { reduceBatch(m, pts, n, tolLen); m.num = 4; }
 }
 
-__device__ void addBatchCluster(Manifold& m, const PC* pts, int n)
+static __device__ void addBatchCluster(Manifold& m, const PC* pts, int n)
 {
 	if(n <= 4) { for(int i = 0; i < n; i++) m.pts[i] = pts[i]; m.num = n; }
 	else { reduceCluster(m, pts, n); m.num = 4; }
 }
 
-__device__ void addBatch2(Manifold& m, const PC* pts, int n)
+static __device__ void addBatch2(Manifold& m, const PC* pts, int n)
 {
 	if(n <= 2) { for(int i = 0; i < n; i++) m.pts[i] = pts[i]; m.num = n; }
 	else { reduceBatch2(m, pts, n); m.num = 2; }
 }
 
-__device__ float boxMargin(V3 ext, float tolLen)
+static __device__ float boxMargin(V3 ext, float tolLen)
 {
 	const float mn = fmin_(ext.x, fmin_(ext.y, ext.z));
 	return fmin_(mn * 0.15f, tolLen * 0.15f);
 }
 
 // ----------------------------------------------------------------- plane
-__device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const Tr& tCap, float cDist, Buffer& out)
+static __device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const Tr& tCap, float cDist, Buffer& out)
 {
 	const Tr& transf0 = tCap;
 	const Tr& transf1 = tPlane;
@@ -462,7 +462,7 @@ __device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const Tr& tCap
 	return m.num > 0;
 }
 
-__device__ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, float tolLen, Buffer& out)
+static __device__ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, float tolLen, Buffer& out)
 {
 	const Tr& transf0 = tBox;
 	const Tr& transf1 = tPlane;
@@ -505,7 +505,7 @@ __device__ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, 
 }
 
 // ----------------------------------------------------------------- capsule-capsule
-__device__ float segSegSq(V3 p1, V3 d1, V3 p2, V3 d2, float& s, float& t)
+static __device__ float segSegSq(V3 p1, V3 d1, V3 p2, V3 d2, float& s, float& t)
 {
 	const float eps = FLT_EPSILON;
 	const V3 r = sub(p1, p2);
@@ -528,7 +528,7 @@ __device__ float segSegSq(V3 p1, V3 d1, V3 p2, V3 d2, float& s, float& t)
 	return dotA(vv, vv);
 }
 
-__device__ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
+static __device__ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const Tr& t0, const Tr& t1, float cDist, Buffer& out)
 {
 	const V3 off = scale(add(t0.p, t1.p), 0.5f);
 	const V3 p0 = sub(t0.p, off), p1 = sub(t1.p, off);
@@ -596,11 +596,11 @@ __device__ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const T
 
 // ----------------------------------------------------------------- box-box
 struct MatTr { M33 R; V3 p; };
-__device__ MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
-__device__ V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
-__device__ V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
-__device__ V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
-__device__ M33 transpose(const M33& m)
+static __device__ MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
+static __device__ V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
+static __device__ V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
+static __device__ V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
+static __device__ M33 transpose(const M33& m)
 {
 	M33 t;
 	t.c0 = v3(m.c0.x, m.c1.x, m.c2.x);
@@ -609,7 +609,7 @@ __device__ M33 transpose(const M33& m)
 	return t;
 }
 // a.transformInv(b) for matrix transforms (PxVecTransform.h:277)
-__device__ MatTr mtInvMul(const MatTr& a, const MatTr& b)
+static __device__ MatTr mtInvMul(const MatTr& a, const MatTr& b)
 {
 	MatTr r;
 	const M33 at = transpose(a.R);
@@ -622,11 +622,11 @@ __device__ MatTr mtInvMul(const MatTr& a, const MatTr& b)
 // Box-box edge-edge fallback (GJK/EPA between the boxes, GuPCMContactBoxBox.cpp:917-957)
 // and the capsule-box full manifold (GuPCMContactCapsuleBox.cpp:73): not restated
 // yet, so these configurations report no contact; the tests identify and skip them.
-__device__ bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
-__device__ bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, PC*, int&, V3&) { return false; }
+static __device__ bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
+static __device__ bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, PC*, int&, V3&) { return false; }
 
 
-__device__ void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V3 ext)
+static __device__ void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V3 ext)
 {
 	float ex = ext.x, ey = ext.y, ez = ext.z;
 	const V3 u0 = t10.R.c0, u1 = t10.R.c1, u2 = t10.R.c2;
@@ -662,13 +662,13 @@ __device__ void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V
 }
 
 // GuPCMContactGenUtil contains(): point-in-polygon on the XY plane with a bounds reject
-__device__ bool containsXY(const V3* verts, int n, V3 p, V3 bmin, V3 bmax)
+static __device__ bool containsXY(const V3* verts, int n, V3 p, V3 bmin, V3 bmax)
 {
 	if(p.x < bmin.x || p.x > bmax.x || p.y < bmin.y || p.y > bmax.y) return false;
 	return polyContainsXY(verts, n, p);
 }
 
-__device__ bool segAABB(V3 p0, V3 d, V3 mx, V3 mn, float& tmin, float& tmax)
+static __device__ bool segAABB(V3 p0, V3 d, V3 mx, V3 mn, float& tmin, float& tmax)
 {
 	const float eps = 1e-6f;
 	const V3 ad = vabs(d);
@@ -695,7 +695,7 @@ __device__ bool segAABB(V3 p0, V3 d, V3 mx, V3 mn, float& tmin, float& tmax)
 	return !(tminf > tmaxf || tminf > 1.0f);
 }
 
-__device__ void calculateContacts(float exX, float exY, V3* pts, V3 incN, V3 localN, PC* mc, int& num, float cDist)
+static __device__ void calculateContacts(float exX, float exY, V3* pts, V3 incN, V3 localN, PC* mc, int& num, float cDist)
 {
 	const float FMAX = FLT_MAX;
 	const float extX = exX * 1.0001f, extY = exY * 1.0001f;
@@ -774,7 +774,7 @@ __device__ void calculateContacts(float exX, float exY, V3* pts, V3 incN, V3 loc
 }
 
 // doBoxBoxGenerateContacts (GuPCMContactBoxBox.cpp:332); returns false on separation
-__device__ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr& T1, float cDist, PC* mc, int& num)
+static __device__ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr& T1, float cDist, PC* mc, int& num)
 {
 	const float ea[3] = {e0.x, e0.y, e0.z}, eb[3] = {e1.x, e1.y, e1.z};
 	const MatTr t10 = mtInvMul(T0, T1);
@@ -923,7 +923,7 @@ __device__ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr& T1, f
 	return true;
 }
 
-__device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen, Buffer& out)
+static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen, Buffer& out)
 {
 	const Tr cur = trInvMul(tB, tA);
 	const float m0 = boxMargin(e0, tolLen), m1 = boxMargin(e1, tolLen);
@@ -961,7 +961,7 @@ __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, fl
 }
 
 // ----------------------------------------------------------------- capsule-box
-__device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Buffer& out)
+static __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Buffer& out)
 {
 	const Tr cur = trInvMul(tBox, tCap);
 	const MatTr aToB = matFromTr(cur);
@@ -979,7 +979,7 @@ __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& 
 	return m.num > 0;
 }
 
-__device__ int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Buffer& out)
+static __device__ int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Buffer& out)
 {
 	switch(t0 * 4 + t1)
 	{
@@ -997,7 +997,7 @@ __device__ int generate(int t0, const float* g0, int t1, const float* g1, const 
 	return out.count;
 }
 
-__device__ Tr loadTr(const float* p)
+static __device__ Tr loadTr(const float* p)
 {
 	Tr t;
 	t.q.x = p[0]; t.q.y = p[1]; t.q.z = p[2]; t.q.w = p[3];

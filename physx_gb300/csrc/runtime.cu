@@ -26,3 +26,9 @@ GBPX_API int gbpx_device_synchronize(void)
 	GBPX_CUDA_TRY(cudaDeviceSynchronize());
 	return GBPX_OK;
 }
+
+GBPX_API int gbpx_set_device(int device)
+{
+	GBPX_CUDA_TRY(cudaSetDevice(device));
+	return GBPX_OK;
+}

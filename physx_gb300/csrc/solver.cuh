@@ -1,0 +1,562 @@
+// TGS contact solver building blocks for the GB300 rigid-body step.
+//
+// Follows the reference's immediate-mode TGS contact path:
+//   body construction: bodyCoreComputeUnconstrainedVelocity
+//     (physx/source/lowleveldynamics/src/DyBodyCoreIntegrator.h:38) and
+//     copyToSolverBodyDataStep (DyTGSDynamics.cpp:154);
+//   batching: classifyConstraintDesc / writeConstraintDesc
+//     (DyConstraintPartition.cpp:476,571) and createHeaders
+//     (physx/source/immediatemode/src/NpImmediateMode.cpp:159);
+//   rows: createContactPatches / correlatePatches / growPatches
+//     (DyFrictionCorrelation.cpp:56,133,187), setupFinalizeSolverConstraints
+//     and constructContactConstraintStep (DyTGSContactPrep.cpp:426,322);
+//   solve: solveContact / solveDynamicContactsStep (DyTGSContactPrep.cpp:1581,1492);
+//   integration: integrateCoreStep (DyTGSDynamics.cpp:1403) and
+//     PxIntegrateSolverBodiesTGS (NpImmediateMode.cpp:1719).
+// Settings are those of immediate-mode callers: fresh friction patches, unit
+// mass scales, zero rest distance and offset slop, no torsional friction.
+//
+// GB300 layout: a pair has at most 4 contacts, so a constraint's rows fit a
+// fixed 1 KB record (<= 4 patches, <= 4 point rows, <= 8 friction rows) that
+// the prep pass writes once and every solve iteration re-reads from L2; the
+// partitioning (batching) rule guarantees that the constraints of one
+// partition touch disjoint dynamic bodies, so a partition is solved as one
+// parallel wave and reproduces the reference's sequential order.
+#pragma once
+#include "vmath.cuh"
+
+namespace gbpx
+{
+namespace tgs
+{
+constexpr int MAX_CONTACTS = 4;
+constexpr int MAX_FRICTION = 8;
+
+struct RigidBody   // PxRigidBodyData (physx/include/PxImmediateMode.h:68), 96 bytes
+{
+	float linVel[3]; float invMass;
+	float angVel[3]; float maxDepenetrationVelocity;
+	float invInertia[3]; float maxContactImpulse;
+	float q[4]; float p[3];
+	float linearDamping, angularDamping, maxLinearVelocitySq, maxAngularVelocitySq;
+	uint32_t pad;
+};
+static_assert(sizeof(RigidBody) == 96, "PxRigidBodyData layout");
+
+struct BodyVel { V3 lin, ang, dLin, dAng; float maxAngVel; int kinematic; };      // PxTGSSolverBodyVel fields
+struct BodyTx { Q dq; V3 p; M33 sqrtInvInertia; };                                 // PxTGSSolverBodyTxInertia
+struct BodyData { V3 origLin, origAng; float maxContactImpulse, penBiasClamp, invMass; };  // PxTGSSolverBodyData
+
+struct Contact { V3 n; float sep; V3 p; float staticFriction, dynamicFriction, restitution; };
+
+struct PointRow { V3 raXnI, rbXnI; float velMultiplier, separation, biasCoefficient, targetVelocity, recipResponse, maxImpulse; };
+struct FrictionRow { V3 normal; float error; V3 raXnI; float targetVel; V3 rbXnI; float velMultiplier, frictionScale, biasScale; };
+struct PatchRows
+{
+	V3 normal;
+	float invMass0, invMass1, maxPenBias, staticFriction, dynamicFriction;
+	int pointStart, nbPoints, frictionStart, nbFriction;
+};
+struct ConstraintRecord
+{
+	int bodyA, bodyB, nbPatches, pad;
+	PatchRows patch[MAX_CONTACTS];
+	PointRow point[MAX_CONTACTS];
+	FrictionRow friction[MAX_FRICTION];
+	float force[MAX_CONTACTS];
+	float frictionForce[MAX_FRICTION];
+};
+
+// ------------------------------------------------------------- bodies
+__host__ __device__ __forceinline__ float selPos(float x) { return x >= 0.0f ? x : 0.0f; }
+
+__device__ __forceinline__ M33 transformInertia(V3 d, const M33& M)
+{
+	// Cm::transformInertiaTensor (physx/source/common/src/CmUtils.h:57), M(r, c) = column c row r
+	const float m00 = M.c0.x, m10 = M.c0.y, m20 = M.c0.z;
+	const float m01 = M.c1.x, m11 = M.c1.y, m21 = M.c1.z;
+	const float m02 = M.c2.x, m12 = M.c2.y, m22 = M.c2.z;
+	const float axx = d.x * m00, axy = d.x * m10, axz = d.x * m20;
+	const float byx = d.y * m01, byy = d.y * m11, byz = d.y * m21;
+	const float czx = d.z * m02, czy = d.z * m12, czz = d.z * m22;
+	const float i00 = axx * m00 + byx * m01 + czx * m02;
+	const float i11 = axy * m10 + byy * m11 + czy * m12;
+	const float i22 = axz * m20 + byz * m21 + czz * m22;
+	const float i01 = axx * m10 + byx * m11 + czx * m12;
+	const float i02 = axx * m20 + byx * m21 + czx * m22;
+	const float i12 = axy * m20 + byy * m21 + czy * m22;
+	M33 r;
+	r.c0 = v3(i00, i01, i02);
+	r.c1 = v3(i01, i11, i12);
+	r.c2 = v3(i02, i12, i22);
+	return r;
+}
+
+__device__ __forceinline__ void copyToSolverBody(V3 lv, V3 av, float invMass, V3 invInertia, const Tr& pose, float maxDepen, float maxImpulse,
+                                                 float maxAngVelSq, bool kinematic, BodyVel& vel, BodyTx& tx, BodyData& data)
+{
+	const M33 rot = m33FromQuatCol(pose.q);   // PxMat33Padded
+	const V3 sqrtInv = v3(invInertia.x == 0.0f ? 0.0f : sqrtf(invInertia.x), invInertia.y == 0.0f ? 0.0f : sqrtf(invInertia.y),
+	                      invInertia.z == 0.0f ? 0.0f : sqrtf(invInertia.z));
+	const V3 sqrtBody = v3(sqrtInv.x == 0.0f ? 0.0f : 1.0f / sqrtInv.x, sqrtInv.y == 0.0f ? 0.0f : 1.0f / sqrtInv.y,
+	                       sqrtInv.z == 0.0f ? 0.0f : 1.0f / sqrtInv.z);
+	tx.sqrtInvInertia = transformInertia(sqrtInv, rot);
+	tx.p = pose.p;
+	tx.dq.x = tx.dq.y = tx.dq.z = 0.0f;
+	tx.dq.w = 1.0f;
+	const M33 sqrtInertia = transformInertia(sqrtBody, rot);
+	vel.lin = lv;
+	vel.ang = m33MulVS(sqrtInertia, av);
+	vel.dLin = zero3();
+	vel.dAng = zero3();
+	vel.kinematic = kinematic ? 1 : 0;
+	vel.maxAngVel = sqrtf(maxAngVelSq);
+	data.invMass = invMass;
+	data.penBiasClamp = maxDepen;
+	data.maxContactImpulse = maxImpulse;
+	data.origLin = lv;
+	data.origAng = av;
+}
+
+// PxConstructSolverBodiesTGS for one body (gravity*dt, damping, clamps, solver body)
+__device__ __forceinline__ void constructDynamicBody(const RigidBody& r, V3 g, float dt, BodyVel& vel, BodyTx& tx, BodyData& data, Tr& pose)
+{
+	V3 lv = v3(r.linVel[0], r.linVel[1], r.linVel[2]);
+	V3 av = v3(r.angVel[0], r.angVel[1], r.angVel[2]);
+	const float oml = 1.0f - r.linearDamping * dt, oma = 1.0f - r.angularDamping * dt;
+	lv = add(lv, scale(scale(g, dt), 1.0f));
+	lv = scale(lv, selPos(oml));
+	av = scale(av, selPos(oma));
+	const float l2 = lenSqS(lv);
+	if(l2 > r.maxLinearVelocitySq) lv = scale(lv, sqrtf(r.maxLinearVelocitySq / l2));
+	const float a2 = lenSqS(av);
+	if(a2 > r.maxAngularVelocitySq) av = scale(av, sqrtf(r.maxAngularVelocitySq / a2));
+	pose.q.x = r.q[0]; pose.q.y = r.q[1]; pose.q.z = r.q[2]; pose.q.w = r.q[3];
+	pose.p = v3(r.p[0], r.p[1], r.p[2]);
+	copyToSolverBody(lv, av, r.invMass, v3(r.invInertia[0], r.invInertia[1], r.invInertia[2]), pose, -r.maxDepenetrationVelocity,
+	                 r.maxContactImpulse, r.maxAngularVelocitySq, false, vel, tx, data);
+}
+
+// PxConstructStaticSolverBodyTGS (statics are flagged kinematic by the reference)
+__device__ __forceinline__ void constructStaticBody(const Tr& pose, BodyVel& vel, BodyTx& tx, BodyData& data)
+{
+	copyToSolverBody(zero3(), zero3(), 0.0f, zero3(), pose, -FLT_MAX, FLT_MAX, FLT_MAX, true, vel, tx, data);
+}
+
+// ------------------------------------------------------------- friction correlation (fresh patches, <= 4 contacts)
+struct Correlation
+{
+	int cpStart[MAX_CONTACTS], cpCount[MAX_CONTACTS], cpNext[MAX_CONTACTS];
+	float cpRest[MAX_CONTACTS], cpSF[MAX_CONTACTS], cpDF[MAX_CONTACTS];
+	V3 cpMin[MAX_CONTACTS], cpMax[MAX_CONTACTS];
+	int contactPatchCount;
+	V3 fpWorldNormal[MAX_CONTACTS];
+	V3 fpAnchor0[MAX_CONTACTS][2], fpAnchor1[MAX_CONTACTS][2];
+	int fpAnchorCount[MAX_CONTACTS];
+	float fpRest[MAX_CONTACTS], fpSF[MAX_CONTACTS], fpDF[MAX_CONTACTS];
+	int fpContactCount[MAX_CONTACTS];
+	V3 fpMin[MAX_CONTACTS], fpMax[MAX_CONTACTS];
+	int listHead[MAX_CONTACTS];
+	int frictionPatchCount;
+};
+
+__device__ __forceinline__ void createContactPatches(Correlation& c, const Contact* cb, int n, float tol)
+{
+	c.contactPatchCount = 0;
+	if(!n) return;
+	int pc = 0;
+	int cur = 0;
+	c.cpStart[0] = 0; c.cpCount[0] = 1; c.cpNext[0] = 0;
+	c.cpRest[0] = cb[0].restitution; c.cpSF[0] = cb[0].staticFriction; c.cpDF[0] = cb[0].dynamicFriction;
+	pc = 1;
+	V3 mn = cb[0].p, mx = cb[0].p;
+	int patchIndex = 0, count = 1;
+	for(int i = 1; i < n; i++)
+	{
+		const Contact& cc = cb[i];
+		const Contact& p0 = cb[patchIndex];
+		if(cc.staticFriction == p0.staticFriction && cc.dynamicFriction == p0.dynamicFriction && cc.restitution == p0.restitution &&
+		   dotS(cc.n, p0.n) >= tol)
+		{
+			mn = vmin(mn, cc.p);
+			mx = vmax(mx, cc.p);
+			count++;
+		}
+		else
+		{
+			patchIndex = i;
+			c.cpCount[cur] = count;
+			count = 1;
+			c.cpMin[cur] = mn; c.cpMax[cur] = mx;
+			cur = pc;
+			c.cpStart[pc] = i; c.cpCount[pc] = 1; c.cpNext[pc] = 0;
+			c.cpRest[pc] = cc.restitution; c.cpSF[pc] = cc.staticFriction; c.cpDF[pc] = cc.dynamicFriction;
+			pc++;
+			mn = cc.p; mx = cc.p;
+		}
+	}
+	if(count != 1) c.cpCount[cur] = count;
+	c.cpMin[cur] = mn; c.cpMax[cur] = mx;
+	c.contactPatchCount = pc;
+}
+
+__device__ __forceinline__ void correlatePatches(Correlation& c, const Contact* cb, float tol)
+{
+	int fpc = 0;
+	for(int i = 0; i < c.contactPatchCount; i++)
+	{
+		const V3 n = cb[c.cpStart[i]].n;
+		int j = 0;
+		for(; j < fpc && ((dotS(n, c.fpWorldNormal[j]) < tol) || c.fpRest[j] != c.cpRest[i] || c.fpSF[j] != c.cpSF[i] || c.fpDF[j] != c.cpDF[i]); j++)
+			;
+		if(j == fpc)
+		{
+			c.fpAnchorCount[fpc] = 0;
+			c.fpSF[fpc] = c.cpSF[i]; c.fpDF[fpc] = c.cpDF[i]; c.fpRest[fpc] = c.cpRest[i];
+			c.fpWorldNormal[j] = n;
+			c.fpContactCount[fpc] = c.cpCount[i];
+			c.fpMin[fpc] = c.cpMin[i]; c.fpMax[fpc] = c.cpMax[i];
+			fpc++;
+			c.cpNext[i] = -1;
+		}
+		else
+		{
+			c.fpMin[j] = vmin(c.fpMin[j], c.cpMin[i]);
+			c.fpMax[j] = vmax(c.fpMax[j], c.cpMax[i]);
+			c.fpContactCount[j] += c.cpCount[i];
+			c.cpNext[i] = c.listHead[j];
+		}
+		c.listHead[j] = i;
+	}
+	c.frictionPatchCount = fpc;
+}
+
+__device__ __forceinline__ V3 trTransformS(const Tr& t, V3 v) { return add(qRotateS(t.q, v), t.p); }
+__device__ __forceinline__ V3 trTransformInvS(const Tr& t, V3 v) { return qRotateInvS(t.q, sub(v, t.p)); }
+
+__device__ __forceinline__ void growPatches(Correlation& c, const Contact* cb, const Tr& f0, const Tr& f1, float thr)
+{
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		// fresh patches: anchorCount == 0 and the list is non-empty
+		V3 wa[2];
+		int ac = 0;
+		float pointDistSq = 0.0f, d0, d1;
+		const float eps = 1e-8f;
+		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch])
+		{
+			for(int j = 0; j < c.cpCount[patch]; j++)
+			{
+				const V3 wp = cb[c.cpStart[patch] + j].p;
+				if(cb[c.cpStart[patch] + j].sep < thr)
+				{
+					if(ac == 0) { wa[0] = wp; ac++; }
+					else if(ac == 1)
+					{
+						pointDistSq = lenSqS(sub(wp, wa[0]));
+						if(pointDistSq > eps) { wa[1] = wp; ac++; }
+					}
+					else
+					{
+						d0 = lenSqS(sub(wp, wa[0]));
+						d1 = lenSqS(sub(wp, wa[1]));
+						if(d0 > d1)
+						{
+							if(d0 > pointDistSq) { wa[1] = wp; pointDistSq = d0; }
+						}
+						else if(d1 > pointDistSq) { wa[0] = wp; pointDistSq = d1; }
+					}
+				}
+			}
+		}
+		for(int j = 0; j < ac; j++)
+		{
+			c.fpAnchor0[i][j] = trTransformInvS(f0, wa[j]);
+			c.fpAnchor1[i][j] = trTransformInvS(f1, wa[j]);
+		}
+		if(ac == 0) c.fpAnchor0[i][0] = c.fpAnchor1[i][0] = zero3();
+		c.fpAnchorCount[i] = ac;
+	}
+}
+
+// ------------------------------------------------------------- rows
+struct PrepParams
+{
+	float invStepDt, invTotalDt, totalDt, stepDt, bounceThreshold, frictionOffsetThreshold, biasCoefficient;
+};
+
+__device__ __forceinline__ float constructPoint(const M33& s0, const M33& s1, float imn0, float imn1, V3 p0, V3 p1, V3 n, float nv0, float nv1,
+                                                V3 av0, V3 av1, float invDtp8, float invStepDt, float totalDt, float invTotalDt,
+                                                float restitution, float bounce, const Contact& ct, bool kin0, bool kin1, PointRow& row)
+{
+	const float zero = 0.0f;
+	const float cTarget = dotA(n, zero3());
+	const V3 ra = sub(ct.p, p0), rb = sub(ct.p, p1);
+	const V3 raXn = cross(ra, n), rbXn = cross(rb, n);
+	const float angV0 = dotA(raXn, av0), angV1 = dotA(rbXn, av1);
+	const float vrel1 = nv0 + angV0, vrel2 = nv1 + angV1;
+	const float vrel = vrel1 - vrel2;
+	const V3 ri0 = m33MulV(s0, raXn), ri1 = m33MulV(s1, rbXn);
+	const float i0 = dotA(ri0, ri0) * 1.0f, i1 = dotA(ri1, ri1) * 1.0f;
+	const float resp0 = imn0 + i0, resp1 = i1 - imn1;
+	const float unitResponse = resp0 + resp1;
+	const float penetration = ct.sep - 0.0f;
+	const bool isSeparated = penetration > zero;
+	const float penInvDt = penetration * invTotalDt;
+	const bool isGreater2 = (restitution > zero && bounce > vrel) && (-vrel > penInvDt);
+	const float ratio = totalDt + (isGreater2 ? penetration / vrel : -totalDt);
+	const float recipResponse = unitResponse > zero ? 1.0f / unitResponse : zero;
+	const float biasCoeff = -(isSeparated ? invStepDt : invDtp8);
+	float totalError = penetration;
+	float targetVelocity = cTarget + (isGreater2 ? (-vrel) * restitution : zero);
+	totalError = targetVelocity * ratio + totalError;
+	if(kin0) targetVelocity = targetVelocity - vrel1;
+	if(kin1) targetVelocity = targetVelocity + vrel2;
+	row.raXnI = ri0;
+	row.rbXnI = ri1;
+	row.velMultiplier = recipResponse;
+	row.separation = totalError;
+	row.biasCoefficient = biasCoeff;
+	row.targetVelocity = targetVelocity;
+	row.recipResponse = recipResponse;
+	row.maxImpulse = FLT_MAX;
+	return penetration;
+}
+
+// Builds one constraint's rows (createFinalizeSolverContactsStep with fresh friction).
+__device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbContacts, int a, int b, const BodyVel& va, const BodyVel& vb,
+                                               const BodyTx& ta, const BodyTx& tb, const BodyData& d0, const BodyData& d1, const Tr& f0,
+                                               const Tr& f1, const PrepParams& pp, ConstraintRecord& rec)
+{
+	rec.bodyA = a;
+	rec.bodyB = b;
+	rec.nbPatches = 0;
+	if(nbContacts == 0) return;
+	Correlation c;
+	createContactPatches(c, contacts, nbContacts, 0.999f);
+	correlatePatches(c, contacts, 0.999f);
+	growPatches(c, contacts, f0, f1, pp.frictionOffsetThreshold + 0.0f);
+
+	const bool kin0 = va.kinematic != 0, kin1 = vb.kinematic != 0;
+	const float invMass0 = 1.0f * d0.invMass;
+	const float invMass1 = (-1.0f) * d1.invMass;
+	const float maxPenBias = fmax_(d0.penBiasClamp, d1.penBiasClamp);
+	const V3 p0 = f0.p, p1 = f1.p;
+	const V3 lv0 = d0.origLin, lv1 = d1.origLin, av0 = d0.origAng, av1 = d1.origAng;
+	const M33& s0 = ta.sqrtInvInertia;
+	const M33& s1 = tb.sqrtInvInertia;
+	const float invDt = pp.invStepDt;
+	const float p8 = fmin_(0.8f, pp.biasCoefficient);
+	const float invDtp8 = invDt * p8;
+	const float frictionBiasScale = invDt * p8;
+	int nPoints = 0, nFriction = 0;
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		if(c.fpContactCount[i] == 0) continue;
+		const int first = c.listHead[i];
+		const Contact& base0 = contacts[c.cpStart[first]];
+		PatchRows& pr = rec.patch[rec.nbPatches];
+		pr.invMass0 = invMass0;
+		pr.invMass1 = -invMass1;
+		const V3 n = contacts[c.cpStart[c.listHead[i]]].n;
+		const float nLenSq = dotA(n, n);
+		const float nv0 = dotA(lv0, n), nv1 = dotA(lv1, n);
+		const float imn0 = invMass0 * nLenSq, imn1 = invMass1 * nLenSq;
+		pr.normal = n;
+		pr.maxPenBias = base0.restitution < 0.0f ? -FLT_MAX : maxPenBias;
+		pr.pointStart = nPoints;
+		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch])
+			for(int j = 0; j < c.cpCount[patch]; j++)
+			{
+				constructPoint(s0, s1, imn0, imn1, p0, p1, n, nv0, nv1, av0, av1, invDtp8, invDt, pp.totalDt, pp.invTotalDt, base0.restitution,
+				               pp.bounceThreshold, contacts[c.cpStart[patch] + j], kin0, kin1, rec.point[nPoints]);
+				rec.force[nPoints] = 0.0f;
+				nPoints++;
+			}
+		pr.nbPoints = nPoints - pr.pointStart;
+		pr.staticFriction = base0.staticFriction;
+		pr.dynamicFriction = base0.dynamicFriction;
+		const int anchors = c.fpAnchorCount[i];
+		pr.frictionStart = nFriction;
+		pr.nbFriction = anchors ? anchors * 2 : 0;
+		if(anchors)
+		{
+			const V3 linVrel = sub(lv0, lv1);
+			const V3 t0f1 = v3(0.0f, -n.z, n.y), t0f2 = v3(-n.y, n.x, 0.0f);
+			const V3 t0Fallback = 0.70710678f > fabsf(n.x) ? t0f1 : t0f2;
+			V3 t0 = sub(linVrel, scale(n, dotA(n, linVrel)));
+			t0 = dotA(t0, t0) > 0.0001f ? t0 : t0Fallback;
+			t0 = normalizeA(t0);
+			const V3 t1 = normalizeA(cross(n, t0));
+			const float nv00 = dotA(lv0, t0), nv01 = dotA(lv1, t0), nv10 = dotA(lv0, t1), nv11 = dotA(lv1, t1);
+			const V3 relTr = sub(p0, p1);
+			const float frictionScale = anchors == 2 ? 0.5f : 1.0f;
+			for(int j = 0; j < anchors; j++)
+			{
+				const V3 ra = qRotate(f0.q, c.fpAnchor0[i][j]);
+				const V3 rb = qRotate(f1.q, c.fpAnchor1[i][j]);
+				const V3 error = add(sub(ra, rb), relTr);
+				for(int dir = 0; dir < 2; dir++)
+				{
+					const V3 t = dir == 0 ? t0 : t1;
+					FrictionRow& fr = rec.friction[nFriction];
+					const V3 raXn = cross(ra, t), rbXn = cross(rb, t);
+					const V3 ri0 = m33MulV(s0, raXn), ri1 = m33MulV(s1, rbXn);
+					const float resp0 = imn0 + dotA(ri0, ri0) * 1.0f;
+					const float resp1 = dotA(ri1, ri1) * 1.0f - imn1;
+					const float unitResponse = resp0 + resp1;
+					const float velMultiplier = unitResponse > 0.0f ? p8 / unitResponse : 0.0f;
+					float targetVel = dotA(zero3(), t);
+					if(kin0) targetVel = targetVel - ((dir == 0 ? nv00 : nv10) + dotA(raXn, av0));
+					if(kin1) targetVel = targetVel + ((dir == 0 ? nv01 : nv11) + dotA(rbXn, av1));
+					fr.normal = t;
+					fr.error = dotA(error, t);
+					fr.raXnI = ri0;
+					fr.targetVel = targetVel;
+					fr.rbXnI = ri1;
+					fr.velMultiplier = velMultiplier;
+					fr.frictionScale = frictionScale;
+					fr.biasScale = frictionBiasScale;
+					rec.frictionForce[nFriction] = 0.0f;
+					nFriction++;
+				}
+			}
+		}
+		rec.nbPatches++;
+	}
+}
+
+// ------------------------------------------------------------- solve
+// solveContact (DyTGSContactPrep.cpp:1581) for one constraint.  b0/b1 are the
+// constraint's two bodies (b1 may be a static/kinematic body, never written
+// back when it is not dynamic: its invMass and sqrtInvInertia are zero).
+__device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+{
+	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
+	const V3 angM0 = b0.dAng, angM1 = b1.dAng;
+	const V3 relMotion = sub(b0.dLin, b1.dLin);
+	for(int p = 0; p < rec.nbPatches; p++)
+	{
+		const PatchRows& pr = rec.patch[p];
+		const V3 n = pr.normal;
+		const float invMassA = pr.invMass0, invMassB = pr.invMass1;
+		const V3 nIM0 = scale(n, invMassA), nIM1 = scale(n, invMassB);
+		const float deltaV = dotA(relMotion, n);
+		float accumulated = 0.0f;
+		for(int i = 0; i < pr.nbPoints; i++)
+		{
+			const int k = pr.pointStart + i;
+			const PointRow& c = rec.point[k];
+			const float angDelta0 = dotA(angM0, c.raXnI), angDelta1 = dotA(angM1, c.rbXnI);
+			const float deltaAng = angDelta0 - angDelta1;
+			const float targetVel = c.targetVelocity;
+			const float deltaBias = (deltaV + deltaAng) - targetVel * elapsed;
+			const float sep = fmax_(minPen, c.separation + deltaBias);
+			const float bias = fmin_(-pr.maxPenBias, c.biasCoefficient * sep);
+			const V3 v0 = add(mul(lin0, n), mul(ang0, c.raXnI));
+			const V3 v1 = add(mul(lin1, n), mul(ang1, c.rbXnI));
+			const float normalVel = sumElems(sub(v0, v1));
+			const float biasNV = bias * c.recipResponse;
+			const float lambda = biasNV - (normalVel - targetVel) * c.velMultiplier;
+			const float applied = rec.force[k];
+			const float _deltaF = fmax_(lambda, -applied);
+			const float _newForce = applied + _deltaF;
+			const float newForce = fmin_(_newForce, c.maxImpulse);
+			const float deltaF = newForce - applied;
+			lin0 = scaleAdd(nIM0, deltaF, lin0);
+			lin1 = negScaleSub(nIM1, deltaF, lin1);
+			ang0 = scaleAdd(c.raXnI, deltaF * 1.0f, ang0);
+			ang1 = negScaleSub(c.rbXnI, deltaF * 1.0f, ang1);
+			rec.force[k] = newForce;
+			accumulated = accumulated + newForce;
+		}
+		if(pr.nbFriction)
+		{
+			const float maxF = pr.staticFriction * accumulated;
+			const float maxDynF = pr.dynamicFriction * accumulated;
+			const int pairs = pr.nbFriction & 6;
+			for(int i = 0; i < pairs; i += 2)
+			{
+				const int k0 = pr.frictionStart + i, k1 = k0 + 1;
+				const FrictionRow& f0 = rec.friction[k0];
+				const FrictionRow& f1 = rec.friction[k1];
+				const float fs = f0.frictionScale;
+				const float biasScale = f0.biasScale;
+				float dv0 = (dotA(f0.raXnI, angM0) - dotA(f0.rbXnI, angM1)) + dotA(f0.normal, relMotion);
+				float dv1 = (dotA(f1.raXnI, angM0) - dotA(f1.rbXnI, angM1)) + dotA(f1.normal, relMotion);
+				dv0 = dv0 - f0.targetVel * elapsed;
+				dv1 = dv1 - f1.targetVel * elapsed;
+				const float e0 = f0.error + dv0, e1 = f1.error + dv1;
+				const float bias0 = e0 * biasScale, bias1 = e1 * biasScale;
+				const V3 dl00 = scale(f0.normal, invMassA), dl10 = scale(f0.normal, invMassB);
+				const V3 dl01 = scale(f1.normal, invMassA), dl11 = scale(f1.normal, invMassB);
+				const float nvel0 = sumElems(sub(add(mul(lin0, f0.normal), mul(ang0, f0.raXnI)), add(mul(lin1, f0.normal), mul(ang1, f0.rbXnI))));
+				const float nvel1 = sumElems(sub(add(mul(lin0, f1.normal), mul(ang0, f1.raXnI)), add(mul(lin1, f1.normal), mul(ang1, f1.rbXnI))));
+				const float a0 = rec.frictionForce[k0], a1 = rec.frictionForce[k1];
+				const float tmp10 = a0 - (bias0 - f0.targetVel) * f0.velMultiplier;
+				const float tmp11 = a1 - (bias1 - f1.targetVel) * f1.velMultiplier;
+				const float ti0 = tmp10 - nvel0 * f0.velMultiplier;
+				const float ti1 = tmp11 - nvel1 * f1.velMultiplier;
+				const float total = sqrtf(ti0 * ti0 + ti1 * ti1);
+				const bool clamp = total > fs * maxF;
+				const float totalClamped = clamp ? fmin_(fs * maxDynF, total) : total;
+				const float ratio = total > 0.0f ? totalClamped / total : 0.0f;
+				const float nf0 = ti0 * ratio, nf1 = ti1 * ratio;
+				const float df0 = nf0 - a0, df1 = nf1 - a1;
+				lin0 = scaleAdd(dl00, df0, scaleAdd(dl01, df1, lin0));
+				lin1 = negScaleSub(dl10, df0, negScaleSub(dl11, df1, lin1));
+				ang0 = scaleAdd(f0.raXnI, df0 * 1.0f, scaleAdd(f1.raXnI, df1 * 1.0f, ang0));
+				ang1 = negScaleSub(f0.rbXnI, df0 * 1.0f, negScaleSub(f1.rbXnI, df1 * 1.0f, ang1));
+				rec.frictionForce[k0] = nf0;
+				rec.frictionForce[k1] = nf1;
+			}
+		}
+	}
+	b0.lin = lin0;
+	b0.ang = ang0;
+	if(writeB1)
+	{
+		b1.lin = lin1;
+		b1.ang = ang1;
+	}
+}
+
+// integrateCoreStep (DyTGSDynamics.cpp:1403)
+__device__ __forceinline__ void integrateStep(BodyVel& v, BodyTx& t, float dt)
+{
+	const V3 delta = scale(v.lin, dt);
+	const V3 unmolested = v.ang;
+	const V3 angMotion = m33MulVS(t.sqrtInvInertia, v.ang);
+	const float w2 = lenSqS(angMotion);
+	t.p = add(t.p, delta);
+	if(w2 != 0.0f)
+	{
+		const float w = sqrtf(w2);
+		const float vv = dt * w * 0.5f;
+		float s, q;
+		sincosf(vv, &s, &q);
+		s /= w;
+		const V3 pqr = scale(angMotion, s);
+		const Q qv_ = {pqr.x, pqr.y, pqr.z, 0.0f};
+		Q r = qMulS(qv_, t.dq);
+		r.x += t.dq.x * q; r.y += t.dq.y * q; r.z += t.dq.z * q; r.w += t.dq.w * q;
+		const float m = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w);
+		const float inv = 1.0f / m;
+		t.dq.x = r.x * inv; t.dq.y = r.y * inv; t.dq.z = r.z * inv; t.dq.w = r.w * inv;
+	}
+	v.dAng = add(v.dAng, scale(unmolested, dt));
+	v.dLin = add(v.dLin, delta);
+}
+
+// PxIntegrateSolverBodiesTGS (NpImmediateMode.cpp:1719): world angular velocity and new pose
+__device__ __forceinline__ void finalizeBody(const BodyVel& v, const BodyTx& t, Tr& pose, V3& angWorld)
+{
+	angWorld = m33MulVS(t.sqrtInvInertia, v.ang);
+	Q q = qMulS(t.dq, pose.q);
+	const float m = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+	const float inv = 1.0f / m;
+	pose.q.x = q.x * inv; pose.q.y = q.y * inv; pose.q.z = q.z * inv; pose.q.w = q.w * inv;
+	pose.p = t.p;
+}
+} // namespace tgs
+} // namespace gbpx

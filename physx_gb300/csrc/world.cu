@@ -1,0 +1,956 @@
+// Batched multi-scene rigid-body step for the GB300.
+//
+// Thousands of independent scenes advance in ONE persistent launch per step:
+// each warp takes the next scene from a work table sorted by decreasing size
+// (largest first, so the tail is short) and runs the whole immediate-mode
+// pipeline for it:
+//   1. bounds + broadphase: AABBs, warp bitonic sort by encoded min X, sweep
+//      with the reference ABP's closed-interval test (X as encodeFloat keys,
+//      Y/Z as floats), bitonic sort of the pair keys -> pairs ordered by
+//      (id0, id1), statics after the dynamic bodies;
+//   2. narrowphase: PxGenerateContacts semantics per pair (contacts.cuh);
+//   3. TGS: solver bodies, the PxBatchConstraintsTGS partition rule (lane 0),
+//      contact rows, position iterations with per-substep integration and the
+//      velocity iteration, solved partition by partition across the 32 lanes
+//      (constraints of one partition touch disjoint bodies; __syncwarp between
+//      partitions), then PxIntegrateSolverBodiesTGS and write-back.
+// All scene state stays resident in HBM; a step is capturable in a CUDA graph
+// (a memset of the work counter + one kernel).
+//
+// The step is the reference immediate-mode snippet's frame (physx/snippets/
+// snippetimmediatemode/SnippetImmediateMode.cpp:473 stepPhysics) with a fresh
+// PxBroadPhase, fresh PxCache and fresh friction data per frame: bounds
+// inflated by a margin, ABP pairs, PxGenerateContacts, PxConstructSolverBodiesTGS,
+// PxBatchConstraintsTGS, PxCreateContactConstraintsTGS, PxSolveConstraintsTGS,
+// PxIntegrateSolverBodiesTGS.
+#include "common.cuh"
+#include "contacts.cuh"
+#include "solver.cuh"
+#include <vector>
+#include <algorithm>
+#include <numeric>
+
+namespace gbpx
+{
+namespace world
+{
+constexpr uint32_t MAX_PARTITIONS = 128;
+enum : uint32_t { ST_PAIR_OVERFLOW = 1, ST_PARTITION_OVERFLOW = 2 };
+
+struct SceneDesc
+{
+	uint32_t bodyStart, nbBodies;      // dynamic bodies [bodyStart, bodyStart + nbBodies)
+	uint32_t staticStart, nbStatics;   // static shapes
+	uint32_t solverStart;              // solver bodies [solverStart, + nbBodies + nbStatics)
+	uint32_t keyStart, keyCap;         // sort keys (power of two >= nbBodies)
+	uint32_t pairStart, pairCap;       // pair / contact / constraint slots (power of two)
+};
+
+struct StepParams
+{
+	float dt, gx, gy, gz;
+	float contactDistance, toleranceLength, boundsMargin;
+	float bounceThreshold, frictionOffsetThreshold, correlationDistance, staticFriction;
+	uint32_t nbPos, nbVel;
+};
+
+struct WorldDev
+{
+	const SceneDesc* scenes;
+	const uint32_t* workOrder;
+	uint32_t nbScenes;
+	uint32_t* workCounter;
+	tgs::RigidBody* bodies;
+	const int* types;
+	const float4* geoms;
+	const float* friction;
+	const float* staticPose;   // 7 floats
+	const int* staticTypes;
+	const float4* staticGeoms;
+	float* aabb;               // 6 floats per dynamic body
+	unsigned long long* keys;
+	uint32_t* pairs;
+	uint32_t* pairCount;
+	float4* contacts;          // 8 float4 per pair slot
+	uint32_t* contactCount;
+	uint32_t* ordered;         // per pair slot: constraint order (pair index)
+	uint32_t* consList;        // per pair slot: pairs with contacts
+	uint32_t* tag;             // per pair slot: (round << 8) | partition, 0xffff for static constraints
+	tgs::ConstraintRecord* recs;
+	tgs::BodyVel* vel;
+	tgs::BodyTx* tx;
+	tgs::BodyData* data;
+	Tr* pose;
+	uint32_t* progress;        // per solver body
+	uint32_t* maxNormal;
+	uint32_t* maxStatic;
+	uint32_t* staticProgress;
+	uint32_t* partEnds;        // MAX_PARTITIONS per scene
+	uint32_t* status;
+};
+
+__device__ __forceinline__ Tr loadStaticPose(const float* s)
+{
+	Tr t;
+	t.q.x = s[0]; t.q.y = s[1]; t.q.z = s[2]; t.q.w = s[3];
+	t.p = v3(s[4], s[5], s[6]);
+	return t;
+}
+
+// World-space AABB of a shape, before the margin (sphere, capsule along local
+// X, box); planes are unbounded.
+__device__ __forceinline__ void shapeBounds(int type, const float4 g, const Tr& pose, V3& mn, V3& mx)
+{
+	V3 e;
+	if(type == 0) e = v3(g.x, g.x, g.x);
+	else if(type == 2)
+	{
+		const V3 ax = qBasis0(pose.q);
+		e = v3(fabsf(ax.x) * g.y + g.x, fabsf(ax.y) * g.y + g.x, fabsf(ax.z) * g.y + g.x);
+	}
+	else if(type == 3)
+	{
+		const M33 R = m33FromQuatCol(pose.q);
+		e = v3((fabsf(R.c0.x) * g.x + fabsf(R.c1.x) * g.y) + fabsf(R.c2.x) * g.z,
+		       (fabsf(R.c0.y) * g.x + fabsf(R.c1.y) * g.y) + fabsf(R.c2.y) * g.z,
+		       (fabsf(R.c0.z) * g.x + fabsf(R.c1.z) * g.y) + fabsf(R.c2.z) * g.z);
+	}
+	else
+	{
+		mn = v3(-1e30f, -1e30f, -1e30f);
+		mx = v3(1e30f, 1e30f, 1e30f);
+		return;
+	}
+	mn = sub(pose.p, e);
+	mx = add(pose.p, e);
+}
+
+__device__ __forceinline__ bool overlapBoxes(const float* a, const float* b)
+{
+	// ABP semantics: X on encoded keys, Y/Z closed float intervals
+	const uint32_t aminx = encodeFloatBits(__float_as_uint(a[0])), amaxx = encodeFloatBits(__float_as_uint(a[3]));
+	const uint32_t bminx = encodeFloatBits(__float_as_uint(b[0])), bmaxx = encodeFloatBits(__float_as_uint(b[3]));
+	if(bminx > amaxx || aminx > bmaxx) return false;
+	return !(b[4] < a[1] || a[4] < b[1] || b[5] < a[2] || a[5] < b[2]);
+}
+
+template <typename K>
+__device__ __forceinline__ void warpBitonicSort(K* keys, uint32_t n)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	for(uint32_t k = 2; k <= n; k <<= 1)
+	{
+		for(uint32_t j = k >> 1; j > 0; j >>= 1)
+		{
+			for(uint32_t i = lane; i < n; i += 32)
+			{
+				const uint32_t ixj = i ^ j;
+				if(ixj > i)
+				{
+					const K a = keys[i], b = keys[ixj];
+					const bool up = (i & k) == 0;
+					if(up ? (a > b) : (a < b)) { keys[i] = b; keys[ixj] = a; }
+				}
+			}
+			__syncwarp();
+		}
+	}
+}
+
+__device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t n = sc.nbBodies, m = sc.nbStatics;
+	float* aabb = w.aabb + 6 * size_t(sc.bodyStart);
+	unsigned long long* keys = w.keys + sc.keyStart;
+	for(uint32_t i = lane; i < sc.keyCap; i += 32)
+	{
+		if(i < n)
+		{
+			const tgs::RigidBody& rb = w.bodies[sc.bodyStart + i];
+			Tr pose;
+			pose.q.x = rb.q[0]; pose.q.y = rb.q[1]; pose.q.z = rb.q[2]; pose.q.w = rb.q[3];
+			pose.p = v3(rb.p[0], rb.p[1], rb.p[2]);
+			V3 mn, mx;
+			shapeBounds(w.types[sc.bodyStart + i], w.geoms[sc.bodyStart + i], pose, mn, mx);
+			const float mg = sp.boundsMargin;
+			float* a = aabb + 6 * size_t(i);
+			a[0] = mn.x - mg; a[1] = mn.y - mg; a[2] = mn.z - mg;
+			a[3] = mx.x + mg; a[4] = mx.y + mg; a[5] = mx.z + mg;
+			keys[i] = (static_cast<unsigned long long>(encodeFloatBits(__float_as_uint(a[0]))) << 32) | i;
+		}
+		else
+			keys[i] = ~0ull;
+	}
+	if(lane == 0) w.pairCount[sid] = 0;
+	__syncwarp();
+	warpBitonicSort(keys, sc.keyCap);
+	uint32_t* pairs = w.pairs + sc.pairStart;
+	uint32_t local = 0;   // lane-private overflow flag
+	for(uint32_t p = lane; p < n; p += 32)
+	{
+		const uint32_t i = uint32_t(keys[p]);
+		const float* a = aabb + 6 * size_t(i);
+		const uint32_t amaxx = encodeFloatBits(__float_as_uint(a[3]));
+		for(uint32_t q = p + 1; q < n; q++)
+		{
+			const unsigned long long kq = keys[q];
+			if(uint32_t(kq >> 32) > amaxx) break;
+			const uint32_t j = uint32_t(kq);
+			const float* b = aabb + 6 * size_t(j);
+			if(!(b[4] < a[1] || a[4] < b[1] || b[5] < a[2] || a[5] < b[2]))
+			{
+				const uint32_t slot = atomicAdd(&w.pairCount[sid], 1u);
+				const uint32_t lo = i < j ? i : j, hi = i < j ? j : i;
+				if(slot < sc.pairCap) pairs[slot] = (lo << 16) | hi; else local = 1;
+			}
+		}
+		for(uint32_t s = 0; s < m; s++)
+		{
+			V3 mn, mx;
+			const Tr sp7 = loadStaticPose(w.staticPose + 7 * size_t(sc.staticStart + s));
+			shapeBounds(w.staticTypes[sc.staticStart + s], w.staticGeoms[sc.staticStart + s], sp7, mn, mx);
+			const float mg = sp.boundsMargin;
+			const float b[6] = {mn.x - mg, mn.y - mg, mn.z - mg, mx.x + mg, mx.y + mg, mx.z + mg};
+			if(overlapBoxes(a, b))
+			{
+				const uint32_t slot = atomicAdd(&w.pairCount[sid], 1u);
+				if(slot < sc.pairCap) pairs[slot] = (i << 16) | (n + s); else local = 1;
+			}
+		}
+	}
+	__syncwarp();
+	if(__any_sync(0xffffffffu, local) && lane == 0) atomicOr(&w.status[sid], ST_PAIR_OVERFLOW);
+	uint32_t count = atomicAdd(&w.pairCount[sid], 0u);
+	count = count < sc.pairCap ? count : sc.pairCap;
+	uint32_t pw = 1;
+	while(pw < count) pw <<= 1;
+	for(uint32_t k = count + lane; k < pw; k += 32) pairs[k] = 0xffffffffu;
+	__syncwarp();
+	if(count > 1) warpBitonicSort(pairs, pw);
+	if(lane == 0) w.pairCount[sid] = count;
+	__syncwarp();
+}
+
+__device__ __forceinline__ void pairShape(const WorldDev& w, const SceneDesc& sc, uint32_t id, int& type, float g[4], Tr& pose)
+{
+	if(id < sc.nbBodies)
+	{
+		const uint32_t b = sc.bodyStart + id;
+		type = w.types[b];
+		const float4 gg = w.geoms[b];
+		g[0] = gg.x; g[1] = gg.y; g[2] = gg.z; g[3] = gg.w;
+		const tgs::RigidBody& rb = w.bodies[b];
+		pose.q.x = rb.q[0]; pose.q.y = rb.q[1]; pose.q.z = rb.q[2]; pose.q.w = rb.q[3];
+		pose.p = v3(rb.p[0], rb.p[1], rb.p[2]);
+	}
+	else
+	{
+		const uint32_t s = sc.staticStart + (id - sc.nbBodies);
+		type = w.staticTypes[s];
+		const float4 gg = w.staticGeoms[s];
+		g[0] = gg.x; g[1] = gg.y; g[2] = gg.z; g[3] = gg.w;
+		pose = loadStaticPose(w.staticPose + 7 * size_t(s));
+	}
+}
+
+__device__ __forceinline__ void sceneNarrowphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t count = w.pairCount[sid];
+	for(uint32_t k = lane; k < count; k += 32)
+	{
+		const uint32_t key = w.pairs[sc.pairStart + k];
+		const uint32_t i = key >> 16, j = key & 0xffffu;
+		int ta, tb;
+		float ga[4], gb[4];
+		Tr pa, pb;
+		pairShape(w, sc, i, ta, ga, pa);
+		pairShape(w, sc, j, tb, gb, pb);
+		const bool swap = ta > tb;
+		if(swap)
+		{
+			const int t = ta; ta = tb; tb = t;
+			for(int c = 0; c < 4; c++) { const float x = ga[c]; ga[c] = gb[c]; gb[c] = x; }
+			const Tr t2 = pa; pa = pb; pb = t2;
+		}
+		np::Buffer buf;
+		np::generate(ta, ga, tb, gb, pa, pb, sp.contactDistance, sp.toleranceLength, buf);
+		float4* o = w.contacts + size_t(sc.pairStart + k) * 8;
+		for(int c = 0; c < buf.count; c++)
+		{
+			V3 nn = buf.c[c].n;
+			if(swap) nn = neg(nn);
+			o[2 * c] = make_float4(nn.x, nn.y, nn.z, buf.c[c].sep);
+			o[2 * c + 1] = make_float4(buf.c[c].p.x, buf.c[c].p.y, buf.c[c].p.z, 0.0f);
+		}
+		w.contactCount[sc.pairStart + k] = uint32_t(buf.count);
+	}
+	__syncwarp();
+}
+
+// PxBatchConstraintsTGS partition rule for one scene, run by one lane
+// (the rule is sequential in constraint order; see batching.h for the
+// reference citations).  Fills ordered[] (pair indices in solve order) and
+// the partition end offsets; returns the partition count, 0 on overflow.
+__device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t sid, uint32_t nc)
+{
+	const uint32_t n = sc.nbBodies;
+	uint32_t* progress = w.progress + sc.solverStart;
+	uint32_t* maxNormal = w.maxNormal + sc.solverStart;
+	uint32_t* maxStatic = w.maxStatic + sc.solverStart;
+	uint32_t* staticProgress = w.staticProgress + sc.solverStart;
+	uint32_t* perPart = w.partEnds + size_t(sid) * MAX_PARTITIONS;
+	const uint32_t* cons = w.consList + sc.pairStart;
+	uint32_t* tag = w.tag + sc.pairStart;
+	uint32_t* ordered = w.ordered + sc.pairStart;
+	for(uint32_t b = 0; b < n; b++) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
+	for(uint32_t p = 0; p < MAX_PARTITIONS; p++) perPart[p] = 0;
+	// pass 1: dynamic-dynamic constraints take the lowest free partition bit;
+	// constraints that find none retry in the next round of 32 partitions
+	for(uint32_t c = 0; c < nc; c++) tag[c] = 0;
+	uint32_t nbPart = 0, maxRound = 0;
+	for(uint32_t round = 0;; round++)
+	{
+		if(round) for(uint32_t b = 0; b < n; b++) progress[b] = 0;
+		bool deferred = false;
+		for(uint32_t c = 0; c < nc; c++)
+		{
+			const uint32_t key = w.pairs[sc.pairStart + cons[c]];
+			const uint32_t a = key >> 16, b = key & 0xffffu;
+			if(a < n && b < n)
+			{
+				if((tag[c] >> 8) != round) continue;
+				const uint32_t mask = ~progress[a] & ~progress[b];
+				if(!mask) { tag[c] = (round + 1) << 8; deferred = true; continue; }
+				const uint32_t part = __ffs(mask) - 1;
+				progress[a] |= 1u << part;
+				progress[b] |= 1u << part;
+				const uint32_t gp = round * 32 + part;
+				if(gp >= MAX_PARTITIONS) return 0;
+				tag[c] = (round << 8) | gp;
+				perPart[gp]++;
+				maxNormal[a] = max(maxNormal[a], gp + 1);
+				maxNormal[b] = max(maxNormal[b], gp + 1);
+				nbPart = max(nbPart, gp + 1);
+				maxRound = max(maxRound, round);
+			}
+			else if(round == 0)
+			{
+				tag[c] = 0xffffu;
+				if(a < n) maxStatic[a]++;
+				if(b < n) maxStatic[b]++;
+			}
+		}
+		if(!deferred) break;
+	}
+	// statics of a body follow its last dynamic partition, one per partition
+	for(uint32_t b = 0; b < n; b++)
+	{
+		const uint32_t need = maxNormal[b] + maxStatic[b];
+		if(need > MAX_PARTITIONS) return 0;
+		nbPart = max(nbPart, need);
+		for(uint32_t k = 0; k < maxStatic[b]; k++) perPart[maxNormal[b] + k]++;
+	}
+	uint32_t acc = 0;
+	for(uint32_t p = 0; p < nbPart; p++) { const uint32_t t = perPart[p]; perPart[p] = acc; acc += t; }
+	// pass 2: round-0 dynamic constraints and all static constraints in input
+	// order, then each later round in input order
+	for(uint32_t round = 0; round <= maxRound; round++)
+		for(uint32_t c = 0; c < nc; c++)
+		{
+			const uint32_t t = tag[c];
+			if(t == 0xffffu)
+			{
+				if(round) continue;
+				const uint32_t key = w.pairs[sc.pairStart + cons[c]];
+				const uint32_t a = key >> 16, b = key & 0xffffu;
+				const uint32_t d = a < n ? a : b;
+				ordered[perPart[maxNormal[d] + staticProgress[d]++]++] = cons[c];
+			}
+			else if((t >> 8) == round)
+				ordered[perPart[t & 0xffu]++] = cons[c];
+		}
+	return nbPart;
+}
+
+__device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
+	tgs::BodyVel* vel = w.vel + sc.solverStart;
+	tgs::BodyTx* tx = w.tx + sc.solverStart;
+	tgs::BodyData* data = w.data + sc.solverStart;
+	Tr* pose = w.pose + sc.solverStart;
+	const V3 g = v3(sp.gx, sp.gy, sp.gz);
+	// 1. solver bodies (PxConstructSolverBodiesTGS / PxConstructStaticSolverBodyTGS)
+	for(uint32_t i = lane; i < nTot; i += 32)
+	{
+		if(i < n)
+		{
+			Tr p;
+			tgs::constructDynamicBody(w.bodies[sc.bodyStart + i], g, sp.dt, vel[i], tx[i], data[i], p);
+			pose[i] = p;
+		}
+		else
+		{
+			const Tr p = loadStaticPose(w.staticPose + 7 * size_t(sc.staticStart + (i - n)));
+			tgs::constructStaticBody(p, vel[i], tx[i], data[i]);
+			pose[i] = p;
+		}
+	}
+	// 2. constraints = pairs with contacts, in pair order
+	const uint32_t count = w.pairCount[sid];
+	uint32_t nc = 0;
+	for(uint32_t base = 0; base < count; base += 32)
+	{
+		const uint32_t k = base + lane;
+		const bool has = k < count && w.contactCount[sc.pairStart + k] > 0;
+		const uint32_t bal = __ballot_sync(0xffffffffu, has);
+		if(has) w.consList[sc.pairStart + nc + __popc(bal & laneMaskLt())] = k;
+		nc += __popc(bal);
+	}
+	__syncwarp();
+	// 3. batching (one lane)
+	uint32_t nbPart = 0;
+	if(lane == 0)
+	{
+		nbPart = sceneBatch(w, sc, sid, nc);
+		if(!nbPart && nc) atomicOr(&w.status[sid], ST_PARTITION_OVERFLOW);
+	}
+	nbPart = __shfl_sync(0xffffffffu, nbPart, 0);
+	__syncwarp();
+	if(!nbPart && nc) return;   // leave the scene unchanged; the host sees the status bit
+	// 4. contact rows
+	const float invDt = 1.0f / sp.dt;
+	tgs::PrepParams pp;
+	pp.invStepDt = invDt * float(sp.nbPos);
+	pp.invTotalDt = invDt;
+	pp.totalDt = 1.0f / invDt;
+	pp.stepDt = 1.0f / pp.invStepDt;
+	pp.bounceThreshold = sp.bounceThreshold;
+	pp.frictionOffsetThreshold = sp.frictionOffsetThreshold;
+	pp.biasCoefficient = 2.0f * sqrtf(invDt / pp.invStepDt);
+	for(uint32_t r = lane; r < nc; r += 32)
+	{
+		const uint32_t k = w.ordered[sc.pairStart + r];
+		const uint32_t key = w.pairs[sc.pairStart + k];
+		const uint32_t a = key >> 16, b = key & 0xffffu;
+		const float fa = w.friction[sc.bodyStart + a];
+		const float fb = b < n ? w.friction[sc.bodyStart + b] : sp.staticFriction;
+		const float mu = (fa + fb) * 0.5f;
+		tgs::Contact cs[tgs::MAX_CONTACTS];
+		const uint32_t cnt = w.contactCount[sc.pairStart + k];
+		const float4* src = w.contacts + size_t(sc.pairStart + k) * 8;
+		for(uint32_t c = 0; c < cnt; c++)
+		{
+			const float4 nn = src[2 * c], pp4 = src[2 * c + 1];
+			cs[c].n = v3(nn.x, nn.y, nn.z);
+			cs[c].sep = nn.w;
+			cs[c].p = v3(pp4.x, pp4.y, pp4.z);
+			cs[c].staticFriction = mu;
+			cs[c].dynamicFriction = mu;
+			cs[c].restitution = 0.0f;
+		}
+		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp,
+		                    w.recs[sc.pairStart + r]);
+	}
+	__syncwarp();
+	// 5. position iterations (each followed by integration), then velocity iterations
+	const uint32_t* ends = w.partEnds + size_t(sid) * MAX_PARTITIONS;
+	const float stepDt = sp.dt / float(sp.nbPos);
+	float elapsed = 0.0f;
+	for(uint32_t it = 0; it < sp.nbPos + sp.nbVel; it++)
+	{
+		const bool posIter = it < sp.nbPos;
+		const float minPen = posIter ? -FLT_MAX : 0.0f;
+		uint32_t begin = 0;
+		for(uint32_t p = 0; p < nbPart; p++)
+		{
+			const uint32_t end = ends[p];
+			for(uint32_t r = begin + lane; r < end; r += 32)
+			{
+				tgs::ConstraintRecord& rec = w.recs[sc.pairStart + r];
+				if(rec.nbPatches == 0) continue;
+				const uint32_t a = uint32_t(rec.bodyA), b = uint32_t(rec.bodyB);
+				tgs::BodyVel b0 = vel[a], b1 = vel[b];
+				const bool dynB = b < n;
+				tgs::solveConstraint(rec, b0, b1, dynB, minPen, elapsed);
+				vel[a].lin = b0.lin;
+				vel[a].ang = b0.ang;
+				if(dynB)
+				{
+					vel[b].lin = b1.lin;
+					vel[b].ang = b1.ang;
+				}
+			}
+			begin = end;
+			__syncwarp();
+		}
+		if(posIter)
+		{
+			for(uint32_t i = lane; i < n; i += 32) tgs::integrateStep(vel[i], tx[i], stepDt);
+			elapsed += stepDt;
+			__syncwarp();
+		}
+	}
+	// 6. PxIntegrateSolverBodiesTGS + write-back of velocities and poses
+	for(uint32_t i = lane; i < n; i += 32)
+	{
+		Tr p = pose[i];
+		V3 wv;
+		tgs::finalizeBody(vel[i], tx[i], p, wv);
+		tgs::RigidBody& rb = w.bodies[sc.bodyStart + i];
+		rb.linVel[0] = vel[i].lin.x; rb.linVel[1] = vel[i].lin.y; rb.linVel[2] = vel[i].lin.z;
+		rb.angVel[0] = wv.x; rb.angVel[1] = wv.y; rb.angVel[2] = wv.z;
+		rb.q[0] = p.q.x; rb.q[1] = p.q.y; rb.q[2] = p.q.z; rb.q[3] = p.q.w;
+		rb.p[0] = p.p.x; rb.p[1] = p.p.y; rb.p[2] = p.p.z;
+	}
+	__syncwarp();
+}
+
+// One step of every scene: a persistent grid of warps pulls scenes from the
+// size-sorted work table.
+__global__ void __launch_bounds__(128) stepKernel(WorldDev w, StepParams sp)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	for(;;)
+	{
+		uint32_t item = 0;
+		if(lane == 0) item = atomicAdd(w.workCounter, 1u);
+		item = __shfl_sync(0xffffffffu, item, 0);
+		if(item >= w.nbScenes) break;
+		const uint32_t sid = w.workOrder[item];
+		const SceneDesc sc = w.scenes[sid];
+		sceneBroadphase(w, sc, sid, sp);
+		sceneNarrowphase(w, sc, sid, sp);
+		sceneSolve(w, sc, sid, sp);
+	}
+}
+// Totals over all scenes after a step: pairs, pairs with contacts, contacts.
+__global__ void statsKernel(const SceneDesc* __restrict__ scenes, uint32_t nbScenes, const uint32_t* __restrict__ pairCount,
+                            const uint32_t* __restrict__ contactCount, unsigned long long* __restrict__ out)
+{
+	const uint32_t sid = blockIdx.x;
+	if(sid >= nbScenes) return;
+	const SceneDesc sc = scenes[sid];
+	const uint32_t count = pairCount[sid];
+	unsigned long long withContacts = 0, contacts = 0;
+	for(uint32_t k = threadIdx.x; k < count; k += blockDim.x)
+	{
+		const uint32_t c = contactCount[sc.pairStart + k];
+		withContacts += c ? 1 : 0;
+		contacts += c;
+	}
+	for(int o = 16; o > 0; o >>= 1)
+	{
+		withContacts += __shfl_down_sync(0xffffffffu, withContacts, o);
+		contacts += __shfl_down_sync(0xffffffffu, contacts, o);
+	}
+	if((threadIdx.x & 31) == 0)
+	{
+		atomicAdd(&out[1], withContacts);
+		atomicAdd(&out[2], contacts);
+	}
+	if(threadIdx.x == 0) atomicAdd(&out[0], static_cast<unsigned long long>(count));
+}
+} // namespace world
+
+// Host-side world: scene table, resident state, scratch, graph.
+struct World
+{
+	cudaStream_t stream = 0;
+	cudaGraphExec_t graphExec = nullptr;
+	uint32_t graphSteps = 0;
+	world::StepParams params;
+	std::vector<world::SceneDesc> hScenes;
+	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
+	uint32_t gridBlocks = 0;
+	DevBuf<world::SceneDesc> scenes;
+	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
+	    staticProgress, partEnds, status;
+	DevBuf<tgs::RigidBody> bodies;
+	DevBuf<int> types, staticTypes;
+	DevBuf<float4> geoms, staticGeoms, contacts;
+	DevBuf<float> friction, staticPose, aabb;
+	DevBuf<unsigned long long> keys, stats;
+	DevBuf<uint32_t> identity;
+	DevBuf<tgs::ConstraintRecord> recs;
+	DevBuf<tgs::BodyVel> vel;
+	DevBuf<tgs::BodyTx> tx;
+	DevBuf<tgs::BodyData> data;
+	DevBuf<Tr> pose;
+	HostBuf<tgs::RigidBody> hStage;
+	size_t deviceBytes = 0;
+
+	static uint32_t pow2(uint32_t x) { uint32_t p = 1; while(p < x) p <<= 1; return p; }
+
+	world::WorldDev dev()
+	{
+		world::WorldDev w;
+		w.scenes = scenes.ptr; w.workOrder = workOrder.ptr; w.nbScenes = nbScenes; w.workCounter = workCounter.ptr;
+		w.bodies = bodies.ptr; w.types = types.ptr; w.geoms = geoms.ptr; w.friction = friction.ptr;
+		w.staticPose = staticPose.ptr; w.staticTypes = staticTypes.ptr; w.staticGeoms = staticGeoms.ptr;
+		w.aabb = aabb.ptr; w.keys = keys.ptr; w.pairs = pairs.ptr; w.pairCount = pairCount.ptr; w.contacts = contacts.ptr;
+		w.contactCount = contactCount.ptr; w.ordered = ordered.ptr; w.consList = consList.ptr; w.tag = tag.ptr; w.recs = recs.ptr;
+		w.vel = vel.ptr; w.tx = tx.ptr; w.data = data.ptr; w.pose = pose.ptr; w.progress = progress.ptr; w.maxNormal = maxNormal.ptr;
+		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
+		return w;
+	}
+
+	int create(uint32_t S, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, const void* rigid, const int* typesIn,
+	           const float* geomsIn, const float* frictionIn, const float* staticPoseIn, const int* staticTypesIn, const float* staticGeomsIn,
+	           uint32_t pairsPerBody, const world::StepParams& sp)
+	{
+		params = sp;
+		nbScenes = S;
+		hScenes.resize(S);
+		uint32_t b = 0, st = 0, key = 0, pair = 0;
+		for(uint32_t s = 0; s < S; s++)
+		{
+			world::SceneDesc& d = hScenes[s];
+			if(sceneBodyCount[s] == 0 || sceneBodyCount[s] + sceneStaticCount[s] > 65535u) return GBPX_ERR_INVALID;
+			d.bodyStart = b; d.nbBodies = sceneBodyCount[s];
+			d.staticStart = st; d.nbStatics = sceneStaticCount[s];
+			d.solverStart = b + st;
+			d.keyStart = key; d.keyCap = pow2(d.nbBodies);
+			d.pairStart = pair; d.pairCap = pow2(d.nbBodies * pairsPerBody + d.nbBodies * d.nbStatics);
+			b += d.nbBodies; st += d.nbStatics; key += d.keyCap; pair += d.pairCap;
+		}
+		nbBodies = b; nbStatics = st; nbSolver = b + st; nbKeys = key; nbPairSlots = pair;
+		std::vector<uint32_t> order(S);
+		std::iota(order.begin(), order.end(), 0u);
+		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
+		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(1) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
+		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
+		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
+		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
+		   vel.reserve(nbSolver) || tx.reserve(nbSolver) || data.reserve(nbSolver) || pose.reserve(nbSolver) || progress.reserve(nbSolver) ||
+		   maxNormal.reserve(nbSolver) || maxStatic.reserve(nbSolver) || staticProgress.reserve(nbSolver) ||
+		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(3) ||
+		   identity.reserve(S))
+			return GBPX_ERR_NOMEM;
+		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
+		              size_t(nbSolver) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + size_t(key) * 8;
+		cudaStream_t s = stream;
+		GBPX_CUDA_TRY(cudaMemcpyAsync(scenes.ptr, hScenes.data(), S * sizeof(world::SceneDesc), cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(workOrder.ptr, order.data(), S * 4, cudaMemcpyHostToDevice, s));
+		std::vector<uint32_t> ident(S);
+		std::iota(ident.begin(), ident.end(), 0u);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(identity.ptr, ident.data(), S * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(bodies.ptr, rigid, size_t(b) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(types.ptr, typesIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(geoms.ptr, geomsIn, size_t(b) * 16, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(friction.ptr, frictionIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
+		if(st)
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticPose.ptr, staticPoseIn, size_t(st) * 28, cudaMemcpyHostToDevice, s));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticTypes.ptr, staticTypesIn, size_t(st) * 4, cudaMemcpyHostToDevice, s));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticGeoms.ptr, staticGeomsIn, size_t(st) * 16, cudaMemcpyHostToDevice, s));
+		}
+		GBPX_CUDA_TRY(cudaMemsetAsync(status.ptr, 0, S * 4, s));
+		int dev = 0, sms = 0, perSm = 0;
+		GBPX_CUDA_TRY(cudaGetDevice(&dev));
+		GBPX_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		GBPX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, world::stepKernel, 128, 0));
+		gridBlocks = uint32_t(std::max(1, sms * std::max(1, perSm)));
+		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+		return GBPX_OK;
+	}
+
+	int launchStep()
+	{
+		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, 4, stream));
+		world::stepKernel<<<gridBlocks, 128, 0, stream>>>(dev(), params);
+		GBPX_CUDA_TRY(cudaGetLastError());
+		return GBPX_OK;
+	}
+
+	// Captures `steps` consecutive steps into one CUDA graph (replayed by step()).
+	int capture(uint32_t steps)
+	{
+		if(graphExec) { cudaGraphExecDestroy(graphExec); graphExec = nullptr; }
+		cudaGraph_t graph;
+		GBPX_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+		for(uint32_t i = 0; i < steps; i++)
+		{
+			const int rc = launchStep();
+			if(rc) { cudaStreamEndCapture(stream, &graph); return rc; }
+		}
+		GBPX_CUDA_TRY(cudaStreamEndCapture(stream, &graph));
+		GBPX_CUDA_TRY(cudaGraphInstantiate(&graphExec, graph, 0));
+		GBPX_CUDA_TRY(cudaGraphDestroy(graph));
+		graphSteps = steps;
+		return GBPX_OK;
+	}
+
+	int step(uint32_t steps, bool useGraph)
+	{
+		if(useGraph)
+		{
+			if(!graphExec || graphSteps != 1)
+			{
+				const int rc = capture(1);
+				if(rc) return rc;
+			}
+			for(uint32_t i = 0; i < steps; i++) GBPX_CUDA_TRY(cudaGraphLaunch(graphExec, stream));
+		}
+		else
+			for(uint32_t i = 0; i < steps; i++)
+			{
+				const int rc = launchStep();
+				if(rc) return rc;
+			}
+		return GBPX_OK;
+	}
+
+	// One scene per launch: no batching across scenes, no graph, no
+	// persistence (the comparison point of the batched step).
+	int stepPlain(uint32_t first, uint32_t count)
+	{
+		for(uint32_t s = first; s < first + count && s < nbScenes; s++)
+		{
+			world::WorldDev w = dev();
+			w.workOrder = identity.ptr + s;
+			w.nbScenes = 1;
+			GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, 4, stream));
+			world::stepKernel<<<1, 32, 0, stream>>>(w, params);
+		}
+		GBPX_CUDA_TRY(cudaGetLastError());
+		return GBPX_OK;
+	}
+
+	void release()
+	{
+		if(stream) cudaStreamSynchronize(stream);
+		if(graphExec) cudaGraphExecDestroy(graphExec);
+		graphExec = nullptr;
+		scenes.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
+		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
+		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
+		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
+		keys.release(); stats.release(); identity.release(); recs.release(); vel.release(); tx.release(); data.release(); pose.release(); hStage.release();
+		if(stream) cudaStreamDestroy(stream);
+		stream = 0;
+	}
+};
+} // namespace gbpx
+
+using gbpx::World;
+
+// Creates a world of nbScenes independent scenes.  Scene s owns
+// sceneBodyCount[s] consecutive dynamic bodies (PxRigidBodyData records with
+// shape type, 4 geometry floats and a friction coefficient each) and
+// sceneStaticCount[s] consecutive static shapes (PxTransform pose, type,
+// geometry; friction `staticFriction`).  params: dt, gravity xyz,
+// contactDistance, toleranceLength, boundsMargin, bounceThreshold,
+// frictionOffsetThreshold, correlationDistance, staticFriction (11 floats);
+// iterations: nbPositionIterations, nbVelocityIterations.
+GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, const void* rigidBodies,
+                               const int* types, const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes,
+                               const float* staticGeoms, const float* params, const uint32_t* iterations, uint32_t pairsPerBody,
+                               void** outWorld)
+{
+	if(!outWorld || !nbScenes || !sceneBodyCount || !sceneStaticCount || !rigidBodies || !types || !geoms || !friction || !params ||
+	   !iterations || !iterations[0] || !iterations[1] || !pairsPerBody)
+		return GBPX_ERR_INVALID;
+	gbpx::world::StepParams sp;
+	sp.dt = params[0]; sp.gx = params[1]; sp.gy = params[2]; sp.gz = params[3];
+	sp.contactDistance = params[4]; sp.toleranceLength = params[5]; sp.boundsMargin = params[6];
+	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
+	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
+	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
+	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
+		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
+			if(uint32_t(types[b]) > 3u || types[b] == 1) return GBPX_ERR_INVALID;   // dynamic planes are not allowed
+	World* w = new World;
+	const int rc = w->create(nbScenes, sceneBodyCount, sceneStaticCount, rigidBodies, types, geoms, friction, staticPoses, staticTypes,
+	                         staticGeoms, pairsPerBody, sp);
+	if(rc) { w->release(); delete w; return rc; }
+	*outWorld = w;
+	return GBPX_OK;
+}
+
+GBPX_API void gbpx_world_release(void* w)
+{
+	if(!w) return;
+	static_cast<World*>(w)->release();
+	delete static_cast<World*>(w);
+}
+
+// Advances every scene by nbSteps on the device (asynchronous; state stays in
+// HBM).  useGraph replays a captured CUDA graph of one step.
+GBPX_API int gbpx_world_step(void* w, uint32_t nbSteps, int useGraph)
+{
+	if(!w) return GBPX_ERR_INVALID;
+	return static_cast<World*>(w)->step(nbSteps, useGraph != 0);
+}
+
+GBPX_API int gbpx_world_synchronize(void* w)
+{
+	if(!w) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaStreamSynchronize(static_cast<World*>(w)->stream));
+	return GBPX_OK;
+}
+
+// Copies every dynamic body (PxRigidBodyData) to / from host memory.
+GBPX_API int gbpx_world_get_bodies(void* wv, void* outRigid)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !outRigid) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outRigid, w->bodies.ptr, size_t(w->nbBodies) * sizeof(gbpx::tgs::RigidBody), cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+GBPX_API int gbpx_world_set_bodies(void* wv, const void* rigid)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !rigid) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(w->bodies.ptr, rigid, size_t(w->nbBodies) * sizeof(gbpx::tgs::RigidBody), cudaMemcpyHostToDevice, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// Per-scene status words (bit 0: pair buffer overflow, bit 1: partition
+// overflow), cleared after reading.
+GBPX_API int gbpx_world_status(void* wv, uint32_t* outStatus)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !outStatus) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outStatus, w->status.ptr, size_t(w->nbScenes) * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaMemsetAsync(w->status.ptr, 0, size_t(w->nbScenes) * 4, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// nbScenes, nbBodies, nbStatics, pair slots, persistent grid blocks, device bytes
+GBPX_API int gbpx_world_info(void* wv, uint64_t* out6)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !out6) return GBPX_ERR_INVALID;
+	out6[0] = w->nbScenes; out6[1] = w->nbBodies; out6[2] = w->nbStatics; out6[3] = w->nbPairSlots; out6[4] = w->gridBlocks;
+	out6[5] = w->deviceBytes;
+	return GBPX_OK;
+}
+
+// Pair list of one scene after the last step: (id0 << 16 | id1) keys sorted,
+// statics numbered after the scene's dynamic bodies; and contact counts.
+GBPX_API int gbpx_world_scene_pairs(void* wv, uint32_t scene, uint32_t* outKeys, uint32_t* outContactCounts, uint32_t capacity,
+                                    uint32_t* outCount)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || scene >= w->nbScenes || !outCount) return GBPX_ERR_INVALID;
+	uint32_t count = 0;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(&count, w->pairCount.ptr + scene, 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	*outCount = count;
+	const uint32_t m = count < capacity ? count : capacity;
+	const uint32_t start = w->hScenes[scene].pairStart;
+	if(m && outKeys) GBPX_CUDA_TRY(cudaMemcpyAsync(outKeys, w->pairs.ptr + start, size_t(m) * 4, cudaMemcpyDeviceToHost, w->stream));
+	if(m && outContactCounts)
+		GBPX_CUDA_TRY(cudaMemcpyAsync(outContactCounts, w->contactCount.ptr + start, size_t(m) * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// Times nbSteps steps with CUDA events on the world's stream (device-resident
+// state, no host traffic); returns milliseconds.
+GBPX_API int gbpx_world_time_steps(void* wv, uint32_t nbSteps, int useGraph, float* outMs)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !outMs) return GBPX_ERR_INVALID;
+	if(useGraph && (!w->graphExec || w->graphSteps != 1))
+	{
+		const int rc = w->capture(1);
+		if(rc) return rc;
+	}
+	cudaEvent_t e0, e1;
+	GBPX_CUDA_TRY(cudaEventCreate(&e0));
+	GBPX_CUDA_TRY(cudaEventCreate(&e1));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	GBPX_CUDA_TRY(cudaEventRecord(e0, w->stream));
+	const int rc = w->step(nbSteps, useGraph != 0);
+	GBPX_CUDA_TRY(cudaEventRecord(e1, w->stream));
+	GBPX_CUDA_TRY(cudaEventSynchronize(e1));
+	GBPX_CUDA_TRY(cudaEventElapsedTime(outMs, e0, e1));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+// Steps scenes [first, first + count) one scene per launch (no cross-scene
+// batching, no graph) and returns the elapsed milliseconds (CUDA events).
+GBPX_API int gbpx_world_time_plain(void* wv, uint32_t first, uint32_t count, float* outMs)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !outMs) return GBPX_ERR_INVALID;
+	cudaEvent_t e0, e1;
+	GBPX_CUDA_TRY(cudaEventCreate(&e0));
+	GBPX_CUDA_TRY(cudaEventCreate(&e1));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	GBPX_CUDA_TRY(cudaEventRecord(e0, w->stream));
+	const int rc = w->stepPlain(first, count);
+	GBPX_CUDA_TRY(cudaEventRecord(e1, w->stream));
+	GBPX_CUDA_TRY(cudaEventSynchronize(e1));
+	GBPX_CUDA_TRY(cudaEventElapsedTime(outMs, e0, e1));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+// Totals of the last step: pairs, pairs with contacts (constraints), contacts.
+GBPX_API int gbpx_world_stats(void* wv, uint64_t* out3)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !out3) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemsetAsync(w->stats.ptr, 0, 3 * 8, w->stream));
+	gbpx::world::statsKernel<<<w->nbScenes, 256, 0, w->stream>>>(w->scenes.ptr, w->nbScenes, w->pairCount.ptr, w->contactCount.ptr, w->stats.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(out3, w->stats.ptr, 3 * 8, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// End-to-end step through host memory: uploads the bodies from `rigidIn`
+// (host, PxRigidBodyData), advances every scene by nbSteps and downloads them
+// into `rigidOut`; returns the elapsed milliseconds measured with CUDA events
+// around the copies and the step.
+GBPX_API int gbpx_world_step_host(void* wv, const void* rigidIn, void* rigidOut, uint32_t nbSteps, int useGraph, float* outMs)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !rigidIn || !rigidOut) return GBPX_ERR_INVALID;
+	if(useGraph && (!w->graphExec || w->graphSteps != 1))
+	{
+		const int rc = w->capture(1);
+		if(rc) return rc;
+	}
+	cudaEvent_t e0, e1;
+	GBPX_CUDA_TRY(cudaEventCreate(&e0));
+	GBPX_CUDA_TRY(cudaEventCreate(&e1));
+	GBPX_CUDA_TRY(cudaEventRecord(e0, w->stream));
+	const size_t bytes = size_t(w->nbBodies) * sizeof(gbpx::tgs::RigidBody);
+	GBPX_CUDA_TRY(cudaMemcpyAsync(w->bodies.ptr, rigidIn, bytes, cudaMemcpyHostToDevice, w->stream));
+	const int rc = w->step(nbSteps, useGraph != 0);
+	GBPX_CUDA_TRY(cudaMemcpyAsync(rigidOut, w->bodies.ptr, bytes, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaEventRecord(e1, w->stream));
+	GBPX_CUDA_TRY(cudaEventSynchronize(e1));
+	if(outMs) GBPX_CUDA_TRY(cudaEventElapsedTime(outMs, e0, e1));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+// Pinned host allocation for world body arrays (fast copies); free with gbpx_host_free.
+GBPX_API int gbpx_host_alloc(size_t bytes, void** out)
+{
+	if(!out) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMallocHost(out, bytes));
+	return GBPX_OK;
+}
+
+GBPX_API void gbpx_host_free(void* p)
+{
+	if(p) cudaFreeHost(p);
+}

@@ -1,0 +1,81 @@
+"""Immediate-mode TGS mirror over the GB300 solver kernels.
+
+Mirrors physx/include/PxImmediateMode.h:592-729: PxConstructSolverBodiesTGS,
+PxBatchConstraintsTGS and one full TGS step (PxCreateContactConstraintsTGS +
+PxSolveConstraintsTGS + PxIntegrateSolverBodiesTGS) from given contacts.
+Rigid bodies are PxRigidBodyData records (numpy structured array, 96 bytes).
+"""
+import ctypes
+
+import numpy as np
+
+from . import check, lib
+
+_p = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+
+
+def _setup():
+    L = lib()
+    if not getattr(L, "_tgs_ready", False):
+        L.gbpx_batch_constraints_tgs.restype = ctypes.c_uint32
+        L.gbpx_batch_constraints_tgs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                                 ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_construct_solver_bodies_tgs.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_float,
+                                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_tgs_solve.argtypes = ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 5 +
+                                     [ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float] + [ctypes.c_void_p] * 6)
+        L._tgs_ready = True
+    return L
+
+
+def batch_constraints(body_a, body_b, nb_dynamic, nb_static=0):
+    """Returns (header_start, header_stride, order)."""
+    L = _setup()
+    a = np.ascontiguousarray(body_a, np.uint32)
+    b = np.ascontiguousarray(body_b, np.uint32)
+    n = len(a)
+    hs = np.zeros(max(n, 1), np.uint32)
+    hst = np.zeros(max(n, 1), np.uint32)
+    order = np.zeros(max(n, 1), np.uint32)
+    nh = L.gbpx_batch_constraints_tgs(_p(a), _p(b), n, nb_dynamic, nb_static, _p(hs), _p(hst), _p(order))
+    return hs[:nh].copy(), hst[:nh].copy(), order[:n].copy()
+
+
+def construct_solver_bodies(rigid, gravity, dt):
+    """Returns raw (PxTGSSolverBodyVel, PxTGSSolverBodyTxInertia, PxTGSSolverBodyData) records as float32 views."""
+    L = _setup()
+    rigid = np.ascontiguousarray(rigid)
+    n = len(rigid)
+    vel = np.zeros((n, 16), np.float32)
+    tx = np.zeros((n, 16), np.float32)
+    data = np.zeros((n, 12), np.float32)
+    g = np.asarray(gravity, np.float32)
+    check(L.gbpx_construct_solver_bodies_tgs(_p(rigid), n, _p(g), dt, _p(vel), _p(tx), _p(data)), "PxConstructSolverBodiesTGS")
+    return vel, tx, data
+
+
+def tgs_step(rigid, static_poses, body_a, body_b, contact_start, contact_count, contacts, material, dt=1.0 / 60.0,
+             nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0), bounce=-2.0, friction_offset=0.04, correlation=0.025):
+    """Returns (velocities (n,6), poses (n,7), header_start, header_stride, order)."""
+    L = _setup()
+    rigid = np.ascontiguousarray(rigid)
+    n = len(rigid)
+    sp = np.ascontiguousarray(static_poses, np.float32)
+    a = np.ascontiguousarray(body_a, np.uint32)
+    b = np.ascontiguousarray(body_b, np.uint32)
+    nc = len(a)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nc, 1) * 2, np.uint32)
+    hst = np.zeros(max(nc, 1) * 2, np.uint32)
+    order = np.zeros(max(nc, 1), np.uint32)
+    nh = ctypes.c_uint32(0)
+    g = np.asarray(gravity, np.float32)
+    check(L.gbpx_tgs_solve(_p(rigid), n, _p(sp), len(sp), _p(a), _p(b), nc,
+                           _p(np.ascontiguousarray(contact_start, np.uint32)), _p(np.ascontiguousarray(contact_count, np.uint32)),
+                           _p(np.ascontiguousarray(contacts, np.float32)), _p(np.ascontiguousarray(material, np.float32)), _p(g),
+                           dt, nb_pos, nb_vel, bounce, friction_offset, correlation, _p(vel), _p(pose), _p(hs), _p(hst),
+                           _p(order), ctypes.byref(nh)), "TGS step")
+    return vel, pose, hs[:nh.value].copy(), hst[:nh.value].copy(), order[:nc].copy()

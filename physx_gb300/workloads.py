@@ -1,0 +1,115 @@
+"""Synthetic workloads of the rigid-body step (seeded, no external data).
+
+batched_scenes() is the batched workload: independent scenes with body counts
+log-uniform in [8, 512] (sphere / box / capsule mix), dropped from U(1, 20) m
+onto a per-scene ground plane.  Rigid bodies are PxRigidBodyData records
+(physx/include/PxImmediateMode.h:68) with the reference's rigid-dynamic
+defaults (physx/source/simulationcontroller/src/ScBodyCore.cpp:50-54).
+"""
+import numpy as np
+
+def random_quat(rng, n):
+    """Haar-uniform unit quaternions (Shoemake), (n, 4) as (x, y, z, w)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    q = np.stack([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+                  np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)], axis=1)
+    return q.astype(np.float32)
+
+def plane_pose_y_up():
+    """PxTransformFromPlaneEquation(PxPlane(0,1,0,0)): x axis of the plane frame -> +y."""
+    s = np.float32(np.sqrt(0.5))
+    return np.array([0.0, 0.0, s, s, 0.0, 0.0, 0.0], np.float32)
+
+def rigid_body_data(n):
+    """Zeroed PxRigidBodyData array (physx/include/PxImmediateMode.h:68), 96 bytes each,
+    with the reference's rigid-dynamic defaults (ScBodyCore.cpp:50-54, PxvDynamics.h:140)."""
+    dt = np.dtype([("linVel", "<f4", 3), ("invMass", "<f4"), ("angVel", "<f4", 3), ("maxDepenetrationVelocity", "<f4"),
+                   ("invInertia", "<f4", 3), ("maxContactImpulse", "<f4"), ("q", "<f4", 4), ("p", "<f4", 3),
+                   ("linearDamping", "<f4"), ("angularDamping", "<f4"), ("maxLinearVelocitySq", "<f4"),
+                   ("maxAngularVelocitySq", "<f4"), ("pad", "<u4")])
+    assert dt.itemsize == 96
+    r = np.zeros(n, dt)
+    r["q"][:, 3] = 1.0
+    r["maxDepenetrationVelocity"] = 1e32
+    r["maxContactImpulse"] = 1e32
+    r["linearDamping"] = 0.0
+    r["angularDamping"] = 0.05
+    r["maxLinearVelocitySq"] = 1e32
+    r["maxAngularVelocitySq"] = 100.0 * 100.0
+    return r
+
+def mass_properties(t, g, density=1000.0):
+    """Mass and mass-space inverse inertia diagonal of a sphere / capsule (along x) / box."""
+    if t == 0:
+        r = g[0]
+        m = density * 4.0 / 3.0 * np.pi * r ** 3
+        i = np.full(3, 0.4 * m * r * r)
+    elif t == 3:
+        hx, hy, hz = g[:3]
+        m = density * 8.0 * hx * hy * hz
+        i = np.array([m / 3.0 * (hy * hy + hz * hz), m / 3.0 * (hx * hx + hz * hz), m / 3.0 * (hx * hx + hy * hy)])
+    else:
+        r, hh = g[0], g[1]
+        mc = density * np.pi * r * r * 2.0 * hh       # cylinder
+        ms = density * 4.0 / 3.0 * np.pi * r ** 3      # two hemispheres
+        m = mc + ms
+        ix = mc * r * r / 2.0 + ms * 0.4 * r * r
+        iyz = mc * (r * r / 4.0 + (2 * hh) ** 2 / 12.0) + ms * (0.4 * r * r + hh * hh + 0.75 * hh * r)
+        i = np.array([ix, iyz, iyz])
+    return np.float32(1.0 / m), (1.0 / i).astype(np.float32)
+
+def batched_scenes(seed, nb_scenes, nmin=8, nmax=512, shapes=(0, 2, 3), drop=(1.0, 20.0), friction=(0.3, 0.8)):
+    """Independent scenes (the batched workload's shape): body counts log-uniform in
+    [nmin, nmax], sphere/box/capsule mix, drop heights U(drop) m above a per-scene
+    plane y=0, xz spread U(-sqrt(N), sqrt(N)) m, random orientations, zero velocity."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1), nb_scenes)).astype(np.int64)
+    counts = np.clip(counts, nmin, nmax).astype(np.uint32)
+    N = int(counts.sum())
+    types = rng.choice(np.array(shapes, np.int32), size=N)
+    geoms = np.zeros((N, 4), np.float32)
+    r = rng.uniform(0.25, 1.0, N)
+    geoms[types == 0, 0] = r[types == 0]
+    geoms[types == 3, :3] = rng.uniform(0.25, 1.0, (int((types == 3).sum()), 3))
+    cap = types == 2
+    geoms[cap, 0] = rng.uniform(0.2, 0.5, int(cap.sum()))
+    geoms[cap, 1] = rng.uniform(0.25, 1.0, int(cap.sum()))
+    rb = rigid_body_data(N)
+    rb["q"] = random_quat(rng, N)
+    spread = np.repeat(np.sqrt(counts.astype(np.float64)), counts)
+    rb["p"][:, 0] = rng.uniform(-1, 1, N) * spread
+    rb["p"][:, 2] = rng.uniform(-1, 1, N) * spread
+    rb["p"][:, 1] = rng.uniform(drop[0], drop[1], N)
+    im, ii = mass_properties_batch(types, geoms)
+    rb["invMass"] = im
+    rb["invInertia"] = ii
+    fr = rng.uniform(friction[0], friction[1], N).astype(np.float32)
+    S = nb_scenes
+    return dict(body_count=counts, static_count=np.ones(S, np.uint32), rigid=rb, types=types.astype(np.int32), geoms=geoms,
+                friction=fr, static_poses=np.tile(plane_pose_y_up(), (S, 1)), static_types=np.ones(S, np.int32),
+                static_geoms=np.zeros((S, 4), np.float32))
+
+
+
+def mass_properties_batch(types, geoms, density=1000.0):
+    """Vectorised mass_properties: (invMass (n,), invInertia (n, 3))."""
+    g = geoms.astype(np.float64)
+    m = np.zeros(len(types))
+    inertia = np.zeros((len(types), 3))
+    sph = types == 0
+    r = g[sph, 0]
+    m[sph] = density * 4.0 / 3.0 * np.pi * r ** 3
+    inertia[sph] = (0.4 * m[sph] * r * r)[:, None]
+    box = types == 3
+    hx, hy, hz = g[box, 0], g[box, 1], g[box, 2]
+    m[box] = density * 8.0 * hx * hy * hz
+    inertia[box] = np.stack([m[box] / 3.0 * (hy * hy + hz * hz), m[box] / 3.0 * (hx * hx + hz * hz), m[box] / 3.0 * (hx * hx + hy * hy)], 1)
+    cap = types == 2
+    r, hh = g[cap, 0], g[cap, 1]
+    mc = density * np.pi * r * r * 2.0 * hh
+    ms = density * 4.0 / 3.0 * np.pi * r ** 3
+    m[cap] = mc + ms
+    ix = mc * r * r / 2.0 + ms * 0.4 * r * r
+    iyz = mc * (r * r / 4.0 + (2 * hh) ** 2 / 12.0) + ms * (0.4 * r * r + hh * hh + 0.75 * hh * r)
+    inertia[cap] = np.stack([ix, iyz, iyz], 1)
+    return (1.0 / m).astype(np.float32), (1.0 / inertia).astype(np.float32)

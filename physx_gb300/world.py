@@ -1,0 +1,149 @@
+"""Batched multi-scene world: thousands of independent scenes stepped in one
+persistent launch per step (optionally replayed from a CUDA graph), all state
+resident in HBM.  Each scene's frame is the reference immediate-mode loop
+(ABP broadphase, PxGenerateContacts, TGS) with fresh per-frame caches.
+"""
+import ctypes
+
+import numpy as np
+
+from . import check, lib
+
+_p = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+
+DEFAULT_PARAMS = dict(dt=1.0 / 60.0, gravity=(0.0, -9.81, 0.0), contact_distance=0.04, tolerance_length=1.0, bounds_margin=0.02,
+                      bounce_threshold=-2.0, friction_offset_threshold=0.04, correlation_distance=0.025, static_friction=0.5,
+                      nb_pos=4, nb_vel=1)
+
+
+def param_vector(p):
+    g = p["gravity"]
+    params = np.array([p["dt"], g[0], g[1], g[2], p["contact_distance"], p["tolerance_length"], p["bounds_margin"],
+                       p["bounce_threshold"], p["friction_offset_threshold"], p["correlation_distance"], p["static_friction"]],
+                      np.float32)
+    return params, np.array([p["nb_pos"], p["nb_vel"]], np.uint32)
+
+
+def _setup():
+    L = lib()
+    if not getattr(L, "_world_ready", False):
+        L.gbpx_world_create.argtypes = [ctypes.c_uint32] + [ctypes.c_void_p] * 12 + [ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+        L.gbpx_world_release.argtypes = [ctypes.c_void_p]
+        L.gbpx_world_step.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int]
+        L.gbpx_world_synchronize.argtypes = [ctypes.c_void_p]
+        L.gbpx_world_get_bodies.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_set_bodies.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_scene_pairs.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                             ctypes.POINTER(ctypes.c_uint32)]
+        L.gbpx_world_time_steps.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.gbpx_world_time_plain.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+        L.gbpx_world_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_float)]
+        L.gbpx_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+        L.gbpx_host_free.argtypes = [ctypes.c_void_p]
+        L._world_ready = True
+    return L
+
+
+class World:
+    """`scenes` dict: body_count (S,), static_count (S,), rigid (PxRigidBodyData records),
+    types (N,), geoms (N,4), friction (N,), static_poses (M,7), static_types (M,), static_geoms (M,4)."""
+
+    def __init__(self, scenes, pairs_per_body=8, **params):
+        L = _setup()
+        p = dict(DEFAULT_PARAMS)
+        p.update(params)
+        self.params = p
+        pv, it = param_vector(p)
+        self._keep = [np.ascontiguousarray(scenes["body_count"], np.uint32), np.ascontiguousarray(scenes["static_count"], np.uint32),
+                      np.ascontiguousarray(scenes["rigid"]), np.ascontiguousarray(scenes["types"], np.int32),
+                      np.ascontiguousarray(scenes["geoms"], np.float32), np.ascontiguousarray(scenes["friction"], np.float32),
+                      np.ascontiguousarray(scenes["static_poses"], np.float32), np.ascontiguousarray(scenes["static_types"], np.int32),
+                      np.ascontiguousarray(scenes["static_geoms"], np.float32), pv, it]
+        h = ctypes.c_void_p()
+        k = self._keep
+        check(L.gbpx_world_create(len(k[0]), _p(k[0]), _p(k[1]), _p(k[2]), _p(k[3]), _p(k[4]), _p(k[5]), _p(k[6]), _p(k[7]), _p(k[8]),
+                                  _p(pv), _p(it), pairs_per_body, ctypes.byref(h)), "gbpx_world_create")
+        self._h, self._L = h, L
+        self.nb_bodies = len(k[2])
+        self.rigid_dtype = k[2].dtype
+
+    def release(self):
+        if self._h:
+            self._L.gbpx_world_release(self._h)
+            self._h = None
+        for ptr in getattr(self, "_pinned", []):
+            self._L.gbpx_host_free(ptr)
+        self._pinned = []
+
+    __del__ = release
+
+    def step(self, n=1, graph=True):
+        check(self._L.gbpx_world_step(self._h, n, int(graph)), "gbpx_world_step")
+
+    def synchronize(self):
+        check(self._L.gbpx_world_synchronize(self._h), "gbpx_world_synchronize")
+
+    def get_bodies(self, out=None):
+        out = np.empty(self.nb_bodies, self.rigid_dtype) if out is None else out
+        check(self._L.gbpx_world_get_bodies(self._h, _p(out)), "gbpx_world_get_bodies")
+        return out
+
+    def set_bodies(self, rigid):
+        rigid = np.ascontiguousarray(rigid)
+        check(self._L.gbpx_world_set_bodies(self._h, _p(rigid)), "gbpx_world_set_bodies")
+
+    def status(self):
+        st = np.zeros(len(self._keep[0]), np.uint32)
+        check(self._L.gbpx_world_status(self._h, _p(st)), "gbpx_world_status")
+        return st
+
+    def info(self):
+        out = np.zeros(6, np.uint64)
+        check(self._L.gbpx_world_info(self._h, _p(out)), "gbpx_world_info")
+        return dict(scenes=int(out[0]), bodies=int(out[1]), statics=int(out[2]), pair_slots=int(out[3]), grid_blocks=int(out[4]),
+                    device_bytes=int(out[5]))
+
+    def time_steps(self, n, graph=True):
+        """Milliseconds for n device-resident steps (CUDA events on the world stream)."""
+        ms = ctypes.c_float(0)
+        check(self._L.gbpx_world_time_steps(self._h, n, int(graph), ctypes.byref(ms)), "gbpx_world_time_steps")
+        return ms.value
+
+    def time_plain(self, first, count):
+        """Milliseconds to step scenes [first, first+count) one scene per launch."""
+        ms = ctypes.c_float(0)
+        check(self._L.gbpx_world_time_plain(self._h, first, count, ctypes.byref(ms)), "gbpx_world_time_plain")
+        return ms.value
+
+    def stats(self):
+        out = np.zeros(3, np.uint64)
+        check(self._L.gbpx_world_stats(self._h, _p(out)), "gbpx_world_stats")
+        return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]))
+
+    def step_host(self, rigid_in, rigid_out, n=1, graph=True):
+        """Upload bodies from host memory, step, download; returns event-timed milliseconds."""
+        ms = ctypes.c_float(0)
+        check(self._L.gbpx_world_step_host(self._h, _p(rigid_in), _p(rigid_out), n, int(graph), ctypes.byref(ms)), "gbpx_world_step_host")
+        return ms.value
+
+    def pinned_bodies(self):
+        """A pinned host array of PxRigidBodyData records sized for this world."""
+        ptr = ctypes.c_void_p()
+        nbytes = self.nb_bodies * self.rigid_dtype.itemsize
+        check(self._L.gbpx_host_alloc(nbytes, ctypes.byref(ptr)), "gbpx_host_alloc")
+        buf = (ctypes.c_uint8 * nbytes).from_address(ptr.value)
+        arr = np.frombuffer(buf, dtype=self.rigid_dtype, count=self.nb_bodies)
+        self._pinned = getattr(self, "_pinned", []) + [ptr]
+        return arr
+
+    def scene_pairs(self, scene, capacity=1 << 16):
+        keys = np.zeros(capacity, np.uint32)
+        cnt = np.zeros(capacity, np.uint32)
+        n = ctypes.c_uint32(0)
+        check(self._L.gbpx_world_scene_pairs(self._h, scene, _p(keys), _p(cnt), capacity, ctypes.byref(n)), "gbpx_world_scene_pairs")
+        m = min(n.value, capacity)
+        return np.stack([keys[:m] >> 16, keys[:m] & 0xffff], 1), cnt[:m]

@@ -9,6 +9,7 @@ Run on the development machine, where the reference sources exist:
 Each fixture stores its inputs and the reference's outputs, so the tests on
 machines without the reference need neither the reference nor this script.
 """
+import ctypes
 import os
 import sys
 
@@ -17,8 +18,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_libs import CpuBroadPhase, reference, run_contacts  # noqa: E402
-from scenarios import bp_frames, np_pairs  # noqa: E402
+from oracle_libs import CpuBroadPhase, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
+from scenarios import bp_frames, np_pairs, pile_scenes, random_scene  # noqa: E402
 
 BP_CASES = [
     # name, seed, boxes, frames, extent
@@ -60,11 +61,60 @@ def make_np():
         print("wrote", name)
 
 
+TGS_CASES = [
+    # name, seed, bodies: a settled-looking pile of spheres/capsules/boxes on a plane
+    ("tgs_pile_small", 31, 24),
+    ("tgs_pile", 32, 160),
+]
+
+
+def make_tgs():
+    for name, seed, n in TGS_CASES:
+        sc = random_scene(seed, n)
+        A, B = scene_pairs(sc)
+        a, b, s_, c, ct, mat = scene_contacts("pxref", sc, A, B)
+        vel, pose, hs, hst, order = run_tgs("pxref", sc, a, b, s_, c, ct, mat)
+        L = reference()
+        bv = np.zeros((n, 16), np.float32)
+        btx = np.zeros((n, 16), np.float32)
+        bd = np.zeros((n, 12), np.float32)
+        g = np.array([0.0, -9.81, 0.0], np.float32)
+        P = lambda x: x.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        L.pxref_construct_bodies_tgs(P(sc["rigid"]), ctypes.c_uint32(n), P(g), ctypes.c_float(1.0 / 60.0), P(bv), P(btx), P(bd))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), rigid=sc["rigid"].view(np.uint8).reshape(n, 96),
+                            static_poses=sc["static_poses"], body_a=a, body_b=b, contact_start=s_, contact_count=c,
+                            contacts=ct, material=mat, ref_velocity=vel, ref_pose=pose, ref_header_start=hs,
+                            ref_header_stride=hst, ref_order=order, ref_body_vel=bv, ref_body_txi=btx, ref_body_data=bd)
+        print("wrote", name)
+
+
+SCENE_CASES = [
+    # name, seed, scenes, bodies per scene, shapes: one full frame (bounds, ABP, contacts, TGS) per scene
+    ("scene_spheres_capsules", 41, 4, 48, (0, 2)),
+]
+
+
+def make_scene():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from physx_gb300.world import DEFAULT_PARAMS
+    for name, seed, S, n, shapes in SCENE_CASES:
+        sc = pile_scenes(seed, S, n, shapes=shapes)
+        out = run_scene_step("pxref", sc, DEFAULT_PARAMS, steps=1)
+        arrays = {k: v for k, v in sc.items() if k != "rigid"}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), rigid=sc["rigid"].view(np.uint8).reshape(-1, 96),
+                            ref_rigid=out.view(np.uint8).reshape(-1, 96), **arrays)
+        print("wrote", name)
+
+
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np"]
+    which = sys.argv[1:] or ["bp", "np", "tgs", "scene"]
     if "bp" in which:
         make_bp()
     if "np" in which:
         make_np()
+    if "tgs" in which:
+        make_tgs()
+    if "scene" in which:
+        make_scene()

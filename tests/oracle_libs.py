@@ -162,3 +162,22 @@ def run_tgs(which, scene, A, B, start, count, contacts, mat, dt=1.0 / 60.0, nb_p
             ctypes.c_uint32(nb_pos), ctypes.c_uint32(nb_vel), ctypes.c_float(bounce), ctypes.c_float(friction_offset),
             ctypes.c_float(correlation), _p(vel), _p(pose), _p(hs), _p(hst), _p(order), None, None)
     return vel, pose, hs[:nh].copy(), hst[:nh].copy(), order[:nc].copy()
+
+
+def run_scene_step(which, scenes, params, steps=1):
+    """Steps every scene `steps` times through the oracle ("orc") or the reference
+    ("pxref"); returns the updated PxRigidBodyData array."""
+    import sys
+    sys.path.insert(0, ROOT)
+    from physx_gb300.world import param_vector
+    pv, it = param_vector(params)
+    rb = np.ascontiguousarray(scenes["rigid"]).copy()
+    L = oracle() if which == "orc" else reference()
+    fn = L.orc_scene_step if which == "orc" else L.pxref_scene_step
+    keep = [np.ascontiguousarray(scenes[k], d) for k, d in (("body_count", np.uint32), ("static_count", np.uint32), ("types", np.int32),
+                                                              ("geoms", np.float32), ("friction", np.float32), ("static_poses", np.float32),
+                                                              ("static_types", np.int32), ("static_geoms", np.float32))]
+    for _ in range(steps):
+        fn(ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]), _p(keep[5]),
+           _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
+    return rb

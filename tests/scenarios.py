@@ -6,7 +6,14 @@ by N(0, sigma) each frame) plus edge cases the reference handles: touching
 faces, +0/-0 coordinates, equal min-X keys, static/kinematic/dynamic groups,
 shared (compound) group ids, per-object distances, removals and re-creations.
 """
+import os
+import sys
+
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from physx_gb300.workloads import (batched_scenes, mass_properties, plane_pose_y_up, random_quat,  # noqa: E402,F401
+                                  rigid_body_data)
 
 
 def filter_group(kind, i):
@@ -98,18 +105,6 @@ def sorted_pairs(a):
     return a[order]
 
 
-def random_quat(rng, n):
-    """Haar-uniform unit quaternions (Shoemake), (n, 4) as (x, y, z, w)."""
-    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
-    q = np.stack([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
-                  np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)], axis=1)
-    return q.astype(np.float32)
-
-
-def plane_pose_y_up():
-    """PxTransformFromPlaneEquation(PxPlane(0,1,0,0)): x axis of the plane frame -> +y."""
-    s = np.float32(np.sqrt(0.5))
-    return np.array([0.0, 0.0, s, s, 0.0, 0.0, 0.0], np.float32)
 
 
 def shape_params(rng, t):
@@ -186,44 +181,6 @@ def np_pairs(seed, n, types=None, spread=0.6, flat_frac=0.2):
     return dict(type0=t0, geom0=g0, type1=t1, geom1=g1, pose0=p0, pose1=p1)
 
 
-def rigid_body_data(n):
-    """Zeroed PxRigidBodyData array (physx/include/PxImmediateMode.h:68), 96 bytes each,
-    with the reference's rigid-dynamic defaults (ScBodyCore.cpp:50-54, PxvDynamics.h:140)."""
-    dt = np.dtype([("linVel", "<f4", 3), ("invMass", "<f4"), ("angVel", "<f4", 3), ("maxDepenetrationVelocity", "<f4"),
-                   ("invInertia", "<f4", 3), ("maxContactImpulse", "<f4"), ("q", "<f4", 4), ("p", "<f4", 3),
-                   ("linearDamping", "<f4"), ("angularDamping", "<f4"), ("maxLinearVelocitySq", "<f4"),
-                   ("maxAngularVelocitySq", "<f4"), ("pad", "<u4")])
-    assert dt.itemsize == 96
-    r = np.zeros(n, dt)
-    r["q"][:, 3] = 1.0
-    r["maxDepenetrationVelocity"] = 1e32
-    r["maxContactImpulse"] = 1e32
-    r["linearDamping"] = 0.0
-    r["angularDamping"] = 0.05
-    r["maxLinearVelocitySq"] = 1e32
-    r["maxAngularVelocitySq"] = 100.0 * 100.0
-    return r
-
-
-def mass_properties(t, g, density=1000.0):
-    """Mass and mass-space inverse inertia diagonal of a sphere / capsule (along x) / box."""
-    if t == 0:
-        r = g[0]
-        m = density * 4.0 / 3.0 * np.pi * r ** 3
-        i = np.full(3, 0.4 * m * r * r)
-    elif t == 3:
-        hx, hy, hz = g[:3]
-        m = density * 8.0 * hx * hy * hz
-        i = np.array([m / 3.0 * (hy * hy + hz * hz), m / 3.0 * (hx * hx + hz * hz), m / 3.0 * (hx * hx + hy * hy)])
-    else:
-        r, hh = g[0], g[1]
-        mc = density * np.pi * r * r * 2.0 * hh       # cylinder
-        ms = density * 4.0 / 3.0 * np.pi * r ** 3      # two hemispheres
-        m = mc + ms
-        ix = mc * r * r / 2.0 + ms * 0.4 * r * r
-        iyz = mc * (r * r / 4.0 + (2 * hh) ** 2 / 12.0) + ms * (0.4 * r * r + hh * hh + 0.75 * hh * r)
-        i = np.array([ix, iyz, iyz])
-    return np.float32(1.0 / m), (1.0 / i).astype(np.float32)
 
 
 def random_scene(seed, nbodies, spread=None, shapes=(0, 2, 3), drop=(0.2, 3.0), friction=(0.3, 0.8), plane=True,
@@ -250,3 +207,14 @@ def random_scene(seed, nbodies, spread=None, shapes=(0, 2, 3), drop=(0.2, 3.0), 
     statics = np.array([plane_pose_y_up()]) if plane else np.zeros((0, 7), np.float32)
     return dict(types=types, geoms=geoms.astype(np.float32), rigid=rb, friction=mats, static_poses=statics,
                 static_types=np.ones(len(statics), np.int32), static_geoms=np.zeros((len(statics), 4), np.float32))
+
+
+
+def pile_scenes(seed, nb_scenes, n, **kw):
+    """Like batched_scenes but every scene is a compact pile already in contact (for parity tests)."""
+    out = [random_scene(seed + k, n, **kw) for k in range(nb_scenes)]
+    rb = np.concatenate([o["rigid"] for o in out])
+    return dict(body_count=np.full(nb_scenes, n, np.uint32), static_count=np.ones(nb_scenes, np.uint32), rigid=rb,
+                types=np.concatenate([o["types"] for o in out]), geoms=np.concatenate([o["geoms"] for o in out]),
+                friction=np.concatenate([o["friction"] for o in out]), static_poses=np.tile(plane_pose_y_up(), (nb_scenes, 1)),
+                static_types=np.ones(nb_scenes, np.int32), static_geoms=np.zeros((nb_scenes, 4), np.float32))

@@ -75,3 +75,81 @@ def test_oracle_contacts_match_reference_golden(path):
     # the analytic pairs are reproduced bit for bit
     for k in ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule"):
         assert rep[k]["maxdiff"] == 0.0, (k, rep[k])
+
+
+TGS_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "tgs_*.npz")))
+
+# Velocity tolerance of one TGS solve against the reference, relative to the
+# body's speed (floor 1e-2 m/s): the reference solves 4-constraint headers
+# through its 4-wide SIMD block path (DyTGSContactPrepBlock.cpp:1398,
+# solveContact4_Block :2280), which reassociates the per-pair arithmetic this
+# build follows; the resulting differences stay below 2e-4 relative.  Poses are
+# compared at 2e-6 absolute.
+TGS_VEL_REL_TOL = 2e-4
+TGS_POSE_TOL = 2e-6
+
+
+def load_tgs_fixture(path):
+    z = np.load(path)
+    from scenarios import rigid_body_data
+    rb = rigid_body_data(len(z["rigid"]))
+    rb.view(np.uint8).reshape(len(rb), 96)[:] = z["rigid"]
+    return rb, {k: z[k] for k in z.files if k != "rigid"}
+
+
+def velocity_error(ref, got):
+    lin = np.linalg.norm(ref[:, :3], axis=1)
+    ang = np.linalg.norm(ref[:, 3:], axis=1)
+    scale = np.maximum(np.stack([lin] * 3 + [ang] * 3, 1), 1e-2)
+    return float((np.abs(ref - got) / scale).max())
+
+
+@pytest.mark.parametrize("path", TGS_FIXTURES, ids=[os.path.basename(p) for p in TGS_FIXTURES])
+def test_oracle_tgs_matches_reference_golden(path):
+    from oracle_libs import run_tgs
+    rb, z = load_tgs_fixture(path)
+    sc = dict(types=np.zeros(len(rb), np.int32), rigid=rb, static_poses=z["static_poses"])
+    vel, pose, hs, hst, order = run_tgs("orc", sc, z["body_a"], z["body_b"], z["contact_start"], z["contact_count"], z["contacts"],
+                                        z["material"])
+    # batching is reproduced exactly
+    assert np.array_equal(hs, z["ref_header_start"]) and np.array_equal(hst, z["ref_header_stride"])
+    assert np.array_equal(order, z["ref_order"])
+    assert velocity_error(z["ref_velocity"], vel) <= TGS_VEL_REL_TOL
+    assert np.abs(pose - z["ref_pose"]).max() <= TGS_POSE_TOL
+
+
+SCENE_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "scene_*.npz")))
+
+
+def load_scene_fixture(path):
+    from scenarios import rigid_body_data
+    z = np.load(path)
+    rb = rigid_body_data(len(z["rigid"]))
+    rb.view(np.uint8).reshape(len(rb), 96)[:] = z["rigid"]
+    ref = rigid_body_data(len(z["rigid"]))
+    ref.view(np.uint8).reshape(len(ref), 96)[:] = z["ref_rigid"]
+    scenes = {k: z[k] for k in z.files if k not in ("rigid", "ref_rigid")}
+    scenes["rigid"] = rb
+    return scenes, ref
+
+
+def rigid_velocity(rb):
+    return np.concatenate([rb["linVel"], rb["angVel"]], axis=1)
+
+
+@pytest.mark.parametrize("path", SCENE_FIXTURES, ids=[os.path.basename(p) for p in SCENE_FIXTURES])
+def test_oracle_scene_step_matches_reference_golden(path):
+    from oracle_libs import run_scene_step
+    sys_path_root()
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes, ref = load_scene_fixture(path)
+    out = run_scene_step("orc", scenes, DEFAULT_PARAMS, steps=1)
+    assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= TGS_VEL_REL_TOL
+    assert np.abs(out["p"] - ref["p"]).max() <= TGS_POSE_TOL and np.abs(out["q"] - ref["q"]).max() <= TGS_POSE_TOL
+
+
+def sys_path_root():
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
