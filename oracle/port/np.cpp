@@ -13,11 +13,9 @@
 //   GuPCMContactCapsuleBox.cpp:73 with GuPCMContactGenSphereCapsule.cpp:379;
 // manifold reduction/output follow GuPersistentContactManifold.cpp:552-1313.
 // Floating-point evaluation order follows the reference's SSE2 vector layer
-// (see pxmath.h).  The one deliberate difference: the reference's box-box
-// edge clipping uses an approximate reciprocal (V3RecipFast = rcpps,
-// GuPCMContactBoxBox.cpp:140, relative error up to 1.5*2^-12); this file uses
-// an exact IEEE reciprocal, so points produced by edge clipping can differ from
-// the reference by up to ~4e-4 of the clipped edge length.
+// (see pxmath.h), including its approximate reciprocal in the box-box edge
+// clipping (V3RecipFast = RCPPS, GuPCMContactBoxBox.cpp:140, restated as
+// recipFast).  GJK/EPA (edge-edge box pairs, capsule-box) follow np_gjk.h.
 #include "pxmath.h"
 #include "np_gjk.h"
 #include <string.h>
@@ -566,36 +564,22 @@ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, const Tr& t0, cons
 }
 
 // ----------------------------------------------------------------- box-box
-struct MatTr { M33 R; V3 p; };
 MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
 V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
 V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
 V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
-M33 transpose(const M33& m)
-{
-	M33 t;
-	t.c0 = v3(m.c0.x, m.c1.x, m.c2.x);
-	t.c1 = v3(m.c0.y, m.c1.y, m.c2.y);
-	t.c2 = v3(m.c0.z, m.c1.z, m.c2.z);
-	return t;
-}
+V3 mtTransformInv(const MatTr& m, V3 v) { return m33TMulV(m.R, sub(v, m.p)); }
 // a.transformInv(b) for matrix transforms (PxVecTransform.h:277)
 MatTr mtInvMul(const MatTr& a, const MatTr& b)
 {
 	MatTr r;
-	const M33 at = transpose(a.R);
+	const M33 at = transpose33(a.R);
 	r.R.c0 = m33MulV(at, b.R.c0);
 	r.R.c1 = m33MulV(at, b.R.c1);
 	r.R.c2 = m33MulV(at, b.R.c2);
 	r.p = m33TMulV(a.R, sub(b.p, a.p));
 	return r;
 }
-// Box-box edge-edge fallback (GJK/EPA between the boxes, GuPCMContactBoxBox.cpp:917-957)
-// and the capsule-box full manifold (GuPCMContactCapsuleBox.cpp:73): not restated
-// yet, so these configurations report no contact; the tests identify and skip them.
-bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
-bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, PC*, int&, V3&) { return false; }
-
 
 void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V3 ext)
 {
@@ -650,7 +634,7 @@ bool segAABB(V3 p0, V3 d, V3 mx, V3 mn, float& tmin, float& tmax)
 	float t1[3], t2[3];
 	for(int k = 0; k < 3; k++)
 	{
-		const float odd = 1.0f / dd[k];
+		const float odd = recipFast(dd[k]);   // V3RecipFast (GuPCMContactBoxBox.cpp:140)
 		t1[k] = par[k] ? 0.0f : (lo[k] - p[k]) * odd;
 		t2[k] = par[k] ? FLT_MAX : (hi[k] - p[k]) * odd;
 	}
@@ -749,7 +733,7 @@ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr& T1, float cDist,
 {
 	const float ea[3] = {e0.x, e0.y, e0.z}, eb[3] = {e1.x, e1.y, e1.z};
 	const MatTr t10 = mtInvMul(T0, T1);
-	const M33 r01 = transpose(t10.R);
+	const M33 r01 = transpose33(t10.R);
 	const V3 uEps = v3(1e-6f, 1e-6f, 1e-6f);
 	const float tx = t10.p.x, ty = t10.p.y, tz = t10.p.z;
 	const V3 col[3] = {t10.R.c0, t10.R.c1, t10.R.c2};
@@ -913,13 +897,17 @@ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen,
 		for(int i = 0; i < m.num; i++) out.add(mtTransform(T1, m.pts[i].b), wn, m.pts[i].pen);
 		return true;
 	}
-	// Edge-edge configuration: the reference falls back to GJK / EPA between the boxes
+	// Edge-edge configuration: GJK / EPA between the core boxes
 	// (GuPCMContactBoxBox.cpp:917-957), producing a single point.
-	GjkResult g;
 	const MatTr aToB = matFromTr(cur);
-	if(!gjkEpaBoxBox(e0, e1, aToB, cDist, tolLen, g)) return false;
+	const GjkConvex ca = makeRelativeBox(e0, aToB);
+	const GjkConvex cb = makeBox(e1);
+	GjkOut g;
+	int status = gjkPenetration(ca, cb, aToB.p, cDist, g);
+	if(status == EPA_CONTACT) status = epaPenetration(ca, cb, g, tolLen, g);
+	if(status != GJK_CONTACT && status != EPA_CONTACT) return false;
 	PC c;
-	c.a = mtRotateInv(aToB, sub(g.closestA, aToB.p));
+	c.a = mtTransformInv(aToB, g.closestA);
 	c.b = g.closestB;
 	c.n = g.normal;
 	c.pen = g.penDep;
@@ -932,22 +920,296 @@ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen,
 }
 
 // ----------------------------------------------------------------- capsule-box
+// PCMPolygonalBox (GuPCMShapeConvex.cpp:50): 8 vertices, 6 quads, plane
+// normals and the minimum-vertex index per face.
+const uint8_t kBoxQuads[24] = {0, 3, 2, 1, 1, 2, 6, 5, 5, 6, 7, 4, 4, 7, 3, 0, 3, 7, 6, 2, 4, 0, 1, 5};
+const int kBoxFaceAxis[6] = {2, 0, 2, 0, 1, 1};
+const float kBoxFaceSign[6] = {-1.0f, 1.0f, 1.0f, -1.0f, 1.0f, -1.0f};
+const int kBoxFaceMinVert[6] = {4, 0, 0, 1, 0, 2};
+
+struct PolyBox
+{
+	V3 verts[8];
+	V3 n[6];
+	float d[6];
+	explicit PolyBox(V3 h)
+	{
+		const V3 lo = neg(h);
+		verts[0] = v3(lo.x, lo.y, lo.z); verts[1] = v3(h.x, lo.y, lo.z);
+		verts[2] = v3(h.x, h.y, lo.z);   verts[3] = v3(lo.x, h.y, lo.z);
+		verts[4] = v3(lo.x, lo.y, h.z);  verts[5] = v3(h.x, lo.y, h.z);
+		verts[6] = v3(h.x, h.y, h.z);    verts[7] = v3(lo.x, h.y, h.z);
+		for(int i = 0; i < 6; i++)
+		{
+			float c[3] = {0.0f, 0.0f, 0.0f};
+			c[kBoxFaceAxis[i]] = kBoxFaceSign[i];
+			n[i] = v3(c[0], c[1], c[2]);
+			d[i] = -getc(h, kBoxFaceAxis[i]);
+		}
+	}
+	V3 vert(int face, int k) const { return verts[kBoxQuads[face * 4 + k]]; }
+};
+
+// PxPlane::distance with PxVec3::dot
+inline float planeDistance(V3 n, float d, V3 p) { return dotS(n, p) + d; }
+
+// testPolyDataAxis + testSATCapsulePoly (GuPCMContactGenSphereCapsule.cpp:41/:154)
+bool satCapsuleBox(V3 p0, V3 p1, float r, const PolyBox& pb, V3 ext, float cDist, V3& axisOut)
+{
+	float minOverlap = FLT_MAX;
+	V3 axis = v3(0, 1, 0);
+	for(int i = 0; i < 6; i++)
+	{
+		const V3 n = pb.n[i];
+		const float magnitude = 1.0f / sqrtf(dotA(n, n));
+		const V3 planeN = scale(n, magnitude);
+		const float min0 = dotA(n, pb.verts[kBoxFaceMinVert[i]]) * magnitude;
+		const float max0 = (-pb.d[i]) * magnitude;
+		const float t0 = dotA(p0, planeN), t1 = dotA(p1, planeN);
+		const float min1 = fmin_(t0, t1) - r, max1 = fmax_(t0, t1) + r;
+		if(min1 > max0 + cDist || min0 > max1 + cDist) return false;
+		const float ov = max0 - min1;
+		if(minOverlap > ov) { minOverlap = ov; axis = planeN; }
+	}
+	const V3 capAxis = sub(p1, p0);
+	for(int i = 0; i < 6; i++)
+	{
+		for(int s = 0, e = 3; s < 4; e = s++)
+		{
+			const V3 edge = sub(pb.vert(i, e), pb.vert(i, s));
+			const V3 dir = cross(capAxis, edge);
+			const float lenSq = dotA(dir, dir);
+			if(FLT_EPSILON > lenSq) continue;
+			const V3 n = scaleInv(dir, sqrtf(lenSq));
+			const V3 sp = v3(n.x > 0.0f ? ext.x : -ext.x, n.y > 0.0f ? ext.y : -ext.y, n.z > 0.0f ? ext.z : -ext.z);
+			const float max0 = dotA(n, sp), min0 = -max0;
+			const float t0 = dotA(p0, n), t1 = dotA(p1, n);
+			const float min1 = fmin_(t0, t1) - r, max1 = fmax_(t0, t1) + r;
+			if(min1 > max0 + cDist || min0 > max1 + cDist) return false;
+			const float ov = max0 - min1;
+			if(minOverlap > ov) { minOverlap = ov; axis = n; }
+		}
+	}
+	axisOut = axis;
+	return true;
+}
+
+// getPolygonIndex for a box (no edge data; GuPCMContactGenUtil.cpp:83)
+int boxPolygonIndex(const PolyBox& pb, V3 normal)
+{
+	float minProj = dotA(normal, pb.n[0]);
+	int best = 0;
+	for(int i = 1; i < 6; i++)
+	{
+		const float proj = dotA(normal, pb.n[i]);
+		if(minProj > proj) { minProj = proj; best = i; }
+	}
+	return best;
+}
+
+// getWitnessPolygonIndex (GuPCMContactGenUtil.cpp:201)
+int boxWitnessPolygonIndex(const PolyBox& pb, V3 normal, V3 closest, float tolerance)
+{
+	float pd[6];
+	const float eps = -tolerance;
+	float dist = planeDistance(pb.n[0], pb.d[0], closest);
+	float minDist = dist >= eps ? fabsf(dist) : FLT_MAX;
+	pd[0] = minDist;
+	float maxDist = dist;
+	int closestFace = 0, maxFace = 0;
+	for(int i = 1; i < 6; i++)
+	{
+		dist = planeDistance(pb.n[i], pb.d[i], closest);
+		pd[i] = dist >= eps ? fabsf(dist) : FLT_MAX;
+		if(minDist > pd[i]) { minDist = pd[i]; closestFace = i; }
+		if(dist > maxDist) { maxDist = dist; maxFace = i; }
+	}
+	if(minDist == FLT_MAX) return maxFace;
+	float bestProj = dotA(normalizeA(pb.n[closestFace]), normal);
+	const int first = closestFace;
+	for(int i = 0; i < 6; i++)
+	{
+		if(tolerance > pd[i] - minDist && first != i)
+		{
+			const float proj = dotA(normalizeA(pb.n[i]), normal);
+			if(bestProj > proj) { closestFace = i; bestProj = proj; }
+		}
+	}
+	return closestFace;
+}
+
+// findRotationMatrixFromZAxis (GuPersistentContactManifold.cpp:289)
+M33 rotationFromZAxis(V3 to)
+{
+	const float e = to.z, f = fabsf(e);
+	M33 m;
+	if(0.9999f > f)
+	{
+		const float vx = -to.y, vy = to.x;
+		const float h = 1.0f / (1.0f + e);
+		const float hvx = h * vx, hvxy = hvx * vy;
+		m.c0 = v3(hvx * vx + e, hvxy, vy);
+		m.c1 = v3(hvxy, h * (vy * vy) + e, -vx);
+		m.c2 = v3(-vy, vx, e);
+		return m;
+	}
+	const V3 u = v3(0.0f, 1.0f, -1.0f);   // (0,1,0) - (0,0,1)
+	const V3 v = sub(v3(0, 1, 0), to);
+	const float dotU = dotA(u, u), dotV = dotA(v, v), dotUV = dotA(u, v);
+	const float c1 = -(2.0f / dotU), c2 = -(2.0f / dotV);
+	const float c3 = c1 * (c2 * dotUV);
+	const V3 c1u = scale(u, c1), c2v = scale(v, c2), c3v = scale(v, c3);
+	m.c0 = scaleAdd(u, c1u.x, scaleAdd(v, c2v.x, scale(u, c3v.x)));
+	m.c0.x = m.c0.x + 1.0f;
+	m.c1 = scaleAdd(u, c1u.y, scaleAdd(v, c2v.y, scale(u, c3v.y)));
+	m.c1.y = m.c1.y + 1.0f;
+	m.c2 = scaleAdd(u, c1u.z, scaleAdd(v, c2v.z, scale(u, c3v.z)));
+	m.c2.z = m.c2.z + 1.0f;
+	return m;
+}
+
+// generatedCapsuleBoxFaceContacts (GuPCMContactGenSphereCapsule.cpp:221)
+void capsuleBoxFaceContacts(V3 p0, V3 p1, float r, const PolyBox& pb, int face, const MatTr& aToB, PC* mc, int& num, float cDist, V3 normal)
+{
+	const float radius = r + cDist;
+	const V3 planeN = normalizeA(pb.n[face]);
+	const V3 a = pb.vert(face, 0);
+	const float denom0 = dotA(planeN, sub(p0, a)), denom1 = dotA(planeN, sub(p1, a));
+	const float proj = dotA(planeN, normal);
+	const float numer = proj > 0.0f ? 1.0f / proj : 0.0f;
+	const float t0 = denom0 * numer, t1 = denom1 * numer;
+	const bool con0 = radius >= t0, con1 = radius >= t1;
+	if(!(con0 || con1)) return;
+	const M33 rot = rotationFromZAxis(planeN);
+	V3 pts[4];
+	V3 bmin = v3(FLT_MAX, FLT_MAX, FLT_MAX), bmax = neg(bmin);
+	for(int i = 0; i < 4; i++)
+	{
+		pts[i] = m33MulV(rot, pb.vert(face, i));
+		bmin = vmin(bmin, pts[i]);
+		bmax = vmax(bmax, pts[i]);
+	}
+	if(con0)
+	{
+		const V3 q = negScaleSub(normal, t0, p0);
+		if(containsXY(pts, 4, m33MulV(rot, q), bmin, bmax))
+		{
+			mc[num].a = mtTransformInv(aToB, p0); mc[num].b = q; mc[num].n = normal; mc[num].pen = t0; num++;
+		}
+	}
+	if(con1)
+	{
+		const V3 q = negScaleSub(normal, t1, p1);
+		if(containsXY(pts, 4, m33MulV(rot, q), bmin, bmax))
+		{
+			mc[num].a = mtTransformInv(aToB, p1); mc[num].b = q; mc[num].n = normal; mc[num].pen = t1; num++;
+		}
+	}
+}
+
+// generateEE (GuPCMContactGenSphereCapsule.cpp:312)
+void capsuleBoxEE(V3 p, V3 q, V3 normal, V3 a, V3 b, const MatTr& aToB, PC* mc, int& num, float inflatedRadius)
+{
+	const float expandedRatio = 0.005f;
+	const V3 ab = sub(b, a);
+	const V3 n = cross(ab, normal);
+	const float d = dotA(n, a), np = dotA(n, p), nq = dotA(n, q);
+	const float signP = np - d, signQ = nq - d;
+	if(signP * signQ > 0.0f) return;
+	const V3 pq = sub(q, p);
+	const float npq = dotA(n, pq);
+	if(npq == 0.0f) return;
+	const float segT = (d - np) / npq;
+	const V3 lpA = scaleAdd(pq, segT, p);
+	const V3 perN = cross(normal, pq);
+	const V3 ap = sub(lpA, a);
+	const float nom = dotA(perN, ap), den = dotA(perN, ab);
+	const float t = nom / den;
+	const float mx = 1.0f + expandedRatio, mn = 0.0f - expandedRatio;
+	if(t > mx || mn > t) return;
+	const V3 v = negScaleSub(ab, t, ap);
+	const float sd = dotA(v, normal);
+	if(inflatedRadius >= sd)
+	{
+		mc[num].a = mtTransformInv(aToB, lpA);
+		mc[num].b = sub(lpA, v);
+		mc[num].n = normal;
+		mc[num].pen = sd;
+		num++;
+	}
+}
+
+// generateCapsuleBoxFullContactManifold (GuPCMContactGenSphereCapsule.cpp:379)
+bool capsuleBoxFull(V3 p0, V3 p1, float r, V3 ext, const MatTr& aToB, PC* mc, int& num, float cDist, V3& normal, V3 closest,
+                    float margin, bool overlapTest, float tolLen)
+{
+	const PolyBox pb(ext);
+	const int orig = num;
+	int face;
+	if(overlapTest)
+	{
+		if(!satCapsuleBox(p0, p1, r, pb, ext, cDist, normal)) return false;
+		face = boxPolygonIndex(pb, neg(normal));
+	}
+	else
+	{
+		const float lo = tolLen * 1e-2f, hi = tolLen * 5e-2f;
+		const float tolerance = fmin_(hi, fmax_(lo, margin));
+		face = boxWitnessPolygonIndex(pb, neg(normal), closest, tolerance);
+	}
+	capsuleBoxFaceContacts(p0, p1, r, pb, face, aToB, mc, num, cDist, normal);
+	if(num - orig < 2)
+	{
+		const float inflated = r + cDist;
+		for(int s = 0, e = 3; s < 4; e = s++) capsuleBoxEE(p0, p1, normal, pb.vert(face, s), pb.vert(face, e), aToB, mc, num, inflated);
+	}
+	return true;
+}
+
+// pcmContactCapsuleBox with a fresh manifold (GuPCMContactCapsuleBox.cpp:73)
 bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Buffer& out)
 {
 	const Tr cur = trInvMul(tBox, tCap);
 	const MatTr aToB = matFromTr(cur);
-	// capsule segment in the box's local space
 	const V3 axis = mtRotate(aToB, scale(unitX(), hh));
 	const V3 p0 = add(aToB.p, axis), p1 = sub(aToB.p, axis);
+	const GjkConvex cap = makeCapsule(p0, p1, r);
+	const GjkConvex box = makeBox(ext);
+	// the reference seeds the search with the capsule centre minus the box's world position
+	const V3 initialDir = sub(aToB.p, tBox.p);
+	GjkOut g;
+	int status = gjkPenetration(cap, box, initialDir, cDist, g);
+	if(status == GJK_NON_INTERSECT) return false;
 	PC mc[MAXC];
 	int num = 0;
-	V3 normal;
-	if(!capsuleBoxManifold(p0, p1, r, ext, aToB, cDist, tolLen, mc, num, normal)) return false;
+	bool overlapTest = false;
+	if(status == GJK_DEGENERATE)
+		overlapTest = true;
+	else if(status == GJK_CONTACT)
+	{
+		mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+	}
+	else
+	{
+		status = epaPenetration(cap, box, g, tolLen, g);
+		if(status == EPA_CONTACT)
+		{
+			mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+		}
+		else
+			overlapTest = true;
+	}
+	// fullContactsGenerationCapsuleBox (GuPCMContactCapsuleBox.cpp:43)
+	V3 normal = g.normal;
+	const int orig = num;
+	if(!capsuleBoxFull(p0, p1, r, ext, aToB, mc, num, cDist, normal, g.closestB, box.margin, overlapTest, tolLen)) return false;
+	int first = 0;
+	if(orig != 0 && num != orig) { num--; first = 1; }
 	Manifold m;
-	addBatch2(m, mc, num);
+	addBatch2(m, mc + first, num);
 	const V3 wn = qRotate(tBox.q, normal);
 	outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
-	return m.num > 0;
+	return true;
 }
 
 int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Buffer& out)
@@ -1007,4 +1269,10 @@ OX int orc_np_run(const int* type0, const float* geom0, const int* type1, const 
 		}
 	}
 	return overflow;
+}
+
+// The restated approximate reciprocal, for checking against the reference.
+OX void orc_recip_fast(const float* in, float* out, uint32_t n)
+{
+	for(uint32_t i = 0; i < n; i++) out[i] = recipFast(in[i]);
 }

@@ -6,6 +6,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <float.h>
+#include <string.h>
 
 namespace orc
 {
@@ -44,6 +45,31 @@ static inline float fsel(bool c, float a, float b) { return c ? a : b; }
 static inline float fmin_(float a, float b) { return a < b ? a : b; }   // SSE minps: second operand on unordered
 static inline float fmax_(float a, float b) { return a > b ? a : b; }
 static inline float fclamp(float a, float lo, float hi) { return fmax_(fmin_(a, hi), lo); }
+// V3RecipFast of the reference's SSE2 build (RCPPS, PxVecMathSSE.h).  On the
+// x86 processors that run the reference here, RCPPS returns the reciprocal of
+// the midpoint of the input's 2^-11 mantissa cell rounded to 13 significant
+// bits (zero/denormal -> inf, inf -> 0, results below the normal range -> 0);
+// this statement matched RCPPS on all 2^32 inputs on that host and is pinned by
+// tests/golden/recip_fast.npz.
+static inline float recipFast(float x)
+{
+	uint32_t b;
+	memcpy(&b, &x, 4);
+	const uint32_t s = b & 0x80000000u, ex = (b >> 23) & 0xffu, i = (b >> 12) & 0x7ffu;
+	uint32_t r;
+	if(ex == 0xffu) r = (b & 0x7fffffu) ? (b | 0x400000u) : s;
+	else if(ex == 0u) r = s | 0x7f800000u;
+	else
+	{
+		const uint32_t D = 4097u + 2u * i;
+		const uint32_t k = ((1u << 26) + D) / (2u * D);     // round(2^25 / D), never a tie (D odd)
+		const int rex = 253 - int(ex);
+		r = rex <= 0 ? s : (s | (uint32_t(rex) << 23) | ((k - 4096u) << 11));
+	}
+	float f;
+	memcpy(&f, &r, 4);
+	return f;
+}
 static inline V3 unitX() { return v3(1, 0, 0); }
 static inline V3 zero3() { return v3(0, 0, 0); }
 static inline float getc(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }

@@ -51,12 +51,6 @@ __device__ __forceinline__ bool polyContainsXY(const V3* verts, int numVerts, V3
 	return intersections > 0;
 }
 
-struct GjkResult
-{
-	V3 closestA, closestB, normal;
-	float penDep;
-};
-
 enum { SPHERE = 0, PLANE = 1, CAPSULE = 2, BOX = 3 };
 const int MAXC = 16;    // largest pre-reduction count: box-box clipping (4 + 4 + 8)
 const int MAXOUT = 4;   // largest per-pair output after manifold reduction
@@ -600,6 +594,7 @@ static __device__ MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t
 static __device__ V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
 static __device__ V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
 static __device__ V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
+static __device__ V3 mtTransformInv(const MatTr& m, V3 v) { return m33TMulV(m.R, sub(v, m.p)); }
 static __device__ M33 transpose(const M33& m)
 {
 	M33 t;
@@ -619,11 +614,6 @@ static __device__ MatTr mtInvMul(const MatTr& a, const MatTr& b)
 	r.p = m33TMulV(a.R, sub(b.p, a.p));
 	return r;
 }
-// Box-box edge-edge fallback (GJK/EPA between the boxes, GuPCMContactBoxBox.cpp:917-957)
-// and the capsule-box full manifold (GuPCMContactCapsuleBox.cpp:73): not restated
-// yet, so these configurations report no contact; the tests identify and skip them.
-static __device__ bool gjkEpaBoxBox(V3, V3, const MatTr&, float, float, GjkResult&) { return false; }
-static __device__ bool capsuleBoxManifold(V3, V3, float, V3, const MatTr&, float, float, PC*, int&, V3&) { return false; }
 
 
 static __device__ void incidentPolygon(V3* pts, V3& faceN, V3 axis, const MatTr& t10, V3 ext)
@@ -679,7 +669,7 @@ static __device__ bool segAABB(V3 p0, V3 d, V3 mx, V3 mn, float& tmin, float& tm
 	float t1[3], t2[3];
 	for(int k = 0; k < 3; k++)
 	{
-		const float odd = 1.0f / dd[k];
+		const float odd = recipFast(dd[k]);   // V3RecipFast (GuPCMContactBoxBox.cpp:140)
 		t1[k] = par[k] ? 0.0f : (lo[k] - p[k]) * odd;
 		t2[k] = par[k] ? FLT_MAX : (hi[k] - p[k]) * odd;
 	}
@@ -923,6 +913,8 @@ static __device__ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr
 	return true;
 }
 
+#include "gjk_epa.cuh"
+
 static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen, Buffer& out)
 {
 	const Tr cur = trInvMul(tB, tA);
@@ -942,13 +934,17 @@ static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cD
 		for(int i = 0; i < m.num; i++) out.add(mtTransform(T1, m.pts[i].b), wn, m.pts[i].pen);
 		return true;
 	}
-	// Edge-edge configuration: the reference falls back to GJK / EPA between the boxes
+	// Edge-edge configuration: GJK / EPA between the core boxes
 	// (GuPCMContactBoxBox.cpp:917-957), producing a single point.
-	GjkResult g;
 	const MatTr aToB = matFromTr(cur);
-	if(!gjkEpaBoxBox(e0, e1, aToB, cDist, tolLen, g)) return false;
+	const GjkConvex ca = makeRelativeBox(e0, aToB);
+	const GjkConvex cb = makeBox(e1);
+	GjkOut g;
+	int status = gjkPenetration(ca, cb, aToB.p, cDist, g);
+	if(status == EPA_CONTACT) status = epaPenetration(ca, cb, g, tolLen, g);
+	if(status != GJK_CONTACT && status != EPA_CONTACT) return false;
 	PC c;
-	c.a = mtRotateInv(aToB, sub(g.closestA, aToB.p));
+	c.a = mtTransformInv(aToB, g.closestA);
 	c.b = g.closestB;
 	c.n = g.normal;
 	c.pen = g.penDep;
@@ -961,22 +957,50 @@ static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cD
 }
 
 // ----------------------------------------------------------------- capsule-box
+// pcmContactCapsuleBox with a fresh manifold (GuPCMContactCapsuleBox.cpp:73)
 static __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Buffer& out)
 {
 	const Tr cur = trInvMul(tBox, tCap);
 	const MatTr aToB = matFromTr(cur);
-	// capsule segment in the box's local space
 	const V3 axis = mtRotate(aToB, scale(unitX(), hh));
 	const V3 p0 = add(aToB.p, axis), p1 = sub(aToB.p, axis);
+	const GjkConvex cap = makeCapsule(p0, p1, r);
+	const GjkConvex box = makeBox(ext);
+	// the reference seeds the search with the capsule centre minus the box's world position
+	const V3 initialDir = sub(aToB.p, tBox.p);
+	GjkOut g;
+	int status = gjkPenetration(cap, box, initialDir, cDist, g);
+	if(status == GJK_NON_INTERSECT) return false;
 	PC mc[MAXC];
 	int num = 0;
-	V3 normal;
-	if(!capsuleBoxManifold(p0, p1, r, ext, aToB, cDist, tolLen, mc, num, normal)) return false;
+	bool overlapTest = false;
+	if(status == GJK_DEGENERATE)
+		overlapTest = true;
+	else if(status == GJK_CONTACT)
+	{
+		mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+	}
+	else
+	{
+		status = epaPenetration(cap, box, g, tolLen, g);
+		if(status == EPA_CONTACT)
+		{
+			mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+		}
+		else
+			overlapTest = true;
+	}
+	// fullContactsGenerationCapsuleBox (GuPCMContactCapsuleBox.cpp:43)
+	V3 normal = g.normal;
+	const int orig = num;
+	if(!capsuleBoxFull(p0, p1, r, ext, aToB, mc, num, cDist, normal, g.closestB, box.margin, overlapTest, tolLen)) return false;
+	int first = 0;
+	if(orig != 0 && num != orig) { num--; first = 1; }
 	Manifold m;
-	addBatch2(m, mc, num);
+	addBatch2(m, mc + first, num);
 	const V3 wn = qRotate(tBox.q, normal);
 	outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
-	return m.num > 0;
+	return true;
 }
 
 static __device__ int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Buffer& out)

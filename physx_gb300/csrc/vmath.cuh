@@ -45,6 +45,26 @@ __device__ __forceinline__ float fsel(bool c, float a, float b) { return c ? a :
 __device__ __forceinline__ float fmin_(float a, float b) { return a < b ? a : b; }   // SSE minps: second operand on unordered
 __device__ __forceinline__ float fmax_(float a, float b) { return a > b ? a : b; }
 __device__ __forceinline__ float fclamp(float a, float lo, float hi) { return fmax_(fmin_(a, hi), lo); }
+// V3RecipFast of the reference's SSE2 build (RCPPS): the reciprocal of the
+// midpoint of the input's 2^-11 mantissa cell rounded to 13 significant bits
+// (zero/denormal -> inf, inf -> 0, results below the normal range -> 0), which
+// is what RCPPS returns on the x86 hosts that run the reference.
+__device__ __forceinline__ float recipFast(float x)
+{
+	const uint32_t b = __float_as_uint(x);
+	const uint32_t s = b & 0x80000000u, ex = (b >> 23) & 0xffu, i = (b >> 12) & 0x7ffu;
+	uint32_t r;
+	if(ex == 0xffu) r = (b & 0x7fffffu) ? (b | 0x400000u) : s;
+	else if(ex == 0u) r = s | 0x7f800000u;
+	else
+	{
+		const uint32_t D = 4097u + 2u * i;
+		const uint32_t k = ((1u << 26) + D) / (2u * D);
+		const int rex = 253 - int(ex);
+		r = rex <= 0 ? s : (s | (uint32_t(rex) << 23) | ((k - 4096u) << 11));
+	}
+	return __uint_as_float(r);
+}
 __device__ __forceinline__ V3 unitX() { return v3(1, 0, 0); }
 __device__ __forceinline__ V3 zero3() { return v3(0, 0, 0); }
 __device__ __forceinline__ float getc(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }

@@ -27,7 +27,7 @@ def param_vector(p):
 def _setup():
     L = lib()
     if not getattr(L, "_world_ready", False):
-        L.gbpx_world_create.argtypes = [ctypes.c_uint32] + [ctypes.c_void_p] * 12 + [ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+        L.gbpx_world_create.argtypes = [ctypes.c_uint32] + [ctypes.c_void_p] * 11 + [ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
         L.gbpx_world_release.argtypes = [ctypes.c_void_p]
         L.gbpx_world_step.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int]
         L.gbpx_world_synchronize.argtypes = [ctypes.c_void_p]
@@ -51,6 +51,8 @@ def _setup():
 class World:
     """`scenes` dict: body_count (S,), static_count (S,), rigid (PxRigidBodyData records),
     types (N,), geoms (N,4), friction (N,), static_poses (M,7), static_types (M,), static_geoms (M,4)."""
+
+    _h = None
 
     def __init__(self, scenes, pairs_per_body=8, **params):
         L = _setup()

@@ -91,6 +91,8 @@ def make_tgs():
 SCENE_CASES = [
     # name, seed, scenes, bodies per scene, shapes: one full frame (bounds, ABP, contacts, TGS) per scene
     ("scene_spheres_capsules", 41, 4, 48, (0, 2)),
+    ("scene_mixed", 42, 4, 40, (0, 2, 3)),
+    ("scene_boxes", 43, 4, 32, (3,)),
 ]
 
 
@@ -106,10 +108,25 @@ def make_scene():
         print("wrote", name)
 
 
+def make_recip():
+    """The reference's approximate reciprocal (V3RecipFast): one input per 2^-11
+    mantissa cell of [1, 2), random magnitudes of both signs, and special values."""
+    rng = np.random.default_rng(61)
+    cells = (np.arange(2048, dtype=np.uint32) << 12) | np.uint32(0x3F800000)
+    rnd = rng.uniform(-40.0, 40.0, 20000)
+    x = np.concatenate([cells.view(np.float32), (np.sign(rng.standard_normal(20000)) * np.exp2(rnd)).astype(np.float32),
+                        np.array([0.0, -0.0, np.inf, -np.inf, 1e-40, -1e-40, 3e38, -3e38, 1e-6, 1.0], np.float32)])
+    x = np.ascontiguousarray(x, np.float32)
+    ref = np.zeros_like(x)
+    reference().pxref_recip_fast(x.ctypes.data_as(ctypes.c_void_p), ref.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(len(x)))
+    np.savez_compressed(os.path.join(HERE, "recip_fast.npz"), x=x, ref=ref)
+    print("wrote recip_fast")
+
+
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np", "tgs", "scene"]
+    which = sys.argv[1:] or ["bp", "np", "tgs", "scene", "recip"]
     if "bp" in which:
         make_bp()
     if "np" in which:
@@ -118,3 +135,5 @@ if __name__ == "__main__":
         make_tgs()
     if "scene" in which:
         make_scene()
+    if "recip" in which:
+        make_recip()

@@ -33,3 +33,31 @@ def test_no_visible_internal_symbols(gbpx_built):
     out = os.popen("nm -D --defined-only %s" % gbpx_built).read()
     exported = [l.split()[-1] for l in out.splitlines() if " T " in l]
     assert exported and all(s.startswith("gbpx_") for s in exported), [s for s in exported if not s.startswith("gbpx_")][:10]
+
+
+def declared_arity():
+    """Parameter count of every gbpx_* function declared in include/*.h."""
+    arity = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for name, args in re.findall(r"\b(gbpx_\w+)\s*\(([^)]*)\)\s*;", text):
+            args = args.strip()
+            arity[name] = 0 if args in ("", "void") else args.count(",") + 1
+    return arity
+
+
+def test_python_bindings_match_header_arity(gbpx_built):
+    """Every ctypes prototype the Python mirror installs has the header's parameter count."""
+    from physx_gb300 import broadphase, contacts, lib, solver, world
+    for mod in (broadphase, contacts, solver, world):
+        mod._setup()
+    L = lib()
+    arity = declared_arity()
+    checked = 0
+    for name, n in arity.items():
+        fn = getattr(L, name)
+        if getattr(fn, "argtypes", None) is not None:
+            assert len(fn.argtypes) == n, (name, len(fn.argtypes), n)
+            checked += 1
+    assert checked >= 20, checked

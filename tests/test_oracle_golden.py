@@ -72,9 +72,37 @@ def test_oracle_contacts_match_reference_golden(path):
     oc, oo = run_contacts("orc", pairs, contact_distance=cd, tolerance_length=tl, max_per_pair=8)
     rep = compare(pairs, rc, unpack(rc, rpacked), oc, [oo[i, :oc[i]] for i in range(len(oc))])
     assert_report(rep)
-    # the analytic pairs are reproduced bit for bit
-    for k in ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule"):
+    # every pair kind, including the GJK/EPA paths, is reproduced bit for bit
+    for k in ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule",
+              "capsule-box", "box-box"):
         assert rep[k]["maxdiff"] == 0.0, (k, rep[k])
+
+
+def test_oracle_recip_fast_matches_reference_golden():
+    """The approximate reciprocal of the box-box edge clipping (V3RecipFast) against
+    the reference's own outputs: one input per 2^-11 mantissa cell plus random and
+    special values."""
+    import ctypes
+    from oracle_libs import oracle
+    z = np.load(os.path.join(GOLDEN, "recip_fast.npz"))
+    x = np.ascontiguousarray(z["x"], np.float32)
+    out = np.zeros_like(x)
+    oracle().orc_recip_fast(x.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(len(x)))
+    assert np.array_equal(out.view(np.uint32), z["ref"].view(np.uint32))
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed,types", [(51, None), (52, [(2, 3), (3, 2), (3, 3)])])
+def test_oracle_contacts_match_reference_live(seed, types):
+    from contact_compare import assert_report, compare
+    from oracle_libs import run_contacts
+    from scenarios import np_pairs
+    pairs = np_pairs(seed, 6000, types=types)
+    rc, ro = run_contacts("pxref", pairs, max_per_pair=8)
+    oc, oo = run_contacts("orc", pairs, max_per_pair=8)
+    rep = compare(pairs, rc, [ro[i, :rc[i]] for i in range(len(rc))], oc, [oo[i, :oc[i]] for i in range(len(oc))])
+    assert_report(rep)
+    assert all(r["maxdiff"] == 0.0 for r in rep.values()), rep
 
 
 TGS_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "tgs_*.npz")))
