@@ -67,8 +67,9 @@ def _cpu_worker(payload):
 
 def split_scenes(scenes, idx):
     import numpy as np
-    counts = scenes["body_count"]
-    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    counts = scenes["body_count"].astype(np.int64)
+    starts = np.zeros(len(counts), np.int64)
+    starts[1:] = np.cumsum(counts)[:-1]
     sel = np.concatenate([np.arange(starts[i], starts[i] + counts[i]) for i in idx]) if len(idx) else np.zeros(0, np.int64)
     return dict(body_count=counts[idx], static_count=scenes["static_count"][idx], rigid=scenes["rigid"][sel], types=scenes["types"][sel],
                 geoms=scenes["geoms"][sel], friction=scenes["friction"][sel], static_poses=scenes["static_poses"][idx],

@@ -14,6 +14,7 @@
 #ifndef GBPX_H
 #define GBPX_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus

@@ -68,7 +68,9 @@ def test_world_batched_workload_shape_and_determinism(cuda_device):
 
 
 def test_world_reports_pair_overflow(cuda_device):
-    scenes = pile_scenes(73, 2, 60, shapes=(0,))
+    # 60 spheres packed into a ~1 m region overlap pairwise (~1770 pairs), far above
+    # the 128 slots that one pair per body gives the scene
+    scenes = pile_scenes(73, 2, 60, shapes=(0,), spread=1.0)
     w = _world(scenes, pairs_per_body=1)
     w.step(1)
     st = w.status()
