@@ -87,7 +87,33 @@ struct WorldDev
 	uint32_t* staticProgress;
 	uint32_t* partEnds;        // MAX_PARTITIONS per scene
 	uint32_t* status;
+	uint32_t* typeCount;       // pairs queued per pair kind (NB_KINDS)
+	uint32_t* typeQueue;       // NB_KINDS queues of pair slots, queueCap entries each
+	uint32_t queueCap;
+	const uint32_t* slotScene; // owning scene of every pair slot
 };
+
+// Pair kinds: shape types ordered (t0 <= t1), code t0 * 4 + t1.  Dynamic
+// bodies are spheres, capsules or boxes; statics may also be planes, so nine
+// kinds occur (plane-plane never does: statics are not paired together).
+constexpr uint32_t NB_KINDS = 9;
+__device__ __forceinline__ uint32_t kindOf(int t0, int t1)
+{
+	const int a = t0 < t1 ? t0 : t1, b = t0 < t1 ? t1 : t0;
+	switch(a * 4 + b)
+	{
+	case 0: return 0;    // sphere-sphere
+	case 1: return 1;    // sphere-plane
+	case 2: return 2;    // sphere-capsule
+	case 3: return 3;    // sphere-box
+	case 6: return 4;    // plane-capsule
+	case 7: return 5;    // plane-box
+	case 10: return 6;   // capsule-capsule
+	case 11: return 7;   // capsule-box
+	case 15: return 8;   // box-box
+	default: return NB_KINDS;
+	}
+}
 
 __device__ __forceinline__ Tr loadStaticPose(const float* s)
 {
@@ -230,6 +256,28 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 	if(count > 1) warpBitonicSort(pairs, pw);
 	if(lane == 0) w.pairCount[sid] = count;
 	__syncwarp();
+	// queue every pair slot under its pair kind (one atomic per kind per 32 pairs)
+	for(uint32_t base = 0; base < count; base += 32)
+	{
+		const uint32_t k = base + lane;
+		const bool valid = k < count;
+		uint32_t kind = NB_KINDS + 1;
+		if(valid)
+		{
+			const uint32_t key = pairs[k];
+			const uint32_t i = key >> 16, j = key & 0xffffu;
+			const int ti = w.types[sc.bodyStart + i];
+			const int tj = j < n ? w.types[sc.bodyStart + j] : w.staticTypes[sc.staticStart + (j - n)];
+			kind = kindOf(ti, tj);
+			if(kind == NB_KINDS) w.contactCount[sc.pairStart + k] = 0;
+		}
+		const uint32_t peers = __match_any_sync(0xffffffffu, kind);
+		const uint32_t leader = __ffs(peers) - 1;
+		uint32_t qbase = 0;
+		if(kind < NB_KINDS && lane == leader) qbase = atomicAdd(&w.typeCount[kind], uint32_t(__popc(peers)));
+		qbase = __shfl_sync(0xffffffffu, qbase, leader);
+		if(kind < NB_KINDS) w.typeQueue[size_t(kind) * w.queueCap + qbase + __popc(peers & laneMaskLt())] = sc.pairStart + k;
+	}
 }
 
 __device__ __forceinline__ void pairShape(const WorldDev& w, const SceneDesc& sc, uint32_t id, int& type, float g[4], Tr& pose)
@@ -254,13 +302,35 @@ __device__ __forceinline__ void pairShape(const WorldDev& w, const SceneDesc& sc
 	}
 }
 
-__device__ __forceinline__ void sceneNarrowphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+// Contacts of one pair kind (shape types TA <= TB), PxGenerateContacts semantics.
+template <int TA, int TB>
+__device__ __forceinline__ void generateKind(const float* ga, const float* gb, const Tr& pa, const Tr& pb, const StepParams& sp, np::Buffer& out)
 {
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t count = w.pairCount[sid];
-	for(uint32_t k = lane; k < count; k += 32)
+	const float cd = sp.contactDistance, tl = sp.toleranceLength;
+	if constexpr(TA == 0 && TB == 0) np::sphereSphere(ga[0], gb[0], pa, pb, cd, out);
+	else if constexpr(TA == 0 && TB == 1) np::spherePlane(ga[0], pa, pb, cd, out);
+	else if constexpr(TA == 0 && TB == 2) np::sphereCapsule(ga[0], gb[0], gb[1], pa, pb, cd, out);
+	else if constexpr(TA == 0 && TB == 3) np::sphereBox(ga[0], v3(gb[0], gb[1], gb[2]), pa, pb, cd, out);
+	else if constexpr(TA == 1 && TB == 2) np::planeCapsule(gb[0], gb[1], pa, pb, cd, out);
+	else if constexpr(TA == 1 && TB == 3) np::planeBox(v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
+	else if constexpr(TA == 2 && TB == 2) np::capsuleCapsule(ga[0], ga[1], gb[0], gb[1], pa, pb, cd, out);
+	else if constexpr(TA == 2 && TB == 3) np::capsuleBox(ga[0], ga[1], v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
+	else if constexpr(TA == 3 && TB == 3) np::boxBox(v3(ga[0], ga[1], ga[2]), v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
+}
+
+// Narrowphase of one pair kind over every scene: a thread per queued pair slot,
+// so each warp runs one contact generator on uniform work.
+template <int TA, int TB>
+__global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams sp)
+{
+	constexpr uint32_t KIND = TA == 0 ? uint32_t(TB) : (TA == 1 ? uint32_t(TB + 2) : (TA == 2 ? uint32_t(TB + 4) : 8u));
+	const uint32_t count = w.typeCount[KIND];
+	const uint32_t* queue = w.typeQueue + size_t(KIND) * w.queueCap;
+	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
 	{
-		const uint32_t key = w.pairs[sc.pairStart + k];
+		const uint32_t slot = queue[q];
+		const SceneDesc sc = w.scenes[w.slotScene[slot]];
+		const uint32_t key = w.pairs[slot];
 		const uint32_t i = key >> 16, j = key & 0xffffu;
 		int ta, tb;
 		float ga[4], gb[4];
@@ -268,15 +338,10 @@ __device__ __forceinline__ void sceneNarrowphase(const WorldDev& w, const SceneD
 		pairShape(w, sc, i, ta, ga, pa);
 		pairShape(w, sc, j, tb, gb, pb);
 		const bool swap = ta > tb;
-		if(swap)
-		{
-			const int t = ta; ta = tb; tb = t;
-			for(int c = 0; c < 4; c++) { const float x = ga[c]; ga[c] = gb[c]; gb[c] = x; }
-			const Tr t2 = pa; pa = pb; pb = t2;
-		}
 		np::Buffer buf;
-		np::generate(ta, ga, tb, gb, pa, pb, sp.contactDistance, sp.toleranceLength, buf);
-		float4* o = w.contacts + size_t(sc.pairStart + k) * 8;
+		if(swap) generateKind<TA, TB>(gb, ga, pb, pa, sp, buf);
+		else generateKind<TA, TB>(ga, gb, pa, pb, sp, buf);
+		float4* o = w.contacts + size_t(slot) * 8;
 		for(int c = 0; c < buf.count; c++)
 		{
 			V3 nn = buf.c[c].n;
@@ -284,9 +349,8 @@ __device__ __forceinline__ void sceneNarrowphase(const WorldDev& w, const SceneD
 			o[2 * c] = make_float4(nn.x, nn.y, nn.z, buf.c[c].sep);
 			o[2 * c + 1] = make_float4(buf.c[c].p.x, buf.c[c].p.y, buf.c[c].p.z, 0.0f);
 		}
-		w.contactCount[sc.pairStart + k] = uint32_t(buf.count);
+		w.contactCount[slot] = uint32_t(buf.count);
 	}
-	__syncwarp();
 }
 
 // PxBatchConstraintsTGS partition rule for one scene, run by one lane
@@ -509,24 +573,39 @@ __device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& s
 	__syncwarp();
 }
 
-// One step of every scene: a persistent grid of warps pulls scenes from the
-// size-sorted work table.
-__global__ void __launch_bounds__(128) stepKernel(WorldDev w, StepParams sp)
+// Stage kernels of one step.  Broadphase and solve run a persistent grid of
+// warps that pull scenes from the size-sorted work table (largest first);
+// the narrowphase runs one kernel per pair kind over all scenes' pairs.
+__global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams sp)
 {
 	const uint32_t lane = threadIdx.x & 31;
 	for(;;)
 	{
 		uint32_t item = 0;
-		if(lane == 0) item = atomicAdd(w.workCounter, 1u);
+		if(lane == 0) item = atomicAdd(&w.workCounter[0], 1u);
 		item = __shfl_sync(0xffffffffu, item, 0);
 		if(item >= w.nbScenes) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
 		sceneBroadphase(w, sc, sid, sp);
-		sceneNarrowphase(w, sc, sid, sp);
+	}
+}
+
+__global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	for(;;)
+	{
+		uint32_t item = 0;
+		if(lane == 0) item = atomicAdd(&w.workCounter[1], 1u);
+		item = __shfl_sync(0xffffffffu, item, 0);
+		if(item >= w.nbScenes) break;
+		const uint32_t sid = w.workOrder[item];
+		const SceneDesc sc = w.scenes[sid];
 		sceneSolve(w, sc, sid, sp);
 	}
 }
+
 // Totals over all scenes after a step: pairs, pairs with contacts, contacts.
 __global__ void statsKernel(const SceneDesc* __restrict__ scenes, uint32_t nbScenes, const uint32_t* __restrict__ pairCount,
                             const uint32_t* __restrict__ contactCount, unsigned long long* __restrict__ out)
@@ -565,8 +644,9 @@ struct World
 	world::StepParams params;
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
-	uint32_t gridBlocks = 0;
+	uint32_t gridBlocks = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
 	DevBuf<world::SceneDesc> scenes;
+	DevBuf<uint32_t> typeQueue, slotScene;
 	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
 	    staticProgress, partEnds, status;
 	DevBuf<tgs::RigidBody> bodies;
@@ -584,6 +664,8 @@ struct World
 	size_t deviceBytes = 0;
 
 	static uint32_t pow2(uint32_t x) { uint32_t p = 1; while(p < x) p <<= 1; return p; }
+	// work counters of the broadphase and solve kernels, then the per-kind pair counts
+	static constexpr uint32_t COUNTERS = 8 + world::NB_KINDS;
 
 	world::WorldDev dev()
 	{
@@ -595,6 +677,7 @@ struct World
 		w.contactCount = contactCount.ptr; w.ordered = ordered.ptr; w.consList = consList.ptr; w.tag = tag.ptr; w.recs = recs.ptr;
 		w.vel = vel.ptr; w.tx = tx.ptr; w.data = data.ptr; w.pose = pose.ptr; w.progress = progress.ptr; w.maxNormal = maxNormal.ptr;
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
+		w.typeCount = workCounter.ptr + 8; w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
 		return w;
 	}
 
@@ -622,7 +705,7 @@ struct World
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
 		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(1) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
+		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
 		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
 		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
 		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
@@ -631,11 +714,15 @@ struct World
 		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(3) ||
 		   identity.reserve(S))
 			return GBPX_ERR_NOMEM;
-		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
+		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
 		              size_t(nbSolver) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + size_t(key) * 8;
 		cudaStream_t s = stream;
 		GBPX_CUDA_TRY(cudaMemcpyAsync(scenes.ptr, hScenes.data(), S * sizeof(world::SceneDesc), cudaMemcpyHostToDevice, s));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(workOrder.ptr, order.data(), S * 4, cudaMemcpyHostToDevice, s));
+		std::vector<uint32_t> owner(pair);
+		for(uint32_t sc = 0; sc < S; sc++)
+			std::fill(owner.begin() + hScenes[sc].pairStart, owner.begin() + hScenes[sc].pairStart + hScenes[sc].pairCap, sc);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(slotScene.ptr, owner.data(), size_t(pair) * 4, cudaMemcpyHostToDevice, s));
 		std::vector<uint32_t> ident(S);
 		std::iota(ident.begin(), ident.end(), 0u);
 		GBPX_CUDA_TRY(cudaMemcpyAsync(identity.ptr, ident.data(), S * 4, cudaMemcpyHostToDevice, s));
@@ -650,19 +737,53 @@ struct World
 			GBPX_CUDA_TRY(cudaMemcpyAsync(staticGeoms.ptr, staticGeomsIn, size_t(st) * 16, cudaMemcpyHostToDevice, s));
 		}
 		GBPX_CUDA_TRY(cudaMemsetAsync(status.ptr, 0, S * 4, s));
-		int dev = 0, sms = 0, perSm = 0;
+		int dev = 0, sms = 0;
 		GBPX_CUDA_TRY(cudaGetDevice(&dev));
 		GBPX_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		GBPX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, world::stepKernel, 128, 0));
-		gridBlocks = uint32_t(std::max(1, sms * std::max(1, perSm)));
+		GBPX_CUDA_TRY(gridFor(world::broadphaseKernel, sms, gridBlocks));
+		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve));
+		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 		return GBPX_OK;
 	}
 
-	int launchStep()
+	typedef void (*StageKernel)(world::WorldDev, world::StepParams);
+	static const StageKernel* npKernels()
 	{
-		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, 4, stream));
-		world::stepKernel<<<gridBlocks, 128, 0, stream>>>(dev(), params);
+		static const StageKernel k[world::NB_KINDS] = {
+		    world::narrowphaseKernel<0, 0>, world::narrowphaseKernel<0, 1>, world::narrowphaseKernel<0, 2>,
+		    world::narrowphaseKernel<0, 3>, world::narrowphaseKernel<1, 2>, world::narrowphaseKernel<1, 3>,
+		    world::narrowphaseKernel<2, 2>, world::narrowphaseKernel<2, 3>, world::narrowphaseKernel<3, 3>};
+		return k;
+	}
+	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
+	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid)
+	{
+		int perSm = 0;
+		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, 128, 0);
+		grid = uint32_t(sms * (perSm > 0 ? perSm : 1));
+		return e;
+	}
+
+	// One step: clear the counters, broadphase, one narrowphase kernel per
+	// pair kind, solve.  `plainScene` < nbScenes steps that scene alone with
+	// single-warp scene stages (the unbatched comparison point).
+	int launchStep(uint32_t plainScene = ~0u)
+	{
+		world::WorldDev w = dev();
+		uint32_t gBp = gridBlocks, gSolve = gridSolve, threads = 128;
+		if(plainScene < nbScenes)
+		{
+			w.workOrder = identity.ptr + plainScene;
+			w.nbScenes = 1;
+			gBp = gSolve = 1;
+			threads = 32;
+		}
+		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
+		world::broadphaseKernel<<<gBp, threads, 0, stream>>>(w, params);
+		for(uint32_t k = 0; k < world::NB_KINDS; k++)
+			npKernels()[k]<<<plainScene < nbScenes ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
+		world::solveKernel<<<gSolve, threads, 0, stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
@@ -705,19 +826,15 @@ struct World
 		return GBPX_OK;
 	}
 
-	// One scene per launch: no batching across scenes, no graph, no
+	// One scene per launch sequence: no batching across scenes, no graph, no
 	// persistence (the comparison point of the batched step).
 	int stepPlain(uint32_t first, uint32_t count)
 	{
 		for(uint32_t s = first; s < first + count && s < nbScenes; s++)
 		{
-			world::WorldDev w = dev();
-			w.workOrder = identity.ptr + s;
-			w.nbScenes = 1;
-			GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, 4, stream));
-			world::stepKernel<<<1, 32, 0, stream>>>(w, params);
+			const int rc = launchStep(s);
+			if(rc) return rc;
 		}
-		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
 
@@ -726,7 +843,7 @@ struct World
 		if(stream) cudaStreamSynchronize(stream);
 		if(graphExec) cudaGraphExecDestroy(graphExec);
 		graphExec = nullptr;
-		scenes.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
+		scenes.release(); typeQueue.release(); slotScene.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
