@@ -283,7 +283,7 @@ def main():
                 e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=bodies * 96, d2h_bytes_per_step=bodies * 96),
                 plain_gpu=dict(value=plain_value, unit=UNIT, sample="%d scenes (%d bodies), one scene per launch" % (len(idx), plain_bodies),
                                batched_over_plain=value / plain_value),
-                roofline=roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps,
+                roofline=roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps * info["kernels_per_step"],
                 contacts_per_s=st["contacts"] * a.steps / (ms / 1000.0), pairs_per_s=st["pairs"] * a.steps / (ms / 1000.0),
                 status_nonzero_scenes=int((status != 0).sum()))
     print(json.dumps(line))

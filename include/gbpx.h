@@ -122,7 +122,9 @@ int gbpx_world_synchronize(void* world);
 int gbpx_world_get_bodies(void* world, void* outRigidBodies);
 int gbpx_world_set_bodies(void* world, const void* rigidBodies);
 int gbpx_world_status(void* world, uint32_t* outStatus);
-int gbpx_world_info(void* world, uint64_t* out6);
+/* out8: scenes, dynamic bodies, statics, pair slots, broadphase grid blocks,
+ * device bytes, kernels launched per step, 0 */
+int gbpx_world_info(void* world, uint64_t* out8);
 int gbpx_world_scene_pairs(void* world, uint32_t scene, uint32_t* outKeys, uint32_t* outContactCounts, uint32_t capacity,
                            uint32_t* outCount);
 int gbpx_world_time_steps(void* world, uint32_t nbSteps, int useGraph, float* outMs);

@@ -91,6 +91,9 @@ struct WorldDev
 	uint32_t* typeQueue;       // NB_KINDS queues of pair slots, queueCap entries each
 	uint32_t queueCap;
 	const uint32_t* slotScene; // owning scene of every pair slot
+	uint32_t* nbConstraints;   // per scene: constraints (pairs with contacts) of this step
+	uint32_t* nbPartitions;    // per scene: partitions, 0 when batching overflowed
+	uint32_t* prepQueue;       // constraint slots of all scenes, for the row-preparation kernel
 };
 
 // Pair kinds: shape types ordered (t0 <= t1), code t0 * 4 + t1.  Dynamic
@@ -183,12 +186,64 @@ __device__ __forceinline__ void warpBitonicSort(K* keys, uint32_t n)
 	}
 }
 
-__device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+// Per-warp shared-memory workspace of the broadphase: scenes of up to
+// BP_SMEM_BODIES bodies sort and sweep entirely on chip; larger scenes use the
+// same code on their global scratch arrays.
+constexpr uint32_t BP_SMEM_BODIES = 512;
+constexpr uint32_t STAGE_WARPS = 4;   // warps (scenes in flight) per block of the scene kernels
+struct BpSmem
+{
+	unsigned long long keys[BP_SMEM_BODIES];   // (encoded min X << 32) | body
+	uint32_t maxX[BP_SMEM_BODIES];             // encoded max X
+	float minY[BP_SMEM_BODIES], minZ[BP_SMEM_BODIES], maxY[BP_SMEM_BODIES], maxZ[BP_SMEM_BODIES];
+	uint32_t cnt[BP_SMEM_BODIES];              // pairs per lower body id, then bucket offsets
+	uint32_t found;
+};
+
+// Exclusive prefix sum of v[0..n) by one warp (each lane scans a run of entries).
+__device__ __forceinline__ void warpExclusiveScan(uint32_t* v, uint32_t n)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t per = (n + 31) / 32;
+	const uint32_t b0 = min(lane * per, n), b1 = min(b0 + per, n);
+	uint32_t sum = 0;
+	for(uint32_t k = b0; k < b1; k++) sum += v[k];
+	uint32_t incl = sum;
+	for(int o = 1; o < 32; o <<= 1)
+	{
+		const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+		if(lane >= uint32_t(o)) incl += t;
+	}
+	uint32_t run = incl - sum;
+	for(uint32_t k = b0; k < b1; k++)
+	{
+		const uint32_t c = v[k];
+		v[k] = run;
+		run += c;
+	}
+	__syncwarp();
+}
+
+// Bounds, ABP-equivalent overlap search and the pair list of one scene, sorted
+// by (id0, id1) with statics numbered after the dynamic bodies.
+// The sweep follows ABP's semantics: boxes sorted by encoded min X, X
+// overlap on encoded keys, Y/Z as closed float intervals.  Found pairs are
+// counted per lower id, scattered into their buckets and each bucket sorted by
+// the upper id, which yields the same order as sorting the whole list.
+__device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, BpSmem& sm)
 {
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies, m = sc.nbStatics;
-	float* aabb = w.aabb + 6 * size_t(sc.bodyStart);
-	unsigned long long* keys = w.keys + sc.keyStart;
+	const bool onChip = sc.keyCap <= BP_SMEM_BODIES;
+	unsigned long long* keys = onChip ? sm.keys : w.keys + sc.keyStart;
+	float* ga = w.aabb + 6 * size_t(sc.bodyStart);
+	uint32_t* maxX = onChip ? sm.maxX : reinterpret_cast<uint32_t*>(ga);
+	float* minY = onChip ? sm.minY : ga + n;
+	float* minZ = onChip ? sm.minZ : ga + 2 * size_t(n);
+	float* maxY = onChip ? sm.maxY : ga + 3 * size_t(n);
+	float* maxZ = onChip ? sm.maxZ : ga + 4 * size_t(n);
+	uint32_t* cnt = onChip ? sm.cnt : w.progress + sc.solverStart;
+	const float mg = sp.boundsMargin;
 	for(uint32_t i = lane; i < sc.keyCap; i += 32)
 	{
 		if(i < n)
@@ -199,61 +254,78 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 			pose.p = v3(rb.p[0], rb.p[1], rb.p[2]);
 			V3 mn, mx;
 			shapeBounds(w.types[sc.bodyStart + i], w.geoms[sc.bodyStart + i], pose, mn, mx);
-			const float mg = sp.boundsMargin;
-			float* a = aabb + 6 * size_t(i);
-			a[0] = mn.x - mg; a[1] = mn.y - mg; a[2] = mn.z - mg;
-			a[3] = mx.x + mg; a[4] = mx.y + mg; a[5] = mx.z + mg;
-			keys[i] = (static_cast<unsigned long long>(encodeFloatBits(__float_as_uint(a[0]))) << 32) | i;
+			const float x0 = mn.x - mg;
+			maxX[i] = encodeFloatBits(__float_as_uint(mx.x + mg));
+			minY[i] = mn.y - mg; minZ[i] = mn.z - mg;
+			maxY[i] = mx.y + mg; maxZ[i] = mx.z + mg;
+			cnt[i] = 0;
+			keys[i] = (static_cast<unsigned long long>(encodeFloatBits(__float_as_uint(x0))) << 32) | i;
 		}
 		else
 			keys[i] = ~0ull;
 	}
-	if(lane == 0) w.pairCount[sid] = 0;
+	if(lane == 0) sm.found = 0;
 	__syncwarp();
 	warpBitonicSort(keys, sc.keyCap);
-	uint32_t* pairs = w.pairs + sc.pairStart;
+	uint32_t* scratch = w.ordered + sc.pairStart;   // unsorted pairs (the slot array is free until the solve)
 	uint32_t local = 0;   // lane-private overflow flag
 	for(uint32_t p = lane; p < n; p += 32)
 	{
-		const uint32_t i = uint32_t(keys[p]);
-		const float* a = aabb + 6 * size_t(i);
-		const uint32_t amaxx = encodeFloatBits(__float_as_uint(a[3]));
+		const unsigned long long kp = keys[p];
+		const uint32_t i = uint32_t(kp);
+		const uint32_t amaxx = maxX[i];
+		const float a1 = minY[i], a2 = minZ[i], a4 = maxY[i], a5 = maxZ[i];
 		for(uint32_t q = p + 1; q < n; q++)
 		{
 			const unsigned long long kq = keys[q];
 			if(uint32_t(kq >> 32) > amaxx) break;
 			const uint32_t j = uint32_t(kq);
-			const float* b = aabb + 6 * size_t(j);
-			if(!(b[4] < a[1] || a[4] < b[1] || b[5] < a[2] || a[5] < b[2]))
+			if(!(maxY[j] < a1 || a4 < minY[j] || maxZ[j] < a2 || a5 < minZ[j]))
 			{
-				const uint32_t slot = atomicAdd(&w.pairCount[sid], 1u);
 				const uint32_t lo = i < j ? i : j, hi = i < j ? j : i;
-				if(slot < sc.pairCap) pairs[slot] = (lo << 16) | hi; else local = 1;
+				const uint32_t slot = atomicAdd(&sm.found, 1u);
+				if(slot < sc.pairCap) { scratch[slot] = (lo << 16) | hi; atomicAdd(&cnt[lo], 1u); } else local = 1;
 			}
 		}
-		for(uint32_t s = 0; s < m; s++)
+		if(m)
 		{
-			V3 mn, mx;
-			const Tr sp7 = loadStaticPose(w.staticPose + 7 * size_t(sc.staticStart + s));
-			shapeBounds(w.staticTypes[sc.staticStart + s], w.staticGeoms[sc.staticStart + s], sp7, mn, mx);
-			const float mg = sp.boundsMargin;
-			const float b[6] = {mn.x - mg, mn.y - mg, mn.z - mg, mx.x + mg, mx.y + mg, mx.z + mg};
-			if(overlapBoxes(a, b))
+			const uint32_t aminx = uint32_t(kp >> 32);
+			for(uint32_t s = 0; s < m; s++)
 			{
-				const uint32_t slot = atomicAdd(&w.pairCount[sid], 1u);
-				if(slot < sc.pairCap) pairs[slot] = (i << 16) | (n + s); else local = 1;
+				V3 mn, mx;
+				const Tr sp7 = loadStaticPose(w.staticPose + 7 * size_t(sc.staticStart + s));
+				shapeBounds(w.staticTypes[sc.staticStart + s], w.staticGeoms[sc.staticStart + s], sp7, mn, mx);
+				const uint32_t bminx = encodeFloatBits(__float_as_uint(mn.x - mg)), bmaxx = encodeFloatBits(__float_as_uint(mx.x + mg));
+				if(bminx > amaxx || aminx > bmaxx) continue;
+				if((mx.y + mg) < a1 || a4 < (mn.y - mg) || (mx.z + mg) < a2 || a5 < (mn.z - mg)) continue;
+				const uint32_t slot = atomicAdd(&sm.found, 1u);
+				if(slot < sc.pairCap) { scratch[slot] = (i << 16) | (n + s); atomicAdd(&cnt[i], 1u); } else local = 1;
 			}
 		}
 	}
 	__syncwarp();
 	if(__any_sync(0xffffffffu, local) && lane == 0) atomicOr(&w.status[sid], ST_PAIR_OVERFLOW);
-	uint32_t count = atomicAdd(&w.pairCount[sid], 0u);
-	count = count < sc.pairCap ? count : sc.pairCap;
-	uint32_t pw = 1;
-	while(pw < count) pw <<= 1;
-	for(uint32_t k = count + lane; k < pw; k += 32) pairs[k] = 0xffffffffu;
+	const uint32_t count = min(sm.found, sc.pairCap);
+	// bucket by lower id, then sort each bucket by upper id
+	warpExclusiveScan(cnt, n);
+	uint32_t* pairs = w.pairs + sc.pairStart;
+	for(uint32_t t = lane; t < count; t += 32)
+	{
+		const uint32_t key = scratch[t];
+		pairs[atomicAdd(&cnt[key >> 16], 1u)] = key;
+	}
 	__syncwarp();
-	if(count > 1) warpBitonicSort(pairs, pw);
+	for(uint32_t lo = lane; lo < n; lo += 32)
+	{
+		const uint32_t b0 = lo ? cnt[lo - 1] : 0, b1 = cnt[lo];
+		for(uint32_t x = b0 + 1; x < b1; x++)
+		{
+			const uint32_t v = pairs[x];
+			uint32_t y = x;
+			while(y > b0 && pairs[y - 1] > v) { pairs[y] = pairs[y - 1]; y--; }
+			pairs[y] = v;
+		}
+	}
 	if(lane == 0) w.pairCount[sid] = count;
 	__syncwarp();
 	// queue every pair slot under its pair kind (one atomic per kind per 32 pairs)
@@ -353,92 +425,127 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 	}
 }
 
-// PxBatchConstraintsTGS partition rule for one scene, run by one lane
-// (the rule is sequential in constraint order; see batching.h for the
-// reference citations).  Fills ordered[] (pair indices in solve order) and
-// the partition end offsets; returns the partition count, 0 on overflow.
-__device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t sid, uint32_t nc)
+// Per-warp shared-memory workspace of the solve: batching state per solver
+// body (scenes of up to SOLVE_SMEM_BODIES solver bodies) and the partition
+// offsets.
+constexpr uint32_t SOLVE_SMEM_BODIES = 544;
+struct SolveSmem
 {
+	uint32_t progress[SOLVE_SMEM_BODIES];        // partition bits of the current round
+	uint32_t maxNormal[SOLVE_SMEM_BODIES];       // 1 + last dynamic partition of the body
+	uint32_t maxStatic[SOLVE_SMEM_BODIES];       // static constraints of the body
+	uint32_t staticProgress[SOLVE_SMEM_BODIES];
+	uint32_t perPart[MAX_PARTITIONS];            // constraints per partition, then end offsets
+};
+
+// PxBatchConstraintsTGS partition rule for one scene (the rule is sequential
+// in constraint order; batching.h cites the reference): one lane walks the
+// constraints, the warp does the parallel bookkeeping.  Fills ordered[] (pair
+// indices in solve order) and the partition end offsets in perPart; returns
+// the partition count (all lanes), 0 on overflow.
+__device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t nc, SolveSmem& sm)
+{
+	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies;
-	uint32_t* progress = w.progress + sc.solverStart;
-	uint32_t* maxNormal = w.maxNormal + sc.solverStart;
-	uint32_t* maxStatic = w.maxStatic + sc.solverStart;
-	uint32_t* staticProgress = w.staticProgress + sc.solverStart;
-	uint32_t* perPart = w.partEnds + size_t(sid) * MAX_PARTITIONS;
+	const bool onChip = n + sc.nbStatics <= SOLVE_SMEM_BODIES;
+	uint32_t* progress = onChip ? sm.progress : w.progress + sc.solverStart;
+	uint32_t* maxNormal = onChip ? sm.maxNormal : w.maxNormal + sc.solverStart;
+	uint32_t* maxStatic = onChip ? sm.maxStatic : w.maxStatic + sc.solverStart;
+	uint32_t* staticProgress = onChip ? sm.staticProgress : w.staticProgress + sc.solverStart;
+	uint32_t* perPart = sm.perPart;
 	const uint32_t* cons = w.consList + sc.pairStart;
 	uint32_t* tag = w.tag + sc.pairStart;
 	uint32_t* ordered = w.ordered + sc.pairStart;
-	for(uint32_t b = 0; b < n; b++) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
-	for(uint32_t p = 0; p < MAX_PARTITIONS; p++) perPart[p] = 0;
+	for(uint32_t b = lane; b < n; b += 32) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
+	for(uint32_t p = lane; p < MAX_PARTITIONS; p += 32) perPart[p] = 0;
+	for(uint32_t c = lane; c < nc; c += 32) tag[c] = 0;
+	__syncwarp();
 	// pass 1: dynamic-dynamic constraints take the lowest free partition bit;
 	// constraints that find none retry in the next round of 32 partitions
-	for(uint32_t c = 0; c < nc; c++) tag[c] = 0;
-	uint32_t nbPart = 0, maxRound = 0;
-	for(uint32_t round = 0;; round++)
+	uint32_t nbPart = 0, maxRound = 0, fail = 0;
+	if(lane == 0)
 	{
-		if(round) for(uint32_t b = 0; b < n; b++) progress[b] = 0;
-		bool deferred = false;
-		for(uint32_t c = 0; c < nc; c++)
+		for(uint32_t round = 0;; round++)
 		{
-			const uint32_t key = w.pairs[sc.pairStart + cons[c]];
-			const uint32_t a = key >> 16, b = key & 0xffffu;
-			if(a < n && b < n)
+			if(round) for(uint32_t b = 0; b < n; b++) progress[b] = 0;
+			bool deferred = false;
+			for(uint32_t c = 0; c < nc; c++)
 			{
-				if((tag[c] >> 8) != round) continue;
-				const uint32_t mask = ~progress[a] & ~progress[b];
-				if(!mask) { tag[c] = (round + 1) << 8; deferred = true; continue; }
-				const uint32_t part = __ffs(mask) - 1;
-				progress[a] |= 1u << part;
-				progress[b] |= 1u << part;
-				const uint32_t gp = round * 32 + part;
-				if(gp >= MAX_PARTITIONS) return 0;
-				tag[c] = (round << 8) | gp;
-				perPart[gp]++;
-				maxNormal[a] = max(maxNormal[a], gp + 1);
-				maxNormal[b] = max(maxNormal[b], gp + 1);
-				nbPart = max(nbPart, gp + 1);
-				maxRound = max(maxRound, round);
-			}
-			else if(round == 0)
-			{
-				tag[c] = 0xffffu;
-				if(a < n) maxStatic[a]++;
-				if(b < n) maxStatic[b]++;
-			}
-		}
-		if(!deferred) break;
-	}
-	// statics of a body follow its last dynamic partition, one per partition
-	for(uint32_t b = 0; b < n; b++)
-	{
-		const uint32_t need = maxNormal[b] + maxStatic[b];
-		if(need > MAX_PARTITIONS) return 0;
-		nbPart = max(nbPart, need);
-		for(uint32_t k = 0; k < maxStatic[b]; k++) perPart[maxNormal[b] + k]++;
-	}
-	uint32_t acc = 0;
-	for(uint32_t p = 0; p < nbPart; p++) { const uint32_t t = perPart[p]; perPart[p] = acc; acc += t; }
-	// pass 2: round-0 dynamic constraints and all static constraints in input
-	// order, then each later round in input order
-	for(uint32_t round = 0; round <= maxRound; round++)
-		for(uint32_t c = 0; c < nc; c++)
-		{
-			const uint32_t t = tag[c];
-			if(t == 0xffffu)
-			{
-				if(round) continue;
 				const uint32_t key = w.pairs[sc.pairStart + cons[c]];
 				const uint32_t a = key >> 16, b = key & 0xffffu;
-				const uint32_t d = a < n ? a : b;
-				ordered[perPart[maxNormal[d] + staticProgress[d]++]++] = cons[c];
+				if(a < n && b < n)
+				{
+					if((tag[c] >> 8) != round) continue;
+					const uint32_t mask = ~progress[a] & ~progress[b];
+					if(!mask) { tag[c] = (round + 1) << 8; deferred = true; continue; }
+					const uint32_t part = __ffs(mask) - 1;
+					progress[a] |= 1u << part;
+					progress[b] |= 1u << part;
+					const uint32_t gp = round * 32 + part;
+					if(gp >= MAX_PARTITIONS) { fail = 1; break; }
+					tag[c] = (round << 8) | gp;
+					perPart[gp]++;
+					maxNormal[a] = max(maxNormal[a], gp + 1);
+					maxNormal[b] = max(maxNormal[b], gp + 1);
+					nbPart = max(nbPart, gp + 1);
+					maxRound = max(maxRound, round);
+				}
+				else if(round == 0)
+				{
+					tag[c] = 0xffffu;
+					if(a < n) maxStatic[a]++;
+					if(b < n) maxStatic[b]++;
+				}
 			}
-			else if((t >> 8) == round)
-				ordered[perPart[t & 0xffu]++] = cons[c];
+			if(fail || !deferred) break;
 		}
+	}
+	__syncwarp();
+	fail = __shfl_sync(0xffffffffu, fail, 0);
+	if(fail) return 0;
+	nbPart = __shfl_sync(0xffffffffu, nbPart, 0);
+	maxRound = __shfl_sync(0xffffffffu, maxRound, 0);
+	// statics of a body follow its last dynamic partition, one per partition
+	uint32_t need = nbPart;
+	for(uint32_t b = lane; b < n; b += 32)
+	{
+		const uint32_t mn = maxNormal[b], ms = maxStatic[b];
+		need = max(need, mn + ms);
+		if(mn + ms <= MAX_PARTITIONS)
+			for(uint32_t k = 0; k < ms; k++) atomicAdd(&perPart[mn + k], 1u);
+	}
+	for(int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+	if(need > MAX_PARTITIONS) return 0;
+	nbPart = need;
+	__syncwarp();
+	warpExclusiveScan(perPart, nbPart);
+	// pass 2: round-0 dynamic constraints and all static constraints in input
+	// order, then each later round in input order
+	if(lane == 0)
+	{
+		for(uint32_t round = 0; round <= maxRound; round++)
+			for(uint32_t c = 0; c < nc; c++)
+			{
+				const uint32_t t = tag[c];
+				if(t == 0xffffu)
+				{
+					if(round) continue;
+					const uint32_t key = w.pairs[sc.pairStart + cons[c]];
+					const uint32_t a = key >> 16, b = key & 0xffffu;
+					const uint32_t d = a < n ? a : b;
+					ordered[perPart[maxNormal[d] + staticProgress[d]++]++] = cons[c];
+				}
+				else if((t >> 8) == round)
+					ordered[perPart[t & 0xffu]++] = cons[c];
+			}
+	}
+	__syncwarp();
 	return nbPart;
 }
 
-__device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp)
+// Solver bodies, constraint list and batching of one scene; queues the
+// scene's constraints for row preparation.
+__device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, SolveSmem& sm)
 {
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
@@ -475,17 +582,32 @@ __device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& s
 		nc += __popc(bal);
 	}
 	__syncwarp();
-	// 3. batching (one lane)
-	uint32_t nbPart = 0;
+	// 3. batching
+	const uint32_t nbPart = sceneBatch(w, sc, nc, sm);
+	for(uint32_t p = lane; p < nbPart; p += 32) w.partEnds[size_t(sid) * MAX_PARTITIONS + p] = sm.perPart[p];
 	if(lane == 0)
 	{
-		nbPart = sceneBatch(w, sc, sid, nc);
+		w.nbConstraints[sid] = nc;
+		w.nbPartitions[sid] = nbPart;
 		if(!nbPart && nc) atomicOr(&w.status[sid], ST_PARTITION_OVERFLOW);
 	}
-	nbPart = __shfl_sync(0xffffffffu, nbPart, 0);
-	__syncwarp();
-	if(!nbPart && nc) return;   // leave the scene unchanged; the host sees the status bit
-	// 4. contact rows
+	if(!nbPart) return;   // nothing to solve, or overflow: the scene is left unchanged
+	uint32_t qbase = 0;
+	if(lane == 0) qbase = atomicAdd(&w.workCounter[3], nc);
+	qbase = __shfl_sync(0xffffffffu, qbase, 0);
+	for(uint32_t r = lane; r < nc; r += 32) w.prepQueue[qbase + r] = sc.pairStart + r;
+}
+
+// Contact rows of one constraint (PxCreateContactConstraintsTGS for one
+// descriptor): slot = scene pair start + position in solve order.
+__device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t slot, const StepParams& sp)
+{
+	const SceneDesc sc = w.scenes[w.slotScene[slot]];
+	const uint32_t n = sc.nbBodies;
+	tgs::BodyVel* vel = w.vel + sc.solverStart;
+	tgs::BodyTx* tx = w.tx + sc.solverStart;
+	tgs::BodyData* data = w.data + sc.solverStart;
+	Tr* pose = w.pose + sc.solverStart;
 	const float invDt = 1.0f / sp.dt;
 	tgs::PrepParams pp;
 	pp.invStepDt = invDt * float(sp.nbPos);
@@ -495,33 +617,41 @@ __device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& s
 	pp.bounceThreshold = sp.bounceThreshold;
 	pp.frictionOffsetThreshold = sp.frictionOffsetThreshold;
 	pp.biasCoefficient = 2.0f * sqrtf(invDt / pp.invStepDt);
-	for(uint32_t r = lane; r < nc; r += 32)
+	const uint32_t k = w.ordered[slot];
+	const uint32_t key = w.pairs[sc.pairStart + k];
+	const uint32_t a = key >> 16, b = key & 0xffffu;
+	const float fa = w.friction[sc.bodyStart + a];
+	const float fb = b < n ? w.friction[sc.bodyStart + b] : sp.staticFriction;
+	const float mu = (fa + fb) * 0.5f;
+	tgs::Contact cs[tgs::MAX_CONTACTS];
+	const uint32_t cnt = w.contactCount[sc.pairStart + k];
+	const float4* src = w.contacts + size_t(sc.pairStart + k) * 8;
+	for(uint32_t c = 0; c < cnt; c++)
 	{
-		const uint32_t k = w.ordered[sc.pairStart + r];
-		const uint32_t key = w.pairs[sc.pairStart + k];
-		const uint32_t a = key >> 16, b = key & 0xffffu;
-		const float fa = w.friction[sc.bodyStart + a];
-		const float fb = b < n ? w.friction[sc.bodyStart + b] : sp.staticFriction;
-		const float mu = (fa + fb) * 0.5f;
-		tgs::Contact cs[tgs::MAX_CONTACTS];
-		const uint32_t cnt = w.contactCount[sc.pairStart + k];
-		const float4* src = w.contacts + size_t(sc.pairStart + k) * 8;
-		for(uint32_t c = 0; c < cnt; c++)
-		{
-			const float4 nn = src[2 * c], pp4 = src[2 * c + 1];
-			cs[c].n = v3(nn.x, nn.y, nn.z);
-			cs[c].sep = nn.w;
-			cs[c].p = v3(pp4.x, pp4.y, pp4.z);
-			cs[c].staticFriction = mu;
-			cs[c].dynamicFriction = mu;
-			cs[c].restitution = 0.0f;
-		}
-		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp,
-		                    w.recs[sc.pairStart + r]);
+		const float4 nn = src[2 * c], pp4 = src[2 * c + 1];
+		cs[c].n = v3(nn.x, nn.y, nn.z);
+		cs[c].sep = nn.w;
+		cs[c].p = v3(pp4.x, pp4.y, pp4.z);
+		cs[c].staticFriction = mu;
+		cs[c].dynamicFriction = mu;
+		cs[c].restitution = 0.0f;
 	}
+	tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, w.recs[slot]);
+}
+
+// Position iterations (each followed by integration), velocity iterations,
+// PxIntegrateSolverBodiesTGS and write-back of one scene.
+__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, uint32_t* ends)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t n = sc.nbBodies;
+	const uint32_t nbPart = w.nbPartitions[sid];
+	if(!nbPart && w.nbConstraints[sid]) return;   // batching overflowed: leave the scene unchanged
+	tgs::BodyVel* vel = w.vel + sc.solverStart;
+	tgs::BodyTx* tx = w.tx + sc.solverStart;
+	Tr* pose = w.pose + sc.solverStart;
+	for(uint32_t p = lane; p < nbPart; p += 32) ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
 	__syncwarp();
-	// 5. position iterations (each followed by integration), then velocity iterations
-	const uint32_t* ends = w.partEnds + size_t(sid) * MAX_PARTITIONS;
 	const float stepDt = sp.dt / float(sp.nbPos);
 	float elapsed = 0.0f;
 	for(uint32_t it = 0; it < sp.nbPos + sp.nbVel; it++)
@@ -558,7 +688,6 @@ __device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& s
 			__syncwarp();
 		}
 	}
-	// 6. PxIntegrateSolverBodiesTGS + write-back of velocities and poses
 	for(uint32_t i = lane; i < n; i += 32)
 	{
 		Tr p = pose[i];
@@ -578,6 +707,8 @@ __device__ __forceinline__ void sceneSolve(const WorldDev& w, const SceneDesc& s
 // the narrowphase runs one kernel per pair kind over all scenes' pairs.
 __global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams sp)
 {
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	BpSmem& sm = reinterpret_cast<BpSmem*>(stageSmem)[threadIdx.x >> 5];
 	const uint32_t lane = threadIdx.x & 31;
 	for(;;)
 	{
@@ -587,12 +718,14 @@ __global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams s
 		if(item >= w.nbScenes) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
-		sceneBroadphase(w, sc, sid, sp);
+		sceneBroadphase(w, sc, sid, sp, sm);
 	}
 }
 
-__global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
+__global__ void __launch_bounds__(128) batchKernel(WorldDev w, StepParams sp)
 {
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	SolveSmem& sm = reinterpret_cast<SolveSmem*>(stageSmem)[threadIdx.x >> 5];
 	const uint32_t lane = threadIdx.x & 31;
 	for(;;)
 	{
@@ -602,7 +735,30 @@ __global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
 		if(item >= w.nbScenes) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
-		sceneSolve(w, sc, sid, sp);
+		sceneBatchStage(w, sc, sid, sp, sm);
+	}
+}
+
+// Row preparation of every scene's constraints: a thread per constraint.
+__global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
+{
+	const uint32_t count = w.workCounter[3];
+	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
+}
+
+__global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
+{
+	__shared__ uint32_t ends[4][MAX_PARTITIONS];
+	const uint32_t lane = threadIdx.x & 31;
+	for(;;)
+	{
+		uint32_t item = 0;
+		if(lane == 0) item = atomicAdd(&w.workCounter[2], 1u);
+		item = __shfl_sync(0xffffffffu, item, 0);
+		if(item >= w.nbScenes) break;
+		const uint32_t sid = w.workOrder[item];
+		const SceneDesc sc = w.scenes[sid];
+		sceneIterate(w, sc, sid, sp, ends[threadIdx.x >> 5]);
 	}
 }
 
@@ -644,9 +800,9 @@ struct World
 	world::StepParams params;
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
-	uint32_t gridBlocks = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
+	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
 	DevBuf<world::SceneDesc> scenes;
-	DevBuf<uint32_t> typeQueue, slotScene;
+	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue;
 	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
 	    staticProgress, partEnds, status;
 	DevBuf<tgs::RigidBody> bodies;
@@ -666,6 +822,8 @@ struct World
 	static uint32_t pow2(uint32_t x) { uint32_t p = 1; while(p < x) p <<= 1; return p; }
 	// work counters of the broadphase and solve kernels, then the per-kind pair counts
 	static constexpr uint32_t COUNTERS = 8 + world::NB_KINDS;
+	// broadphase, one narrowphase kernel per pair kind, batching, row preparation, solve
+	static constexpr uint32_t KERNELS_PER_STEP = 4 + world::NB_KINDS;
 
 	world::WorldDev dev()
 	{
@@ -678,6 +836,7 @@ struct World
 		w.vel = vel.ptr; w.tx = tx.ptr; w.data = data.ptr; w.pose = pose.ptr; w.progress = progress.ptr; w.maxNormal = maxNormal.ptr;
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
 		w.typeCount = workCounter.ptr + 8; w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
+		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr;
 		return w;
 	}
 
@@ -705,7 +864,7 @@ struct World
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
 		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
+		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
 		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
 		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
 		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
@@ -740,7 +899,11 @@ struct World
 		int dev = 0, sms = 0;
 		GBPX_CUDA_TRY(cudaGetDevice(&dev));
 		GBPX_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		GBPX_CUDA_TRY(gridFor(world::broadphaseKernel, sms, gridBlocks));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::broadphaseKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bpSmemBytes(world::STAGE_WARPS))));
+		GBPX_CUDA_TRY(gridFor(world::broadphaseKernel, sms, gridBlocks, bpSmemBytes(world::STAGE_WARPS)));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solveSmemBytes(world::STAGE_WARPS))));
+		GBPX_CUDA_TRY(gridFor(world::batchKernel, sms, gridBatch, solveSmemBytes(world::STAGE_WARPS)));
+		GBPX_CUDA_TRY(gridFor(world::prepKernel, sms, gridPrep));
 		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve));
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
@@ -756,11 +919,13 @@ struct World
 		    world::narrowphaseKernel<2, 2>, world::narrowphaseKernel<2, 3>, world::narrowphaseKernel<3, 3>};
 		return k;
 	}
+	static size_t bpSmemBytes(uint32_t warps) { return warps * sizeof(world::BpSmem); }
+	static size_t solveSmemBytes(uint32_t warps) { return warps * sizeof(world::SolveSmem); }
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
-	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid)
+	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid, size_t smem = 0)
 	{
 		int perSm = 0;
-		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, 128, 0);
+		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, 128, smem);
 		grid = uint32_t(sms * (perSm > 0 ? perSm : 1));
 		return e;
 	}
@@ -771,18 +936,22 @@ struct World
 	int launchStep(uint32_t plainScene = ~0u)
 	{
 		world::WorldDev w = dev();
-		uint32_t gBp = gridBlocks, gSolve = gridSolve, threads = 128;
-		if(plainScene < nbScenes)
+		uint32_t gBp = gridBlocks, gBatch = gridBatch, gPrep = gridPrep, gSolve = gridSolve, threads = 128;
+		const bool plain = plainScene < nbScenes;
+		if(plain)
 		{
 			w.workOrder = identity.ptr + plainScene;
 			w.nbScenes = 1;
-			gBp = gSolve = 1;
+			gBp = gBatch = gSolve = 1;
+			gPrep = std::min(gridPrep, 8u);
 			threads = 32;
 		}
 		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
-		world::broadphaseKernel<<<gBp, threads, 0, stream>>>(w, params);
+		world::broadphaseKernel<<<gBp, threads, bpSmemBytes(threads / 32), stream>>>(w, params);
 		for(uint32_t k = 0; k < world::NB_KINDS; k++)
-			npKernels()[k]<<<plainScene < nbScenes ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
+			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
+		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
+		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
 		world::solveKernel<<<gSolve, threads, 0, stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
@@ -843,7 +1012,7 @@ struct World
 		if(stream) cudaStreamSynchronize(stream);
 		if(graphExec) cudaGraphExecDestroy(graphExec);
 		graphExec = nullptr;
-		scenes.release(); typeQueue.release(); slotScene.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
+		scenes.release(); typeQueue.release(); slotScene.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
@@ -942,13 +1111,14 @@ GBPX_API int gbpx_world_status(void* wv, uint32_t* outStatus)
 	return GBPX_OK;
 }
 
-// nbScenes, nbBodies, nbStatics, pair slots, persistent grid blocks, device bytes
-GBPX_API int gbpx_world_info(void* wv, uint64_t* out6)
+// nbScenes, nbBodies, nbStatics, pair slots, persistent grid blocks of the
+// broadphase, device bytes, kernels launched per step, reserved (0)
+GBPX_API int gbpx_world_info(void* wv, uint64_t* out8)
 {
 	World* w = static_cast<World*>(wv);
-	if(!w || !out6) return GBPX_ERR_INVALID;
-	out6[0] = w->nbScenes; out6[1] = w->nbBodies; out6[2] = w->nbStatics; out6[3] = w->nbPairSlots; out6[4] = w->gridBlocks;
-	out6[5] = w->deviceBytes;
+	if(!w || !out8) return GBPX_ERR_INVALID;
+	out8[0] = w->nbScenes; out8[1] = w->nbBodies; out8[2] = w->nbStatics; out8[3] = w->nbPairSlots; out8[4] = w->gridBlocks;
+	out8[5] = w->deviceBytes; out8[6] = World::KERNELS_PER_STEP; out8[7] = 0;
 	return GBPX_OK;
 }
 

@@ -113,3 +113,49 @@ def mass_properties_batch(types, geoms, density=1000.0):
     iyz = mc * (r * r / 4.0 + (2 * hh) ** 2 / 12.0) + ms * (0.4 * r * r + hh * hh + 0.75 * hh * r)
     inertia[cap] = np.stack([ix, iyz, iyz], 1)
     return (1.0 / m).astype(np.float32), (1.0 / inertia).astype(np.float32)
+
+
+def pyramid_scene(seed=1, levels=20, half=0.5, density=1000.0, friction=0.5, jitter=0.01, yaw_deg=2.0):
+    """The box pyramid of the reference's immediate-mode snippet
+    (physx/snippets/snippetimmediatemode/SnippetImmediateMode.cpp:283-298):
+    `levels` rows of unit boxes (half extent `half`), row i holding levels - i
+    boxes at x = (2j - (levels - i)) * half, y = (2i + 1) * half, z = 0, each
+    jittered by U(-jitter, jitter) m in x and z and U(-yaw, yaw) degrees about y;
+    one static plane y = 0.  Returns one scene in the world layout."""
+    rng = np.random.default_rng(seed)
+    pos = []
+    for i in range(levels):
+        for j in range(levels - i):
+            pos.append(((2 * j - (levels - i)) * half, (2 * i + 1) * half, 0.0))
+    n = len(pos)
+    pos = np.array(pos, np.float64)
+    pos[:, 0] += rng.uniform(-jitter, jitter, n)
+    pos[:, 2] += rng.uniform(-jitter, jitter, n)
+    yaw = np.radians(rng.uniform(-yaw_deg, yaw_deg, n))
+    rb = rigid_body_data(n)
+    rb["p"] = pos.astype(np.float32)
+    rb["q"] = np.stack([np.zeros(n), np.sin(yaw / 2), np.zeros(n), np.cos(yaw / 2)], 1).astype(np.float32)
+    types = np.full(n, 3, np.int32)
+    geoms = np.zeros((n, 4), np.float32)
+    geoms[:, :3] = half
+    im, ii = mass_properties_batch(types, geoms, density)
+    rb["invMass"] = im
+    rb["invInertia"] = ii
+    return dict(body_count=np.array([n], np.uint32), static_count=np.ones(1, np.uint32), rigid=rb, types=types, geoms=geoms,
+                friction=np.full(n, friction, np.float32), static_poses=plane_pose_y_up()[None, :].copy(),
+                static_types=np.ones(1, np.int32), static_geoms=np.zeros((1, 4), np.float32))
+
+
+def kinetic_energy(rigid):
+    """Translational + rotational kinetic energy of PxRigidBodyData records (mass-space
+    inertia, world angular velocity rotated into the body frame)."""
+    m = 1.0 / rigid["invMass"].astype(np.float64)
+    v = rigid["linVel"].astype(np.float64)
+    w = rigid["angVel"].astype(np.float64)
+    q = rigid["q"].astype(np.float64)
+    # rotate w into the body frame: q^-1 * w
+    qv, qw = -q[:, :3], q[:, 3:4]
+    t = 2.0 * np.cross(qv, w)
+    wl = w + qw * t + np.cross(qv, t)
+    inertia = 1.0 / rigid["invInertia"].astype(np.float64)
+    return float(0.5 * (m * (v * v).sum(1)).sum() + 0.5 * (inertia * wl * wl).sum())

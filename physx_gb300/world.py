@@ -104,10 +104,10 @@ class World:
         return st
 
     def info(self):
-        out = np.zeros(6, np.uint64)
+        out = np.zeros(8, np.uint64)
         check(self._L.gbpx_world_info(self._h, _p(out)), "gbpx_world_info")
         return dict(scenes=int(out[0]), bodies=int(out[1]), statics=int(out[2]), pair_slots=int(out[3]), grid_blocks=int(out[4]),
-                    device_bytes=int(out[5]))
+                    device_bytes=int(out[5]), kernels_per_step=int(out[6]))
 
     def time_steps(self, n, graph=True):
         """Milliseconds for n device-resident steps (CUDA events on the world stream)."""

@@ -123,10 +123,33 @@ def make_recip():
     print("wrote recip_fast")
 
 
+def pyramid_trace(which, steps=300):
+    """Long-horizon statistics of the 210-box pyramid stepped `steps` times: kinetic
+    energy and highest / lowest box centre per step, final horizontal drift."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from physx_gb300.workloads import kinetic_energy, pyramid_scene
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = pyramid_scene()
+    rb = sc["rigid"].copy()
+    ke, top, low = [], [], []
+    for _ in range(steps):
+        rb = run_scene_step(which, dict(sc, rigid=rb), DEFAULT_PARAMS, steps=1)
+        ke.append(kinetic_energy(rb))
+        top.append(float(rb["p"][:, 1].max()))
+        low.append(float(rb["p"][:, 1].min()))
+    drift = float(np.abs(rb["p"][:, 0] - sc["rigid"]["p"][:, 0]).mean())
+    return dict(ke=np.array(ke), top=np.array(top), low=np.array(low), drift=np.float64(drift))
+
+
+def make_pyramid():
+    np.savez_compressed(os.path.join(HERE, "pyramid_stats.npz"), **pyramid_trace("pxref"))
+    print("wrote pyramid_stats")
+
+
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np", "tgs", "scene", "recip"]
+    which = sys.argv[1:] or ["bp", "np", "tgs", "scene", "recip", "pyramid"]
     if "bp" in which:
         make_bp()
     if "np" in which:
@@ -137,3 +160,5 @@ if __name__ == "__main__":
         make_scene()
     if "recip" in which:
         make_recip()
+    if "pyramid" in which:
+        make_pyramid()
