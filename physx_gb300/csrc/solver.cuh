@@ -49,22 +49,33 @@ struct BodyData { V3 origLin, origAng; float maxContactImpulse, penBiasClamp, in
 
 struct Contact { V3 n; float sep; V3 p; float staticFriction, dynamicFriction, restitution; };
 
-struct PointRow { V3 raXnI, rbXnI; float velMultiplier, separation, biasCoefficient, targetVelocity, recipResponse, maxImpulse; };
+struct __align__(16) PointRow { V3 raXnI, rbXnI; float velMultiplier, separation, biasCoefficient, targetVelocity, recipResponse, maxImpulse; };
 struct FrictionRow { V3 normal; float error; V3 raXnI; float targetVel; V3 rbXnI; float velMultiplier, frictionScale, biasScale; };
-struct PatchRows
+struct __align__(16) PatchRows
 {
 	V3 normal;
 	float invMass0, invMass1, maxPenBias, staticFriction, dynamicFriction;
 	int pointStart, nbPoints, frictionStart, nbFriction;
 };
-struct ConstraintRecord
+// One constraint's rows, packed after a 16-byte header so that a constraint
+// touches as few cache lines as it has rows: patches, points, friction rows
+// (two per anchor), normal impulses, friction impulses.
+struct __align__(16) ConstraintRecord
 {
-	int bodyA, bodyB, nbPatches, pad;
-	PatchRows patch[MAX_CONTACTS];
-	PointRow point[MAX_CONTACTS];
-	FrictionRow friction[MAX_FRICTION];
-	float force[MAX_CONTACTS];
-	float frictionForce[MAX_FRICTION];
+	int bodyA, bodyB, nbPatches, counts;   // counts = points | friction rows << 16
+	float4 rows[(MAX_CONTACTS * sizeof(PatchRows) + MAX_CONTACTS * sizeof(PointRow) + MAX_FRICTION * sizeof(FrictionRow) +
+	             (MAX_CONTACTS + MAX_FRICTION) * 4 + 15) / 16];
+
+	__device__ __forceinline__ int nbPoints() const { return counts & 0xffff; }
+	__device__ __forceinline__ int nbFriction() const { return counts >> 16; }
+	__device__ __forceinline__ PatchRows* patch() { return reinterpret_cast<PatchRows*>(rows); }
+	__device__ __forceinline__ PointRow* point() { return reinterpret_cast<PointRow*>(reinterpret_cast<char*>(rows) + nbPatches * sizeof(PatchRows)); }
+	__device__ __forceinline__ FrictionRow* friction()
+	{
+		return reinterpret_cast<FrictionRow*>(reinterpret_cast<char*>(point()) + nbPoints() * sizeof(PointRow));
+	}
+	__device__ __forceinline__ float* force() { return reinterpret_cast<float*>(friction() + nbFriction()); }
+	__device__ __forceinline__ float* frictionForce() { return force() + nbPoints(); }
 };
 
 // ------------------------------------------------------------- bodies
@@ -331,12 +342,30 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 	rec.bodyA = a;
 	rec.bodyB = b;
 	rec.nbPatches = 0;
+	rec.counts = 0;
 	if(nbContacts == 0) return;
 	Correlation c;
 	createContactPatches(c, contacts, nbContacts, 0.999f);
 	correlatePatches(c, contacts, 0.999f);
 	growPatches(c, contacts, f0, f1, pp.frictionOffsetThreshold + 0.0f);
 
+	// row counts first: the rows are packed in this order
+	int usedPatches = 0, totalPoints = 0, totalFriction = 0;
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		if(c.fpContactCount[i] == 0) continue;
+		usedPatches++;
+		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch]) totalPoints += c.cpCount[patch];
+		totalFriction += c.fpAnchorCount[i] * 2;
+	}
+	rec.nbPatches = usedPatches;
+	rec.counts = totalPoints | (totalFriction << 16);
+	PatchRows* patchRows = rec.patch();
+	PointRow* pointRows = rec.point();
+	FrictionRow* frictionRows = rec.friction();
+	float* force = rec.force();
+	float* frictionForce = rec.frictionForce();
+	int patchOut = 0;
 	const bool kin0 = va.kinematic != 0, kin1 = vb.kinematic != 0;
 	const float invMass0 = 1.0f * d0.invMass;
 	const float invMass1 = (-1.0f) * d1.invMass;
@@ -355,7 +384,7 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 		if(c.fpContactCount[i] == 0) continue;
 		const int first = c.listHead[i];
 		const Contact& base0 = contacts[c.cpStart[first]];
-		PatchRows& pr = rec.patch[rec.nbPatches];
+		PatchRows& pr = patchRows[patchOut];
 		pr.invMass0 = invMass0;
 		pr.invMass1 = -invMass1;
 		const V3 n = contacts[c.cpStart[c.listHead[i]]].n;
@@ -369,8 +398,8 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 			for(int j = 0; j < c.cpCount[patch]; j++)
 			{
 				constructPoint(s0, s1, imn0, imn1, p0, p1, n, nv0, nv1, av0, av1, invDtp8, invDt, pp.totalDt, pp.invTotalDt, base0.restitution,
-				               pp.bounceThreshold, contacts[c.cpStart[patch] + j], kin0, kin1, rec.point[nPoints]);
-				rec.force[nPoints] = 0.0f;
+				               pp.bounceThreshold, contacts[c.cpStart[patch] + j], kin0, kin1, pointRows[nPoints]);
+				force[nPoints] = 0.0f;
 				nPoints++;
 			}
 		pr.nbPoints = nPoints - pr.pointStart;
@@ -399,7 +428,7 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 				for(int dir = 0; dir < 2; dir++)
 				{
 					const V3 t = dir == 0 ? t0 : t1;
-					FrictionRow& fr = rec.friction[nFriction];
+					FrictionRow& fr = frictionRows[nFriction];
 					const V3 raXn = cross(ra, t), rbXn = cross(rb, t);
 					const V3 ri0 = m33MulV(s0, raXn), ri1 = m33MulV(s1, rbXn);
 					const float resp0 = imn0 + dotA(ri0, ri0) * 1.0f;
@@ -417,12 +446,12 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 					fr.velMultiplier = velMultiplier;
 					fr.frictionScale = frictionScale;
 					fr.biasScale = frictionBiasScale;
-					rec.frictionForce[nFriction] = 0.0f;
+					frictionForce[nFriction] = 0.0f;
 					nFriction++;
 				}
 			}
 		}
-		rec.nbPatches++;
+		patchOut++;
 	}
 }
 
@@ -435,9 +464,14 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
 	const V3 angM0 = b0.dAng, angM1 = b1.dAng;
 	const V3 relMotion = sub(b0.dLin, b1.dLin);
+	const PatchRows* patchRows = rec.patch();
+	const PointRow* pointRows = rec.point();
+	const FrictionRow* frictionRows = rec.friction();
+	float* force = rec.force();
+	float* frictionForce = rec.frictionForce();
 	for(int p = 0; p < rec.nbPatches; p++)
 	{
-		const PatchRows& pr = rec.patch[p];
+		const PatchRows pr = patchRows[p];
 		const V3 n = pr.normal;
 		const float invMassA = pr.invMass0, invMassB = pr.invMass1;
 		const V3 nIM0 = scale(n, invMassA), nIM1 = scale(n, invMassB);
@@ -446,7 +480,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 		for(int i = 0; i < pr.nbPoints; i++)
 		{
 			const int k = pr.pointStart + i;
-			const PointRow& c = rec.point[k];
+			const PointRow c = pointRows[k];
 			const float angDelta0 = dotA(angM0, c.raXnI), angDelta1 = dotA(angM1, c.rbXnI);
 			const float deltaAng = angDelta0 - angDelta1;
 			const float targetVel = c.targetVelocity;
@@ -458,7 +492,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 			const float normalVel = sumElems(sub(v0, v1));
 			const float biasNV = bias * c.recipResponse;
 			const float lambda = biasNV - (normalVel - targetVel) * c.velMultiplier;
-			const float applied = rec.force[k];
+			const float applied = force[k];
 			const float _deltaF = fmax_(lambda, -applied);
 			const float _newForce = applied + _deltaF;
 			const float newForce = fmin_(_newForce, c.maxImpulse);
@@ -467,7 +501,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 			lin1 = negScaleSub(nIM1, deltaF, lin1);
 			ang0 = scaleAdd(c.raXnI, deltaF * 1.0f, ang0);
 			ang1 = negScaleSub(c.rbXnI, deltaF * 1.0f, ang1);
-			rec.force[k] = newForce;
+			force[k] = newForce;
 			accumulated = accumulated + newForce;
 		}
 		if(pr.nbFriction)
@@ -478,8 +512,8 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 			for(int i = 0; i < pairs; i += 2)
 			{
 				const int k0 = pr.frictionStart + i, k1 = k0 + 1;
-				const FrictionRow& f0 = rec.friction[k0];
-				const FrictionRow& f1 = rec.friction[k1];
+				const FrictionRow& f0 = frictionRows[k0];
+				const FrictionRow& f1 = frictionRows[k1];
 				const float fs = f0.frictionScale;
 				const float biasScale = f0.biasScale;
 				float dv0 = (dotA(f0.raXnI, angM0) - dotA(f0.rbXnI, angM1)) + dotA(f0.normal, relMotion);
@@ -492,7 +526,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 				const V3 dl01 = scale(f1.normal, invMassA), dl11 = scale(f1.normal, invMassB);
 				const float nvel0 = sumElems(sub(add(mul(lin0, f0.normal), mul(ang0, f0.raXnI)), add(mul(lin1, f0.normal), mul(ang1, f0.rbXnI))));
 				const float nvel1 = sumElems(sub(add(mul(lin0, f1.normal), mul(ang0, f1.raXnI)), add(mul(lin1, f1.normal), mul(ang1, f1.rbXnI))));
-				const float a0 = rec.frictionForce[k0], a1 = rec.frictionForce[k1];
+				const float a0 = frictionForce[k0], a1 = frictionForce[k1];
 				const float tmp10 = a0 - (bias0 - f0.targetVel) * f0.velMultiplier;
 				const float tmp11 = a1 - (bias1 - f1.targetVel) * f1.velMultiplier;
 				const float ti0 = tmp10 - nvel0 * f0.velMultiplier;
@@ -507,8 +541,8 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 				lin1 = negScaleSub(dl10, df0, negScaleSub(dl11, df1, lin1));
 				ang0 = scaleAdd(f0.raXnI, df0 * 1.0f, scaleAdd(f1.raXnI, df1 * 1.0f, ang0));
 				ang1 = negScaleSub(f0.rbXnI, df0 * 1.0f, negScaleSub(f1.rbXnI, df1 * 1.0f, ang1));
-				rec.frictionForce[k0] = nf0;
-				rec.frictionForce[k1] = nf1;
+				frictionForce[k0] = nf0;
+				frictionForce[k1] = nf1;
 			}
 		}
 	}

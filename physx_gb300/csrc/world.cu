@@ -639,18 +639,42 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t slot, const
 	tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, w.recs[slot]);
 }
 
+// Velocities of one scene's solver bodies during the iterations: linear and
+// (momentum-space) angular velocity, the values every constraint solve
+// reads and writes.  Scenes of up to SOLVE_SMEM_BODIES solver bodies keep
+// them in shared memory; larger scenes use the BodyVel records in HBM.
+struct VelSmem
+{
+	V3 lin[SOLVE_SMEM_BODIES];
+	V3 ang[SOLVE_SMEM_BODIES];
+};
+struct SharedVel
+{
+	VelSmem& s;
+	__device__ __forceinline__ V3 lin(uint32_t i) const { return s.lin[i]; }
+	__device__ __forceinline__ V3 ang(uint32_t i) const { return s.ang[i]; }
+	__device__ __forceinline__ void set(uint32_t i, V3 l, V3 a) const { s.lin[i] = l; s.ang[i] = a; }
+};
+struct GlobalVel
+{
+	tgs::BodyVel* v;
+	__device__ __forceinline__ V3 lin(uint32_t i) const { return v[i].lin; }
+	__device__ __forceinline__ V3 ang(uint32_t i) const { return v[i].ang; }
+	__device__ __forceinline__ void set(uint32_t i, V3 l, V3 a) const { v[i].lin = l; v[i].ang = a; }
+};
+
 // Position iterations (each followed by integration), velocity iterations,
 // PxIntegrateSolverBodiesTGS and write-back of one scene.
-__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, uint32_t* ends)
+template <typename Vel>
+__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, const uint32_t* ends,
+                                             uint32_t nbPart, const Vel& V)
 {
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t n = sc.nbBodies;
-	const uint32_t nbPart = w.nbPartitions[sid];
-	if(!nbPart && w.nbConstraints[sid]) return;   // batching overflowed: leave the scene unchanged
+	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
 	tgs::BodyVel* vel = w.vel + sc.solverStart;
 	tgs::BodyTx* tx = w.tx + sc.solverStart;
 	Tr* pose = w.pose + sc.solverStart;
-	for(uint32_t p = lane; p < nbPart; p += 32) ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+	for(uint32_t i = lane; i < nTot; i += 32) V.set(i, vel[i].lin, vel[i].ang);
 	__syncwarp();
 	const float stepDt = sp.dt / float(sp.nbPos);
 	float elapsed = 0.0f;
@@ -667,34 +691,42 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 				tgs::ConstraintRecord& rec = w.recs[sc.pairStart + r];
 				if(rec.nbPatches == 0) continue;
 				const uint32_t a = uint32_t(rec.bodyA), b = uint32_t(rec.bodyB);
-				tgs::BodyVel b0 = vel[a], b1 = vel[b];
+				tgs::BodyVel b0, b1;
+				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = vel[a].dLin; b0.dAng = vel[a].dAng;
+				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = vel[b].dLin; b1.dAng = vel[b].dAng;
 				const bool dynB = b < n;
 				tgs::solveConstraint(rec, b0, b1, dynB, minPen, elapsed);
-				vel[a].lin = b0.lin;
-				vel[a].ang = b0.ang;
-				if(dynB)
-				{
-					vel[b].lin = b1.lin;
-					vel[b].ang = b1.ang;
-				}
+				V.set(a, b0.lin, b0.ang);
+				if(dynB) V.set(b, b1.lin, b1.ang);
 			}
 			begin = end;
 			__syncwarp();
 		}
 		if(posIter)
 		{
-			for(uint32_t i = lane; i < n; i += 32) tgs::integrateStep(vel[i], tx[i], stepDt);
+			for(uint32_t i = lane; i < n; i += 32)
+			{
+				tgs::BodyVel v = vel[i];
+				v.lin = V.lin(i);
+				v.ang = V.ang(i);
+				tgs::integrateStep(v, tx[i], stepDt);
+				vel[i].dLin = v.dLin;
+				vel[i].dAng = v.dAng;
+			}
 			elapsed += stepDt;
 			__syncwarp();
 		}
 	}
 	for(uint32_t i = lane; i < n; i += 32)
 	{
+		tgs::BodyVel v = vel[i];
+		v.lin = V.lin(i);
+		v.ang = V.ang(i);
 		Tr p = pose[i];
 		V3 wv;
-		tgs::finalizeBody(vel[i], tx[i], p, wv);
+		tgs::finalizeBody(v, tx[i], p, wv);
 		tgs::RigidBody& rb = w.bodies[sc.bodyStart + i];
-		rb.linVel[0] = vel[i].lin.x; rb.linVel[1] = vel[i].lin.y; rb.linVel[2] = vel[i].lin.z;
+		rb.linVel[0] = v.lin.x; rb.linVel[1] = v.lin.y; rb.linVel[2] = v.lin.z;
 		rb.angVel[0] = wv.x; rb.angVel[1] = wv.y; rb.angVel[2] = wv.z;
 		rb.q[0] = p.q.x; rb.q[1] = p.q.y; rb.q[2] = p.q.z; rb.q[3] = p.q.w;
 		rb.p[0] = p.p.x; rb.p[1] = p.p.y; rb.p[2] = p.p.z;
@@ -746,9 +778,16 @@ __global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
 }
 
+struct IterSmem
+{
+	uint32_t ends[MAX_PARTITIONS];
+	VelSmem vel;
+};
+
 __global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
 {
-	__shared__ uint32_t ends[4][MAX_PARTITIONS];
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	IterSmem& sm = reinterpret_cast<IterSmem*>(stageSmem)[threadIdx.x >> 5];
 	const uint32_t lane = threadIdx.x & 31;
 	for(;;)
 	{
@@ -758,7 +797,12 @@ __global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
 		if(item >= w.nbScenes) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
-		sceneIterate(w, sc, sid, sp, ends[threadIdx.x >> 5]);
+		const uint32_t nbPart = w.nbPartitions[sid];
+		if(!nbPart && w.nbConstraints[sid]) continue;   // batching overflowed: the scene is left unchanged
+		for(uint32_t p = lane; p < nbPart; p += 32) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+		__syncwarp();
+		if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm.ends, nbPart, SharedVel{sm.vel});
+		else sceneIterate(w, sc, sid, sp, sm.ends, nbPart, GlobalVel{w.vel + sc.solverStart});
 	}
 }
 
@@ -904,7 +948,8 @@ struct World
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solveSmemBytes(world::STAGE_WARPS))));
 		GBPX_CUDA_TRY(gridFor(world::batchKernel, sms, gridBatch, solveSmemBytes(world::STAGE_WARPS)));
 		GBPX_CUDA_TRY(gridFor(world::prepKernel, sms, gridPrep));
-		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::STAGE_WARPS))));
+		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve, iterSmemBytes(world::STAGE_WARPS)));
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 		return GBPX_OK;
@@ -921,6 +966,7 @@ struct World
 	}
 	static size_t bpSmemBytes(uint32_t warps) { return warps * sizeof(world::BpSmem); }
 	static size_t solveSmemBytes(uint32_t warps) { return warps * sizeof(world::SolveSmem); }
+	static size_t iterSmemBytes(uint32_t warps) { return warps * sizeof(world::IterSmem); }
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
 	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid, size_t smem = 0)
 	{
@@ -952,7 +998,7 @@ struct World
 			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
-		world::solveKernel<<<gSolve, threads, 0, stream>>>(w, params);
+		world::solveKernel<<<gSolve, threads, iterSmemBytes(threads / 32), stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
