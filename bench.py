@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--cpu-scenes", type=int, default=1024, help="scenes in the bounded CPU-baseline sample")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--plain-scenes", type=int, default=256, help="scenes timed one-per-launch for the plain comparison")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the Poisson serving run (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=20000.0, help="request arrivals per second")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the serving pool")
     return ap.parse_args()
 
 
@@ -274,6 +277,14 @@ def main():
         pool.close()
     if rank != 0:
         return
+    w.release()
+    serving = None
+    if a.serve_seconds > 0:
+        from physx_gb300.serve_load import run_poisson
+        serving = run_poisson(duration=a.serve_seconds, rate=a.serve_rate, budget_bytes=a.serve_budget_gb * 1e9, seed=a.seed + 1)
+        serving["workload"] = ("Poisson %.0f req/s of 'advance scene k by n~U{1..8} steps' over a pool of scenes log-uniform [16,4096] "
+                               "bodies admitted against a %.0f GB budget, retired after U(500,5000) steps; %.0f s run" %
+                               (a.serve_rate, a.serve_budget_gb, a.serve_seconds))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
@@ -285,9 +296,8 @@ def main():
                                batched_over_plain=value / plain_value),
                 roofline=roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps * info["kernels_per_step"],
                 contacts_per_s=st["contacts"] * a.steps / (ms / 1000.0), pairs_per_s=st["pairs"] * a.steps / (ms / 1000.0),
-                status_nonzero_scenes=int((status != 0).sum()))
+                status_nonzero_scenes=int((status != 0).sum()), serving=serving)
     print(json.dumps(line))
-    w.release()
 
 
 if __name__ == "__main__":

@@ -132,6 +132,35 @@ int gbpx_world_time_plain(void* world, uint32_t firstScene, uint32_t nbScenes, f
 int gbpx_world_stats(void* world, uint64_t* out3);
 int gbpx_world_step_host(void* world, const void* rigidIn, void* rigidOut, uint32_t nbSteps, int useGraph, float* outMs);
 int gbpx_host_alloc(size_t bytes, void** out);
+
+/* ------------------------------------------------------------- serving
+ * Request loop over a live pool of scenes resident in HBM (no reference
+ * counterpart: it drives the batched step above).  Scenes are admitted into
+ * fixed-capacity slots grouped by body-count class (class c: slots[c] slots of
+ * capacity[c] bodies, staticsPerSlot statics); each class steps on its own
+ * stream.  A request advances one scene by n steps; each pump issues, per
+ * class, one step over every scene that still owes steps (continuous
+ * batching), with at most two steps in flight per class, and completes
+ * requests whose steps have finished.  Latency runs from the request's
+ * arrival time to the host observing its last step done. */
+int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, const float* params,
+                       const uint32_t* iterations, uint32_t pairsPerBody, void** outServer);
+void gbpx_server_release(void* server);
+/* device bytes of one slot (for sizing a pool against a memory budget); not a status code */
+uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody);
+/* GBPX_ERR_BUDGET when no free slot of sufficient capacity exists */
+int gbpx_server_admit(void* server, uint32_t nbBodies, const void* rigidBodies, const int* types, const float* geoms, const float* friction,
+                      uint32_t nbStatics, const float* staticPoses, const int* staticTypes, const float* staticGeoms, uint32_t* outScene);
+/* GBPX_ERR_STATE while the scene still owes requested steps */
+int gbpx_server_retire(void* server, uint32_t scene);
+/* arrival: seconds on the server clock, negative for now */
+int gbpx_server_submit(void* server, uint32_t scene, uint32_t nbSteps, uint64_t tag, double arrival);
+int gbpx_server_pump(void* server, uint32_t* outIssued);
+int gbpx_server_clock(void* server, double* outSeconds);
+int gbpx_server_poll(void* server, uint64_t* outTags, double* outLatencySeconds, uint32_t capacity, uint32_t* outCount);
+int gbpx_server_read_scene(void* server, uint32_t scene, void* outRigidBodies);
+/* out4: body-steps completed, class steps completed, live scenes, steps in flight */
+int gbpx_server_stats(void* server, uint64_t* out4);
 void gbpx_host_free(void* p);
 
 #ifdef __cplusplus

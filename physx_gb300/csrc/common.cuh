@@ -91,4 +91,13 @@ __device__ __forceinline__ uint32_t laneMaskLt()
 	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
 	return m;
 }
+
+// Asynchronous 16-byte global -> shared copy (cp.async; complete in the issuing
+// thread after cpAsyncWaitAll).  Both addresses must be 16-byte aligned.
+__device__ __forceinline__ void cpAsync16(void* smem, const void* gmem)
+{
+	const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 } // namespace gbpx

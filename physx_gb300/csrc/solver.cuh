@@ -76,6 +76,12 @@ struct __align__(16) ConstraintRecord
 	}
 	__device__ __forceinline__ float* force() { return reinterpret_cast<float*>(friction() + nbFriction()); }
 	__device__ __forceinline__ float* frictionForce() { return force() + nbPoints(); }
+	// bytes the header and packed rows occupy
+	__device__ __forceinline__ uint32_t bytes() const
+	{
+		return 16u + uint32_t(nbPatches) * uint32_t(sizeof(PatchRows)) + uint32_t(nbPoints()) * uint32_t(sizeof(PointRow) + 4) +
+		       uint32_t(nbFriction()) * uint32_t(sizeof(FrictionRow) + 4);
+	}
 };
 
 // ------------------------------------------------------------- bodies

@@ -29,6 +29,8 @@
 #include <vector>
 #include <algorithm>
 #include <numeric>
+#include <chrono>
+#include <deque>
 
 namespace gbpx
 {
@@ -57,8 +59,8 @@ struct StepParams
 struct WorldDev
 {
 	const SceneDesc* scenes;
-	const uint32_t* workOrder;
-	uint32_t nbScenes;
+	const uint32_t* workOrder;  // scenes to step, largest first
+	const uint32_t* nbActive;   // entries of workOrder to step (device word, so a captured step serves any scene set)
 	uint32_t* workCounter;
 	tgs::RigidBody* bodies;
 	const int* types;
@@ -94,6 +96,7 @@ struct WorldDev
 	uint32_t* nbConstraints;   // per scene: constraints (pairs with contacts) of this step
 	uint32_t* nbPartitions;    // per scene: partitions, 0 when batching overflowed
 	uint32_t* prepQueue;       // constraint slots of all scenes, for the row-preparation kernel
+	uint8_t* recChunks;        // per constraint slot: 16-byte chunks its packed rows occupy
 };
 
 // Pair kinds: shape types ordered (t0 <= t1), code t0 * 4 + t1.  Dynamic
@@ -429,6 +432,7 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 // body (scenes of up to SOLVE_SMEM_BODIES solver bodies) and the partition
 // offsets.
 constexpr uint32_t SOLVE_SMEM_BODIES = 544;
+constexpr uint32_t SOLVE_SMEM_CONSTRAINTS = 1024;
 struct SolveSmem
 {
 	uint32_t progress[SOLVE_SMEM_BODIES];        // partition bits of the current round
@@ -436,6 +440,8 @@ struct SolveSmem
 	uint32_t maxStatic[SOLVE_SMEM_BODIES];       // static constraints of the body
 	uint32_t staticProgress[SOLVE_SMEM_BODIES];
 	uint32_t perPart[MAX_PARTITIONS];            // constraints per partition, then end offsets
+	uint32_t keys[SOLVE_SMEM_CONSTRAINTS];       // pair key of each constraint, in constraint order
+	uint16_t tags[SOLVE_SMEM_CONSTRAINTS];       // (round << 8) | partition, 0xffff for static constraints
 };
 
 // PxBatchConstraintsTGS partition rule for one scene (the rule is sequential
@@ -454,12 +460,19 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 	uint32_t* staticProgress = onChip ? sm.staticProgress : w.staticProgress + sc.solverStart;
 	uint32_t* perPart = sm.perPart;
 	const uint32_t* cons = w.consList + sc.pairStart;
-	uint32_t* tag = w.tag + sc.pairStart;
 	uint32_t* ordered = w.ordered + sc.pairStart;
+	// the walk below is sequential: its operands sit in shared memory when they fit
+	const bool consOnChip = nc <= SOLVE_SMEM_CONSTRAINTS;
 	for(uint32_t b = lane; b < n; b += 32) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
 	for(uint32_t p = lane; p < MAX_PARTITIONS; p += 32) perPart[p] = 0;
-	for(uint32_t c = lane; c < nc; c += 32) tag[c] = 0;
+	if(consOnChip)
+		for(uint32_t c = lane; c < nc; c += 32) { sm.keys[c] = w.pairs[sc.pairStart + cons[c]]; sm.tags[c] = 0; }
+	else
+		for(uint32_t c = lane; c < nc; c += 32) w.tag[sc.pairStart + c] = 0;
 	__syncwarp();
+	auto keyOf = [&](uint32_t c) { return consOnChip ? sm.keys[c] : w.pairs[sc.pairStart + cons[c]]; };
+	auto getTag = [&](uint32_t c) { return consOnChip ? uint32_t(sm.tags[c]) : w.tag[sc.pairStart + c]; };
+	auto setTag = [&](uint32_t c, uint32_t t) { if(consOnChip) sm.tags[c] = uint16_t(t); else w.tag[sc.pairStart + c] = t; };
 	// pass 1: dynamic-dynamic constraints take the lowest free partition bit;
 	// constraints that find none retry in the next round of 32 partitions
 	uint32_t nbPart = 0, maxRound = 0, fail = 0;
@@ -471,19 +484,19 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 			bool deferred = false;
 			for(uint32_t c = 0; c < nc; c++)
 			{
-				const uint32_t key = w.pairs[sc.pairStart + cons[c]];
+				const uint32_t key = keyOf(c);
 				const uint32_t a = key >> 16, b = key & 0xffffu;
 				if(a < n && b < n)
 				{
-					if((tag[c] >> 8) != round) continue;
+					if((getTag(c) >> 8) != round) continue;
 					const uint32_t mask = ~progress[a] & ~progress[b];
-					if(!mask) { tag[c] = (round + 1) << 8; deferred = true; continue; }
+					if(!mask) { setTag(c, (round + 1) << 8); deferred = true; continue; }
 					const uint32_t part = __ffs(mask) - 1;
 					progress[a] |= 1u << part;
 					progress[b] |= 1u << part;
 					const uint32_t gp = round * 32 + part;
 					if(gp >= MAX_PARTITIONS) { fail = 1; break; }
-					tag[c] = (round << 8) | gp;
+					setTag(c, (round << 8) | gp);
 					perPart[gp]++;
 					maxNormal[a] = max(maxNormal[a], gp + 1);
 					maxNormal[b] = max(maxNormal[b], gp + 1);
@@ -492,7 +505,7 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 				}
 				else if(round == 0)
 				{
-					tag[c] = 0xffffu;
+					setTag(c, 0xffffu);
 					if(a < n) maxStatic[a]++;
 					if(b < n) maxStatic[b]++;
 				}
@@ -526,11 +539,11 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 		for(uint32_t round = 0; round <= maxRound; round++)
 			for(uint32_t c = 0; c < nc; c++)
 			{
-				const uint32_t t = tag[c];
+				const uint32_t t = getTag(c);
 				if(t == 0xffffu)
 				{
 					if(round) continue;
-					const uint32_t key = w.pairs[sc.pairStart + cons[c]];
+					const uint32_t key = keyOf(c);
 					const uint32_t a = key >> 16, b = key & 0xffffu;
 					const uint32_t d = a < n ? a : b;
 					ordered[perPart[maxNormal[d] + staticProgress[d]++]++] = cons[c];
@@ -636,7 +649,9 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t slot, const
 		cs[c].dynamicFriction = mu;
 		cs[c].restitution = 0.0f;
 	}
-	tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, w.recs[slot]);
+	tgs::ConstraintRecord& rec = w.recs[slot];
+	tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec);
+	w.recChunks[slot] = uint8_t((rec.bytes() + 15) / 16);
 }
 
 // Velocities of one scene's solver bodies during the iterations: linear and
@@ -665,15 +680,33 @@ struct GlobalVel
 
 // Position iterations (each followed by integration), velocity iterations,
 // PxIntegrateSolverBodiesTGS and write-back of one scene.
+// Each lane stages the packed rows of the constraint it solves in shared
+// memory with asynchronous 16-byte copies (one memory round trip per
+// constraint instead of one per row), solves from there and writes the
+// updated impulses back.  Rows larger than the staging slot are used in place.
+constexpr uint32_t RECBUF_CHUNKS = 32;   // 512 bytes per lane
+struct __align__(16) IterSmem
+{
+	float4 recBuf[32][RECBUF_CHUNKS + 1];   // padded rows: lanes' slots start in different banks
+	VelSmem vel;
+	uint32_t ends[MAX_PARTITIONS];
+	uint8_t chunks[SOLVE_SMEM_CONSTRAINTS];
+};
+
 template <typename Vel>
-__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, const uint32_t* ends,
+__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, IterSmem& sm,
                                              uint32_t nbPart, const Vel& V)
 {
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
+	const uint32_t* ends = sm.ends;
 	tgs::BodyVel* vel = w.vel + sc.solverStart;
 	tgs::BodyTx* tx = w.tx + sc.solverStart;
 	Tr* pose = w.pose + sc.solverStart;
+	const uint32_t nc = nbPart ? ends[nbPart - 1] : 0;
+	const bool chunksOnChip = nc <= SOLVE_SMEM_CONSTRAINTS;
+	if(chunksOnChip)
+		for(uint32_t r = lane; r < nc; r += 32) sm.chunks[r] = w.recChunks[sc.pairStart + r];
 	for(uint32_t i = lane; i < nTot; i += 32) V.set(i, vel[i].lin, vel[i].ang);
 	__syncwarp();
 	const float stepDt = sp.dt / float(sp.nbPos);
@@ -688,16 +721,34 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 			const uint32_t end = ends[p];
 			for(uint32_t r = begin + lane; r < end; r += 32)
 			{
-				tgs::ConstraintRecord& rec = w.recs[sc.pairStart + r];
-				if(rec.nbPatches == 0) continue;
-				const uint32_t a = uint32_t(rec.bodyA), b = uint32_t(rec.bodyB);
+				tgs::ConstraintRecord* src = w.recs + sc.pairStart + r;
+				const uint32_t chunks = chunksOnChip ? sm.chunks[r] : w.recChunks[sc.pairStart + r];
+				tgs::ConstraintRecord* rec = src;
+				if(chunks <= RECBUF_CHUNKS)
+				{
+					float4* dst = sm.recBuf[lane];
+					const float4* g = reinterpret_cast<const float4*>(src);
+					for(uint32_t k = 0; k < chunks; k++) cpAsync16(dst + k, g + k);
+					cpAsyncWaitAll();
+					rec = reinterpret_cast<tgs::ConstraintRecord*>(dst);
+				}
+				if(rec->nbPatches == 0) continue;
+				const uint32_t a = uint32_t(rec->bodyA), b = uint32_t(rec->bodyB);
 				tgs::BodyVel b0, b1;
 				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = vel[a].dLin; b0.dAng = vel[a].dAng;
 				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = vel[b].dLin; b1.dAng = vel[b].dAng;
 				const bool dynB = b < n;
-				tgs::solveConstraint(rec, b0, b1, dynB, minPen, elapsed);
+				tgs::solveConstraint(*rec, b0, b1, dynB, minPen, elapsed);
 				V.set(a, b0.lin, b0.ang);
 				if(dynB) V.set(b, b1.lin, b1.ang);
+				if(rec != src)
+				{
+					// the impulses are the only rows the solve updates
+					const float* f = rec->force();
+					float* gf = src->force();
+					const int nf = rec->nbPoints() + rec->nbFriction();
+					for(int k = 0; k < nf; k++) gf[k] = f[k];
+				}
 			}
 			begin = end;
 			__syncwarp();
@@ -747,7 +798,7 @@ __global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams s
 		uint32_t item = 0;
 		if(lane == 0) item = atomicAdd(&w.workCounter[0], 1u);
 		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= w.nbScenes) break;
+		if(item >= *w.nbActive) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
 		sceneBroadphase(w, sc, sid, sp, sm);
@@ -764,7 +815,7 @@ __global__ void __launch_bounds__(128) batchKernel(WorldDev w, StepParams sp)
 		uint32_t item = 0;
 		if(lane == 0) item = atomicAdd(&w.workCounter[1], 1u);
 		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= w.nbScenes) break;
+		if(item >= *w.nbActive) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
 		sceneBatchStage(w, sc, sid, sp, sm);
@@ -778,13 +829,8 @@ __global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
 }
 
-struct IterSmem
-{
-	uint32_t ends[MAX_PARTITIONS];
-	VelSmem vel;
-};
-
-__global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
+constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the solve kernel
+__global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
 	IterSmem& sm = reinterpret_cast<IterSmem*>(stageSmem)[threadIdx.x >> 5];
@@ -794,15 +840,15 @@ __global__ void __launch_bounds__(128) solveKernel(WorldDev w, StepParams sp)
 		uint32_t item = 0;
 		if(lane == 0) item = atomicAdd(&w.workCounter[2], 1u);
 		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= w.nbScenes) break;
+		if(item >= *w.nbActive) break;
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
 		const uint32_t nbPart = w.nbPartitions[sid];
 		if(!nbPart && w.nbConstraints[sid]) continue;   // batching overflowed: the scene is left unchanged
 		for(uint32_t p = lane; p < nbPart; p += 32) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
 		__syncwarp();
-		if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm.ends, nbPart, SharedVel{sm.vel});
-		else sceneIterate(w, sc, sid, sp, sm.ends, nbPart, GlobalVel{w.vel + sc.solverStart});
+		if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm, nbPart, SharedVel{sm.vel});
+		else sceneIterate(w, sc, sid, sp, sm, nbPart, GlobalVel{w.vel + sc.solverStart});
 	}
 }
 
@@ -846,7 +892,8 @@ struct World
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
 	DevBuf<world::SceneDesc> scenes;
-	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue;
+	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue, activeCount;
+	DevBuf<uint8_t> recChunks;
 	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
 	    staticProgress, partEnds, status;
 	DevBuf<tgs::RigidBody> bodies;
@@ -872,7 +919,7 @@ struct World
 	world::WorldDev dev()
 	{
 		world::WorldDev w;
-		w.scenes = scenes.ptr; w.workOrder = workOrder.ptr; w.nbScenes = nbScenes; w.workCounter = workCounter.ptr;
+		w.scenes = scenes.ptr; w.workOrder = workOrder.ptr; w.nbActive = activeCount.ptr; w.workCounter = workCounter.ptr;
 		w.bodies = bodies.ptr; w.types = types.ptr; w.geoms = geoms.ptr; w.friction = friction.ptr;
 		w.staticPose = staticPose.ptr; w.staticTypes = staticTypes.ptr; w.staticGeoms = staticGeoms.ptr;
 		w.aabb = aabb.ptr; w.keys = keys.ptr; w.pairs = pairs.ptr; w.pairCount = pairCount.ptr; w.contacts = contacts.ptr;
@@ -880,7 +927,7 @@ struct World
 		w.vel = vel.ptr; w.tx = tx.ptr; w.data = data.ptr; w.pose = pose.ptr; w.progress = progress.ptr; w.maxNormal = maxNormal.ptr;
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
 		w.typeCount = workCounter.ptr + 8; w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
-		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr;
+		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.recChunks = recChunks.ptr;
 		return w;
 	}
 
@@ -908,7 +955,7 @@ struct World
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
 		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
+		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || activeCount.reserve(2) || recChunks.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
 		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
 		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
 		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
@@ -929,11 +976,24 @@ struct World
 		std::vector<uint32_t> ident(S);
 		std::iota(ident.begin(), ident.end(), 0u);
 		GBPX_CUDA_TRY(cudaMemcpyAsync(identity.ptr, ident.data(), S * 4, cudaMemcpyHostToDevice, s));
-		GBPX_CUDA_TRY(cudaMemcpyAsync(bodies.ptr, rigid, size_t(b) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, s));
-		GBPX_CUDA_TRY(cudaMemcpyAsync(types.ptr, typesIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
-		GBPX_CUDA_TRY(cudaMemcpyAsync(geoms.ptr, geomsIn, size_t(b) * 16, cudaMemcpyHostToDevice, s));
-		GBPX_CUDA_TRY(cudaMemcpyAsync(friction.ptr, frictionIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
-		if(st)
+		const uint32_t activeInit[2] = {S, 1u};   // all scenes; one scene (the unbatched path)
+		GBPX_CUDA_TRY(cudaMemcpyAsync(activeCount.ptr, activeInit, 8, cudaMemcpyHostToDevice, s));
+		if(!rigid)
+		{
+			// capacity only (serving slots): contents arrive with each admitted scene
+			GBPX_CUDA_TRY(cudaMemsetAsync(bodies.ptr, 0, size_t(b) * sizeof(tgs::RigidBody), s));
+			GBPX_CUDA_TRY(cudaMemsetAsync(types.ptr, 0, size_t(b) * 4, s));
+			GBPX_CUDA_TRY(cudaMemsetAsync(geoms.ptr, 0, size_t(b) * 16, s));
+			GBPX_CUDA_TRY(cudaMemsetAsync(friction.ptr, 0, size_t(b) * 4, s));
+		}
+		else
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(bodies.ptr, rigid, size_t(b) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, s));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(types.ptr, typesIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(geoms.ptr, geomsIn, size_t(b) * 16, cudaMemcpyHostToDevice, s));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(friction.ptr, frictionIn, size_t(b) * 4, cudaMemcpyHostToDevice, s));
+		}
+		if(st && staticPoseIn)
 		{
 			GBPX_CUDA_TRY(cudaMemcpyAsync(staticPose.ptr, staticPoseIn, size_t(st) * 28, cudaMemcpyHostToDevice, s));
 			GBPX_CUDA_TRY(cudaMemcpyAsync(staticTypes.ptr, staticTypesIn, size_t(st) * 4, cudaMemcpyHostToDevice, s));
@@ -948,8 +1008,8 @@ struct World
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solveSmemBytes(world::STAGE_WARPS))));
 		GBPX_CUDA_TRY(gridFor(world::batchKernel, sms, gridBatch, solveSmemBytes(world::STAGE_WARPS)));
 		GBPX_CUDA_TRY(gridFor(world::prepKernel, sms, gridPrep));
-		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::STAGE_WARPS))));
-		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve, iterSmemBytes(world::STAGE_WARPS)));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::SOLVE_WARPS))));
+		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve, iterSmemBytes(world::SOLVE_WARPS), world::SOLVE_WARPS * 32));
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 		return GBPX_OK;
@@ -968,10 +1028,10 @@ struct World
 	static size_t solveSmemBytes(uint32_t warps) { return warps * sizeof(world::SolveSmem); }
 	static size_t iterSmemBytes(uint32_t warps) { return warps * sizeof(world::IterSmem); }
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
-	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid, size_t smem = 0)
+	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid, size_t smem = 0, int threads = 128)
 	{
 		int perSm = 0;
-		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, 128, smem);
+		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, threads, smem);
 		grid = uint32_t(sms * (perSm > 0 ? perSm : 1));
 		return e;
 	}
@@ -987,7 +1047,7 @@ struct World
 		if(plain)
 		{
 			w.workOrder = identity.ptr + plainScene;
-			w.nbScenes = 1;
+			w.nbActive = activeCount.ptr + 1;
 			gBp = gBatch = gSolve = 1;
 			gPrep = std::min(gridPrep, 8u);
 			threads = 32;
@@ -998,7 +1058,8 @@ struct World
 			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
-		world::solveKernel<<<gSolve, threads, iterSmemBytes(threads / 32), stream>>>(w, params);
+		const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
+		world::solveKernel<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32), stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
@@ -1053,12 +1114,37 @@ struct World
 		return GBPX_OK;
 	}
 
+	// Places a scene into slot `slot` (capacity fixed at creation): its bodies,
+	// shapes and statics are copied in and the slot's live counts updated, in
+	// stream order with the steps.
+	int admit(uint32_t slot, uint32_t nb, const void* rigid, const int* typesIn, const float* geomsIn, const float* frictionIn, uint32_t ns,
+	          const float* staticPoseIn, const int* staticTypesIn, const float* staticGeomsIn)
+	{
+		world::SceneDesc& d = hScenes[slot];
+		const uint32_t b = d.bodyStart, st = d.staticStart;
+		GBPX_CUDA_TRY(cudaMemcpyAsync(bodies.ptr + b, rigid, size_t(nb) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, stream));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(types.ptr + b, typesIn, size_t(nb) * 4, cudaMemcpyHostToDevice, stream));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(geoms.ptr + b, geomsIn, size_t(nb) * 16, cudaMemcpyHostToDevice, stream));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(friction.ptr + b, frictionIn, size_t(nb) * 4, cudaMemcpyHostToDevice, stream));
+		if(ns)
+		{
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticPose.ptr + 7 * size_t(st), staticPoseIn, size_t(ns) * 28, cudaMemcpyHostToDevice, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticTypes.ptr + st, staticTypesIn, size_t(ns) * 4, cudaMemcpyHostToDevice, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(staticGeoms.ptr + st, staticGeomsIn, size_t(ns) * 16, cudaMemcpyHostToDevice, stream));
+		}
+		d.nbBodies = nb;
+		d.nbStatics = ns;
+		GBPX_CUDA_TRY(cudaMemcpyAsync(scenes.ptr + slot, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
+		GBPX_CUDA_TRY(cudaMemsetAsync(status.ptr + slot, 0, 4, stream));
+		return GBPX_OK;
+	}
+
 	void release()
 	{
 		if(stream) cudaStreamSynchronize(stream);
 		if(graphExec) cudaGraphExecDestroy(graphExec);
 		graphExec = nullptr;
-		scenes.release(); typeQueue.release(); slotScene.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
+		scenes.release(); typeQueue.release(); slotScene.release(); activeCount.release(); recChunks.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
@@ -1286,4 +1372,323 @@ GBPX_API int gbpx_host_alloc(size_t bytes, void** out)
 GBPX_API void gbpx_host_free(void* p)
 {
 	if(p) cudaFreeHost(p);
+}
+
+// ------------------------------------------------------------------ serving
+// A request loop over a live pool of scenes kept resident in HBM.  Scenes are
+// admitted into fixed-capacity slots grouped by body-count class; each class
+// is a lane (a world of slots with its own stream and captured step), so
+// small scenes never wait behind large ones.  A request "advance scene k by n
+// steps" queues behind the scene's earlier requests; every pump issues one
+// step per lane over the scenes that still owe steps (continuous batching:
+// requests that arrive while a step runs join the next one), with up to two
+// steps in flight per lane.  A scene's arithmetic does not depend on which
+// other scenes share its step.
+namespace gbpx
+{
+struct Server
+{
+	struct Request { uint64_t tag; uint64_t target; double arrival; };
+	struct Scene { uint32_t lane = 0, slot = 0, nbBodies = 0; bool live = false; uint64_t requested = 0, issued = 0, done = 0; std::deque<Request> reqs; };
+	struct Lane
+	{
+		World w;
+		uint32_t capacity = 0, staticCap = 0, base = 0, slots = 0;
+		std::vector<uint32_t> freeSlots;
+		uint32_t* pinned[2] = {nullptr, nullptr};   // active list + count per in-flight step
+		cudaEvent_t ev[2] = {nullptr, nullptr};
+		std::vector<uint32_t> inflight[2];
+		int head = 0, nbInflight = 0;
+	};
+	std::vector<Lane*> lanes;
+	std::vector<Scene> scenes;
+	std::vector<uint64_t> doneTags;
+	std::vector<double> doneLatency;
+	uint64_t bodySteps = 0, steps = 0;
+	std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+
+	double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+
+	// Device bytes of one slot of `capacity` bodies and `statics` statics (the world layout).
+	static size_t slotBytes(uint32_t capacity, uint32_t statics, uint32_t pairsPerBody)
+	{
+		const size_t pair = World::pow2(capacity * pairsPerBody + capacity * statics);
+		const size_t key = World::pow2(capacity);
+		return pair * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + 4 + 4 + sizeof(tgs::ConstraintRecord)) + size_t(capacity) * (96 + 4 + 16 + 4 + 24) +
+		       size_t(capacity + statics) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + key * 8 +
+		       statics * 48 + world::MAX_PARTITIONS * 4 + 64;
+	}
+
+	int create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, uint32_t pairsPerBody,
+	           const world::StepParams& sp)
+	{
+		uint32_t base = 0;
+		for(uint32_t c = 0; c < nbClasses; c++)
+		{
+			if(!slots[c]) continue;
+			Lane* L = new Lane;
+			lanes.push_back(L);
+			L->capacity = capacity[c];
+			L->slots = slots[c];
+			L->staticCap = staticsPerSlot;
+			L->base = base;
+			std::vector<uint32_t> cap(slots[c], capacity[c]), st(slots[c], staticsPerSlot);
+			int rc = L->w.create(slots[c], cap.data(), st.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, pairsPerBody, sp);
+			if(rc) return rc;
+			rc = L->w.capture(1);
+			if(rc) return rc;
+			for(uint32_t k = slots[c]; k > 0; k--) L->freeSlots.push_back(k - 1);
+			for(int i = 0; i < 2; i++)
+			{
+				GBPX_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&L->pinned[i]), (size_t(slots[c]) + 1) * 4, cudaHostAllocDefault));
+				GBPX_CUDA_TRY(cudaEventCreateWithFlags(&L->ev[i], cudaEventDisableTiming));
+			}
+			base += slots[c];
+		}
+		scenes.resize(base);
+		return lanes.empty() ? GBPX_ERR_INVALID : GBPX_OK;
+	}
+
+	int admit(uint32_t nb, const void* rigid, const int* types, const float* geoms, const float* friction, uint32_t ns, const float* staticPoses,
+	          const int* staticTypes, const float* staticGeoms, uint32_t* outScene)
+	{
+		Lane* best = nullptr;
+		for(Lane* L : lanes)
+			if(L->capacity >= nb && !L->freeSlots.empty() && ns <= L->staticCap &&
+			   (!best || L->capacity < best->capacity))
+				best = L;
+		if(!best) return GBPX_ERR_BUDGET;
+		const uint32_t slot = best->freeSlots.back();
+		const int rc = best->w.admit(slot, nb, rigid, types, geoms, friction, ns, staticPoses, staticTypes, staticGeoms);
+		if(rc) return rc;
+		best->freeSlots.pop_back();
+		const uint32_t id = best->base + slot;
+		Scene& s = scenes[id];
+		s = Scene();
+		s.lane = uint32_t(std::find(lanes.begin(), lanes.end(), best) - lanes.begin());
+		s.slot = slot;
+		s.nbBodies = nb;
+		s.live = true;
+		*outScene = id;
+		return GBPX_OK;
+	}
+
+	int retire(uint32_t id)
+	{
+		if(id >= scenes.size() || !scenes[id].live) return GBPX_ERR_INVALID;
+		Scene& s = scenes[id];
+		if(s.done != s.requested) return GBPX_ERR_STATE;   // owes steps
+		s.live = false;
+		lanes[s.lane]->freeSlots.push_back(s.slot);
+		return GBPX_OK;
+	}
+
+	int submit(uint32_t id, uint32_t nbSteps, uint64_t tag, double arrival)
+	{
+		if(id >= scenes.size() || !scenes[id].live || !nbSteps) return GBPX_ERR_INVALID;
+		Scene& s = scenes[id];
+		s.requested += nbSteps;
+		s.reqs.push_back(Request{tag, s.requested, arrival < 0.0 ? now() : arrival});
+		return GBPX_OK;
+	}
+
+	// Completes finished steps and issues new ones; returns the number of steps issued.
+	int pump(uint32_t* outIssued)
+	{
+		uint32_t issued = 0;
+		for(Lane* L : lanes)
+		{
+			while(L->nbInflight)
+			{
+				const int tail = (L->head + 2 - L->nbInflight) & 1;
+				const cudaError_t q = cudaEventQuery(L->ev[tail]);
+				if(q == cudaErrorNotReady) break;
+				if(q != cudaSuccess) return GBPX_ERR_CUDA;
+				const double t = now();
+				for(uint32_t slot : L->inflight[tail])
+				{
+					Scene& s = scenes[L->base + slot];
+					s.done++;
+					bodySteps += s.nbBodies;
+					while(!s.reqs.empty() && s.reqs.front().target <= s.done)
+					{
+						doneTags.push_back(s.reqs.front().tag);
+						doneLatency.push_back(t - s.reqs.front().arrival);
+						s.reqs.pop_front();
+					}
+				}
+				steps++;
+				L->nbInflight--;
+			}
+			if(L->nbInflight == 2) continue;
+			std::vector<uint32_t>& list = L->inflight[L->head];
+			list.clear();
+			for(uint32_t slot = 0; slot < L->slots; slot++)
+			{
+				const Scene& s = scenes[L->base + slot];
+				if(s.live && s.issued < s.requested) list.push_back(slot);
+			}
+			if(list.empty()) continue;
+			std::stable_sort(list.begin(), list.end(),
+			                 [&](uint32_t x, uint32_t y) { return scenes[L->base + x].nbBodies > scenes[L->base + y].nbBodies; });
+			uint32_t* buf = L->pinned[L->head];
+			std::copy(list.begin(), list.end(), buf);
+			buf[L->slots] = uint32_t(list.size());
+			GBPX_CUDA_TRY(cudaMemcpyAsync(L->w.workOrder.ptr, buf, list.size() * 4, cudaMemcpyHostToDevice, L->w.stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(L->w.activeCount.ptr, buf + L->slots, 4, cudaMemcpyHostToDevice, L->w.stream));
+			GBPX_CUDA_TRY(cudaGraphLaunch(L->w.graphExec, L->w.stream));
+			GBPX_CUDA_TRY(cudaEventRecord(L->ev[L->head], L->w.stream));
+			for(uint32_t slot : list) scenes[L->base + slot].issued++;
+			L->head ^= 1;
+			L->nbInflight++;
+			issued++;
+		}
+		if(outIssued) *outIssued = issued;
+		return GBPX_OK;
+	}
+
+	int readScene(uint32_t id, void* out)
+	{
+		if(id >= scenes.size() || !scenes[id].live) return GBPX_ERR_INVALID;
+		const Scene& s = scenes[id];
+		Lane* L = lanes[s.lane];
+		GBPX_CUDA_TRY(cudaStreamSynchronize(L->w.stream));
+		GBPX_CUDA_TRY(cudaMemcpy(out, L->w.bodies.ptr + L->w.hScenes[s.slot].bodyStart, size_t(s.nbBodies) * sizeof(tgs::RigidBody),
+		                         cudaMemcpyDeviceToHost));
+		return GBPX_OK;
+	}
+
+	void release()
+	{
+		for(Lane* L : lanes)
+		{
+			L->w.release();
+			for(int i = 0; i < 2; i++)
+			{
+				if(L->pinned[i]) cudaFreeHost(L->pinned[i]);
+				if(L->ev[i]) cudaEventDestroy(L->ev[i]);
+			}
+			delete L;
+		}
+		lanes.clear();
+	}
+};
+} // namespace gbpx
+
+using gbpx::Server;
+
+// Creates a serving pool: nbClasses body-count classes, class c holding
+// slots[c] slots of capacity[c] bodies and staticsPerSlot statics each.
+// params/iterations as gbpx_world_create.
+GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, const float* params,
+                                const uint32_t* iterations, uint32_t pairsPerBody, void** outServer)
+{
+	if(!outServer || !nbClasses || !capacity || !slots || !params || !iterations || !iterations[0] || !iterations[1] || !pairsPerBody)
+		return GBPX_ERR_INVALID;
+	for(uint32_t c = 0; c < nbClasses; c++)
+		if(!capacity[c] || capacity[c] + staticsPerSlot > 65535u) return GBPX_ERR_INVALID;
+	gbpx::world::StepParams sp;
+	sp.dt = params[0]; sp.gx = params[1]; sp.gy = params[2]; sp.gz = params[3];
+	sp.contactDistance = params[4]; sp.toleranceLength = params[5]; sp.boundsMargin = params[6];
+	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
+	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
+	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
+	Server* s = new Server;
+	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);
+	if(rc) { s->release(); delete s; return rc; }
+	*outServer = s;
+	return GBPX_OK;
+}
+
+GBPX_API void gbpx_server_release(void* s)
+{
+	if(!s) return;
+	static_cast<Server*>(s)->release();
+	delete static_cast<Server*>(s);
+}
+
+// Device bytes one slot of a class takes (for sizing a pool against a memory budget).
+GBPX_API uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody)
+{
+	return Server::slotBytes(capacity, staticsPerSlot, pairsPerBody);
+}
+
+// Admits a scene (layout as one scene of gbpx_world_create) into the smallest
+// free slot that holds it; GBPX_ERR_BUDGET when none is free.
+GBPX_API int gbpx_server_admit(void* sv, uint32_t nbBodies, const void* rigidBodies, const int* types, const float* geoms, const float* friction,
+                               uint32_t nbStatics, const float* staticPoses, const int* staticTypes, const float* staticGeoms, uint32_t* outScene)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !nbBodies || !rigidBodies || !types || !geoms || !friction || !outScene || (nbStatics && (!staticPoses || !staticTypes || !staticGeoms)))
+		return GBPX_ERR_INVALID;
+	for(uint32_t i = 0; i < nbBodies; i++)
+		if(uint32_t(types[i]) > 3u || types[i] == 1) return GBPX_ERR_INVALID;
+	return s->admit(nbBodies, rigidBodies, types, geoms, friction, nbStatics, staticPoses, staticTypes, staticGeoms, outScene);
+}
+
+// Frees a scene's slot; GBPX_ERR_STATE while it still owes requested steps.
+GBPX_API int gbpx_server_retire(void* sv, uint32_t scene)
+{
+	Server* s = static_cast<Server*>(sv);
+	return s ? s->retire(scene) : GBPX_ERR_INVALID;
+}
+
+// Queues "advance `scene` by nbSteps"; `arrival` (seconds on the server clock,
+// negative = now) is the time latency is measured from.
+GBPX_API int gbpx_server_submit(void* sv, uint32_t scene, uint32_t nbSteps, uint64_t tag, double arrival)
+{
+	Server* s = static_cast<Server*>(sv);
+	return s ? s->submit(scene, nbSteps, tag, arrival) : GBPX_ERR_INVALID;
+}
+
+GBPX_API int gbpx_server_pump(void* sv, uint32_t* outIssued)
+{
+	Server* s = static_cast<Server*>(sv);
+	return s ? s->pump(outIssued) : GBPX_ERR_INVALID;
+}
+
+// Seconds since the server was created (the clock of arrivals and latencies).
+GBPX_API int gbpx_server_clock(void* sv, double* outSeconds)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !outSeconds) return GBPX_ERR_INVALID;
+	*outSeconds = s->now();
+	return GBPX_OK;
+}
+
+// Completed requests since the last poll: tags and latencies (seconds).
+GBPX_API int gbpx_server_poll(void* sv, uint64_t* outTags, double* outLatency, uint32_t capacity, uint32_t* outCount)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !outCount) return GBPX_ERR_INVALID;
+	const uint32_t n = uint32_t(std::min<size_t>(capacity, s->doneTags.size()));
+	for(uint32_t i = 0; i < n; i++)
+	{
+		if(outTags) outTags[i] = s->doneTags[i];
+		if(outLatency) outLatency[i] = s->doneLatency[i];
+	}
+	s->doneTags.erase(s->doneTags.begin(), s->doneTags.begin() + n);
+	s->doneLatency.erase(s->doneLatency.begin(), s->doneLatency.begin() + n);
+	*outCount = n;
+	return GBPX_OK;
+}
+
+// Bodies of a live scene (PxRigidBodyData) after its completed steps.
+GBPX_API int gbpx_server_read_scene(void* sv, uint32_t scene, void* outRigidBodies)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !outRigidBodies) return GBPX_ERR_INVALID;
+	return s->readScene(scene, outRigidBodies);
+}
+
+// out4: body-steps completed, lane steps completed, live scenes, steps in flight
+GBPX_API int gbpx_server_stats(void* sv, uint64_t* out4)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !out4) return GBPX_ERR_INVALID;
+	uint64_t live = 0, inflight = 0;
+	for(const auto& sc : s->scenes) live += sc.live ? 1 : 0;
+	for(const auto* L : s->lanes) inflight += L->nbInflight;
+	out4[0] = s->bodySteps; out4[1] = s->steps; out4[2] = live; out4[3] = inflight;
+	return GBPX_OK;
 }
