@@ -43,7 +43,8 @@ struct DevBuf
 	int reserve(size_t n, cudaStream_t s = 0, bool keep = false, size_t keepCount = 0)
 	{
 		if(n <= cap) return GBPX_OK;
-		size_t nc = cap ? cap : 256;
+		// first allocation exact (large resident pools); later growth doubles
+		size_t nc = cap ? cap : n;
 		while(nc < n) nc *= 2;
 		T* np = nullptr;
 		if(cudaMalloc(&np, nc * sizeof(T)) != cudaSuccess) return GBPX_ERR_NOMEM;
@@ -65,7 +66,8 @@ struct HostBuf
 	int reserve(size_t n, bool keep = false)
 	{
 		if(n <= cap) return GBPX_OK;
-		size_t nc = cap ? cap : 256;
+		// first allocation exact (large resident pools); later growth doubles
+		size_t nc = cap ? cap : n;
 		while(nc < n) nc *= 2;
 		T* np = nullptr;
 		if(cudaMallocHost(&np, nc * sizeof(T)) != cudaSuccess) return GBPX_ERR_NOMEM;
