@@ -441,7 +441,8 @@ struct SolveSmem
 	uint32_t staticProgress[SOLVE_SMEM_BODIES];
 	uint32_t perPart[MAX_PARTITIONS];            // constraints per partition, then end offsets
 	uint32_t keys[SOLVE_SMEM_CONSTRAINTS];       // pair key of each constraint, in constraint order
-	uint16_t tags[SOLVE_SMEM_CONSTRAINTS];       // (round << 8) | partition, 0xffff for static constraints
+	uint16_t tags[SOLVE_SMEM_CONSTRAINTS];       // (round << 8) | partition; 0x8000 | rank for static constraints
+	uint32_t bucket[MAX_PARTITIONS * 4];         // (partition, placement round) counts, then offsets
 };
 
 // PxBatchConstraintsTGS partition rule for one scene (the rule is sequential
@@ -505,9 +506,10 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 				}
 				else if(round == 0)
 				{
-					setTag(c, 0xffffu);
-					if(a < n) maxStatic[a]++;
-					if(b < n) maxStatic[b]++;
+					// static constraint: tagged with its rank among the body's static constraints
+					const uint32_t d = a < n ? a : b;
+					setTag(c, 0x8000u | min(maxStatic[d], 0x7fffu));
+					maxStatic[d]++;
 				}
 			}
 			if(fail || !deferred) break;
@@ -532,26 +534,48 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 	nbPart = need;
 	__syncwarp();
 	warpExclusiveScan(perPart, nbPart);
-	// pass 2: round-0 dynamic constraints and all static constraints in input
-	// order, then each later round in input order
-	if(lane == 0)
+	// pass 2: a static constraint goes to partition maxNormal[body] + its rank
+	// among the body's static constraints; within a partition the reference
+	// places round-0 and static constraints in input order, then each later
+	// round's constraints in input order.  That is a stable counting sort by
+	// (partition, placement round), done here by the whole warp.
+	uint32_t* bucket = sm.bucket;
+	const uint32_t nbBuckets = nbPart * 4;
+	for(uint32_t i = lane; i < nbBuckets; i += 32) bucket[i] = 0;
+	__syncwarp();
+	auto bucketOf = [&](uint32_t c) -> uint32_t {
+		const uint32_t t = getTag(c);
+		if(t & 0x8000u)
+		{
+			const uint32_t key = keyOf(c);
+			const uint32_t a = key >> 16, b = key & 0xffffu;
+			return (maxNormal[a < n ? a : b] + (t & 0x7fffu)) * 4;
+		}
+		return (t & 0xffu) * 4 + (t >> 8);
+	};
+	for(uint32_t c = lane; c < nc; c += 32) atomicAdd(&bucket[bucketOf(c)], 1u);
+	__syncwarp();
+	warpExclusiveScan(bucket, nbBuckets);
+	for(uint32_t base = 0; base < nc; base += 32)
 	{
-		for(uint32_t round = 0; round <= maxRound; round++)
-			for(uint32_t c = 0; c < nc; c++)
-			{
-				const uint32_t t = getTag(c);
-				if(t == 0xffffu)
-				{
-					if(round) continue;
-					const uint32_t key = keyOf(c);
-					const uint32_t a = key >> 16, b = key & 0xffffu;
-					const uint32_t d = a < n ? a : b;
-					ordered[perPart[maxNormal[d] + staticProgress[d]++]++] = cons[c];
-				}
-				else if((t >> 8) == round)
-					ordered[perPart[t & 0xffu]++] = cons[c];
-			}
+		const uint32_t c = base + lane;
+		const bool valid = c < nc;
+		const uint32_t b = valid ? bucketOf(c) : 0xffffffffu;
+		const uint32_t peers = __match_any_sync(0xffffffffu, b);
+		const uint32_t start = valid ? bucket[b] : 0;
+		__syncwarp();
+		if(valid)
+		{
+			ordered[start + __popc(peers & laneMaskLt())] = cons[c];
+			if(lane == uint32_t(__ffs(peers) - 1)) bucket[b] = start + __popc(peers);
+		}
+		__syncwarp();
 	}
+	// partition end offsets
+	uint32_t endv[MAX_PARTITIONS / 32];
+	for(uint32_t p = lane, k = 0; p < nbPart; p += 32, k++) endv[k] = p + 1 < nbPart ? perPart[p + 1] : nc;
+	__syncwarp();
+	for(uint32_t p = lane, k = 0; p < nbPart; p += 32, k++) perPart[p] = endv[k];
 	__syncwarp();
 	return nbPart;
 }

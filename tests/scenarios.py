@@ -218,3 +218,28 @@ def pile_scenes(seed, nb_scenes, n, **kw):
                 types=np.concatenate([o["types"] for o in out]), geoms=np.concatenate([o["geoms"] for o in out]),
                 friction=np.concatenate([o["friction"] for o in out]), static_poses=np.tile(plane_pose_y_up(), (nb_scenes, 1)),
                 static_types=np.ones(nb_scenes, np.int32), static_geoms=np.zeros((nb_scenes, 4), np.float32))
+
+
+def hub_scene(nb_spheres=40, seed=0):
+    """One wide box on the ground plane carrying `nb_spheres` separated spheres: the
+    box takes part in more than 32 dynamic constraints, so the batching needs a
+    second round of 32 partitions, and the plane adds a static constraint."""
+    from physx_gb300.workloads import mass_properties_batch, plane_pose_y_up, rigid_body_data
+    rng = np.random.default_rng(seed)
+    n = 1 + nb_spheres
+    types = np.array([3] + [0] * nb_spheres, np.int32)
+    geoms = np.zeros((n, 4), np.float32)
+    geoms[0, :3] = (5.0, 0.5, 5.0)
+    geoms[1:, 0] = 0.3
+    rb = rigid_body_data(n)
+    rb["p"][0] = (0.0, 0.49, 0.0)
+    k = np.arange(nb_spheres)
+    rb["p"][1:, 0] = (k % 7) * 1.2 - 3.6 + rng.uniform(-0.05, 0.05, nb_spheres)
+    rb["p"][1:, 2] = (k // 7) * 1.2 - 3.6 + rng.uniform(-0.05, 0.05, nb_spheres)
+    rb["p"][1:, 1] = 0.99 + 0.28 + rng.uniform(-0.01, 0.01, nb_spheres)
+    im, ii = mass_properties_batch(types, geoms)
+    rb["invMass"] = im
+    rb["invInertia"] = ii
+    return dict(body_count=np.array([n], np.uint32), static_count=np.ones(1, np.uint32), rigid=rb, types=types, geoms=geoms,
+                friction=np.full(n, 0.5, np.float32), static_poses=plane_pose_y_up()[None, :].copy(), static_types=np.ones(1, np.int32),
+                static_geoms=np.zeros((1, 4), np.float32))

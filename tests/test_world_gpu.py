@@ -86,3 +86,19 @@ def test_world_rejects_bad_input(cuda_device):
     bad["types"][0] = 1   # dynamic plane
     with pytest.raises(GbpxError):
         _world(bad)
+
+
+def test_world_multi_round_batching_matches_oracle(cuda_device):
+    """A body in more than 32 constraints: the second round of partitions and the
+    static constraint's placement after it follow the reference's rule."""
+    from physx_gb300.world import DEFAULT_PARAMS
+    from scenarios import hub_scene
+    scene = hub_scene()
+    w = _world(scene)
+    w.step(1)
+    out = w.get_bodies()
+    assert not w.status().any()
+    ref = run_scene_step("orc", scene, DEFAULT_PARAMS, steps=1)
+    assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5
+    assert np.abs(out["p"] - ref["p"]).max() <= 1e-6
+    w.release()
