@@ -74,6 +74,21 @@ int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type
                            const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
                            float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts);
 
+/* No counterpart in the reference: the same contact generation for callers
+ * that may not allocate device memory during the call (a cudaMalloc or
+ * cudaFree in a frame loop synchronises the device and fragments the pool;
+ * some host applications own all device memory through their own pools).
+ * Inputs and outputs are the caller's device arrays (layouts as above;
+ * dOutContacts holds 4 contacts x 8 floats per pair and is 16-byte aligned),
+ * the work is enqueued on `stream` (a cudaStream_t, NULL = default stream).
+ * Scratch is a fixed 1 MiB device array, so nbPairs <= 262144
+ * (GBPX_ERR_CAPACITY above).  The scratch is shared by every call on a
+ * device: calls that may overlap must be serialised by the caller.  The first
+ * call on a device looks the scratch address up. */
+int gbpx_generate_contacts_device_noalloc(const int* dType0, const float* dGeom0, const int* dType1, const float* dGeom1,
+                                          const float* dPose0, const float* dPose1, uint32_t nbPairs, float contactDistance,
+                                          float toleranceLength, float* dOutContacts, uint32_t* dOutCounts, void* stream);
+
 /* ---------------------------------------------------------------------- TGS
  * Rigid bodies use PxRigidBodyData (physx/include/PxImmediateMode.h:68, 96 B).
  *

@@ -173,3 +173,66 @@ GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const 
 	}
 	return rc;
 }
+
+// ------------------------------------------------------------------ no-allocation variant
+// The same narrowphase over caller-owned device arrays, with its bucketing
+// scratch (16 bin counters, 16 bin cursors and the pair permutation) in a
+// fixed file-scope device array instead of per-call allocations.
+namespace gbpx
+{
+constexpr uint32_t NP_NOALLOC_MAX_PAIRS = 262144;                  // 1 MiB of permutation
+constexpr uint32_t NP_NOALLOC_SCRATCH_WORDS = 32 + NP_NOALLOC_MAX_PAIRS;
+static __device__ __align__(256) uint32_t gNpNoAllocScratch[NP_NOALLOC_SCRATCH_WORDS];
+constexpr int NP_NOALLOC_MAX_DEVICES = 64;
+
+// Address of the scratch array on the current device, looked up once per device.
+static int npNoAllocScratch(uint32_t** out)
+{
+	static uint32_t* cache[NP_NOALLOC_MAX_DEVICES] = {};
+	int dev = 0;
+	GBPX_CUDA_TRY(cudaGetDevice(&dev));
+	if(dev < 0 || dev >= NP_NOALLOC_MAX_DEVICES) return GBPX_ERR_INVALID;
+	if(!cache[dev])
+	{
+		void* p = nullptr;
+		GBPX_CUDA_TRY(cudaGetSymbolAddress(&p, gNpNoAllocScratch));
+		cache[dev] = static_cast<uint32_t*>(p);
+	}
+	*out = cache[dev];
+	return GBPX_OK;
+}
+} // namespace gbpx
+
+// PxGenerateContacts over nbPairs pairs held in device memory (layouts as
+// gbpx_generate_contacts; contacts: 4 slots of 8 floats per pair, 16-byte
+// aligned), enqueued on `stream` (a cudaStream_t, NULL for the default
+// stream).  Allocates nothing: the bucketing scratch is a fixed 1 MiB device
+// array, so nbPairs is limited to 262144 (GBPX_ERR_CAPACITY above).  The
+// scratch is shared by all calls on a device: calls that may overlap (other
+// streams, other host threads) race and must be serialised by the caller.
+// The first call on a device looks up the scratch address.
+GBPX_API int gbpx_generate_contacts_device_noalloc(const int* dType0, const float* dGeom0, const int* dType1, const float* dGeom1,
+                                                   const float* dPose0, const float* dPose1, uint32_t nbPairs, float contactDistance,
+                                                   float toleranceLength, float* dOutContacts, uint32_t* dOutCounts, void* stream)
+{
+	if(!nbPairs) return GBPX_OK;
+	if(!dType0 || !dGeom0 || !dType1 || !dGeom1 || !dPose0 || !dPose1 || !dOutContacts || !dOutCounts) return GBPX_ERR_INVALID;
+	if(!(contactDistance > 0.0f) || !(toleranceLength > 0.0f)) return GBPX_ERR_INVALID;
+	if(reinterpret_cast<uintptr_t>(dOutContacts) & 15u) return GBPX_ERR_INVALID;
+	if(nbPairs > NP_NOALLOC_MAX_PAIRS) return GBPX_ERR_CAPACITY;
+	uint32_t* scratch = nullptr;
+	const int rc = npNoAllocScratch(&scratch);
+	if(rc) return rc;
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	// the bin counters start at zero; the cursors and the permutation are fully rewritten
+	GBPX_CUDA_TRY(cudaMemsetAsync(scratch, 0, 32 * 4, s));
+	np::PairRef pr = {dType0, dGeom0, dType1, dGeom1, dPose0, dPose1};
+	const uint32_t blocks = divUp(nbPairs, 256);
+	np::bucketCountKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch);
+	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(scratch);
+	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch + 16, scratch + 32);
+	np::generateKernel<<<divUp(nbPairs, 128), 128, 0, s>>>(pr, scratch + 32, nbPairs, contactDistance, toleranceLength,
+	                                                        reinterpret_cast<float4*>(dOutContacts), dOutCounts);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	return GBPX_OK;
+}
