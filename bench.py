@@ -150,14 +150,15 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """dram bytes per step-kernel launch from the committed ncu summary, scaled to the workload, if present."""
-    path = os.path.join(ROOT, "profiles", "step_kernel_batched.txt")
+def profiled_traffic(stage):
+    """DRAM bytes (read + write) per launch of a stage's kernel on the bench workload, from the
+    committed ncu summary (profiles/dram_traffic_world_step.txt, lines `<stage>: <bytes>`), if present."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_world_step.txt")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_body_step:"):
-                return float(line.split(":", 1)[1])
-    except OSError:
+            if line.startswith(stage + ":"):
+                return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError, IndexError):
         pass
     return None
 
@@ -261,15 +262,38 @@ def main():
         plain_bodies += int(counts[i])
     plain_value = plain_bodies / (plain_ms / 1000.0)
 
-    # roofline of the step kernel: compulsory HBM bytes per step (bodies read+written,
-    # pair records, contacts written and read) over the event-timed step
-    bytes_step = bodies * (96 + 52) + st["pairs"] * 108 + st["contacts"] * 64
-    achieved = bytes_step / (ms / a.steps / 1000.0) / 1e9
+    # Per-kernel device times (un-captured steps, CUDA events between the launches on
+    # the world's stream) and the roofline of the dominant kernel.  Algorithmic
+    # (compulsory) HBM bytes per launch, from the step's own counts:
+    #   broadphase   48 B per body (pose, type, shape) + 12 B per pair (key, kind queue)
+    #   narrowphase  108 B per pair (two poses and shapes, key, slot, count) + 32 B per contact
+    #   batching     280 B per body (PxRigidBodyData in, solver body records out) + 12 B per constraint
+    #   preparation  32 B per contact in + 2 x 184 B solver bodies per constraint + packed rows written
+    #   solve        packed rows read once per iteration, plus per body 48 B velocities in, per position
+    #                iteration 176 B of integration state, 124 B write-back
+    st = w.stats()
+    stage_ms = w.time_stages(max(3, a.steps // 3))
+    nbPos, nbVel = DEFAULT_PARAMS["nb_pos"], DEFAULT_PARAMS["nb_vel"]
+    np_ms = sum(v for k, v in stage_ms.items() if k.startswith("np "))
+    stage_bytes = {
+        "broadphase": bodies * 48 + st["pairs"] * 12,
+        "narrowphase": st["pairs"] * 108 + st["contacts"] * 32,
+        "batching": bodies * 280 + st["constraints"] * 12,
+        "row preparation": st["contacts"] * 32 + st["constraints"] * 368 + st["row_bytes"],
+        "solve": (nbPos + nbVel) * st["row_bytes"] + bodies * (48 + nbPos * 176 + 124),
+    }
+    stage_time = {"broadphase": stage_ms["broadphase"], "narrowphase": np_ms, "batching": stage_ms["batching"],
+                  "row preparation": stage_ms["row preparation"], "solve": stage_ms["solve"]}
     peak, peak_kind = measured_peak()
-    traffic_per_body = profiled_traffic()
-    roofline = dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
-                    traffic=(traffic_per_body * bodies if traffic_per_body else None), peak_source=peak_kind,
-                    algorithmic_bytes_per_step=bytes_step)
+    stages = {k: dict(ms=stage_time[k], gbs=stage_bytes[k] / (stage_time[k] / 1000.0) / 1e9, bytes=stage_bytes[k]) for k in stage_time}
+    dominant = max(stage_time, key=stage_time.get)
+    achieved = stages[dominant]["gbs"]
+    traffic = profiled_traffic(dominant)
+    roofline = dict(bound="hbm", kernel=dominant, achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                    traffic=traffic, peak_source=peak_kind, algorithmic_bytes_per_launch=stage_bytes[dominant],
+                    launch_ms=stage_time[dominant])
+    bytes_step = sum(stage_bytes.values())
+    step_roofline = dict(algorithmic_bytes_per_step=bytes_step, achieved=bytes_step / (ms / a.steps / 1000.0) / 1e9, unit="GB/s")
     cpu = None
     if rank == 0:
         cpu = cpu_baseline(dict(scenes, rigid=state), DEFAULT_PARAMS, a.cpu_scenes, a.cpu_steps, pool, cores)
@@ -294,7 +318,7 @@ def main():
                 e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=bodies * 96, d2h_bytes_per_step=bodies * 96),
                 plain_gpu=dict(value=plain_value, unit=UNIT, sample="%d scenes (%d bodies), one scene per launch" % (len(idx), plain_bodies),
                                batched_over_plain=value / plain_value),
-                roofline=roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps * info["kernels_per_step"],
+                roofline=roofline, stages=stages, step_roofline=step_roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps * info["kernels_per_step"],
                 contacts_per_s=st["contacts"] * a.steps / (ms / 1000.0), pairs_per_s=st["pairs"] * a.steps / (ms / 1000.0),
                 status_nonzero_scenes=int((status != 0).sum()), serving=serving)
     print(json.dumps(line))

@@ -144,7 +144,11 @@ int gbpx_world_scene_pairs(void* world, uint32_t scene, uint32_t* outKeys, uint3
                            uint32_t* outCount);
 int gbpx_world_time_steps(void* world, uint32_t nbSteps, int useGraph, float* outMs);
 int gbpx_world_time_plain(void* world, uint32_t firstScene, uint32_t nbScenes, float* outMs);
-int gbpx_world_stats(void* world, uint64_t* out3);
+/* out4: pairs, pairs with contacts, contacts, bytes of packed constraint rows (last step) */
+int gbpx_world_stats(void* world, uint64_t* out4);
+/* average device milliseconds per kernel of a step (un-captured steps, events
+ * between launches), in launch order; outMs has "kernels per step" entries */
+int gbpx_world_time_stages(void* world, uint32_t nbSteps, float* outMs);
 int gbpx_world_step_host(void* world, const void* rigidIn, void* rigidOut, uint32_t nbSteps, int useGraph, float* outMs);
 int gbpx_host_alloc(size_t bytes, void** out);
 

@@ -877,29 +877,36 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, Step
 }
 
 // Totals over all scenes after a step: pairs, pairs with contacts, contacts.
+// Totals of the last step: pairs, pairs with contacts, contacts, bytes of packed
+// constraint rows (what every solver iteration reads).
 __global__ void statsKernel(const SceneDesc* __restrict__ scenes, uint32_t nbScenes, const uint32_t* __restrict__ pairCount,
-                            const uint32_t* __restrict__ contactCount, unsigned long long* __restrict__ out)
+                            const uint32_t* __restrict__ contactCount, const uint32_t* __restrict__ nbConstraints,
+                            const uint32_t* __restrict__ nbPartitions, const uint8_t* __restrict__ recChunks, unsigned long long* __restrict__ out)
 {
 	const uint32_t sid = blockIdx.x;
 	if(sid >= nbScenes) return;
 	const SceneDesc sc = scenes[sid];
 	const uint32_t count = pairCount[sid];
-	unsigned long long withContacts = 0, contacts = 0;
+	const uint32_t nc = nbPartitions[sid] ? nbConstraints[sid] : 0;
+	unsigned long long withContacts = 0, contacts = 0, rowBytes = 0;
 	for(uint32_t k = threadIdx.x; k < count; k += blockDim.x)
 	{
 		const uint32_t c = contactCount[sc.pairStart + k];
 		withContacts += c ? 1 : 0;
 		contacts += c;
 	}
+	for(uint32_t r = threadIdx.x; r < nc; r += blockDim.x) rowBytes += 16ull * recChunks[sc.pairStart + r];
 	for(int o = 16; o > 0; o >>= 1)
 	{
 		withContacts += __shfl_down_sync(0xffffffffu, withContacts, o);
 		contacts += __shfl_down_sync(0xffffffffu, contacts, o);
+		rowBytes += __shfl_down_sync(0xffffffffu, rowBytes, o);
 	}
 	if((threadIdx.x & 31) == 0)
 	{
 		atomicAdd(&out[1], withContacts);
 		atomicAdd(&out[2], contacts);
+		atomicAdd(&out[3], rowBytes);
 	}
 	if(threadIdx.x == 0) atomicAdd(&out[0], static_cast<unsigned long long>(count));
 }
@@ -985,7 +992,7 @@ struct World
 		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
 		   vel.reserve(nbSolver) || tx.reserve(nbSolver) || data.reserve(nbSolver) || pose.reserve(nbSolver) || progress.reserve(nbSolver) ||
 		   maxNormal.reserve(nbSolver) || maxStatic.reserve(nbSolver) || staticProgress.reserve(nbSolver) ||
-		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(3) ||
+		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(4) ||
 		   identity.reserve(S))
 			return GBPX_ERR_NOMEM;
 		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
@@ -1124,6 +1131,46 @@ struct World
 				if(rc) return rc;
 			}
 		return GBPX_OK;
+	}
+
+	int timeStages(uint32_t steps, float* outMs)
+	{
+		const uint32_t K = KERNELS_PER_STEP;
+		std::vector<cudaEvent_t> ev(K + 1, nullptr);
+		for(auto& e : ev) GBPX_CUDA_TRY(cudaEventCreate(&e));
+		std::vector<double> acc(K, 0.0);
+		const world::WorldDev w = dev();
+		int rc = GBPX_OK;
+		for(uint32_t s = 0; s < steps && rc == GBPX_OK; s++)
+		{
+			GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
+			uint32_t k = 0;
+			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			world::broadphaseKernel<<<gridBlocks, 128, bpSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
+			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			for(uint32_t t = 0; t < world::NB_KINDS; t++)
+			{
+				npKernels()[t]<<<gridNp[t], 128, 0, stream>>>(w, params);
+				GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			}
+			world::batchKernel<<<gridBatch, 128, solveSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
+			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			world::prepKernel<<<gridPrep, 128, 0, stream>>>(w, params);
+			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			world::solveKernel<<<gridSolve, world::SOLVE_WARPS * 32, iterSmemBytes(world::SOLVE_WARPS), stream>>>(w, params);
+			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			GBPX_CUDA_TRY(cudaGetLastError());
+			GBPX_CUDA_TRY(cudaEventSynchronize(ev[K]));
+			for(uint32_t i = 0; i < K; i++)
+			{
+				float ms = 0.0f;
+				GBPX_CUDA_TRY(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+				acc[i] += ms;
+			}
+		}
+		for(uint32_t i = 0; i < K; i++) outMs[i] = float(acc[i] / steps);
+		for(auto& e : ev) cudaEventDestroy(e);
+		return rc;
 	}
 
 	// One scene per launch sequence: no batching across scenes, no graph, no
@@ -1343,17 +1390,30 @@ GBPX_API int gbpx_world_time_plain(void* wv, uint32_t first, uint32_t count, flo
 	return rc;
 }
 
-// Totals of the last step: pairs, pairs with contacts (constraints), contacts.
-GBPX_API int gbpx_world_stats(void* wv, uint64_t* out3)
+// Totals of the last step: pairs, pairs with contacts (constraints), contacts,
+// bytes of packed constraint rows.
+GBPX_API int gbpx_world_stats(void* wv, uint64_t* out4)
 {
 	World* w = static_cast<World*>(wv);
-	if(!w || !out3) return GBPX_ERR_INVALID;
-	GBPX_CUDA_TRY(cudaMemsetAsync(w->stats.ptr, 0, 3 * 8, w->stream));
-	gbpx::world::statsKernel<<<w->nbScenes, 256, 0, w->stream>>>(w->scenes.ptr, w->nbScenes, w->pairCount.ptr, w->contactCount.ptr, w->stats.ptr);
+	if(!w || !out4) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemsetAsync(w->stats.ptr, 0, 4 * 8, w->stream));
+	gbpx::world::statsKernel<<<w->nbScenes, 256, 0, w->stream>>>(w->scenes.ptr, w->nbScenes, w->pairCount.ptr, w->contactCount.ptr,
+	                                                              w->nbConstraints.ptr, w->nbPartitions.ptr, w->recChunks.ptr, w->stats.ptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
-	GBPX_CUDA_TRY(cudaMemcpyAsync(out3, w->stats.ptr, 3 * 8, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(out4, w->stats.ptr, 4 * 8, cudaMemcpyDeviceToHost, w->stream));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
 	return GBPX_OK;
+}
+
+// Average device time of each kernel of a step over nbSteps un-captured steps
+// (CUDA events between the launches on the world's stream), in launch order:
+// broadphase, the narrowphase kernels per pair kind, batching, row
+// preparation, solve.  outMs has KERNELS_PER_STEP entries (gbpx_world_info).
+GBPX_API int gbpx_world_time_stages(void* wv, uint32_t nbSteps, float* outMs)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !outMs || !nbSteps) return GBPX_ERR_INVALID;
+	return w->timeStages(nbSteps, outMs);
 }
 
 // End-to-end step through host memory: uploads the bodies from `rigidIn`

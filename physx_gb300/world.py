@@ -40,6 +40,7 @@ def _setup():
         L.gbpx_world_time_steps.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_time_plain.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_time_stages.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_float)]
         L.gbpx_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
@@ -122,9 +123,19 @@ class World:
         return ms.value
 
     def stats(self):
-        out = np.zeros(3, np.uint64)
+        out = np.zeros(4, np.uint64)
         check(self._L.gbpx_world_stats(self._h, _p(out)), "gbpx_world_stats")
-        return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]))
+        return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]), row_bytes=int(out[3]))
+
+    STAGES = ("broadphase", "np sphere-sphere", "np sphere-plane", "np sphere-capsule", "np sphere-box", "np plane-capsule",
+              "np plane-box", "np capsule-capsule", "np capsule-box", "np box-box", "batching", "row preparation", "solve")
+
+    def time_stages(self, n):
+        """Average device milliseconds per kernel of a step, {stage name: ms} (un-captured steps)."""
+        k = self.info()["kernels_per_step"]
+        out = np.zeros(k, np.float32)
+        check(self._L.gbpx_world_time_stages(self._h, n, _p(out)), "gbpx_world_time_stages")
+        return dict(zip(self.STAGES, (float(x) for x in out)))
 
     def step_host(self, rigid_in, rigid_out, n=1, graph=True):
         """Upload bodies from host memory, step, download; returns event-timed milliseconds."""
