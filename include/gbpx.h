@@ -118,6 +118,32 @@ int gbpx_tgs_solve(const void* rigidBodies, uint32_t nbDynamic, const float* sta
                    float* outVelocity, float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder,
                    uint32_t* outNbHeaders);
 
+/* Split-phase TGS on solver bodies in the reference's layouts, the stages a
+ * caller of physx::immediate drives itself (used by libgbpx_immediate.so):
+ *   PxConstructStaticSolverBodyTGS   physx/include/PxImmediateMode.h:601
+ *   PxCreateContactConstraintsTGS    physx/include/PxImmediateMode.h:642
+ *   PxSolveConstraintsTGS            physx/include/PxImmediateMode.h:716
+ *   PxIntegrateSolverBodiesTGS       physx/include/PxImmediateMode.h:729
+ * Constraint rows are this build's own format, gbpx_constraint_row_stride()
+ * bytes per constraint at most. */
+uint32_t gbpx_constraint_row_stride(void);
+int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void* outVel, void* outTxI, void* outData);
+/* one descriptor per constraint: both bodies' records (64/64/48 B), frames
+ * (PxTransform) and PxContactPoints (80 B); invDt = nbPositionIterations / dt,
+ * invTotalDt = 1 / dt.  Rows to outRows + k * stride, used bytes to outRowBytes[k]. */
+int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
+                                        const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
+                                        const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, float invDt, float invTotalDt,
+                                        float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, void* outRows,
+                                        uint32_t* outRowBytes);
+/* rows (n x stride, solve order, impulses updated in place); constraint k joins
+ * bodyA[k], bodyB[k]; constraints in [waveEnds[w-1], waveEnds[w]) touch distinct
+ * bodies; the first nbIntegrate bodies are integrated every position iteration;
+ * dt = time step / nbPositionIterations. */
+int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
+                               void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt);
+int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* poses, uint32_t n);
+
 /* -------------------------------------------------------- batched world
  * Many independent scenes advanced together: one persistent launch per step
  * (optionally a CUDA graph), all state resident on the device.  Each scene's

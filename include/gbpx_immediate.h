@@ -1,0 +1,217 @@
+/*
+ * gbpx_immediate.h -- the reference's immediate-mode entry points on the path,
+ * exported by libgbpx_immediate.so under their own (C-linkage) names:
+ *
+ *   PxGenerateContacts               physx/include/PxImmediateMode.h:267
+ *   PxConstructSolverBodiesTGS       physx/include/PxImmediateMode.h:592
+ *   PxConstructStaticSolverBodyTGS   physx/include/PxImmediateMode.h:601
+ *   PxBatchConstraintsTGS            physx/include/PxImmediateMode.h:620
+ *   PxCreateContactConstraintsTGS    physx/include/PxImmediateMode.h:642
+ *   PxSolveConstraintsTGS            physx/include/PxImmediateMode.h:716
+ *   PxIntegrateSolverBodiesTGS       physx/include/PxImmediateMode.h:729
+ *
+ * The reference declares these PX_C_EXPORT (extern "C"), so a program built
+ * against the reference's headers links them from this library instead.  This
+ * header restates, in namespace gbpx_px, the byte layouts those signatures use
+ * (checked against the reference by tests/test_immediate_layout.py) and the
+ * callback interfaces with the same virtual-function order.  It is for building
+ * the library and its tests; a PhysX program keeps including PhysX's headers.
+ * Do not include it together with PxImmediateMode.h.
+ *
+ * Behaviour: every contact generation call is a fresh-cache call (PxCache and
+ * PxCacheAllocator are not used); friction patches are not persisted
+ * (reserveFrictionData is not called, frictionPtr/frictionCount are left 0);
+ * the supported pair set is sphere / plane / capsule / box; contact descriptors
+ * must use unit inverse-mass scales, restDistance 0 and no maximum impulse, and
+ * articulations are not supported (the functions return false, or do nothing,
+ * for input outside this set).  All arithmetic runs on the GPU through libgbpx.
+ */
+#ifndef GBPX_IMMEDIATE_H
+#define GBPX_IMMEDIATE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gbpx_px
+{
+struct PxVec3 { float x, y, z; };
+struct PxQuat { float x, y, z, w; };
+struct PxTransform { PxQuat q; PxVec3 p; };
+struct PxMat33 { PxVec3 column0, column1, column2; };
+
+// PxGeometryType: eSPHERE 0, ePLANE 1, eCAPSULE 2, eBOX 3
+struct PxGeometry { int mType; float mTypePadding; };
+struct PxSphereGeometry : PxGeometry { float radius; };
+struct PxCapsuleGeometry : PxGeometry { float radius, halfHeight; };
+struct PxBoxGeometry : PxGeometry { PxVec3 halfExtents; };
+struct PxPlaneGeometry : PxGeometry {};
+
+struct alignas(16) PxContactPoint
+{
+	alignas(16) PxVec3 normal;
+	float separation;
+	alignas(16) PxVec3 point;
+	float maxImpulse;
+	alignas(16) PxVec3 targetVel;
+	float staticFriction;
+	uint8_t materialFlags;
+	uint32_t internalFaceIndex1;
+	float dynamicFriction;
+	float restitution;
+	float damping;
+};
+
+struct PxCache { uint8_t* mCachedData; uint16_t mCachedSize; uint8_t mPairData; uint8_t mManifoldFlags; };
+
+class PxCacheAllocator
+{
+public:
+	virtual uint8_t* allocateCacheData(const uint32_t byteSize) = 0;
+	virtual ~PxCacheAllocator() {}
+};
+
+class PxContactRecorder
+{
+public:
+	virtual bool recordContacts(const PxContactPoint* contactPoints, uint32_t nbContacts, uint32_t index) = 0;
+	virtual ~PxContactRecorder() {}
+};
+
+struct alignas(16) PxRigidBodyData
+{
+	alignas(16) PxVec3 linearVelocity;
+	float invMass;
+	PxVec3 angularVelocity;
+	float maxDepenetrationVelocity;
+	PxVec3 invInertia;
+	float maxContactImpulse;
+	PxTransform body2World;
+	float linearDamping, angularDamping, maxLinearVelocitySq, maxAngularVelocitySq;
+	uint32_t pad;
+};
+
+struct alignas(16) PxTGSSolverBodyVel
+{
+	alignas(16) PxVec3 linearVelocity;
+	uint16_t maxDynamicPartition;
+	uint16_t nbStaticInteractions;
+	PxVec3 angularVelocity;
+	uint32_t partitionMask;
+	PxVec3 deltaAngDt;
+	float maxAngVel;
+	PxVec3 deltaLinDt;
+	uint16_t lockFlags;
+	bool isKinematic;
+	uint8_t pad;
+};
+
+struct PxTGSSolverBodyTxInertia
+{
+	PxQuat deltaBody2WorldQ;
+	PxVec3 body2WorldP;
+	PxMat33 sqrtInvInertia;
+};
+
+struct alignas(16) PxTGSSolverBodyData
+{
+	alignas(16) PxVec3 originalLinearVelocity;
+	float maxContactImpulse;
+	PxVec3 originalAngularVelocity;
+	float penBiasClamp;
+	float invMass;
+	uint32_t nodeIndex;
+	float reportThreshold;
+	uint32_t pad;
+};
+
+struct PxConstraintBatchHeader { uint32_t startIndex; uint16_t stride; uint16_t constraintType; };
+
+struct alignas(16) PxSolverConstraintDesc
+{
+	PxTGSSolverBodyVel* tgsBodyA;
+	PxTGSSolverBodyVel* tgsBodyB;
+	uint32_t bodyADataIndex, bodyBDataIndex;
+	uint32_t linkIndexA, linkIndexB;
+	uint8_t* constraint;
+	void* writeBack;
+	void* writeBackFriction;
+	uint16_t progressA, progressB;
+	uint16_t constraintLengthOver16;   // constraintType before preparation
+};
+
+struct alignas(16) PxConstraintInvMassScale { float linear0, angular0, linear1, angular1; };
+
+// PxSolverConstraintPrepDescBase::BodyState
+enum { eDYNAMIC_BODY = 1, eSTATIC_BODY = 2, eKINEMATIC_BODY = 4, eARTICULATION = 8 };
+
+struct PxTGSSolverContactDesc
+{
+	PxConstraintInvMassScale invMassScales;
+	PxSolverConstraintDesc* desc;
+	const PxTGSSolverBodyVel* body0;
+	const PxTGSSolverBodyVel* body1;
+	const PxTGSSolverBodyTxInertia* body0TxI;
+	const PxTGSSolverBodyTxInertia* body1TxI;
+	const PxTGSSolverBodyData* bodyData0;
+	const PxTGSSolverBodyData* bodyData1;
+	PxTransform bodyFrame0;
+	PxTransform bodyFrame1;
+	int bodyState0;
+	int bodyState1;
+	void* shapeInteraction;
+	uint8_t* frictionPtr;
+	const PxContactPoint* contacts;
+	uint32_t numContacts;
+	uint8_t frictionCount;
+	bool hasMaxImpulse;
+	bool disableStrongFriction;
+	bool hasForceThresholds;
+	float restDistance;
+	float maxCCDSeparation;
+	float* contactForces;
+	uint32_t startFrictionPatchIndex;
+	uint32_t numFrictionPatches;
+	uint32_t startContactPatchIndex;
+	uint16_t numContactPatches;
+	uint16_t axisConstraintCount;
+	float maxImpulse;
+	float torsionalPatchRadius;
+	float minTorsionalPatchRadius;
+	float offsetSlop;
+};
+
+class PxConstraintAllocator
+{
+public:
+	virtual uint8_t* reserveConstraintData(const uint32_t byteSize) = 0;
+	virtual uint8_t* reserveFrictionData(const uint32_t byteSize) = 0;
+	virtual ~PxConstraintAllocator() {}
+};
+} // namespace gbpx_px
+
+extern "C" {
+bool PxGenerateContacts(const gbpx_px::PxGeometry* const* geom0, const gbpx_px::PxGeometry* const* geom1, const gbpx_px::PxTransform* pose0,
+                        const gbpx_px::PxTransform* pose1, gbpx_px::PxCache* contactCache, uint32_t nbPairs,
+                        gbpx_px::PxContactRecorder& contactRecorder, float contactDistance, float meshContactMargin, float toleranceLength,
+                        gbpx_px::PxCacheAllocator& allocator);
+void PxConstructSolverBodiesTGS(const gbpx_px::PxRigidBodyData* inRigidData, gbpx_px::PxTGSSolverBodyVel* outSolverBodyVel,
+                                gbpx_px::PxTGSSolverBodyTxInertia* outSolverBodyTxInertia, gbpx_px::PxTGSSolverBodyData* outSolverBodyData,
+                                uint32_t nbBodies, const gbpx_px::PxVec3& gravity, float dt, bool gyroscopicForces);
+void PxConstructStaticSolverBodyTGS(const gbpx_px::PxTransform& globalPose, gbpx_px::PxTGSSolverBodyVel& solverBodyVel,
+                                    gbpx_px::PxTGSSolverBodyTxInertia& solverBodyTxInertia, gbpx_px::PxTGSSolverBodyData& solverBodyData);
+uint32_t PxBatchConstraintsTGS(const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, uint32_t nbConstraints,
+                               gbpx_px::PxTGSSolverBodyVel* solverBodies, uint32_t nbBodies, gbpx_px::PxConstraintBatchHeader* outBatchHeaders,
+                               gbpx_px::PxSolverConstraintDesc* outOrderedConstraintDescs, void** articulations, uint32_t nbArticulations);
+bool PxCreateContactConstraintsTGS(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, gbpx_px::PxTGSSolverContactDesc* contactDescs,
+                                   gbpx_px::PxConstraintAllocator& allocator, float invDt, float invTotalDt, float bounceThreshold,
+                                   float frictionOffsetThreshold, float correlationDistance);
+void PxSolveConstraintsTGS(const gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders,
+                           const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, gbpx_px::PxTGSSolverBodyVel* solverBodies,
+                           gbpx_px::PxTGSSolverBodyTxInertia* txInertias, uint32_t nbSolverBodies, uint32_t nbPositionIterations,
+                           uint32_t nbVelocityIterations, float dt, float invDt, uint32_t nbSolverArticulations, void** solverArticulations,
+                           void* Z, void* deltaV);
+void PxIntegrateSolverBodiesTGS(gbpx_px::PxTGSSolverBodyVel* solverBody, const gbpx_px::PxTGSSolverBodyTxInertia* txInertia,
+                                gbpx_px::PxTransform* poses, uint32_t nbBodiesToIntegrate, float dt);
+}
+
+#endif /* GBPX_IMMEDIATE_H */

@@ -1,7 +1,9 @@
 """Builds libgbpx.so (the CUDA kernels + C ABI) in-tree for sm_103a.
 
 Every ``csrc/*.cu`` translation unit is compiled in parallel with nvcc and
-linked into ``physx_gb300/libgbpx.so``.  Nothing is installed anywhere.
+linked into ``physx_gb300/libgbpx.so``; ``csrc/immediate.cpp`` (the
+reference's immediate-mode entry points over that C ABI) becomes
+``physx_gb300/libgbpx_immediate.so``.  Nothing is installed anywhere.
 """
 import os
 import shutil
@@ -13,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbpx.so")
+LIB_IMMEDIATE = os.path.join(HERE, "libgbpx_immediate.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no fused multiply-add, so contact and solver arithmetic rounds
@@ -55,15 +58,32 @@ def build(verbose=False):
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s), srcs))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+        if verbose:
+            print("built", LIB, file=sys.stderr)
+    _build_immediate(verbose)
+    return LIB
+
+
+def _build_immediate(verbose=False):
+    src = os.path.join(CSRC, "immediate.cpp")
+    include = os.path.join(os.path.dirname(HERE), "include")
+    deps = [src, LIB, os.path.join(include, "gbpx.h"), os.path.join(include, "gbpx_immediate.h")]
+    if os.path.exists(LIB_IMMEDIATE) and os.path.getmtime(LIB_IMMEDIATE) >= max(os.path.getmtime(d) for d in deps):
+        return LIB_IMMEDIATE
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-fvisibility=hidden", "-I" + include, src, "-o", LIB_IMMEDIATE,
+           "-L" + HERE, "-lgbpx", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+        raise RuntimeError("immediate-mode library build failed:\n%s\n%s" % (r.stdout, r.stderr))
     if verbose:
-        print("built", LIB, file=sys.stderr)
-    return LIB
+        print("built", LIB_IMMEDIATE, file=sys.stderr)
+    return LIB_IMMEDIATE
 
 
 if __name__ == "__main__":

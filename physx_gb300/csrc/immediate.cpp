@@ -1,0 +1,278 @@
+// libgbpx_immediate.so: the reference's immediate-mode entry points on the
+// rigid-body path (physx/include/PxImmediateMode.h:267, 592-729) under their
+// own C-linkage names, implemented on the GB300 through libgbpx's C ABI.  A
+// program written against physx::immediate links these symbols from here.
+//
+// Each call moves the caller's arrays to the device and back (the reference's
+// interface is host memory); many independent scenes should use gbpx_world_*
+// instead.  What is not supported returns false / does nothing (see
+// include/gbpx_immediate.h).
+#include "gbpx.h"
+#include "gbpx_immediate.h"
+
+#include <algorithm>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+using namespace gbpx_px;
+
+#define GX extern "C" __attribute__((visibility("default")))
+
+namespace
+{
+const uint32_t NO_FACE_INDEX = 0xffffffffu;   // PXC_CONTACT_NO_FACE_INDEX
+
+bool packShape(const PxGeometry& g, int& type, float* out)
+{
+	out[0] = out[1] = out[2] = out[3] = 0.0f;
+	type = g.mType;
+	switch(type)
+	{
+	case 0: out[0] = static_cast<const PxSphereGeometry&>(g).radius; return true;
+	case 1: return true;
+	case 2:
+		out[0] = static_cast<const PxCapsuleGeometry&>(g).radius;
+		out[1] = static_cast<const PxCapsuleGeometry&>(g).halfHeight;
+		return true;
+	case 3:
+	{
+		const PxVec3& h = static_cast<const PxBoxGeometry&>(g).halfExtents;
+		out[0] = h.x; out[1] = h.y; out[2] = h.z;
+		return true;
+	}
+	default: return false;
+	}
+}
+
+uint32_t stridesTotal(const PxConstraintBatchHeader* headers, uint32_t nbHeaders)
+{
+	uint32_t n = 0;
+	for(uint32_t h = 0; h < nbHeaders; h++) n += headers[h].stride;
+	return n;
+}
+} // namespace
+
+// immediate::PxGenerateContacts (fresh caches: the cache and its allocator are not used).
+GX bool PxGenerateContacts(const PxGeometry* const* geom0, const PxGeometry* const* geom1, const PxTransform* pose0, const PxTransform* pose1,
+                           PxCache* contactCache, uint32_t nbPairs, PxContactRecorder& contactRecorder, float contactDistance,
+                           float meshContactMargin, float toleranceLength, PxCacheAllocator& allocator)
+{
+	(void)contactCache;
+	(void)allocator;
+	if(!nbPairs) return true;
+	std::vector<int> t0(nbPairs), t1(nbPairs);
+	std::vector<float> g0(4 * size_t(nbPairs)), g1(4 * size_t(nbPairs)), p0(7 * size_t(nbPairs)), p1(7 * size_t(nbPairs));
+	for(uint32_t i = 0; i < nbPairs; i++)
+	{
+		if(!packShape(*geom0[i], t0[i], &g0[4 * size_t(i)]) || !packShape(*geom1[i], t1[i], &g1[4 * size_t(i)])) return false;
+		memcpy(&p0[7 * size_t(i)], &pose0[i], 28);
+		memcpy(&p1[7 * size_t(i)], &pose1[i], 28);
+	}
+	std::vector<float> out(size_t(nbPairs) * 4 * 8);
+	std::vector<uint32_t> counts(nbPairs);
+	if(gbpx_generate_contacts(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), nbPairs, contactDistance, meshContactMargin,
+	                          toleranceLength, out.data(), 4, counts.data()) != GBPX_OK)
+		return false;
+	for(uint32_t i = 0; i < nbPairs; i++)
+	{
+		if(!counts[i]) continue;
+		PxContactPoint cp[4];
+		memset(cp, 0, sizeof(cp));
+		for(uint32_t c = 0; c < counts[i]; c++)
+		{
+			const float* s = &out[(size_t(i) * 4 + c) * 8];
+			cp[c].normal = PxVec3{s[0], s[1], s[2]};
+			cp[c].separation = s[3];
+			cp[c].point = PxVec3{s[4], s[5], s[6]};
+			cp[c].internalFaceIndex1 = NO_FACE_INDEX;
+		}
+		contactRecorder.recordContacts(cp, counts[i], i);
+	}
+	return true;
+}
+
+GX void PxConstructSolverBodiesTGS(const PxRigidBodyData* inRigidData, PxTGSSolverBodyVel* outSolverBodyVel, PxTGSSolverBodyTxInertia* outSolverBodyTxInertia,
+                                   PxTGSSolverBodyData* outSolverBodyData, uint32_t nbBodies, const PxVec3& gravity, float dt, bool gyroscopicForces)
+{
+	(void)gyroscopicForces;   // gyroscopic integration is not on this path
+	gbpx_construct_solver_bodies_tgs(inRigidData, nbBodies, &gravity.x, dt, outSolverBodyVel, outSolverBodyTxInertia, outSolverBodyData);
+}
+
+GX void PxConstructStaticSolverBodyTGS(const PxTransform& globalPose, PxTGSSolverBodyVel& solverBodyVel, PxTGSSolverBodyTxInertia& solverBodyTxInertia,
+                                       PxTGSSolverBodyData& solverBodyData)
+{
+	gbpx_construct_static_solver_bodies_tgs(&globalPose.q.x, 1, &solverBodyVel, &solverBodyTxInertia, &solverBodyData);
+}
+
+// PxBatchConstraintsTGS: bodies inside [solverBodies, solverBodies + nbBodies)
+// are dynamic, every other body static or kinematic (as the reference).
+GX uint32_t PxBatchConstraintsTGS(const PxSolverConstraintDesc* descs, uint32_t nbConstraints, PxTGSSolverBodyVel* solverBodies, uint32_t nbBodies,
+                                  PxConstraintBatchHeader* outBatchHeaders, PxSolverConstraintDesc* outOrdered, void** articulations,
+                                  uint32_t nbArticulations)
+{
+	(void)articulations;
+	if(!nbConstraints || nbArticulations) return 0;
+	std::vector<uint32_t> a(nbConstraints), b(nbConstraints), hs(nbConstraints), hst(nbConstraints), order(nbConstraints);
+	auto index = [&](const PxTGSSolverBodyVel* p) {
+		return (p >= solverBodies && p < solverBodies + nbBodies) ? uint32_t(p - solverBodies) : nbBodies;
+	};
+	for(uint32_t i = 0; i < nbConstraints; i++)
+	{
+		a[i] = index(descs[i].tgsBodyA);
+		b[i] = index(descs[i].tgsBodyB);
+	}
+	const uint32_t nbHeaders = gbpx_batch_constraints_tgs(a.data(), b.data(), nbConstraints, nbBodies, 1, hs.data(), hst.data(), order.data());
+	for(uint32_t i = 0; i < nbConstraints; i++) outOrdered[i] = descs[order[i]];
+	for(uint32_t h = 0; h < nbHeaders; h++)
+	{
+		outBatchHeaders[h].startIndex = hs[h];
+		outBatchHeaders[h].stride = uint16_t(hst[h]);
+		outBatchHeaders[h].constraintType = outOrdered[hs[h]].constraintLengthOver16;   // the descriptors' constraint type
+	}
+	return nbHeaders;
+}
+
+// PxCreateContactConstraintsTGS: rows per descriptor into the allocator's
+// constraint memory (desc->constraint, desc->constraintLengthOver16).
+GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, PxTGSSolverContactDesc* contactDescs,
+                                      PxConstraintAllocator& allocator, float invDt, float invTotalDt, float bounceThreshold,
+                                      float frictionOffsetThreshold, float correlationDistance)
+{
+	const uint32_t n = stridesTotal(batchHeaders, nbHeaders);
+	if(!n) return true;
+	static const PxTGSSolverBodyVel zeroVel = [] { PxTGSSolverBodyVel v; memset(&v, 0, sizeof(v)); v.isKinematic = true; return v; }();
+	static const PxTGSSolverBodyTxInertia zeroTx = [] { PxTGSSolverBodyTxInertia t; memset(&t, 0, sizeof(t)); t.deltaBody2WorldQ.w = 1.0f; return t; }();
+	static const PxTGSSolverBodyData zeroData = [] { PxTGSSolverBodyData d; memset(&d, 0, sizeof(d)); d.maxContactImpulse = 3.4e38f; return d; }();
+	std::vector<PxTGSSolverBodyVel> v0(n), v1(n);
+	std::vector<PxTGSSolverBodyTxInertia> x0(n), x1(n);
+	std::vector<PxTGSSolverBodyData> d0(n), d1(n);
+	std::vector<PxTransform> f0(n), f1(n);
+	std::vector<uint32_t> cs(n), cc(n);
+	std::vector<PxContactPoint> points;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxTGSSolverContactDesc& d = contactDescs[k];
+		if(d.numContacts > 4 || d.restDistance != 0.0f || d.hasMaxImpulse || d.invMassScales.linear0 != 1.0f || d.invMassScales.angular0 != 1.0f ||
+		   d.invMassScales.linear1 != 1.0f || d.invMassScales.angular1 != 1.0f || (d.bodyState0 & eARTICULATION) || (d.bodyState1 & eARTICULATION))
+			return false;
+		v0[k] = d.body0 ? *d.body0 : zeroVel;
+		v1[k] = d.body1 ? *d.body1 : zeroVel;
+		if(d.bodyState0 != eDYNAMIC_BODY) v0[k].isKinematic = true;
+		if(d.bodyState1 != eDYNAMIC_BODY) v1[k].isKinematic = true;
+		x0[k] = d.body0TxI ? *d.body0TxI : zeroTx;
+		x1[k] = d.body1TxI ? *d.body1TxI : zeroTx;
+		d0[k] = d.bodyData0 ? *d.bodyData0 : zeroData;
+		d1[k] = d.bodyData1 ? *d.bodyData1 : zeroData;
+		f0[k] = d.bodyFrame0;
+		f1[k] = d.bodyFrame1;
+		cs[k] = uint32_t(points.size());
+		cc[k] = d.numContacts;
+		points.insert(points.end(), d.contacts, d.contacts + d.numContacts);
+	}
+	const uint32_t stride = gbpx_constraint_row_stride();
+	std::vector<uint8_t> rows(size_t(n) * stride);
+	std::vector<uint32_t> bytes(n);
+	if(gbpx_create_contact_constraints_tgs(n, v0.data(), v1.data(), x0.data(), x1.data(), d0.data(), d1.data(), &f0[0].q.x, &f1[0].q.x, cs.data(),
+	                                       cc.data(), points.data(), uint32_t(points.size()), invDt, invTotalDt, bounceThreshold,
+	                                       frictionOffsetThreshold, correlationDistance, rows.data(), bytes.data()) != GBPX_OK)
+		return false;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		PxTGSSolverContactDesc& d = contactDescs[k];
+		const uint32_t size = (bytes[k] + 15u) & ~15u;
+		uint8_t* mem = allocator.reserveConstraintData(size);
+		if(!mem) return false;
+		memcpy(mem, &rows[size_t(k) * stride], size);
+		d.desc->constraint = mem;
+		d.desc->constraintLengthOver16 = uint16_t(size / 16);
+		d.frictionPtr = nullptr;
+		d.frictionCount = 0;
+		d.numFrictionPatches = 0;
+	}
+	return true;
+}
+
+// PxSolveConstraintsTGS: headers are solved in order; consecutive headers whose
+// constraints touch distinct dynamic bodies run as one parallel wave.
+GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders, const PxSolverConstraintDesc* descs,
+                              PxTGSSolverBodyVel* solverBodies, PxTGSSolverBodyTxInertia* txInertias, uint32_t nbSolverBodies, uint32_t nbPositionIterations,
+                              uint32_t nbVelocityIterations, float dt, float invDt, uint32_t nbSolverArticulations, void** solverArticulations, void* Z,
+                              void* deltaV)
+{
+	(void)invDt;
+	(void)solverArticulations;
+	(void)Z;
+	(void)deltaV;
+	if(nbSolverArticulations || !nbSolverBodies) return;
+	const uint32_t n = stridesTotal(batchHeaders, nbBatchHeaders);
+	// bodies: the caller's solver bodies, then every other (static / kinematic) body the constraints reference
+	std::vector<PxTGSSolverBodyVel> vel(solverBodies, solverBodies + nbSolverBodies);
+	std::vector<PxTGSSolverBodyTxInertia> tx(txInertias, txInertias + nbSolverBodies);
+	std::unordered_map<const PxTGSSolverBodyVel*, uint32_t> extra;
+	PxTGSSolverBodyTxInertia zeroTx;
+	memset(&zeroTx, 0, sizeof(zeroTx));
+	zeroTx.deltaBody2WorldQ.w = 1.0f;
+	auto index = [&](const PxTGSSolverBodyVel* p) -> uint32_t {
+		if(p >= solverBodies && p < solverBodies + nbSolverBodies) return uint32_t(p - solverBodies);
+		auto it = extra.find(p);
+		if(it != extra.end()) return it->second;
+		const uint32_t id = uint32_t(vel.size());
+		extra[p] = id;
+		vel.push_back(*p);
+		tx.push_back(zeroTx);
+		return id;
+	};
+	const uint32_t stride = gbpx_constraint_row_stride();
+	std::vector<uint8_t> rows(size_t(n) * stride, 0);
+	std::vector<uint32_t> a(n), b(n), waveEnds;
+	std::vector<uint32_t> lastWave;   // per dynamic body: wave that last used it (+1)
+	lastWave.assign(nbSolverBodies, 0);
+	uint32_t wave = 1;
+	bool waveOpen = false;
+	for(uint32_t h = 0, k = 0; h < nbBatchHeaders; h++)
+	{
+		const PxConstraintBatchHeader& hd = batchHeaders[h];
+		bool clash = false;
+		for(uint32_t j = 0; j < hd.stride; j++)
+		{
+			const PxSolverConstraintDesc& d = descs[hd.startIndex + j];
+			const uint32_t ia = index(d.tgsBodyA), ib = index(d.tgsBodyB);
+			clash = clash || (ia < nbSolverBodies && lastWave[ia] == wave) || (ib < nbSolverBodies && lastWave[ib] == wave);
+		}
+		if(clash && waveOpen)
+		{
+			waveEnds.push_back(k);
+			wave++;
+		}
+		for(uint32_t j = 0; j < hd.stride; j++, k++)
+		{
+			const PxSolverConstraintDesc& d = descs[hd.startIndex + j];
+			a[k] = index(d.tgsBodyA);
+			b[k] = index(d.tgsBodyB);
+			if(a[k] < nbSolverBodies) lastWave[a[k]] = wave;
+			if(b[k] < nbSolverBodies) lastWave[b[k]] = wave;
+			if(d.constraint) memcpy(&rows[size_t(k) * stride], d.constraint, std::min<size_t>(size_t(d.constraintLengthOver16) * 16, stride));
+		}
+		waveOpen = true;
+	}
+	if(n) waveEnds.push_back(n);
+	if(gbpx_solve_constraints_tgs(n ? rows.data() : nullptr, a.data(), b.data(), n, waveEnds.data(), uint32_t(waveEnds.size()), vel.data(), tx.data(),
+	                              uint32_t(vel.size()), nbSolverBodies, nbPositionIterations, nbVelocityIterations, dt) != GBPX_OK)
+		return;
+	memcpy(solverBodies, vel.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyVel));
+	memcpy(txInertias, tx.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyTxInertia));
+	for(uint32_t h = 0, k = 0; h < nbBatchHeaders; h++)
+		for(uint32_t j = 0; j < batchHeaders[h].stride; j++, k++)
+		{
+			const PxSolverConstraintDesc& d = descs[batchHeaders[h].startIndex + j];
+			if(d.constraint) memcpy(d.constraint, &rows[size_t(k) * stride], std::min<size_t>(size_t(d.constraintLengthOver16) * 16, stride));
+		}
+}
+
+GX void PxIntegrateSolverBodiesTGS(PxTGSSolverBodyVel* solverBody, const PxTGSSolverBodyTxInertia* txInertia, PxTransform* poses, uint32_t nbBodiesToIntegrate,
+                                   float dt)
+{
+	(void)dt;
+	gbpx_integrate_solver_bodies_tgs(solverBody, txInertia, &poses[0].q.x, nbBodiesToIntegrate);
+}

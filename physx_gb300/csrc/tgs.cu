@@ -106,33 +106,171 @@ __global__ void finalizeKernel(const BodyVel* __restrict__ vel, const BodyTx* __
 	q[4] = p.p.x; q[5] = p.p.y; q[6] = p.p.z;
 }
 
-// Solver bodies in the reference's byte layouts (PxTGSSolverBodyVel 64 B,
+// One solver body in the reference's byte layouts (PxTGSSolverBodyVel 64 B,
 // PxTGSSolverBodyTxInertia 64 B, PxTGSSolverBodyData 48 B).
+__device__ __forceinline__ void exportBodiesKernelBody(const BodyVel& vel, const BodyTx& tx, const BodyData& data, float* v, float* t, float* d)
+{
+	v[0] = vel.lin.x; v[1] = vel.lin.y; v[2] = vel.lin.z; v[3] = 0.0f;
+	v[4] = vel.ang.x; v[5] = vel.ang.y; v[6] = vel.ang.z; v[7] = 0.0f;
+	v[8] = vel.dAng.x; v[9] = vel.dAng.y; v[10] = vel.dAng.z; v[11] = vel.maxAngVel;
+	v[12] = vel.dLin.x; v[13] = vel.dLin.y; v[14] = vel.dLin.z;
+	uint32_t lockAndKin = vel.kinematic ? (1u << 16) : 0u;   // lockFlags (u16) = 0, isKinematic (u8), pad (u8)
+	memcpy(&v[15], &lockAndKin, 4);
+	t[0] = tx.dq.x; t[1] = tx.dq.y; t[2] = tx.dq.z; t[3] = tx.dq.w;
+	t[4] = tx.p.x; t[5] = tx.p.y; t[6] = tx.p.z;
+	const M33& m = tx.sqrtInvInertia;
+	t[7] = m.c0.x; t[8] = m.c0.y; t[9] = m.c0.z; t[10] = m.c1.x; t[11] = m.c1.y; t[12] = m.c1.z; t[13] = m.c2.x; t[14] = m.c2.y; t[15] = m.c2.z;
+	d[0] = data.origLin.x; d[1] = data.origLin.y; d[2] = data.origLin.z; d[3] = data.maxContactImpulse;
+	d[4] = data.origAng.x; d[5] = data.origAng.y; d[6] = data.origAng.z; d[7] = data.penBiasClamp;
+	d[8] = data.invMass;
+	const uint32_t invalidNode = 0x7fffffffu;   // nodeIndex: immediate mode passes PX_INVALID_NODE
+	memcpy(&d[9], &invalidNode, 4);
+	d[10] = FLT_MAX;                            // reportThreshold
+	d[11] = 0.0f;
+}
+
 __global__ void exportBodiesKernel(const BodyVel* __restrict__ vel, const BodyTx* __restrict__ tx, const BodyData* __restrict__ data, uint32_t n,
                                    float* __restrict__ outVel, float* __restrict__ outTx, float* __restrict__ outData)
 {
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n) return;
-	float* v = outVel + 16 * size_t(i);
-	v[0] = vel[i].lin.x; v[1] = vel[i].lin.y; v[2] = vel[i].lin.z; v[3] = 0.0f;
-	v[4] = vel[i].ang.x; v[5] = vel[i].ang.y; v[6] = vel[i].ang.z; v[7] = 0.0f;
-	v[8] = vel[i].dAng.x; v[9] = vel[i].dAng.y; v[10] = vel[i].dAng.z; v[11] = vel[i].maxAngVel;
-	v[12] = vel[i].dLin.x; v[13] = vel[i].dLin.y; v[14] = vel[i].dLin.z;
-	uint32_t lockAndKin = vel[i].kinematic ? (1u << 16) : 0u;   // lockFlags (u16) = 0, isKinematic (u8), pad (u8)
-	memcpy(&v[15], &lockAndKin, 4);
-	float* t = outTx + 16 * size_t(i);
-	t[0] = tx[i].dq.x; t[1] = tx[i].dq.y; t[2] = tx[i].dq.z; t[3] = tx[i].dq.w;
-	t[4] = tx[i].p.x; t[5] = tx[i].p.y; t[6] = tx[i].p.z;
-	const M33& m = tx[i].sqrtInvInertia;
-	t[7] = m.c0.x; t[8] = m.c0.y; t[9] = m.c0.z; t[10] = m.c1.x; t[11] = m.c1.y; t[12] = m.c1.z; t[13] = m.c2.x; t[14] = m.c2.y; t[15] = m.c2.z;
-	float* d = outData + 12 * size_t(i);
-	d[0] = data[i].origLin.x; d[1] = data[i].origLin.y; d[2] = data[i].origLin.z; d[3] = data[i].maxContactImpulse;
-	d[4] = data[i].origAng.x; d[5] = data[i].origAng.y; d[6] = data[i].origAng.z; d[7] = data[i].penBiasClamp;
-	d[8] = data[i].invMass;
-	const uint32_t invalidNode = 0x7fffffffu;   // nodeIndex: immediate mode passes PX_INVALID_NODE
-	memcpy(&d[9], &invalidNode, 4);
-	d[10] = FLT_MAX;                            // reportThreshold
-	d[11] = 0.0f;
+	exportBodiesKernelBody(vel[i], tx[i], data[i], outVel + 16 * size_t(i), outTx + 16 * size_t(i), outData + 12 * size_t(i));
+}
+// ---- records in the reference's solver-body layouts, used in place
+// (PxTGSSolverBodyVel 16 floats, PxTGSSolverBodyTxInertia 16, PxTGSSolverBodyData 12)
+__device__ __forceinline__ BodyVel loadVelRef(const float* v)
+{
+	BodyVel o;
+	o.lin = v3(v[0], v[1], v[2]);
+	o.ang = v3(v[4], v[5], v[6]);
+	o.dAng = v3(v[8], v[9], v[10]);
+	o.maxAngVel = v[11];
+	o.dLin = v3(v[12], v[13], v[14]);
+	o.kinematic = reinterpret_cast<const uint8_t*>(v)[62] ? 1 : 0;
+	return o;
+}
+__device__ __forceinline__ BodyTx loadTxRef(const float* t)
+{
+	BodyTx o;
+	o.dq.x = t[0]; o.dq.y = t[1]; o.dq.z = t[2]; o.dq.w = t[3];
+	o.p = v3(t[4], t[5], t[6]);
+	o.sqrtInvInertia.c0 = v3(t[7], t[8], t[9]);
+	o.sqrtInvInertia.c1 = v3(t[10], t[11], t[12]);
+	o.sqrtInvInertia.c2 = v3(t[13], t[14], t[15]);
+	return o;
+}
+__device__ __forceinline__ BodyData loadDataRef(const float* d)
+{
+	BodyData o;
+	o.origLin = v3(d[0], d[1], d[2]);
+	o.maxContactImpulse = d[3];
+	o.origAng = v3(d[4], d[5], d[6]);
+	o.penBiasClamp = d[7];
+	o.invMass = d[8];
+	return o;
+}
+
+// PxConstructStaticSolverBodyTGS for n poses (zero velocity, zero inverse inertia, flagged kinematic).
+__global__ void staticBodiesKernel(const float* __restrict__ poses, uint32_t n, float* __restrict__ outVel, float* __restrict__ outTx,
+                                   float* __restrict__ outData)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const float* s = poses + 7 * size_t(i);
+	Tr p;
+	p.q.x = s[0]; p.q.y = s[1]; p.q.z = s[2]; p.q.w = s[3];
+	p.p = v3(s[4], s[5], s[6]);
+	BodyVel v;
+	BodyTx t;
+	BodyData d;
+	constructStaticBody(p, v, t, d);
+	exportBodiesKernelBody(v, t, d, outVel + 16 * size_t(i), outTx + 16 * size_t(i), outData + 12 * size_t(i));
+}
+
+// PxCreateContactConstraintsTGS for one descriptor per thread: both bodies'
+// records, frames and the descriptor's PxContactPoints (80 bytes each:
+// normal, separation, point, ..., staticFriction at 44, dynamicFriction at 56,
+// restitution at 60).  Rows go to outRows[k] (bodyA/bodyB set by the solve).
+__global__ void prepDescKernel(uint32_t n, const float* __restrict__ vel0, const float* __restrict__ vel1, const float* __restrict__ tx0,
+                               const float* __restrict__ tx1, const float* __restrict__ data0, const float* __restrict__ data1,
+                               const float* __restrict__ frame0, const float* __restrict__ frame1, const uint32_t* __restrict__ cStart,
+                               const uint32_t* __restrict__ cCount, const float* __restrict__ points, PrepParams pp,
+                               ConstraintRecord* __restrict__ recs, uint32_t* __restrict__ recBytes)
+{
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= n) return;
+	Contact cs[MAX_CONTACTS];
+	const uint32_t cnt = cCount[k] < MAX_CONTACTS ? cCount[k] : MAX_CONTACTS;
+	for(uint32_t c = 0; c < cnt; c++)
+	{
+		const float* s = points + 20 * size_t(cStart[k] + c);
+		cs[c].n = v3(s[0], s[1], s[2]);
+		cs[c].sep = s[3];
+		cs[c].p = v3(s[4], s[5], s[6]);
+		cs[c].staticFriction = s[11];
+		cs[c].dynamicFriction = s[14];
+		cs[c].restitution = s[15];
+	}
+	const BodyVel va = loadVelRef(vel0 + 16 * size_t(k)), vb = loadVelRef(vel1 + 16 * size_t(k));
+	const BodyTx ta = loadTxRef(tx0 + 16 * size_t(k)), tb = loadTxRef(tx1 + 16 * size_t(k));
+	const BodyData da = loadDataRef(data0 + 12 * size_t(k)), db = loadDataRef(data1 + 12 * size_t(k));
+	Tr f0, f1;
+	const float* a = frame0 + 7 * size_t(k);
+	const float* b = frame1 + 7 * size_t(k);
+	f0.q.x = a[0]; f0.q.y = a[1]; f0.q.z = a[2]; f0.q.w = a[3]; f0.p = v3(a[4], a[5], a[6]);
+	f1.q.x = b[0]; f1.q.y = b[1]; f1.q.z = b[2]; f1.q.w = b[3]; f1.p = v3(b[4], b[5], b[6]);
+	prepConstraint(cs, int(cnt), 0, 1, va, vb, ta, tb, da, db, f0, f1, pp, recs[k]);
+	recBytes[k] = recs[k].bytes();
+}
+
+// One wave of independent constraints on solver bodies held in the
+// reference's layouts: rows[k] joins bodyA[k], bodyB[k].
+__global__ void solveWaveRefKernel(ConstraintRecord* __restrict__ recs, const uint32_t* __restrict__ bodyA, const uint32_t* __restrict__ bodyB,
+                                   uint32_t begin, uint32_t end, float* __restrict__ vel, float minPen, float elapsed)
+{
+	const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= end) return;
+	ConstraintRecord& r = recs[k];
+	if(r.nbPatches == 0) return;
+	float* va = vel + 16 * size_t(bodyA[k]);
+	float* vb = vel + 16 * size_t(bodyB[k]);
+	BodyVel b0 = loadVelRef(va), b1 = loadVelRef(vb);
+	solveConstraint(r, b0, b1, true, minPen, elapsed);
+	va[0] = b0.lin.x; va[1] = b0.lin.y; va[2] = b0.lin.z; va[4] = b0.ang.x; va[5] = b0.ang.y; va[6] = b0.ang.z;
+	vb[0] = b1.lin.x; vb[1] = b1.lin.y; vb[2] = b1.lin.z; vb[4] = b1.ang.x; vb[5] = b1.ang.y; vb[6] = b1.ang.z;
+}
+
+// integrateCoreStep on records in the reference's layouts.
+__global__ void integrateRefKernel(float* __restrict__ vel, float* __restrict__ tx, uint32_t n, float dt)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	float* v = vel + 16 * size_t(i);
+	float* t = tx + 16 * size_t(i);
+	BodyVel bv = loadVelRef(v);
+	BodyTx bt = loadTxRef(t);
+	integrateStep(bv, bt, dt);
+	v[8] = bv.dAng.x; v[9] = bv.dAng.y; v[10] = bv.dAng.z;
+	v[12] = bv.dLin.x; v[13] = bv.dLin.y; v[14] = bv.dLin.z;
+	t[0] = bt.dq.x; t[1] = bt.dq.y; t[2] = bt.dq.z; t[3] = bt.dq.w;
+	t[4] = bt.p.x; t[5] = bt.p.y; t[6] = bt.p.z;
+}
+
+// PxIntegrateSolverBodiesTGS: world angular velocity into the velocity record, new poses.
+__global__ void finalizeRefKernel(float* __restrict__ vel, const float* __restrict__ tx, float* __restrict__ poses, uint32_t n)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	float* v = vel + 16 * size_t(i);
+	float* q = poses + 7 * size_t(i);
+	Tr p;
+	p.q.x = q[0]; p.q.y = q[1]; p.q.z = q[2]; p.q.w = q[3];
+	p.p = v3(q[4], q[5], q[6]);
+	V3 w;
+	finalizeBody(loadVelRef(v), loadTxRef(tx + 16 * size_t(i)), p, w);
+	v[4] = w.x; v[5] = w.y; v[6] = w.z;
+	q[0] = p.q.x; q[1] = p.q.y; q[2] = p.q.z; q[3] = p.q.w;
+	q[4] = p.p.x; q[5] = p.p.y; q[6] = p.p.z;
 }
 } // namespace tgs
 
@@ -304,5 +442,189 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	}
 	for(uint32_t i = 0; i < nbConstraints; i++) outOrder[i] = batch.order[i];
 	*outNbHeaders = uint32_t(batch.headerStart.size());
+	return GBPX_OK;
+}
+
+// ---------------------------------------------------------------- split-phase TGS on reference layouts
+// The stages of the reference's immediate-mode TGS as separate calls, on solver
+// bodies in the reference's layouts (PxTGSSolverBodyVel / TxInertia / Data),
+// for callers that drive the stages themselves.
+
+namespace gbpx
+{
+struct TgsStageWorkspace
+{
+	cudaStream_t stream = 0;
+	DevBuf<float> vel0, vel1, tx0, tx1, data0, data1, frame0, frame1, points, vel, tx, poses;
+	DevBuf<uint32_t> cStart, cCount, bodyA, bodyB, recBytes;
+	DevBuf<tgs::ConstraintRecord> recs;
+	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
+};
+static TgsStageWorkspace* tgsStageWorkspace()
+{
+	static TgsStageWorkspace* ws = nullptr;
+	if(!ws)
+	{
+		ws = new TgsStageWorkspace;
+		if(ws->init()) { delete ws; ws = nullptr; }
+	}
+	return ws;
+}
+} // namespace gbpx
+
+// Bytes of one constraint's row block (the stride of gbpx_create_contact_constraints_tgs outputs).
+GBPX_API uint32_t gbpx_constraint_row_stride(void)
+{
+	return uint32_t(sizeof(tgs::ConstraintRecord));
+}
+
+// PxConstructStaticSolverBodyTGS for n poses (PxTransform in, reference solver-body layouts out).
+GBPX_API int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void* outVel, void* outTxI, void* outData)
+{
+	if(!n) return GBPX_OK;
+	if(!poses || !outVel || !outTxI || !outData) return GBPX_ERR_INVALID;
+	TgsStageWorkspace* ws = tgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	if(ws->poses.reserve(7 * size_t(n)) || ws->vel.reserve(16 * size_t(n)) || ws->tx.reserve(16 * size_t(n)) || ws->data0.reserve(12 * size_t(n)))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->poses.ptr, poses, size_t(n) * 28, cudaMemcpyHostToDevice, s));
+	tgs::staticBodiesKernel<<<divUp(n, 128), 128, 0, s>>>(ws->poses.ptr, n, ws->vel.ptr, ws->tx.ptr, ws->data0.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outVel, ws->vel.ptr, size_t(n) * 64, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outTxI, ws->tx.ptr, size_t(n) * 64, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outData, ws->data0.ptr, size_t(n) * 48, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxCreateContactConstraintsTGS, one contact descriptor per constraint: the two
+// bodies' records (vel0/vel1: 64 B each, txI0/txI1: 64 B, data0/data1: 48 B),
+// the body frames (PxTransform), and contactPoints[contactStart[k] .. +contactCount[k]]
+// (PxContactPoint, 80 B, <= 4 per constraint; friction and restitution are read
+// from the points).  invDt = 1 / (dt / nbPositionIterations), invTotalDt = 1 / dt.
+// Writes each constraint's rows to outRows + k * gbpx_constraint_row_stride()
+// and their used size to outRowBytes[k].
+GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
+                                                 const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
+                                                 const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, float invDt, float invTotalDt,
+                                                 float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, void* outRows,
+                                                 uint32_t* outRowBytes)
+{
+	(void)correlationDistance;
+	if(!n) return GBPX_OK;
+	if(!vel0 || !vel1 || !txI0 || !txI1 || !data0 || !data1 || !frame0 || !frame1 || !contactStart || !contactCount || !outRows || !outRowBytes ||
+	   (nbPoints && !contactPoints) || !(invDt > 0.0f) || !(invTotalDt > 0.0f))
+		return GBPX_ERR_INVALID;
+	for(uint32_t k = 0; k < n; k++)
+		if(contactCount[k] > tgs::MAX_CONTACTS || contactStart[k] + contactCount[k] > nbPoints) return GBPX_ERR_INVALID;
+	TgsStageWorkspace* ws = tgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	const size_t m = n;
+	if(ws->vel0.reserve(16 * m) || ws->vel1.reserve(16 * m) || ws->tx0.reserve(16 * m) || ws->tx1.reserve(16 * m) || ws->data0.reserve(12 * m) ||
+	   ws->data1.reserve(12 * m) || ws->frame0.reserve(7 * m) || ws->frame1.reserve(7 * m) || ws->cStart.reserve(m) || ws->cCount.reserve(m) ||
+	   ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->recs.reserve(m) || ws->recBytes.reserve(m))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel0.ptr, vel0, m * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel1.ptr, vel1, m * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx0.ptr, txI0, m * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx1.ptr, txI1, m * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->data0.ptr, data0, m * 48, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->data1.ptr, data1, m * 48, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->frame0.ptr, frame0, m * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->frame1.ptr, frame1, m * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cStart.ptr, contactStart, m * 4, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cCount.ptr, contactCount, m * 4, cudaMemcpyHostToDevice, s));
+	if(nbPoints) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->points.ptr, contactPoints, size_t(nbPoints) * 80, cudaMemcpyHostToDevice, s));
+	tgs::PrepParams pp;
+	pp.invStepDt = invDt;
+	pp.invTotalDt = invTotalDt;
+	pp.totalDt = 1.0f / invTotalDt;
+	pp.stepDt = 1.0f / invDt;
+	pp.bounceThreshold = bounceThreshold;
+	pp.frictionOffsetThreshold = frictionOffsetThreshold;
+	pp.biasCoefficient = 2.0f * sqrtf(invTotalDt / invDt);
+	tgs::prepDescKernel<<<divUp(n, 128), 128, 0, s>>>(n, ws->vel0.ptr, ws->vel1.ptr, ws->tx0.ptr, ws->tx1.ptr, ws->data0.ptr, ws->data1.ptr,
+	                                                  ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr, ws->points.ptr, pp,
+	                                                  ws->recs.ptr, ws->recBytes.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outRows, ws->recs.ptr, m * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outRowBytes, ws->recBytes.ptr, m * 4, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxSolveConstraintsTGS: rows (n blocks of gbpx_constraint_row_stride() bytes,
+// in solve order, updated in place with the accumulated impulses), constraint
+// k joining bodies bodyA[k], bodyB[k] of the body arrays; the constraints
+// [waveEnds[w-1], waveEnds[w]) touch distinct bodies.  bodyVel/bodyTxI:
+// nbBodies records in the reference's layouts, updated in place; the first
+// nbIntegrate bodies are integrated after every position iteration.
+// dt = time step / nbPositionIterations.
+GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
+                                        void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt)
+{
+	if(!bodyVel || !bodyTxI || !nbBodies || nbIntegrate > nbBodies || !nbPos || !(dt > 0.0f)) return GBPX_ERR_INVALID;
+	if(n && (!rows || !bodyA || !bodyB || !waveEnds || !nbWaves || waveEnds[nbWaves - 1] != n)) return GBPX_ERR_INVALID;
+	for(uint32_t k = 0; k < n; k++)
+		if(bodyA[k] >= nbBodies || bodyB[k] >= nbBodies) return GBPX_ERR_INVALID;
+	TgsStageWorkspace* ws = tgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	const size_t m = n ? n : 1;
+	if(ws->vel.reserve(16 * size_t(nbBodies)) || ws->tx.reserve(16 * size_t(nbBodies)) || ws->bodyA.reserve(m) || ws->bodyB.reserve(m) ||
+	   ws->recs.reserve(m))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel.ptr, bodyVel, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx.ptr, bodyTxI, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
+	if(n)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodyA.ptr, bodyA, size_t(n) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodyB.ptr, bodyB, size_t(n) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->recs.ptr, rows, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyHostToDevice, s));
+	}
+	float elapsed = 0.0f;
+	auto sweep = [&](float minPen) {
+		for(uint32_t w = 0; w < nbWaves; w++)
+		{
+			const uint32_t b = w ? waveEnds[w - 1] : 0u, e = waveEnds[w];
+			if(e > b) tgs::solveWaveRefKernel<<<divUp(e - b, 128), 128, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, minPen, elapsed);
+		}
+	};
+	for(uint32_t it = 0; it < nbPos; it++)
+	{
+		if(n) sweep(-FLT_MAX);
+		if(nbIntegrate) tgs::integrateRefKernel<<<divUp(nbIntegrate, 128), 128, 0, s>>>(ws->vel.ptr, ws->tx.ptr, nbIntegrate, dt);
+		elapsed += dt;
+	}
+	for(uint32_t it = 0; it < nbVel; it++)
+		if(n) sweep(0.0f);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyVel, ws->vel.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyTxI, ws->tx.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
+	if(n) GBPX_CUDA_TRY(cudaMemcpyAsync(rows, ws->recs.ptr, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxIntegrateSolverBodiesTGS: world angular velocity written back into the
+// velocity records, poses (PxTransform) updated in place.
+GBPX_API int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* poses, uint32_t n)
+{
+	if(!n) return GBPX_OK;
+	if(!bodyVel || !bodyTxI || !poses) return GBPX_ERR_INVALID;
+	TgsStageWorkspace* ws = tgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	if(ws->vel.reserve(16 * size_t(n)) || ws->tx.reserve(16 * size_t(n)) || ws->poses.reserve(7 * size_t(n))) return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel.ptr, bodyVel, size_t(n) * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx.ptr, bodyTxI, size_t(n) * 64, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->poses.ptr, poses, size_t(n) * 28, cudaMemcpyHostToDevice, s));
+	tgs::finalizeRefKernel<<<divUp(n, 128), 128, 0, s>>>(ws->vel.ptr, ws->tx.ptr, ws->poses.ptr, n);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyVel, ws->vel.ptr, size_t(n) * 64, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(poses, ws->poses.ptr, size_t(n) * 28, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 	return GBPX_OK;
 }

@@ -1,0 +1,55 @@
+// Layout probe of the immediate-mode types: prints sizeof / offsetof as JSON.
+// Built against the reference's headers (-DPROBE_REFERENCE, by
+// tests/golden/make_layouts.py) or against include/gbpx_immediate.h (by
+// tests/test_immediate_layout.py); the two tables must agree.
+#ifdef PROBE_REFERENCE
+#include "PxImmediateMode.h"
+#include "geometry/PxSphereGeometry.h"
+#include "geometry/PxCapsuleGeometry.h"
+#include "geometry/PxBoxGeometry.h"
+#include "geometry/PxPlaneGeometry.h"
+#include "geomutils/PxContactPoint.h"
+#include "collision/PxCollisionDefs.h"
+#include "solver/PxSolverDefs.h"
+using namespace physx;
+using namespace physx::immediate;
+#else
+#include "gbpx_immediate.h"
+using namespace gbpx_px;
+#endif
+#include <cstdio>
+#include <cstddef>
+#define S(T) printf("\"%s\": %zu,\n", #T, sizeof(T))
+#define O(T, f) printf("\"%s.%s\": %zu,\n", #T, #f, offsetof(T, f))
+int main(){
+ printf("{\n");
+ S(PxTransform); S(PxGeometry); S(PxSphereGeometry); S(PxCapsuleGeometry); S(PxBoxGeometry); S(PxPlaneGeometry);
+ O(PxSphereGeometry, radius); O(PxCapsuleGeometry, radius); O(PxCapsuleGeometry, halfHeight); O(PxBoxGeometry, halfExtents);
+ S(PxContactPoint); O(PxContactPoint, normal); O(PxContactPoint, separation); O(PxContactPoint, point); O(PxContactPoint, maxImpulse);
+ O(PxContactPoint, targetVel); O(PxContactPoint, staticFriction); O(PxContactPoint, materialFlags); O(PxContactPoint, internalFaceIndex1);
+ O(PxContactPoint, dynamicFriction); O(PxContactPoint, restitution); O(PxContactPoint, damping);
+ S(PxCache); O(PxCache, mCachedData); O(PxCache, mCachedSize); O(PxCache, mPairData); O(PxCache, mManifoldFlags);
+ S(PxRigidBodyData); O(PxRigidBodyData, invMass); O(PxRigidBodyData, angularVelocity); O(PxRigidBodyData, body2World); O(PxRigidBodyData, pad);
+ S(PxTGSSolverBodyVel); O(PxTGSSolverBodyVel, angularVelocity); O(PxTGSSolverBodyVel, partitionMask); O(PxTGSSolverBodyVel, deltaAngDt);
+ O(PxTGSSolverBodyVel, maxAngVel); O(PxTGSSolverBodyVel, deltaLinDt); O(PxTGSSolverBodyVel, lockFlags); O(PxTGSSolverBodyVel, isKinematic);
+ S(PxTGSSolverBodyTxInertia); O(PxTGSSolverBodyTxInertia, body2WorldP); O(PxTGSSolverBodyTxInertia, sqrtInvInertia);
+ S(PxTGSSolverBodyData); O(PxTGSSolverBodyData, maxContactImpulse); O(PxTGSSolverBodyData, originalAngularVelocity); O(PxTGSSolverBodyData, penBiasClamp);
+ O(PxTGSSolverBodyData, invMass); O(PxTGSSolverBodyData, nodeIndex); O(PxTGSSolverBodyData, reportThreshold);
+ S(PxConstraintBatchHeader); O(PxConstraintBatchHeader, stride); O(PxConstraintBatchHeader, constraintType);
+ S(PxSolverConstraintDesc); O(PxSolverConstraintDesc, tgsBodyA); O(PxSolverConstraintDesc, tgsBodyB); O(PxSolverConstraintDesc, bodyADataIndex);
+ O(PxSolverConstraintDesc, bodyBDataIndex); O(PxSolverConstraintDesc, linkIndexA); O(PxSolverConstraintDesc, linkIndexB); O(PxSolverConstraintDesc, constraint);
+ O(PxSolverConstraintDesc, writeBack); O(PxSolverConstraintDesc, writeBackFriction); O(PxSolverConstraintDesc, progressA); O(PxSolverConstraintDesc, progressB);
+ O(PxSolverConstraintDesc, constraintLengthOver16);
+ S(PxConstraintInvMassScale);
+ S(PxTGSSolverContactDesc); O(PxTGSSolverContactDesc, invMassScales); O(PxTGSSolverContactDesc, desc); O(PxTGSSolverContactDesc, body0); O(PxTGSSolverContactDesc, body1);
+ O(PxTGSSolverContactDesc, body0TxI); O(PxTGSSolverContactDesc, body1TxI); O(PxTGSSolverContactDesc, bodyData0); O(PxTGSSolverContactDesc, bodyData1);
+ O(PxTGSSolverContactDesc, bodyFrame0); O(PxTGSSolverContactDesc, bodyFrame1); O(PxTGSSolverContactDesc, bodyState0); O(PxTGSSolverContactDesc, bodyState1);
+ O(PxTGSSolverContactDesc, shapeInteraction); O(PxTGSSolverContactDesc, frictionPtr); O(PxTGSSolverContactDesc, contacts); O(PxTGSSolverContactDesc, numContacts);
+ O(PxTGSSolverContactDesc, frictionCount); O(PxTGSSolverContactDesc, hasMaxImpulse); O(PxTGSSolverContactDesc, disableStrongFriction); O(PxTGSSolverContactDesc, hasForceThresholds);
+ O(PxTGSSolverContactDesc, restDistance); O(PxTGSSolverContactDesc, maxCCDSeparation); O(PxTGSSolverContactDesc, contactForces); O(PxTGSSolverContactDesc, startFrictionPatchIndex);
+ O(PxTGSSolverContactDesc, numFrictionPatches); O(PxTGSSolverContactDesc, startContactPatchIndex); O(PxTGSSolverContactDesc, numContactPatches);
+ O(PxTGSSolverContactDesc, axisConstraintCount); O(PxTGSSolverContactDesc, maxImpulse); O(PxTGSSolverContactDesc, torsionalPatchRadius);
+ O(PxTGSSolverContactDesc, minTorsionalPatchRadius); O(PxTGSSolverContactDesc, offsetSlop);
+ printf("\"end\": 0\n}\n");
+ return 0;
+}

@@ -61,3 +61,16 @@ def test_python_bindings_match_header_arity(gbpx_built):
             assert len(fn.argtypes) == n, (name, len(fn.argtypes), n)
             checked += 1
     assert checked >= 20, checked
+
+
+def test_immediate_library_exports_the_reference_entry_points(gbpx_built):
+    """libgbpx_immediate.so exports, with C linkage, every physx::immediate entry
+    point include/gbpx_immediate.h declares, and nothing else."""
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gbpx_immediate.h")).read(), flags=re.S)
+    block = text[text.index('extern "C"'):]
+    declared = sorted(set(re.findall(r"\b(Px\w+)\s*\(", block)))
+    assert len(declared) == 7, declared
+    lib = os.path.join(os.path.dirname(gbpx_built), "libgbpx_immediate.so")
+    out = os.popen("nm -D --defined-only %s" % lib).read()
+    exported = sorted(l.split()[-1] for l in out.splitlines() if " T " in l)
+    assert exported == declared, (exported, declared)
