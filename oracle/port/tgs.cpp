@@ -15,9 +15,11 @@
 //   PxIntegrateSolverBodiesTGS (NpImmediateMode.cpp:1719)
 // with fresh friction data (frictionPtr = NULL), unit mass scales, zero rest
 // distance / offset slop, no torsional friction: the settings of the reference's
-// immediate-mode snippet.  All contacts of a pair are solved through the per-pair
-// row layout (the reference's 4-wide block path computes the same rows with SIMD
-// lanes; its results are compared against this one in the tests).
+// immediate-mode snippet.  Headers of stride 4 follow the reference's 4-wide block
+// path (createFinalizeSolverContacts4Step / setupFinalizeSolverConstraints4Step,
+// lowleveldynamics/src/DyTGSContactPrepBlock.cpp:1398,219; solveContact4_Block
+// :2280), restated one lane at a time; every other constraint follows the
+// per-pair path.  The results equal the reference's bit for bit (tests).
 #include "pxmath.h"
 #include <string.h>
 #include <vector>
@@ -64,7 +66,9 @@ struct PatchRows
 	float invMass0, invMass1, angDom0, angDom1, maxPenBias, staticFriction, dynamicFriction;
 	int pointStart, nbPoints, frictionStart, nbFriction;
 };
-struct ConstraintRows { int bodyA, bodyB; int patchStart, nbPatches; };
+// block: the constraint is one lane of a 4-wide header and uses the block
+// path's rows and solve (createFinalizeSolverContacts4Step, solveContact4_Block)
+struct ConstraintRows { int bodyA, bodyB; int patchStart, nbPatches; bool block; };
 
 struct ContactIn { V3 n; float sep; V3 p; float staticFriction, dynamicFriction, restitution; };
 
@@ -495,6 +499,7 @@ void prepConstraint(int ci, const ContactIn* contacts, int nbContacts, int a, in
 	cr.bodyA = a; cr.bodyB = b;
 	cr.patchStart = int(rows.patches.size());
 	cr.nbPatches = 0;
+	cr.block = false;
 	if(nbContacts == 0) { rows.cons[ci] = cr; return; }
 	Correlation c;
 	createContactPatches(c, contacts, nbContacts, 0.999f);
@@ -602,6 +607,200 @@ void prepConstraint(int ci, const ContactIn* contacts, int nbContacts, int a, in
 	rows.cons[ci] = cr;
 }
 
+// ------------------------------------------------------------ 4-wide block path, one lane
+// PxCreateContactConstraintsTGS sends every header of stride 4 whose four
+// descriptors hold at most 64 contacts through createFinalizeSolverContacts4Step
+// (lowleveldynamics/src/DyTGSContactPrepBlock.cpp:1398), which builds the rows of
+// the four constraints side by side in SIMD lanes
+// (setupFinalizeSolverConstraints4Step, :219), and PxSolveConstraintsTGS solves
+// them with solveContact4_Block (:2280).  The lanes never mix: a lane whose
+// constraint has fewer patches, contacts or anchors than another is padded with
+// rows of zero response that leave every value unchanged.  So each lane is the
+// per-constraint computation below, with the block path's own arithmetic:
+// sums in the order of its multiply-add chains, the transposed inertia product,
+// the unit normal assumed in the solve, friction coefficients pre-scaled by the
+// anchor count and the friction clamp carried across a patch's anchors.
+
+// x*x' + y*y' then + z*z' (V4MulAdd(z, .., V4MulAdd(y, .., V4Mul(x, ..))))
+inline float dotXYZ(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+// z*z' + y*y' then + x*x' (V4MulAdd(x, .., V4MulAdd(y, .., V4Mul(z, ..))))
+inline float dotZYX(V3 a, V3 b) { return (a.z * b.z + a.y * b.y) + a.x * b.x; }
+// the block path's sqrtInvInertia product: lane-transposed columns dotted with v
+inline V3 m33TMulXYZ(const M33& m, V3 v) { return v3(dotXYZ(m.c0, v), dotXYZ(m.c1, v), dotXYZ(m.c2, v)); }
+// QuatRotate4V (physx/include/foundation/PxVecQuat.h:208): V4Dot3 = (x + y) + z
+inline V3 qRotate4V(Q q, V3 v)
+{
+	const float w2 = q.w * q.w + (-0.5f);
+	const V3 a = scale(v, w2);
+	const V3 u = qv(q);
+	const V3 temp = scaleAdd(cross(u, v), q.w, a);
+	return scale(scaleAdd(u, dotXYZ(u, v), temp), 2.0f);
+}
+
+// One lane of setupFinalizeSolverConstraints4Step.  blockDynamic: some
+// constraint of the header has a dynamic body B (the header-wide isDynamic);
+// kinematic bodies B add their velocity terms as the reference's hasKinematic
+// branch does.
+void prepConstraintBlock(int ci, const ContactIn* contacts, int nbContacts, int a, int b, const BodyVel* vels, const BodyTx* txs,
+                         const BodyData* datas, const Tr& f0, const Tr& f1, float invStepDt, float invTotalDt, float totalDt, float bounce,
+                         float fricOffset, float biasCoefficient, bool blockDynamic, Rows& rows)
+{
+	ConstraintRows cr;
+	cr.bodyA = a; cr.bodyB = b;
+	cr.patchStart = int(rows.patches.size());
+	cr.nbPatches = 0;
+	cr.block = true;
+	if(nbContacts == 0) { rows.cons[ci] = cr; return; }
+	Correlation c;
+	createContactPatches(c, contacts, nbContacts, 0.999f);
+	correlatePatches(c, contacts, f0, f1, 0.999f);
+	growPatches(c, contacts, f0, f1, fricOffset + 0.0f);
+
+	const BodyData& d0 = datas[a];
+	const BodyData& d1 = datas[b];
+	// kinematicScale: 1 for a solver body flagged kinematic (static bodies are,
+	// PxConstructStaticSolverBodyTGS); the descriptors of this path carry no
+	// eKINEMATIC_BODY state, so the hasKinematic branch is never taken
+	const float kin0 = vels[a].kinematic ? 1.0f : 0.0f;
+	const float kin1 = vels[b].kinematic ? 1.0f : 0.0f;
+	const bool bKinematic = false;
+	const float invMass0D0 = 1.0f * d0.invMass, invMass1D1 = 1.0f * d1.invMass;
+	const float angDom0 = 1.0f, angDom1 = 1.0f;
+	const float maxPenBias = fmax_(d0.penBiasClamp, d1.penBiasClamp);
+	const V3 p0 = f0.p, p1 = f1.p;
+	const V3 lv0 = d0.origLin, lv1 = d1.origLin, av0 = d0.origAng, av1 = d1.origAng;
+	const M33& s0 = txs[a].sqrtInvInertia;
+	const M33& s1 = txs[b].sqrtInvInertia;
+	const float invDt = invStepDt;
+	const float p8 = std::min(0.8f, biasCoefficient);
+	const float frictionBiasScale = invDt * p8;
+	const float invDtp8 = invDt * p8;
+	const V3 vrel = sub(lv0, lv1);
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		const int count = c.frictionPatchContactCounts[i];
+		if(count == 0) continue;
+		const FrictionPatch& fp = c.frictionPatches[i];
+		const ContactIn& base0 = contacts[c.contactPatches[c.correlationListHeads[i]].start];
+		const float restitution = -base0.restitution;   // the block setup negates restitution
+		PatchRows pr;
+		pr.invMass0 = invMass0D0;
+		pr.invMass1 = invMass1D1;
+		pr.angDom0 = angDom0; pr.angDom1 = angDom1;
+		const V3 n = base0.n;
+		pr.normal = n;
+		pr.maxPenBias = maxPenBias;
+		const float norVel0 = dotXYZ(n, lv0), norVel1 = dotXYZ(n, lv1);
+		const float relNorVel = norVel0 - norVel1;
+		pr.pointStart = int(rows.points.size());
+		for(int patch = c.correlationListHeads[i]; patch != -1; patch = c.contactPatches[patch].next)
+		{
+			const Correlation::ContactPatch& cp = c.contactPatches[patch];
+			for(int j = 0; j < cp.count; j++)
+			{
+				const ContactIn& ct = contacts[cp.start + j];
+				PointRow row;
+				const float cTargetNorVel = dotZYX(zero3(), n);   // contact target velocity is zero
+				const V3 ra = sub(ct.p, p0), rb = sub(ct.p, p1);
+				const V3 raXn = cross(ra, n), rbXn = cross(rb, n);
+				const float relAngVel0 = dotXYZ(raXn, av0), relAngVel1 = dotXYZ(rbXn, av1);
+				// offsetSlop == 0: no raXn/rbXn component is cleared
+				const V3 dav0 = m33TMulXYZ(s0, raXn);
+				const float dot0 = dotZYX(dav0, dav0);
+				float unitResponse = dot0 * angDom0 + invMass0D0;
+				const float vrel0 = norVel0 + relAngVel0, vrel1 = norVel1 + relAngVel1;
+				V3 dav1 = zero3();
+				if(blockDynamic)
+				{
+					dav1 = m33TMulXYZ(s1, rbXn);
+					const float dot1 = dotZYX(dav1, dav1);
+					unitResponse = unitResponse + (dot1 * angDom1 + invMass1D1);
+				}
+				const float vrelD = vrel0 - vrel1;
+				float penetration = ct.sep - 0.0f;
+				const float penInvDt = penetration * invTotalDt;
+				const bool isSeparated = penetration > 0.0f;
+				const bool isGreater2 = (0.0f > restitution && bounce > vrelD) && (-vrelD > penInvDt);
+				const float ratio = isGreater2 ? totalDt + penetration / vrelD : 0.0f;
+				const float recipResponse = unitResponse > 0.0f ? 1.0f / unitResponse : 0.0f;
+				// restitution >= 0: not a compliant contact
+				const float velMultiplier = recipResponse;
+				const float scaledBias = -(isSeparated ? invDt : invDtp8);
+				const float targetVelocity = (vrel1 * kin1 + (isGreater2 ? vrelD * restitution : 0.0f)) - vrel0 * kin0;
+				penetration = targetVelocity * ratio + penetration;
+				row.raXnI = dav0;
+				row.rbXnI = dav1;
+				row.velMultiplier = velMultiplier;
+				row.targetVelocity = cTargetNorVel + targetVelocity;
+				row.separation = penetration;
+				row.biasCoefficient = scaledBias;
+				row.recipResponse = recipResponse;
+				row.maxImpulse = FLT_MAX;
+				row.force = 0.0f;
+				rows.points.push_back(row);
+			}
+		}
+		pr.nbPoints = int(rows.points.size()) - pr.pointStart;
+		const float coeff = fp.anchorCount == 2 ? 0.5f : 1.0f;
+		pr.staticFriction = base0.staticFriction * coeff;
+		pr.dynamicFriction = base0.dynamicFriction * coeff;
+		pr.frictionStart = int(rows.friction.size());
+		pr.nbFriction = fp.anchorCount * 2;
+		if(fp.anchorCount)
+		{
+			const bool cond = 0.70710678f > fabsf(n.x);
+			const V3 fallback = cond ? v3(0.0f, -n.z, n.y) : v3(-n.y, n.x, 0.0f);
+			const V3 vs = v3(vrel.x - n.x * relNorVel, vrel.y - n.y * relNorVel, vrel.z - n.z * relNorVel);
+			V3 t0 = dotZYX(vs, vs) > 0.0001f ? vs : fallback;
+			const float recipLen = 1.0f / sqrtf(dotXYZ(t0, t0));
+			t0 = scale(t0, recipLen);
+			const V3 t1 = cross(n, t0);
+			for(int j = 0; j < fp.anchorCount; j++)
+			{
+				const V3 ra = qRotate4V(f0.q, fp.body0Anchors[j]);
+				const V3 rb = qRotate4V(f1.q, fp.body1Anchors[j]);
+				const V3 error = sub(add(ra, p0), add(rb, p1));
+				for(int dir = 0; dir < 2; dir++)
+				{
+					const V3 t = dir == 0 ? t0 : t1;
+					const V3 raXn = cross(ra, t);
+					const V3 dav0 = m33TMulXYZ(s0, raXn);
+					float resp = dotXYZ(dav0, dav0) * angDom0 + invMass0D0;
+					const float tVel0 = dotXYZ(t, lv0);
+					const float vrel0 = ((tVel0 + raXn.x * av0.x) + raXn.y * av0.y) + raXn.z * av0.z;
+					V3 dav1 = zero3();
+					float vrel1 = 0.0f;
+					if(blockDynamic || bKinematic)
+					{
+						const V3 rbXn = cross(rb, t);
+						if(blockDynamic)
+						{
+							dav1 = m33TMulXYZ(s1, rbXn);
+							resp = resp + (dotXYZ(dav1, dav1) * angDom1 + invMass1D1);
+						}
+						const float tVel1 = dotXYZ(t, lv1);
+						vrel1 = ((tVel1 + rbXn.x * av1.x) + rbXn.y * av1.y) + rbXn.z * av1.z;
+					}
+					FrictionRow fr;
+					fr.normal = t;
+					fr.raXnI = dav0;
+					fr.rbXnI = dav1;
+					fr.velMultiplier = resp > 0.0f ? p8 / resp : 0.0f;
+					fr.error = dotXYZ(t, error);
+					fr.targetVel = (vrel1 * kin1 + dotXYZ(t, zero3())) - vrel0 * kin0;
+					fr.biasScale = frictionBiasScale;
+					fr.frictionScale = 1.0f;
+					fr.appliedForce = 0.0f;
+					rows.friction.push_back(fr);
+				}
+			}
+		}
+		rows.patches.push_back(pr);
+		cr.nbPatches++;
+	}
+	rows.cons[ci] = cr;
+}
+
 // ------------------------------------------------------------ solve
 void solveConstraint(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float minPen, float elapsed)
 {
@@ -686,6 +885,97 @@ void solveConstraint(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float 
 		}
 	}
 	b0.lin = lin0; b1.lin = lin1; b0.ang = ang0; b1.ang = ang1;
+}
+
+// One lane of solveContact4_Block (DyTGSContactPrepBlock.cpp:2280).  The linear
+// part of the normal velocity is carried as relVel1 += (invMassA + invMassB) *
+// deltaF and the linear velocities move once per patch; friction uses the
+// pre-scaled coefficients, a 1e-5 allowance on the static bound, and once one
+// anchor pair of a patch exceeds it the rest of the patch is clamped to the
+// dynamic bound too.
+void solveConstraintBlock(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float minPen, float elapsed)
+{
+	BodyVel& b0 = vels[cr.bodyA];
+	BodyVel& b1 = vels[cr.bodyB];
+	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
+	const V3 angD0v = b0.dAng, angD1v = b1.dAng;
+	const V3 linDelta = sub(b0.dLin, b1.dLin);
+	for(int p = 0; p < cr.nbPatches; p++)
+	{
+		PatchRows& pr = rows.patches[cr.patchStart + p];
+		const V3 n = pr.normal;
+		const float invMassA = pr.invMass0, invMassB = pr.invMass1;
+		const float sumInvMass = invMassA + invMassB;
+		const float angD0 = pr.angDom0, angD1 = pr.angDom1;
+		float relVel1 = dotXYZ(lin0, n) - dotXYZ(lin1, n);
+		const float deltaNormalV = dotXYZ(linDelta, n);
+		float accumDeltaF = 0.0f, accumulated = 0.0f;
+		for(int i = 0; i < pr.nbPoints; i++)
+		{
+			PointRow& c = rows.points[pr.pointStart + i];
+			const float applied = c.force;
+			const float normalVel = relVel1 + (dotXYZ(c.raXnI, ang0) - dotXYZ(c.rbXnI, ang1));
+			const float deltaAng = dotXYZ(angD0v, c.raXnI) - dotXYZ(angD1v, c.rbXnI);
+			const float targetVel = c.targetVelocity;
+			const float deltaBias = (deltaNormalV + deltaAng) - targetVel * elapsed;
+			const float sep = fmax_(minPen, c.separation + deltaBias);
+			const float bias = fmin_(-pr.maxPenBias, c.biasCoefficient * sep);
+			const float tVelBias = bias * c.recipResponse;
+			const float _deltaF = fmax_(tVelBias - (normalVel - targetVel) * c.velMultiplier, -applied);
+			const float newForce = fmin_(applied + _deltaF, c.maxImpulse);
+			const float deltaF = newForce - applied;
+			accumDeltaF = accumDeltaF + deltaF;
+			const float angDeltaF0 = deltaF * angD0, angDeltaF1 = deltaF * angD1;
+			relVel1 = sumInvMass * deltaF + relVel1;
+			ang0 = add(scale(c.raXnI, angDeltaF0), ang0);
+			ang1 = sub(ang1, scale(c.rbXnI, angDeltaF1));
+			c.force = newForce;
+			accumulated = accumulated + newForce;
+		}
+		const float accIM0 = accumDeltaF * invMassA, accIM1 = accumDeltaF * invMassB;
+		lin0 = add(scale(n, accIM0), lin0);
+		lin1 = sub(lin1, scale(n, accIM1));
+		if(pr.nbFriction)
+		{
+			const float maxF = pr.staticFriction * accumulated + 1e-5f;
+			const float maxDynF = pr.dynamicFriction * accumulated;
+			bool broken = false;
+			for(int i = 0; i < pr.nbFriction; i += 2)
+			{
+				FrictionRow& f0 = rows.friction[pr.frictionStart + i];
+				FrictionRow& f1 = rows.friction[pr.frictionStart + i + 1];
+				const float nv0 = (dotXYZ(lin0, f0.normal) + dotXYZ(f0.raXnI, ang0)) - (dotXYZ(lin1, f0.normal) + dotXYZ(f0.rbXnI, ang1));
+				const float nv1 = (dotXYZ(lin0, f1.normal) + dotXYZ(f1.raXnI, ang0)) - (dotXYZ(lin1, f1.normal) + dotXYZ(f1.rbXnI, ang1));
+				const float dv0 = dotXYZ(linDelta, f0.normal), dv1 = dotXYZ(linDelta, f1.normal);
+				const float da0 = dotXYZ(angD0v, f0.raXnI) - dotXYZ(angD1v, f0.rbXnI);
+				const float da1 = dotXYZ(angD0v, f1.raXnI) - dotXYZ(angD1v, f1.rbXnI);
+				const float e0 = f0.error + ((dv0 + da0) - f0.targetVel * elapsed);
+				const float e1 = f1.error + ((dv1 + da1) - f1.targetVel * elapsed);
+				const float bias0 = e0 * f0.biasScale, bias1 = e1 * f1.biasScale;
+				const float tmp10 = f0.appliedForce - (bias0 - f0.targetVel) * f0.velMultiplier;
+				const float tmp11 = f1.appliedForce - (bias1 - f1.targetVel) * f1.velMultiplier;
+				const float ti0 = tmp10 - nv0 * f0.velMultiplier;
+				const float ti1 = tmp11 - nv1 * f1.velMultiplier;
+				const float total = sqrtf(ti0 * ti0 + ti1 * ti1);
+				broken = broken || total > maxF;
+				const float totalClamped = broken ? fmin_(total, maxDynF) : total;
+				const float ratio = total > 0.0f ? totalClamped / total : 0.0f;
+				const float nf0 = ti0 * ratio, nf1 = ti1 * ratio;
+				const float df0 = nf0 - f0.appliedForce, df1 = nf1 - f1.appliedForce;
+				f0.appliedForce = nf0;
+				f1.appliedForce = nf1;
+				const float im00 = df0 * invMassA, im10 = df0 * invMassB, ad00 = df0 * angD0, ad10 = df0 * angD1;
+				const float im01 = df1 * invMassA, im11 = df1 * invMassB, ad01 = df1 * angD0, ad11 = df1 * angD1;
+				lin0 = add(scale(f0.normal, im00), add(scale(f1.normal, im01), lin0));
+				lin1 = sub(sub(lin1, scale(f1.normal, im11)), scale(f0.normal, im10));
+				ang0 = add(scale(f0.raXnI, ad00), add(scale(f1.raXnI, ad01), ang0));
+				ang1 = sub(sub(ang1, scale(f1.rbXnI, ad11)), scale(f0.rbXnI, ad10));
+			}
+		}
+	}
+	b0.lin = lin0; b0.ang = ang0;
+	// body B is stored only when its data index is not 0 (:2731-2750)
+	if(cr.bodyB != 0) { b1.lin = lin1; b1.ang = ang1; }
 }
 
 void integrateStep(BodyVel& v, BodyTx& t, float dt)
@@ -792,6 +1082,25 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 	const float prepDt = 1.0f / invStepDt;
 	Rows rows;
 	rows.cons.resize(nbConstraints);
+	// headers of stride 4 holding at most 64 contacts take the block path
+	// (NpImmediateMode.cpp:1422-1444); isDynamic is per header
+	std::vector<char> inBlock(nbConstraints, 0), blockDynamic(nbConstraints, 0);
+	for(size_t h = 0; h < batch.headerStart.size(); h++)
+	{
+		if(batch.headerStride[h] != 4) continue;
+		const uint32_t s = batch.headerStart[h];
+		uint32_t total = 0;
+		bool dyn = false;
+		for(uint32_t l = 0; l < 4; l++)
+		{
+			const int ci = batch.order[s + l];
+			if(ci < 0) continue;
+			total += contactCount[ci];
+			dyn = dyn || pairB[ci] < nbDyn;
+		}
+		if(total > 64) continue;
+		for(uint32_t l = 0; l < 4; l++) { inBlock[s + l] = 1; blockDynamic[s + l] = dyn; }
+	}
 	std::vector<ContactIn> cin;
 	for(uint32_t k = 0; k < nbConstraints; k++)
 	{
@@ -808,21 +1117,30 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 			cin[c].dynamicFriction = material[3 * ci + 1];
 			cin[c].restitution = material[3 * ci + 2];
 		}
-		prepConstraint(ci, cin.data(), int(contactCount[ci]), int(pairA[ci]), int(pairB[ci]), vels.data(), txs.data(), datas.data(),
-		               poses[pairA[ci]], poses[pairB[ci]], invStepDt, invDt, totalDt, prepDt, bounceThreshold, frictionOffsetThreshold,
-		               biasCoefficient, rows);
+		if(inBlock[k])
+			prepConstraintBlock(ci, cin.data(), int(contactCount[ci]), int(pairA[ci]), int(pairB[ci]), vels.data(), txs.data(), datas.data(),
+			                    poses[pairA[ci]], poses[pairB[ci]], invStepDt, invDt, totalDt, bounceThreshold, frictionOffsetThreshold,
+			                    biasCoefficient, blockDynamic[k] != 0, rows);
+		else
+			prepConstraint(ci, cin.data(), int(contactCount[ci]), int(pairA[ci]), int(pairB[ci]), vels.data(), txs.data(), datas.data(),
+			               poses[pairA[ci]], poses[pairB[ci]], invStepDt, invDt, totalDt, prepDt, bounceThreshold, frictionOffsetThreshold,
+			               biasCoefficient, rows);
 	}
+	auto solve = [&](const ConstraintRows& cr, float minPen, float el) {
+		if(cr.block) solveConstraintBlock(cr, rows, vels.data(), minPen, el);
+		else solveConstraint(cr, rows, vels.data(), minPen, el);
+	};
 	float elapsed = 0.0f;
 	for(uint32_t it = 0; it < nbPos; it++)
 	{
 		for(uint32_t k = 0; k < nbConstraints; k++)
-			if(batch.order[k] >= 0) solveConstraint(rows.cons[batch.order[k]], rows, vels.data(), -FLT_MAX, elapsed);
+			if(batch.order[k] >= 0) solve(rows.cons[batch.order[k]], -FLT_MAX, elapsed);
 		for(uint32_t j = 0; j < nbDyn; j++) integrateStep(vels[j], txs[j], stepDt);
 		elapsed += stepDt;
 	}
 	for(uint32_t it = 0; it < nbVel; it++)
 		for(uint32_t k = 0; k < nbConstraints; k++)
-			if(batch.order[k] >= 0) solveConstraint(rows.cons[batch.order[k]], rows, vels.data(), 0.0f, elapsed);
+			if(batch.order[k] >= 0) solve(rows.cons[batch.order[k]], 0.0f, elapsed);
 	// PxIntegrateSolverBodiesTGS
 	for(uint32_t a = 0; a < nbDyn; a++)
 	{

@@ -41,6 +41,9 @@ def test_oracle_pyramid_statistics_match_reference():
         top.append(rb["p"][:, 1].max())
         low.append(rb["p"][:, 1].min())
     check_stats(ref, np.array(ke), np.array(top), np.array(low), float(np.abs(rb["p"][:, 0] - sc["rigid"]["p"][:, 0]).mean()))
+    # the oracle follows the reference's arithmetic exactly: its 300-step trace is the reference's
+    assert np.array_equal(np.array(ke), ref["ke"]) and np.array_equal(np.array(top), ref["top"])
+    assert np.array_equal(np.array(low), ref["low"])
 
 
 @pytest.mark.gpu

@@ -108,13 +108,13 @@ def test_oracle_contacts_match_reference_live(seed, types):
 TGS_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "tgs_*.npz")))
 
 # Velocity tolerance of one TGS solve against the reference, relative to the
-# body's speed (floor 1e-2 m/s): the reference solves 4-constraint headers
-# through its 4-wide SIMD block path (DyTGSContactPrepBlock.cpp:1398,
-# solveContact4_Block :2280), which reassociates the per-pair arithmetic this
-# build follows; the resulting differences stay below 2e-4 relative.  Poses are
-# compared at 2e-6 absolute.
-TGS_VEL_REL_TOL = 2e-4
-TGS_POSE_TOL = 2e-6
+# body's speed (floor 1e-2 m/s), and pose tolerance (absolute).  The oracle
+# restates both of the reference's contact paths (per-pair rows, and the 4-wide
+# block path of DyTGSContactPrepBlock.cpp:1398 / solveContact4_Block :2280 for
+# headers of stride 4) in the reference's evaluation order, so the oracle is
+# held to exact equality; the device code is held to these bounds.
+TGS_VEL_REL_TOL = 1e-5
+TGS_POSE_TOL = 1e-6
 
 
 def load_tgs_fixture(path):
@@ -142,8 +142,7 @@ def test_oracle_tgs_matches_reference_golden(path):
     # batching is reproduced exactly
     assert np.array_equal(hs, z["ref_header_start"]) and np.array_equal(hst, z["ref_header_stride"])
     assert np.array_equal(order, z["ref_order"])
-    assert velocity_error(z["ref_velocity"], vel) <= TGS_VEL_REL_TOL
-    assert np.abs(pose - z["ref_pose"]).max() <= TGS_POSE_TOL
+    assert np.array_equal(vel, z["ref_velocity"]) and np.array_equal(pose, z["ref_pose"])
 
 
 SCENE_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "scene_*.npz")))
@@ -172,8 +171,22 @@ def test_oracle_scene_step_matches_reference_golden(path):
     from physx_gb300.world import DEFAULT_PARAMS
     scenes, ref = load_scene_fixture(path)
     out = run_scene_step("orc", scenes, DEFAULT_PARAMS, steps=1)
-    assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= TGS_VEL_REL_TOL
-    assert np.abs(out["p"] - ref["p"]).max() <= TGS_POSE_TOL and np.abs(out["q"] - ref["q"]).max() <= TGS_POSE_TOL
+    assert np.array_equal(rigid_velocity(ref), rigid_velocity(out))
+    assert np.array_equal(out["p"], ref["p"]) and np.array_equal(out["q"], ref["q"])
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed", [100, 101, 102])
+def test_oracle_scene_steps_match_reference_live(seed):
+    """Mixed sphere/capsule/box piles, 20 frames: the oracle equals the reference bit for bit."""
+    from oracle_libs import run_scene_step
+    from scenarios import pile_scenes
+    sys_path_root()
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = pile_scenes(seed, 3, 60)
+    a = run_scene_step("orc", sc, DEFAULT_PARAMS, steps=20)
+    b = run_scene_step("pxref", sc, DEFAULT_PARAMS, steps=20)
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
 def sys_path_root():
