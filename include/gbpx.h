@@ -129,13 +129,17 @@ int gbpx_tgs_solve(const void* rigidBodies, uint32_t nbDynamic, const float* sta
 uint32_t gbpx_constraint_row_stride(void);
 int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void* outVel, void* outTxI, void* outData);
 /* one descriptor per constraint: both bodies' records (64/64/48 B), frames
- * (PxTransform) and PxContactPoints (80 B); invDt = nbPositionIterations / dt,
- * invTotalDt = 1 / dt.  Rows to outRows + k * stride, used bytes to outRowBytes[k]. */
+ * (PxTransform) and PxContactPoints (80 B); laneFlags[k] (null: all per-pair):
+ * bit 0 = lane of a stride-4 header on the reference's 4-wide block path
+ * (createFinalizeSolverContacts4Step, lowleveldynamics/src/DyTGSContactPrepBlock.cpp:1398),
+ * bit 1 = that header has a dynamic body B, bit 2 = bodyBDataIndex is 0;
+ * invDt = nbPositionIterations / dt, invTotalDt = 1 / dt.  Rows to
+ * outRows + k * stride, used bytes to outRowBytes[k]. */
 int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
                                         const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
-                                        const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, float invDt, float invTotalDt,
-                                        float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, void* outRows,
-                                        uint32_t* outRowBytes);
+                                        const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, const uint8_t* laneFlags,
+                                        float invDt, float invTotalDt, float bounceThreshold, float frictionOffsetThreshold,
+                                        float correlationDistance, void* outRows, uint32_t* outRowBytes);
 /* rows (n x stride, solve order, impulses updated in place); constraint k joins
  * bodyA[k], bodyB[k]; constraints in [waveEnds[w-1], waveEnds[w]) touch distinct
  * bodies; the first nbIntegrate bodies are integrated every position iteration;

@@ -153,7 +153,7 @@ GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uin
 	for(uint32_t k = 0; k < n; k++)
 	{
 		const PxTGSSolverContactDesc& d = contactDescs[k];
-		if(d.numContacts > 4 || d.restDistance != 0.0f || d.hasMaxImpulse || d.invMassScales.linear0 != 1.0f || d.invMassScales.angular0 != 1.0f ||
+		if(!d.desc || d.numContacts > 4 || d.restDistance != 0.0f || d.hasMaxImpulse || d.invMassScales.linear0 != 1.0f || d.invMassScales.angular0 != 1.0f ||
 		   d.invMassScales.linear1 != 1.0f || d.invMassScales.angular1 != 1.0f || (d.bodyState0 & eARTICULATION) || (d.bodyState1 & eARTICULATION))
 			return false;
 		v0[k] = d.body0 ? *d.body0 : zeroVel;
@@ -170,12 +170,29 @@ GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uin
 		cc[k] = d.numContacts;
 		points.insert(points.end(), d.contacts, d.contacts + d.numContacts);
 	}
+	// a header of stride 4 with at most 64 contacts is built by the reference's
+	// 4-wide block path (NpImmediateMode.cpp:1422-1444); isDynamic is per header
+	std::vector<uint8_t> laneFlags(n, 0);
+	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
+	{
+		if(batchHeaders[h].stride != 4) continue;
+		uint32_t total = 0;
+		bool dyn = false;
+		for(uint32_t l = 0; l < 4; l++)
+		{
+			total += contactDescs[k + l].numContacts;
+			dyn = dyn || contactDescs[k + l].bodyState1 == eDYNAMIC_BODY;
+		}
+		if(total > 64) continue;
+		for(uint32_t l = 0; l < 4; l++)
+			laneFlags[k + l] = uint8_t(1u | (dyn ? 2u : 0u) | (contactDescs[k + l].desc->bodyBDataIndex == 0 ? 4u : 0u));
+	}
 	const uint32_t stride = gbpx_constraint_row_stride();
 	std::vector<uint8_t> rows(size_t(n) * stride);
 	std::vector<uint32_t> bytes(n);
 	if(gbpx_create_contact_constraints_tgs(n, v0.data(), v1.data(), x0.data(), x1.data(), d0.data(), d1.data(), &f0[0].q.x, &f1[0].q.x, cs.data(),
-	                                       cc.data(), points.data(), uint32_t(points.size()), invDt, invTotalDt, bounceThreshold,
-	                                       frictionOffsetThreshold, correlationDistance, rows.data(), bytes.data()) != GBPX_OK)
+	                                       cc.data(), points.data(), uint32_t(points.size()), laneFlags.data(), invDt, invTotalDt,
+	                                       bounceThreshold, frictionOffsetThreshold, correlationDistance, rows.data(), bytes.data()) != GBPX_OK)
 		return false;
 	for(uint32_t k = 0; k < n; k++)
 	{

@@ -60,14 +60,22 @@ struct __align__(16) PatchRows
 // One constraint's rows, packed after a 16-byte header so that a constraint
 // touches as few cache lines as it has rows: patches, points, friction rows
 // (two per anchor), normal impulses, friction impulses.
+// Flags in the high byte of ConstraintRecord::counts.  REC_BLOCK: the rows were
+// built, and are solved, by the 4-wide block path (one lane of a header of
+// stride 4).  REC_KEEP_B: the block solve leaves body B's velocity as it was
+// (the reference stores body B only when its data index is not 0).
+constexpr int REC_BLOCK = 1 << 24;
+constexpr int REC_KEEP_B = 1 << 25;
 struct __align__(16) ConstraintRecord
 {
-	int bodyA, bodyB, nbPatches, counts;   // counts = points | friction rows << 16
+	int bodyA, bodyB, nbPatches, counts;   // counts = points | friction rows << 16 | flags
 	float4 rows[(MAX_CONTACTS * sizeof(PatchRows) + MAX_CONTACTS * sizeof(PointRow) + MAX_FRICTION * sizeof(FrictionRow) +
 	             (MAX_CONTACTS + MAX_FRICTION) * 4 + 15) / 16];
 
 	__device__ __forceinline__ int nbPoints() const { return counts & 0xffff; }
-	__device__ __forceinline__ int nbFriction() const { return counts >> 16; }
+	__device__ __forceinline__ int nbFriction() const { return (counts >> 16) & 0xff; }
+	__device__ __forceinline__ bool isBlock() const { return (counts & REC_BLOCK) != 0; }
+	__device__ __forceinline__ bool keepB() const { return (counts & REC_KEEP_B) != 0; }
 	__device__ __forceinline__ PatchRows* patch() { return reinterpret_cast<PatchRows*>(rows); }
 	__device__ __forceinline__ PointRow* point() { return reinterpret_cast<PointRow*>(reinterpret_cast<char*>(rows) + nbPatches * sizeof(PatchRows)); }
 	__device__ __forceinline__ FrictionRow* friction()
@@ -461,6 +469,188 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 	}
 }
 
+// ------------------------------------------------------------- 4-wide block path, one lane
+// PxCreateContactConstraintsTGS builds a header of stride 4 (at most 64
+// contacts) with createFinalizeSolverContacts4Step
+// (lowleveldynamics/src/DyTGSContactPrepBlock.cpp:1398, rows from
+// setupFinalizeSolverConstraints4Step :219) and PxSolveConstraintsTGS solves it
+// with solveContact4_Block (:2280).  Its four SIMD lanes never exchange values
+// (a lane with fewer patches, points or anchors gets rows of zero response), so
+// one lane is the per-constraint computation below, in the block path's own
+// evaluation order.  A GB300 thread runs one lane.
+
+// x*x' + y*y' then + z*z' (the block path's V4MulAdd(z, .., V4MulAdd(y, .., V4Mul(x, ..))))
+__device__ __forceinline__ float dotXYZ(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+// z*z' + y*y' then + x*x'
+__device__ __forceinline__ float dotZYX(V3 a, V3 b) { return (a.z * b.z + a.y * b.y) + a.x * b.x; }
+// sqrtInvInertia product of the block path: lane-transposed columns dotted with v
+__device__ __forceinline__ V3 m33TMulXYZ(const M33& m, V3 v) { return v3(dotXYZ(m.c0, v), dotXYZ(m.c1, v), dotXYZ(m.c2, v)); }
+// QuatRotate4V (physx/include/foundation/PxVecQuat.h:208), V4Dot3 = (x + y) + z
+__device__ __forceinline__ V3 qRotate4V(Q q, V3 v)
+{
+	const float w2 = q.w * q.w + (-0.5f);
+	const V3 a = scale(v, w2);
+	const V3 u = qv(q);
+	const V3 temp = scaleAdd(cross(u, v), q.w, a);
+	return scale(scaleAdd(u, dotXYZ(u, v), temp), 2.0f);
+}
+
+// Rows of one lane.  blockDynamic: some constraint of the header has a dynamic
+// body B (the header-wide isDynamic; passing "this lane's body B is dynamic"
+// gives the same values when no body B is kinematic).  keepB: body B's data
+// index is 0, so the block solve does not store body B.
+__device__ __forceinline__ void prepConstraintBlock(const Contact* contacts, int nbContacts, int a, int b, const BodyVel& va, const BodyVel& vb,
+                                                    const BodyTx& ta, const BodyTx& tb, const BodyData& d0, const BodyData& d1, const Tr& f0,
+                                                    const Tr& f1, const PrepParams& pp, bool blockDynamic, bool keepB, ConstraintRecord& rec)
+{
+	rec.bodyA = a;
+	rec.bodyB = b;
+	rec.nbPatches = 0;
+	rec.counts = REC_BLOCK | (keepB ? REC_KEEP_B : 0);
+	if(nbContacts == 0) return;
+	Correlation c;
+	createContactPatches(c, contacts, nbContacts, 0.999f);
+	correlatePatches(c, contacts, 0.999f);
+	growPatches(c, contacts, f0, f1, pp.frictionOffsetThreshold + 0.0f);
+
+	int usedPatches = 0, totalPoints = 0, totalFriction = 0;
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		if(c.fpContactCount[i] == 0) continue;
+		usedPatches++;
+		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch]) totalPoints += c.cpCount[patch];
+		totalFriction += c.fpAnchorCount[i] * 2;
+	}
+	rec.nbPatches = usedPatches;
+	rec.counts |= totalPoints | (totalFriction << 16);
+	PatchRows* patchRows = rec.patch();
+	PointRow* pointRows = rec.point();
+	FrictionRow* frictionRows = rec.friction();
+	float* force = rec.force();
+	float* frictionForce = rec.frictionForce();
+	// kinematicScale: 1 for a solver body flagged kinematic (statics are); no
+	// descriptor of this path has the eKINEMATIC_BODY state
+	const float kin0 = va.kinematic ? 1.0f : 0.0f, kin1 = vb.kinematic ? 1.0f : 0.0f;
+	const float invMass0D0 = 1.0f * d0.invMass, invMass1D1 = 1.0f * d1.invMass;
+	const float angDom0 = 1.0f, angDom1 = 1.0f;
+	const float maxPenBias = fmax_(d0.penBiasClamp, d1.penBiasClamp);
+	const V3 p0 = f0.p, p1 = f1.p;
+	const V3 lv0 = d0.origLin, lv1 = d1.origLin, av0 = d0.origAng, av1 = d1.origAng;
+	const M33& s0 = ta.sqrtInvInertia;
+	const M33& s1 = tb.sqrtInvInertia;
+	const float invDt = pp.invStepDt;
+	const float p8 = fmin_(0.8f, pp.biasCoefficient);
+	const float frictionBiasScale = invDt * p8;
+	const float invDtp8 = invDt * p8;
+	const V3 vrel = sub(lv0, lv1);
+	int patchOut = 0, nPoints = 0, nFriction = 0;
+	for(int i = 0; i < c.frictionPatchCount; i++)
+	{
+		if(c.fpContactCount[i] == 0) continue;
+		const Contact& base0 = contacts[c.cpStart[c.listHead[i]]];
+		const float restitution = -base0.restitution;   // negated by the block setup
+		PatchRows& pr = patchRows[patchOut];
+		pr.invMass0 = invMass0D0;
+		pr.invMass1 = invMass1D1;
+		const V3 n = base0.n;
+		pr.normal = n;
+		pr.maxPenBias = maxPenBias;
+		const float norVel0 = dotXYZ(n, lv0), norVel1 = dotXYZ(n, lv1);
+		const float relNorVel = norVel0 - norVel1;
+		pr.pointStart = nPoints;
+		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch])
+			for(int j = 0; j < c.cpCount[patch]; j++)
+			{
+				const Contact& ct = contacts[c.cpStart[patch] + j];
+				PointRow& row = pointRows[nPoints];
+				const float cTargetNorVel = dotZYX(zero3(), n);
+				const V3 ra = sub(ct.p, p0), rb = sub(ct.p, p1);
+				const V3 raXn = cross(ra, n), rbXn = cross(rb, n);
+				const float relAngVel0 = dotXYZ(raXn, av0), relAngVel1 = dotXYZ(rbXn, av1);
+				const V3 dav0 = m33TMulXYZ(s0, raXn);
+				float unitResponse = dotZYX(dav0, dav0) * angDom0 + invMass0D0;
+				const float vrel0 = norVel0 + relAngVel0, vrel1 = norVel1 + relAngVel1;
+				V3 dav1 = zero3();
+				if(blockDynamic)
+				{
+					dav1 = m33TMulXYZ(s1, rbXn);
+					unitResponse = unitResponse + (dotZYX(dav1, dav1) * angDom1 + invMass1D1);
+				}
+				const float vrelD = vrel0 - vrel1;
+				float penetration = ct.sep - 0.0f;
+				const float penInvDt = penetration * pp.invTotalDt;
+				const bool isSeparated = penetration > 0.0f;
+				const bool isGreater2 = (0.0f > restitution && pp.bounceThreshold > vrelD) && (-vrelD > penInvDt);
+				const float ratio = isGreater2 ? pp.totalDt + penetration / vrelD : 0.0f;
+				const float recipResponse = unitResponse > 0.0f ? 1.0f / unitResponse : 0.0f;
+				const float targetVelocity = (vrel1 * kin1 + (isGreater2 ? vrelD * restitution : 0.0f)) - vrel0 * kin0;
+				penetration = targetVelocity * ratio + penetration;
+				row.raXnI = dav0;
+				row.rbXnI = dav1;
+				row.velMultiplier = recipResponse;
+				row.targetVelocity = cTargetNorVel + targetVelocity;
+				row.separation = penetration;
+				row.biasCoefficient = -(isSeparated ? invDt : invDtp8);
+				row.recipResponse = recipResponse;
+				row.maxImpulse = FLT_MAX;
+				force[nPoints] = 0.0f;
+				nPoints++;
+			}
+		pr.nbPoints = nPoints - pr.pointStart;
+		const int anchors = c.fpAnchorCount[i];
+		const float coeff = anchors == 2 ? 0.5f : 1.0f;
+		pr.staticFriction = base0.staticFriction * coeff;
+		pr.dynamicFriction = base0.dynamicFriction * coeff;
+		pr.frictionStart = nFriction;
+		pr.nbFriction = anchors * 2;
+		if(anchors)
+		{
+			const bool cond = 0.70710678f > fabsf(n.x);
+			const V3 fallback = cond ? v3(0.0f, -n.z, n.y) : v3(-n.y, n.x, 0.0f);
+			const V3 vs = v3(vrel.x - n.x * relNorVel, vrel.y - n.y * relNorVel, vrel.z - n.z * relNorVel);
+			V3 t0 = dotZYX(vs, vs) > 0.0001f ? vs : fallback;
+			const float recipLen = 1.0f / sqrtf(dotXYZ(t0, t0));
+			t0 = scale(t0, recipLen);
+			const V3 t1 = cross(n, t0);
+			for(int j = 0; j < anchors; j++)
+			{
+				const V3 ra = qRotate4V(f0.q, c.fpAnchor0[i][j]);
+				const V3 rb = qRotate4V(f1.q, c.fpAnchor1[i][j]);
+				const V3 error = sub(add(ra, p0), add(rb, p1));
+				for(int dir = 0; dir < 2; dir++)
+				{
+					const V3 t = dir == 0 ? t0 : t1;
+					FrictionRow& fr = frictionRows[nFriction];
+					const V3 raXn = cross(ra, t);
+					const V3 dav0 = m33TMulXYZ(s0, raXn);
+					float resp = dotXYZ(dav0, dav0) * angDom0 + invMass0D0;
+					const float vrel0 = ((dotXYZ(t, lv0) + raXn.x * av0.x) + raXn.y * av0.y) + raXn.z * av0.z;
+					V3 dav1 = zero3();
+					float vrel1 = 0.0f;
+					if(blockDynamic)
+					{
+						const V3 rbXn = cross(rb, t);
+						dav1 = m33TMulXYZ(s1, rbXn);
+						resp = resp + (dotXYZ(dav1, dav1) * angDom1 + invMass1D1);
+						vrel1 = ((dotXYZ(t, lv1) + rbXn.x * av1.x) + rbXn.y * av1.y) + rbXn.z * av1.z;
+					}
+					fr.normal = t;
+					fr.raXnI = dav0;
+					fr.rbXnI = dav1;
+					fr.velMultiplier = resp > 0.0f ? p8 / resp : 0.0f;
+					fr.error = dotXYZ(t, error);
+					fr.targetVel = (vrel1 * kin1 + dotXYZ(t, zero3())) - vrel0 * kin0;
+					fr.biasScale = frictionBiasScale;
+					fr.frictionScale = 1.0f;
+					frictionForce[nFriction] = 0.0f;
+					nFriction++;
+				}
+			}
+		}
+		patchOut++;
+	}
+}
+
 // ------------------------------------------------------------- solve
 // solveContact (DyTGSContactPrep.cpp:1581) for one constraint.  b0/b1 are the
 // constraint's two bodies (b1 may be a static/kinematic body, never written
@@ -559,6 +749,105 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 		b1.lin = lin1;
 		b1.ang = ang1;
 	}
+}
+
+// One lane of solveContact4_Block (DyTGSContactPrepBlock.cpp:2280): the normal
+// velocity's linear part is carried as relVel1 += (invMassA + invMassB) * deltaF
+// and the linear velocities move once per patch; friction uses the pre-scaled
+// coefficients and a 1e-5 allowance on the static bound, and once an anchor
+// pair of a patch exceeds that bound the rest of the patch is clamped to the
+// dynamic bound as well.
+__device__ __forceinline__ void solveConstraintBlock(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+{
+	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
+	const V3 angD0v = b0.dAng, angD1v = b1.dAng;
+	const V3 linDelta = sub(b0.dLin, b1.dLin);
+	const PatchRows* patchRows = rec.patch();
+	const PointRow* pointRows = rec.point();
+	const FrictionRow* frictionRows = rec.friction();
+	float* force = rec.force();
+	float* frictionForce = rec.frictionForce();
+	for(int p = 0; p < rec.nbPatches; p++)
+	{
+		const PatchRows pr = patchRows[p];
+		const V3 n = pr.normal;
+		const float invMassA = pr.invMass0, invMassB = pr.invMass1;
+		const float sumInvMass = invMassA + invMassB;
+		float relVel1 = dotXYZ(lin0, n) - dotXYZ(lin1, n);
+		const float deltaNormalV = dotXYZ(linDelta, n);
+		float accumDeltaF = 0.0f, accumulated = 0.0f;
+		for(int i = 0; i < pr.nbPoints; i++)
+		{
+			const int k = pr.pointStart + i;
+			const PointRow c = pointRows[k];
+			const float applied = force[k];
+			const float normalVel = relVel1 + (dotXYZ(c.raXnI, ang0) - dotXYZ(c.rbXnI, ang1));
+			const float deltaAng = dotXYZ(angD0v, c.raXnI) - dotXYZ(angD1v, c.rbXnI);
+			const float deltaBias = (deltaNormalV + deltaAng) - c.targetVelocity * elapsed;
+			const float sep = fmax_(minPen, c.separation + deltaBias);
+			const float bias = fmin_(-pr.maxPenBias, c.biasCoefficient * sep);
+			const float _deltaF = fmax_(bias * c.recipResponse - (normalVel - c.targetVelocity) * c.velMultiplier, -applied);
+			const float newForce = fmin_(applied + _deltaF, c.maxImpulse);
+			const float deltaF = newForce - applied;
+			accumDeltaF = accumDeltaF + deltaF;
+			relVel1 = sumInvMass * deltaF + relVel1;
+			ang0 = add(scale(c.raXnI, deltaF * 1.0f), ang0);
+			ang1 = sub(ang1, scale(c.rbXnI, deltaF * 1.0f));
+			force[k] = newForce;
+			accumulated = accumulated + newForce;
+		}
+		const float accIM0 = accumDeltaF * invMassA, accIM1 = accumDeltaF * invMassB;
+		lin0 = add(scale(n, accIM0), lin0);
+		lin1 = sub(lin1, scale(n, accIM1));
+		if(pr.nbFriction)
+		{
+			const float maxF = pr.staticFriction * accumulated + 1e-5f;
+			const float maxDynF = pr.dynamicFriction * accumulated;
+			bool broken = false;
+			for(int i = 0; i < pr.nbFriction; i += 2)
+			{
+				const int k0 = pr.frictionStart + i, k1 = k0 + 1;
+				const FrictionRow& f0 = frictionRows[k0];
+				const FrictionRow& f1 = frictionRows[k1];
+				const float nv0 = (dotXYZ(lin0, f0.normal) + dotXYZ(f0.raXnI, ang0)) - (dotXYZ(lin1, f0.normal) + dotXYZ(f0.rbXnI, ang1));
+				const float nv1 = (dotXYZ(lin0, f1.normal) + dotXYZ(f1.raXnI, ang0)) - (dotXYZ(lin1, f1.normal) + dotXYZ(f1.rbXnI, ang1));
+				const float da0 = dotXYZ(angD0v, f0.raXnI) - dotXYZ(angD1v, f0.rbXnI);
+				const float da1 = dotXYZ(angD0v, f1.raXnI) - dotXYZ(angD1v, f1.rbXnI);
+				const float e0 = f0.error + ((dotXYZ(linDelta, f0.normal) + da0) - f0.targetVel * elapsed);
+				const float e1 = f1.error + ((dotXYZ(linDelta, f1.normal) + da1) - f1.targetVel * elapsed);
+				const float a0 = frictionForce[k0], a1 = frictionForce[k1];
+				const float ti0 = (a0 - (e0 * f0.biasScale - f0.targetVel) * f0.velMultiplier) - nv0 * f0.velMultiplier;
+				const float ti1 = (a1 - (e1 * f1.biasScale - f1.targetVel) * f1.velMultiplier) - nv1 * f1.velMultiplier;
+				const float total = sqrtf(ti0 * ti0 + ti1 * ti1);
+				broken = broken || total > maxF;
+				const float totalClamped = broken ? fmin_(total, maxDynF) : total;
+				const float ratio = total > 0.0f ? totalClamped / total : 0.0f;
+				const float nf0 = ti0 * ratio, nf1 = ti1 * ratio;
+				const float df0 = nf0 - a0, df1 = nf1 - a1;
+				frictionForce[k0] = nf0;
+				frictionForce[k1] = nf1;
+				const float im00 = df0 * invMassA, im10 = df0 * invMassB, im01 = df1 * invMassA, im11 = df1 * invMassB;
+				lin0 = add(scale(f0.normal, im00), add(scale(f1.normal, im01), lin0));
+				lin1 = sub(sub(lin1, scale(f1.normal, im11)), scale(f0.normal, im10));
+				ang0 = add(scale(f0.raXnI, df0 * 1.0f), add(scale(f1.raXnI, df1 * 1.0f), ang0));
+				ang1 = sub(sub(ang1, scale(f1.rbXnI, df1 * 1.0f)), scale(f0.rbXnI, df0 * 1.0f));
+			}
+		}
+	}
+	b0.lin = lin0;
+	b0.ang = ang0;
+	if(writeB1 && !rec.keepB())
+	{
+		b1.lin = lin1;
+		b1.ang = ang1;
+	}
+}
+
+// The solve of a constraint record by the path that built it.
+__device__ __forceinline__ void solveRecord(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+{
+	if(rec.isBlock()) solveConstraintBlock(rec, b0, b1, writeB1, minPen, elapsed);
+	else solveConstraint(rec, b0, b1, writeB1, minPen, elapsed);
 }
 
 // integrateCoreStep (DyTGSDynamics.cpp:1403)

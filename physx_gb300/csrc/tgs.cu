@@ -39,11 +39,27 @@ __global__ void constructBodiesKernel(const RigidBody* __restrict__ rigid, uint3
 	}
 }
 
+// Lane flags of a constraint (one byte each): LANE_BLOCK = one lane of a
+// header of stride 4 (the 4-wide block path), LANE_BLOCK_DYNAMIC = that header
+// has a dynamic body B, LANE_KEEP_B = body B's data index is 0.
+constexpr uint8_t LANE_BLOCK = 1, LANE_BLOCK_DYNAMIC = 2, LANE_KEEP_B = 4;
+
+__device__ __forceinline__ void prepByFlags(uint8_t flags, const Contact* cs, int cnt, int a, int b, const BodyVel& va, const BodyVel& vb,
+                                            const BodyTx& ta, const BodyTx& tb, const BodyData& da, const BodyData& db, const Tr& f0, const Tr& f1,
+                                            const PrepParams& pp, ConstraintRecord& rec)
+{
+	if(flags & LANE_BLOCK)
+		prepConstraintBlock(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, (flags & LANE_BLOCK_DYNAMIC) != 0, (flags & LANE_KEEP_B) != 0, rec);
+	else
+		prepConstraint(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, rec);
+}
+
 // Rows for constraint k of the ordered list (ordered[k] = caller's constraint index).
 __global__ void prepKernel(const uint32_t* __restrict__ ordered, uint32_t n, const uint32_t* __restrict__ pairA, const uint32_t* __restrict__ pairB,
                            const uint32_t* __restrict__ cStart, const uint32_t* __restrict__ cCount, const float* __restrict__ contacts,
                            const float* __restrict__ material, const BodyVel* __restrict__ vel, const BodyTx* __restrict__ tx,
-                           const BodyData* __restrict__ data, const Tr* __restrict__ pose, PrepParams pp, ConstraintRecord* __restrict__ recs)
+                           const BodyData* __restrict__ data, const Tr* __restrict__ pose, const uint8_t* __restrict__ laneFlags, PrepParams pp,
+                           ConstraintRecord* __restrict__ recs)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= n) return;
@@ -61,7 +77,7 @@ __global__ void prepKernel(const uint32_t* __restrict__ ordered, uint32_t n, con
 		cs[c].dynamicFriction = material[3 * ci + 1];
 		cs[c].restitution = material[3 * ci + 2];
 	}
-	prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, recs[k]);
+	prepByFlags(laneFlags[k], cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, recs[k]);
 }
 
 __global__ void solvePartitionKernel(ConstraintRecord* __restrict__ recs, uint32_t begin, uint32_t end, BodyVel* __restrict__ vel, uint32_t nbDyn,
@@ -74,7 +90,7 @@ __global__ void solvePartitionKernel(ConstraintRecord* __restrict__ recs, uint32
 	BodyVel b0 = vel[r.bodyA];
 	BodyVel b1 = vel[r.bodyB];
 	const bool dynB = uint32_t(r.bodyB) < nbDyn;
-	solveConstraint(r, b0, b1, dynB, minPen, elapsed);
+	solveRecord(r, b0, b1, dynB, minPen, elapsed);
 	vel[r.bodyA].lin = b0.lin;
 	vel[r.bodyA].ang = b0.ang;
 	if(dynB)
@@ -194,8 +210,8 @@ __global__ void staticBodiesKernel(const float* __restrict__ poses, uint32_t n, 
 __global__ void prepDescKernel(uint32_t n, const float* __restrict__ vel0, const float* __restrict__ vel1, const float* __restrict__ tx0,
                                const float* __restrict__ tx1, const float* __restrict__ data0, const float* __restrict__ data1,
                                const float* __restrict__ frame0, const float* __restrict__ frame1, const uint32_t* __restrict__ cStart,
-                               const uint32_t* __restrict__ cCount, const float* __restrict__ points, PrepParams pp,
-                               ConstraintRecord* __restrict__ recs, uint32_t* __restrict__ recBytes)
+                               const uint32_t* __restrict__ cCount, const float* __restrict__ points, const uint8_t* __restrict__ laneFlags,
+                               PrepParams pp, ConstraintRecord* __restrict__ recs, uint32_t* __restrict__ recBytes)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= n) return;
@@ -219,7 +235,7 @@ __global__ void prepDescKernel(uint32_t n, const float* __restrict__ vel0, const
 	const float* b = frame1 + 7 * size_t(k);
 	f0.q.x = a[0]; f0.q.y = a[1]; f0.q.z = a[2]; f0.q.w = a[3]; f0.p = v3(a[4], a[5], a[6]);
 	f1.q.x = b[0]; f1.q.y = b[1]; f1.q.z = b[2]; f1.q.w = b[3]; f1.p = v3(b[4], b[5], b[6]);
-	prepConstraint(cs, int(cnt), 0, 1, va, vb, ta, tb, da, db, f0, f1, pp, recs[k]);
+	prepByFlags(laneFlags ? laneFlags[k] : uint8_t(0), cs, int(cnt), 0, 1, va, vb, ta, tb, da, db, f0, f1, pp, recs[k]);
 	recBytes[k] = recs[k].bytes();
 }
 
@@ -235,7 +251,7 @@ __global__ void solveWaveRefKernel(ConstraintRecord* __restrict__ recs, const ui
 	float* va = vel + 16 * size_t(bodyA[k]);
 	float* vb = vel + 16 * size_t(bodyB[k]);
 	BodyVel b0 = loadVelRef(va), b1 = loadVelRef(vb);
-	solveConstraint(r, b0, b1, true, minPen, elapsed);
+	solveRecord(r, b0, b1, true, minPen, elapsed);
 	va[0] = b0.lin.x; va[1] = b0.lin.y; va[2] = b0.lin.z; va[4] = b0.ang.x; va[5] = b0.ang.y; va[6] = b0.ang.z;
 	vb[0] = b1.lin.x; vb[1] = b1.lin.y; vb[2] = b1.lin.z; vb[4] = b1.ang.x; vb[5] = b1.ang.y; vb[6] = b1.ang.z;
 }
@@ -280,6 +296,7 @@ struct TgsWorkspace
 	DevBuf<tgs::RigidBody> rigid;
 	DevBuf<float> statics, contacts, material, outVel, outPose, outTx, outData;
 	DevBuf<uint32_t> pairA, pairB, cStart, cCount, ordered;
+	DevBuf<uint8_t> laneFlags;
 	DevBuf<tgs::BodyVel> vel;
 	DevBuf<tgs::BodyTx> tx;
 	DevBuf<tgs::BodyData> data;
@@ -373,6 +390,25 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	if(!ws) return GBPX_ERR_CUDA;
 	batching::Result batch;
 	if(nbConstraints) batching::partition(pairA, pairB, nbConstraints, nbDyn, batch);
+	// headers of stride 4 with at most 64 contacts take the 4-wide block path
+	// (PxCreateContactConstraintsTGS, NpImmediateMode.cpp:1422-1444)
+	std::vector<uint8_t> laneFlags(nbConstraints ? nbConstraints : 1, 0);
+	for(size_t h = 0; h < batch.headerStart.size(); h++)
+	{
+		if(batch.headerStride[h] != 4) continue;
+		const uint32_t s0 = batch.headerStart[h];
+		uint32_t total = 0;
+		bool dyn = false;
+		for(uint32_t l = 0; l < 4; l++)
+		{
+			const uint32_t ci = batch.order[s0 + l];
+			total += contactCount[ci];
+			dyn = dyn || pairB[ci] < nbDyn;
+		}
+		if(total > 64) continue;
+		for(uint32_t l = 0; l < 4; l++)
+			laneFlags[s0 + l] = uint8_t(tgs::LANE_BLOCK | (dyn ? tgs::LANE_BLOCK_DYNAMIC : 0) | (pairB[batch.order[s0 + l]] == 0 ? tgs::LANE_KEEP_B : 0));
+	}
 	uint32_t nbContacts = 0;
 	for(uint32_t i = 0; i < nbConstraints; i++) nbContacts = std::max(nbContacts, contactStart[i] + contactCount[i]);
 	const uint32_t nbTotal = nbDyn + nbStatic;
@@ -380,7 +416,8 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	if(ws->rigid.reserve(nbDyn) || ws->statics.reserve(7 * size_t(nbStatic) + 1) || ws->pairA.reserve(nc) || ws->pairB.reserve(nc) ||
 	   ws->cStart.reserve(nc) || ws->cCount.reserve(nc) || ws->ordered.reserve(nc) || ws->contacts.reserve(8 * size_t(nbContacts) + 8) ||
 	   ws->material.reserve(3 * size_t(nc)) || ws->vel.reserve(nbTotal) || ws->tx.reserve(nbTotal) || ws->data.reserve(nbTotal) ||
-	   ws->pose.reserve(nbTotal) || ws->recs.reserve(nc) || ws->outVel.reserve(6 * size_t(nbDyn)) || ws->outPose.reserve(7 * size_t(nbDyn)))
+	   ws->pose.reserve(nbTotal) || ws->recs.reserve(nc) || ws->outVel.reserve(6 * size_t(nbDyn)) || ws->outPose.reserve(7 * size_t(nbDyn)) ||
+	   ws->laneFlags.reserve(nc))
 		return GBPX_ERR_NOMEM;
 	cudaStream_t s = ws->stream;
 	if(cudaMemcpyAsync(ws->rigid.ptr, rigid, size_t(nbDyn) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, s) != cudaSuccess) return GBPX_ERR_CUDA;
@@ -393,6 +430,7 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 		   cudaMemcpyAsync(ws->cCount.ptr, contactCount, size_t(nbConstraints) * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
 		   cudaMemcpyAsync(ws->ordered.ptr, batch.order.data(), size_t(nbConstraints) * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
 		   cudaMemcpyAsync(ws->material.ptr, material, size_t(nbConstraints) * 12, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+		   cudaMemcpyAsync(ws->laneFlags.ptr, laneFlags.data(), size_t(nbConstraints), cudaMemcpyHostToDevice, s) != cudaSuccess ||
 		   (nbContacts && cudaMemcpyAsync(ws->contacts.ptr, contacts, size_t(nbContacts) * 32, cudaMemcpyHostToDevice, s) != cudaSuccess))
 			return GBPX_ERR_CUDA;
 	}
@@ -412,7 +450,7 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	if(nbConstraints)
 		tgs::prepKernel<<<divUp(nbConstraints, 128), 128, 0, s>>>(ws->ordered.ptr, nbConstraints, ws->pairA.ptr, ws->pairB.ptr, ws->cStart.ptr,
 		                                                          ws->cCount.ptr, ws->contacts.ptr, ws->material.ptr, ws->vel.ptr, ws->tx.ptr,
-		                                                          ws->data.ptr, ws->pose.ptr, pp, ws->recs.ptr);
+		                                                          ws->data.ptr, ws->pose.ptr, ws->laneFlags.ptr, pp, ws->recs.ptr);
 	float elapsed = 0.0f;
 	auto sweep = [&](float minPen) {
 		for(size_t p = 0; p < batch.partitionEnds.size(); p++)
@@ -457,6 +495,7 @@ struct TgsStageWorkspace
 	cudaStream_t stream = 0;
 	DevBuf<float> vel0, vel1, tx0, tx1, data0, data1, frame0, frame1, points, vel, tx, poses;
 	DevBuf<uint32_t> cStart, cCount, bodyA, bodyB, recBytes;
+	DevBuf<uint8_t> laneFlags;
 	DevBuf<tgs::ConstraintRecord> recs;
 	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
 };
@@ -502,14 +541,18 @@ GBPX_API int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_
 // bodies' records (vel0/vel1: 64 B each, txI0/txI1: 64 B, data0/data1: 48 B),
 // the body frames (PxTransform), and contactPoints[contactStart[k] .. +contactCount[k]]
 // (PxContactPoint, 80 B, <= 4 per constraint; friction and restitution are read
-// from the points).  invDt = 1 / (dt / nbPositionIterations), invTotalDt = 1 / dt.
+// from the points).  laneFlags[k] (may be null: every constraint on the
+// per-pair path): bit 0 = one of the four constraints of a header of stride 4
+// that takes the reference's 4-wide block path, bit 1 = that header has a
+// dynamic body B, bit 2 = the descriptor's bodyBDataIndex is 0.
+// invDt = 1 / (dt / nbPositionIterations), invTotalDt = 1 / dt.
 // Writes each constraint's rows to outRows + k * gbpx_constraint_row_stride()
 // and their used size to outRowBytes[k].
 GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
                                                  const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
-                                                 const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, float invDt, float invTotalDt,
-                                                 float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, void* outRows,
-                                                 uint32_t* outRowBytes)
+                                                 const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, const uint8_t* laneFlags,
+                                                 float invDt, float invTotalDt, float bounceThreshold, float frictionOffsetThreshold,
+                                                 float correlationDistance, void* outRows, uint32_t* outRowBytes)
 {
 	(void)correlationDistance;
 	if(!n) return GBPX_OK;
@@ -523,7 +566,7 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	const size_t m = n;
 	if(ws->vel0.reserve(16 * m) || ws->vel1.reserve(16 * m) || ws->tx0.reserve(16 * m) || ws->tx1.reserve(16 * m) || ws->data0.reserve(12 * m) ||
 	   ws->data1.reserve(12 * m) || ws->frame0.reserve(7 * m) || ws->frame1.reserve(7 * m) || ws->cStart.reserve(m) || ws->cCount.reserve(m) ||
-	   ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->recs.reserve(m) || ws->recBytes.reserve(m))
+	   ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->recs.reserve(m) || ws->recBytes.reserve(m) || ws->laneFlags.reserve(m))
 		return GBPX_ERR_NOMEM;
 	cudaStream_t s = ws->stream;
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel0.ptr, vel0, m * 64, cudaMemcpyHostToDevice, s));
@@ -537,6 +580,7 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cStart.ptr, contactStart, m * 4, cudaMemcpyHostToDevice, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cCount.ptr, contactCount, m * 4, cudaMemcpyHostToDevice, s));
 	if(nbPoints) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->points.ptr, contactPoints, size_t(nbPoints) * 80, cudaMemcpyHostToDevice, s));
+	if(laneFlags) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->laneFlags.ptr, laneFlags, m, cudaMemcpyHostToDevice, s));
 	tgs::PrepParams pp;
 	pp.invStepDt = invDt;
 	pp.invTotalDt = invTotalDt;
@@ -546,8 +590,8 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	pp.frictionOffsetThreshold = frictionOffsetThreshold;
 	pp.biasCoefficient = 2.0f * sqrtf(invTotalDt / invDt);
 	tgs::prepDescKernel<<<divUp(n, 128), 128, 0, s>>>(n, ws->vel0.ptr, ws->vel1.ptr, ws->tx0.ptr, ws->tx1.ptr, ws->data0.ptr, ws->data1.ptr,
-	                                                  ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr, ws->points.ptr, pp,
-	                                                  ws->recs.ptr, ws->recBytes.ptr);
+	                                                  ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr, ws->points.ptr,
+	                                                  laneFlags ? ws->laneFlags.ptr : nullptr, pp, ws->recs.ptr, ws->recBytes.ptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(outRows, ws->recs.ptr, m * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(outRowBytes, ws->recBytes.ptr, m * 4, cudaMemcpyDeviceToHost, s));

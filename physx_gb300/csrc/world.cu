@@ -632,13 +632,32 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 	uint32_t qbase = 0;
 	if(lane == 0) qbase = atomicAdd(&w.workCounter[3], nc);
 	qbase = __shfl_sync(0xffffffffu, qbase, 0);
-	for(uint32_t r = lane; r < nc; r += 32) w.prepQueue[qbase + r] = sc.pairStart + r;
+	// PxBatchConstraintsTGS's headers are runs of up to 4 consecutive constraints
+	// of one partition (createHeaders, NpImmediateMode.cpp:159; every partition
+	// here is non-empty, so each one is below its maxPartition); full runs of 4
+	// take the 4-wide block path (<= 16 contacts, under its 64-contact limit).
+	// Bit 31 of the queue entry marks those constraints.
+	for(uint32_t r = lane; r < nc; r += 32)
+	{
+		uint32_t lo = 0, hi = nbPart - 1;   // first partition whose end is above r
+		while(lo < hi)
+		{
+			const uint32_t mid = (lo + hi) >> 1;
+			if(sm.perPart[mid] > r) hi = mid;
+			else lo = mid + 1;
+		}
+		const uint32_t start = lo ? sm.perPart[lo - 1] : 0u, size = sm.perPart[lo] - start;
+		const bool block = (r - start) < (size & ~3u);
+		w.prepQueue[qbase + r] = (sc.pairStart + r) | (block ? 0x80000000u : 0u);
+	}
 }
 
 // Contact rows of one constraint (PxCreateContactConstraintsTGS for one
 // descriptor): slot = scene pair start + position in solve order.
-__device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t slot, const StepParams& sp)
+__device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, const StepParams& sp)
 {
+	const uint32_t slot = entry & 0x7fffffffu;
+	const bool block = (entry >> 31) != 0;
 	const SceneDesc sc = w.scenes[w.slotScene[slot]];
 	const uint32_t n = sc.nbBodies;
 	tgs::BodyVel* vel = w.vel + sc.solverStart;
@@ -674,7 +693,11 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t slot, const
 		cs[c].restitution = 0.0f;
 	}
 	tgs::ConstraintRecord& rec = w.recs[slot];
-	tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec);
+	if(block)
+		tgs::prepConstraintBlock(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, b < n, b == 0,
+		                         rec);
+	else
+		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec);
 	w.recChunks[slot] = uint8_t((rec.bytes() + 15) / 16);
 }
 
@@ -762,7 +785,7 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = vel[a].dLin; b0.dAng = vel[a].dAng;
 				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = vel[b].dLin; b1.dAng = vel[b].dAng;
 				const bool dynB = b < n;
-				tgs::solveConstraint(*rec, b0, b1, dynB, minPen, elapsed);
+				tgs::solveRecord(*rec, b0, b1, dynB, minPen, elapsed);
 				V.set(a, b0.lin, b0.ang);
 				if(dynB) V.set(b, b1.lin, b1.ang);
 				if(rec != src)
@@ -979,6 +1002,7 @@ struct World
 			d.solverStart = b + st;
 			d.keyStart = key; d.keyCap = pow2(d.nbBodies);
 			d.pairStart = pair; d.pairCap = pow2(d.nbBodies * pairsPerBody + d.nbBodies * d.nbStatics);
+			if(uint64_t(pair) + d.pairCap >= (1ull << 31)) return GBPX_ERR_CAPACITY;   // pair slots are 31-bit queue entries
 			b += d.nbBodies; st += d.nbStatics; key += d.keyCap; pair += d.pairCap;
 		}
 		nbBodies = b; nbStatics = st; nbSolver = b + st; nbKeys = key; nbPairSlots = pair;
