@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the Poisson serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="request arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the serving pool")
+    ap.add_argument("--extras", type=int, default=1, help="also measure the pyramid and the 1M-AABB broadphase workloads")
+    ap.add_argument("--pyramid-steps", type=int, default=300)
+    ap.add_argument("--bp-frames", type=int, default=10)
+    ap.add_argument("--bp-cpu-frames", type=int, default=1)
     return ap.parse_args()
 
 
@@ -161,6 +165,74 @@ def profiled_traffic(stage):
     except (OSError, ValueError, IndexError):
         pass
     return None
+
+
+def bench_pyramid(steps):
+    """The 210-box pyramid of the reference's immediate-mode snippet (one scene, the world
+    API), against the oracle restatement of the same frame on one host thread."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import run_scene_step
+    from physx_gb300.workloads import pyramid_scene
+    from physx_gb300.world import DEFAULT_PARAMS, World
+    sc = pyramid_scene()
+    w = World(sc)
+    w.step(3, graph=True)
+    w.synchronize()
+    ms = w.time_steps(steps, graph=True)
+    w.release()
+    t = time.perf_counter()
+    run_scene_step("orc", sc, DEFAULT_PARAMS, steps=steps)
+    cpu_s = time.perf_counter() - t
+    n = len(sc["rigid"])
+    return dict(workload="210-box pyramid (20 levels, h 0.5, jitter 0.01 m / 2 deg), plane, TGS 4/1, dt 1/60", bodies=n, steps=steps,
+                ms_per_step=ms / steps, value=n * steps / (ms / 1000.0), unit=UNIT,
+                cpu_baseline=dict(value=n * steps / cpu_s, unit=UNIT, cores=1, kind="port",
+                                  sample="the same %d steps, oracle restatement, one thread" % steps))
+
+
+def bench_broadphase(frames, cpu_frames):
+    """1M AABBs, 10% moved per frame: PxBroadPhase (eABP) update + fetchResults through the
+    C ABI with host arrays, per frame; the oracle ABP restatement on one host thread."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import CpuBroadPhase
+    from physx_gb300.broadphase import BroadPhase
+    from physx_gb300.workloads import aabb_stress_frames
+
+    def algorithmic(fr, n_total, active, created, lost):
+        return 36 * len(fr["updated"]) + 28 * n_total + 16 * active + 8 * (created + lost)
+
+    bp = BroadPhase()
+    times, pairs, byts = [], [], []
+    for f, fr in enumerate(aabb_stress_frames(frames=frames + 1)):
+        t = time.perf_counter()
+        bp.update(fr["created"], fr["updated"], fr["removed"], fr["bounds"], fr["groups"], fr["distances"], fr["capacity"])
+        c, l = bp.fetch_results()
+        dt = time.perf_counter() - t
+        st = bp.stats()
+        if f == 0:
+            continue   # the first frame creates every box
+        times.append(dt)
+        pairs.append(st["active"] + len(c) + len(l))
+        byts.append(algorithmic(fr, st["live"], st["active"], len(c), len(l)))
+    bp.release()
+    ms = 1000.0 * float(np.median(times))
+    k = int(np.argsort(times)[len(times) // 2])
+    cpu = CpuBroadPhase("orc")
+    ct = []
+    for f, fr in enumerate(aabb_stress_frames(frames=cpu_frames + 1)):
+        t = time.perf_counter()
+        cpu.update(fr)
+        if f:
+            ct.append(time.perf_counter() - t)
+    cpu.release()
+    cpu_ms = 1000.0 * float(np.median(ct))
+    return dict(workload="1M AABBs U(0,1000)^3, half-extents lognormal(ln 0.5, 0.5), all dynamic, distance 0; 10% moved N(0, 0.2 m) per frame",
+                frames=frames, ms_per_frame=ms, value=pairs[k] / (ms / 1000.0), unit="pairs/s (active + created + lost)",
+                e2e_note="host arrays in, created/lost pairs out (PxBroadPhase::update + fetchResults)",
+                algorithmic_gbs=byts[k] / (ms / 1000.0) / 1e9,
+                cpu_baseline=dict(value=pairs[k] / (cpu_ms / 1000.0), ms_per_frame=cpu_ms, unit="pairs/s", cores=1, kind="port",
+                                  sample="%d frames, oracle ABP restatement, one thread" % cpu_frames))
 
 
 def dist_setup(n):
@@ -309,6 +381,9 @@ def main():
         serving["workload"] = ("Poisson %.0f req/s of 'advance scene k by n~U{1..8} steps' over a pool of scenes log-uniform [16,4096] "
                                "bodies admitted against a %.0f GB budget, retired after U(500,5000) steps; %.0f s run" %
                                (a.serve_rate, a.serve_budget_gb, a.serve_seconds))
+    extras = None
+    if a.extras:
+        extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
@@ -320,7 +395,7 @@ def main():
                                batched_over_plain=value / plain_value),
                 roofline=roofline, stages=stages, step_roofline=step_roofline, cpu_baseline=cpu, clocks=clk, gpu_launches=a.steps * info["kernels_per_step"],
                 contacts_per_s=st["contacts"] * a.steps / (ms / 1000.0), pairs_per_s=st["pairs"] * a.steps / (ms / 1000.0),
-                status_nonzero_scenes=int((status != 0).sum()), serving=serving)
+                status_nonzero_scenes=int((status != 0).sum()), serving=serving, workloads=extras)
     print(json.dumps(line))
 
 

@@ -159,3 +159,30 @@ def kinetic_energy(rigid):
     wl = w + qw * t + np.cross(qv, t)
     inertia = 1.0 / rigid["invInertia"].astype(np.float64)
     return float(0.5 * (m * (v * v).sum(1)).sum() + 0.5 * (inertia * wl * wl).sum())
+
+
+def aabb_stress_frames(seed=3, n=1_000_000, frames=10, extent=1000.0, move_frac=0.1, sigma=0.2):
+    """Broadphase stress workload: n AABBs, centres U(0, extent)^3, per-axis
+    half-extents lognormal(ln 0.5, 0.5), every box dynamic with its own filter
+    group (PxGetBroadPhaseDynamicFilterGroup(i)), distance 0.  The first frame
+    creates every box; each later frame moves move_frac of them (chosen without
+    replacement) by N(0, sigma) m per axis and submits them as updated.  Yields
+    dicts of created / updated / removed / bounds / groups / distances / capacity
+    (bounds hold capacity + 1 rows, PxBounds3 layout)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.0, extent, size=(n, 3)).astype(np.float32)
+    half = np.exp(rng.normal(np.log(0.5), 0.5, size=(n, 3))).astype(np.float32)
+    bounds = np.zeros((n + 1, 6), np.float32)
+    bounds[:n, :3] = centres - half
+    bounds[:n, 3:] = centres + half
+    groups = ((np.arange(n, dtype=np.uint32) + 1) << 3) | 2
+    dist = np.zeros(n, np.float32)
+    empty = np.zeros(0, np.uint32)
+    yield dict(created=np.arange(n, dtype=np.uint32), updated=empty, removed=empty, bounds=bounds, groups=groups, distances=dist, capacity=n)
+    m = max(1, int(n * move_frac))
+    for _ in range(1, frames):
+        moved = rng.choice(n, size=m, replace=False).astype(np.uint32)
+        d = rng.normal(0.0, sigma, size=(m, 3)).astype(np.float32)
+        bounds[moved, :3] += d
+        bounds[moved, 3:] += d
+        yield dict(created=empty, updated=np.sort(moved), removed=empty, bounds=bounds, groups=groups, distances=dist, capacity=n)

@@ -18,8 +18,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_libs import CpuBroadPhase, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
-from scenarios import bp_frames, np_pairs, pile_scenes, random_scene  # noqa: E402
+from oracle_libs import CachedContacts, CpuBroadPhase, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
+from scenarios import bp_frames, moving_pairs, np_pairs, pile_scenes, random_scene  # noqa: E402
 
 BP_CASES = [
     # name, seed, boxes, frames, extent
@@ -58,6 +58,29 @@ def make_np():
         packed = np.concatenate([out[i, :cnt[i]] for i in range(n) if cnt[i]]) if cnt.sum() else np.zeros((0, 8), np.float32)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), counts=cnt, contacts=packed.astype(np.float32),
                             contact_distance=np.float32(0.04), tolerance_length=np.float32(1.0), **pairs)
+        print("wrote", name)
+
+
+NP_CACHED_CASES = [
+    # name, seed, pairs, frames: the cached pair kinds moving a little every frame
+    ("pcm_cached", 18, 630, 8),
+]
+
+
+def make_np_cached():
+    for name, seed, n, frames in NP_CACHED_CASES:
+        pairs, poses = moving_pairs(seed, n, frames)
+        ref = CachedContacts("pxref", n)
+        out = dict(frames=np.array(frames), contact_distance=np.float32(0.04), tolerance_length=np.float32(1.0),
+                   **{k: pairs[k] for k in ("type0", "geom0", "type1", "geom1")})
+        for f, (p0, p1) in enumerate(poses):
+            cnt, res = ref.run(dict(pairs, pose0=p0, pose1=p1))
+            out["f%d_pose0" % f], out["f%d_pose1" % f] = p0, p1
+            out["f%d_counts" % f] = cnt
+            out["f%d_contacts" % f] = (np.concatenate([res[i, :cnt[i]] for i in range(n) if cnt[i]]) if cnt.sum()
+                                        else np.zeros((0, 8), np.float32))
+        ref.release()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print("wrote", name)
 
 
@@ -149,11 +172,13 @@ def make_pyramid():
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np", "tgs", "scene", "recip", "pyramid"]
+    which = sys.argv[1:] or ["bp", "np", "np_cached", "tgs", "scene", "recip", "pyramid"]
     if "bp" in which:
         make_bp()
     if "np" in which:
         make_np()
+    if "np_cached" in which:
+        make_np_cached()
     if "tgs" in which:
         make_tgs()
     if "scene" in which:

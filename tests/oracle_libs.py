@@ -181,3 +181,39 @@ def run_scene_step(which, scenes, params, steps=1):
         fn(ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]), _p(keep[5]),
            _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
     return rb
+
+
+class CachedContacts:
+    """PxGenerateContacts over the same pairs frame after frame with persistent caches
+    (PCM manifolds carried between calls): the oracle keeps 288-byte manifold records,
+    the reference build its own PxCache array."""
+
+    def __init__(self, which, n):
+        self.which, self.n = which, n
+        if which == "orc":
+            self.L = oracle()
+            self.state = np.zeros(n * 288, np.uint8)
+        else:
+            self.L = reference()
+            self.L.pxref_np_create.restype = ctypes.c_void_p
+            self.ctx = ctypes.c_void_p(self.L.pxref_np_create(ctypes.c_uint32(n)))
+
+    def run(self, pairs, contact_distance=0.04, mesh_margin=0.01, tolerance_length=1.0, max_per_pair=8):
+        n = self.n
+        out = np.zeros((n, max_per_pair, 8), np.float32)
+        cnt = np.zeros(n, np.uint32)
+        args = [_p(np.ascontiguousarray(pairs[k])) for k in ("type0", "geom0", "type1", "geom1", "pose0", "pose1")]
+        if self.which == "orc":
+            rc = self.L.orc_np_run_cached(*args, ctypes.c_uint32(n), ctypes.c_float(contact_distance), ctypes.c_float(mesh_margin),
+                                          ctypes.c_float(tolerance_length), _p(out), ctypes.c_uint32(max_per_pair), _p(cnt),
+                                          _p(self.state))
+        else:
+            rc = self.L.pxref_np_run(self.ctx, *args, ctypes.c_uint32(n), ctypes.c_float(contact_distance), ctypes.c_float(mesh_margin),
+                                     ctypes.c_float(tolerance_length), 0, _p(out), ctypes.c_uint32(max_per_pair), _p(cnt))
+        assert rc == 0, "contact buffer overflow"
+        return cnt, out
+
+    def release(self):
+        if self.which != "orc" and self.ctx:
+            self.L.pxref_np_release(self.ctx)
+            self.ctx = None

@@ -243,3 +243,49 @@ def hub_scene(nb_spheres=40, seed=0):
     return dict(body_count=np.array([n], np.uint32), static_count=np.ones(1, np.uint32), rigid=rb, types=types, geoms=geoms,
                 friction=np.full(n, 0.5, np.float32), static_poses=plane_pose_y_up()[None, :].copy(), static_types=np.ones(1, np.int32),
                 static_geoms=np.zeros((1, 4), np.float32))
+
+
+def _quat_mul(a, b):
+    ax, ay, az, aw = a.T
+    bx, by, bz, bw = b.T
+    return np.stack([aw * bx + ax * bw + ay * bz - az * by, aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw, aw * bw - ax * bx - ay * by - az * bz], 1)
+
+
+def perturb_poses(rng, pose, lin, ang):
+    """Moves every pose by N(0, lin) m per axis and turns it by N(0, ang) rad about a random axis."""
+    n = len(pose)
+    out = pose.copy()
+    out[:, 4:] += rng.normal(0, lin, size=(n, 3)).astype(np.float32)
+    axis = rng.normal(size=(n, 3))
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    th = rng.normal(0, ang, size=n)
+    dq = np.concatenate([axis * np.sin(th / 2)[:, None], np.cos(th / 2)[:, None]], 1)
+    q = _quat_mul(dq, out[:, :4].astype(np.float64))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    out[:, :4] = q.astype(np.float32)
+    return out
+
+
+CACHED_KINDS = [(1, 2), (2, 1), (1, 3), (3, 1), (2, 3), (3, 2), (3, 3)]
+
+
+def moving_pairs(seed, n, frames, types=None):
+    """Near-contact pairs of the kinds whose contact manifold persists between frames
+    (plane-capsule, plane-box, capsule-box, box-box), then `frames - 1` small motions:
+    one body of every pair moves ~2 mm / 0.3 deg per frame, every fourth frame ~2 cm /
+    3 deg (enough to invalidate a manifold).  Returns the pair dict of frame 0 and the
+    (pose0, pose1) of every frame."""
+    pairs = np_pairs(seed, n, types=types or CACHED_KINDS)
+    rng = np.random.default_rng(seed + 1000)
+    poses = [(pairs["pose0"].copy(), pairs["pose1"].copy())]
+    for f in range(1, frames):
+        p0, p1 = poses[-1]
+        big = f % 4 == 0
+        lin, ang = (0.02, 0.05) if big else (0.002, 0.005)
+        if f % 2:
+            p1 = perturb_poses(rng, p1, lin, ang)
+        else:
+            p0 = perturb_poses(rng, p0, lin, ang)
+        poses.append((p0, p1))
+    return pairs, poses

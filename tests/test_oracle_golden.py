@@ -105,6 +105,47 @@ def test_oracle_contacts_match_reference_live(seed, types):
     assert all(r["maxdiff"] == 0.0 for r in rep.values()), rep
 
 
+def load_np_cached_fixture(path):
+    """The pairs, and per frame their poses with the reference's counts and packed contacts."""
+    z = np.load(path)
+    pairs = {k: z[k] for k in ("type0", "geom0", "type1", "geom1")}
+    frames = [dict(pose0=z["f%d_pose0" % f], pose1=z["f%d_pose1" % f], counts=z["f%d_counts" % f], contacts=z["f%d_contacts" % f])
+              for f in range(int(z["frames"]))]
+    return pairs, frames
+
+
+def test_oracle_cached_contacts_match_reference_golden():
+    """PxGenerateContacts with persistent caches (the PCM manifold of plane-capsule,
+    plane-box, capsule-box and box-box pairs carried between frames: refresh,
+    invalidation, incremental points, GJK warm start) over 8 moving frames."""
+    from contact_compare import unpack
+    from oracle_libs import CachedContacts
+    pairs, frames = load_np_cached_fixture(os.path.join(GOLDEN, "pcm_cached.npz"))
+    n = len(pairs["type0"])
+    orc = CachedContacts("orc", n)
+    for f, fr in enumerate(frames):
+        oc, oo = orc.run(dict(pairs, pose0=fr["pose0"], pose1=fr["pose1"]))
+        assert np.array_equal(oc, fr["counts"]), "frame %d counts" % f
+        ref = unpack(fr["counts"], fr["contacts"])
+        for i in range(n):
+            assert np.array_equal(oo[i, :oc[i]], ref[i]), "frame %d pair %d" % (f, i)
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed", [63, 64])
+def test_oracle_cached_contacts_match_reference_live(seed):
+    from oracle_libs import CachedContacts
+    from scenarios import moving_pairs
+    pairs, poses = moving_pairs(seed, 1400, 10)
+    orc, ref = CachedContacts("orc", 1400), CachedContacts("pxref", 1400)
+    for p0, p1 in poses:
+        fr = dict(pairs, pose0=p0, pose1=p1)
+        oc, oo = orc.run(fr)
+        rc, ro = ref.run(fr)
+        assert np.array_equal(oc, rc) and np.array_equal(oo, ro)
+    ref.release()
+
+
 TGS_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "tgs_*.npz")))
 
 # Velocity tolerance of one TGS solve against the reference, relative to the
