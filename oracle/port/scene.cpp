@@ -10,7 +10,9 @@
 // directory; the reference harness (oracle/ref/harness.cpp, pxref_scene_step)
 // does the same with the reference's own functions.
 #include "pxmath.h"
+#include "tgs_frame.h"
 #include <string.h>
+#include <map>
 #include <vector>
 #include <algorithm>
 
@@ -26,6 +28,9 @@ extern "C" uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float
                                   const float* contacts, const float* material, const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel,
                                   float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, float* outVel, float* outPose,
                                   uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder, void* outBodyVelRaw, void* outTxIRaw);
+extern "C" int orc_np_run_cached(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                                 const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin, float toleranceLength,
+                                 float* outContacts, uint32_t maxPerPair, uint32_t* outCounts, void* manifolds);
 
 namespace
 {
@@ -74,6 +79,41 @@ bool overlap(const float* a, const float* b)
 }
 } // namespace
 
+// Persistent pair state between frames (the snippet's WITH_PERSISTENCY mode,
+// SnippetImmediateMode.cpp:47): per overlapping pair its contact manifold
+// (288-byte record of np.cpp, zero = fresh cache) and the friction patches its
+// contact constraint left.  A pair starts fresh when it starts overlapping and
+// loses its state when it stops; a pair without contacts loses its friction.
+namespace
+{
+struct PairState
+{
+	uint8_t manifold[288];
+	std::vector<FrictionPatch> friction;
+	PairState() { memset(manifold, 0, sizeof(manifold)); }
+};
+struct Persistent
+{
+	std::vector<std::map<std::pair<uint32_t, uint32_t>, PairState>> scenes;
+};
+
+int sceneStep(Persistent* ps, uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, void* rigidIO, const int* types,
+              const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+              const float* params, const uint32_t* iterations);
+} // namespace
+
+OX void* orc_persistent_create() { return new Persistent; }
+OX void orc_persistent_release(void* h) { delete static_cast<Persistent*>(h); }
+
+// orc_scene_step with persistent contact manifolds and friction patches (state in h).
+OX int orc_scene_step_persistent(void* h, uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, void* rigidIO,
+                                 const int* types, const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes,
+                                 const float* staticGeoms, const float* params, const uint32_t* iterations)
+{
+	return sceneStep(static_cast<Persistent*>(h), nbScenes, sceneBodyCount, sceneStaticCount, rigidIO, types, geoms, friction, staticPoses,
+	                 staticTypes, staticGeoms, params, iterations);
+}
+
 // Steps every scene once.  rigid: all dynamic bodies (PxRigidBodyData) scene by
 // scene; params as gbpx_world_create (dt, g xyz, contactDistance,
 // toleranceLength, boundsMargin, bounceThreshold, frictionOffsetThreshold,
@@ -82,6 +122,17 @@ OX int orc_scene_step(uint32_t nbScenes, const uint32_t* sceneBodyCount, const u
                       const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
                       const float* params, const uint32_t* iterations)
 {
+	return sceneStep(nullptr, nbScenes, sceneBodyCount, sceneStaticCount, rigidIO, types, geoms, friction, staticPoses, staticTypes, staticGeoms,
+	                 params, iterations);
+}
+
+namespace
+{
+int sceneStep(Persistent* ps, uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, void* rigidIO, const int* types,
+              const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+              const float* params, const uint32_t* iterations)
+{
+	if(ps && ps->scenes.size() < nbScenes) ps->scenes.resize(nbScenes);
 	Rigid* rigid = static_cast<Rigid*>(rigidIO);
 	const float dt = params[0];
 	const float g[3] = {params[1], params[2], params[3]};
@@ -141,13 +192,47 @@ OX int orc_scene_step(uint32_t nbScenes, const uint32_t* sceneBodyCount, const u
 		}
 		std::vector<float> cts(np * 4 * 8);
 		std::vector<uint32_t> cnt(np);
-		if(np) orc_np_run(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), uint32_t(np), cDist, 0.01f, tolLen, cts.data(), 4,
-		                  cnt.data());
+		std::vector<PairState*> state(np, nullptr);
+		if(ps)
+		{
+			std::map<std::pair<uint32_t, uint32_t>, PairState> next;
+			std::map<std::pair<uint32_t, uint32_t>, PairState>& cur = ps->scenes[s];
+			for(size_t k = 0; k < np; k++)
+			{
+				const std::pair<uint32_t, uint32_t> key(A[k], B[k]);
+				auto it = cur.find(key);
+				next[key] = it != cur.end() ? it->second : PairState();
+			}
+			cur.swap(next);
+			std::vector<uint8_t> rec(np * 288 + 288);
+			for(size_t k = 0; k < np; k++)
+			{
+				state[k] = &cur[std::make_pair(A[k], B[k])];
+				memcpy(&rec[k * 288], state[k]->manifold, 288);
+			}
+			if(np) orc_np_run_cached(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), uint32_t(np), cDist, 0.01f, tolLen, cts.data(),
+			                         4, cnt.data(), rec.data());
+			for(size_t k = 0; k < np; k++)
+			{
+				memcpy(state[k]->manifold, &rec[k * 288], 288);
+				if(!cnt[k]) state[k]->friction.clear();
+			}
+		}
+		else if(np)
+			orc_np_run(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), uint32_t(np), cDist, 0.01f, tolLen, cts.data(), 4,
+			           cnt.data());
 		std::vector<uint32_t> ca, cb, cs, cc;
 		std::vector<float> packed, mat;
+		std::vector<std::vector<FrictionPatch>> fric;
+		std::vector<PairState*> cstate;
 		for(size_t k = 0; k < np; k++)
 		{
 			if(!cnt[k]) continue;
+			if(ps)
+			{
+				cstate.push_back(state[k]);
+				fric.push_back(state[k]->friction);
+			}
 			ca.push_back(A[k]); cb.push_back(B[k]);
 			cs.push_back(uint32_t(packed.size() / 8)); cc.push_back(cnt[k]);
 			packed.insert(packed.end(), &cts[k * 32], &cts[k * 32] + 8 * cnt[k]);
@@ -160,9 +245,17 @@ OX int orc_scene_step(uint32_t nbScenes, const uint32_t* sceneBodyCount, const u
 		std::vector<uint32_t> hs(2 * ca.size() + 2), hst(2 * ca.size() + 2), ord(ca.size() + 1);
 		std::vector<float> statics(7 * size_t(m));
 		for(uint32_t k = 0; k < m; k++) memcpy(&statics[7 * k], staticPoses + 7 * size_t(s0 + k), 28);
-		orc_tgs_solve(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), uint32_t(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(),
-		              g, dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(),
-		              ord.data(), nullptr, nullptr);
+		if(ps)
+		{
+			tgsFrame(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), uint32_t(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(), g,
+			         dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(), ord.data(),
+			         &fric);
+			for(size_t k = 0; k < cstate.size(); k++) cstate[k]->friction = fric[k];
+		}
+		else
+			orc_tgs_solve(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), uint32_t(ca.size()), cs.data(), cc.data(), packed.data(),
+			              mat.data(), g, dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(),
+			              hst.data(), ord.data(), nullptr, nullptr);
 		for(uint32_t i = 0; i < n; i++)
 		{
 			Rigid& r = rigid[b0 + i];
@@ -176,3 +269,4 @@ OX int orc_scene_step(uint32_t nbScenes, const uint32_t* sceneBodyCount, const u
 	}
 	return 0;
 }
+} // namespace

@@ -21,6 +21,7 @@
 // :2280), restated one lane at a time; every other constraint follows the
 // per-pair path.  The results equal the reference's bit for bit (tests).
 #include "pxmath.h"
+#include "tgs_frame.h"
 #include <string.h>
 #include <vector>
 #include <algorithm>
@@ -65,10 +66,14 @@ struct PatchRows
 	V3 normal;
 	float invMass0, invMass1, angDom0, angDom1, maxPenBias, staticFriction, dynamicFriction;
 	int pointStart, nbPoints, frictionStart, nbFriction;
+	int anchorCount;     // anchors of the friction patch the rows were built from
+	int brokenSlot;      // written friction patch that receives this patch's broken flag
+	int broken;          // friction clamped during the latest solve of the patch
 };
 // block: the constraint is one lane of a 4-wide header and uses the block
 // path's rows and solve (createFinalizeSolverContacts4Step, solveContact4_Block)
-struct ConstraintRows { int bodyA, bodyB; int patchStart, nbPatches; bool block; };
+// written: the friction patches the constraint leaves for the next frame
+struct ConstraintRows { int bodyA, bodyB; int patchStart, nbPatches; bool block; std::vector<FrictionPatch> written; };
 
 struct ContactIn { V3 n; float sep; V3 p; float staticFriction, dynamicFriction, restitution; };
 
@@ -278,14 +283,6 @@ void batchConstraints(const uint32_t* bodyA, const uint32_t* bodyB, int n, int n
 }
 
 // ------------------------------------------------------------ friction correlation (fresh patches)
-struct FrictionPatch
-{
-	V3 body0Normal, body1Normal;
-	V3 body0Anchors[2], body1Anchors[2];
-	int anchorCount;
-	float staticFriction, dynamicFriction, restitution;
-};
-
 struct Correlation
 {
 	struct ContactPatch { int start, count, next; float restitution, staticFriction, dynamicFriction; V3 bmin, bmax; };
@@ -339,6 +336,43 @@ void createContactPatches(Correlation& c, const ContactIn* cb, int n, float tol)
 	c.contactPatchCount = pc;
 }
 
+// getFrictionPatches (lowleveldynamics/src/DyContactPrepShared.h:73): last
+// frame's patches that are not broken, have anchors, still face each other
+// (body normals within PXC_SAME_NORMAL) and whose anchors have not separated
+// along the normal by the correlation distance start the patch list, without
+// contacts yet.
+void getFrictionPatches(Correlation& c, const FrictionPatch* prev, int count, const Tr& f0, const Tr& f1, float correlationDistance)
+{
+	if(!prev || !count) return;
+	const Q qinv = qConj(f0.q);
+	Tr b1to0;
+	b1to0.p = qRotateS(qinv, sub(f1.p, f0.p));
+	b1to0.q = qMulS(qinv, f1.q);
+	for(int k = 0; k < count; k++)
+	{
+		const FrictionPatch& patch = prev[k];
+		if(patch.broken || patch.anchorCount == 0) continue;
+		if(!(dotS(patch.body0Normal, qRotateS(b1to0.q, patch.body1Normal)) > 0.999f)) continue;
+		bool separated = false;
+		for(int a = 0; a < patch.anchorCount; a++)
+		{
+			const V3 p1in0 = add(qRotateS(b1to0.q, patch.body1Anchors[a]), b1to0.p);
+			if(!(fabsf(dotS(sub(patch.body0Anchors[a], p1in0), patch.body0Normal)) < correlationDistance)) { separated = true; break; }
+		}
+		if(separated) continue;
+		if(c.frictionPatchCount == 32) return;
+		const int i = c.frictionPatchCount++;
+		c.contactID[i][0] = 0xffff;
+		c.contactID[i][1] = 0xffff;
+		c.frictionPatchWorldNormal[i] = qRotateS(f0.q, patch.body0Normal);
+		c.frictionPatchContactCounts[i] = 0;
+		c.patchMin[i] = v3(FLT_MAX, FLT_MAX, FLT_MAX);     // PxBounds3::setEmpty
+		c.patchMax[i] = v3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+		c.correlationListHeads[i] = -1;
+		c.frictionPatches[i] = patch;
+	}
+}
+
 void correlatePatches(Correlation& c, const ContactIn* cb, const Tr& f0, const Tr& f1, float tol)
 {
 	int fpc = c.frictionPatchCount;
@@ -357,7 +391,9 @@ void correlatePatches(Correlation& c, const ContactIn* cb, const Tr& f0, const T
 			FrictionPatch& fp = c.frictionPatches[fpc];
 			fp.body0Normal = qRotateInvS(f0.q, n);
 			fp.body1Normal = qRotateInvS(f1.q, n);
+			fp.relativeQuat = qMulS(qConj(f0.q), f1.q);
 			fp.anchorCount = 0;
+			fp.broken = 0;
 			fp.staticFriction = cp.staticFriction; fp.dynamicFriction = cp.dynamicFriction; fp.restitution = cp.restitution;
 			c.frictionPatchWorldNormal[j] = n;
 			c.frictionPatchContactCounts[fpc] = cp.count;
@@ -491,9 +527,11 @@ float constructPoint(const M33& s0, const M33& s1, float imn0, float imn1, V3 p0
 	return penetration;
 }
 
+// prev / prevCount: the friction patches this constraint left last frame
+// (frictionPtr / frictionCount; none for a fresh pair).
 void prepConstraint(int ci, const ContactIn* contacts, int nbContacts, int a, int b, const BodyVel* vels, const BodyTx* txs, const BodyData* datas,
                     const Tr& f0, const Tr& f1, float invStepDt, float invTotalDt, float totalDt, float stepDt, float bounce, float fricOffset,
-                    float biasCoefficient, Rows& rows)
+                    float correlationDistance, float biasCoefficient, const FrictionPatch* prev, int prevCount, Rows& rows)
 {
 	ConstraintRows cr;
 	cr.bodyA = a; cr.bodyB = b;
@@ -502,6 +540,7 @@ void prepConstraint(int ci, const ContactIn* contacts, int nbContacts, int a, in
 	cr.block = false;
 	if(nbContacts == 0) { rows.cons[ci] = cr; return; }
 	Correlation c;
+	getFrictionPatches(c, prev, prevCount, f0, f1, correlationDistance);
 	createContactPatches(c, contacts, nbContacts, 0.999f);
 	correlatePatches(c, contacts, f0, f1, 0.999f);
 	growPatches(c, contacts, f0, f1, fricOffset + 0.0f);
@@ -601,10 +640,16 @@ void prepConstraint(int ci, const ContactIn* contacts, int nbContacts, int a, in
 				}
 			}
 		}
+		// the patch is written to the friction memory in this order
+		// (createFinalizeSolverContactsStep, DyTGSContactPrep.cpp:1391-1398)
+		pr.anchorCount = fp.anchorCount;
+		pr.brokenSlot = int(cr.written.size());
+		pr.broken = 0;
+		cr.written.push_back(fp);
 		rows.patches.push_back(pr);
 		cr.nbPatches++;
 	}
-	rows.cons[ci] = cr;
+	rows.cons[ci] = std::move(cr);
 }
 
 // ------------------------------------------------------------ 4-wide block path, one lane
@@ -643,7 +688,8 @@ inline V3 qRotate4V(Q q, V3 v)
 // branch does.
 void prepConstraintBlock(int ci, const ContactIn* contacts, int nbContacts, int a, int b, const BodyVel* vels, const BodyTx* txs,
                          const BodyData* datas, const Tr& f0, const Tr& f1, float invStepDt, float invTotalDt, float totalDt, float bounce,
-                         float fricOffset, float biasCoefficient, bool blockDynamic, Rows& rows)
+                         float fricOffset, float correlationDistance, float biasCoefficient, bool blockDynamic, const FrictionPatch* prev,
+                         int prevCount, Rows& rows)
 {
 	ConstraintRows cr;
 	cr.bodyA = a; cr.bodyB = b;
@@ -652,9 +698,25 @@ void prepConstraintBlock(int ci, const ContactIn* contacts, int nbContacts, int 
 	cr.block = true;
 	if(nbContacts == 0) { rows.cons[ci] = cr; return; }
 	Correlation c;
+	getFrictionPatches(c, prev, prevCount, f0, f1, correlationDistance);
 	createContactPatches(c, contacts, nbContacts, 0.999f);
 	correlatePatches(c, contacts, f0, f1, 0.999f);
 	growPatches(c, contacts, f0, f1, fricOffset + 0.0f);
+	// The block path then drops the patches that received no contact
+	// (createFinalizeSolverContacts4Step, DyTGSContactPrepBlock.cpp:1452-1466)
+	// by moving the later list heads and contact counts down -- but not the
+	// patches themselves, so a later patch's contacts pair with an earlier
+	// patch's anchors, and the earlier patches are the ones written out.
+	for(int p = c.frictionPatchCount; p > 0; --p)
+		if(c.correlationListHeads[p - 1] == -1)
+		{
+			for(int p2 = p; p2 < c.frictionPatchCount; ++p2)
+			{
+				c.correlationListHeads[p2 - 1] = c.correlationListHeads[p2];
+				c.frictionPatchContactCounts[p2 - 1] = c.frictionPatchContactCounts[p2];
+			}
+			c.frictionPatchCount--;
+		}
 
 	const BodyData& d0 = datas[a];
 	const BodyData& d1 = datas[b];
@@ -795,10 +857,15 @@ void prepConstraintBlock(int ci, const ContactIn* contacts, int nbContacts, int 
 				}
 			}
 		}
+		// written in patch order; the broken-flag slot is completed per header
+		pr.anchorCount = fp.anchorCount;
+		pr.brokenSlot = int(cr.written.size());
+		pr.broken = 0;
+		cr.written.push_back(fp);
 		rows.patches.push_back(pr);
 		cr.nbPatches++;
 	}
-	rows.cons[ci] = cr;
+	rows.cons[ci] = std::move(cr);
 }
 
 // ------------------------------------------------------------ solve
@@ -849,6 +916,7 @@ void solveConstraint(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float 
 			const float maxF = pr.staticFriction * accumulated;
 			const float maxDynF = pr.dynamicFriction * accumulated;
 			const int pairs = pr.nbFriction & 6;
+			bool broken = false;
 			for(int i = 0; i < pairs; i += 2)
 			{
 				FrictionRow& f0 = rows.friction[pr.frictionStart + i];
@@ -871,6 +939,7 @@ void solveConstraint(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float 
 				const float ti1 = tmp11 - nvel1 * f1.velMultiplier;
 				const float total = sqrtf(ti0 * ti0 + ti1 * ti1);
 				const bool clamp = total > fs * maxF;
+				broken = broken || clamp;
 				const float totalClamped = clamp ? fmin_(fs * maxDynF, total) : total;
 				const float ratio = total > 0.0f ? totalClamped / total : 0.0f;
 				const float nf0 = ti0 * ratio, nf1 = ti1 * ratio;
@@ -882,6 +951,7 @@ void solveConstraint(const ConstraintRows& cr, Rows& rows, BodyVel* vels, float 
 				f0.appliedForce = nf0;
 				f1.appliedForce = nf1;
 			}
+			pr.broken = broken;
 		}
 	}
 	b0.lin = lin0; b1.lin = lin1; b0.ang = ang0; b1.ang = ang1;
@@ -971,6 +1041,7 @@ void solveConstraintBlock(const ConstraintRows& cr, Rows& rows, BodyVel* vels, f
 				ang0 = add(scale(f0.raXnI, ad00), add(scale(f1.raXnI, ad01), ang0));
 				ang1 = sub(sub(ang1, scale(f1.rbXnI, ad11)), scale(f0.rbXnI, ad10));
 			}
+			pr.broken = broken;
 		}
 	}
 	b0.lin = lin0; b0.ang = ang0;
@@ -1028,16 +1099,14 @@ OX uint32_t orc_batch_constraints_tgs(const uint32_t* bodyA, const uint32_t* bod
 	return uint32_t(out.headerStart.size());
 }
 
-// Same argument layout as the reference harness's pxref_tgs_solve.
-OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* staticPose, uint32_t nbStatic, const uint32_t* pairA,
-                          const uint32_t* pairB, uint32_t nbConstraints, const uint32_t* contactStart, const uint32_t* contactCount,
-                          const float* contacts, const float* material, const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel,
-                          float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, float* outVel, float* outPose,
-                          uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder, void* outBodyVelRaw, void* outTxIRaw)
+// The snippet's sequence PxConstructSolverBodiesTGS ... PxIntegrateSolverBodiesTGS;
+// friction is indexed by the caller's constraint index (frictionPtr / frictionCount).
+uint32_t orc::tgsFrame(const void* rigid, uint32_t nbDyn, const float* staticPose, uint32_t nbStatic, const uint32_t* pairA, const uint32_t* pairB,
+                  uint32_t nbConstraints, const uint32_t* contactStart, const uint32_t* contactCount, const float* contacts, const float* material,
+                  const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel, float bounceThreshold, float frictionOffsetThreshold,
+                  float correlationDistance, float* outVel, float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder,
+                  std::vector<std::vector<FrictionPatch>>* friction)
 {
-	(void)correlationDistance;
-	(void)outBodyVelRaw;
-	(void)outTxIRaw;
 	const uint32_t nbTotal = nbDyn + nbStatic;
 	std::vector<BodyVel> vels(nbTotal);
 	std::vector<BodyTx> txs(nbTotal);
@@ -1117,14 +1186,45 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 			cin[c].dynamicFriction = material[3 * ci + 1];
 			cin[c].restitution = material[3 * ci + 2];
 		}
+		const FrictionPatch* prev = friction && !(*friction)[ci].empty() ? (*friction)[ci].data() : nullptr;
+		const int prevCount = friction ? int((*friction)[ci].size()) : 0;
 		if(inBlock[k])
 			prepConstraintBlock(ci, cin.data(), int(contactCount[ci]), int(pairA[ci]), int(pairB[ci]), vels.data(), txs.data(), datas.data(),
 			                    poses[pairA[ci]], poses[pairB[ci]], invStepDt, invDt, totalDt, bounceThreshold, frictionOffsetThreshold,
-			                    biasCoefficient, blockDynamic[k] != 0, rows);
+			                    correlationDistance, biasCoefficient, blockDynamic[k] != 0, prev, prevCount, rows);
 		else
 			prepConstraint(ci, cin.data(), int(contactCount[ci]), int(pairA[ci]), int(pairB[ci]), vels.data(), txs.data(), datas.data(),
 			               poses[pairA[ci]], poses[pairB[ci]], invStepDt, invDt, totalDt, prepDt, bounceThreshold, frictionOffsetThreshold,
-			               biasCoefficient, rows);
+			               correlationDistance, biasCoefficient, prev, prevCount, rows);
+	}
+	// Block headers: the broken flag of a lane's patch i goes to the written
+	// patch counted by the header's earlier patch rows that had friction in any
+	// lane (the block setup advances its write-back address only for those,
+	// DyTGSContactPrepBlock.cpp:1218-1222).
+	for(size_t h = 0; h < batch.headerStart.size(); h++)
+	{
+		const uint32_t s0 = batch.headerStart[h];
+		if(batch.headerStride[h] != 4 || !inBlock[s0]) continue;
+		int maxPatches = 0;
+		for(uint32_t l = 0; l < 4; l++)
+			if(batch.order[s0 + l] >= 0) maxPatches = std::max(maxPatches, rows.cons[batch.order[s0 + l]].nbPatches);
+		int slot = 0;
+		for(int i = 0; i < maxPatches; i++)
+		{
+			int maxAnchors = 0;
+			for(uint32_t l = 0; l < 4; l++)
+			{
+				if(batch.order[s0 + l] < 0) continue;
+				const ConstraintRows& cr = rows.cons[batch.order[s0 + l]];
+				if(i < cr.nbPatches)
+				{
+					PatchRows& pr = rows.patches[cr.patchStart + i];
+					pr.brokenSlot = slot;
+					maxAnchors = std::max(maxAnchors, pr.anchorCount);
+				}
+			}
+			if(maxAnchors) slot++;
+		}
 	}
 	auto solve = [&](const ConstraintRows& cr, float minPen, float el) {
 		if(cr.block) solveConstraintBlock(cr, rows, vels.data(), minPen, el);
@@ -1141,6 +1241,20 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 	for(uint32_t it = 0; it < nbVel; it++)
 		for(uint32_t k = 0; k < nbConstraints; k++)
 			if(batch.order[k] >= 0) solve(rows.cons[batch.order[k]], 0.0f, elapsed);
+	// write-back of the last iteration: a patch whose friction was clamped
+	// marks its written friction patch broken (writeBackContact,
+	// DyTGSContactPrep.cpp:1907; writeBackContact4_Block, DyTGSContactPrepBlock.cpp:2891)
+	if(friction)
+		for(uint32_t ci = 0; ci < nbConstraints; ci++)
+		{
+			ConstraintRows& cr = rows.cons[ci];
+			for(int p = 0; p < cr.nbPatches; p++)
+			{
+				const PatchRows& pr = rows.patches[cr.patchStart + p];
+				if(pr.nbFriction && pr.broken && pr.brokenSlot < int(cr.written.size())) cr.written[pr.brokenSlot].broken = 1;
+			}
+			(*friction)[ci] = cr.written;
+		}
 	// PxIntegrateSolverBodiesTGS
 	for(uint32_t a = 0; a < nbDyn; a++)
 	{
@@ -1156,4 +1270,18 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 		o[4] = txs[a].p.x; o[5] = txs[a].p.y; o[6] = txs[a].p.z;
 	}
 	return uint32_t(batch.headerStart.size());
+}
+
+// Same argument layout as the reference harness's pxref_tgs_solve.
+OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* staticPose, uint32_t nbStatic, const uint32_t* pairA,
+                          const uint32_t* pairB, uint32_t nbConstraints, const uint32_t* contactStart, const uint32_t* contactCount,
+                          const float* contacts, const float* material, const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel,
+                          float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, float* outVel, float* outPose,
+                          uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder, void* outBodyVelRaw, void* outTxIRaw)
+{
+	(void)outBodyVelRaw;
+	(void)outTxIRaw;
+	return tgsFrame(rigid, nbDyn, staticPose, nbStatic, pairA, pairB, nbConstraints, contactStart, contactCount, contacts, material, gravity, dt,
+	                nbPos, nbVel, bounceThreshold, frictionOffsetThreshold, correlationDistance, outVel, outPose, outHeaderStart, outHeaderStride,
+	                outOrder, nullptr);
 }

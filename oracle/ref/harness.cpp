@@ -382,14 +382,17 @@ HX PxU32 pxref_batch_constraints_tgs(const PxU32* bodyA, const PxU32* bodyB, PxU
 //             angular one in world space after PxIntegrateSolverBodiesTGS),
 //             poses after integration (7 floats per dynamic body),
 //             headers and order as pxref_batch_constraints_tgs.
-HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
+// frictionPtr / frictionCount (per constraint, may be null): the friction data
+// each constraint left last frame, replaced by what it leaves this frame (in
+// alloc's friction memory, which lives two frames), as the snippet's persistent
+// pairs keep it.
+static PxU32 tgsFrameRef(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
 	const PxU32* pairA, const PxU32* pairB, PxU32 nbConstraints, const PxU32* contactStart, const PxU32* contactCount,
 	const float* contacts, const float* material, const float* gravity, float dt, PxU32 nbPos, PxU32 nbVel,
 	float bounceThreshold, float frictionOffsetThreshold, float correlationDistance,
 	float* outVel, float* outPose, PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outOrder,
-	void* outBodyVelRaw, void* outTxIRaw)
+	void* outBodyVelRaw, void* outTxIRaw, FrameConstraintAllocator& alloc, PxU8** frictionPtr, PxU32* frictionCount)
 {
-	ensureFoundation();
 	const PxU32 nbTotal = nbDyn + nbStatic;
 	std::vector<PxTGSSolverBodyVel> bodies(nbTotal);
 	std::vector<PxTGSSolverBodyTxInertia> txI(nbTotal);
@@ -463,7 +466,6 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 	const PxReal invDt = 1.0f / dt;
 	const PxReal stepDt = dt / PxReal(nbPos);
 	const PxReal invStepDt = invDt * PxReal(nbPos);
-	FrameConstraintAllocator alloc;
 	for(PxU32 h = 0; h < nbHeaders; h++)
 	{
 		PxConstraintBatchHeader& header = headers[h];
@@ -485,8 +487,8 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 			c.contactForces = &forces[contactStart[ci]];
 			c.contacts = &points[contactStart[ci]];
 			c.numContacts = contactCount[ci];
-			c.frictionPtr = NULL;
-			c.frictionCount = 0;
+			c.frictionPtr = frictionPtr ? frictionPtr[ci] : NULL;
+			c.frictionCount = frictionCount ? PxU8(frictionCount[ci]) : 0;
 			c.shapeInteraction = NULL;
 			c.maxCCDSeparation = PX_MAX_F32;
 			c.bodyState0 = desc.bodyADataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
@@ -495,6 +497,12 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 			c.invMassScales.angular0 = c.invMassScales.angular1 = c.invMassScales.linear0 = c.invMassScales.linear1 = 1.0f;
 		}
 		PxCreateContactConstraintsTGS(&header, 1, cd, alloc, invStepDt, invDt, bounceThreshold, frictionOffsetThreshold, correlationDistance);
+		for(PxU32 a = 0; frictionPtr && a < header.stride; a++)
+		{
+			const PxU32 ci = outOrder[header.startIndex + a];
+			frictionPtr[ci] = cd[a].frictionPtr;
+			frictionCount[ci] = cd[a].frictionCount;
+		}
 	}
 
 	PxSolveConstraintsTGS(headers.data(), nbHeaders, ordered.data(), bodies.data(), txI.data(), nbDyn, nbPos, nbVel, stepDt, invStepDt);
@@ -512,6 +520,20 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 		storePose(outPose + 7 * a, poses[a]);
 	}
 	return nbHeaders;
+}
+
+HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
+	const PxU32* pairA, const PxU32* pairB, PxU32 nbConstraints, const PxU32* contactStart, const PxU32* contactCount,
+	const float* contacts, const float* material, const float* gravity, float dt, PxU32 nbPos, PxU32 nbVel,
+	float bounceThreshold, float frictionOffsetThreshold, float correlationDistance,
+	float* outVel, float* outPose, PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outOrder,
+	void* outBodyVelRaw, void* outTxIRaw)
+{
+	ensureFoundation();
+	FrameConstraintAllocator alloc;
+	return tgsFrameRef(rigid, nbDyn, staticPose, nbStatic, pairA, pairB, nbConstraints, contactStart, contactCount, contacts, material, gravity, dt,
+		nbPos, nbVel, bounceThreshold, frictionOffsetThreshold, correlationDistance, outVel, outPose, outHeaderStart, outHeaderStride, outOrder,
+		outBodyVelRaw, outTxIRaw, alloc, NULL, NULL);
 }
 
 //////////////////////////////////////////////////////////////////////////////
@@ -553,11 +575,70 @@ void sceneShapeBounds(int type, const float* g, const float* pose7, float margin
 }
 }
 
+// Persistent pair state across frames, as the snippet keeps it with
+// WITH_PERSISTENCY (SnippetImmediateMode.cpp:47, 563-600, 657-676, 941-978):
+// per overlapping pair its PxCache and the friction data its contact
+// constraint left; a pair gets fresh state when the broadphase reports it and
+// loses it when the pair stops overlapping; friction data is dropped for a
+// pair whose contact generation found no contact.
+namespace
+{
+struct PairStateRef
+{
+	PxCache cache;
+	PxU8* frictions = NULL;
+	PxU32 nbFrictions = 0;
+};
+struct PersistentRef
+{
+	std::vector<std::map<std::pair<PxU32, PxU32>, PairStateRef>> scenes;
+	FrameCacheAllocator cacheAlloc;
+	FrameConstraintAllocator constraintAlloc;
+};
+
+int sceneStepRef(PersistentRef* ps, PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32* sceneStaticCount, void* rigidIO, const int* types,
+	const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+	const float* params, const PxU32* iterations);
+}
+
+HX void* pxref_persistent_create()
+{
+	ensureFoundation();
+	return new PersistentRef;
+}
+
+HX void pxref_persistent_release(void* h) { delete static_cast<PersistentRef*>(h); }
+
+// pxref_scene_step with persistent contact caches and friction data (state in h).
+HX int pxref_scene_step_persistent(void* h, PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32* sceneStaticCount, void* rigidIO,
+	const int* types, const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+	const float* params, const PxU32* iterations)
+{
+	return sceneStepRef(static_cast<PersistentRef*>(h), nbScenes, sceneBodyCount, sceneStaticCount, rigidIO, types, geoms, friction, staticPoses,
+		staticTypes, staticGeoms, params, iterations);
+}
+
 HX int pxref_scene_step(PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32* sceneStaticCount, void* rigidIO, const int* types,
 	const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
 	const float* params, const PxU32* iterations)
 {
+	return sceneStepRef(NULL, nbScenes, sceneBodyCount, sceneStaticCount, rigidIO, types, geoms, friction, staticPoses, staticTypes, staticGeoms,
+		params, iterations);
+}
+
+namespace
+{
+int sceneStepRef(PersistentRef* ps, PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32* sceneStaticCount, void* rigidIO, const int* types,
+	const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes, const float* staticGeoms,
+	const float* params, const PxU32* iterations)
+{
 	ensureFoundation();
+	if(ps)
+	{
+		if(ps->scenes.size() < nbScenes) ps->scenes.resize(nbScenes);
+		ps->cacheAlloc.nextFrame();
+		ps->constraintAlloc.nextFrame();
+	}
 	PxRigidBodyData* rigid = static_cast<PxRigidBodyData*>(rigidIO);
 	const float dt = params[0];
 	const float cDist = params[4], tolLen = params[5], margin = params[6];
@@ -617,14 +698,60 @@ HX int pxref_scene_step(PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32
 		}
 		std::vector<float> cts(np * 8 * 8 + 8);
 		std::vector<PxU32> cnt(np + 1);
-		void* np_ = pxref_np_create(PxU32(np));
-		if(np) pxref_np_run(np_, t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), PxU32(np), cDist, 0.01f, tolLen, 1, cts.data(), 8, cnt.data());
-		pxref_np_release(np_);
-		std::vector<PxU32> ca, cb, cs, cc;
+		std::vector<PairStateRef*> state(np, NULL);
+		if(ps)
+		{
+			// pairs that stopped overlapping lose their state; new ones start fresh
+			std::map<std::pair<PxU32, PxU32>, PairStateRef> next;
+			std::map<std::pair<PxU32, PxU32>, PairStateRef>& cur = ps->scenes[s];
+			for(size_t k = 0; k < np; k++)
+			{
+				auto it = cur.find(pairs[k]);
+				next[pairs[k]] = it != cur.end() ? it->second : PairStateRef();
+			}
+			cur.swap(next);
+			for(size_t k = 0; k < np; k++) state[k] = &cur[pairs[k]];
+			BufferRecorder rec;
+			rec.out = cts.data();
+			rec.counts = cnt.data();
+			rec.maxPerPair = 8;
+			for(size_t k = 0; k < np; k++)
+			{
+				cnt[k] = 0;
+				GeomHolder h0, h1;
+				const PxGeometry* gg0 = h0.set(t0[k], &g0[4 * k]);
+				const PxGeometry* gg1 = h1.set(t1[k], &g1[4 * k]);
+				const PxTransform tr0 = loadPose(&p0[7 * k]), tr1 = loadPose(&p1[7 * k]);
+				struct Rebase : PxContactRecorder
+				{
+					BufferRecorder* r; PxU32 slot;
+					bool recordContacts(const PxContactPoint* p, PxU32 nn, PxU32) override { return r->recordContacts(p, nn, slot); }
+				} rb;
+				rb.r = &rec;
+				rb.slot = PxU32(k);
+				PxGenerateContacts(&gg0, &gg1, &tr0, &tr1, &state[k]->cache, 1, rb, cDist, 0.01f, tolLen, ps->cacheAlloc);
+				if(!cnt[k]) { state[k]->frictions = NULL; state[k]->nbFrictions = 0; }
+			}
+		}
+		else
+		{
+			void* np_ = pxref_np_create(PxU32(np));
+			if(np) pxref_np_run(np_, t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), PxU32(np), cDist, 0.01f, tolLen, 1, cts.data(), 8, cnt.data());
+			pxref_np_release(np_);
+		}
+		std::vector<PxU32> ca, cb, cs, cc, fcount;
 		std::vector<float> packed, mat;
+		std::vector<PxU8*> fptr;
+		std::vector<PairStateRef*> cstate;
 		for(size_t k = 0; k < np; k++)
 		{
 			if(!cnt[k]) continue;
+			if(ps)
+			{
+				cstate.push_back(state[k]);
+				fptr.push_back(state[k]->frictions);
+				fcount.push_back(state[k]->nbFrictions);
+			}
 			ca.push_back(pairs[k].first); cb.push_back(pairs[k].second);
 			cs.push_back(PxU32(packed.size() / 8)); cc.push_back(cnt[k]);
 			packed.insert(packed.end(), &cts[k * 64], &cts[k * 64] + 8 * cnt[k]);
@@ -637,8 +764,16 @@ HX int pxref_scene_step(PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32
 		std::vector<PxU32> hs(2 * ca.size() + 2), hst(2 * ca.size() + 2), ord(ca.size() + 1);
 		for(PxU32 k = 0; k < m; k++) memcpy(&statics[7 * k], staticPoses + 7 * size_t(s0 + k), 28);
 		const float g[3] = {params[1], params[2], params[3]};
-		pxref_tgs_solve(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), PxU32(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(), g,
-			dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(), ord.data(), NULL, NULL);
+		if(ps)
+		{
+			tgsFrameRef(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), PxU32(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(), g,
+				dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(), ord.data(), NULL,
+				NULL, ps->constraintAlloc, fptr.data(), fcount.data());
+			for(size_t k = 0; k < cstate.size(); k++) { cstate[k]->frictions = fptr[k]; cstate[k]->nbFrictions = fcount[k]; }
+		}
+		else
+			pxref_tgs_solve(&rigid[b0], n, statics.data(), m, ca.data(), cb.data(), PxU32(ca.size()), cs.data(), cc.data(), packed.data(), mat.data(), g,
+				dt, iterations[0], iterations[1], params[7], params[8], params[9], vel.data(), outPose.data(), hs.data(), hst.data(), ord.data(), NULL, NULL);
 		for(PxU32 i = 0; i < n; i++)
 		{
 			PxRigidBodyData& r = rigid[b0 + i];
@@ -652,6 +787,7 @@ HX int pxref_scene_step(PxU32 nbScenes, const PxU32* sceneBodyCount, const PxU32
 	}
 	return 0;
 }
+} // namespace
 
 // The reference's approximate reciprocal (aos::V3RecipFast, used by the box-box
 // edge clipping in GuPCMContactBoxBox.cpp:140), four lanes at a time.

@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_libs import CachedContacts, CpuBroadPhase, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
+from oracle_libs import CachedContacts, CpuBroadPhase, PersistentScenes, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
 from scenarios import bp_frames, moving_pairs, np_pairs, pile_scenes, random_scene  # noqa: E402
 
 BP_CASES = [
@@ -131,6 +131,28 @@ def make_scene():
         print("wrote", name)
 
 
+PERSISTENT_CASES = [
+    # name, seed, scenes, bodies per scene, frames: contact caches and friction data carried between frames
+    ("persist_piles", 44, 3, 48, 24),
+]
+
+
+def make_persistent():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from physx_gb300.world import DEFAULT_PARAMS
+    for name, seed, S, n, frames in PERSISTENT_CASES:
+        sc = pile_scenes(seed, S, n)
+        ref = PersistentScenes("pxref", sc, DEFAULT_PARAMS)
+        out = {}
+        for f in range(frames):
+            out["ref_rigid_%d" % f] = ref.step().view(np.uint8).reshape(-1, 96).copy()
+        ref.release()
+        arrays = {k: v for k, v in sc.items() if k != "rigid"}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), rigid=sc["rigid"].view(np.uint8).reshape(-1, 96), frames=np.array(frames),
+                            **out, **arrays)
+        print("wrote", name)
+
+
 def make_recip():
     """The reference's approximate reciprocal (V3RecipFast): one input per 2^-11
     mantissa cell of [1, 2), random magnitudes of both signs, and special values."""
@@ -146,7 +168,7 @@ def make_recip():
     print("wrote recip_fast")
 
 
-def pyramid_trace(which, steps=300):
+def pyramid_trace(which, steps=300, persistent=False):
     """Long-horizon statistics of the 210-box pyramid stepped `steps` times: kinetic
     energy and highest / lowest box centre per step, final horizontal drift."""
     sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
@@ -155,8 +177,9 @@ def pyramid_trace(which, steps=300):
     sc = pyramid_scene()
     rb = sc["rigid"].copy()
     ke, top, low = [], [], []
+    ps = PersistentScenes(which, sc, DEFAULT_PARAMS) if persistent else None
     for _ in range(steps):
-        rb = run_scene_step(which, dict(sc, rigid=rb), DEFAULT_PARAMS, steps=1)
+        rb = ps.step().copy() if ps else run_scene_step(which, dict(sc, rigid=rb), DEFAULT_PARAMS, steps=1)
         ke.append(kinetic_energy(rb))
         top.append(float(rb["p"][:, 1].max()))
         low.append(float(rb["p"][:, 1].min()))
@@ -167,12 +190,14 @@ def pyramid_trace(which, steps=300):
 def make_pyramid():
     np.savez_compressed(os.path.join(HERE, "pyramid_stats.npz"), **pyramid_trace("pxref"))
     print("wrote pyramid_stats")
+    np.savez_compressed(os.path.join(HERE, "pyramid_stats_persistent.npz"), **pyramid_trace("pxref", persistent=True))
+    print("wrote pyramid_stats_persistent")
 
 
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np", "np_cached", "tgs", "scene", "recip", "pyramid"]
+    which = sys.argv[1:] or ["bp", "np", "np_cached", "tgs", "scene", "persistent", "recip", "pyramid"]
     if "bp" in which:
         make_bp()
     if "np" in which:
@@ -183,6 +208,8 @@ if __name__ == "__main__":
         make_tgs()
     if "scene" in which:
         make_scene()
+    if "persistent" in which:
+        make_persistent()
     if "recip" in which:
         make_recip()
     if "pyramid" in which:

@@ -217,3 +217,38 @@ class CachedContacts:
         if self.which != "orc" and self.ctx:
             self.L.pxref_np_release(self.ctx)
             self.ctx = None
+
+
+class PersistentScenes:
+    """Scene frames with persistent pair state (contact caches and friction data
+    carried between frames, the snippet's WITH_PERSISTENCY mode) through the oracle
+    ("orc") or the reference ("pxref")."""
+
+    def __init__(self, which, scenes, params):
+        import sys
+        sys.path.insert(0, ROOT)
+        from physx_gb300.world import param_vector
+        self.which = which
+        self.pv, self.it = param_vector(params)
+        self.L = oracle() if which == "orc" else reference()
+        create = self.L.orc_persistent_create if which == "orc" else self.L.pxref_persistent_create
+        create.restype = ctypes.c_void_p
+        self.h = ctypes.c_void_p(create())
+        self.fn = self.L.orc_scene_step_persistent if which == "orc" else self.L.pxref_scene_step_persistent
+        self.keep = [np.ascontiguousarray(scenes[k], d) for k, d in (("body_count", np.uint32), ("static_count", np.uint32),
+                                                                       ("types", np.int32), ("geoms", np.float32), ("friction", np.float32),
+                                                                       ("static_poses", np.float32), ("static_types", np.int32),
+                                                                       ("static_geoms", np.float32))]
+        self.rb = np.ascontiguousarray(scenes["rigid"]).copy()
+
+    def step(self, steps=1):
+        k = self.keep
+        for _ in range(steps):
+            self.fn(self.h, ctypes.c_uint32(len(k[0])), _p(k[0]), _p(k[1]), _p(self.rb), _p(k[2]), _p(k[3]), _p(k[4]), _p(k[5]), _p(k[6]),
+                    _p(k[7]), _p(self.pv), _p(self.it))
+        return self.rb
+
+    def release(self):
+        if self.h:
+            (self.L.orc_persistent_release if self.which == "orc" else self.L.pxref_persistent_release)(self.h)
+            self.h = None

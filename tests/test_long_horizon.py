@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pyramid_stats.npz")
+GOLDEN_PERSISTENT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pyramid_stats_persistent.npz")
 STEPS = 300
 
 
@@ -42,6 +43,26 @@ def test_oracle_pyramid_statistics_match_reference():
         low.append(rb["p"][:, 1].min())
     check_stats(ref, np.array(ke), np.array(top), np.array(low), float(np.abs(rb["p"][:, 0] - sc["rigid"]["p"][:, 0]).mean()))
     # the oracle follows the reference's arithmetic exactly: its 300-step trace is the reference's
+    assert np.array_equal(np.array(ke), ref["ke"]) and np.array_equal(np.array(top), ref["top"])
+    assert np.array_equal(np.array(low), ref["low"])
+
+
+def test_oracle_pyramid_persistent_trace_equals_reference():
+    """The snippet's default mode: contact caches and friction data persist between
+    frames.  The oracle's 300-step trace is the reference's, bit for bit."""
+    from oracle_libs import PersistentScenes
+    from physx_gb300.workloads import kinetic_energy, pyramid_scene
+    from physx_gb300.world import DEFAULT_PARAMS
+    ref = np.load(GOLDEN_PERSISTENT)
+    sc = pyramid_scene()
+    ps = PersistentScenes("orc", sc, DEFAULT_PARAMS)
+    ke, top, low = [], [], []
+    for _ in range(STEPS):
+        rb = ps.step()
+        ke.append(kinetic_energy(rb))
+        top.append(rb["p"][:, 1].max())
+        low.append(rb["p"][:, 1].min())
+    ps.release()
     assert np.array_equal(np.array(ke), ref["ke"]) and np.array_equal(np.array(top), ref["top"])
     assert np.array_equal(np.array(low), ref["low"])
 

@@ -230,6 +230,55 @@ def test_oracle_scene_steps_match_reference_live(seed):
     assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
+def load_persistent_fixture(path):
+    from scenarios import rigid_body_data
+    z = np.load(path)
+    rb = rigid_body_data(len(z["rigid"]))
+    rb.view(np.uint8).reshape(len(rb), 96)[:] = z["rigid"]
+    frames = []
+    for f in range(int(z["frames"])):
+        r = rigid_body_data(len(z["rigid"]))
+        r.view(np.uint8).reshape(len(r), 96)[:] = z["ref_rigid_%d" % f]
+        frames.append(r)
+    scenes = {k: z[k] for k in z.files if k != "rigid" and k != "frames" and not k.startswith("ref_rigid_")}
+    scenes["rigid"] = rb
+    return scenes, frames
+
+
+PERSISTENT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "persist_*.npz")))
+
+
+@pytest.mark.parametrize("path", PERSISTENT_FIXTURES, ids=[os.path.basename(p) for p in PERSISTENT_FIXTURES])
+def test_oracle_persistent_frames_match_reference_golden(path):
+    """Frames with persistent pair state (PCM caches and friction patches carried
+    between frames, broken-friction flags, block-path patch handling): every frame
+    equals the reference's bit for bit."""
+    from oracle_libs import PersistentScenes
+    sys_path_root()
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes, frames = load_persistent_fixture(path)
+    orc = PersistentScenes("orc", scenes, DEFAULT_PARAMS)
+    for f, ref in enumerate(frames):
+        out = orc.step()
+        assert np.array_equal(out.view(np.uint8), ref.view(np.uint8)), "frame %d" % f
+    orc.release()
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed", [210, 211])
+def test_oracle_persistent_frames_match_reference_live(seed):
+    from oracle_libs import PersistentScenes
+    from scenarios import pile_scenes
+    sys_path_root()
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = pile_scenes(seed, 3, 60)
+    orc, ref = PersistentScenes("orc", sc, DEFAULT_PARAMS), PersistentScenes("pxref", sc, DEFAULT_PARAMS)
+    for _ in range(30):
+        assert np.array_equal(orc.step().view(np.uint8), ref.step().view(np.uint8))
+    orc.release()
+    ref.release()
+
+
 def sys_path_root():
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
