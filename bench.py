@@ -65,11 +65,16 @@ def _cpu_worker(payload):
                                                               ("geoms", np.float32), ("friction", np.float32), ("static_poses", np.float32),
                                                               ("static_types", np.int32), ("static_geoms", np.float32))]
     rb = np.ascontiguousarray(scenes["rigid"]).copy()
+    # the reference snippet's persistent mode (contact caches and friction data kept between steps), as the world runs
+    L.orc_persistent_create.restype = ctypes.c_void_p
+    h = ctypes.c_void_p(L.orc_persistent_create())
     t = time.perf_counter()
     for _ in range(steps):
-        L.orc_scene_step(ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]),
-                         _p(keep[5]), _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
-    return time.perf_counter() - t, int(keep[0].sum())
+        L.orc_scene_step_persistent(h, ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]),
+                                    _p(keep[5]), _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
+    elapsed = time.perf_counter() - t
+    L.orc_persistent_release(h)
+    return elapsed, int(keep[0].sum())
 
 
 def split_scenes(scenes, idx):
@@ -171,7 +176,7 @@ def bench_pyramid(steps):
     """The 210-box pyramid of the reference's immediate-mode snippet (one scene, the world
     API), against the oracle restatement of the same frame on one host thread."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle_libs import run_scene_step
+    from oracle_libs import PersistentScenes
     from physx_gb300.workloads import pyramid_scene
     from physx_gb300.world import DEFAULT_PARAMS, World
     sc = pyramid_scene()
@@ -180,9 +185,11 @@ def bench_pyramid(steps):
     w.synchronize()
     ms = w.time_steps(steps, graph=True)
     w.release()
+    ps = PersistentScenes("orc", sc, DEFAULT_PARAMS)
     t = time.perf_counter()
-    run_scene_step("orc", sc, DEFAULT_PARAMS, steps=steps)
+    ps.step(steps)
     cpu_s = time.perf_counter() - t
+    ps.release()
     n = len(sc["rigid"])
     return dict(workload="210-box pyramid (20 levels, h 0.5, jitter 0.01 m / 2 deg), plane, TGS 4/1, dt 1/60", bodies=n, steps=steps,
                 ms_per_step=ms / steps, value=n * steps / (ms / 1000.0), unit=UNIT,

@@ -73,6 +73,16 @@ uint32_t gbpx_bp_kinematic_filter_group(uint32_t id);
 int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
                            const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
                            float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts);
+/* The same with persistent caches, as PxGenerateContacts with a PxCache per pair
+ * kept between calls: manifolds (nbPairs x 288 bytes, host memory, zero for a
+ * fresh cache) carries the contact manifold of the plane-capsule, plane-box,
+ * capsule-box and box-box pairs (gEnablePCMCaching,
+ * physx/source/lowlevel/software/src/PxsContext.cpp:89) from one call to the
+ * next: refresh and invalidation (geomutils/src/pcm/GuPersistentContactManifold.h:190-271),
+ * incremental points and the GJK warm start.  It is read and updated. */
+int gbpx_generate_contacts_cached(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                                  const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
+                                  float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts, void* manifolds);
 
 /* No counterpart in the reference: the same contact generation for callers
  * that may not allocate device memory during the call (a cudaMalloc or
@@ -152,12 +162,16 @@ int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* 
  * Many independent scenes advanced together: one persistent launch per step
  * (optionally a CUDA graph), all state resident on the device.  Each scene's
  * frame is the reference immediate-mode loop (physx/snippets/
- * snippetimmediatemode/SnippetImmediateMode.cpp:473) with a fresh broadphase,
- * PxCache and friction data per frame.  No single reference function is
- * replaced: this is the multi-scene driver of the functions above.
- * params (11 floats): dt, gravity xyz, contactDistance, toleranceLength,
+ * snippetimmediatemode/SnippetImmediateMode.cpp:473): all overlapping pairs,
+ * contacts, TGS.  With persistence on (the snippet's WITH_PERSISTENCY default)
+ * every overlapping pair keeps its PCM contact manifold and the friction
+ * patches of its contact constraint from step to step; a pair starts fresh
+ * when it starts overlapping.  With persistence off every step uses fresh
+ * caches and friction data.  No single reference function is replaced: this
+ * is the multi-scene driver of the functions above.
+ * params (12 floats): dt, gravity xyz, contactDistance, toleranceLength,
  * boundsMargin, bounceThreshold, frictionOffsetThreshold, correlationDistance,
- * staticFriction; iterations: position, velocity. */
+ * staticFriction, persistence (0 or 1); iterations: position, velocity. */
 int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, const void* rigidBodies,
                       const int* types, const float* geoms, const float* friction, const float* staticPoses, const int* staticTypes,
                       const float* staticGeoms, const float* params, const uint32_t* iterations, uint32_t pairsPerBody, void** outWorld);

@@ -39,3 +39,43 @@ def generate_contacts(pairs, contact_distance=0.04, mesh_contact_margin=0.01, to
     if rc == -3:
         raise GbpxError(rc, "PxGenerateContacts (more contacts than max_per_pair)")
     return cnt, out
+
+
+MANIFOLD_BYTES = 288
+
+
+class CachedContacts:
+    """PxGenerateContacts over the same pairs frame after frame with persistent
+    caches: each pair's contact manifold (plane-capsule, plane-box, capsule-box and
+    box-box keep one, as PxCache does) is carried from one call to the next in a
+    288-byte record per pair held here."""
+
+    def __init__(self, nb_pairs):
+        L = _setup()
+        if not getattr(L, "_np_cached_ready", False):
+            L.gbpx_generate_contacts_cached.argtypes = ([ctypes.c_void_p] * 6 + [ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                                                                  ctypes.c_float, ctypes.c_void_p, ctypes.c_uint32,
+                                                                                  ctypes.c_void_p, ctypes.c_void_p])
+            L._np_cached_ready = True
+        self.L = L
+        self.state = np.zeros(nb_pairs * MANIFOLD_BYTES, np.uint8)
+
+    def reset(self):
+        """Fresh caches for every pair."""
+        self.state[:] = 0
+
+    def run(self, pairs, contact_distance=0.04, mesh_contact_margin=0.01, tolerance_length=1.0, max_per_pair=4):
+        arrs = [np.ascontiguousarray(pairs[k], dtype=d) for k, d in zip(_ARG_KEYS, _DTYPES)]
+        n = len(arrs[0])
+        if n * MANIFOLD_BYTES != len(self.state):
+            raise ValueError("pair count differs from the cache count")
+        out = np.zeros((n, max_per_pair, 8), np.float32)
+        cnt = np.zeros(n, np.uint32)
+        rc = self.L.gbpx_generate_contacts_cached(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], n, contact_distance,
+                                                  mesh_contact_margin, tolerance_length, out.ctypes.data_as(ctypes.c_void_p),
+                                                  max_per_pair, cnt.ctypes.data_as(ctypes.c_void_p),
+                                                  self.state.ctypes.data_as(ctypes.c_void_p))
+        if rc == -3:
+            raise GbpxError(rc, "PxGenerateContacts (more contacts than max_per_pair)")
+        check(rc, "PxGenerateContacts")
+        return cnt, out

@@ -66,10 +66,23 @@ struct Buffer
 // PersistentContact: local point on A, local point on B, local normal + penetration
 struct PC { V3 a, b, n; float pen; };
 
+// PersistentContactManifold state (GuPersistentContactManifold.h:144): the
+// points, and what the next frame's refresh / invalidate tests read -- the
+// relative transform when contacts were last generated (p = FLT_MAX when
+// cleared) and, for box-box, both bodies' orientations then.
 struct Manifold
 {
 	PC pts[4];
 	int num = 0;
+	Tr rel;
+	Q quatA, quatB;
+	int warmA[4], warmB[4], warmSize = 0;   // GJK warm start: last simplex's vertex indices
+	__device__ Manifold()
+	{
+		rel.q = Q{0.0f, 0.0f, 0.0f, 1.0f};
+		rel.p = v3(FLT_MAX, FLT_MAX, FLT_MAX);
+		quatA = quatB = Q{0.0f, 0.0f, 0.0f, 1.0f};
+	}
 };
 
 static __device__ float distPointSegSq(V3 a, V3 b, V3 p)
@@ -177,6 +190,13 @@ static __device__ bool sphereBox(float r, V3 ext, const Tr& t0, const Tr& t1, fl
 }
 
 // ----------------------------------------------------------------- manifold helpers
+// PxMatTransformV
+struct MatTr { M33 R; V3 p; };
+static __device__ MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
+static __device__ V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
+static __device__ V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
+static __device__ V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
+static __device__ V3 mtTransformInv(const MatTr& m, V3 v) { return m33TMulV(m.R, sub(v, m.p)); }
 static __device__ bool replacePoint(Manifold& m, const PC& c, float thr)
 {
 	const float sd = thr * thr;
@@ -419,6 +439,199 @@ static __device__ void addBatch2(Manifold& m, const PC* pts, int n)
 	else { reduceBatch2(m, pts, n); m.num = 2; }
 }
 
+// ----------------------------------------------------------------- manifold persistence
+// GuPersistentContactManifold.cpp:175-187
+static __device__ __forceinline__ float kInvalidateThresholds(int n) { return n == 0 ? 0.5f : (n == 1 ? 0.125f : (n == 2 ? 0.25f : 0.375f)); }
+static __device__ __forceinline__ float kInvalidateThresholds2(int n) { return n == 0 ? 0.5f : (n == 1 ? 0.1f : 0.75f); }
+static __device__ __forceinline__ float kInvalidateQuatThresholds(int n) { return n == 0 ? 0.9998f : 0.9999f; }
+static __device__ __forceinline__ float kInvalidateQuatThresholds2(int n) { return n == 0 ? 0.9995f : (n == 1 ? 0.9999f : 0.9997f); }
+
+// V4Dot / QuatDot of the SSE2 layer: (y*y' + w*w') + (z*z' + x*x')
+static __device__ float quatDot(Q a, Q b) { return (a.y * b.y + a.w * b.w) + (a.z * b.z + a.x * b.x); }
+
+// refreshContactPoints (GuPersistentContactManifold.h:723): re-project every
+// point with the current relative transform, drop those that slid further than
+// the threshold, update the penetration of the rest.
+static __device__ void refreshManifold(Manifold& m, const MatTr& aToB, float projectBreakingThreshold)
+{
+	const float sq = projectBreakingThreshold * projectBreakingThreshold;
+	for(int i = m.num; i > 0; --i)
+	{
+		PC& p = m.pts[i - 1];
+		const V3 aInB = add(m33MulV(aToB.R, p.a), aToB.p);
+		const V3 v = sub(aInB, p.b);
+		const float dist = dotA(v, p.n);
+		const V3 projected = negScaleSub(p.n, dist, aInB);
+		const V3 diff = sub(p.b, projected);
+		if(dotA(diff, diff) > sq)
+		{
+			m.num--;
+			m.pts[i - 1] = m.pts[m.num];
+		}
+		else
+			p.pen = dist;
+	}
+}
+
+// maxTransformPositionDelta: V4ExtractMax(|curP - rel.p|, w = 0)
+static __device__ float maxPositionDelta(const Manifold& m, V3 curP)
+{
+	const V3 d = vabs(sub(curP, m.rel.p));
+	return fmax_(fmax_(d.x, 0.0f), fmax_(d.z, d.y));
+}
+
+// invalidate_BoxConvex (GuPersistentContactManifold.h:190)
+static __device__ bool invalidateBoxConvex(const Manifold& m, const Tr& cur, Q quatA, Q quatB, float minMargin, float radiusA, float radiusB)
+{
+	const float thresholdP = minMargin * kInvalidateThresholds(m.num);
+	const float deltaP = maxPositionDelta(m, cur.p);
+	const float thresholdQ = kInvalidateQuatThresholds(m.num);
+	const float dqA = quatDot(quatA, m.quatA), dqB = quatDot(quatB, m.quatB);
+	if(deltaP > thresholdP || thresholdQ > dqA || thresholdQ > dqB) return true;
+	const float aRadian = dqA < 1.0f ? acosf(dqA) : 0.0f;
+	const float bRadian = dqB < 1.0f ? acosf(dqB) : 0.0f;
+	return aRadian * radiusA > thresholdP || bRadian * radiusB > thresholdP;
+}
+
+// invalidate_SphereCapsule (GuPersistentContactManifold.h:227)
+static __device__ bool invalidateSphereCapsule(const Manifold& m, const Tr& cur, float minMargin)
+{
+	const float thresholdP = minMargin * kInvalidateThresholds2(m.num);
+	const float deltaP = maxPositionDelta(m, cur.p);
+	const float dq = quatDot(cur.q, m.rel.q);
+	return deltaP > thresholdP || kInvalidateQuatThresholds2(m.num) > dq;
+}
+
+// invalidate_PrimitivesPlane (GuPersistentContactManifold.h:245)
+static __device__ bool invalidatePrimitivesPlane(const Manifold& m, const Tr& cur, float minMargin, float ratio)
+{
+	const float thresholdP = minMargin * ratio;
+	const float deltaP = maxPositionDelta(m, cur.p);
+	const float dq = quatDot(cur.q, m.rel.q);
+	return deltaP > thresholdP || 0.99996f > dq;
+}
+
+// getWorldNormal (GuPersistentContactManifold.h:691): the manifold's summed
+// normal (first point's if the sum vanishes), rotated into world space and
+// normalized (QuatRotateAndNormalize)
+static __device__ V3 manifoldWorldNormal(const Manifold& m, const Tr& trB)
+{
+	V3 n = m.pts[0].n;
+	for(int i = 1; i < m.num; i++) n = add(n, m.pts[i].n);
+	const V3 nn = dotA(n, n) > FLT_EPSILON ? n : m.pts[0].n;
+	const Q q = trB.q;
+	const float w2 = q.w * q.w + (-0.5f);
+	const V3 u = qv(q);
+	const V3 temp = scaleAdd(cross(u, nn), q.w, scale(nn, w2));
+	return normalizeA(scaleAdd(u, dotA(u, nn), temp));
+}
+
+// distancePointTriangleSquaredLocal (GuPersistentContactManifold.cpp:61)
+static __device__ float distPointTriangleSq(V3 p, V3 a, V3 b, V3 c)
+{
+	const V3 ab = sub(b, a), ac = sub(c, a), bc = sub(c, b);
+	const V3 ap = sub(p, a), bp = sub(p, b), cp = sub(p, c);
+	const float d1 = dotA(ab, ap), d2 = dotA(ac, ap), d3 = dotA(ab, bp);
+	const float d4 = dotA(ac, bp), d5 = dotA(ab, cp), d6 = dotA(ac, cp);
+	const float unom = d4 - d3, udenom = d5 - d6;
+	if(0.0f > d1 && 0.0f > d2) { const V3 vv = sub(p, a); return dotA(vv, vv); }
+	if(d3 >= 0.0f && d3 >= d4) { const V3 vv = sub(p, b); return dotA(vv, vv); }
+	if(d6 >= 0.0f && d6 >= d5) { const V3 vv = sub(p, c); return dotA(vv, vv); }
+	const float vc = d1 * d4 - d3 * d2;
+	if(0.0f > vc && d1 >= 0.0f && 0.0f > d3)
+	{
+		const float s = d1 / (d1 - d3);
+		const V3 vv = sub(p, scaleAdd(ab, s, a));
+		return dotA(vv, vv);
+	}
+	const float va = d3 * d6 - d5 * d4;
+	if(0.0f > va && d4 >= d3 && d5 >= d6)
+	{
+		const float u = unom / (unom + udenom);
+		const V3 vv = sub(p, scaleAdd(bc, u, b));
+		return dotA(vv, vv);
+	}
+	const float vb = d5 * d2 - d1 * d6;
+	if(0.0f > vb && d2 >= 0.0f && 0.0f > d6)
+	{
+		const float t = d2 / (d2 - d6);
+		const V3 vv = sub(p, scaleAdd(ac, t, a));
+		return dotA(vv, vv);
+	}
+	const V3 n = cross(ab, ac);
+	const float nn = dotA(n, n);
+	const float t = nn > 0.0f ? dotA(n, sub(a, p)) / nn : 0.0f;
+	const V3 vv = sub(p, add(p, scale(n, t)));
+	return dotA(vv, vv);
+}
+
+// reduceContactsForPCM (GuPersistentContactManifold.cpp:603): four manifold
+// points plus a new one down to four
+static __device__ void reduceForPCM(Manifold& m, const PC& c)
+{
+	bool chosen[5] = {false, false, false, false, false};
+	PC tmp[5];
+	for(int i = 0; i < 4; i++) tmp[i] = m.pts[i];
+	tmp[4] = c;
+	float maxDist = c.pen;
+	int index = 4;
+	for(int i = 0; i < 4; i++)
+		if(maxDist > tmp[i].pen) { maxDist = tmp[i].pen; index = i; }
+	chosen[index] = true;
+	m.pts[0] = tmp[index];
+	V3 dir = sub(tmp[0].b, m.pts[0].b);
+	maxDist = dotA(dir, dir);
+	index = 0;
+	for(int i = 1; i < 5; i++)
+		if(!chosen[i])
+		{
+			dir = sub(tmp[i].b, m.pts[0].b);
+			const float d = dotA(dir, dir);
+			if(d > maxDist) { maxDist = d; index = i; }
+		}
+	chosen[index] = true;
+	m.pts[1] = tmp[index];
+	maxDist = -FLT_MAX;
+	for(int i = 0; i < 5; i++)
+		if(!chosen[i])
+		{
+			const float d = distPointSegSq(m.pts[0].b, m.pts[1].b, tmp[i].b);
+			if(d > maxDist) { maxDist = d; index = i; }
+		}
+	chosen[index] = true;
+	m.pts[2] = tmp[index];
+	maxDist = -FLT_MAX;
+	for(int i = 0; i < 5; i++)
+		if(!chosen[i])
+		{
+			const float d = distPointTriangleSq(tmp[i].b, m.pts[0].b, m.pts[1].b, m.pts[2].b);
+			if(d > maxDist) { maxDist = d; index = i; }
+		}
+	if(chosen[index]) { m.num = 3; return; }
+	chosen[index] = true;
+	m.pts[3] = tmp[index];
+	int notChosen = 0;
+	for(int a = 0; a < 5; a++)
+		if(!chosen[a]) { notChosen = a; break; }
+	float closest = FLT_MAX;
+	index = 0;
+	for(int a = 0; a < 4; a++)
+	{
+		const V3 dif = sub(m.pts[a].a, tmp[notChosen].a);
+		const float d2 = dotA(dif, dif);
+		if(closest > d2) { closest = d2; index = a; }
+	}
+	if(m.pts[index].pen > tmp[notChosen].pen) m.pts[index] = tmp[notChosen];
+}
+
+// addManifoldPoint (GuPersistentContactManifold.cpp:1246)
+static __device__ void addPoint4(Manifold& m, const PC& c, float thr)
+{
+	if(replacePoint(m, c, thr)) return;
+	if(m.num < 4) { m.pts[m.num++] = c; return; }
+	reduceForPCM(m, c);
+}
+
 static __device__ float boxMargin(V3 ext, float tolLen)
 {
 	const float mn = fmin_(ext.x, fmin_(ext.y, ext.z));
@@ -426,7 +639,9 @@ static __device__ float boxMargin(V3 ext, float tolLen)
 }
 
 // ----------------------------------------------------------------- plane
-static __device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const Tr& tCap, float cDist, Buffer& out)
+// pcmContactPlaneCapsule (GuPCMContactPlaneCapsule.cpp:36); m is the pair's
+// persistent manifold (a fresh one for a fresh cache)
+static __device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const Tr& tCap, float cDist, Manifold& m, Buffer& out)
 {
 	const Tr& transf0 = tCap;
 	const Tr& transf1 = tPlane;
@@ -439,62 +654,80 @@ static __device__ bool planeCapsule(float r, float hh, const Tr& tPlane, const T
 	const V3 s = add(aToB.p, tmp), e = sub(aToB.p, tmp);
 	const float infl = r + cDist;
 	const float replaceThr = r * 0.001f;
-	Manifold m;
-	const float sd0 = s.x;
-	if(infl > sd0)
+	const float projectThr = r * 0.05f;
+	const int initial = m.num;
+	refreshManifold(m, matFromTr(aToB), projectThr);
+	const bool lost = m.num != initial;
+	if(lost || invalidatePrimitivesPlane(m, aToB, r, 0.02f))
 	{
-		PC c; c.a = trTransformInv(aToB, s); c.b = negScaleSub(localN, sd0, s); c.n = localN; c.pen = sd0;
-		addPoint2(m, c, replaceThr);
-	}
-	const float sd1 = e.x;
-	if(infl > sd1)
-	{
-		PC c; c.a = trTransformInv(aToB, e); c.b = negScaleSub(localN, sd1, e); c.n = localN; c.pen = sd1;
-		addPoint2(m, c, replaceThr);
+		m.num = 0;
+		m.rel = aToB;
+		const float sd0 = s.x;
+		if(infl > sd0)
+		{
+			PC c; c.a = trTransformInv(aToB, s); c.b = negScaleSub(localN, sd0, s); c.n = localN; c.pen = sd0;
+			addPoint2(m, c, replaceThr);
+		}
+		const float sd1 = e.x;
+		if(infl > sd1)
+		{
+			PC c; c.a = trTransformInv(aToB, e); c.b = negScaleSub(localN, sd1, e); c.n = localN; c.pen = sd1;
+			addPoint2(m, c, replaceThr);
+		}
 	}
 	outputCapsuleLike(m, cn, planeN, transf0, r, cDist, out);
 	return m.num > 0;
 }
 
-static __device__ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, float tolLen, Buffer& out)
+// pcmContactPlaneBox (GuPCMContactPlaneBox.cpp:36)
+static __device__ bool planeBox(V3 ext, const Tr& tPlane, const Tr& tBox, float cDist, float tolLen, Manifold& m, Buffer& out)
 {
 	const Tr& transf0 = tBox;
 	const Tr& transf1 = tPlane;
 	const Tr cur = trInvMul(transf1, transf0);
 	const V3 negN = normalizeA(neg(qBasis0(transf1.q)));
 	const V3 localN = unitX();
+	const float margin = boxMargin(ext, tolLen);
+	const float projectThr = margin * 0.2f;
 	// PxMatTransformV(cur): rotation matrix columns from the quaternion
-	const M33 R = m33FromQuatCol(cur.q);
-	const float bx = ext.x, by = ext.y, bz = ext.z;
-	const V3 t0 = scale(R.c0, bx), t1 = scale(R.c1, by), t2 = scale(R.c2, bz);
-	const V3 nt2 = neg(t2);
-	const float px = cur.p.x;
-	const V3 t01 = add(t0, t1), t02 = sub(t0, t1);
-	const float s[8] = {add(t2, t01).x, add(nt2, t01).x, add(t2, t02).x, add(nt2, t02).x,
-	                    sub(t2, t02).x, sub(nt2, t02).x, sub(t2, t01).x, sub(nt2, t01).x};
-	const V3 corners[8] = {v3(bx, by, bz), v3(bx, by, -bz), v3(bx, -by, bz), v3(bx, -by, -bz),
-	                       v3(-bx, by, bz), v3(-bx, by, -bz), v3(-bx, -by, bz), v3(-bx, -by, -bz)};
-	const float acc = cDist - px;
-	PC pts[8];
-	int n = 0;
-	for(int k = 0; k < 8; k++)
+	const MatTr aToB = matFromTr(cur);
+	const int initial = m.num;
+	refreshManifold(m, aToB, projectThr);
+	const bool lost = m.num != initial;
+	if(lost || invalidatePrimitivesPlane(m, cur, margin, 0.2f))
 	{
-		if(acc > s[k])
+		m.num = 0;
+		m.rel = cur;
+		const M33& R = aToB.R;
+		const float bx = ext.x, by = ext.y, bz = ext.z;
+		const V3 t0 = scale(R.c0, bx), t1 = scale(R.c1, by), t2 = scale(R.c2, bz);
+		const V3 nt2 = neg(t2);
+		const float px = cur.p.x;
+		const V3 t01 = add(t0, t1), t02 = sub(t0, t1);
+		const float sv[8] = {add(t2, t01).x, add(nt2, t01).x, add(t2, t02).x, add(nt2, t02).x,
+		                     sub(t2, t02).x, sub(nt2, t02).x, sub(t2, t01).x, sub(nt2, t01).x};
+		const V3 corners[8] = {v3(bx, by, bz), v3(bx, by, -bz), v3(bx, -by, bz), v3(bx, -by, -bz),
+		                       v3(-bx, by, bz), v3(-bx, by, -bz), v3(-bx, -by, bz), v3(-bx, -by, -bz)};
+		const float acc = cDist - px;
+		PC pts[8];
+		int n = 0;
+		for(int k = 0; k < 8; k++)
 		{
-			const float pen = s[k] + px;
-			// aToB.transform(p) with the matrix form of the relative transform
-			const V3 wp = add(m33MulV(R, corners[k]), cur.p);
-			pts[n].a = corners[k];
-			pts[n].b = negScaleSub(localN, pen, wp);
-			pts[n].n = localN;
-			pts[n].pen = pen;
-			n++;
+			if(acc > sv[k])
+			{
+				const float pen = sv[k] + px;
+				// aToB.transform(p) with the matrix form of the relative transform
+				const V3 wp = add(m33MulV(R, corners[k]), cur.p);
+				pts[n].a = corners[k];
+				pts[n].b = negScaleSub(localN, pen, wp);
+				pts[n].n = localN;
+				pts[n].pen = pen;
+				n++;
+			}
 		}
+		addBatchCluster(m, pts, n);
 	}
-	Manifold m;
-	addBatchCluster(m, pts, n);
 	outputWithOffset(m, negN, transf1, cDist, out);
-	(void)tolLen;
 	return m.num > 0;
 }
 
@@ -589,12 +822,6 @@ static __device__ bool capsuleCapsule(float r0, float hh0, float r1, float hh1, 
 }
 
 // ----------------------------------------------------------------- box-box
-struct MatTr { M33 R; V3 p; };
-static __device__ MatTr matFromTr(const Tr& t) { MatTr m; m.R = m33FromQuatCol(t.q); m.p = t.p; return m; }
-static __device__ V3 mtTransform(const MatTr& m, V3 v) { return add(m33MulV(m.R, v), m.p); }
-static __device__ V3 mtRotate(const MatTr& m, V3 v) { return m33MulV(m.R, v); }
-static __device__ V3 mtRotateInv(const MatTr& m, V3 v) { return m33TMulV(m.R, v); }
-static __device__ V3 mtTransformInv(const MatTr& m, V3 v) { return m33TMulV(m.R, sub(v, m.p)); }
 static __device__ M33 transpose(const M33& m)
 {
 	M33 t;
@@ -915,95 +1142,155 @@ static __device__ bool boxBoxGenerate(V3 e0, V3 e1, const MatTr& T0, const MatTr
 
 #include "gjk_epa.cuh"
 
-static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen, Buffer& out)
+// the simplex indices gjkPenetration leaves in the manifold for the next call
+static __device__ void keepWarmStart(Manifold& m, const GjkOut& g)
+{
+	m.warmSize = g.warmSize;
+	for(int i = 0; i < g.warmSize; i++) { m.warmA[i] = g.aInd[i]; m.warmB[i] = g.bInd[i]; }
+}
+
+
+// pcmContactBoxBox (GuPCMContactBoxBox.cpp:848)
+static __device__ bool boxBox(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float cDist, float tolLen, Manifold& m, Buffer& out)
 {
 	const Tr cur = trInvMul(tB, tA);
+	const MatTr aToB = matFromTr(cur);
 	const float m0 = boxMargin(e0, tolLen), m1 = boxMargin(e1, tolLen);
 	const float minMargin = fmin_(m0, m1);
-	MatTr T0 = matFromTr(tA), T1 = matFromTr(tB);
-	T0.R.c0 = normalizeA(T0.R.c0); T0.R.c1 = normalizeA(T0.R.c1); T0.R.c2 = normalizeA(T0.R.c2);
-	T1.R.c0 = normalizeA(T1.R.c0); T1.R.c1 = normalizeA(T1.R.c1); T1.R.c2 = normalizeA(T1.R.c2);
-	PC mc[MAXC];
-	int num = 0;
-	if(!boxBoxGenerate(e0, e1, T0, T1, cDist, mc, num)) return false;
-	Manifold m;
-	if(num > 0)
+	const int initial = m.num;
+	refreshManifold(m, aToB, minMargin * 0.8f);
+	const bool lost = m.num != initial;
+	const float radiusA = sqrtf(dotA(e0, e0)), radiusB = sqrtf(dotA(e1, e1));
+	if(lost || invalidateBoxConvex(m, cur, tA.q, tB.q, minMargin, radiusA, radiusB))
 	{
-		addBatch(m, mc, num, tolLen);
-		const V3 wn = normalizeA(mtRotate(T1, m.pts[0].n));
-		for(int i = 0; i < m.num; i++) out.add(mtTransform(T1, m.pts[i].b), wn, m.pts[i].pen);
+		m.rel = cur;
+		m.quatA = tA.q;
+		m.quatB = tB.q;
+		MatTr T0 = matFromTr(tA), T1 = matFromTr(tB);
+		T0.R.c0 = normalizeA(T0.R.c0); T0.R.c1 = normalizeA(T0.R.c1); T0.R.c2 = normalizeA(T0.R.c2);
+		T1.R.c0 = normalizeA(T1.R.c0); T1.R.c1 = normalizeA(T1.R.c1); T1.R.c2 = normalizeA(T1.R.c2);
+		PC mc[MAXC];
+		int num = 0;
+		if(!boxBoxGenerate(e0, e1, T0, T1, cDist, mc, num)) return false;
+		if(num > 0)
+		{
+			addBatch(m, mc, num, tolLen);
+			const V3 wn = normalizeA(mtRotate(T1, m.pts[0].n));
+			for(int i = 0; i < m.num; i++) out.add(mtTransform(T1, m.pts[i].b), wn, m.pts[i].pen);
+			return true;
+		}
+		// Edge-edge configuration: GJK / EPA between the core boxes
+		// (GuPCMContactBoxBox.cpp:917-957), one point added to the manifold.
+		const GjkConvex ca = makeRelativeBox(e0, aToB);
+		const GjkConvex cb = makeBox(e1);
+		GjkOut g;
+		int status = gjkPenetration(ca, cb, aToB.p, cDist, g);   // the warm start is cleared first
+		keepWarmStart(m, g);
+		if(status == EPA_CONTACT) status = epaPenetration(ca, cb, g, tolLen, g);
+		if(status != GJK_CONTACT && status != EPA_CONTACT) return false;
+		PC c;
+		c.a = mtTransformInv(aToB, g.closestA);
+		c.b = g.closestB;
+		c.n = g.normal;
+		c.pen = g.penDep;
+		addPoint4(m, c, minMargin * 0.05f);
+		const V3 wn = normalizeA(qRotate(tB.q, g.normal));
+		outputWithOffset(m, wn, tB, cDist, out);
 		return true;
 	}
-	// Edge-edge configuration: GJK / EPA between the core boxes
-	// (GuPCMContactBoxBox.cpp:917-957), producing a single point.
-	const MatTr aToB = matFromTr(cur);
-	const GjkConvex ca = makeRelativeBox(e0, aToB);
-	const GjkConvex cb = makeBox(e1);
-	GjkOut g;
-	int status = gjkPenetration(ca, cb, aToB.p, cDist, g);
-	if(status == EPA_CONTACT) status = epaPenetration(ca, cb, g, tolLen, g);
-	if(status != GJK_CONTACT && status != EPA_CONTACT) return false;
-	PC c;
-	c.a = mtTransformInv(aToB, g.closestA);
-	c.b = g.closestB;
-	c.n = g.normal;
-	c.pen = g.penDep;
-	m.pts[0] = c;
-	m.num = 1;
-	const V3 wn = normalizeA(qRotate(tB.q, g.normal));
-	outputWithOffset(m, wn, tB, cDist, out);
-	(void)minMargin;
-	return true;
+	if(m.num > 0)
+	{
+		outputWithOffset(m, manifoldWorldNormal(m, tB), tB, cDist, out);
+		return true;
+	}
+	return false;
 }
 
 // ----------------------------------------------------------------- capsule-box
-// pcmContactCapsuleBox with a fresh manifold (GuPCMContactCapsuleBox.cpp:73)
-static __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Buffer& out)
+// pcmContactCapsuleBox (GuPCMContactCapsuleBox.cpp:73)
+static __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, const Tr& tBox, float cDist, float tolLen, Manifold& m, Buffer& out)
 {
 	const Tr cur = trInvMul(tBox, tCap);
 	const MatTr aToB = matFromTr(cur);
-	const V3 axis = mtRotate(aToB, scale(unitX(), hh));
-	const V3 p0 = add(aToB.p, axis), p1 = sub(aToB.p, axis);
-	const GjkConvex cap = makeCapsule(p0, p1, r);
-	const GjkConvex box = makeBox(ext);
-	// the reference seeds the search with the capsule centre minus the box's world position
-	const V3 initialDir = sub(aToB.p, tBox.p);
-	GjkOut g;
-	int status = gjkPenetration(cap, box, initialDir, cDist, g);
-	if(status == GJK_NON_INTERSECT) return false;
-	PC mc[MAXC];
-	int num = 0;
-	bool overlapTest = false;
-	if(status == GJK_DEGENERATE)
-		overlapTest = true;
-	else if(status == GJK_CONTACT)
+	const int initial = m.num;
+	const float margin = boxMargin(ext, tolLen);
+	const float minMargin = fmin_(margin, r);
+	refreshManifold(m, aToB, minMargin * 0.8f);
+	const bool lost = m.num != initial;
+	if(lost || invalidateSphereCapsule(m, cur, minMargin))
 	{
-		mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
-	}
-	else
-	{
-		status = epaPenetration(cap, box, g, tolLen, g);
-		if(status == EPA_CONTACT)
-		{
-			mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
-		}
-		else
+		m.rel = cur;
+		const V3 axis = mtRotate(aToB, scale(unitX(), hh));
+		const V3 p0 = add(aToB.p, axis), p1 = sub(aToB.p, axis);
+		const GjkConvex cap = makeCapsule(p0, p1, r);
+		const GjkConvex box = makeBox(ext);
+		// the reference seeds the search with the capsule centre minus the box's world position
+		const V3 initialDir = sub(aToB.p, tBox.p);
+		GjkOut g;
+		int status = gjkPenetration(cap, box, initialDir, cDist, g, m.warmA, m.warmB, m.warmSize);
+		keepWarmStart(m, g);
+		if(status == GJK_NON_INTERSECT) return false;
+		PC mc[MAXC];
+		int num = 0;
+		bool overlapTest = false;
+		bool full = true;
+		if(status == GJK_DEGENERATE)
 			overlapTest = true;
+		else
+		{
+			if(status == GJK_CONTACT)
+			{
+				mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+			}
+			else
+			{
+				status = epaPenetration(cap, box, g, tolLen, g);
+				if(status == EPA_CONTACT)
+				{
+					mc[num].a = mtTransformInv(aToB, g.closestA); mc[num].b = g.closestB; mc[num].n = g.normal; mc[num].pen = g.penDep; num++;
+				}
+				else
+					overlapTest = true;
+			}
+			full = initial == 0 || lost || overlapTest;
+		}
+		if(!full)
+		{
+			// a GJK / EPA point added to the existing manifold
+			PC c;
+			c.a = trTransformInv(cur, g.closestA);
+			c.b = g.closestB;
+			c.n = g.normal;
+			c.pen = g.penDep;
+			addPoint2(m, c, minMargin * 0.1f);
+			const V3 wn = qRotate(tBox.q, g.normal);
+			outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
+			return true;
+		}
+		// fullContactsGenerationCapsuleBox (GuPCMContactCapsuleBox.cpp:43)
+		V3 normal = g.normal;
+		const int orig = num;
+		if(!capsuleBoxFull(p0, p1, r, ext, aToB, mc, num, cDist, normal, g.closestB, box.margin, overlapTest, tolLen)) return false;
+		int first = 0;
+		if(orig != 0 && num != orig) { num--; first = 1; }
+		addBatch2(m, mc + first, num);
+		const V3 wn = qRotate(tBox.q, normal);
+		outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
+		return true;
 	}
-	// fullContactsGenerationCapsuleBox (GuPCMContactCapsuleBox.cpp:43)
-	V3 normal = g.normal;
-	const int orig = num;
-	if(!capsuleBoxFull(p0, p1, r, ext, aToB, mc, num, cDist, normal, g.closestB, box.margin, overlapTest, tolLen)) return false;
-	int first = 0;
-	if(orig != 0 && num != orig) { num--; first = 1; }
-	Manifold m;
-	addBatch2(m, mc + first, num);
-	const V3 wn = qRotate(tBox.q, normal);
-	outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
-	return true;
+	if(m.num > 0)
+	{
+		const V3 wn = manifoldWorldNormal(m, tBox);
+		outputCapsuleLike(m, wn, wn, tCap, r, cDist, out);
+		return true;
+	}
+	return false;
 }
 
-static __device__ int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Buffer& out)
+// One pair (types in the reference's table order, t0 <= t1).  m: the pair's
+// persistent manifold, read and updated by the cached kinds (plane-capsule,
+// plane-box, capsule-box, box-box: gEnablePCMCaching, PxsContext.cpp:89).
+static __device__ int generate(int t0, const float* g0, int t1, const float* g1, const Tr& p0, const Tr& p1, float cDist, float tolLen, Manifold& m, Buffer& out)
 {
 	switch(t0 * 4 + t1)
 	{
@@ -1011,14 +1298,80 @@ static __device__ int generate(int t0, const float* g0, int t1, const float* g1,
 	case SPHERE * 4 + PLANE: spherePlane(g0[0], p0, p1, cDist, out); break;
 	case SPHERE * 4 + CAPSULE: sphereCapsule(g0[0], g1[0], g1[1], p0, p1, cDist, out); break;
 	case SPHERE * 4 + BOX: sphereBox(g0[0], v3(g1[0], g1[1], g1[2]), p0, p1, cDist, out); break;
-	case PLANE * 4 + CAPSULE: planeCapsule(g1[0], g1[1], p0, p1, cDist, out); break;
-	case PLANE * 4 + BOX: planeBox(v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, out); break;
+	case PLANE * 4 + CAPSULE: planeCapsule(g1[0], g1[1], p0, p1, cDist, m, out); break;
+	case PLANE * 4 + BOX: planeBox(v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, m, out); break;
 	case CAPSULE * 4 + CAPSULE: capsuleCapsule(g0[0], g0[1], g1[0], g1[1], p0, p1, cDist, out); break;
-	case CAPSULE * 4 + BOX: capsuleBox(g0[0], g0[1], v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, out); break;
-	case BOX * 4 + BOX: boxBox(v3(g0[0], g0[1], g0[2]), v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, out); break;
+	case CAPSULE * 4 + BOX: capsuleBox(g0[0], g0[1], v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, m, out); break;
+	case BOX * 4 + BOX: boxBox(v3(g0[0], g0[1], g0[2]), v3(g1[0], g1[1], g1[2]), p0, p1, cDist, tolLen, m, out); break;
 	default: break;  // plane-plane: no contact generation in the reference table
 	}
 	return out.count;
+}
+
+// One pair's persistent contact manifold between calls (the state a PxCache
+// carries for the cached pair kinds), 288 bytes: relative transform (q, p),
+// both bodies' orientations, point count, a flag (0 = fresh cache), the GJK
+// warm start and up to four points (local point on A, local point on B, local
+// normal, penetration).
+struct __align__(16) ManifoldRecord
+{
+	float relQ[4], relP[4], quatA[4], quatB[4];
+	uint32_t num, used, warmSize, pad;
+	float pts[4][12];
+	uint8_t warmA[4], warmB[4];
+	uint32_t pad2[2];
+};
+static_assert(sizeof(ManifoldRecord) == 288, "manifold record layout");
+
+// does the pair kind (types ordered t0 <= t1) keep a manifold between frames
+// (gEnablePCMCaching, physx/source/lowlevel/software/src/PxsContext.cpp:89)
+static __device__ __forceinline__ bool cachedKind(int t0, int t1)
+{
+	return (t0 == PLANE && (t1 == CAPSULE || t1 == BOX)) || (t0 == CAPSULE && t1 == BOX) || (t0 == BOX && t1 == BOX);
+}
+
+static __device__ void loadManifold(const ManifoldRecord& r, Manifold& m)
+{
+	if(!r.used) { m = Manifold(); return; }
+	m.rel.q.x = r.relQ[0]; m.rel.q.y = r.relQ[1]; m.rel.q.z = r.relQ[2]; m.rel.q.w = r.relQ[3];
+	m.rel.p = v3(r.relP[0], r.relP[1], r.relP[2]);
+	m.quatA.x = r.quatA[0]; m.quatA.y = r.quatA[1]; m.quatA.z = r.quatA[2]; m.quatA.w = r.quatA[3];
+	m.quatB.x = r.quatB[0]; m.quatB.y = r.quatB[1]; m.quatB.z = r.quatB[2]; m.quatB.w = r.quatB[3];
+	m.num = int(r.num);
+	m.warmSize = int(r.warmSize);
+	for(int i = 0; i < 4; i++) { m.warmA[i] = r.warmA[i]; m.warmB[i] = r.warmB[i]; }
+	for(int i = 0; i < m.num; i++)
+	{
+		const float* f = r.pts[i];
+		m.pts[i].a = v3(f[0], f[1], f[2]);
+		m.pts[i].b = v3(f[4], f[5], f[6]);
+		m.pts[i].n = v3(f[8], f[9], f[10]);
+		m.pts[i].pen = f[11];
+	}
+}
+
+static __device__ void storeManifold(const Manifold& m, ManifoldRecord& r)
+{
+	r.relQ[0] = m.rel.q.x; r.relQ[1] = m.rel.q.y; r.relQ[2] = m.rel.q.z; r.relQ[3] = m.rel.q.w;
+	r.relP[0] = m.rel.p.x; r.relP[1] = m.rel.p.y; r.relP[2] = m.rel.p.z; r.relP[3] = 0.0f;
+	r.quatA[0] = m.quatA.x; r.quatA[1] = m.quatA.y; r.quatA[2] = m.quatA.z; r.quatA[3] = m.quatA.w;
+	r.quatB[0] = m.quatB.x; r.quatB[1] = m.quatB.y; r.quatB[2] = m.quatB.z; r.quatB[3] = m.quatB.w;
+	r.num = uint32_t(m.num);
+	r.used = 1;
+	r.warmSize = uint32_t(m.warmSize);
+	r.pad = 0;
+	for(int i = 0; i < 4; i++)
+	{
+		r.warmA[i] = i < m.warmSize ? uint8_t(m.warmA[i]) : 0;
+		r.warmB[i] = i < m.warmSize ? uint8_t(m.warmB[i]) : 0;
+	}
+	for(int i = 0; i < m.num; i++)
+	{
+		float* f = r.pts[i];
+		f[0] = m.pts[i].a.x; f[1] = m.pts[i].a.y; f[2] = m.pts[i].a.z; f[3] = 0.0f;
+		f[4] = m.pts[i].b.x; f[5] = m.pts[i].b.y; f[6] = m.pts[i].b.z; f[7] = 0.0f;
+		f[8] = m.pts[i].n.x; f[9] = m.pts[i].n.y; f[10] = m.pts[i].n.z; f[11] = m.pts[i].pen;
+	}
 }
 
 static __device__ Tr loadTr(const float* p)

@@ -314,8 +314,13 @@ struct GjkOut
 	int warmSize;
 };
 
-// gjkPenetration, takeCoreShape = true, no warm start (GuGJKPenetration.h:88)
-static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkConvex& b, V3 initialDir, float contactDist, GjkOut& out)
+// gjkPenetration, takeCoreShape = true (GuGJKPenetration.h:88).  warmA/warmB/
+// warmSize: the simplex vertex indices kept from the pair's previous call
+// (the manifold's warm start), 0 for none.  Every exit records the final
+// simplex's indices in out (assignWarmStartValue), the degenerate exit one
+// vertex fewer.
+static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkConvex& b, V3 initialDir, float contactDist, GjkOut& out,
+                                 const int* warmA = nullptr, const int* warmB = nullptr, int warmSize = 0)
 {
 	const float minMargin = fmin_(a.minMargin, b.minMargin);
 	const float eps = minMargin * 0.1f;
@@ -328,8 +333,36 @@ static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkC
 	bool notTerminated = true, notDegenerated = true;
 	Simplex s;
 	s.size = 0;
-	V3 closest = dotA(initialDir, initialDir) > 0.0f ? initialDir : unitX();
-	V3 v = normalizeA(closest);
+	V3 closest, v;
+	auto record = [&](int n) {
+		out.warmSize = n;
+		for(int i = 0; i < n; i++) { out.aInd[i] = s.aInd[i]; out.bInd[i] = s.bInd[i]; }
+	};
+	if(warmSize != 0)
+	{
+		V3 support = zero3();
+		for(int i = 0; i < warmSize; i++)
+		{
+			s.aInd[i] = warmA[i];
+			s.bInd[i] = warmB[i];
+			const V3 sa = a.supportPoint(warmA[i]), sb = b.supportPoint(warmB[i]);
+			support = sub(sa, sb);
+			s.A[s.size] = sa;
+			s.B[s.size] = sb;
+			s.Q[s.size++] = support;
+		}
+		closest = gjkDoSimplex(s, support);
+		dist = sqrtf(dotA(closest, closest));
+		v = scaleInv(closest, dist);
+		prevDist = dist;
+		prevClos = closest;
+		notTerminated = dist > eps;
+	}
+	else
+	{
+		closest = dotA(initialDir, initialDir) > 0.0f ? initialDir : unitX();
+		v = normalizeA(closest);
+	}
 	// The distance strictly decreases every iteration over a finite set of
 	// support points, so the loop ends; the cap only bounds pathological input.
 	for(int iter = 0; notTerminated; iter++)
@@ -345,11 +378,18 @@ static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkC
 		int ia, ib;
 		const V3 sa = a.support(neg(closest), ia);
 		const V3 sb = b.support(closest, ib);
+		s.aInd[s.size] = ia;
+		s.bInd[s.size] = ib;
 		const V3 support = sub(sa, sb);
 		const float vw = dotA(v, support);
-		if(vw > sumExpandedMargin) return GJK_NON_INTERSECT;
+		if(vw > sumExpandedMargin)
+		{
+			record(s.size);
+			return GJK_NON_INTERSECT;
+		}
 		if(vw > dist * relDif)
 		{
+			record(s.size);
 			out.normal = v;
 			gjkClosestPoints(s, closest, out.closestA, out.closestB, s.size);
 			out.penDep = dist;
@@ -357,8 +397,6 @@ static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkC
 		}
 		s.A[s.size] = sa;
 		s.B[s.size] = sb;
-		s.aInd[s.size] = ia;
-		s.bInd[s.size] = ib;
 		s.Q[s.size++] = support;
 		closest = gjkDoSimplex(s, support);
 		dist = sqrtf(dotA(closest, closest));
@@ -368,6 +406,7 @@ static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkC
 	}
 	if(!notDegenerated)
 	{
+		record(s.size - 1);
 		V3 ca = zero3(), cb = zero3();
 		gjkClosestPoints(s, prevClos, ca, cb, s.size);
 		out.normal = scaleInv(prevClos, prevDist);
@@ -376,8 +415,7 @@ static __device__ __noinline__ int gjkPenetration(const GjkConvex& a, const GjkC
 		out.penDep = prevDist;
 		return GJK_DEGENERATE;
 	}
-	out.warmSize = s.size;
-	for(int i = 0; i < s.size; i++) { out.aInd[i] = s.aInd[i]; out.bInd[i] = s.bInd[i]; }
+	record(s.size);
 	return EPA_CONTACT;
 }
 

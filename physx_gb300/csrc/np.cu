@@ -1,7 +1,7 @@
 // Narrowphase for the GB300 rigid-body step: immediate::PxGenerateContacts
 // (physx/include/PxImmediateMode.h:267, physx/source/immediatemode/src/NpImmediateMode.cpp:732)
-// over a batch of sphere / plane / capsule / box pairs, with fresh-cache
-// semantics (the persistent manifold is regenerated for every call).
+// over a batch of sphere / plane / capsule / box pairs, with fresh caches or
+// with each pair's persistent contact manifold carried between calls.
 //
 // GB300 layout: the batch is bucketed by (type0, type1) with a 16-bin counting
 // pass so every warp runs a single generator (no divergence between pair
@@ -63,8 +63,10 @@ __global__ void bucketScatterKernel(PairRef pr, uint32_t n, uint32_t* __restrict
 }
 
 // One lane per pair (in bucket order).  out: n x 4 contacts x 2 float4.
+// manifolds: per pair, the persistent manifold read and updated (null: fresh caches).
 __global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t* __restrict__ perm, uint32_t n, float contactDistance,
-                                                      float toleranceLength, float4* __restrict__ out, uint32_t* __restrict__ counts)
+                                                      float toleranceLength, float4* __restrict__ out, uint32_t* __restrict__ counts,
+                                                      ManifoldRecord* __restrict__ manifolds)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= n) return;
@@ -82,7 +84,11 @@ __global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t
 		const Tr t2 = pa; pa = pb; pb = t2;
 	}
 	Buffer buf;
-	generate(ta, ga, tb, gb, pa, pb, contactDistance, toleranceLength, buf);
+	Manifold m;
+	const bool cached = manifolds && cachedKind(ta, tb);
+	if(cached) loadManifold(manifolds[i], m);
+	generate(ta, ga, tb, gb, pa, pb, contactDistance, toleranceLength, m, buf);
+	if(cached) storeManifold(m, manifolds[i]);
 	counts[i] = uint32_t(buf.count);
 	float4* o = out + size_t(i) * 8;
 	for(int c = 0; c < buf.count; c++)
@@ -103,6 +109,7 @@ struct NpWorkspace
 	DevBuf<float> g0, g1, p0, p1;
 	DevBuf<uint32_t> hist, perm, counts;
 	DevBuf<float4> out;
+	DevBuf<np::ManifoldRecord> manifolds;
 	HostBuf<float4> hOut;
 	HostBuf<uint32_t> hCounts;
 	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
@@ -127,11 +134,10 @@ using namespace gbpx;
 // floats per shape, poses 7 floats, contacts 8 floats (normal, separation,
 // point, 0) with maxPerPair slots per pair.  Returns GBPX_ERR_CAPACITY if a
 // pair produced more than maxPerPair contacts (counts are still exact).
-GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
-                                    const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
-                                    float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts)
+static int generateContactsHost(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0, const float* pose1,
+                                uint32_t nbPairs, float contactDistance, float toleranceLength, float* outContacts, uint32_t maxPerPair,
+                                uint32_t* outCounts, void* manifolds)
 {
-	(void)meshContactMargin;
 	if(!nbPairs) return GBPX_OK;
 	if(!type0 || !geom0 || !type1 || !geom1 || !pose0 || !pose1 || !outContacts || !outCounts || !maxPerPair) return GBPX_ERR_INVALID;
 	if(!(contactDistance > 0.0f) || !(toleranceLength > 0.0f)) return GBPX_ERR_INVALID;
@@ -142,7 +148,7 @@ GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const 
 	const size_t n = nbPairs;
 	if(ws->t0.reserve(n) || ws->t1.reserve(n) || ws->g0.reserve(4 * n) || ws->g1.reserve(4 * n) || ws->p0.reserve(7 * n) ||
 	   ws->p1.reserve(7 * n) || ws->hist.reserve(32) || ws->perm.reserve(n) || ws->counts.reserve(n) || ws->out.reserve(8 * n) ||
-	   ws->hOut.reserve(8 * n) || ws->hCounts.reserve(n))
+	   ws->hOut.reserve(8 * n) || ws->hCounts.reserve(n) || (manifolds && ws->manifolds.reserve(n)))
 		return GBPX_ERR_NOMEM;
 	cudaStream_t s = ws->stream;
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->t0.ptr, type0, n * 4, cudaMemcpyHostToDevice, s));
@@ -157,8 +163,11 @@ GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const 
 	np::bucketCountKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr);
 	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(ws->hist.ptr);
 	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr + 16, ws->perm.ptr);
-	np::generateKernel<<<divUp(n, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPairs, contactDistance, toleranceLength, ws->out.ptr, ws->counts.ptr);
+	if(manifolds) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->manifolds.ptr, manifolds, n * sizeof(np::ManifoldRecord), cudaMemcpyHostToDevice, s));
+	np::generateKernel<<<divUp(n, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPairs, contactDistance, toleranceLength, ws->out.ptr, ws->counts.ptr,
+	                                                 manifolds ? ws->manifolds.ptr : nullptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
+	if(manifolds) GBPX_CUDA_TRY(cudaMemcpyAsync(manifolds, ws->manifolds.ptr, n * sizeof(np::ManifoldRecord), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->hCounts.ptr, ws->counts.ptr, n * 4, cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->hOut.ptr, ws->out.ptr, n * 8 * sizeof(float4), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
@@ -172,6 +181,29 @@ GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const 
 		memcpy(outContacts + i * maxPerPair * 8, ws->hOut.ptr + i * 8, size_t(m) * 8 * sizeof(float));
 	}
 	return rc;
+}
+
+GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                                    const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
+                                    float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts)
+{
+	(void)meshContactMargin;
+	return generateContactsHost(type0, geom0, type1, geom1, pose0, pose1, nbPairs, contactDistance, toleranceLength, outContacts, maxPerPair,
+	                            outCounts, nullptr);
+}
+
+// PxGenerateContacts with persistent caches: manifolds (nbPairs x 288 bytes,
+// host memory, all zero for a fresh cache) carries each pair's contact
+// manifold from one call to the next, as PxCache does for the plane-capsule,
+// plane-box, capsule-box and box-box pairs; it is read and updated.
+GBPX_API int gbpx_generate_contacts_cached(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0,
+                                           const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
+                                           float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts, void* manifolds)
+{
+	(void)meshContactMargin;
+	if(nbPairs && !manifolds) return GBPX_ERR_INVALID;
+	return generateContactsHost(type0, geom0, type1, geom1, pose0, pose1, nbPairs, contactDistance, toleranceLength, outContacts, maxPerPair,
+	                            outCounts, manifolds);
 }
 
 // ------------------------------------------------------------------ no-allocation variant
@@ -232,7 +264,7 @@ GBPX_API int gbpx_generate_contacts_device_noalloc(const int* dType0, const floa
 	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(scratch);
 	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch + 16, scratch + 32);
 	np::generateKernel<<<divUp(nbPairs, 128), 128, 0, s>>>(pr, scratch + 32, nbPairs, contactDistance, toleranceLength,
-	                                                        reinterpret_cast<float4*>(dOutContacts), dOutCounts);
+	                                                        reinterpret_cast<float4*>(dOutContacts), dOutCounts, nullptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	return GBPX_OK;
 }

@@ -168,22 +168,96 @@ __device__ __forceinline__ void constructStaticBody(const Tr& pose, BodyVel& vel
 	copyToSolverBody(zero3(), zero3(), 0.0f, zero3(), pose, -FLT_MAX, FLT_MAX, FLT_MAX, true, vel, tx, data);
 }
 
-// ------------------------------------------------------------- friction correlation (fresh patches, <= 4 contacts)
+// ------------------------------------------------------------- persistent friction patches
+// FrictionPatch (lowleveldynamics/src/DyFrictionPatch.h:43): what a contact
+// constraint leaves for the next frame (frictionPtr / frictionCount) and
+// reads back then.  A pair of <= 4 contacts writes <= 4 patches.
+struct __align__(16) FrictionPatchDev
+{
+	V3 body0Normal; int broken;
+	V3 body1Normal; int anchorCount;
+	V3 body0Anchors[2];
+	V3 body1Anchors[2];
+	float staticFriction, dynamicFriction, restitution, pad;
+	Q relativeQuat;
+};
+static_assert(sizeof(FrictionPatchDev) == 112, "friction patch layout");
+struct __align__(16) FrictionState
+{
+	uint32_t count, pad[3];
+	FrictionPatchDev patches[MAX_CONTACTS];
+};
+
+// ------------------------------------------------------------- friction correlation (<= 4 contacts, <= 4 kept patches)
+constexpr int MAX_FPATCH = 2 * MAX_CONTACTS;   // last frame's patches, then this frame's
 struct Correlation
 {
 	int cpStart[MAX_CONTACTS], cpCount[MAX_CONTACTS], cpNext[MAX_CONTACTS];
 	float cpRest[MAX_CONTACTS], cpSF[MAX_CONTACTS], cpDF[MAX_CONTACTS];
 	V3 cpMin[MAX_CONTACTS], cpMax[MAX_CONTACTS];
 	int contactPatchCount;
-	V3 fpWorldNormal[MAX_CONTACTS];
-	V3 fpAnchor0[MAX_CONTACTS][2], fpAnchor1[MAX_CONTACTS][2];
-	int fpAnchorCount[MAX_CONTACTS];
-	float fpRest[MAX_CONTACTS], fpSF[MAX_CONTACTS], fpDF[MAX_CONTACTS];
-	int fpContactCount[MAX_CONTACTS];
-	V3 fpMin[MAX_CONTACTS], fpMax[MAX_CONTACTS];
-	int listHead[MAX_CONTACTS];
+	V3 fpWorldNormal[MAX_FPATCH];
+	V3 fpAnchor0[MAX_FPATCH][2], fpAnchor1[MAX_FPATCH][2];
+	int fpAnchorCount[MAX_FPATCH];
+	float fpRest[MAX_FPATCH], fpSF[MAX_FPATCH], fpDF[MAX_FPATCH];
+	int fpContactCount[MAX_FPATCH];
+	V3 fpMin[MAX_FPATCH], fpMax[MAX_FPATCH];
+	int listHead[MAX_FPATCH];
+	V3 fpN0[MAX_FPATCH], fpN1[MAX_FPATCH];   // body0Normal, body1Normal
+	Q fpQ[MAX_FPATCH];                       // relativeQuat
+	int fpBroken[MAX_FPATCH];
 	int frictionPatchCount;
+
+	__device__ void exportPatch(int i, FrictionPatchDev& o) const
+	{
+		o.body0Normal = fpN0[i]; o.body1Normal = fpN1[i];
+		o.broken = fpBroken[i]; o.anchorCount = fpAnchorCount[i];
+		o.body0Anchors[0] = fpAnchor0[i][0]; o.body0Anchors[1] = fpAnchor0[i][1];
+		o.body1Anchors[0] = fpAnchor1[i][0]; o.body1Anchors[1] = fpAnchor1[i][1];
+		o.staticFriction = fpSF[i]; o.dynamicFriction = fpDF[i]; o.restitution = fpRest[i]; o.pad = 0.0f;
+		o.relativeQuat = fpQ[i];
+	}
 };
+
+// getFrictionPatches (lowleveldynamics/src/DyContactPrepShared.h:73): last
+// frame's patches that are not broken, have anchors, still face each other and
+// whose anchors have not separated along the normal by the correlation
+// distance start the list, without contacts.
+__device__ __forceinline__ void getFrictionPatches(Correlation& c, const FrictionState* prev, const Tr& f0, const Tr& f1, float correlationDistance)
+{
+	c.frictionPatchCount = 0;
+	if(!prev) return;
+	const uint32_t count = prev->count < uint32_t(MAX_CONTACTS) ? prev->count : uint32_t(MAX_CONTACTS);
+	if(!count) return;
+	const Q qinv = qConj(f0.q);
+	const V3 b1to0p = qRotateS(qinv, sub(f1.p, f0.p));
+	const Q b1to0q = qMulS(qinv, f1.q);
+	for(uint32_t k = 0; k < count; k++)
+	{
+		const FrictionPatchDev patch = prev->patches[k];
+		if(patch.broken || patch.anchorCount == 0) continue;
+		if(!(dotS(patch.body0Normal, qRotateS(b1to0q, patch.body1Normal)) > 0.999f)) continue;
+		bool separated = false;
+		for(int a = 0; a < patch.anchorCount; a++)
+		{
+			const V3 p1in0 = add(qRotateS(b1to0q, patch.body1Anchors[a]), b1to0p);
+			if(!(fabsf(dotS(sub(patch.body0Anchors[a], p1in0), patch.body0Normal)) < correlationDistance)) { separated = true; break; }
+		}
+		if(separated) continue;
+		const int i = c.frictionPatchCount++;
+		c.fpWorldNormal[i] = qRotateS(f0.q, patch.body0Normal);
+		c.fpContactCount[i] = 0;
+		c.fpMin[i] = v3(FLT_MAX, FLT_MAX, FLT_MAX);
+		c.fpMax[i] = v3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+		c.listHead[i] = -1;
+		c.fpN0[i] = patch.body0Normal; c.fpN1[i] = patch.body1Normal;
+		c.fpBroken[i] = patch.broken; c.fpAnchorCount[i] = patch.anchorCount;
+		c.fpAnchor0[i][0] = patch.body0Anchors[0]; c.fpAnchor0[i][1] = patch.body0Anchors[1];
+		c.fpAnchor1[i][0] = patch.body1Anchors[0]; c.fpAnchor1[i][1] = patch.body1Anchors[1];
+		c.fpSF[i] = patch.staticFriction; c.fpDF[i] = patch.dynamicFriction; c.fpRest[i] = patch.restitution;
+		c.fpQ[i] = patch.relativeQuat;
+	}
+}
 
 __device__ __forceinline__ void createContactPatches(Correlation& c, const Contact* cb, int n, float tol)
 {
@@ -225,9 +299,9 @@ __device__ __forceinline__ void createContactPatches(Correlation& c, const Conta
 	c.contactPatchCount = pc;
 }
 
-__device__ __forceinline__ void correlatePatches(Correlation& c, const Contact* cb, float tol)
+__device__ __forceinline__ void correlatePatches(Correlation& c, const Contact* cb, const Tr& f0, const Tr& f1, float tol)
 {
-	int fpc = 0;
+	int fpc = c.frictionPatchCount;
 	for(int i = 0; i < c.contactPatchCount; i++)
 	{
 		const V3 n = cb[c.cpStart[i]].n;
@@ -237,6 +311,10 @@ __device__ __forceinline__ void correlatePatches(Correlation& c, const Contact* 
 		if(j == fpc)
 		{
 			c.fpAnchorCount[fpc] = 0;
+			c.fpBroken[fpc] = 0;
+			c.fpN0[fpc] = qRotateInvS(f0.q, n);
+			c.fpN1[fpc] = qRotateInvS(f1.q, n);
+			c.fpQ[fpc] = qMulS(qConj(f0.q), f1.q);
 			c.fpSF[fpc] = c.cpSF[i]; c.fpDF[fpc] = c.cpDF[i]; c.fpRest[fpc] = c.cpRest[i];
 			c.fpWorldNormal[j] = n;
 			c.fpContactCount[fpc] = c.cpCount[i];
@@ -263,11 +341,20 @@ __device__ __forceinline__ void growPatches(Correlation& c, const Contact* cb, c
 {
 	for(int i = 0; i < c.frictionPatchCount; i++)
 	{
-		// fresh patches: anchorCount == 0 and the list is non-empty
+		// a kept patch with two well-spread anchors, or one without contacts,
+		// stays as it is (DyFrictionCorrelation.cpp:198-210)
+		if(c.fpAnchorCount[i] == 2 || c.listHead[i] == -1)
+		{
+			const float diag = lenSqS(sub(c.fpMax[i], c.fpMin[i]));
+			const float an = lenSqS(sub(c.fpAnchor0[i][0], c.fpAnchor0[i][1]));
+			if(c.fpContactCount[i] == 0 || (an * 4.0f) >= diag) continue;
+			c.fpAnchorCount[i] = 0;
+		}
 		V3 wa[2];
 		int ac = 0;
 		float pointDistSq = 0.0f, d0, d1;
 		const float eps = 1e-8f;
+		if(c.fpAnchorCount[i] == 1) wa[ac++] = trTransformS(f0, c.fpAnchor0[i][0]);   // a kept anchor stays
 		for(int patch = c.listHead[i]; patch != -1; patch = c.cpNext[patch])
 		{
 			for(int j = 0; j < c.cpCount[patch]; j++)
@@ -294,7 +381,7 @@ __device__ __forceinline__ void growPatches(Correlation& c, const Contact* cb, c
 				}
 			}
 		}
-		for(int j = 0; j < ac; j++)
+		for(int j = c.fpAnchorCount[i]; j < ac; j++)
 		{
 			c.fpAnchor0[i][j] = trTransformInvS(f0, wa[j]);
 			c.fpAnchor1[i][j] = trTransformInvS(f1, wa[j]);
@@ -307,7 +394,7 @@ __device__ __forceinline__ void growPatches(Correlation& c, const Contact* cb, c
 // ------------------------------------------------------------- rows
 struct PrepParams
 {
-	float invStepDt, invTotalDt, totalDt, stepDt, bounceThreshold, frictionOffsetThreshold, biasCoefficient;
+	float invStepDt, invTotalDt, totalDt, stepDt, bounceThreshold, frictionOffsetThreshold, biasCoefficient, correlationDistance;
 };
 
 __device__ __forceinline__ float constructPoint(const M33& s0, const M33& s1, float imn0, float imn1, V3 p0, V3 p1, V3 n, float nv0, float nv1,
@@ -348,19 +435,24 @@ __device__ __forceinline__ float constructPoint(const M33& s0, const M33& s1, fl
 	return penetration;
 }
 
-// Builds one constraint's rows (createFinalizeSolverContactsStep with fresh friction).
+// Builds one constraint's rows (createFinalizeSolverContactsStep).  prev: the
+// friction patches the pair left last frame (null: fresh friction data);
+// written (may be null): the patches it leaves this frame, in patch order.
 __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbContacts, int a, int b, const BodyVel& va, const BodyVel& vb,
                                                const BodyTx& ta, const BodyTx& tb, const BodyData& d0, const BodyData& d1, const Tr& f0,
-                                               const Tr& f1, const PrepParams& pp, ConstraintRecord& rec)
+                                               const Tr& f1, const PrepParams& pp, ConstraintRecord& rec, const FrictionState* prev = nullptr,
+                                               FrictionState* written = nullptr)
 {
 	rec.bodyA = a;
 	rec.bodyB = b;
 	rec.nbPatches = 0;
 	rec.counts = 0;
+	if(written) written->count = 0;
 	if(nbContacts == 0) return;
 	Correlation c;
+	getFrictionPatches(c, prev, f0, f1, pp.correlationDistance);
 	createContactPatches(c, contacts, nbContacts, 0.999f);
-	correlatePatches(c, contacts, 0.999f);
+	correlatePatches(c, contacts, f0, f1, 0.999f);
 	growPatches(c, contacts, f0, f1, pp.frictionOffsetThreshold + 0.0f);
 
 	// row counts first: the rows are packed in this order
@@ -465,7 +557,9 @@ __device__ __forceinline__ void prepConstraint(const Contact* contacts, int nbCo
 				}
 			}
 		}
+		if(written) c.exportPatch(i, written->patches[patchOut]);
 		patchOut++;
+		if(written) written->count = uint32_t(patchOut);
 	}
 }
 
@@ -501,17 +595,35 @@ __device__ __forceinline__ V3 qRotate4V(Q q, V3 v)
 // index is 0, so the block solve does not store body B.
 __device__ __forceinline__ void prepConstraintBlock(const Contact* contacts, int nbContacts, int a, int b, const BodyVel& va, const BodyVel& vb,
                                                     const BodyTx& ta, const BodyTx& tb, const BodyData& d0, const BodyData& d1, const Tr& f0,
-                                                    const Tr& f1, const PrepParams& pp, bool blockDynamic, bool keepB, ConstraintRecord& rec)
+                                                    const Tr& f1, const PrepParams& pp, bool blockDynamic, bool keepB, ConstraintRecord& rec,
+                                                    const FrictionState* prev = nullptr, FrictionState* written = nullptr)
 {
 	rec.bodyA = a;
 	rec.bodyB = b;
 	rec.nbPatches = 0;
 	rec.counts = REC_BLOCK | (keepB ? REC_KEEP_B : 0);
+	if(written) written->count = 0;
 	if(nbContacts == 0) return;
 	Correlation c;
+	getFrictionPatches(c, prev, f0, f1, pp.correlationDistance);
 	createContactPatches(c, contacts, nbContacts, 0.999f);
-	correlatePatches(c, contacts, 0.999f);
+	correlatePatches(c, contacts, f0, f1, 0.999f);
 	growPatches(c, contacts, f0, f1, pp.frictionOffsetThreshold + 0.0f);
+	// The block path then drops the patches that received no contact
+	// (createFinalizeSolverContacts4Step, DyTGSContactPrepBlock.cpp:1452-1466)
+	// by moving the later list heads and contact counts down -- not the
+	// patches themselves, so a later patch's contacts pair with an earlier
+	// patch's anchors, and the earlier patches are the ones written out.
+	for(int p = c.frictionPatchCount; p > 0; --p)
+		if(c.listHead[p - 1] == -1)
+		{
+			for(int p2 = p; p2 < c.frictionPatchCount; ++p2)
+			{
+				c.listHead[p2 - 1] = c.listHead[p2];
+				c.fpContactCount[p2 - 1] = c.fpContactCount[p2];
+			}
+			c.frictionPatchCount--;
+		}
 
 	int usedPatches = 0, totalPoints = 0, totalFriction = 0;
 	for(int i = 0; i < c.frictionPatchCount; i++)
@@ -647,7 +759,9 @@ __device__ __forceinline__ void prepConstraintBlock(const Contact* contacts, int
 				}
 			}
 		}
+		if(written) c.exportPatch(i, written->patches[patchOut]);
 		patchOut++;
+		if(written) written->count = uint32_t(patchOut);
 	}
 }
 
@@ -655,7 +769,11 @@ __device__ __forceinline__ void prepConstraintBlock(const Contact* contacts, int
 // solveContact (DyTGSContactPrep.cpp:1581) for one constraint.  b0/b1 are the
 // constraint's two bodies (b1 may be a static/kinematic body, never written
 // back when it is not dynamic: its invMass and sqrtInvInertia are zero).
-__device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+// brokenMask (may be null): bit p set when patch p's friction was clamped in
+// this solve (the header's broken flag, written back to the patch's friction
+// data after the last iteration).
+__device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed,
+                                                uint32_t* brokenMask = nullptr)
 {
 	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
 	const V3 angM0 = b0.dAng, angM1 = b1.dAng;
@@ -705,6 +823,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 			const float maxF = pr.staticFriction * accumulated;
 			const float maxDynF = pr.dynamicFriction * accumulated;
 			const int pairs = pr.nbFriction & 6;
+			bool broken = false;
 			for(int i = 0; i < pairs; i += 2)
 			{
 				const int k0 = pr.frictionStart + i, k1 = k0 + 1;
@@ -729,6 +848,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 				const float ti1 = tmp11 - nvel1 * f1.velMultiplier;
 				const float total = sqrtf(ti0 * ti0 + ti1 * ti1);
 				const bool clamp = total > fs * maxF;
+				broken = broken || clamp;
 				const float totalClamped = clamp ? fmin_(fs * maxDynF, total) : total;
 				const float ratio = total > 0.0f ? totalClamped / total : 0.0f;
 				const float nf0 = ti0 * ratio, nf1 = ti1 * ratio;
@@ -740,6 +860,7 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 				frictionForce[k0] = nf0;
 				frictionForce[k1] = nf1;
 			}
+			if(brokenMask && broken) *brokenMask |= 1u << p;
 		}
 	}
 	b0.lin = lin0;
@@ -757,7 +878,8 @@ __device__ __forceinline__ void solveConstraint(ConstraintRecord& rec, BodyVel& 
 // coefficients and a 1e-5 allowance on the static bound, and once an anchor
 // pair of a patch exceeds that bound the rest of the patch is clamped to the
 // dynamic bound as well.
-__device__ __forceinline__ void solveConstraintBlock(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+__device__ __forceinline__ void solveConstraintBlock(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed,
+                                                     uint32_t* brokenMask = nullptr)
 {
 	V3 lin0 = b0.lin, lin1 = b1.lin, ang0 = b0.ang, ang1 = b1.ang;
 	const V3 angD0v = b0.dAng, angD1v = b1.dAng;
@@ -832,6 +954,7 @@ __device__ __forceinline__ void solveConstraintBlock(ConstraintRecord& rec, Body
 				ang0 = add(scale(f0.raXnI, df0 * 1.0f), add(scale(f1.raXnI, df1 * 1.0f), ang0));
 				ang1 = sub(sub(ang1, scale(f1.rbXnI, df1 * 1.0f)), scale(f0.rbXnI, df0 * 1.0f));
 			}
+			if(brokenMask && broken) *brokenMask |= 1u << p;
 		}
 	}
 	b0.lin = lin0;
@@ -844,10 +967,29 @@ __device__ __forceinline__ void solveConstraintBlock(ConstraintRecord& rec, Body
 }
 
 // The solve of a constraint record by the path that built it.
-__device__ __forceinline__ void solveRecord(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed)
+__device__ __forceinline__ void solveRecord(ConstraintRecord& rec, BodyVel& b0, BodyVel& b1, bool writeB1, float minPen, float elapsed,
+                                            uint32_t* brokenMask = nullptr)
 {
-	if(rec.isBlock()) solveConstraintBlock(rec, b0, b1, writeB1, minPen, elapsed);
-	else solveConstraint(rec, b0, b1, writeB1, minPen, elapsed);
+	if(rec.isBlock()) solveConstraintBlock(rec, b0, b1, writeB1, minPen, elapsed, brokenMask);
+	else solveConstraint(rec, b0, b1, writeB1, minPen, elapsed, brokenMask);
+}
+
+// The written friction patch that receives patch p's broken flag.  Per pair
+// (single path) it is patch p itself.  A block lane's write-back address
+// advances only for the header's patch rows that had friction in any of the
+// four lanes (DyTGSContactPrepBlock.cpp:1218-1222): group[0..3] are the
+// header's records.
+__device__ __forceinline__ int blockBrokenSlot(ConstraintRecord* const* group, int p)
+{
+	int slot = 0;
+	for(int j = 0; j < p; j++)
+	{
+		bool anyFriction = false;
+		for(int l = 0; l < 4; l++)
+			if(group[l] && j < group[l]->nbPatches && group[l]->patch()[j].nbFriction > 0) anyFriction = true;
+		if(anyFriction) slot++;
+	}
+	return slot;
 }
 
 // integrateCoreStep (DyTGSDynamics.cpp:1403)

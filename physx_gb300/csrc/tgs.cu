@@ -378,7 +378,6 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
                                  float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, float* outVel, float* outPose,
                                  uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder, uint32_t* outNbHeaders)
 {
-	(void)correlationDistance;
 	if(!nbDyn || !rigid || !gravity || !outVel || !outPose || !outNbHeaders || !(dt > 0.0f) || !nbPos || !nbVel) return GBPX_ERR_INVALID;
 	if(nbConstraints && (!pairA || !pairB || !contactStart || !contactCount || !contacts || !material || !outHeaderStart || !outHeaderStride || !outOrder))
 		return GBPX_ERR_INVALID;
@@ -447,6 +446,7 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	pp.bounceThreshold = bounceThreshold;
 	pp.frictionOffsetThreshold = frictionOffsetThreshold;
 	pp.biasCoefficient = 2.0f * sqrtf(invDt / invStepDt);
+	pp.correlationDistance = correlationDistance;
 	if(nbConstraints)
 		tgs::prepKernel<<<divUp(nbConstraints, 128), 128, 0, s>>>(ws->ordered.ptr, nbConstraints, ws->pairA.ptr, ws->pairB.ptr, ws->cStart.ptr,
 		                                                          ws->cCount.ptr, ws->contacts.ptr, ws->material.ptr, ws->vel.ptr, ws->tx.ptr,
@@ -554,7 +554,6 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
                                                  float invDt, float invTotalDt, float bounceThreshold, float frictionOffsetThreshold,
                                                  float correlationDistance, void* outRows, uint32_t* outRowBytes)
 {
-	(void)correlationDistance;
 	if(!n) return GBPX_OK;
 	if(!vel0 || !vel1 || !txI0 || !txI1 || !data0 || !data1 || !frame0 || !frame1 || !contactStart || !contactCount || !outRows || !outRowBytes ||
 	   (nbPoints && !contactPoints) || !(invDt > 0.0f) || !(invTotalDt > 0.0f))
@@ -589,6 +588,7 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	pp.bounceThreshold = bounceThreshold;
 	pp.frictionOffsetThreshold = frictionOffsetThreshold;
 	pp.biasCoefficient = 2.0f * sqrtf(invTotalDt / invDt);
+	pp.correlationDistance = correlationDistance;
 	tgs::prepDescKernel<<<divUp(n, 128), 128, 0, s>>>(n, ws->vel0.ptr, ws->vel1.ptr, ws->tx0.ptr, ws->tx1.ptr, ws->data0.ptr, ws->data1.ptr,
 	                                                  ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr, ws->points.ptr,
 	                                                  laneFlags ? ws->laneFlags.ptr : nullptr, pp, ws->recs.ptr, ws->recBytes.ptr);

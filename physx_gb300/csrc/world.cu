@@ -54,6 +54,7 @@ struct StepParams
 	float contactDistance, toleranceLength, boundsMargin;
 	float bounceThreshold, frictionOffsetThreshold, correlationDistance, staticFriction;
 	uint32_t nbPos, nbVel;
+	uint32_t persistent;   // carry contact manifolds and friction patches between steps
 };
 
 struct WorldDev
@@ -97,7 +98,17 @@ struct WorldDev
 	uint32_t* nbPartitions;    // per scene: partitions, 0 when batching overflowed
 	uint32_t* prepQueue;       // constraint slots of all scenes, for the row-preparation kernel
 	uint8_t* recChunks;        // per constraint slot: 16-byte chunks its packed rows occupy
+	// Persistent pair state (the reference snippet's persistent mode): per pair
+	// slot a contact manifold and the friction patches its constraint left, in
+	// two buffers; sceneParity[scene] names the one holding the last step's.
+	uint32_t* pairsPrev;       // per pair slot: last step's pair keys
+	uint32_t* pairCountPrev;   // per scene
+	uint32_t* prevSlot;        // per pair slot: the pair's index in last step's list, or NO_PREV
+	uint32_t* sceneParity;     // per scene
+	np::ManifoldRecord* manifolds[2];
+	tgs::FrictionState* frictionState[2];
 };
+constexpr uint32_t NO_PREV = 0xffffffffu;
 
 // Pair kinds: shape types ordered (t0 <= t1), code t0 * 4 + t1.  Dynamic
 // bodies are spheres, capsules or boxes; statics may also be planes, so nine
@@ -247,6 +258,13 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 	float* maxZ = onChip ? sm.maxZ : ga + 4 * size_t(n);
 	uint32_t* cnt = onChip ? sm.cnt : w.progress + sc.solverStart;
 	const float mg = sp.boundsMargin;
+	if(sp.persistent)
+	{
+		// last step's pair list, for matching this step's pairs to their state
+		const uint32_t prevCount = w.pairCount[sid];
+		for(uint32_t t = lane; t < prevCount; t += 32) w.pairsPrev[sc.pairStart + t] = w.pairs[sc.pairStart + t];
+		if(lane == 0) w.pairCountPrev[sid] = prevCount;
+	}
 	for(uint32_t i = lane; i < sc.keyCap; i += 32)
 	{
 		if(i < n)
@@ -379,18 +397,19 @@ __device__ __forceinline__ void pairShape(const WorldDev& w, const SceneDesc& sc
 
 // Contacts of one pair kind (shape types TA <= TB), PxGenerateContacts semantics.
 template <int TA, int TB>
-__device__ __forceinline__ void generateKind(const float* ga, const float* gb, const Tr& pa, const Tr& pb, const StepParams& sp, np::Buffer& out)
+__device__ __forceinline__ void generateKind(const float* ga, const float* gb, const Tr& pa, const Tr& pb, const StepParams& sp, np::Manifold& m,
+                                             np::Buffer& out)
 {
 	const float cd = sp.contactDistance, tl = sp.toleranceLength;
 	if constexpr(TA == 0 && TB == 0) np::sphereSphere(ga[0], gb[0], pa, pb, cd, out);
 	else if constexpr(TA == 0 && TB == 1) np::spherePlane(ga[0], pa, pb, cd, out);
 	else if constexpr(TA == 0 && TB == 2) np::sphereCapsule(ga[0], gb[0], gb[1], pa, pb, cd, out);
 	else if constexpr(TA == 0 && TB == 3) np::sphereBox(ga[0], v3(gb[0], gb[1], gb[2]), pa, pb, cd, out);
-	else if constexpr(TA == 1 && TB == 2) np::planeCapsule(gb[0], gb[1], pa, pb, cd, out);
-	else if constexpr(TA == 1 && TB == 3) np::planeBox(v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
+	else if constexpr(TA == 1 && TB == 2) np::planeCapsule(gb[0], gb[1], pa, pb, cd, m, out);
+	else if constexpr(TA == 1 && TB == 3) np::planeBox(v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, m, out);
 	else if constexpr(TA == 2 && TB == 2) np::capsuleCapsule(ga[0], ga[1], gb[0], gb[1], pa, pb, cd, out);
-	else if constexpr(TA == 2 && TB == 3) np::capsuleBox(ga[0], ga[1], v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
-	else if constexpr(TA == 3 && TB == 3) np::boxBox(v3(ga[0], ga[1], ga[2]), v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, out);
+	else if constexpr(TA == 2 && TB == 3) np::capsuleBox(ga[0], ga[1], v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, m, out);
+	else if constexpr(TA == 3 && TB == 3) np::boxBox(v3(ga[0], ga[1], ga[2]), v3(gb[0], gb[1], gb[2]), pa, pb, cd, tl, m, out);
 }
 
 // Narrowphase of one pair kind over every scene: a thread per queued pair slot,
@@ -404,9 +423,26 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
 	{
 		const uint32_t slot = queue[q];
-		const SceneDesc sc = w.scenes[w.slotScene[slot]];
+		const uint32_t sid = w.slotScene[slot];
+		const SceneDesc sc = w.scenes[sid];
 		const uint32_t key = w.pairs[slot];
 		const uint32_t i = key >> 16, j = key & 0xffffu;
+		// persistent mode: the pair's place in last step's (sorted) list
+		uint32_t prev = NO_PREV, par = 0;
+		if(sp.persistent)
+		{
+			par = w.sceneParity[sid];
+			uint32_t lo = 0, hi = w.pairCountPrev[sid];
+			const uint32_t* pk = w.pairsPrev + sc.pairStart;
+			while(lo < hi)
+			{
+				const uint32_t mid = (lo + hi) >> 1;
+				if(pk[mid] < key) lo = mid + 1;
+				else hi = mid;
+			}
+			if(lo < w.pairCountPrev[sid] && pk[lo] == key) prev = lo;
+			w.prevSlot[slot] = prev;
+		}
 		int ta, tb;
 		float ga[4], gb[4];
 		Tr pa, pb;
@@ -414,8 +450,16 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 		pairShape(w, sc, j, tb, gb, pb);
 		const bool swap = ta > tb;
 		np::Buffer buf;
-		if(swap) generateKind<TA, TB>(gb, ga, pb, pa, sp, buf);
-		else generateKind<TA, TB>(ga, gb, pa, pb, sp, buf);
+		np::Manifold m;
+		constexpr bool CACHED = (TA == 1 && (TB == 2 || TB == 3)) || (TA == 2 && TB == 3) || (TA == 3 && TB == 3);
+		if(CACHED && sp.persistent && prev != NO_PREV) np::loadManifold(w.manifolds[par][sc.pairStart + prev], m);
+		if(swap) generateKind<TA, TB>(gb, ga, pb, pa, sp, m, buf);
+		else generateKind<TA, TB>(ga, gb, pa, pb, sp, m, buf);
+		if(sp.persistent)
+		{
+			if(CACHED) np::storeManifold(m, w.manifolds[par ^ 1u][slot]);
+			w.frictionState[par ^ 1u][slot].count = 0;   // the row preparation writes a constraint's patches
+		}
 		float4* o = w.contacts + size_t(slot) * 8;
 		for(int c = 0; c < buf.count; c++)
 		{
@@ -673,6 +717,7 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, cons
 	pp.bounceThreshold = sp.bounceThreshold;
 	pp.frictionOffsetThreshold = sp.frictionOffsetThreshold;
 	pp.biasCoefficient = 2.0f * sqrtf(invDt / pp.invStepDt);
+	pp.correlationDistance = sp.correlationDistance;
 	const uint32_t k = w.ordered[slot];
 	const uint32_t key = w.pairs[sc.pairStart + k];
 	const uint32_t a = key >> 16, b = key & 0xffffu;
@@ -693,11 +738,21 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, cons
 		cs[c].restitution = 0.0f;
 	}
 	tgs::ConstraintRecord& rec = w.recs[slot];
+	const tgs::FrictionState* prevFriction = nullptr;
+	tgs::FrictionState* written = nullptr;
+	if(sp.persistent)
+	{
+		const uint32_t par = w.sceneParity[w.slotScene[slot]];
+		const uint32_t prev = w.prevSlot[sc.pairStart + k];
+		if(prev != NO_PREV) prevFriction = w.frictionState[par] + sc.pairStart + prev;
+		written = w.frictionState[par ^ 1u] + sc.pairStart + k;
+	}
 	if(block)
 		tgs::prepConstraintBlock(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, b < n, b == 0,
-		                         rec);
+		                         rec, prevFriction, written);
 	else
-		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec);
+		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec, prevFriction,
+		                    written);
 	w.recChunks[slot] = uint8_t((rec.bytes() + 15) / 16);
 }
 
@@ -785,7 +840,27 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = vel[a].dLin; b0.dAng = vel[a].dAng;
 				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = vel[b].dLin; b1.dAng = vel[b].dAng;
 				const bool dynB = b < n;
-				tgs::solveRecord(*rec, b0, b1, dynB, minPen, elapsed);
+				const bool lastIter = it + 1 == sp.nbPos + sp.nbVel;
+				uint32_t broken = 0;
+				tgs::solveRecord(*rec, b0, b1, dynB, minPen, elapsed, sp.persistent && lastIter ? &broken : nullptr);
+				if(broken)
+				{
+					// write-back of the last iteration: a patch whose friction was
+					// clamped marks the friction patch it wrote broken
+					tgs::FrictionState& fs = w.frictionState[w.sceneParity[sid] ^ 1u][sc.pairStart + w.ordered[sc.pairStart + r]];
+					tgs::ConstraintRecord* group[4] = {nullptr, nullptr, nullptr, nullptr};
+					if(rec->isBlock())
+					{
+						const uint32_t r0 = begin + ((r - begin) & ~3u);
+						for(uint32_t l = 0; l < 4; l++) group[l] = w.recs + sc.pairStart + r0 + l;
+					}
+					for(int pi = 0; pi < rec->nbPatches; pi++)
+						if(broken & (1u << pi))
+						{
+							const int slotIdx = rec->isBlock() ? tgs::blockBrokenSlot(group, pi) : pi;
+							if(uint32_t(slotIdx) < fs.count) fs.patches[slotIdx].broken = 1;
+						}
+				}
 				V.set(a, b0.lin, b0.ang);
 				if(dynB) V.set(b, b1.lin, b1.ang);
 				if(rec != src)
@@ -891,11 +966,16 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, Step
 		const uint32_t sid = w.workOrder[item];
 		const SceneDesc sc = w.scenes[sid];
 		const uint32_t nbPart = w.nbPartitions[sid];
-		if(!nbPart && w.nbConstraints[sid]) continue;   // batching overflowed: the scene is left unchanged
-		for(uint32_t p = lane; p < nbPart; p += 32) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+		if(nbPart || !w.nbConstraints[sid])   // batching overflowed: the scene is left unchanged
+		{
+			for(uint32_t p = lane; p < nbPart; p += 32) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+			__syncwarp();
+			if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm, nbPart, SharedVel{sm.vel});
+			else sceneIterate(w, sc, sid, sp, sm, nbPart, GlobalVel{w.vel + sc.solverStart});
+		}
+		// the state this step wrote becomes the scene's last-step state
 		__syncwarp();
-		if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm, nbPart, SharedVel{sm.vel});
-		else sceneIterate(w, sc, sid, sp, sm, nbPart, GlobalVel{w.vel + sc.solverStart});
+		if(sp.persistent && lane == 0) w.sceneParity[sid] ^= 1u;
 	}
 }
 
@@ -957,6 +1037,9 @@ struct World
 	DevBuf<unsigned long long> keys, stats;
 	DevBuf<uint32_t> identity;
 	DevBuf<tgs::ConstraintRecord> recs;
+	DevBuf<uint32_t> pairsPrev, pairCountPrev, prevSlot, sceneParity;
+	DevBuf<np::ManifoldRecord> manifolds[2];
+	DevBuf<tgs::FrictionState> frictionState[2];
 	DevBuf<tgs::BodyVel> vel;
 	DevBuf<tgs::BodyTx> tx;
 	DevBuf<tgs::BodyData> data;
@@ -982,6 +1065,8 @@ struct World
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
 		w.typeCount = workCounter.ptr + 8; w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
 		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.recChunks = recChunks.ptr;
+		w.pairsPrev = pairsPrev.ptr; w.pairCountPrev = pairCountPrev.ptr; w.prevSlot = prevSlot.ptr; w.sceneParity = sceneParity.ptr;
+		for(int k = 0; k < 2; k++) { w.manifolds[k] = manifolds[k].ptr; w.frictionState[k] = frictionState[k].ptr; }
 		return w;
 	}
 
@@ -1017,10 +1102,15 @@ struct World
 		   vel.reserve(nbSolver) || tx.reserve(nbSolver) || data.reserve(nbSolver) || pose.reserve(nbSolver) || progress.reserve(nbSolver) ||
 		   maxNormal.reserve(nbSolver) || maxStatic.reserve(nbSolver) || staticProgress.reserve(nbSolver) ||
 		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(4) ||
-		   identity.reserve(S))
+		   identity.reserve(S) || pairCountPrev.reserve(S) || sceneParity.reserve(S))
+			return GBPX_ERR_NOMEM;
+		if(sp.persistent &&
+		   (pairsPrev.reserve(pair) || prevSlot.reserve(pair) || manifolds[0].reserve(pair) || manifolds[1].reserve(pair) ||
+		    frictionState[0].reserve(pair) || frictionState[1].reserve(pair)))
 			return GBPX_ERR_NOMEM;
 		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
 		              size_t(nbSolver) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + size_t(key) * 8;
+		if(sp.persistent) deviceBytes += size_t(pair) * (8 + 2 * (sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)));
 		cudaStream_t s = stream;
 		GBPX_CUDA_TRY(cudaMemcpyAsync(scenes.ptr, hScenes.data(), S * sizeof(world::SceneDesc), cudaMemcpyHostToDevice, s));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(workOrder.ptr, order.data(), S * 4, cudaMemcpyHostToDevice, s));
@@ -1055,6 +1145,10 @@ struct World
 			GBPX_CUDA_TRY(cudaMemcpyAsync(staticGeoms.ptr, staticGeomsIn, size_t(st) * 16, cudaMemcpyHostToDevice, s));
 		}
 		GBPX_CUDA_TRY(cudaMemsetAsync(status.ptr, 0, S * 4, s));
+		// no pair has a history yet
+		GBPX_CUDA_TRY(cudaMemsetAsync(pairCount.ptr, 0, S * 4, s));
+		GBPX_CUDA_TRY(cudaMemsetAsync(pairCountPrev.ptr, 0, S * 4, s));
+		GBPX_CUDA_TRY(cudaMemsetAsync(sceneParity.ptr, 0, S * 4, s));
 		int dev = 0, sms = 0;
 		GBPX_CUDA_TRY(cudaGetDevice(&dev));
 		GBPX_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1231,6 +1325,9 @@ struct World
 		d.nbStatics = ns;
 		GBPX_CUDA_TRY(cudaMemcpyAsync(scenes.ptr + slot, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
 		GBPX_CUDA_TRY(cudaMemsetAsync(status.ptr + slot, 0, 4, stream));
+		// an admitted scene starts without pair history
+		GBPX_CUDA_TRY(cudaMemsetAsync(pairCount.ptr + slot, 0, 4, stream));
+		GBPX_CUDA_TRY(cudaMemsetAsync(pairCountPrev.ptr + slot, 0, 4, stream));
 		return GBPX_OK;
 	}
 
@@ -1239,6 +1336,8 @@ struct World
 		if(stream) cudaStreamSynchronize(stream);
 		if(graphExec) cudaGraphExecDestroy(graphExec);
 		graphExec = nullptr;
+		pairsPrev.release(); pairCountPrev.release(); prevSlot.release(); sceneParity.release();
+		for(int k = 0; k < 2; k++) { manifolds[k].release(); frictionState[k].release(); }
 		scenes.release(); typeQueue.release(); slotScene.release(); activeCount.release(); recChunks.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
@@ -1272,6 +1371,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.dt = params[0]; sp.gx = params[1]; sp.gy = params[2]; sp.gz = params[3];
 	sp.contactDistance = params[4]; sp.toleranceLength = params[5]; sp.boundsMargin = params[6];
 	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
+	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
@@ -1699,6 +1799,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.dt = params[0]; sp.gx = params[1]; sp.gy = params[2]; sp.gz = params[3];
 	sp.contactDistance = params[4]; sp.toleranceLength = params[5]; sp.boundsMargin = params[6];
 	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
+	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;

@@ -13,14 +13,14 @@ _p = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa:
 
 DEFAULT_PARAMS = dict(dt=1.0 / 60.0, gravity=(0.0, -9.81, 0.0), contact_distance=0.04, tolerance_length=1.0, bounds_margin=0.02,
                       bounce_threshold=-2.0, friction_offset_threshold=0.04, correlation_distance=0.025, static_friction=0.5,
-                      nb_pos=4, nb_vel=1)
+                      nb_pos=4, nb_vel=1, persistent=True)
 
 
 def param_vector(p):
     g = p["gravity"]
     params = np.array([p["dt"], g[0], g[1], g[2], p["contact_distance"], p["tolerance_length"], p["bounds_margin"],
-                       p["bounce_threshold"], p["friction_offset_threshold"], p["correlation_distance"], p["static_friction"]],
-                      np.float32)
+                       p["bounce_threshold"], p["friction_offset_threshold"], p["correlation_distance"], p["static_friction"],
+                       1.0 if p.get("persistent", True) else 0.0], np.float32)
     return params, np.array([p["nb_pos"], p["nb_vel"]], np.uint32)
 
 

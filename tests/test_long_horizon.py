@@ -68,12 +68,15 @@ def test_oracle_pyramid_persistent_trace_equals_reference():
 
 
 @pytest.mark.gpu
-def test_world_pyramid_statistics_match_reference(cuda_device):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_world_pyramid_statistics_match_reference(cuda_device, persistent):
+    """The world in the snippet's persistent mode against the reference's persistent
+    trace, and with fresh caches against the fresh trace."""
     from physx_gb300.workloads import kinetic_energy, pyramid_scene
     from physx_gb300.world import World
-    ref = np.load(GOLDEN)
+    ref = np.load(GOLDEN_PERSISTENT if persistent else GOLDEN)
     sc = pyramid_scene()
-    w = World(sc)
+    w = World(sc, persistent=persistent)
     ke, top, low = [], [], []
     for _ in range(STEPS):
         w.step(1)

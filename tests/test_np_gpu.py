@@ -52,3 +52,36 @@ def test_contacts_edge_cases(cuda_device):
     bad["type0"] = np.array([7, 0], np.int32)
     with pytest.raises(GbpxError):
         generate_contacts(bad)
+
+
+def test_cached_contacts_match_reference_golden(cuda_device):
+    """Persistent caches over 8 moving frames (pcm_cached.npz, the reference's own
+    outputs): same counts every frame, every value within the contact tolerance."""
+    from contact_compare import CONTACT_TOL
+    from physx_gb300.contacts import CachedContacts
+    from test_oracle_golden import GOLDEN, load_np_cached_fixture
+    import os
+    pairs, frames = load_np_cached_fixture(os.path.join(GOLDEN, "pcm_cached.npz"))
+    n = len(pairs["type0"])
+    gpu = CachedContacts(n)
+    for f, fr in enumerate(frames):
+        gc, go = gpu.run(dict(pairs, pose0=fr["pose0"], pose1=fr["pose1"]))
+        assert np.array_equal(gc, fr["counts"]), "frame %d" % f
+        ref = unpack(fr["counts"], fr["contacts"])
+        for i in np.flatnonzero(gc):
+            assert np.abs(go[i, :gc[i], :7] - ref[i][:, :7]).max() <= CONTACT_TOL, (f, i)
+
+
+def test_cached_contacts_match_oracle(cuda_device):
+    from oracle_libs import CachedContacts as OracleCached
+    from physx_gb300.contacts import CachedContacts
+    from scenarios import moving_pairs
+    pairs, poses = moving_pairs(105, 6000, 12)
+    gpu, orc = CachedContacts(6000), OracleCached("orc", 6000)
+    for p0, p1 in poses:
+        fr = dict(pairs, pose0=p0, pose1=p1)
+        gc, go = gpu.run(fr)
+        oc, oo = orc.run(fr, max_per_pair=4)
+        assert np.array_equal(gc, oc)
+        for i in np.flatnonzero(oc):
+            assert np.abs(go[i, :oc[i], :7] - oo[i, :oc[i], :7]).max() <= 1e-6, i

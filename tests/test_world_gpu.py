@@ -102,3 +102,43 @@ def test_world_multi_round_batching_matches_oracle(cuda_device):
     assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5
     assert np.abs(out["p"] - ref["p"]).max() <= 1e-6
     w.release()
+
+
+def test_world_persistent_steps_match_oracle(cuda_device):
+    """Persistent mode (contact manifolds and friction patches kept between steps,
+    the reference snippet's default) against the oracle's persistent frames, step
+    by step over 10 steps of mixed piles."""
+    from oracle_libs import PersistentScenes
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes = pile_scenes(75, 6, 40)
+    w = _world(scenes)
+    orc = PersistentScenes("orc", scenes, DEFAULT_PARAMS)
+    for step in range(10):
+        w.step(1)
+        out = w.get_bodies()
+        ref = orc.step()
+        assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5, step
+        assert np.abs(out["p"] - ref["p"]).max() <= 1e-6, step
+    assert not w.status().any()
+    orc.release()
+    w.release()
+
+
+def test_world_fresh_mode_steps_match_oracle(cuda_device):
+    """Persistence off: every step uses fresh caches and friction data, as the oracle's
+    stateless frame does."""
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes = pile_scenes(76, 6, 40)
+    w = _world(scenes, persistent=False)
+    rb = scenes["rigid"].copy()
+    for step in range(6):
+        # each step from the same input state (the per-step bar; trajectories of a
+        # pile separate at the rounding level over many steps)
+        w.set_bodies(rb)
+        w.step(1)
+        out = w.get_bodies()
+        ref = run_scene_step("orc", dict(scenes, rigid=rb), DEFAULT_PARAMS, steps=1)
+        assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5, step
+        assert np.abs(out["p"] - ref["p"]).max() <= 1e-6, step
+        rb = ref
+    w.release()
