@@ -209,8 +209,9 @@ int gbpx_host_alloc(size_t bytes, void** out);
 int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, const float* params,
                        const uint32_t* iterations, uint32_t pairsPerBody, void** outServer);
 void gbpx_server_release(void* server);
-/* device bytes of one slot (for sizing a pool against a memory budget); not a status code */
-uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody);
+/* device bytes of one slot (for sizing a pool against a memory budget), with or
+ * without the persistent pair state; not a status code */
+uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody, int persistent);
 /* GBPX_ERR_BUDGET when no free slot of sufficient capacity exists */
 int gbpx_server_admit(void* server, uint32_t nbBodies, const void* rigidBodies, const int* types, const float* geoms, const float* friction,
                       uint32_t nbStatics, const float* staticPoses, const int* staticTypes, const float* staticGeoms, uint32_t* outScene);

@@ -1618,11 +1618,13 @@ struct Server
 	double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 
 	// Device bytes of one slot of `capacity` bodies and `statics` statics (the world layout).
-	static size_t slotBytes(uint32_t capacity, uint32_t statics, uint32_t pairsPerBody)
+	static size_t slotBytes(uint32_t capacity, uint32_t statics, uint32_t pairsPerBody, bool persistent)
 	{
 		const size_t pair = World::pow2(capacity * pairsPerBody + capacity * statics);
 		const size_t key = World::pow2(capacity);
-		return pair * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + 4 + 4 + sizeof(tgs::ConstraintRecord)) + size_t(capacity) * (96 + 4 + 16 + 4 + 24) +
+		const size_t persistentPair = persistent ? 8 + 2 * (sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0;
+		return pair * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + 4 + 4 + sizeof(tgs::ConstraintRecord) + persistentPair) +
+		       size_t(capacity) * (96 + 4 + 16 + 4 + 24) +
 		       size_t(capacity + statics) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + key * 8 +
 		       statics * 48 + world::MAX_PARTITIONS * 4 + 64;
 	}
@@ -1817,9 +1819,9 @@ GBPX_API void gbpx_server_release(void* s)
 }
 
 // Device bytes one slot of a class takes (for sizing a pool against a memory budget).
-GBPX_API uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody)
+GBPX_API uint64_t gbpx_server_slot_bytes(uint32_t capacity, uint32_t staticsPerSlot, uint32_t pairsPerBody, int persistent)
 {
-	return Server::slotBytes(capacity, staticsPerSlot, pairsPerBody);
+	return Server::slotBytes(capacity, staticsPerSlot, pairsPerBody, persistent != 0);
 }
 
 // Admits a scene (layout as one scene of gbpx_world_create) into the smallest

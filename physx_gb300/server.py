@@ -16,7 +16,7 @@ def _setup():
         L.gbpx_server_create.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
         L.gbpx_server_release.argtypes = [ctypes.c_void_p]
-        L.gbpx_server_slot_bytes.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+        L.gbpx_server_slot_bytes.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
         L.gbpx_server_slot_bytes.restype = ctypes.c_uint64
         L.gbpx_server_admit.argtypes = [ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 4 + [ctypes.c_uint32] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(ctypes.c_uint32)]
@@ -31,16 +31,16 @@ def _setup():
     return L
 
 
-def slot_bytes(capacity, statics=1, pairs_per_body=8):
-    return int(_setup().gbpx_server_slot_bytes(capacity, statics, pairs_per_body))
+def slot_bytes(capacity, statics=1, pairs_per_body=8, persistent=True):
+    return int(_setup().gbpx_server_slot_bytes(capacity, statics, pairs_per_body, int(bool(persistent))))
 
 
-def slots_for_budget(capacities, budget_bytes, weights=None, statics=1, pairs_per_body=8):
+def slots_for_budget(capacities, budget_bytes, weights=None, statics=1, pairs_per_body=8, persistent=True):
     """Slots per class so that the pool fits `budget_bytes`; `weights` is the expected
     share of scenes per class (equal by default, the log-uniform body-count case)."""
     w = np.ones(len(capacities)) if weights is None else np.asarray(weights, np.float64)
     w = w / w.sum()
-    per = sum(wi * slot_bytes(c, statics, pairs_per_body) for wi, c in zip(w, capacities))
+    per = sum(wi * slot_bytes(c, statics, pairs_per_body, persistent) for wi, c in zip(w, capacities))
     total = int(budget_bytes // per)
     return [max(1, int(total * wi)) for wi in w]
 
