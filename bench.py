@@ -345,26 +345,33 @@ def main():
     # the world's stream) and the roofline of the dominant kernel.  Algorithmic
     # (compulsory) HBM bytes per launch, from the step's own counts:
     #   broadphase   48 B per body (pose, type, shape) + 12 B per pair (key, kind queue)
-    #   narrowphase  108 B per pair (two poses and shapes, key, slot, count) + 32 B per contact
+    #   narrowphase  108 B per pair (two poses and shapes, key, slot, count) + 32 B per contact; persistent
+    #                mode adds 8 B per pair (previous slot, friction count) and, per pair of a cached kind
+    #                (plane-capsule, plane-box, capsule-box, box-box), its 288 B manifold read and written
     #   batching     280 B per body (PxRigidBodyData in, solver body records out) + 12 B per constraint
-    #   preparation  32 B per contact in + 2 x 184 B solver bodies per constraint + packed rows written
+    #   preparation  32 B per contact in + 2 x 184 B solver bodies per constraint + packed rows written;
+    #                persistent mode adds per constraint a 16 B friction header + one 112 B patch read and written
     #   solve        packed rows read once per iteration, plus per body 48 B velocities in, per position
     #                iteration 176 B of integration state, 124 B write-back
     st = w.stats()
     stage_ms = w.time_stages(max(3, a.steps // 3))
+    kinds = w.kind_counts()
     nbPos, nbVel = DEFAULT_PARAMS["nb_pos"], DEFAULT_PARAMS["nb_vel"]
     np_ms = sum(v for k, v in stage_ms.items() if k.startswith("np "))
+    persistent = bool(DEFAULT_PARAMS["persistent"])
+    cached_pairs = sum(kinds[k] for k in ("np plane-capsule", "np plane-box", "np capsule-box", "np box-box"))
     stage_bytes = {
         "broadphase": bodies * 48 + st["pairs"] * 12,
-        "narrowphase": st["pairs"] * 108 + st["contacts"] * 32,
+        "narrowphase": st["pairs"] * 108 + st["contacts"] * 32 + (st["pairs"] * 8 + cached_pairs * 576 if persistent else 0),
         "batching": bodies * 280 + st["constraints"] * 12,
-        "row preparation": st["contacts"] * 32 + st["constraints"] * 368 + st["row_bytes"],
+        "row preparation": st["contacts"] * 32 + st["constraints"] * 368 + st["row_bytes"] + (st["constraints"] * 256 if persistent else 0),
         "solve": (nbPos + nbVel) * st["row_bytes"] + bodies * (48 + nbPos * 176 + 124),
     }
     stage_time = {"broadphase": stage_ms["broadphase"], "narrowphase": np_ms, "batching": stage_ms["batching"],
                   "row preparation": stage_ms["row preparation"], "solve": stage_ms["solve"]}
     peak, peak_kind = measured_peak()
     stages = {k: dict(ms=stage_time[k], gbs=stage_bytes[k] / (stage_time[k] / 1000.0) / 1e9, bytes=stage_bytes[k]) for k in stage_time}
+    stages["narrowphase"]["kinds"] = {k[3:]: dict(pairs=kinds[k], ms=stage_ms[k]) for k in kinds}
     dominant = max(stage_time, key=stage_time.get)
     achieved = stages[dominant]["gbs"]
     traffic = profiled_traffic(dominant)

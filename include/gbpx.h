@@ -143,19 +143,26 @@ int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void
  * bit 0 = lane of a stride-4 header on the reference's 4-wide block path
  * (createFinalizeSolverContacts4Step, lowleveldynamics/src/DyTGSContactPrepBlock.cpp:1398),
  * bit 1 = that header has a dynamic body B, bit 2 = bodyBDataIndex is 0;
- * invDt = nbPositionIterations / dt, invTotalDt = 1 / dt.  Rows to
- * outRows + k * stride, used bytes to outRowBytes[k]. */
+ * frictionIn / frictionOut (null: fresh friction data, none kept): per
+ * constraint a 464-byte record (uint32 count, 12 bytes padding, 4 friction
+ * patches of 112 bytes), the patches the constraint left last frame
+ * (frictionPtr / frictionCount of PxTGSSolverContactDesc) and the ones it
+ * leaves this frame; invDt = nbPositionIterations / dt, invTotalDt = 1 / dt.
+ * Rows to outRows + k * stride, used bytes to outRowBytes[k]. */
 int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
                                         const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
                                         const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, const uint8_t* laneFlags,
-                                        float invDt, float invTotalDt, float bounceThreshold, float frictionOffsetThreshold,
-                                        float correlationDistance, void* outRows, uint32_t* outRowBytes);
+                                        const void* frictionIn, void* frictionOut, float invDt, float invTotalDt, float bounceThreshold,
+                                        float frictionOffsetThreshold, float correlationDistance, void* outRows, uint32_t* outRowBytes);
 /* rows (n x stride, solve order, impulses updated in place); constraint k joins
  * bodyA[k], bodyB[k]; constraints in [waveEnds[w-1], waveEnds[w]) touch distinct
  * bodies; the first nbIntegrate bodies are integrated every position iteration;
- * dt = time step / nbPositionIterations. */
+ * dt = time step / nbPositionIterations; outBroken (null: not wanted): per
+ * constraint, bit p set when patch p's friction was clamped in the last
+ * iteration, which marks the friction patch it wrote broken. */
 int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
-                               void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt);
+                               void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
+                               uint32_t* outBroken);
 int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* poses, uint32_t n);
 
 /* -------------------------------------------------------- batched world
@@ -190,6 +197,9 @@ int gbpx_world_time_steps(void* world, uint32_t nbSteps, int useGraph, float* ou
 int gbpx_world_time_plain(void* world, uint32_t firstScene, uint32_t nbScenes, float* outMs);
 /* out4: pairs, pairs with contacts, contacts, bytes of packed constraint rows (last step) */
 int gbpx_world_stats(void* world, uint64_t* out4);
+/* Pairs of each pair kind in the last step, in the kind order of the
+ * narrowphase launches (sphere-sphere ... box-box): 9 counts. */
+int gbpx_world_kind_counts(void* world, uint32_t* out9);
 /* average device milliseconds per kernel of a step (un-captured steps, events
  * between launches), in launch order; outMs has "kernels per step" entries */
 int gbpx_world_time_stages(void* world, uint32_t nbSteps, float* outMs);

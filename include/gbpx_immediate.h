@@ -18,13 +18,18 @@
  * the library and its tests; a PhysX program keeps including PhysX's headers.
  * Do not include it together with PxImmediateMode.h.
  *
- * Behaviour: every contact generation call is a fresh-cache call (PxCache and
- * PxCacheAllocator are not used); friction patches are not persisted
- * (reserveFrictionData is not called, frictionPtr/frictionCount are left 0);
- * the supported pair set is sphere / plane / capsule / box; contact descriptors
- * must use unit inverse-mass scales, restDistance 0 and no maximum impulse, and
- * articulations are not supported (the functions return false, or do nothing,
- * for input outside this set).  All arithmetic runs on the GPU through libgbpx.
+ * Behaviour: as the reference's persistent mode, a PxCache handed back keeps
+ * the pair's contact manifold (for plane-capsule, plane-box, capsule-box and
+ * box-box pairs, in memory from the PxCacheAllocator), and a contact
+ * descriptor's frictionPtr / frictionCount handed back keep its friction
+ * patches (memory from reserveFrictionData, broken flags written by
+ * PxSolveConstraintsTGS); fresh caches and null friction pointers start over.
+ * The bytes behind both are this library's own layout, opaque to the caller as
+ * the reference's are.  The supported pair set is sphere / plane / capsule /
+ * box; contact descriptors must use unit inverse-mass scales, restDistance 0
+ * and no maximum impulse, and articulations are not supported (the functions
+ * return false, or do nothing, for input outside this set).  All arithmetic
+ * runs on the GPU through libgbpx.
  */
 #ifndef GBPX_IMMEDIATE_H
 #define GBPX_IMMEDIATE_H

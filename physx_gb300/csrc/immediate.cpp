@@ -51,16 +51,58 @@ uint32_t stridesTotal(const PxConstraintBatchHeader* headers, uint32_t nbHeaders
 	for(uint32_t h = 0; h < nbHeaders; h++) n += headers[h].stride;
 	return n;
 }
+
+// Contact manifold kept in a PxCache between calls: libgbpx's 288-byte record
+// (opaque to the caller, who only hands the cache back), marked in its
+// padding word so that a cache this library did not fill is taken as fresh.
+constexpr uint32_t MANIFOLD_BYTES = 288;
+constexpr uint32_t MANIFOLD_MAGIC_OFFSET = 76;
+constexpr uint32_t MANIFOLD_USED_OFFSET = 68;
+constexpr uint32_t MANIFOLD_MAGIC = 0x58504247u;
+constexpr uint8_t CACHE_IS_MANIFOLD = 1;   // PxCache::mManifoldFlags of a single manifold
+
+// does the pair kind keep a manifold (gEnablePCMCaching,
+// physx/source/lowlevel/software/src/PxsContext.cpp:89): plane-capsule,
+// plane-box, capsule-box, box-box
+bool cachedKind(int t0, int t1)
+{
+	const int a = std::min(t0, t1), b = std::max(t0, t1);
+	return (a == 1 && (b == 2 || b == 3)) || (a == 2 && b == 3) || (a == 3 && b == 3);
+}
+
+// Friction data a contact constraint leaves in the caller's friction memory
+// (frictionPtr / frictionCount): libgbpx's 112-byte friction patches, whose
+// first 16 bytes hold the body-0 normal and the broken flag (offset 12).
+constexpr uint32_t PATCH_BYTES = 112;
+constexpr uint32_t PATCH_BROKEN_OFFSET = 12;
+constexpr uint32_t FRICTION_RECORD_BYTES = 16 + 4 * PATCH_BYTES;   // count, padding, 4 patches
+constexpr uint32_t MAX_PATCHES = 4;
+
+// Written after a constraint's rows in its constraint memory: where its
+// friction patches are and which patch takes each row patch's broken flag.
+struct RowTrailer
+{
+	uint8_t* friction;
+	uint8_t slots[MAX_PATCHES];
+	uint32_t count;
+};
+static_assert(sizeof(RowTrailer) == 16, "row trailer");
+
+// PatchRows of libgbpx's constraint record (rows at +16, 48 bytes per patch,
+// nbFriction at +44); record header: bodyA, bodyB, nbPatches, counts
+uint32_t recordPatches(const uint8_t* rec) { uint32_t v; memcpy(&v, rec + 8, 4); return v; }
+uint32_t recordPatchFriction(const uint8_t* rec, uint32_t p) { uint32_t v; memcpy(&v, rec + 16 + 48 * p + 44, 4); return v; }
 } // namespace
 
-// immediate::PxGenerateContacts (fresh caches: the cache and its allocator are not used).
+// immediate::PxGenerateContacts.  The pair kinds whose contact manifold
+// persists keep it in contactCache[i] (memory from the cache allocator, as the
+// reference allocates it), the others leave the cache empty.
 GX bool PxGenerateContacts(const PxGeometry* const* geom0, const PxGeometry* const* geom1, const PxTransform* pose0, const PxTransform* pose1,
                            PxCache* contactCache, uint32_t nbPairs, PxContactRecorder& contactRecorder, float contactDistance,
                            float meshContactMargin, float toleranceLength, PxCacheAllocator& allocator)
 {
-	(void)contactCache;
-	(void)allocator;
 	if(!nbPairs) return true;
+	if(!contactCache) return false;
 	std::vector<int> t0(nbPairs), t1(nbPairs);
 	std::vector<float> g0(4 * size_t(nbPairs)), g1(4 * size_t(nbPairs)), p0(7 * size_t(nbPairs)), p1(7 * size_t(nbPairs));
 	for(uint32_t i = 0; i < nbPairs; i++)
@@ -71,9 +113,44 @@ GX bool PxGenerateContacts(const PxGeometry* const* geom0, const PxGeometry* con
 	}
 	std::vector<float> out(size_t(nbPairs) * 4 * 8);
 	std::vector<uint32_t> counts(nbPairs);
-	if(gbpx_generate_contacts(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), nbPairs, contactDistance, meshContactMargin,
-	                          toleranceLength, out.data(), 4, counts.data()) != GBPX_OK)
+	std::vector<uint8_t> manifolds(size_t(nbPairs) * MANIFOLD_BYTES, 0);
+	for(uint32_t i = 0; i < nbPairs; i++)
+	{
+		const PxCache& c = contactCache[i];
+		if(c.mCachedData && c.mCachedSize == MANIFOLD_BYTES)
+		{
+			uint32_t magic;
+			memcpy(&magic, c.mCachedData + MANIFOLD_MAGIC_OFFSET, 4);
+			if(magic == MANIFOLD_MAGIC) memcpy(&manifolds[size_t(i) * MANIFOLD_BYTES], c.mCachedData, MANIFOLD_BYTES);
+		}
+	}
+	if(gbpx_generate_contacts_cached(t0.data(), g0.data(), t1.data(), g1.data(), p0.data(), p1.data(), nbPairs, contactDistance,
+	                                 meshContactMargin, toleranceLength, out.data(), 4, counts.data(), manifolds.data()) != GBPX_OK)
 		return false;
+	for(uint32_t i = 0; i < nbPairs; i++)
+	{
+		PxCache& c = contactCache[i];
+		uint8_t* rec = &manifolds[size_t(i) * MANIFOLD_BYTES];
+		uint32_t used;
+		memcpy(&used, rec + MANIFOLD_USED_OFFSET, 4);
+		uint8_t* mem = cachedKind(t0[i], t1[i]) && used ? allocator.allocateCacheData(MANIFOLD_BYTES) : nullptr;
+		if(mem)
+		{
+			memcpy(rec + MANIFOLD_MAGIC_OFFSET, &MANIFOLD_MAGIC, 4);
+			memcpy(mem, rec, MANIFOLD_BYTES);
+			c.mCachedData = mem;
+			c.mCachedSize = uint16_t(MANIFOLD_BYTES);
+			c.mPairData = 0;
+			c.mManifoldFlags = CACHE_IS_MANIFOLD;
+		}
+		else
+		{
+			c.mCachedData = nullptr;
+			c.mCachedSize = 0;
+			c.mPairData = 0;
+			c.mManifoldFlags = 0;
+		}
+	}
 	for(uint32_t i = 0; i < nbPairs; i++)
 	{
 		if(!counts[i]) continue;
@@ -187,25 +264,78 @@ GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uin
 		for(uint32_t l = 0; l < 4; l++)
 			laneFlags[k + l] = uint8_t(1u | (dyn ? 2u : 0u) | (contactDescs[k + l].desc->bodyBDataIndex == 0 ? 4u : 0u));
 	}
+	// last frame's friction patches (frictionPtr / frictionCount)
+	std::vector<uint8_t> frictionIn(size_t(n) * FRICTION_RECORD_BYTES, 0), frictionOut(size_t(n) * FRICTION_RECORD_BYTES, 0);
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxTGSSolverContactDesc& d = contactDescs[k];
+		const uint32_t cnt = d.frictionPtr ? std::min<uint32_t>(d.frictionCount, MAX_PATCHES) : 0u;
+		uint8_t* rec = &frictionIn[size_t(k) * FRICTION_RECORD_BYTES];
+		memcpy(rec, &cnt, 4);
+		if(cnt) memcpy(rec + 16, d.frictionPtr, size_t(cnt) * PATCH_BYTES);
+	}
 	const uint32_t stride = gbpx_constraint_row_stride();
 	std::vector<uint8_t> rows(size_t(n) * stride);
 	std::vector<uint32_t> bytes(n);
 	if(gbpx_create_contact_constraints_tgs(n, v0.data(), v1.data(), x0.data(), x1.data(), d0.data(), d1.data(), &f0[0].q.x, &f1[0].q.x, cs.data(),
-	                                       cc.data(), points.data(), uint32_t(points.size()), laneFlags.data(), invDt, invTotalDt,
-	                                       bounceThreshold, frictionOffsetThreshold, correlationDistance, rows.data(), bytes.data()) != GBPX_OK)
+	                                       cc.data(), points.data(), uint32_t(points.size()), laneFlags.data(), frictionIn.data(),
+	                                       frictionOut.data(), invDt, invTotalDt, bounceThreshold, frictionOffsetThreshold, correlationDistance,
+	                                       rows.data(), bytes.data()) != GBPX_OK)
 		return false;
+	// header of every constraint (position of its header's first lane)
+	std::vector<uint32_t> headerFirst(n, 0);
+	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
+		for(uint32_t l = 0; l < batchHeaders[h].stride; l++) headerFirst[k + l] = k;
 	for(uint32_t k = 0; k < n; k++)
 	{
 		PxTGSSolverContactDesc& d = contactDescs[k];
 		const uint32_t size = (bytes[k] + 15u) & ~15u;
-		uint8_t* mem = allocator.reserveConstraintData(size);
+		uint8_t* mem = allocator.reserveConstraintData(size + uint32_t(sizeof(RowTrailer)));
 		if(!mem) return false;
-		memcpy(mem, &rows[size_t(k) * stride], size);
+		const uint8_t* rec = &rows[size_t(k) * stride];
+		memcpy(mem, rec, size);
 		d.desc->constraint = mem;
 		d.desc->constraintLengthOver16 = uint16_t(size / 16);
-		d.frictionPtr = nullptr;
-		d.frictionCount = 0;
-		d.numFrictionPatches = 0;
+		// the friction patches this constraint leaves, in the caller's friction memory
+		const uint8_t* out = &frictionOut[size_t(k) * FRICTION_RECORD_BYTES];
+		uint32_t cnt;
+		memcpy(&cnt, out, 4);
+		cnt = std::min<uint32_t>(cnt, MAX_PATCHES);
+		uint8_t* fmem = cnt ? allocator.reserveFrictionData(cnt * PATCH_BYTES) : nullptr;
+		if(cnt && !fmem) return false;
+		if(fmem) memcpy(fmem, out + 16, size_t(cnt) * PATCH_BYTES);
+		d.frictionPtr = fmem;
+		d.frictionCount = uint8_t(cnt);
+		d.numFrictionPatches = cnt;
+		// broken-flag slot of each row patch: the patch itself, or for a block
+		// lane the header's earlier patch rows that had friction in any lane
+		// (DyTGSContactPrepBlock.cpp:1218-1222)
+		RowTrailer tr;
+		memset(&tr, 0, sizeof(tr));
+		tr.friction = fmem;
+		tr.count = cnt;
+		const uint32_t np = std::min<uint32_t>(recordPatches(rec), MAX_PATCHES);
+		const bool block = laneFlags[k] & 1u;
+		for(uint32_t p = 0; p < np; p++)
+		{
+			uint32_t slot = p;
+			if(block)
+			{
+				slot = 0;
+				for(uint32_t j = 0; j < p; j++)
+				{
+					bool any = false;
+					for(uint32_t l = 0; l < 4; l++)
+					{
+						const uint8_t* r2 = &rows[size_t(headerFirst[k] + l) * stride];
+						if(j < recordPatches(r2) && recordPatchFriction(r2, j) > 0) any = true;
+					}
+					if(any) slot++;
+				}
+			}
+			tr.slots[p] = uint8_t(slot);
+		}
+		memcpy(mem + size, &tr, sizeof(tr));
 	}
 	return true;
 }
@@ -274,8 +404,9 @@ GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint3
 		waveOpen = true;
 	}
 	if(n) waveEnds.push_back(n);
+	std::vector<uint32_t> broken(n ? n : 1, 0);
 	if(gbpx_solve_constraints_tgs(n ? rows.data() : nullptr, a.data(), b.data(), n, waveEnds.data(), uint32_t(waveEnds.size()), vel.data(), tx.data(),
-	                              uint32_t(vel.size()), nbSolverBodies, nbPositionIterations, nbVelocityIterations, dt) != GBPX_OK)
+	                              uint32_t(vel.size()), nbSolverBodies, nbPositionIterations, nbVelocityIterations, dt, broken.data()) != GBPX_OK)
 		return;
 	memcpy(solverBodies, vel.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyVel));
 	memcpy(txInertias, tx.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyTxInertia));
@@ -283,7 +414,21 @@ GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint3
 		for(uint32_t j = 0; j < batchHeaders[h].stride; j++, k++)
 		{
 			const PxSolverConstraintDesc& d = descs[batchHeaders[h].startIndex + j];
-			if(d.constraint) memcpy(d.constraint, &rows[size_t(k) * stride], std::min<size_t>(size_t(d.constraintLengthOver16) * 16, stride));
+			if(!d.constraint) continue;
+			const size_t size = size_t(d.constraintLengthOver16) * 16;
+			memcpy(d.constraint, &rows[size_t(k) * stride], std::min<size_t>(size, stride));
+			// write-back of the last iteration: clamped friction marks its patch broken
+			if(broken[k])
+			{
+				RowTrailer tr;
+				memcpy(&tr, d.constraint + size, sizeof(tr));
+				for(uint32_t p = 0; p < MAX_PATCHES; p++)
+					if((broken[k] & (1u << p)) && tr.friction && tr.slots[p] < tr.count)
+					{
+						const uint32_t one = 1;
+						memcpy(tr.friction + size_t(tr.slots[p]) * PATCH_BYTES + PATCH_BROKEN_OFFSET, &one, 4);
+					}
+			}
 		}
 }
 

@@ -46,12 +46,14 @@ constexpr uint8_t LANE_BLOCK = 1, LANE_BLOCK_DYNAMIC = 2, LANE_KEEP_B = 4;
 
 __device__ __forceinline__ void prepByFlags(uint8_t flags, const Contact* cs, int cnt, int a, int b, const BodyVel& va, const BodyVel& vb,
                                             const BodyTx& ta, const BodyTx& tb, const BodyData& da, const BodyData& db, const Tr& f0, const Tr& f1,
-                                            const PrepParams& pp, ConstraintRecord& rec)
+                                            const PrepParams& pp, ConstraintRecord& rec, const FrictionState* prev = nullptr,
+                                            FrictionState* written = nullptr)
 {
 	if(flags & LANE_BLOCK)
-		prepConstraintBlock(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, (flags & LANE_BLOCK_DYNAMIC) != 0, (flags & LANE_KEEP_B) != 0, rec);
+		prepConstraintBlock(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, (flags & LANE_BLOCK_DYNAMIC) != 0, (flags & LANE_KEEP_B) != 0, rec,
+		                    prev, written);
 	else
-		prepConstraint(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, rec);
+		prepConstraint(cs, cnt, a, b, va, vb, ta, tb, da, db, f0, f1, pp, rec, prev, written);
 }
 
 // Rows for constraint k of the ordered list (ordered[k] = caller's constraint index).
@@ -211,7 +213,8 @@ __global__ void prepDescKernel(uint32_t n, const float* __restrict__ vel0, const
                                const float* __restrict__ tx1, const float* __restrict__ data0, const float* __restrict__ data1,
                                const float* __restrict__ frame0, const float* __restrict__ frame1, const uint32_t* __restrict__ cStart,
                                const uint32_t* __restrict__ cCount, const float* __restrict__ points, const uint8_t* __restrict__ laneFlags,
-                               PrepParams pp, ConstraintRecord* __restrict__ recs, uint32_t* __restrict__ recBytes)
+                               const FrictionState* __restrict__ frictionIn, FrictionState* __restrict__ frictionOut, PrepParams pp,
+                               ConstraintRecord* __restrict__ recs, uint32_t* __restrict__ recBytes)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= n) return;
@@ -235,14 +238,15 @@ __global__ void prepDescKernel(uint32_t n, const float* __restrict__ vel0, const
 	const float* b = frame1 + 7 * size_t(k);
 	f0.q.x = a[0]; f0.q.y = a[1]; f0.q.z = a[2]; f0.q.w = a[3]; f0.p = v3(a[4], a[5], a[6]);
 	f1.q.x = b[0]; f1.q.y = b[1]; f1.q.z = b[2]; f1.q.w = b[3]; f1.p = v3(b[4], b[5], b[6]);
-	prepByFlags(laneFlags ? laneFlags[k] : uint8_t(0), cs, int(cnt), 0, 1, va, vb, ta, tb, da, db, f0, f1, pp, recs[k]);
+	prepByFlags(laneFlags ? laneFlags[k] : uint8_t(0), cs, int(cnt), 0, 1, va, vb, ta, tb, da, db, f0, f1, pp, recs[k],
+	            frictionIn && frictionIn[k].count ? frictionIn + k : nullptr, frictionOut ? frictionOut + k : nullptr);
 	recBytes[k] = recs[k].bytes();
 }
 
 // One wave of independent constraints on solver bodies held in the
 // reference's layouts: rows[k] joins bodyA[k], bodyB[k].
 __global__ void solveWaveRefKernel(ConstraintRecord* __restrict__ recs, const uint32_t* __restrict__ bodyA, const uint32_t* __restrict__ bodyB,
-                                   uint32_t begin, uint32_t end, float* __restrict__ vel, float minPen, float elapsed)
+                                   uint32_t begin, uint32_t end, float* __restrict__ vel, float minPen, float elapsed, uint32_t* __restrict__ broken)
 {
 	const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= end) return;
@@ -251,7 +255,7 @@ __global__ void solveWaveRefKernel(ConstraintRecord* __restrict__ recs, const ui
 	float* va = vel + 16 * size_t(bodyA[k]);
 	float* vb = vel + 16 * size_t(bodyB[k]);
 	BodyVel b0 = loadVelRef(va), b1 = loadVelRef(vb);
-	solveRecord(r, b0, b1, true, minPen, elapsed);
+	solveRecord(r, b0, b1, true, minPen, elapsed, broken ? broken + k : nullptr);
 	va[0] = b0.lin.x; va[1] = b0.lin.y; va[2] = b0.lin.z; va[4] = b0.ang.x; va[5] = b0.ang.y; va[6] = b0.ang.z;
 	vb[0] = b1.lin.x; vb[1] = b1.lin.y; vb[2] = b1.lin.z; vb[4] = b1.ang.x; vb[5] = b1.ang.y; vb[6] = b1.ang.z;
 }
@@ -494,8 +498,9 @@ struct TgsStageWorkspace
 {
 	cudaStream_t stream = 0;
 	DevBuf<float> vel0, vel1, tx0, tx1, data0, data1, frame0, frame1, points, vel, tx, poses;
-	DevBuf<uint32_t> cStart, cCount, bodyA, bodyB, recBytes;
+	DevBuf<uint32_t> cStart, cCount, bodyA, bodyB, recBytes, broken;
 	DevBuf<uint8_t> laneFlags;
+	DevBuf<tgs::FrictionState> frictionIn, frictionOut;
 	DevBuf<tgs::ConstraintRecord> recs;
 	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
 };
@@ -545,14 +550,17 @@ GBPX_API int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_
 // per-pair path): bit 0 = one of the four constraints of a header of stride 4
 // that takes the reference's 4-wide block path, bit 1 = that header has a
 // dynamic body B, bit 2 = the descriptor's bodyBDataIndex is 0.
+// frictionIn / frictionOut (may be null): per constraint a 464-byte friction
+// record (count, then <= 4 friction patches of 112 bytes), the patches it left
+// last frame (frictionPtr / frictionCount) and the ones it leaves now.
 // invDt = 1 / (dt / nbPositionIterations), invTotalDt = 1 / dt.
 // Writes each constraint's rows to outRows + k * gbpx_constraint_row_stride()
 // and their used size to outRowBytes[k].
 GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
                                                  const void* data1, const float* frame0, const float* frame1, const uint32_t* contactStart,
                                                  const uint32_t* contactCount, const void* contactPoints, uint32_t nbPoints, const uint8_t* laneFlags,
-                                                 float invDt, float invTotalDt, float bounceThreshold, float frictionOffsetThreshold,
-                                                 float correlationDistance, void* outRows, uint32_t* outRowBytes)
+                                                 const void* frictionIn, void* frictionOut, float invDt, float invTotalDt, float bounceThreshold,
+                                                 float frictionOffsetThreshold, float correlationDistance, void* outRows, uint32_t* outRowBytes)
 {
 	if(!n) return GBPX_OK;
 	if(!vel0 || !vel1 || !txI0 || !txI1 || !data0 || !data1 || !frame0 || !frame1 || !contactStart || !contactCount || !outRows || !outRowBytes ||
@@ -565,7 +573,8 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	const size_t m = n;
 	if(ws->vel0.reserve(16 * m) || ws->vel1.reserve(16 * m) || ws->tx0.reserve(16 * m) || ws->tx1.reserve(16 * m) || ws->data0.reserve(12 * m) ||
 	   ws->data1.reserve(12 * m) || ws->frame0.reserve(7 * m) || ws->frame1.reserve(7 * m) || ws->cStart.reserve(m) || ws->cCount.reserve(m) ||
-	   ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->recs.reserve(m) || ws->recBytes.reserve(m) || ws->laneFlags.reserve(m))
+	   ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->recs.reserve(m) || ws->recBytes.reserve(m) || ws->laneFlags.reserve(m) ||
+	   (frictionIn && ws->frictionIn.reserve(m)) || (frictionOut && ws->frictionOut.reserve(m)))
 		return GBPX_ERR_NOMEM;
 	cudaStream_t s = ws->stream;
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel0.ptr, vel0, m * 64, cudaMemcpyHostToDevice, s));
@@ -580,6 +589,7 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cCount.ptr, contactCount, m * 4, cudaMemcpyHostToDevice, s));
 	if(nbPoints) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->points.ptr, contactPoints, size_t(nbPoints) * 80, cudaMemcpyHostToDevice, s));
 	if(laneFlags) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->laneFlags.ptr, laneFlags, m, cudaMemcpyHostToDevice, s));
+	if(frictionIn) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->frictionIn.ptr, frictionIn, m * sizeof(tgs::FrictionState), cudaMemcpyHostToDevice, s));
 	tgs::PrepParams pp;
 	pp.invStepDt = invDt;
 	pp.invTotalDt = invTotalDt;
@@ -591,10 +601,12 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	pp.correlationDistance = correlationDistance;
 	tgs::prepDescKernel<<<divUp(n, 128), 128, 0, s>>>(n, ws->vel0.ptr, ws->vel1.ptr, ws->tx0.ptr, ws->tx1.ptr, ws->data0.ptr, ws->data1.ptr,
 	                                                  ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr, ws->points.ptr,
-	                                                  laneFlags ? ws->laneFlags.ptr : nullptr, pp, ws->recs.ptr, ws->recBytes.ptr);
+	                                                  laneFlags ? ws->laneFlags.ptr : nullptr, frictionIn ? ws->frictionIn.ptr : nullptr,
+	                                                  frictionOut ? ws->frictionOut.ptr : nullptr, pp, ws->recs.ptr, ws->recBytes.ptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(outRows, ws->recs.ptr, m * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(outRowBytes, ws->recBytes.ptr, m * 4, cudaMemcpyDeviceToHost, s));
+	if(frictionOut) GBPX_CUDA_TRY(cudaMemcpyAsync(frictionOut, ws->frictionOut.ptr, m * sizeof(tgs::FrictionState), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 	return GBPX_OK;
 }
@@ -605,9 +617,12 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 // [waveEnds[w-1], waveEnds[w]) touch distinct bodies.  bodyVel/bodyTxI:
 // nbBodies records in the reference's layouts, updated in place; the first
 // nbIntegrate bodies are integrated after every position iteration.
-// dt = time step / nbPositionIterations.
+// dt = time step / nbPositionIterations.  outBroken (may be null): per
+// constraint, bit p set when patch p's friction was clamped in the last
+// iteration (the broken flag its friction patch gets).
 GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
-                                        void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt)
+                                        void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
+                                        uint32_t* outBroken)
 {
 	if(!bodyVel || !bodyTxI || !nbBodies || nbIntegrate > nbBodies || !nbPos || !(dt > 0.0f)) return GBPX_ERR_INVALID;
 	if(n && (!rows || !bodyA || !bodyB || !waveEnds || !nbWaves || waveEnds[nbWaves - 1] != n)) return GBPX_ERR_INVALID;
@@ -617,8 +632,9 @@ GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const
 	if(!ws) return GBPX_ERR_CUDA;
 	const size_t m = n ? n : 1;
 	if(ws->vel.reserve(16 * size_t(nbBodies)) || ws->tx.reserve(16 * size_t(nbBodies)) || ws->bodyA.reserve(m) || ws->bodyB.reserve(m) ||
-	   ws->recs.reserve(m))
+	   ws->recs.reserve(m) || (outBroken && ws->broken.reserve(m)))
 		return GBPX_ERR_NOMEM;
+	if(outBroken && n) GBPX_CUDA_TRY(cudaMemsetAsync(ws->broken.ptr, 0, size_t(n) * 4, ws->stream));
 	cudaStream_t s = ws->stream;
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel.ptr, bodyVel, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx.ptr, bodyTxI, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
@@ -629,25 +645,28 @@ GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const
 		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->recs.ptr, rows, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyHostToDevice, s));
 	}
 	float elapsed = 0.0f;
-	auto sweep = [&](float minPen) {
+	auto sweep = [&](float minPen, bool last) {
 		for(uint32_t w = 0; w < nbWaves; w++)
 		{
 			const uint32_t b = w ? waveEnds[w - 1] : 0u, e = waveEnds[w];
-			if(e > b) tgs::solveWaveRefKernel<<<divUp(e - b, 128), 128, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, minPen, elapsed);
+			if(e > b)
+				tgs::solveWaveRefKernel<<<divUp(e - b, 128), 128, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, minPen, elapsed,
+				                                                         last && outBroken ? ws->broken.ptr : nullptr);
 		}
 	};
 	for(uint32_t it = 0; it < nbPos; it++)
 	{
-		if(n) sweep(-FLT_MAX);
+		if(n) sweep(-FLT_MAX, !nbVel && it + 1 == nbPos);
 		if(nbIntegrate) tgs::integrateRefKernel<<<divUp(nbIntegrate, 128), 128, 0, s>>>(ws->vel.ptr, ws->tx.ptr, nbIntegrate, dt);
 		elapsed += dt;
 	}
 	for(uint32_t it = 0; it < nbVel; it++)
-		if(n) sweep(0.0f);
+		if(n) sweep(0.0f, it + 1 == nbVel);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyVel, ws->vel.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyTxI, ws->tx.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
 	if(n) GBPX_CUDA_TRY(cudaMemcpyAsync(rows, ws->recs.ptr, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
+	if(n && outBroken) GBPX_CUDA_TRY(cudaMemcpyAsync(outBroken, ws->broken.ptr, size_t(n) * 4, cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 	return GBPX_OK;
 }

@@ -1529,6 +1529,18 @@ GBPX_API int gbpx_world_stats(void* wv, uint64_t* out4)
 	return GBPX_OK;
 }
 
+// Pairs of each pair kind in the last step (sphere-sphere, sphere-plane,
+// sphere-capsule, sphere-box, plane-capsule, plane-box, capsule-capsule,
+// capsule-box, box-box): 9 counts.
+GBPX_API int gbpx_world_kind_counts(void* wv, uint32_t* out9)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !out9) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(out9, w->workCounter.ptr + 8, 9 * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
 // Average device time of each kernel of a step over nbSteps un-captured steps
 // (CUDA events between the launches on the world's stream), in launch order:
 // broadphase, the narrowphase kernels per pair kind, batching, row

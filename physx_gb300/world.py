@@ -40,6 +40,7 @@ def _setup():
         L.gbpx_world_time_steps.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_time_plain.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_kind_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gbpx_world_time_stages.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_float)]
@@ -126,6 +127,12 @@ class World:
         out = np.zeros(4, np.uint64)
         check(self._L.gbpx_world_stats(self._h, _p(out)), "gbpx_world_stats")
         return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]), row_bytes=int(out[3]))
+
+    def kind_counts(self):
+        """Pairs of each pair kind in the last step, {narrowphase stage name: pairs}."""
+        out = np.zeros(9, np.uint32)
+        check(self._L.gbpx_world_kind_counts(self._h, _p(out)), "gbpx_world_kind_counts")
+        return dict(zip(self.STAGES[1:10], (int(x) for x in out)))
 
     STAGES = ("broadphase", "np sphere-sphere", "np sphere-plane", "np sphere-capsule", "np sphere-box", "np plane-capsule",
               "np plane-box", "np capsule-capsule", "np capsule-box", "np box-box", "batching", "row preparation", "solve")

@@ -1,10 +1,16 @@
-"""libgbpx_immediate.so as a drop-in for the reference's immediate-mode TGS path:
-tests/immediate_dropin.cpp is one frame written against the reference's
-interface (PxGenerateContacts, PxConstructSolverBodiesTGS,
-PxConstructStaticSolverBodyTGS, PxBatchConstraintsTGS,
-PxCreateContactConstraintsTGS, PxSolveConstraintsTGS,
-PxIntegrateSolverBodiesTGS) linked against this library; its result matches the
-CPU oracle's frame on the same scene."""
+"""libgbpx_immediate.so as a drop-in for the reference's immediate-mode TGS path.
+Programs written against the reference's interface (PxGenerateContacts,
+PxConstructSolverBodiesTGS, PxConstructStaticSolverBodyTGS,
+PxBatchConstraintsTGS, PxCreateContactConstraintsTGS, PxSolveConstraintsTGS,
+PxIntegrateSolverBodiesTGS) are linked against this library:
+
+* tests/immediate_dropin.cpp, one frame with fresh caches, matches the CPU
+  oracle's frame on the same scene;
+* tests/immediate_contacts.cpp, PxGenerateContacts with PxCache memory kept
+  between frames, matches the reference's own outputs (pcm_cached.npz);
+* tests/immediate_dropin_frames.cpp, frames of one scene in the snippet's
+  persistent mode (pair caches and friction data carried from frame to frame),
+  matches the oracle's persistent frames step by step."""
 import os
 import shutil
 import subprocess
@@ -20,11 +26,11 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _build(tmp):
-    exe = os.path.join(tmp, "immediate_dropin")
+def _build(tmp, name="immediate_dropin"):
+    exe = os.path.join(tmp, name)
     lib_dir = os.path.join(ROOT, "physx_gb300")
-    subprocess.check_call([shutil.which("g++") or "g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-                           os.path.join(ROOT, "tests", "immediate_dropin.cpp"), "-o", exe, "-L", lib_dir, "-lgbpx_immediate",
+    subprocess.check_call([shutil.which("g++") or "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", name + ".cpp"), "-o", exe, "-L", lib_dir, "-lgbpx_immediate",
                            "-Wl,-rpath," + lib_dir])
     return exe
 
@@ -51,3 +57,73 @@ def test_immediate_frame_matches_oracle(cuda_device, tmp_path, shapes):
     vel, pose, _, _, _ = run_tgs("orc", sc, a, b, s, c, ct, mat)
     assert velocity_error(vel, res[:, :6]) <= 1e-5
     assert np.abs(pose - res[:, 6:]).max() <= 1e-6
+
+
+def test_immediate_cached_contacts_match_reference_golden(cuda_device, tmp_path):
+    """PxGenerateContacts with caches kept between 8 moving frames: the reference's
+    counts every frame and every value within the contact tolerance."""
+    from contact_compare import CONTACT_TOL, unpack
+    from test_oracle_golden import GOLDEN, load_np_cached_fixture
+    exe = _build(str(tmp_path), "immediate_contacts")
+    pairs, frames = load_np_cached_fixture(os.path.join(GOLDEN, "pcm_cached.npz"))
+    n = len(pairs["type0"])
+    geom = np.concatenate([np.asarray(pairs["geom0"], np.float32), np.asarray(pairs["geom1"], np.float32)], 1)
+    blob = [np.array([n, len(frames)], np.uint32).tobytes(), np.asarray(pairs["type0"], np.int32).tobytes(),
+            np.asarray(pairs["type1"], np.int32).tobytes(), np.ascontiguousarray(geom).tobytes()]
+    for fr in frames:
+        blob += [np.ascontiguousarray(fr["pose0"], np.float32).tobytes(), np.ascontiguousarray(fr["pose1"], np.float32).tobytes()]
+    out = subprocess.run([exe], input=b"".join(blob), capture_output=True, check=True).stdout
+    words = np.frombuffer(out, np.uint32)
+    k = 0
+    for f, fr in enumerate(frames):
+        ref = unpack(fr["counts"], fr["contacts"])
+        for i in range(n):
+            c = int(words[k])
+            k += 1
+            assert c == fr["counts"][i], (f, i)
+            got = words[k:k + 8 * c].view(np.float32).reshape(c, 8)
+            k += 8 * c
+            if c:
+                assert np.abs(got[:, :7] - ref[i][:, :7]).max() <= CONTACT_TOL, (f, i)
+    assert k == len(words)
+
+
+@pytest.mark.parametrize("seed", [121, 122])
+def test_immediate_persistent_frames_match_oracle(cuda_device, tmp_path, seed):
+    """Ten frames of a pile through the drop-in the way the snippet runs its
+    persistent mode (PxCache per pair, friction data handed back through
+    PxTGSSolverContactDesc::frictionPtr/frictionCount) against the oracle's
+    persistent frames, frame by frame.  Each oracle frame starts from the bodies
+    the drop-in wrote the frame before, while both sides keep their own pair state
+    (caches, friction patches): the per-frame bar holds for the carried state, and
+    the last-ulp differences of sin/cos in the integration (device libm against
+    the host's) cannot grow over frames into a chaotic separation of the pile."""
+    from oracle_libs import PersistentScenes
+    from physx_gb300.world import DEFAULT_PARAMS
+    from scenarios import pile_scenes
+    from test_oracle_golden import rigid_velocity
+    exe = _build(str(tmp_path), "immediate_dropin_frames")
+    frames = 10
+    sc = pile_scenes(seed, 1, 60)
+    n, m = int(sc["body_count"][0]), int(sc["static_count"][0])
+    p = DEFAULT_PARAMS
+    params = np.array([p["dt"], *p["gravity"], p["contact_distance"], p["tolerance_length"], p["bounds_margin"], p["bounce_threshold"],
+                       p["friction_offset_threshold"], p["correlation_distance"], p["static_friction"]], np.float32)
+    blob = b"".join([np.array([n, m, frames], np.uint32).tobytes(), np.ascontiguousarray(sc["rigid"]).tobytes(),
+                     np.ascontiguousarray(sc["types"], np.int32).tobytes(), np.ascontiguousarray(sc["geoms"], np.float32).tobytes(),
+                     np.ascontiguousarray(sc["friction"], np.float32).tobytes(), np.ascontiguousarray(sc["static_poses"], np.float32).tobytes(),
+                     np.ascontiguousarray(sc["static_types"], np.int32).tobytes(), np.ascontiguousarray(sc["static_geoms"], np.float32).tobytes(),
+                     params.tobytes()])
+    out = subprocess.run([exe], input=blob, capture_output=True, check=True).stdout
+    rb_bytes = sc["rigid"].dtype.itemsize * n
+    assert len(out) == frames * (rb_bytes + 4)
+    orc = PersistentScenes("orc", sc, DEFAULT_PARAMS)
+    for f in range(frames):
+        chunk = out[f * (rb_bytes + 4):(f + 1) * (rb_bytes + 4)]
+        got = np.frombuffer(chunk[:rb_bytes], sc["rigid"].dtype)
+        assert int(np.frombuffer(chunk[rb_bytes:], np.uint32)[0]) > 0
+        ref = orc.step().copy()
+        orc.rb[:] = got
+        assert velocity_error(rigid_velocity(ref), rigid_velocity(got)) <= 1e-5, f
+        assert np.abs(got["p"] - ref["p"]).max() <= 1e-6, f
+    orc.release()
