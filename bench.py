@@ -46,10 +46,12 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the Poisson serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="request arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the serving pool")
-    ap.add_argument("--extras", type=int, default=1, help="also measure the pyramid and the 1M-AABB broadphase workloads")
+    ap.add_argument("--extras", type=int, default=1, help="also measure the pyramid, 1M-AABB broadphase and 100k-body scene workloads")
     ap.add_argument("--pyramid-steps", type=int, default=300)
     ap.add_argument("--bp-frames", type=int, default=10)
     ap.add_argument("--bp-cpu-frames", type=int, default=1)
+    ap.add_argument("--large-steps", type=int, default=600, help="frames of the 100k-body single-scene run")
+    ap.add_argument("--large-cpu-frames", type=int, default=1)
     return ap.parse_args()
 
 
@@ -242,6 +244,53 @@ def bench_broadphase(frames, cpu_frames):
                                   sample="%d frames, oracle ABP restatement, one thread" % cpu_frames))
 
 
+def bench_large_scene(steps, cpu_frames):
+    """Single large scene: 100k sphere/box/capsule bodies in a 200 m box above the
+    plane, the full `steps`-frame run through gbpx_scene_* (persistent pair state),
+    then end to end through host memory, and the oracle's persistent frame of the
+    final state on one host thread."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import PersistentScenes
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world, large_scene
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = large_scene()
+    n = len(sc["rigid"])
+    s = Scene(sc)
+    total, stages, chunks, last = 0.0, {}, 0, None
+    for done in range(0, steps, 50):
+        k = min(50, steps - done)
+        ms, st = s.time_steps(k)
+        total += ms * k
+        chunks += 1
+        last = (ms, st, s.stats())
+    ms_step = total / steps
+    tail_ms, tail_stages, tail_stats = last
+    state = s.get_bodies()
+    # end to end: bodies from pinned-free host arrays in and out every frame
+    host_in, host_out = state.copy(), np.empty_like(state)
+    e2e_frames = 10
+    e2e_ms = 0.0
+    for _ in range(e2e_frames):
+        e2e_ms += s.step_host(host_in, host_out, 1)
+        host_in[:] = host_out
+    s.release()
+    ps = PersistentScenes("orc", as_world(dict(sc, rigid=state)), DEFAULT_PARAMS)
+    ps.step(1)   # the first oracle frame builds the pair caches
+    t = time.perf_counter()
+    ps.step(cpu_frames)
+    cpu_s = (time.perf_counter() - t) / cpu_frames
+    ps.release()
+    return dict(workload="one scene of 100k bodies (1/3 spheres r U(0.25,1), 1/3 boxes h U(0.25,1)^3, 1/3 capsules r U(0.2,0.5) hh U(0.25,1)), "
+                         "positions U([-100,100]x[0,200]x[-100,100]) m, random orientations, plane y=0, ABP + contacts + TGS 4/1, dt 1/60",
+                bodies=n, steps=steps, ms_per_step=ms_step, value=n / (ms_step / 1000.0), unit=UNIT,
+                last_50_steps=dict(ms_per_step=tail_ms, stages_ms=tail_stages, **tail_stats),
+                e2e=dict(value=n * e2e_frames / (e2e_ms / 1000.0), unit=UNIT, h2d_bytes_per_step=n * 96, d2h_bytes_per_step=n * 96),
+                cpu_baseline=dict(value=n / cpu_s, unit=UNIT, cores=1, kind="port",
+                                  sample="%d persistent frame(s) of the final state, oracle restatement, one thread" % cpu_frames))
+
+
 def dist_setup(n):
     if n <= 1:
         return 0, 1, None
@@ -397,7 +446,8 @@ def main():
                                (a.serve_rate, a.serve_budget_gb, a.serve_seconds))
     extras = None
     if a.extras:
-        extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames))
+        extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames),
+                      large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],

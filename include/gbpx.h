@@ -237,6 +237,27 @@ int gbpx_server_read_scene(void* server, uint32_t scene, void* outRigidBodies);
 int gbpx_server_stats(void* server, uint64_t* out4);
 void gbpx_host_free(void* p);
 
+/* ---- One large scene (no reference counterpart: the snippet's frame over one
+ * scene of any size, every stage spread over the whole GPU) ----
+ * Layout as one scene of gbpx_world_create (PxRigidBodyData, types, 4-float
+ * geoms and friction per dynamic body; static PxTransforms, types, geoms;
+ * 12 params, 2 iterations).  The broadphase is the ABP of gbpx_bp_* with every
+ * dynamic body updated each frame; PxBatchConstraintsTGS runs on the host. */
+int gbpx_scene_create(uint32_t nbDyn, const void* rigidBodies, const int* types, const float* geoms, const float* friction, uint32_t nbStatic,
+                      const float* staticPoses, const int* staticTypes, const float* staticGeoms, const float* params, const uint32_t* iterations,
+                      void** outScene);
+void gbpx_scene_release(void* scene);
+int gbpx_scene_step(void* scene, uint32_t nbSteps);
+int gbpx_scene_get_bodies(void* scene, void* outRigidBodies);
+int gbpx_scene_set_bodies(void* scene, const void* rigidBodies);
+/* out4: pairs, constraints, contacts, partitions of the last step */
+int gbpx_scene_stats(void* scene, uint64_t* out4);
+/* outMs[0] = ms per frame, outMs[1..6] per stage: bounds + broadphase,
+ * narrowphase, constraint list + batching, bodies + rows, iterations, write-back */
+int gbpx_scene_time_steps(void* scene, uint32_t nbSteps, float* outMs);
+/* end to end: bodies uploaded from rigidIn, nbSteps frames, downloaded to rigidOut */
+int gbpx_scene_step_host(void* scene, const void* rigidIn, void* rigidOut, uint32_t nbSteps, float* outMs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,37 @@ bool overlap(const float* a, const float* b)
 	if(bminx > amaxx || aminx > bmaxx) return false;
 	return !(b[4] < a[1] || a[4] < b[1] || b[5] < a[2] || a[5] < b[2]);
 }
+
+// Every overlapping pair of the n dynamic and m static boxes except static-static,
+// as (id0 < id1) sorted by (id0, id1).  A sweep over the boxes sorted by encoded
+// min X tests each pair whose X intervals overlap exactly once; the set is the
+// one the all-pairs closed-interval test gives.
+void overlappingPairs(const std::vector<float>& box, uint32_t n, uint32_t m, std::vector<uint32_t>& A, std::vector<uint32_t>& B)
+{
+	const uint32_t total = n + m;
+	std::vector<uint32_t> idx(total);
+	for(uint32_t i = 0; i < total; i++) idx[i] = i;
+	auto minKey = [&](uint32_t i) { return encodeFloat(fbits(box[6 * size_t(i)])); };
+	std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return minKey(a) < minKey(b); });
+	std::vector<uint64_t> keys;
+	for(uint32_t s = 0; s < total; s++)
+	{
+		const uint32_t i = idx[s];
+		const uint32_t maxKey = encodeFloat(fbits(box[6 * size_t(i) + 3]));
+		for(uint32_t t = s + 1; t < total && minKey(idx[t]) <= maxKey; t++)
+		{
+			const uint32_t j = idx[t];
+			if(i >= n && j >= n) continue;   // statics are not paired together
+			if(!overlap(&box[6 * size_t(i)], &box[6 * size_t(j)])) continue;
+			const uint32_t a = i < j ? i : j, b = i < j ? j : i;
+			keys.push_back((uint64_t(a) << 32) | b);
+		}
+	}
+	std::sort(keys.begin(), keys.end());
+	A.resize(keys.size());
+	B.resize(keys.size());
+	for(size_t k = 0; k < keys.size(); k++) { A[k] = uint32_t(keys[k] >> 32); B[k] = uint32_t(keys[k]); }
+}
 } // namespace
 
 // Persistent pair state between frames (the snippet's WITH_PERSISTENCY mode,
@@ -167,13 +198,7 @@ int sceneStep(Persistent* ps, uint32_t nbScenes, const uint32_t* sceneBodyCount,
 		}
 		// every overlapping pair, (id0, id1) order, statics after dynamics
 		std::vector<uint32_t> A, B;
-		for(uint32_t i = 0; i < n; i++)
-		{
-			for(uint32_t j = i + 1; j < n; j++)
-				if(overlap(&box[6 * i], &box[6 * j])) { A.push_back(i); B.push_back(j); }
-			for(uint32_t k = 0; k < m; k++)
-				if(overlap(&box[6 * i], &box[6 * (n + k)])) { A.push_back(i); B.push_back(n + k); }
-		}
+		overlappingPairs(box, n, m, A, B);
 		// order (i, j): dynamic partners come first for each i, then statics (n + k > every j)
 		const size_t np = A.size();
 		std::vector<int> t0(np), t1(np);

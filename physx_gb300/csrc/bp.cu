@@ -22,6 +22,7 @@
 // keys (id0 << 32 | id1, id0 < id1), so created/lost lists come out sorted and
 // deterministic.
 #include "common.cuh"
+#include "bp_internal.h"
 #include "radix_sort.cuh"
 #include <vector>
 #include <algorithm>
@@ -82,6 +83,19 @@ __global__ void applyUpdatesKernel(const UpdateRec* __restrict__ recs, uint32_t 
 	if(r.isCreate) groups[r.id] = r.group;
 	live[r.id] = 1;
 	flags[r.id] |= F_UPDATED;
+}
+
+// Bounds of handles [0, n) from device memory (6 floats each: min xyz, max xyz),
+// distance 0: the large-scene step moves every dynamic body every frame.
+__global__ void applyDeviceBoundsKernel(const float* __restrict__ bounds, uint32_t n, uint2* __restrict__ bx, float4* __restrict__ byz,
+                                        uint8_t* __restrict__ flags)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const float* r = bounds + 6 * size_t(i);
+	bx[i] = make_uint2(encodeFloatBits(__float_as_uint(r[0])), encodeFloatBits(__float_as_uint(r[3])));
+	byz[i] = make_float4(-r[1], -r[2], r[4], r[5]);
+	flags[i] |= F_UPDATED;
 }
 
 // Stable compaction of live handles into (key = encoded min X, value = handle).
@@ -230,10 +244,15 @@ __global__ void sweepUpdatedKernel(const uint32_t* __restrict__ updPos, uint32_t
 
 // Pass 2: one thread per non-updated box; scans the updated boxes that come
 // later in sorted order (pairs whose first box in sorted order did not move).
+// A box whose X range covers more than SLEEP_SCAN_MAX updated boxes (a static
+// ground plane covers all of them) is handed to sweepLongKernel as (box, first,
+// end) so that no thread runs a long serial scan.
+constexpr uint32_t SLEEP_SCAN_MAX = 256;
 __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint32_t nbSleep, const uint32_t* __restrict__ updPos,
                                     uint32_t nbUpd, const uint2* __restrict__ sx, const float4* __restrict__ syz,
                                     const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds, uint32_t lutLo,
-                                    uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
+                                    uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter,
+                                    uint3* __restrict__ longScans, uint32_t* __restrict__ longCount)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31;
@@ -257,6 +276,18 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
 			if(updPos[m] <= p) a = m + 1; else b = m;
 		}
 		lo = a;
+		// end of the candidates: updated boxes' min X keys ascend with their position
+		b = nbUpd;
+		while(a < b)
+		{
+			const uint32_t m = (a + b) >> 1;
+			if(sx[updPos[m]].x <= x0.y) a = m + 1; else b = m;
+		}
+		if(a - lo > SLEEP_SCAN_MAX)
+		{
+			longScans[atomicAdd(longCount, 1u)] = make_uint3(p, lo, a);
+			lo = nbUpd;
+		}
 	}
 	bool more = active && lo < nbUpd;
 	uint32_t j = lo;
@@ -290,6 +321,38 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
 				const uint32_t a = min(id0, idq), b = max(id0, idq);
 				if(slot < cap) out[slot] = (static_cast<unsigned long long>(a) << 32) | b;
 			}
+		}
+	}
+}
+
+// The long scans of pass 2: a block per (box, first, end) item, its threads
+// striding over the candidates.
+__global__ void __launch_bounds__(256) sweepLongKernel(const uint3* __restrict__ longScans, const uint32_t* __restrict__ longCount,
+                                                       const uint32_t* __restrict__ updPos, const uint2* __restrict__ sx,
+                                                       const float4* __restrict__ syz, const uint32_t* __restrict__ sgrp,
+                                                       const uint32_t* __restrict__ sortedIds, uint32_t lutLo, uint32_t lutHi,
+                                                       unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
+{
+	const uint32_t count = *longCount;
+	for(uint32_t item = blockIdx.x; item < count; item += gridDim.x)
+	{
+		const uint3 ls = longScans[item];
+		const uint32_t p = ls.x;
+		const float4 yz0 = syz[p];
+		const uint32_t g0 = sgrp[p];
+		const uint32_t id0 = sortedIds[p];
+		for(uint32_t u0 = ls.y; u0 < ls.z; u0 += blockDim.x)
+		{
+			const uint32_t u = u0 + threadIdx.x;
+			bool hit = false;
+			uint32_t idq = 0;
+			if(u < ls.z)
+			{
+				const uint32_t q = updPos[u];
+				idq = sortedIds[q];
+				hit = overlapYZ(yz0, syz[q]) && groupFilter(g0, sgrp[q], lutLo, lutHi);
+			}
+			emitPairs(__ballot_sync(0xffffffffu, hit), id0, idq, out, cap, counter);
 		}
 	}
 }
@@ -399,6 +462,7 @@ struct BroadPhase
 	DevBuf<uint32_t> sgrp, supd, updPos, sleepPos;
 	DevBuf<unsigned long long> found, foundAlt, prev, next, created, lost;
 	DevBuf<uint32_t> counter, cls, sel, pos;
+	DevBuf<uint3> longScans;
 	DevBuf<uint2> createdPairs, lostPairs;
 	HostBuf<uint32_t> hCounts;
 	HostBuf<uint2> hCreated, hLost;
@@ -442,7 +506,7 @@ struct BroadPhase
 		blockCounts.release(); keysA.release(); valsA.release(); keysB.release(); valsB.release(); hist.release();
 		sx.release(); syz.release(); sgrp.release(); supd.release(); updPos.release(); sleepPos.release();
 		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
-		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release();
+		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release(); longScans.release();
 		hCounts.release(); hCreated.release(); hLost.release();
 		if(stream) cudaStreamDestroy(stream);
 		stream = 0;
@@ -578,10 +642,10 @@ struct BroadPhase
 
 		// 4. Sweep.  The found buffer grows and the sweep reruns if it overflowed.
 		uint32_t nFound = 0;
-		if(found.reserve(1024) || foundAlt.reserve(1024)) return GBPX_ERR_NOMEM;
+		if(found.reserve(1024) || foundAlt.reserve(1024) || longScans.reserve(size_t(nbSleep) + 1)) return GBPX_ERR_NOMEM;
 		for(int attempt = 0; attempt < 3; attempt++)
 		{
-			GBPX_CUDA_TRY(cudaMemsetAsync(counter.ptr, 0, 4, stream));
+			GBPX_CUDA_TRY(cudaMemsetAsync(counter.ptr, 0, 8, stream));
 			const uint32_t capF = uint32_t(std::min<size_t>(found.cap, 0xffffffffu));
 			if(nbUpd)
 			{
@@ -590,9 +654,13 @@ struct BroadPhase
 				bp::sweepUpdatedKernel<<<blocks, 256, 0, stream>>>(updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
 				                                                  found.ptr, capF, counter.ptr);
 				if(nbSleep)
+				{
 					bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
 					                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
-					                                                                 counter.ptr);
+					                                                                 counter.ptr, longScans.ptr, counter.ptr + 1);
+					bp::sweepLongKernel<<<std::min<uint32_t>(nbSleep, 152u * 4u), 256, 0, stream>>>(
+					    longScans.ptr, counter.ptr + 1, updPos.ptr, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF, counter.ptr);
+				}
 			}
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, counter.ptr, 4, cudaMemcpyDeviceToHost, stream));
 			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -666,6 +734,21 @@ struct BroadPhase
 		return GBPX_OK;
 	}
 
+	// Handles [0, n) (already created) take new bounds from device memory and are
+	// marked updated; the frame runs at once and its active set stays on the
+	// device (activePairs).  The created/lost lists are not fetched.
+	int updateFromDevice(const float* dBounds, uint32_t n)
+	{
+		if(pending || n > capacity) return GBPX_ERR_STATE;
+		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
+		if(n) bp::applyDeviceBoundsKernel<<<divUp(n, 256), 256, 0, stream>>>(dBounds, n, bx.ptr, byz.ptr, flags.ptr);
+		const int rc = runFrame(n);
+		if(rc) return rc;
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		pending = false;
+		return GBPX_OK;
+	}
+
 	int fetchResults(const uint2** outCreated, uint32_t* nbCreated, const uint2** outLost, uint32_t* nbLost)
 	{
 		if(!pending) return GBPX_ERR_STATE;
@@ -682,6 +765,21 @@ struct BroadPhase
 } // namespace gbpx
 
 using gbpx::BroadPhase;
+
+namespace gbpx
+{
+namespace bpi
+{
+int updateFromDevice(void* bp, const float* dBounds, uint32_t n) { return static_cast<BroadPhase*>(bp)->updateFromDevice(dBounds, n); }
+const unsigned long long* activePairs(void* bp, uint32_t* count)
+{
+	BroadPhase* b = static_cast<BroadPhase*>(bp);
+	*count = b->nPrev;
+	return b->prev.ptr;
+}
+cudaStream_t stream(void* bp) { return static_cast<BroadPhase*>(bp)->stream; }
+} // namespace bpi
+} // namespace gbpx
 
 GBPX_API int gbpx_bp_create(int discardStaticVsKinematic, int discardKinematicVsKinematic, void** outBp)
 {

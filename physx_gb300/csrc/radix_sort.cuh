@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(THREADS) histogramKernel(const K* __restrict__
 }
 
 // Exclusive scan of `count` u32 values in place by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) scanKernel(uint32_t* __restrict__ data, uint32_t count)
+static __global__ void __launch_bounds__(1024) scanKernel(uint32_t* __restrict__ data, uint32_t count)
 {
 	__shared__ uint32_t warpSums[32];
 	__shared__ uint32_t carry;

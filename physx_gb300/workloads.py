@@ -90,6 +90,39 @@ def batched_scenes(seed, nb_scenes, nmin=8, nmax=512, shapes=(0, 2, 3), drop=(1.
                 static_geoms=np.zeros((S, 4), np.float32))
 
 
+def large_scene(seed=2, n=100_000, extent=100.0, height=200.0, friction=(0.3, 0.8)):
+    """Single large scene: n bodies, 1/3 spheres r ~ U(0.25, 1), 1/3 boxes with
+    half-extents ~ U(0.25, 1) per axis, 1/3 capsules r ~ U(0.2, 0.5), half-height
+    ~ U(0.25, 1); positions U([-extent, extent] x [0, height] x [-extent, extent]),
+    Haar-uniform orientations, zero velocity, friction U(friction), density 1000,
+    on the plane y = 0.  Initial overlaps are allowed."""
+    rng = np.random.default_rng(seed)
+    types = np.array([0, 3, 2], np.int32)[np.arange(n) % 3]
+    rng.shuffle(types)
+    geoms = np.zeros((n, 4), np.float32)
+    sph, box, cap = types == 0, types == 3, types == 2
+    geoms[sph, 0] = rng.uniform(0.25, 1.0, int(sph.sum()))
+    geoms[box, :3] = rng.uniform(0.25, 1.0, (int(box.sum()), 3))
+    geoms[cap, 0] = rng.uniform(0.2, 0.5, int(cap.sum()))
+    geoms[cap, 1] = rng.uniform(0.25, 1.0, int(cap.sum()))
+    rb = rigid_body_data(n)
+    rb["q"] = random_quat(rng, n)
+    rb["p"][:, 0] = rng.uniform(-extent, extent, n)
+    rb["p"][:, 1] = rng.uniform(0.0, height, n)
+    rb["p"][:, 2] = rng.uniform(-extent, extent, n)
+    im, ii = mass_properties_batch(types, geoms)
+    rb["invMass"] = im
+    rb["invInertia"] = ii
+    fr = rng.uniform(friction[0], friction[1], n).astype(np.float32)
+    return dict(rigid=rb, types=types, geoms=geoms, friction=fr, static_poses=np.array([plane_pose_y_up()], np.float32),
+                static_types=np.ones(1, np.int32), static_geoms=np.zeros((1, 4), np.float32))
+
+
+def as_world(scene):
+    """One scene's arrays as a one-scene world (body_count / static_count added)."""
+    return dict(scene, body_count=np.array([len(scene["types"])], np.uint32),
+                static_count=np.array([len(scene["static_types"])], np.uint32))
+
 
 def mass_properties_batch(types, geoms, density=1000.0):
     """Vectorised mass_properties: (invMass (n,), invInertia (n, 3))."""

@@ -49,8 +49,8 @@ def declared_arity():
 
 def test_python_bindings_match_header_arity(gbpx_built):
     """Every ctypes prototype the Python mirror installs has the header's parameter count."""
-    from physx_gb300 import broadphase, contacts, lib, server, solver, world
-    for mod in (broadphase, contacts, server, solver, world):
+    from physx_gb300 import broadphase, contacts, lib, scene, server, solver, world
+    for mod in (broadphase, contacts, scene, server, solver, world):
         mod._setup()
     L = lib()
     arity = declared_arity()

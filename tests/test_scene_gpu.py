@@ -1,0 +1,101 @@
+"""One large scene on the GB300 (gbpx_scene_*): the reference snippet's frame
+over one scene with every stage spread over the GPU, the ABP broadphase of
+gbpx_bp, PxBatchConstraintsTGS on the host.  Checked against the batched world
+(the same arithmetic: identical bytes), against the CPU oracle frame by frame
+(persistent and fresh), and at the full 100k-body size against one oracle frame."""
+import numpy as np
+import pytest
+
+from oracle_libs import PersistentScenes, run_scene_step
+from test_oracle_golden import rigid_velocity, velocity_error
+
+pytestmark = pytest.mark.gpu
+
+
+def _pile(seed, n):
+    from scenarios import random_scene
+    # n bodies spread over the plane, most of them touching it or each other
+    return random_scene(seed, n)
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_scene_equals_world(cuda_device, persistent):
+    """The large-scene step and the batched world produce the same bytes for the
+    same scene over 12 steps (same device functions, same batching order)."""
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world
+    from physx_gb300.world import World
+    sc = _pile(131, 400)
+    s = Scene(sc, persistent=persistent)
+    w = World(as_world(sc), persistent=persistent)
+    for step in range(12):
+        s.step(1)
+        w.step(1)
+        a, b = s.get_bodies(), w.get_bodies()
+        assert a.tobytes() == b.tobytes(), step
+    assert s.stats()["constraints"] > 100
+    s.release()
+    w.release()
+
+
+def test_scene_persistent_steps_match_oracle(cuda_device):
+    """Persistent frames against the oracle's persistent frames, step by step; the
+    oracle's bodies are set to the device's after every step (pair state stays each
+    side's own), so last-ulp sin/cos differences cannot grow chaotically."""
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = _pile(132, 3000)
+    s = Scene(sc)
+    orc = PersistentScenes("orc", as_world(sc), DEFAULT_PARAMS)
+    for step in range(8):
+        s.step(1)
+        out = s.get_bodies()
+        ref = orc.step().copy()
+        orc.rb[:] = out
+        assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5, step
+        assert np.abs(out["p"] - ref["p"]).max() <= 1e-6, step
+    st = s.stats()
+    assert st["constraints"] > 1000 and st["partitions"] > 4
+    orc.release()
+    s.release()
+
+
+def test_scene_fresh_step_matches_oracle(cuda_device):
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = _pile(133, 2000)
+    s = Scene(sc, persistent=False)
+    rb = sc["rigid"].copy()
+    for step in range(4):
+        s.set_bodies(rb)
+        s.step(1)
+        out = s.get_bodies()
+        ref = run_scene_step("orc", as_world(dict(sc, rigid=rb)), dict(DEFAULT_PARAMS, persistent=False), steps=1)
+        assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5, step
+        assert np.abs(out["p"] - ref["p"]).max() <= 1e-6, step
+        rb = out.copy()
+    s.release()
+
+
+def test_scene_100k_bodies_step_matches_oracle(cuda_device):
+    """The single-large-scene workload at its full size (100k bodies in a 200 m box
+    above the plane, initial overlaps allowed): after a short pre-roll, one frame
+    from the same state against the oracle's frame."""
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world, large_scene
+    from physx_gb300.world import DEFAULT_PARAMS
+    sc = large_scene()
+    s = Scene(sc, persistent=False)
+    s.step(3)
+    rb = s.get_bodies()
+    s.step(1)
+    out = s.get_bodies()
+    st = s.stats()
+    ref = run_scene_step("orc", as_world(dict(sc, rigid=rb)), dict(DEFAULT_PARAMS, persistent=False), steps=1)
+    assert st["pairs"] > 100_000 and st["constraints"] > 1000
+    assert np.isfinite(out["p"]).all()
+    assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5
+    assert np.abs(out["p"] - ref["p"]).max() <= 1e-6
+    s.release()
