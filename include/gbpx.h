@@ -189,7 +189,7 @@ int gbpx_world_get_bodies(void* world, void* outRigidBodies);
 int gbpx_world_set_bodies(void* world, const void* rigidBodies);
 int gbpx_world_status(void* world, uint32_t* outStatus);
 /* out8: scenes, dynamic bodies, statics, pair slots, broadphase grid blocks,
- * device bytes, kernels launched per step, 0 */
+ * device bytes, kernels launched per step, large-scene threshold */
 int gbpx_world_info(void* world, uint64_t* out8);
 int gbpx_world_scene_pairs(void* world, uint32_t scene, uint32_t* outKeys, uint32_t* outContactCounts, uint32_t capacity,
                            uint32_t* outCount);
@@ -197,6 +197,10 @@ int gbpx_world_time_steps(void* world, uint32_t nbSteps, int useGraph, float* ou
 int gbpx_world_time_plain(void* world, uint32_t firstScene, uint32_t nbScenes, float* outMs);
 /* out4: pairs, pairs with contacts, contacts, bytes of packed constraint rows (last step) */
 int gbpx_world_stats(void* world, uint64_t* out4);
+/* Scenes of more than largeBodies solver bodies (bodies + statics) run the
+ * broadphase, batching and solve one block (8 warps) per scene, smaller scenes
+ * one warp per scene; default 512.  Results do not depend on it. */
+int gbpx_world_set_large_bodies(void* world, uint32_t largeBodies);
 /* Pairs of each pair kind in the last step, in the kind order of the
  * narrowphase launches (sphere-sphere ... box-box): 9 counts. */
 int gbpx_world_kind_counts(void* world, uint32_t* out9);

@@ -17,6 +17,7 @@ struct StepParams
 	float bounceThreshold, frictionOffsetThreshold, correlationDistance, staticFriction;
 	uint32_t nbPos, nbVel;
 	uint32_t persistent;   // carry contact manifolds and friction patches between steps
+	uint32_t largeBodies;  // scenes of more solver bodies run one block per scene (world)
 };
 
 // no slot in last step's pair list (a new pair)

@@ -100,15 +100,42 @@ struct WorldDev
 	np::ManifoldRecord* manifolds[2];
 	tgs::FrictionState* frictionState[2];
 };
-template <typename K>
-__device__ __forceinline__ void warpBitonicSort(K* keys, uint32_t n)
+// A group of G warps working on one scene: G = 1 is one warp (several scenes
+// per block), G > 1 is the whole block (one scene per block, for large scenes).
+template <uint32_t G>
+struct Grp
 {
-	const uint32_t lane = threadIdx.x & 31;
+	static constexpr uint32_t NT = 32 * G;
+	__device__ static __forceinline__ uint32_t tid() { return G == 1 ? (threadIdx.x & 31) : threadIdx.x; }
+	__device__ static __forceinline__ uint32_t warp() { return G == 1 ? 0u : (threadIdx.x >> 5); }
+	__device__ static __forceinline__ void sync()
+	{
+		if constexpr(G == 1) __syncwarp();
+		else __syncthreads();
+	}
+	// value of thread 0, to every thread of the group (slot: shared scratch word)
+	__device__ static __forceinline__ uint32_t bcast(uint32_t v, volatile uint32_t* slot)
+	{
+		if constexpr(G == 1) return __shfl_sync(0xffffffffu, v, 0);
+		else
+		{
+			if(threadIdx.x == 0) *slot = v;
+			__syncthreads();
+			const uint32_t r = *slot;
+			__syncthreads();
+			return r;
+		}
+	}
+};
+
+template <uint32_t G, typename K>
+__device__ __forceinline__ void groupBitonicSort(K* keys, uint32_t n)
+{
 	for(uint32_t k = 2; k <= n; k <<= 1)
 	{
 		for(uint32_t j = k >> 1; j > 0; j >>= 1)
 		{
-			for(uint32_t i = lane; i < n; i += 32)
+			for(uint32_t i = Grp<G>::tid(); i < n; i += Grp<G>::NT)
 			{
 				const uint32_t ixj = i ^ j;
 				if(ixj > i)
@@ -118,31 +145,20 @@ __device__ __forceinline__ void warpBitonicSort(K* keys, uint32_t n)
 					if(up ? (a > b) : (a < b)) { keys[i] = b; keys[ixj] = a; }
 				}
 			}
-			__syncwarp();
+			Grp<G>::sync();
 		}
 	}
 }
 
-// Per-warp shared-memory workspace of the broadphase: scenes of up to
-// BP_SMEM_BODIES bodies sort and sweep entirely on chip; larger scenes use the
-// same code on their global scratch arrays.
-constexpr uint32_t BP_SMEM_BODIES = 512;
-constexpr uint32_t STAGE_WARPS = 4;   // warps (scenes in flight) per block of the scene kernels
-struct BpSmem
+// Exclusive prefix sum of v[0..n) by one group (each thread scans a run of
+// entries); scratch: G shared words (unused for G = 1).
+template <uint32_t G>
+__device__ __forceinline__ void groupExclusiveScan(uint32_t* v, uint32_t n, uint32_t* scratch)
 {
-	unsigned long long keys[BP_SMEM_BODIES];   // (encoded min X << 32) | body
-	uint32_t maxX[BP_SMEM_BODIES];             // encoded max X
-	float minY[BP_SMEM_BODIES], minZ[BP_SMEM_BODIES], maxY[BP_SMEM_BODIES], maxZ[BP_SMEM_BODIES];
-	uint32_t cnt[BP_SMEM_BODIES];              // pairs per lower body id, then bucket offsets
-	uint32_t found;
-};
-
-// Exclusive prefix sum of v[0..n) by one warp (each lane scans a run of entries).
-__device__ __forceinline__ void warpExclusiveScan(uint32_t* v, uint32_t n)
-{
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t per = (n + 31) / 32;
-	const uint32_t b0 = min(lane * per, n), b1 = min(b0 + per, n);
+	constexpr uint32_t NT = Grp<G>::NT;
+	const uint32_t tid = Grp<G>::tid(), lane = threadIdx.x & 31;
+	const uint32_t per = (n + NT - 1) / NT;
+	const uint32_t b0 = min(tid * per, n), b1 = min(b0 + per, n);
 	uint32_t sum = 0;
 	for(uint32_t k = b0; k < b1; k++) sum += v[k];
 	uint32_t incl = sum;
@@ -151,6 +167,15 @@ __device__ __forceinline__ void warpExclusiveScan(uint32_t* v, uint32_t n)
 		const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
 		if(lane >= uint32_t(o)) incl += t;
 	}
+	if constexpr(G > 1)
+	{
+		const uint32_t warp = Grp<G>::warp();
+		if(lane == 31) scratch[warp] = incl;
+		__syncthreads();
+		uint32_t off = 0;
+		for(uint32_t q = 0; q < warp; q++) off += scratch[q];
+		incl += off;
+	}
 	uint32_t run = incl - sum;
 	for(uint32_t k = b0; k < b1; k++)
 	{
@@ -158,8 +183,29 @@ __device__ __forceinline__ void warpExclusiveScan(uint32_t* v, uint32_t n)
 		v[k] = run;
 		run += c;
 	}
-	__syncwarp();
+	Grp<G>::sync();
 }
+
+// Shared-memory workspace of the broadphase of one scene: scenes whose sort
+// keys fit (CAP) sort and sweep entirely on chip; larger scenes use the same
+// code on their global scratch arrays.  Warp groups use BP_SMEM_BODIES, block
+// groups (large scenes) BIG_BP_BODIES.
+constexpr uint32_t BP_SMEM_BODIES = 512;
+constexpr uint32_t BIG_BP_BODIES = 4096;
+constexpr uint32_t STAGE_WARPS = 4;   // warps (scenes in flight) per block of the warp-per-scene kernels
+constexpr uint32_t BIG_WARPS = 8;     // warps per block (one scene) of the large-scene kernels
+template <uint32_t CAP>
+struct BpSmemT
+{
+	unsigned long long keys[CAP];   // (encoded min X << 32) | body
+	uint32_t maxX[CAP];             // encoded max X
+	float minY[CAP], minZ[CAP], maxY[CAP], maxZ[CAP];
+	uint32_t cnt[CAP];              // pairs per lower body id, then bucket offsets
+	uint32_t found, bc;
+	uint32_t scan[32];
+};
+using BpSmem = BpSmemT<BP_SMEM_BODIES>;
+using BpSmemBig = BpSmemT<BIG_BP_BODIES>;
 
 // Bounds, ABP-equivalent overlap search and the pair list of one scene, sorted
 // by (id0, id1) with statics numbered after the dynamic bodies.
@@ -167,11 +213,13 @@ __device__ __forceinline__ void warpExclusiveScan(uint32_t* v, uint32_t n)
 // overlap on encoded keys, Y/Z as closed float intervals.  Found pairs are
 // counted per lower id, scattered into their buckets and each bucket sorted by
 // the upper id, which yields the same order as sorting the whole list.
-__device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, BpSmem& sm)
+template <uint32_t G, uint32_t CAP>
+__device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, BpSmemT<CAP>& sm)
 {
-	const uint32_t lane = threadIdx.x & 31;
+	constexpr uint32_t NT = Grp<G>::NT;
+	const uint32_t tid = Grp<G>::tid(), lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies, m = sc.nbStatics;
-	const bool onChip = sc.keyCap <= BP_SMEM_BODIES;
+	const bool onChip = sc.keyCap <= CAP;
 	unsigned long long* keys = onChip ? sm.keys : w.keys + sc.keyStart;
 	float* ga = w.aabb + 6 * size_t(sc.bodyStart);
 	uint32_t* maxX = onChip ? sm.maxX : reinterpret_cast<uint32_t*>(ga);
@@ -185,10 +233,10 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 	{
 		// last step's pair list, for matching this step's pairs to their state
 		const uint32_t prevCount = w.pairCount[sid];
-		for(uint32_t t = lane; t < prevCount; t += 32) w.pairsPrev[sc.pairStart + t] = w.pairs[sc.pairStart + t];
-		if(lane == 0) w.pairCountPrev[sid] = prevCount;
+		for(uint32_t t = tid; t < prevCount; t += NT) w.pairsPrev[sc.pairStart + t] = w.pairs[sc.pairStart + t];
+		if(tid == 0) w.pairCountPrev[sid] = prevCount;
 	}
-	for(uint32_t i = lane; i < sc.keyCap; i += 32)
+	for(uint32_t i = tid; i < sc.keyCap; i += NT)
 	{
 		if(i < n)
 		{
@@ -208,12 +256,12 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 		else
 			keys[i] = ~0ull;
 	}
-	if(lane == 0) sm.found = 0;
-	__syncwarp();
-	warpBitonicSort(keys, sc.keyCap);
+	if(tid == 0) sm.found = 0;
+	Grp<G>::sync();
+	groupBitonicSort<G>(keys, sc.keyCap);
 	uint32_t* scratch = w.ordered + sc.pairStart;   // unsorted pairs (the slot array is free until the solve)
-	uint32_t local = 0;   // lane-private overflow flag
-	for(uint32_t p = lane; p < n; p += 32)
+	uint32_t local = 0;   // thread-private overflow flag
+	for(uint32_t p = tid; p < n; p += NT)
 	{
 		const unsigned long long kp = keys[p];
 		const uint32_t i = uint32_t(kp);
@@ -247,19 +295,19 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 			}
 		}
 	}
-	__syncwarp();
-	if(__any_sync(0xffffffffu, local) && lane == 0) atomicOr(&w.status[sid], ST_PAIR_OVERFLOW);
+	Grp<G>::sync();
+	if(local) atomicOr(&w.status[sid], ST_PAIR_OVERFLOW);
 	const uint32_t count = min(sm.found, sc.pairCap);
 	// bucket by lower id, then sort each bucket by upper id
-	warpExclusiveScan(cnt, n);
+	groupExclusiveScan<G>(cnt, n, sm.scan);
 	uint32_t* pairs = w.pairs + sc.pairStart;
-	for(uint32_t t = lane; t < count; t += 32)
+	for(uint32_t t = tid; t < count; t += NT)
 	{
 		const uint32_t key = scratch[t];
 		pairs[atomicAdd(&cnt[key >> 16], 1u)] = key;
 	}
-	__syncwarp();
-	for(uint32_t lo = lane; lo < n; lo += 32)
+	Grp<G>::sync();
+	for(uint32_t lo = tid; lo < n; lo += NT)
 	{
 		const uint32_t b0 = lo ? cnt[lo - 1] : 0, b1 = cnt[lo];
 		for(uint32_t x = b0 + 1; x < b1; x++)
@@ -270,10 +318,10 @@ __device__ __forceinline__ void sceneBroadphase(const WorldDev& w, const SceneDe
 			pairs[y] = v;
 		}
 	}
-	if(lane == 0) w.pairCount[sid] = count;
-	__syncwarp();
+	if(tid == 0) w.pairCount[sid] = count;
+	Grp<G>::sync();
 	// queue every pair slot under its pair kind (one atomic per kind per 32 pairs)
-	for(uint32_t base = 0; base < count; base += 32)
+	for(uint32_t base = Grp<G>::warp() * 32; base < count; base += NT)
 	{
 		const uint32_t k = base + lane;
 		const bool valid = k < count;
@@ -378,33 +426,61 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 	}
 }
 
-// Per-warp shared-memory workspace of the solve: batching state per solver
-// body (scenes of up to SOLVE_SMEM_BODIES solver bodies) and the partition
-// offsets.
+// Shared-memory workspace of the batching of one scene: batching state per
+// solver body and constraint (on chip when the scene fits CAPB bodies and CAPC
+// constraints) and the partition offsets.  Warp groups use SOLVE_SMEM_*,
+// block groups (large scenes) BIG_SOLVE_*.
 constexpr uint32_t SOLVE_SMEM_BODIES = 544;
 constexpr uint32_t SOLVE_SMEM_CONSTRAINTS = 1024;
-struct SolveSmem
+constexpr uint32_t BIG_SOLVE_BODIES = 4160;
+constexpr uint32_t BIG_SOLVE_CONSTRAINTS = 8192;
+template <uint32_t CAPB, uint32_t CAPC>
+struct SolveSmemT
 {
-	uint32_t progress[SOLVE_SMEM_BODIES];        // partition bits of the current round
-	uint32_t maxNormal[SOLVE_SMEM_BODIES];       // 1 + last dynamic partition of the body
-	uint32_t maxStatic[SOLVE_SMEM_BODIES];       // static constraints of the body
-	uint32_t staticProgress[SOLVE_SMEM_BODIES];
+	uint32_t progress[CAPB];        // partition bits of the current round
+	uint32_t maxNormal[CAPB];       // 1 + last dynamic partition of the body
+	uint32_t maxStatic[CAPB];       // static constraints of the body
+	uint32_t staticProgress[CAPB];
 	uint32_t perPart[MAX_PARTITIONS];            // constraints per partition, then end offsets
-	uint32_t keys[SOLVE_SMEM_CONSTRAINTS];       // pair key of each constraint, in constraint order
-	uint16_t tags[SOLVE_SMEM_CONSTRAINTS];       // (round << 8) | partition; 0x8000 | rank for static constraints
+	uint32_t keys[CAPC];                         // pair key of each constraint, in constraint order
+	uint16_t tags[CAPC];                         // (round << 8) | partition; 0x8000 | rank for static constraints
 	uint32_t bucket[MAX_PARTITIONS * 4];         // (partition, placement round) counts, then offsets
+	uint32_t scan[32];
+	uint32_t red, bc;
 };
+using SolveSmem = SolveSmemT<SOLVE_SMEM_BODIES, SOLVE_SMEM_CONSTRAINTS>;
+using SolveSmemBig = SolveSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS>;
+
+// Maximum of v over the group (slot: shared scratch word).
+template <uint32_t G>
+__device__ __forceinline__ uint32_t groupMax(uint32_t v, uint32_t* slot)
+{
+	for(int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+	if constexpr(G == 1) return v;
+	else
+	{
+		if(threadIdx.x == 0) *slot = 0;
+		__syncthreads();
+		if((threadIdx.x & 31) == 0) atomicMax(slot, v);
+		__syncthreads();
+		const uint32_t r = *slot;
+		__syncthreads();
+		return r;
+	}
+}
 
 // PxBatchConstraintsTGS partition rule for one scene (the rule is sequential
 // in constraint order; batching.h cites the reference): one lane walks the
-// constraints, the warp does the parallel bookkeeping.  Fills ordered[] (pair
+// constraints, the group does the parallel bookkeeping.  Fills ordered[] (pair
 // indices in solve order) and the partition end offsets in perPart; returns
 // the partition count (all lanes), 0 on overflow.
-__device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t nc, SolveSmem& sm)
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC>
+__device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t nc, SolveSmemT<CAPB, CAPC>& sm)
 {
-	const uint32_t lane = threadIdx.x & 31;
+	constexpr uint32_t NT = Grp<G>::NT;
+	const uint32_t tid = Grp<G>::tid(), lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies;
-	const bool onChip = n + sc.nbStatics <= SOLVE_SMEM_BODIES;
+	const bool onChip = n + sc.nbStatics <= CAPB;
 	uint32_t* progress = onChip ? sm.progress : w.progress + sc.solverStart;
 	uint32_t* maxNormal = onChip ? sm.maxNormal : w.maxNormal + sc.solverStart;
 	uint32_t* maxStatic = onChip ? sm.maxStatic : w.maxStatic + sc.solverStart;
@@ -413,21 +489,21 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 	const uint32_t* cons = w.consList + sc.pairStart;
 	uint32_t* ordered = w.ordered + sc.pairStart;
 	// the walk below is sequential: its operands sit in shared memory when they fit
-	const bool consOnChip = nc <= SOLVE_SMEM_CONSTRAINTS;
-	for(uint32_t b = lane; b < n; b += 32) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
-	for(uint32_t p = lane; p < MAX_PARTITIONS; p += 32) perPart[p] = 0;
+	const bool consOnChip = nc <= CAPC;
+	for(uint32_t b = tid; b < n; b += NT) { progress[b] = 0; maxNormal[b] = 0; maxStatic[b] = 0; staticProgress[b] = 0; }
+	for(uint32_t p = tid; p < MAX_PARTITIONS; p += NT) perPart[p] = 0;
 	if(consOnChip)
-		for(uint32_t c = lane; c < nc; c += 32) { sm.keys[c] = w.pairs[sc.pairStart + cons[c]]; sm.tags[c] = 0; }
+		for(uint32_t c = tid; c < nc; c += NT) { sm.keys[c] = w.pairs[sc.pairStart + cons[c]]; sm.tags[c] = 0; }
 	else
-		for(uint32_t c = lane; c < nc; c += 32) w.tag[sc.pairStart + c] = 0;
-	__syncwarp();
+		for(uint32_t c = tid; c < nc; c += NT) w.tag[sc.pairStart + c] = 0;
+	Grp<G>::sync();
 	auto keyOf = [&](uint32_t c) { return consOnChip ? sm.keys[c] : w.pairs[sc.pairStart + cons[c]]; };
 	auto getTag = [&](uint32_t c) { return consOnChip ? uint32_t(sm.tags[c]) : w.tag[sc.pairStart + c]; };
 	auto setTag = [&](uint32_t c, uint32_t t) { if(consOnChip) sm.tags[c] = uint16_t(t); else w.tag[sc.pairStart + c] = t; };
 	// pass 1: dynamic-dynamic constraints take the lowest free partition bit;
 	// constraints that find none retry in the next round of 32 partitions
 	uint32_t nbPart = 0, maxRound = 0, fail = 0;
-	if(lane == 0)
+	if(tid == 0)
 	{
 		for(uint32_t round = 0;; round++)
 		{
@@ -465,34 +541,34 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 			if(fail || !deferred) break;
 		}
 	}
-	__syncwarp();
-	fail = __shfl_sync(0xffffffffu, fail, 0);
+	Grp<G>::sync();
+	fail = Grp<G>::bcast(fail, &sm.bc);
 	if(fail) return 0;
-	nbPart = __shfl_sync(0xffffffffu, nbPart, 0);
-	maxRound = __shfl_sync(0xffffffffu, maxRound, 0);
+	nbPart = Grp<G>::bcast(nbPart, &sm.bc);
+	maxRound = Grp<G>::bcast(maxRound, &sm.bc);
 	// statics of a body follow its last dynamic partition, one per partition
 	uint32_t need = nbPart;
-	for(uint32_t b = lane; b < n; b += 32)
+	for(uint32_t b = tid; b < n; b += NT)
 	{
 		const uint32_t mn = maxNormal[b], ms = maxStatic[b];
 		need = max(need, mn + ms);
 		if(mn + ms <= MAX_PARTITIONS)
 			for(uint32_t k = 0; k < ms; k++) atomicAdd(&perPart[mn + k], 1u);
 	}
-	for(int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+	need = groupMax<G>(need, &sm.red);
 	if(need > MAX_PARTITIONS) return 0;
 	nbPart = need;
-	__syncwarp();
-	warpExclusiveScan(perPart, nbPart);
+	Grp<G>::sync();
+	groupExclusiveScan<G>(perPart, nbPart, sm.scan);
 	// pass 2: a static constraint goes to partition maxNormal[body] + its rank
 	// among the body's static constraints; within a partition the reference
 	// places round-0 and static constraints in input order, then each later
 	// round's constraints in input order.  That is a stable counting sort by
-	// (partition, placement round), done here by the whole warp.
+	// (partition, placement round): counts by the group, placement by one warp.
 	uint32_t* bucket = sm.bucket;
 	const uint32_t nbBuckets = nbPart * 4;
-	for(uint32_t i = lane; i < nbBuckets; i += 32) bucket[i] = 0;
-	__syncwarp();
+	for(uint32_t i = tid; i < nbBuckets; i += NT) bucket[i] = 0;
+	Grp<G>::sync();
 	auto bucketOf = [&](uint32_t c) -> uint32_t {
 		const uint32_t t = getTag(c);
 		if(t & 0x8000u)
@@ -503,9 +579,10 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 		}
 		return (t & 0xffu) * 4 + (t >> 8);
 	};
-	for(uint32_t c = lane; c < nc; c += 32) atomicAdd(&bucket[bucketOf(c)], 1u);
-	__syncwarp();
-	warpExclusiveScan(bucket, nbBuckets);
+	for(uint32_t c = tid; c < nc; c += NT) atomicAdd(&bucket[bucketOf(c)], 1u);
+	Grp<G>::sync();
+	groupExclusiveScan<G>(bucket, nbBuckets, sm.scan);
+	if(Grp<G>::warp() == 0)
 	for(uint32_t base = 0; base < nc; base += 32)
 	{
 		const uint32_t c = base + lane;
@@ -521,20 +598,23 @@ __device__ uint32_t sceneBatch(const WorldDev& w, const SceneDesc& sc, uint32_t 
 		}
 		__syncwarp();
 	}
+	Grp<G>::sync();
 	// partition end offsets
 	uint32_t endv[MAX_PARTITIONS / 32];
-	for(uint32_t p = lane, k = 0; p < nbPart; p += 32, k++) endv[k] = p + 1 < nbPart ? perPart[p + 1] : nc;
-	__syncwarp();
-	for(uint32_t p = lane, k = 0; p < nbPart; p += 32, k++) perPart[p] = endv[k];
-	__syncwarp();
+	for(uint32_t p = tid, k = 0; p < nbPart; p += NT, k++) endv[k] = p + 1 < nbPart ? perPart[p + 1] : nc;
+	Grp<G>::sync();
+	for(uint32_t p = tid, k = 0; p < nbPart; p += NT, k++) perPart[p] = endv[k];
+	Grp<G>::sync();
 	return nbPart;
 }
 
 // Solver bodies, constraint list and batching of one scene; queues the
 // scene's constraints for row preparation.
-__device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, SolveSmem& sm)
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC>
+__device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, SolveSmemT<CAPB, CAPC>& sm)
 {
-	const uint32_t lane = threadIdx.x & 31;
+	constexpr uint32_t NT = Grp<G>::NT;
+	const uint32_t tid = Grp<G>::tid(), lane = threadIdx.x & 31;
 	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
 	tgs::BodyVel* vel = w.vel + sc.solverStart;
 	tgs::BodyTx* tx = w.tx + sc.solverStart;
@@ -542,7 +622,7 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 	Tr* pose = w.pose + sc.solverStart;
 	const V3 g = v3(sp.gx, sp.gy, sp.gz);
 	// 1. solver bodies (PxConstructSolverBodiesTGS / PxConstructStaticSolverBodyTGS)
-	for(uint32_t i = lane; i < nTot; i += 32)
+	for(uint32_t i = tid; i < nTot; i += NT)
 	{
 		if(i < n)
 		{
@@ -560,19 +640,21 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 	// 2. constraints = pairs with contacts, in pair order
 	const uint32_t count = w.pairCount[sid];
 	uint32_t nc = 0;
-	for(uint32_t base = 0; base < count; base += 32)
-	{
-		const uint32_t k = base + lane;
-		const bool has = k < count && w.contactCount[sc.pairStart + k] > 0;
-		const uint32_t bal = __ballot_sync(0xffffffffu, has);
-		if(has) w.consList[sc.pairStart + nc + __popc(bal & laneMaskLt())] = k;
-		nc += __popc(bal);
-	}
-	__syncwarp();
+	if(Grp<G>::warp() == 0)   // in pair order: one warp
+		for(uint32_t base = 0; base < count; base += 32)
+		{
+			const uint32_t k = base + lane;
+			const bool has = k < count && w.contactCount[sc.pairStart + k] > 0;
+			const uint32_t bal = __ballot_sync(0xffffffffu, has);
+			if(has) w.consList[sc.pairStart + nc + __popc(bal & laneMaskLt())] = k;
+			nc += __popc(bal);
+		}
+	Grp<G>::sync();
+	nc = Grp<G>::bcast(nc, &sm.bc);
 	// 3. batching
-	const uint32_t nbPart = sceneBatch(w, sc, nc, sm);
-	for(uint32_t p = lane; p < nbPart; p += 32) w.partEnds[size_t(sid) * MAX_PARTITIONS + p] = sm.perPart[p];
-	if(lane == 0)
+	const uint32_t nbPart = sceneBatch<G>(w, sc, nc, sm);
+	for(uint32_t p = tid; p < nbPart; p += NT) w.partEnds[size_t(sid) * MAX_PARTITIONS + p] = sm.perPart[p];
+	if(tid == 0)
 	{
 		w.nbConstraints[sid] = nc;
 		w.nbPartitions[sid] = nbPart;
@@ -580,14 +662,14 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 	}
 	if(!nbPart) return;   // nothing to solve, or overflow: the scene is left unchanged
 	uint32_t qbase = 0;
-	if(lane == 0) qbase = atomicAdd(&w.workCounter[3], nc);
-	qbase = __shfl_sync(0xffffffffu, qbase, 0);
+	if(tid == 0) qbase = atomicAdd(&w.workCounter[3], nc);
+	qbase = Grp<G>::bcast(qbase, &sm.bc);
 	// PxBatchConstraintsTGS's headers are runs of up to 4 consecutive constraints
 	// of one partition (createHeaders, NpImmediateMode.cpp:159; every partition
 	// here is non-empty, so each one is below its maxPartition); full runs of 4
 	// take the 4-wide block path (<= 16 contacts, under its 64-contact limit).
 	// Bit 31 of the queue entry marks those constraints.
-	for(uint32_t r = lane; r < nc; r += 32)
+	for(uint32_t r = tid; r < nc; r += NT)
 	{
 		uint32_t lo = 0, hi = nbPart - 1;   // first partition whose end is above r
 		while(lo < hi)
@@ -655,19 +737,15 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, cons
 
 // Velocities of one scene's solver bodies during the iterations: linear and
 // (momentum-space) angular velocity, the values every constraint solve
-// reads and writes.  Scenes of up to SOLVE_SMEM_BODIES solver bodies keep
-// them in shared memory; larger scenes use the BodyVel records in HBM.
-struct VelSmem
-{
-	V3 lin[SOLVE_SMEM_BODIES];
-	V3 ang[SOLVE_SMEM_BODIES];
-};
+// reads and writes.  Scenes that fit the workspace keep them in shared
+// memory; larger scenes use the BodyVel records in HBM.
 struct SharedVel
 {
-	VelSmem& s;
-	__device__ __forceinline__ V3 lin(uint32_t i) const { return s.lin[i]; }
-	__device__ __forceinline__ V3 ang(uint32_t i) const { return s.ang[i]; }
-	__device__ __forceinline__ void set(uint32_t i, V3 l, V3 a) const { s.lin[i] = l; s.ang[i] = a; }
+	V3* l;
+	V3* a;
+	__device__ __forceinline__ V3 lin(uint32_t i) const { return l[i]; }
+	__device__ __forceinline__ V3 ang(uint32_t i) const { return a[i]; }
+	__device__ __forceinline__ void set(uint32_t i, V3 lv, V3 av) const { l[i] = lv; a[i] = av; }
 };
 struct GlobalVel
 {
@@ -679,35 +757,41 @@ struct GlobalVel
 
 // Position iterations (each followed by integration), velocity iterations,
 // PxIntegrateSolverBodiesTGS and write-back of one scene.
-// Each lane stages the packed rows of the constraint it solves in shared
-// memory with asynchronous 16-byte copies (one memory round trip per
-// constraint instead of one per row), solves from there and writes the
-// updated impulses back.  Rows larger than the staging slot are used in place.
+// In warp groups each lane stages the packed rows of the constraint it solves
+// in shared memory with asynchronous 16-byte copies (one memory round trip per
+// constraint instead of one per row), solves from there and writes the updated
+// impulses back; rows larger than the staging slot, and the rows of block
+// groups (large scenes), are used in place.
 constexpr uint32_t RECBUF_CHUNKS = 32;   // 512 bytes per lane
-struct __align__(16) IterSmem
+template <uint32_t CAPB, uint32_t CAPC, bool STAGE>
+struct __align__(16) IterSmemT
 {
-	float4 recBuf[32][RECBUF_CHUNKS + 1];   // padded rows: lanes' slots start in different banks
-	VelSmem vel;
+	float4 recBuf[STAGE ? 32 : 1][RECBUF_CHUNKS + 1];   // padded rows: lanes' slots start in different banks
+	V3 lin[CAPB], ang[CAPB];
 	uint32_t ends[MAX_PARTITIONS];
-	uint8_t chunks[SOLVE_SMEM_CONSTRAINTS];
+	uint8_t chunks[CAPC];
+	uint32_t bc;
 };
+using IterSmem = IterSmemT<SOLVE_SMEM_BODIES, SOLVE_SMEM_CONSTRAINTS, true>;
+using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, false>;
 
-template <typename Vel>
-__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, IterSmem& sm,
-                                             uint32_t nbPart, const Vel& V)
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC, bool STAGE, typename Vel>
+__device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
+                                             IterSmemT<CAPB, CAPC, STAGE>& sm, uint32_t nbPart, const Vel& V)
 {
-	const uint32_t lane = threadIdx.x & 31;
+	constexpr uint32_t NT = Grp<G>::NT;
+	const uint32_t tid = Grp<G>::tid();
 	const uint32_t n = sc.nbBodies, nTot = n + sc.nbStatics;
 	const uint32_t* ends = sm.ends;
 	tgs::BodyVel* vel = w.vel + sc.solverStart;
 	tgs::BodyTx* tx = w.tx + sc.solverStart;
 	Tr* pose = w.pose + sc.solverStart;
 	const uint32_t nc = nbPart ? ends[nbPart - 1] : 0;
-	const bool chunksOnChip = nc <= SOLVE_SMEM_CONSTRAINTS;
+	const bool chunksOnChip = STAGE && nc <= CAPC;
 	if(chunksOnChip)
-		for(uint32_t r = lane; r < nc; r += 32) sm.chunks[r] = w.recChunks[sc.pairStart + r];
-	for(uint32_t i = lane; i < nTot; i += 32) V.set(i, vel[i].lin, vel[i].ang);
-	__syncwarp();
+		for(uint32_t r = tid; r < nc; r += NT) sm.chunks[r] = w.recChunks[sc.pairStart + r];
+	for(uint32_t i = tid; i < nTot; i += NT) V.set(i, vel[i].lin, vel[i].ang);
+	Grp<G>::sync();
 	const float stepDt = sp.dt / float(sp.nbPos);
 	float elapsed = 0.0f;
 	for(uint32_t it = 0; it < sp.nbPos + sp.nbVel; it++)
@@ -718,18 +802,21 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 		for(uint32_t p = 0; p < nbPart; p++)
 		{
 			const uint32_t end = ends[p];
-			for(uint32_t r = begin + lane; r < end; r += 32)
+			for(uint32_t r = begin + tid; r < end; r += NT)
 			{
 				tgs::ConstraintRecord* src = w.recs + sc.pairStart + r;
-				const uint32_t chunks = chunksOnChip ? sm.chunks[r] : w.recChunks[sc.pairStart + r];
 				tgs::ConstraintRecord* rec = src;
-				if(chunks <= RECBUF_CHUNKS)
+				if constexpr(STAGE)
 				{
-					float4* dst = sm.recBuf[lane];
-					const float4* g = reinterpret_cast<const float4*>(src);
-					for(uint32_t k = 0; k < chunks; k++) cpAsync16(dst + k, g + k);
-					cpAsyncWaitAll();
-					rec = reinterpret_cast<tgs::ConstraintRecord*>(dst);
+					const uint32_t chunks = chunksOnChip ? sm.chunks[r] : w.recChunks[sc.pairStart + r];
+					if(chunks <= RECBUF_CHUNKS)
+					{
+						float4* dst = sm.recBuf[threadIdx.x & 31];
+						const float4* g = reinterpret_cast<const float4*>(src);
+						for(uint32_t k = 0; k < chunks; k++) cpAsync16(dst + k, g + k);
+						cpAsyncWaitAll();
+						rec = reinterpret_cast<tgs::ConstraintRecord*>(dst);
+					}
 				}
 				if(rec->nbPatches == 0) continue;
 				const uint32_t a = uint32_t(rec->bodyA), b = uint32_t(rec->bodyB);
@@ -770,11 +857,11 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 				}
 			}
 			begin = end;
-			__syncwarp();
+			Grp<G>::sync();
 		}
 		if(posIter)
 		{
-			for(uint32_t i = lane; i < n; i += 32)
+			for(uint32_t i = tid; i < n; i += NT)
 			{
 				tgs::BodyVel v = vel[i];
 				v.lin = V.lin(i);
@@ -784,10 +871,10 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 				vel[i].dAng = v.dAng;
 			}
 			elapsed += stepDt;
-			__syncwarp();
+			Grp<G>::sync();
 		}
 	}
-	for(uint32_t i = lane; i < n; i += 32)
+	for(uint32_t i = tid; i < n; i += NT)
 	{
 		tgs::BodyVel v = vel[i];
 		v.lin = V.lin(i);
@@ -801,79 +888,116 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 		rb.q[0] = p.q.x; rb.q[1] = p.q.y; rb.q[2] = p.q.z; rb.q[3] = p.q.w;
 		rb.p[0] = p.p.x; rb.p[1] = p.p.y; rb.p[2] = p.p.z;
 	}
-	__syncwarp();
+	Grp<G>::sync();
 }
 
-// Stage kernels of one step.  Broadphase and solve run a persistent grid of
-// warps that pull scenes from the size-sorted work table (largest first);
-// the narrowphase runs one kernel per pair kind over all scenes' pairs.
+// Stage kernels of one step.  The scene stages (broadphase, batching, solve)
+// run persistent grids that pull scenes from the size-sorted work table
+// (largest first): warp-per-scene kernels take the scenes of up to
+// sp.largeBodies solver bodies, block-per-scene kernels (BIG_WARPS warps, the
+// workspace for up to 4096 bodies on chip) the larger ones.  The narrowphase
+// runs one kernel per pair kind over all scenes' pairs.
+__device__ __forceinline__ bool largeScene(const SceneDesc& sc, const StepParams& sp) { return sc.nbBodies + sc.nbStatics > sp.largeBodies; }
+
+// Next scene of the wanted size class from work counter `counter` (all threads of
+// the group get it); false when the table is exhausted.
+template <uint32_t G>
+__device__ __forceinline__ bool nextScene(const WorldDev& w, uint32_t counter, bool wantLarge, const StepParams& sp, uint32_t& sid,
+                                          SceneDesc& sc, volatile uint32_t* slot)
+{
+	for(;;)
+	{
+		uint32_t item = 0;
+		if(Grp<G>::tid() == 0) item = atomicAdd(&w.workCounter[counter], 1u);
+		item = Grp<G>::bcast(item, slot);
+		if(item >= *w.nbActive) return false;
+		sid = w.workOrder[item];
+		sc = w.scenes[sid];
+		if(largeScene(sc, sp) == wantLarge) return true;
+	}
+}
+
+enum : uint32_t { WC_BP = 0, WC_BATCH = 1, WC_SOLVE = 2, WC_PREP = 3, WC_BP_BIG = 4, WC_BATCH_BIG = 5, WC_SOLVE_BIG = 6 };
+
 __global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
 	BpSmem& sm = reinterpret_cast<BpSmem*>(stageSmem)[threadIdx.x >> 5];
-	const uint32_t lane = threadIdx.x & 31;
-	for(;;)
-	{
-		uint32_t item = 0;
-		if(lane == 0) item = atomicAdd(&w.workCounter[0], 1u);
-		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= *w.nbActive) break;
-		const uint32_t sid = w.workOrder[item];
-		const SceneDesc sc = w.scenes[sid];
-		sceneBroadphase(w, sc, sid, sp, sm);
-	}
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<1>(w, WC_BP, false, sp, sid, sc, nullptr)) sceneBroadphase<1>(w, sc, sid, sp, sm);
+}
+
+__global__ void __launch_bounds__(BIG_WARPS * 32) broadphaseBigKernel(WorldDev w, StepParams sp)
+{
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	BpSmemBig& sm = *reinterpret_cast<BpSmemBig*>(stageSmem);
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<BIG_WARPS>(w, WC_BP_BIG, true, sp, sid, sc, &sm.bc)) sceneBroadphase<BIG_WARPS>(w, sc, sid, sp, sm);
 }
 
 __global__ void __launch_bounds__(128) batchKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
 	SolveSmem& sm = reinterpret_cast<SolveSmem*>(stageSmem)[threadIdx.x >> 5];
-	const uint32_t lane = threadIdx.x & 31;
-	for(;;)
-	{
-		uint32_t item = 0;
-		if(lane == 0) item = atomicAdd(&w.workCounter[1], 1u);
-		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= *w.nbActive) break;
-		const uint32_t sid = w.workOrder[item];
-		const SceneDesc sc = w.scenes[sid];
-		sceneBatchStage(w, sc, sid, sp, sm);
-	}
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<1>(w, WC_BATCH, false, sp, sid, sc, nullptr)) sceneBatchStage<1>(w, sc, sid, sp, sm);
+}
+
+__global__ void __launch_bounds__(BIG_WARPS * 32) batchBigKernel(WorldDev w, StepParams sp)
+{
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	SolveSmemBig& sm = *reinterpret_cast<SolveSmemBig*>(stageSmem);
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<BIG_WARPS>(w, WC_BATCH_BIG, true, sp, sid, sc, &sm.bc)) sceneBatchStage<BIG_WARPS>(w, sc, sid, sp, sm);
 }
 
 // Row preparation of every scene's constraints: a thread per constraint.
 __global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
 {
-	const uint32_t count = w.workCounter[3];
+	const uint32_t count = w.workCounter[WC_PREP];
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
 }
 
-constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the solve kernel
+// Iterations of one scene; afterwards the state this step wrote becomes the
+// scene's last-step state.
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC, bool STAGE>
+__device__ __forceinline__ void solveScene(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
+                                           IterSmemT<CAPB, CAPC, STAGE>& sm)
+{
+	const uint32_t tid = Grp<G>::tid();
+	const uint32_t nbPart = w.nbPartitions[sid];
+	if(nbPart || !w.nbConstraints[sid])   // batching overflowed: the scene is left unchanged
+	{
+		for(uint32_t p = tid; p < nbPart; p += Grp<G>::NT) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+		Grp<G>::sync();
+		if(sc.nbBodies + sc.nbStatics <= CAPB) sceneIterate<G>(w, sc, sid, sp, sm, nbPart, SharedVel{sm.lin, sm.ang});
+		else sceneIterate<G>(w, sc, sid, sp, sm, nbPart, GlobalVel{w.vel + sc.solverStart});
+	}
+	Grp<G>::sync();
+	if(sp.persistent && tid == 0) w.sceneParity[sid] ^= 1u;
+}
+
+constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the warp-per-scene solve kernel
 __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
 	IterSmem& sm = reinterpret_cast<IterSmem*>(stageSmem)[threadIdx.x >> 5];
-	const uint32_t lane = threadIdx.x & 31;
-	for(;;)
-	{
-		uint32_t item = 0;
-		if(lane == 0) item = atomicAdd(&w.workCounter[2], 1u);
-		item = __shfl_sync(0xffffffffu, item, 0);
-		if(item >= *w.nbActive) break;
-		const uint32_t sid = w.workOrder[item];
-		const SceneDesc sc = w.scenes[sid];
-		const uint32_t nbPart = w.nbPartitions[sid];
-		if(nbPart || !w.nbConstraints[sid])   // batching overflowed: the scene is left unchanged
-		{
-			for(uint32_t p = lane; p < nbPart; p += 32) sm.ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
-			__syncwarp();
-			if(sc.nbBodies + sc.nbStatics <= SOLVE_SMEM_BODIES) sceneIterate(w, sc, sid, sp, sm, nbPart, SharedVel{sm.vel});
-			else sceneIterate(w, sc, sid, sp, sm, nbPart, GlobalVel{w.vel + sc.solverStart});
-		}
-		// the state this step wrote becomes the scene's last-step state
-		__syncwarp();
-		if(sp.persistent && lane == 0) w.sceneParity[sid] ^= 1u;
-	}
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<1>(w, WC_SOLVE, false, sp, sid, sc, nullptr)) solveScene<1>(w, sc, sid, sp, sm);
+}
+
+__global__ void __launch_bounds__(BIG_WARPS * 32) solveBigKernel(WorldDev w, StepParams sp)
+{
+	extern __shared__ __align__(16) unsigned char stageSmem[];
+	IterSmemBig& sm = *reinterpret_cast<IterSmemBig*>(stageSmem);
+	uint32_t sid;
+	SceneDesc sc;
+	while(nextScene<BIG_WARPS>(w, WC_SOLVE_BIG, true, sp, sid, sc, &sm.bc)) solveScene<BIG_WARPS>(w, sc, sid, sp, sm);
 }
 
 // Totals over all scenes after a step: pairs, pairs with contacts, contacts.
@@ -922,6 +1046,12 @@ struct World
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
+	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0;
+	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
+	// scenes above this many solver bodies run one block per scene (warp per scene below)
+	static constexpr uint32_t DEFAULT_LARGE_BODIES = 512;
+	static constexpr uint32_t BIG_THREADS = world::BIG_WARPS * 32;
+	bool launchLarge() const { return maxSolverBodies > params.largeBodies; }
 	DevBuf<world::SceneDesc> scenes;
 	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue, activeCount;
 	DevBuf<uint8_t> recChunks;
@@ -988,6 +1118,7 @@ struct World
 			b += d.nbBodies; st += d.nbStatics; key += d.keyCap; pair += d.pairCap;
 		}
 		nbBodies = b; nbStatics = st; nbSolver = b + st; nbKeys = key; nbPairSlots = pair;
+		for(const world::SceneDesc& d : hScenes) maxSolverBodies = std::max(maxSolverBodies, d.nbBodies + d.nbStatics);
 		std::vector<uint32_t> order(S);
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
@@ -1057,6 +1188,12 @@ struct World
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::SOLVE_WARPS))));
 		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve, iterSmemBytes(world::SOLVE_WARPS), world::SOLVE_WARPS * 32));
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::broadphaseBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::BpSmemBig))));
+		GBPX_CUDA_TRY(gridFor(world::broadphaseBigKernel, sms, gridBpBig, sizeof(world::BpSmemBig), int(BIG_THREADS)));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::SolveSmemBig))));
+		GBPX_CUDA_TRY(gridFor(world::batchBigKernel, sms, gridBatchBig, sizeof(world::SolveSmemBig), int(BIG_THREADS)));
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::IterSmemBig))));
+		GBPX_CUDA_TRY(gridFor(world::solveBigKernel, sms, gridSolveBig, sizeof(world::IterSmemBig), int(BIG_THREADS)));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 		return GBPX_OK;
 	}
@@ -1098,14 +1235,18 @@ struct World
 			gPrep = std::min(gridPrep, 8u);
 			threads = 32;
 		}
+		const bool big = launchLarge();
 		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
 		world::broadphaseKernel<<<gBp, threads, bpSmemBytes(threads / 32), stream>>>(w, params);
+		if(big) world::broadphaseBigKernel<<<plain ? 1u : gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), stream>>>(w, params);
 		for(uint32_t k = 0; k < world::NB_KINDS; k++)
 			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
+		if(big) world::batchBigKernel<<<plain ? 1u : gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
 		const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
 		world::solveKernel<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32), stream>>>(w, params);
+		if(big) world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
@@ -1155,6 +1296,7 @@ struct World
 		for(auto& e : ev) GBPX_CUDA_TRY(cudaEventCreate(&e));
 		std::vector<double> acc(K, 0.0);
 		const world::WorldDev w = dev();
+		const bool big = launchLarge();
 		int rc = GBPX_OK;
 		for(uint32_t s = 0; s < steps && rc == GBPX_OK; s++)
 		{
@@ -1162,6 +1304,7 @@ struct World
 			uint32_t k = 0;
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			world::broadphaseKernel<<<gridBlocks, 128, bpSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
+			if(big) world::broadphaseBigKernel<<<gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			for(uint32_t t = 0; t < world::NB_KINDS; t++)
 			{
@@ -1169,10 +1312,12 @@ struct World
 				GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			}
 			world::batchKernel<<<gridBatch, 128, solveSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
+			if(big) world::batchBigKernel<<<gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			world::prepKernel<<<gridPrep, 128, 0, stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			world::solveKernel<<<gridSolve, world::SOLVE_WARPS * 32, iterSmemBytes(world::SOLVE_WARPS), stream>>>(w, params);
+			if(big) world::solveBigKernel<<<gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			GBPX_CUDA_TRY(cudaGetLastError());
 			GBPX_CUDA_TRY(cudaEventSynchronize(ev[K]));
@@ -1270,6 +1415,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
+	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -1342,7 +1488,7 @@ GBPX_API int gbpx_world_info(void* wv, uint64_t* out8)
 	World* w = static_cast<World*>(wv);
 	if(!w || !out8) return GBPX_ERR_INVALID;
 	out8[0] = w->nbScenes; out8[1] = w->nbBodies; out8[2] = w->nbStatics; out8[3] = w->nbPairSlots; out8[4] = w->gridBlocks;
-	out8[5] = w->deviceBytes; out8[6] = World::KERNELS_PER_STEP; out8[7] = 0;
+	out8[5] = w->deviceBytes; out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? 3u : 0u); out8[7] = w->params.largeBodies;
 	return GBPX_OK;
 }
 
@@ -1423,6 +1569,23 @@ GBPX_API int gbpx_world_stats(void* wv, uint64_t* out4)
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(out4, w->stats.ptr, 4 * 8, cudaMemcpyDeviceToHost, w->stream));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// Scenes of more than `largeBodies` solver bodies (bodies + statics) run their
+// broadphase, batching and solve one block of 8 warps per scene; smaller ones
+// one warp per scene (default 512).  The arithmetic is the same either way.
+GBPX_API int gbpx_world_set_large_bodies(void* wv, uint32_t largeBodies)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	w->params.largeBodies = largeBodies;
+	if(w->graphExec)
+	{
+		cudaGraphExecDestroy(w->graphExec);
+		w->graphExec = nullptr;
+	}
 	return GBPX_OK;
 }
 
@@ -1712,6 +1875,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.bounceThreshold = params[7]; sp.frictionOffsetThreshold = params[8]; sp.correlationDistance = params[9]; sp.staticFriction = params[10];
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
+	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);

@@ -41,6 +41,7 @@ def _setup():
         L.gbpx_world_time_plain.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gbpx_world_kind_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gbpx_world_set_large_bodies.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         L.gbpx_world_time_stages.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_float)]
@@ -109,7 +110,7 @@ class World:
         out = np.zeros(8, np.uint64)
         check(self._L.gbpx_world_info(self._h, _p(out)), "gbpx_world_info")
         return dict(scenes=int(out[0]), bodies=int(out[1]), statics=int(out[2]), pair_slots=int(out[3]), grid_blocks=int(out[4]),
-                    device_bytes=int(out[5]), kernels_per_step=int(out[6]))
+                    device_bytes=int(out[5]), kernels_per_step=int(out[6]), large_bodies=int(out[7]))
 
     def time_steps(self, n, graph=True):
         """Milliseconds for n device-resident steps (CUDA events on the world stream)."""
@@ -127,6 +128,11 @@ class World:
         out = np.zeros(4, np.uint64)
         check(self._L.gbpx_world_stats(self._h, _p(out)), "gbpx_world_stats")
         return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]), row_bytes=int(out[3]))
+
+    def set_large_bodies(self, n):
+        """Scenes of more than n solver bodies run one block per scene in the scene
+        stages (warp per scene below); results do not depend on it."""
+        check(self._L.gbpx_world_set_large_bodies(self._h, int(n)), "gbpx_world_set_large_bodies")
 
     def kind_counts(self):
         """Pairs of each pair kind in the last step, {narrowphase stage name: pairs}."""

@@ -145,3 +145,56 @@ def test_world_fresh_mode_steps_match_oracle(cuda_device):
         assert np.abs(out["p"] - ref["p"]).max() <= 1e-6, step
         rb = ref
     w.release()
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_world_block_per_scene_equals_warp_per_scene(cuda_device, persistent):
+    """The scene stages run one warp per scene or one block per scene (large
+    scenes); the arithmetic is the same, so both give the same bytes."""
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(141, 24, nmin=64, nmax=1500)
+    a = World(scenes, persistent=persistent)
+    b = World(scenes, persistent=persistent)
+    a.set_large_bodies(1 << 30)   # every scene one warp
+    b.set_large_bodies(0)         # every scene one block
+    for step in range(40):
+        a.step(1)
+        b.step(1)
+        if step % 8 == 7:
+            assert a.get_bodies().tobytes() == b.get_bodies().tobytes(), step
+    assert not a.status().any() and not b.status().any()
+    assert a.stats()["constraints"] > 1000
+    a.release()
+    b.release()
+
+
+def test_world_large_scenes_equal_scene_step(cuda_device):
+    """Scenes above the block-per-scene threshold in a world step exactly like the
+    same scenes stepped alone by the large-scene path."""
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import as_world
+    from physx_gb300.world import World
+    from scenarios import random_scene
+    parts = [random_scene(150 + k, n) for k, n in enumerate((700, 1500, 2600))]
+    merged = dict(body_count=np.array([len(p["types"]) for p in parts], np.uint32), static_count=np.ones(3, np.uint32),
+                  rigid=np.concatenate([p["rigid"] for p in parts]), types=np.concatenate([p["types"] for p in parts]),
+                  geoms=np.concatenate([p["geoms"] for p in parts]), friction=np.concatenate([p["friction"] for p in parts]),
+                  static_poses=np.concatenate([p["static_poses"] for p in parts]), static_types=np.concatenate([p["static_types"] for p in parts]),
+                  static_geoms=np.concatenate([p["static_geoms"] for p in parts]))
+    w = World(merged)
+    assert w.info()["large_bodies"] == 512
+    singles = [Scene(p) for p in parts]
+    for step in range(6):
+        w.step(1)
+        got = w.get_bodies()
+        off = 0
+        for s in singles:
+            s.step(1)
+            ref = s.get_bodies()
+            assert got[off:off + len(ref)].tobytes() == ref.tobytes(), step
+            off += len(ref)
+    assert not w.status().any()
+    for s in singles:
+        s.release()
+    w.release()
