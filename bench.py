@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--bp-cpu-frames", type=int, default=1)
     ap.add_argument("--large-steps", type=int, default=600, help="frames of the 100k-body single-scene run")
     ap.add_argument("--large-cpu-frames", type=int, default=1)
+    ap.add_argument("--large-bodies", type=int, default=0,
+                    help="block-per-scene threshold of the world's scene stages (0 = autotuned for the scene-size histogram)")
+    ap.add_argument("--profile-step", type=int, default=0,
+                    help="only build the state (pre-roll, autotune, warm-up), then run this many un-captured steps inside a "
+                         "profiler range (for ncu --profile-from-start off) and exit")
     return ap.parse_args()
 
 
@@ -347,8 +352,26 @@ def main():
     bodies = info["bodies"]
     # pre-roll to a contact-rich state, then warm up (builds the graph)
     w.step(a.preroll, graph=True)
+    # block-per-scene threshold for this scene-size histogram, timed on a temporary
+    # copy of all scenes in their current state (the world's own state does not
+    # advance; a smaller sample would not load the GPU like the full set does)
+    if a.large_bodies:
+        w.set_large_bodies(a.large_bodies)
+        tuned_threshold, tuned_ms = a.large_bodies, 0.0
+    else:
+        tuned_threshold, tuned_ms = w.autotune(steps=3)
     w.step(a.warmup, graph=True)
     w.synchronize()
+    if a.profile_step:
+        L = physx_gb300.lib()
+        physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+        w.step(a.profile_step, graph=False)
+        physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        print(json.dumps(dict(profiled_steps=a.profile_step, kernels_per_step=w.info()["kernels_per_step"],
+                              large_bodies=w.info()["large_bodies"], **w.stats())))
+        if pool:
+            pool.close()
+        return
     state = w.get_bodies()
     if dist:
         dist.barrier()
@@ -421,12 +444,20 @@ def main():
     peak, peak_kind = measured_peak()
     stages = {k: dict(ms=stage_time[k], gbs=stage_bytes[k] / (stage_time[k] / 1000.0) / 1e9, bytes=stage_bytes[k]) for k in stage_time}
     stages["narrowphase"]["kinds"] = {k[3:]: dict(pairs=kinds[k], ms=stage_ms[k]) for k in kinds}
-    dominant = max(stage_time, key=stage_time.get)
-    achieved = stages[dominant]["gbs"]
+    # the dominant single kernel: the narrowphase is nine kernels (one per pair kind), so
+    # it competes kernel by kernel; a narrowphase kernel's bytes are its share of the
+    # stage's by pairs
+    kernel_ms = {k: v for k, v in stage_time.items() if k != "narrowphase"}
+    kernel_ms.update({k: stage_ms[k] for k in kinds})
+    dominant = max(kernel_ms, key=kernel_ms.get)
+    if dominant in kinds:
+        dom_bytes = stage_bytes["narrowphase"] * kinds[dominant] / max(1, st["pairs"])
+    else:
+        dom_bytes = stage_bytes[dominant]
+    achieved = dom_bytes / (kernel_ms[dominant] / 1000.0) / 1e9
     traffic = profiled_traffic(dominant)
     roofline = dict(bound="hbm", kernel=dominant, achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
-                    traffic=traffic, peak_source=peak_kind, algorithmic_bytes_per_launch=stage_bytes[dominant],
-                    launch_ms=stage_time[dominant])
+                    traffic=traffic, peak_source=peak_kind, algorithmic_bytes_per_launch=dom_bytes, launch_ms=kernel_ms[dominant])
     bytes_step = sum(stage_bytes.values())
     step_roofline = dict(algorithmic_bytes_per_step=bytes_step, achieved=bytes_step / (ms / a.steps / 1000.0) / 1e9, unit="GB/s")
     cpu = None
@@ -452,6 +483,8 @@ def main():
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
                             constraints_per_step=st["constraints"], contacts_per_step=st["contacts"], graph=True,
+                            autotune=dict(key="scene-size histogram", large_bodies=tuned_threshold,
+                                          sample_ms_per_step=tuned_ms),
                             l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
                             parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),
                 e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=bodies * 96, d2h_bytes_per_step=bodies * 96),

@@ -35,6 +35,10 @@ int gbpx_device_count(int* out);
 int gbpx_device_info(int device, char* name, int nameBytes, int* smCount, int* computeCapability);
 int gbpx_device_synchronize(void);
 int gbpx_set_device(int device);
+/* profiler range: a profiler started with capture off records only the
+ * kernels launched between these calls */
+int gbpx_profiler_start(void);
+int gbpx_profiler_stop(void);
 
 /* ---------------------------------------------------------------- broadphase
  * ABP-compatible broadphase.  Replaces:
@@ -201,6 +205,13 @@ int gbpx_world_stats(void* world, uint64_t* out4);
  * broadphase, batching and solve one block (8 warps) per scene, smaller scenes
  * one warp per scene; default 512.  Results do not depend on it. */
 int gbpx_world_set_large_bodies(void* world, uint32_t largeBodies);
+/* Autotuner keyed on the scene-size histogram: times candidate thresholds of
+ * gbpx_world_set_large_bodies on a size-stratified sample of sampleScenes
+ * scenes (a temporary world in the current state, `steps` graph steps each),
+ * sets the fastest and caches it per histogram.  The sample must load the GPU
+ * like the whole world (pass the scene count to copy every scene).  outMs: the
+ * chosen threshold's ms per step on the sample (0 when cached). */
+int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, float* outMs);
 /* Pairs of each pair kind in the last step, in the kind order of the
  * narrowphase launches (sphere-sphere ... box-box): 9 counts. */
 int gbpx_world_kind_counts(void* world, uint32_t* out9);

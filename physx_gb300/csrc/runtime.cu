@@ -1,5 +1,6 @@
 // Device discovery and small runtime helpers exported through the C ABI.
 #include "common.cuh"
+#include <cuda_profiler_api.h>
 
 GBPX_API int gbpx_device_count(int* out)
 {
@@ -30,5 +31,20 @@ GBPX_API int gbpx_device_synchronize(void)
 GBPX_API int gbpx_set_device(int device)
 {
 	GBPX_CUDA_TRY(cudaSetDevice(device));
+	return GBPX_OK;
+}
+
+// Profiler range (cudaProfilerStart/Stop): a profiler started with its capture
+// off records only the kernels launched inside the range.
+GBPX_API int gbpx_profiler_start(void)
+{
+	GBPX_CUDA_TRY(cudaProfilerStart());
+	return GBPX_OK;
+}
+
+GBPX_API int gbpx_profiler_stop(void)
+{
+	GBPX_CUDA_TRY(cudaDeviceSynchronize());
+	GBPX_CUDA_TRY(cudaProfilerStop());
 	return GBPX_OK;
 }

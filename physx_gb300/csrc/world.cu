@@ -32,6 +32,8 @@
 #include <numeric>
 #include <chrono>
 #include <deque>
+#include <map>
+#include <string>
 
 namespace gbpx
 {
@@ -1048,6 +1050,7 @@ struct World
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
 	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0;
 	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
+	uint32_t pairsPerBody = 0;
 	// scenes above this many solver bodies run one block per scene (warp per scene below)
 	static constexpr uint32_t DEFAULT_LARGE_BODIES = 512;
 	static constexpr uint32_t BIG_THREADS = world::BIG_WARPS * 32;
@@ -1099,9 +1102,10 @@ struct World
 
 	int create(uint32_t S, const uint32_t* sceneBodyCount, const uint32_t* sceneStaticCount, const void* rigid, const int* typesIn,
 	           const float* geomsIn, const float* frictionIn, const float* staticPoseIn, const int* staticTypesIn, const float* staticGeomsIn,
-	           uint32_t pairsPerBody, const world::StepParams& sp)
+	           uint32_t pairsPerBodyIn, const world::StepParams& sp)
 	{
 		params = sp;
+		pairsPerBody = pairsPerBodyIn;
 		nbScenes = S;
 		hScenes.resize(S);
 		uint32_t b = 0, st = 0, key = 0, pair = 0;
@@ -1587,6 +1591,130 @@ GBPX_API int gbpx_world_set_large_bodies(void* wv, uint32_t largeBodies)
 		w->graphExec = nullptr;
 	}
 	return GBPX_OK;
+}
+
+// ---- Autotuner of the block-per-scene threshold ----
+// The scene stages run warp-per-scene or block-per-scene kernels by scene size
+// (gbpx_world_set_large_bodies).  The best threshold depends on the scene-size
+// histogram: the autotuner takes a size-stratified sample of the world's scenes
+// in their current state into a temporary world, times a few graph-replayed
+// steps per candidate threshold there, and sets the fastest on the world.  The
+// choice is cached per histogram (scene counts per power-of-two size bucket,
+// quantised to 1/32 of the scenes), so worlds of the same size mix reuse it.
+namespace
+{
+std::string histogramKey(const std::vector<gbpx::world::SceneDesc>& sc)
+{
+	uint32_t buckets[32] = {};
+	for(const auto& d : sc)
+	{
+		uint32_t b = 0;
+		while((1u << b) < d.nbBodies + d.nbStatics) b++;
+		buckets[b]++;
+	}
+	std::string key;
+	for(uint32_t b = 0; b < 32; b++)
+	{
+		const uint32_t q = uint32_t((uint64_t(buckets[b]) * 32 + sc.size() / 2) / sc.size());
+		key += std::to_string(q) + ",";
+	}
+	return key;
+}
+std::map<std::string, uint32_t>& tunedThresholds()
+{
+	static std::map<std::string, uint32_t> m;
+	return m;
+}
+} // namespace
+
+GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, float* outMs)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !sampleScenes || !steps || !outLargeBodies) return GBPX_ERR_INVALID;
+	const std::string key = histogramKey(w->hScenes);
+	auto& cache = tunedThresholds();
+	auto hit = cache.find(key);
+	if(hit != cache.end())
+	{
+		*outLargeBodies = hit->second;
+		if(outMs) *outMs = 0.0f;
+		return gbpx_world_set_large_bodies(wv, hit->second);
+	}
+	// size-stratified sample: every k-th scene in order of size
+	std::vector<uint32_t> order(w->nbScenes);
+	std::iota(order.begin(), order.end(), 0u);
+	std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return w->hScenes[x].nbBodies < w->hScenes[y].nbBodies; });
+	const uint32_t m = std::min(sampleScenes, w->nbScenes);
+	std::vector<uint32_t> pick(m);
+	for(uint32_t k = 0; k < m; k++) pick[k] = order[uint32_t((uint64_t(k) * w->nbScenes + w->nbScenes / 2) / m) % w->nbScenes];
+	// the sample's arrays, read back from the world (current body state)
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	std::vector<uint32_t> bc(m), sc(m);
+	std::vector<gbpx::tgs::RigidBody> rb;
+	std::vector<int> ty, sty;
+	std::vector<float4> ge, sge;
+	std::vector<float> fr, sp7;
+	for(uint32_t k = 0; k < m; k++)
+	{
+		const gbpx::world::SceneDesc& d = w->hScenes[pick[k]];
+		bc[k] = d.nbBodies;
+		sc[k] = d.nbStatics;
+		const size_t b0 = rb.size(), s0 = sty.size();
+		rb.resize(b0 + d.nbBodies); ty.resize(b0 + d.nbBodies); ge.resize(b0 + d.nbBodies); fr.resize(b0 + d.nbBodies);
+		sty.resize(s0 + d.nbStatics); sge.resize(s0 + d.nbStatics); sp7.resize(7 * (s0 + d.nbStatics));
+		GBPX_CUDA_TRY(cudaMemcpy(rb.data() + b0, w->bodies.ptr + d.bodyStart, size_t(d.nbBodies) * sizeof(gbpx::tgs::RigidBody), cudaMemcpyDeviceToHost));
+		GBPX_CUDA_TRY(cudaMemcpy(ty.data() + b0, w->types.ptr + d.bodyStart, size_t(d.nbBodies) * 4, cudaMemcpyDeviceToHost));
+		GBPX_CUDA_TRY(cudaMemcpy(ge.data() + b0, w->geoms.ptr + d.bodyStart, size_t(d.nbBodies) * 16, cudaMemcpyDeviceToHost));
+		GBPX_CUDA_TRY(cudaMemcpy(fr.data() + b0, w->friction.ptr + d.bodyStart, size_t(d.nbBodies) * 4, cudaMemcpyDeviceToHost));
+		if(d.nbStatics)
+		{
+			GBPX_CUDA_TRY(cudaMemcpy(sty.data() + s0, w->staticTypes.ptr + d.staticStart, size_t(d.nbStatics) * 4, cudaMemcpyDeviceToHost));
+			GBPX_CUDA_TRY(cudaMemcpy(sge.data() + s0, w->staticGeoms.ptr + d.staticStart, size_t(d.nbStatics) * 16, cudaMemcpyDeviceToHost));
+			GBPX_CUDA_TRY(cudaMemcpy(sp7.data() + 7 * s0, w->staticPose.ptr + 7 * size_t(d.staticStart), size_t(d.nbStatics) * 28, cudaMemcpyDeviceToHost));
+		}
+	}
+	World* t = new World;
+	int rc = t->create(m, bc.data(), sc.data(), rb.data(), ty.data(), reinterpret_cast<const float*>(ge.data()), fr.data(),
+	                   sp7.empty() ? nullptr : sp7.data(), sty.empty() ? nullptr : sty.data(),
+	                   sge.empty() ? nullptr : reinterpret_cast<const float*>(sge.data()), w->pairsPerBody, w->params);
+	if(rc) { t->release(); delete t; return rc; }
+	// candidates that classify the sample differently
+	const uint32_t cands[] = {64u, 128u, 256u, 512u, 1024u, 2048u, 0xffffffffu};
+	std::vector<uint32_t> sizes;
+	for(uint32_t k = 0; k < m; k++) sizes.push_back(bc[k] + sc[k]);
+	uint32_t best = w->params.largeBodies;
+	float bestMs = 3.4e38f;
+	int lastLarge = -1;
+	cudaEvent_t e0, e1;
+	GBPX_CUDA_TRY(cudaEventCreate(&e0));
+	GBPX_CUDA_TRY(cudaEventCreate(&e1));
+	for(uint32_t c : cands)
+	{
+		const int nLarge = int(std::count_if(sizes.begin(), sizes.end(), [&](uint32_t x) { return x > c; }));
+		if(nLarge == lastLarge) continue;
+		lastLarge = nLarge;
+		t->params.largeBodies = c;
+		if(t->graphExec) { cudaGraphExecDestroy(t->graphExec); t->graphExec = nullptr; }
+		rc = t->step(2, true);
+		if(rc) break;
+		cudaEventRecord(e0, t->stream);
+		rc = t->step(steps, true);
+		if(rc) break;
+		cudaEventRecord(e1, t->stream);
+		cudaEventSynchronize(e1);
+		float ms = 0.0f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if(ms < bestMs) { bestMs = ms; best = c; }
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	t->release();
+	delete t;
+	if(rc) return rc;
+	cache[key] = best;
+	*outLargeBodies = best;
+	if(outMs) *outMs = bestMs / float(steps);
+	return gbpx_world_set_large_bodies(wv, best);
 }
 
 // Pairs of each pair kind in the last step (sphere-sphere, sphere-plane,

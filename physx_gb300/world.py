@@ -42,6 +42,8 @@ def _setup():
         L.gbpx_world_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gbpx_world_kind_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gbpx_world_set_large_bodies.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        L.gbpx_world_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
+                                          ctypes.POINTER(ctypes.c_float)]
         L.gbpx_world_time_stages.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_float)]
@@ -133,6 +135,19 @@ class World:
         """Scenes of more than n solver bodies run one block per scene in the scene
         stages (warp per scene below); results do not depend on it."""
         check(self._L.gbpx_world_set_large_bodies(self._h, int(n)), "gbpx_world_set_large_bodies")
+
+    def autotune(self, sample_scenes=None, steps=3):
+        """Picks the block-per-scene threshold for this world's scene-size histogram
+        (timed on a temporary copy of a size-stratified sample of the scenes, all of
+        them by default; cached per histogram); returns (threshold, ms per step of
+        the sample with it, 0 if cached).  The sample should load the GPU like the
+        whole world: warp-per-scene kernels need many scenes to fill it."""
+        if sample_scenes is None:
+            sample_scenes = len(self._keep[0])
+        t = ctypes.c_uint32(0)
+        ms = ctypes.c_float(0)
+        check(self._L.gbpx_world_autotune(self._h, sample_scenes, steps, ctypes.byref(t), ctypes.byref(ms)), "gbpx_world_autotune")
+        return t.value, ms.value
 
     def kind_counts(self):
         """Pairs of each pair kind in the last step, {narrowphase stage name: pairs}."""

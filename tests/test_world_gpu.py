@@ -198,3 +198,26 @@ def test_world_large_scenes_equal_scene_step(cuda_device):
     for s in singles:
         s.release()
     w.release()
+
+
+def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
+    """The autotuner (keyed on the scene-size histogram) sets a block-per-scene
+    threshold from its candidates; the world's results do not change with it, and
+    a second world of the same histogram takes the cached choice."""
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(142, 64, nmin=16, nmax=2048)
+    a, b = World(scenes), World(scenes)
+    a.step(5)
+    b.step(5)
+    thr, ms = a.autotune(sample_scenes=32, steps=2)
+    assert thr in (64, 128, 256, 512, 1024, 2048, 0xffffffff) and ms > 0
+    assert a.info()["large_bodies"] == thr
+    thr2, ms2 = b.autotune(sample_scenes=32, steps=2)
+    assert thr2 == thr and ms2 == 0.0
+    b.set_large_bodies(512)
+    a.step(10)
+    b.step(10)
+    assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
+    a.release()
+    b.release()
