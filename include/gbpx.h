@@ -206,12 +206,19 @@ int gbpx_world_stats(void* world, uint64_t* out4);
  * one warp per scene; default 512.  Results do not depend on it. */
 int gbpx_world_set_large_bodies(void* world, uint32_t largeBodies);
 /* Autotuner keyed on the scene-size histogram: times candidate thresholds of
- * gbpx_world_set_large_bodies on a size-stratified sample of sampleScenes
+ * gbpx_world_set_large_bodies, then the solve staging slots, on a
+ * size-stratified sample of sampleScenes
  * scenes (a temporary world in the current state, `steps` graph steps each),
  * sets the fastest and caches it per histogram.  The sample must load the GPU
  * like the whole world (pass the scene count to copy every scene).  outMs: the
  * chosen threshold's ms per step on the sample (0 when cached). */
-int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, float* outMs);
+int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, uint32_t* outSolveVariant,
+                        float* outMs);
+/* Staging slot of the warp-per-scene solve: 0 = rows used in place, 1 = 256
+ * bytes per lane, 2 = 512 bytes per lane (default; a smaller slot leaves room
+ * for more warps per SM).  Results do not depend on it.  The autotuner sets it
+ * after the threshold. */
+int gbpx_world_set_solve_variant(void* world, uint32_t variant);
 /* Pairs of each pair kind in the last step, in the kind order of the
  * narrowphase launches (sphere-sphere ... box-box): 9 counts. */
 int gbpx_world_kind_counts(void* world, uint32_t* out9);

@@ -1289,6 +1289,33 @@ static __device__ bool capsuleBox(float r, float hh, V3 ext, const Tr& tCap, con
 	return false;
 }
 
+// Whether box-box / capsule-box contact generation takes its full path this
+// frame: the pair's manifold, refreshed to the current transforms, lost a point
+// or is invalidated (the decision boxBox / capsuleBox above make).  Used only to
+// order the pairs of a kind so that the lanes of a warp take the same path; the
+// generators decide again on their own.
+static __device__ bool boxBoxFullPath(V3 e0, V3 e1, const Tr& tA, const Tr& tB, float tolLen, Manifold m)
+{
+	const Tr cur = trInvMul(tB, tA);
+	const MatTr aToB = matFromTr(cur);
+	const float minMargin = fmin_(boxMargin(e0, tolLen), boxMargin(e1, tolLen));
+	const int initial = m.num;
+	refreshManifold(m, aToB, minMargin * 0.8f);
+	if(m.num != initial) return true;
+	return invalidateBoxConvex(m, cur, tA.q, tB.q, minMargin, sqrtf(dotA(e0, e0)), sqrtf(dotA(e1, e1)));
+}
+
+static __device__ bool capsuleBoxFullPath(float r, V3 ext, const Tr& tCap, const Tr& tBox, float tolLen, Manifold m)
+{
+	const Tr cur = trInvMul(tBox, tCap);
+	const MatTr aToB = matFromTr(cur);
+	const float minMargin = fmin_(boxMargin(ext, tolLen), r);
+	const int initial = m.num;
+	refreshManifold(m, aToB, minMargin * 0.8f);
+	if(m.num != initial) return true;
+	return invalidateSphereCapsule(m, cur, minMargin);
+}
+
 // One pair (types in the reference's table order, t0 <= t1).  m: the pair's
 // persistent manifold, read and updated by the cached kinds (plane-capsule,
 // plane-box, capsule-box, box-box: gEnablePCMCaching, PxsContext.cpp:89).

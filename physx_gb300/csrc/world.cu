@@ -85,6 +85,8 @@ struct WorldDev
 	uint32_t* partEnds;        // MAX_PARTITIONS per scene
 	uint32_t* status;
 	uint32_t* typeCount;       // pairs queued per pair kind (NB_KINDS)
+	uint32_t* pathCount;       // capsule-box, box-box: pairs ordered to the front (refresh) / back (full path)
+	uint32_t* typeQueueSorted; // capsule-box, box-box queues ordered by contact-generation path (persistent mode)
 	uint32_t* typeQueue;       // NB_KINDS queues of pair slots, queueCap entries each
 	uint32_t queueCap;
 	const uint32_t* slotScene; // owning scene of every pair slot
@@ -368,6 +370,72 @@ __device__ __forceinline__ void pairShape(const WorldDev& w, const SceneDesc& sc
 	}
 }
 
+// Persistent mode: the capsule-box and box-box queues reordered so that pairs
+// whose manifold only refreshes come first and pairs that take the full path
+// (GJK/EPA, SAT and clipping) last; each warp then runs one path.  Only the
+// order of the slots changes: every pair's result is written to its own slot.
+__device__ __forceinline__ uint32_t prevSlotOf(const WorldDev& w, const SceneDesc& sc, uint32_t sid, uint32_t key)
+{
+	uint32_t lo = 0, hi = w.pairCountPrev[sid];
+	const uint32_t* pk = w.pairsPrev + sc.pairStart;
+	while(lo < hi)
+	{
+		const uint32_t mid = (lo + hi) >> 1;
+		if(pk[mid] < key) lo = mid + 1;
+		else hi = mid;
+	}
+	return lo < w.pairCountPrev[sid] && pk[lo] == key ? lo : NO_PREV;
+}
+
+__global__ void __launch_bounds__(128) orderByPathKernel(WorldDev w, StepParams sp)
+{
+	const uint32_t c7 = w.typeCount[7], c8 = w.typeCount[8];
+	const uint32_t lane = threadIdx.x & 31;
+	for(uint32_t base = blockIdx.x * blockDim.x; base < c7 + c8; base += gridDim.x * blockDim.x)
+	{
+		const uint32_t q = base + threadIdx.x;
+		const bool valid = q < c7 + c8;
+		const uint32_t k = valid && q >= c7 ? 1u : 0u;   // 0 capsule-box, 1 box-box
+		bool full = true;
+		uint32_t slot = 0;
+		if(valid)
+		{
+			slot = w.typeQueue[size_t(7 + k) * w.queueCap + (k ? q - c7 : q)];
+			const uint32_t sid = w.slotScene[slot];
+			const SceneDesc sc = w.scenes[sid];
+			const uint32_t key = w.pairs[slot];
+			int ta, tb;
+			float ga[4], gb[4];
+			Tr pa, pb;
+			pairShape(w, sc, key >> 16, ta, ga, pa);
+			pairShape(w, sc, key & 0xffffu, tb, gb, pb);
+			const uint32_t prev = prevSlotOf(w, sc, sid, key);
+			np::Manifold m;
+			if(prev != NO_PREV) np::loadManifold(w.manifolds[w.sceneParity[sid]][sc.pairStart + prev], m);
+			if(k) full = np::boxBoxFullPath(v3(ga[0], ga[1], ga[2]), v3(gb[0], gb[1], gb[2]), pa, pb, sp.toleranceLength, m);
+			else if(ta == 2) full = np::capsuleBoxFullPath(ga[0], v3(gb[0], gb[1], gb[2]), pa, pb, sp.toleranceLength, m);
+			else full = np::capsuleBoxFullPath(gb[0], v3(ga[0], ga[1], ga[2]), pb, pa, sp.toleranceLength, m);
+		}
+		// warp-aggregated appends per (kind, path): refresh from the front, full from the back
+		for(uint32_t g = 0; g < 4; g++)
+		{
+			const bool mine = valid && (k * 2 + (full ? 1u : 0u)) == g;
+			const uint32_t peers = __ballot_sync(0xffffffffu, mine);
+			if(!peers) continue;
+			const uint32_t leader = __ffs(peers) - 1;
+			uint32_t b = 0;
+			if(lane == leader) b = atomicAdd(&w.pathCount[g], uint32_t(__popc(peers)));
+			b = __shfl_sync(0xffffffffu, b, leader);
+			if(mine)
+			{
+				const uint32_t r = b + __popc(peers & laneMaskLt());
+				const uint32_t count = (g >> 1) ? c8 : c7;
+				w.typeQueueSorted[size_t(g >> 1) * w.queueCap + ((g & 1) ? count - 1 - r : r)] = slot;
+			}
+		}
+	}
+}
+
 // Narrowphase of one pair kind over every scene: a thread per queued pair slot,
 // so each warp runs one contact generator on uniform work.
 template <int TA, int TB>
@@ -375,7 +443,8 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams 
 {
 	constexpr uint32_t KIND = TA == 0 ? uint32_t(TB) : (TA == 1 ? uint32_t(TB + 2) : (TA == 2 ? uint32_t(TB + 4) : 8u));
 	const uint32_t count = w.typeCount[KIND];
-	const uint32_t* queue = w.typeQueue + size_t(KIND) * w.queueCap;
+	const uint32_t* queue = (KIND == 7 || KIND == 8) && sp.persistent ? w.typeQueueSorted + size_t(KIND - 7) * w.queueCap
+	                                                                   : w.typeQueue + size_t(KIND) * w.queueCap;
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
 	{
 		const uint32_t slot = queue[q];
@@ -765,21 +834,26 @@ struct GlobalVel
 // impulses back; rows larger than the staging slot, and the rows of block
 // groups (large scenes), are used in place.
 constexpr uint32_t RECBUF_CHUNKS = 32;   // 512 bytes per lane
-template <uint32_t CAPB, uint32_t CAPC, bool STAGE>
+template <uint32_t CAPB, uint32_t CAPC, uint32_t RB>
 struct __align__(16) IterSmemT
 {
-	float4 recBuf[STAGE ? 32 : 1][RECBUF_CHUNKS + 1];   // padded rows: lanes' slots start in different banks
+	float4 recBuf[RB ? 32 : 1][RB + 1];   // RB 16-byte chunks per lane, padded: lanes' slots start in different banks
 	V3 lin[CAPB], ang[CAPB];
 	uint32_t ends[MAX_PARTITIONS];
 	uint8_t chunks[CAPC];
 	uint32_t bc;
 };
-using IterSmem = IterSmemT<SOLVE_SMEM_BODIES, SOLVE_SMEM_CONSTRAINTS, true>;
-using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, false>;
+// Warp-per-scene solve variants by staging slot (chunks of 16 bytes per lane):
+// a smaller slot stages fewer rows but leaves room for more warps per SM.
+template <uint32_t RB>
+using IterSmemW = IterSmemT<SOLVE_SMEM_BODIES, SOLVE_SMEM_CONSTRAINTS, RB>;
+using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, 0>;
+constexpr uint32_t SOLVE_VARIANTS = 3;
+__host__ __device__ constexpr uint32_t solveStageChunks(uint32_t variant) { return variant == 0 ? 0u : (variant == 1 ? 16u : RECBUF_CHUNKS); }
 
-template <uint32_t G, uint32_t CAPB, uint32_t CAPC, bool STAGE, typename Vel>
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC, uint32_t RB, typename Vel>
 __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
-                                             IterSmemT<CAPB, CAPC, STAGE>& sm, uint32_t nbPart, const Vel& V)
+                                             IterSmemT<CAPB, CAPC, RB>& sm, uint32_t nbPart, const Vel& V)
 {
 	constexpr uint32_t NT = Grp<G>::NT;
 	const uint32_t tid = Grp<G>::tid();
@@ -789,7 +863,7 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 	tgs::BodyTx* tx = w.tx + sc.solverStart;
 	Tr* pose = w.pose + sc.solverStart;
 	const uint32_t nc = nbPart ? ends[nbPart - 1] : 0;
-	const bool chunksOnChip = STAGE && nc <= CAPC;
+	const bool chunksOnChip = RB > 0 && nc <= CAPC;
 	if(chunksOnChip)
 		for(uint32_t r = tid; r < nc; r += NT) sm.chunks[r] = w.recChunks[sc.pairStart + r];
 	for(uint32_t i = tid; i < nTot; i += NT) V.set(i, vel[i].lin, vel[i].ang);
@@ -808,10 +882,10 @@ __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc&
 			{
 				tgs::ConstraintRecord* src = w.recs + sc.pairStart + r;
 				tgs::ConstraintRecord* rec = src;
-				if constexpr(STAGE)
+				if constexpr(RB > 0)
 				{
 					const uint32_t chunks = chunksOnChip ? sm.chunks[r] : w.recChunks[sc.pairStart + r];
-					if(chunks <= RECBUF_CHUNKS)
+					if(chunks <= RB)
 					{
 						float4* dst = sm.recBuf[threadIdx.x & 31];
 						const float4* g = reinterpret_cast<const float4*>(src);
@@ -966,9 +1040,9 @@ __global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
 
 // Iterations of one scene; afterwards the state this step wrote becomes the
 // scene's last-step state.
-template <uint32_t G, uint32_t CAPB, uint32_t CAPC, bool STAGE>
+template <uint32_t G, uint32_t CAPB, uint32_t CAPC, uint32_t RB>
 __device__ __forceinline__ void solveScene(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
-                                           IterSmemT<CAPB, CAPC, STAGE>& sm)
+                                           IterSmemT<CAPB, CAPC, RB>& sm)
 {
 	const uint32_t tid = Grp<G>::tid();
 	const uint32_t nbPart = w.nbPartitions[sid];
@@ -984,10 +1058,11 @@ __device__ __forceinline__ void solveScene(const WorldDev& w, const SceneDesc& s
 }
 
 constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the warp-per-scene solve kernel
+template <uint32_t RB>
 __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
-	IterSmem& sm = reinterpret_cast<IterSmem*>(stageSmem)[threadIdx.x >> 5];
+	IterSmemW<RB>& sm = reinterpret_cast<IterSmemW<RB>*>(stageSmem)[threadIdx.x >> 5];
 	uint32_t sid;
 	SceneDesc sc;
 	while(nextScene<1>(w, WC_SOLVE, false, sp, sid, sc, nullptr)) solveScene<1>(w, sc, sid, sp, sm);
@@ -1047,8 +1122,8 @@ struct World
 	world::StepParams params;
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
-	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve = 0, gridNp[world::NB_KINDS] = {};
-	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0;
+	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve[world::SOLVE_VARIANTS] = {}, gridNp[world::NB_KINDS] = {};
+	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0;
 	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
 	uint32_t pairsPerBody = 0;
 	// scenes above this many solver bodies run one block per scene (warp per scene below)
@@ -1056,6 +1131,7 @@ struct World
 	static constexpr uint32_t BIG_THREADS = world::BIG_WARPS * 32;
 	bool launchLarge() const { return maxSolverBodies > params.largeBodies; }
 	DevBuf<world::SceneDesc> scenes;
+	DevBuf<uint32_t> typeQueueSorted;
 	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue, activeCount;
 	DevBuf<uint8_t> recChunks;
 	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
@@ -1079,7 +1155,7 @@ struct World
 
 	static uint32_t pow2(uint32_t x) { uint32_t p = 1; while(p < x) p <<= 1; return p; }
 	// work counters of the broadphase and solve kernels, then the per-kind pair counts
-	static constexpr uint32_t COUNTERS = 8 + world::NB_KINDS;
+	static constexpr uint32_t COUNTERS = 8 + world::NB_KINDS + 4;
 	// broadphase, one narrowphase kernel per pair kind, batching, row preparation, solve
 	static constexpr uint32_t KERNELS_PER_STEP = 4 + world::NB_KINDS;
 
@@ -1093,7 +1169,8 @@ struct World
 		w.contactCount = contactCount.ptr; w.ordered = ordered.ptr; w.consList = consList.ptr; w.tag = tag.ptr; w.recs = recs.ptr;
 		w.vel = vel.ptr; w.tx = tx.ptr; w.data = data.ptr; w.pose = pose.ptr; w.progress = progress.ptr; w.maxNormal = maxNormal.ptr;
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
-		w.typeCount = workCounter.ptr + 8; w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
+		w.typeCount = workCounter.ptr + 8; w.pathCount = workCounter.ptr + 8 + world::NB_KINDS; w.typeQueueSorted = typeQueueSorted.ptr;
+		w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
 		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.recChunks = recChunks.ptr;
 		w.pairsPrev = pairsPrev.ptr; w.pairCountPrev = pairCountPrev.ptr; w.prevSlot = prevSlot.ptr; w.sceneParity = sceneParity.ptr;
 		for(int k = 0; k < 2; k++) { w.manifolds[k] = manifolds[k].ptr; w.frictionState[k] = frictionState[k].ptr; }
@@ -1138,7 +1215,7 @@ struct World
 			return GBPX_ERR_NOMEM;
 		if(sp.persistent &&
 		   (pairsPrev.reserve(pair) || prevSlot.reserve(pair) || manifolds[0].reserve(pair) || manifolds[1].reserve(pair) ||
-		    frictionState[0].reserve(pair) || frictionState[1].reserve(pair)))
+		    frictionState[0].reserve(pair) || frictionState[1].reserve(pair) || typeQueueSorted.reserve(2 * size_t(pair))))
 			return GBPX_ERR_NOMEM;
 		deviceBytes = size_t(pair) * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + sizeof(tgs::ConstraintRecord)) + size_t(b) * (96 + 4 + 16 + 4 + 24) +
 		              size_t(nbSolver) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + size_t(key) * 8;
@@ -1189,9 +1266,13 @@ struct World
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solveSmemBytes(world::STAGE_WARPS))));
 		GBPX_CUDA_TRY(gridFor(world::batchKernel, sms, gridBatch, solveSmemBytes(world::STAGE_WARPS)));
 		GBPX_CUDA_TRY(gridFor(world::prepKernel, sms, gridPrep));
-		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::SOLVE_WARPS))));
-		GBPX_CUDA_TRY(gridFor(world::solveKernel, sms, gridSolve, iterSmemBytes(world::SOLVE_WARPS), world::SOLVE_WARPS * 32));
+		for(uint32_t v = 0; v < world::SOLVE_VARIANTS; v++)
+		{
+			GBPX_CUDA_TRY(cudaFuncSetAttribute(solveKernels()[v], cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::SOLVE_WARPS, v))));
+			GBPX_CUDA_TRY(gridFor(solveKernels()[v], sms, gridSolve[v], iterSmemBytes(world::SOLVE_WARPS, v), world::SOLVE_WARPS * 32));
+		}
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
+		GBPX_CUDA_TRY(gridFor(world::orderByPathKernel, sms, gridOrder));
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::broadphaseBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::BpSmemBig))));
 		GBPX_CUDA_TRY(gridFor(world::broadphaseBigKernel, sms, gridBpBig, sizeof(world::BpSmemBig), int(BIG_THREADS)));
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::SolveSmemBig))));
@@ -1213,7 +1294,16 @@ struct World
 	}
 	static size_t bpSmemBytes(uint32_t warps) { return warps * sizeof(world::BpSmem); }
 	static size_t solveSmemBytes(uint32_t warps) { return warps * sizeof(world::SolveSmem); }
-	static size_t iterSmemBytes(uint32_t warps) { return warps * sizeof(world::IterSmem); }
+	static size_t iterSmemBytes(uint32_t warps, uint32_t variant)
+	{
+		const size_t per = variant == 0 ? sizeof(world::IterSmemW<0>) : (variant == 1 ? sizeof(world::IterSmemW<16>) : sizeof(world::IterSmemW<32>));
+		return warps * per;
+	}
+	static const StageKernel* solveKernels()
+	{
+		static const StageKernel k[world::SOLVE_VARIANTS] = {world::solveKernel<0>, world::solveKernel<16>, world::solveKernel<world::RECBUF_CHUNKS>};
+		return k;
+	}
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
 	static cudaError_t gridFor(StageKernel k, int sms, uint32_t& grid, size_t smem = 0, int threads = 128)
 	{
@@ -1229,7 +1319,8 @@ struct World
 	int launchStep(uint32_t plainScene = ~0u)
 	{
 		world::WorldDev w = dev();
-		uint32_t gBp = gridBlocks, gBatch = gridBatch, gPrep = gridPrep, gSolve = gridSolve, threads = 128;
+		const uint32_t sv = params.solveVariant;
+		uint32_t gBp = gridBlocks, gBatch = gridBatch, gPrep = gridPrep, gSolve = gridSolve[sv], threads = 128;
 		const bool plain = plainScene < nbScenes;
 		if(plain)
 		{
@@ -1244,12 +1335,15 @@ struct World
 		world::broadphaseKernel<<<gBp, threads, bpSmemBytes(threads / 32), stream>>>(w, params);
 		if(big) world::broadphaseBigKernel<<<plain ? 1u : gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), stream>>>(w, params);
 		for(uint32_t k = 0; k < world::NB_KINDS; k++)
+		{
+			if(k == 7 && params.persistent) world::orderByPathKernel<<<plain ? std::min(gridOrder, 8u) : gridOrder, 128, 0, stream>>>(w, params);
 			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
+		}
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
 		if(big) world::batchBigKernel<<<plain ? 1u : gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
 		const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
-		world::solveKernel<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32), stream>>>(w, params);
+		solveKernels()[sv]<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32, sv), stream>>>(w, params);
 		if(big) world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
@@ -1312,6 +1406,7 @@ struct World
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			for(uint32_t t = 0; t < world::NB_KINDS; t++)
 			{
+				if(t == 7 && params.persistent) world::orderByPathKernel<<<gridOrder, 128, 0, stream>>>(w, params);
 				npKernels()[t]<<<gridNp[t], 128, 0, stream>>>(w, params);
 				GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			}
@@ -1320,7 +1415,8 @@ struct World
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			world::prepKernel<<<gridPrep, 128, 0, stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
-			world::solveKernel<<<gridSolve, world::SOLVE_WARPS * 32, iterSmemBytes(world::SOLVE_WARPS), stream>>>(w, params);
+			solveKernels()[params.solveVariant]<<<gridSolve[params.solveVariant], world::SOLVE_WARPS * 32,
+			                                      iterSmemBytes(world::SOLVE_WARPS, params.solveVariant), stream>>>(w, params);
 			if(big) world::solveBigKernel<<<gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			GBPX_CUDA_TRY(cudaGetLastError());
@@ -1384,6 +1480,7 @@ struct World
 		graphExec = nullptr;
 		pairsPrev.release(); pairCountPrev.release(); prevSlot.release(); sceneParity.release();
 		for(int k = 0; k < 2; k++) { manifolds[k].release(); frictionState[k].release(); }
+		typeQueueSorted.release();
 		scenes.release(); typeQueue.release(); slotScene.release(); activeCount.release(); recChunks.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
@@ -1420,6 +1517,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
+	sp.solveVariant = gbpx::world::SOLVE_VARIANTS - 1;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -1492,7 +1590,9 @@ GBPX_API int gbpx_world_info(void* wv, uint64_t* out8)
 	World* w = static_cast<World*>(wv);
 	if(!w || !out8) return GBPX_ERR_INVALID;
 	out8[0] = w->nbScenes; out8[1] = w->nbBodies; out8[2] = w->nbStatics; out8[3] = w->nbPairSlots; out8[4] = w->gridBlocks;
-	out8[5] = w->deviceBytes; out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? 3u : 0u); out8[7] = w->params.largeBodies;
+	out8[5] = w->deviceBytes;
+	out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? 3u : 0u) + (w->params.persistent ? 1u : 0u);
+	out8[7] = w->params.largeBodies;
 	return GBPX_OK;
 }
 
@@ -1593,7 +1693,9 @@ GBPX_API int gbpx_world_set_large_bodies(void* wv, uint32_t largeBodies)
 	return GBPX_OK;
 }
 
-// ---- Autotuner of the block-per-scene threshold ----
+GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant);
+
+// ---- Autotuner of the block-per-scene threshold and the solve staging slot ----
 // The scene stages run warp-per-scene or block-per-scene kernels by scene size
 // (gbpx_world_set_large_bodies).  The best threshold depends on the scene-size
 // histogram: the autotuner takes a size-stratified sample of the world's scenes
@@ -1620,25 +1722,28 @@ std::string histogramKey(const std::vector<gbpx::world::SceneDesc>& sc)
 	}
 	return key;
 }
-std::map<std::string, uint32_t>& tunedThresholds()
+std::map<std::string, std::pair<uint32_t, uint32_t>>& tunedThresholds()
 {
-	static std::map<std::string, uint32_t> m;
+	static std::map<std::string, std::pair<uint32_t, uint32_t>> m;
 	return m;
 }
 } // namespace
 
-GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, float* outMs)
+GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, uint32_t* outSolveVariant,
+                                 float* outMs)
 {
 	World* w = static_cast<World*>(wv);
-	if(!w || !sampleScenes || !steps || !outLargeBodies) return GBPX_ERR_INVALID;
+	if(!w || !sampleScenes || !steps || !outLargeBodies || !outSolveVariant) return GBPX_ERR_INVALID;
 	const std::string key = histogramKey(w->hScenes);
 	auto& cache = tunedThresholds();
 	auto hit = cache.find(key);
 	if(hit != cache.end())
 	{
-		*outLargeBodies = hit->second;
+		*outLargeBodies = hit->second.first;
+		*outSolveVariant = hit->second.second;
 		if(outMs) *outMs = 0.0f;
-		return gbpx_world_set_large_bodies(wv, hit->second);
+		const int rc = gbpx_world_set_large_bodies(wv, hit->second.first);
+		return rc ? rc : gbpx_world_set_solve_variant(wv, hit->second.second);
 	}
 	// size-stratified sample: every k-th scene in order of size
 	std::vector<uint32_t> order(w->nbScenes);
@@ -1682,39 +1787,73 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	const uint32_t cands[] = {64u, 128u, 256u, 512u, 1024u, 2048u, 0xffffffffu};
 	std::vector<uint32_t> sizes;
 	for(uint32_t k = 0; k < m; k++) sizes.push_back(bc[k] + sc[k]);
-	uint32_t best = w->params.largeBodies;
-	float bestMs = 3.4e38f;
-	int lastLarge = -1;
 	cudaEvent_t e0, e1;
 	GBPX_CUDA_TRY(cudaEventCreate(&e0));
 	GBPX_CUDA_TRY(cudaEventCreate(&e1));
+	auto timeConfig = [&](uint32_t threshold, uint32_t variant, float& ms) -> int {
+		t->params.largeBodies = threshold;
+		t->params.solveVariant = variant;
+		if(t->graphExec) { cudaGraphExecDestroy(t->graphExec); t->graphExec = nullptr; }
+		int r = t->step(2, true);
+		if(r) return r;
+		GBPX_CUDA_TRY(cudaEventRecord(e0, t->stream));
+		r = t->step(steps, true);
+		if(r) return r;
+		GBPX_CUDA_TRY(cudaEventRecord(e1, t->stream));
+		GBPX_CUDA_TRY(cudaEventSynchronize(e1));
+		GBPX_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+		return GBPX_OK;
+	};
+	// the threshold first (default staging), then the staging slot at that threshold
+	uint32_t best = w->params.largeBodies, bestVariant = w->params.solveVariant;
+	float bestMs = 3.4e38f;
+	int lastLarge = -1;
 	for(uint32_t c : cands)
 	{
 		const int nLarge = int(std::count_if(sizes.begin(), sizes.end(), [&](uint32_t x) { return x > c; }));
 		if(nLarge == lastLarge) continue;
 		lastLarge = nLarge;
-		t->params.largeBodies = c;
-		if(t->graphExec) { cudaGraphExecDestroy(t->graphExec); t->graphExec = nullptr; }
-		rc = t->step(2, true);
-		if(rc) break;
-		cudaEventRecord(e0, t->stream);
-		rc = t->step(steps, true);
-		if(rc) break;
-		cudaEventRecord(e1, t->stream);
-		cudaEventSynchronize(e1);
 		float ms = 0.0f;
-		cudaEventElapsedTime(&ms, e0, e1);
+		rc = timeConfig(c, bestVariant, ms);
+		if(rc) break;
 		if(ms < bestMs) { bestMs = ms; best = c; }
+	}
+	const bool anySmall = std::any_of(sizes.begin(), sizes.end(), [&](uint32_t x) { return x <= best; });
+	for(uint32_t v = 0; v < gbpx::world::SOLVE_VARIANTS && !rc && anySmall; v++)
+	{
+		if(v == bestVariant) continue;
+		float ms = 0.0f;
+		rc = timeConfig(best, v, ms);
+		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	t->release();
 	delete t;
 	if(rc) return rc;
-	cache[key] = best;
+	cache[key] = std::make_pair(best, bestVariant);
 	*outLargeBodies = best;
+	*outSolveVariant = bestVariant;
 	if(outMs) *outMs = bestMs / float(steps);
-	return gbpx_world_set_large_bodies(wv, best);
+	rc = gbpx_world_set_large_bodies(wv, best);
+	return rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
+}
+
+// Staging slot of the warp-per-scene solve kernel: 0 = rows used in place,
+// 1 = 256 bytes per lane, 2 = 512 bytes per lane (default).  A smaller slot
+// leaves shared memory for more warps per SM.  Results do not depend on it.
+GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || variant >= gbpx::world::SOLVE_VARIANTS) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	w->params.solveVariant = variant;
+	if(w->graphExec)
+	{
+		cudaGraphExecDestroy(w->graphExec);
+		w->graphExec = nullptr;
+	}
+	return GBPX_OK;
 }
 
 // Pairs of each pair kind in the last step (sphere-sphere, sphere-plane,
@@ -1822,7 +1961,7 @@ struct Server
 	{
 		const size_t pair = World::pow2(capacity * pairsPerBody + capacity * statics);
 		const size_t key = World::pow2(capacity);
-		const size_t persistentPair = persistent ? 8 + 2 * (sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0;
+		const size_t persistentPair = persistent ? 16 + 2 * (sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0;
 		return pair * (4 + 128 + 4 * 4 + 4 + 4 * world::NB_KINDS + 4 + 4 + sizeof(tgs::ConstraintRecord) + persistentPair) +
 		       size_t(capacity) * (96 + 4 + 16 + 4 + 24) +
 		       size_t(capacity + statics) * (sizeof(tgs::BodyVel) + sizeof(tgs::BodyTx) + sizeof(tgs::BodyData) + sizeof(Tr) + 16) + key * 8 +
@@ -2004,6 +2143,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
+	sp.solveVariant = gbpx::world::SOLVE_VARIANTS - 1;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);

@@ -43,7 +43,8 @@ def _setup():
         L.gbpx_world_kind_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gbpx_world_set_large_bodies.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         L.gbpx_world_autotune.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
-                                          ctypes.POINTER(ctypes.c_float)]
+                                          ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_float)]
+        L.gbpx_world_set_solve_variant.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         L.gbpx_world_time_stages.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         L.gbpx_world_step_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_float)]
@@ -139,15 +140,23 @@ class World:
     def autotune(self, sample_scenes=None, steps=3):
         """Picks the block-per-scene threshold for this world's scene-size histogram
         (timed on a temporary copy of a size-stratified sample of the scenes, all of
-        them by default; cached per histogram); returns (threshold, ms per step of
-        the sample with it, 0 if cached).  The sample should load the GPU like the
-        whole world: warp-per-scene kernels need many scenes to fill it."""
+        them by default; cached per histogram), then the solve staging slot; returns
+        (threshold, ms per step of the sample with them, 0 if cached) and keeps the
+        slot in self.solve_variant.  The sample should load the GPU like the whole
+        world: warp-per-scene kernels need many scenes to fill it."""
         if sample_scenes is None:
             sample_scenes = len(self._keep[0])
         t = ctypes.c_uint32(0)
+        v = ctypes.c_uint32(0)
         ms = ctypes.c_float(0)
-        check(self._L.gbpx_world_autotune(self._h, sample_scenes, steps, ctypes.byref(t), ctypes.byref(ms)), "gbpx_world_autotune")
+        check(self._L.gbpx_world_autotune(self._h, sample_scenes, steps, ctypes.byref(t), ctypes.byref(v), ctypes.byref(ms)),
+              "gbpx_world_autotune")
+        self.solve_variant = v.value
         return t.value, ms.value
+
+    def set_solve_variant(self, v):
+        """Staging slot of the warp-per-scene solve (0 none, 1 256 B, 2 512 B per lane)."""
+        check(self._L.gbpx_world_set_solve_variant(self._h, int(v)), "gbpx_world_set_solve_variant")
 
     def kind_counts(self):
         """Pairs of each pair kind in the last step, {narrowphase stage name: pairs}."""
