@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(128) orderByPathKernel(WorldDev w, StepParams 
 // Narrowphase of one pair kind over every scene: a thread per queued pair slot,
 // so each warp runs one contact generator on uniform work.
 template <int TA, int TB>
-__global__ void __launch_bounds__(128) narrowphaseKernel(WorldDev w, StepParams sp)
+__global__ void __launch_bounds__(128, (TA == 3 && TB == 3) ? 4 : 5) narrowphaseKernel(WorldDev w, StepParams sp)
 {
 	constexpr uint32_t KIND = TA == 0 ? uint32_t(TB) : (TA == 1 ? uint32_t(TB + 2) : (TA == 2 ? uint32_t(TB + 4) : 8u));
 	const uint32_t count = w.typeCount[KIND];
@@ -1032,7 +1032,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) batchBigKernel(WorldDev w, Ste
 }
 
 // Row preparation of every scene's constraints: a thread per constraint.
-__global__ void __launch_bounds__(128) prepKernel(WorldDev w, StepParams sp)
+__global__ void __launch_bounds__(128, 5) prepKernel(WorldDev w, StepParams sp)
 {
 	const uint32_t count = w.workCounter[WC_PREP];
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
@@ -1117,6 +1117,8 @@ __global__ void statsKernel(const SceneDesc* __restrict__ scenes, uint32_t nbSce
 struct World
 {
 	cudaStream_t stream = 0;
+	cudaStream_t sideStream = 0;   // block-per-scene kernels run beside the warp-per-scene ones
+	cudaEvent_t forkEv[3] = {}, joinEv[3] = {};
 	cudaGraphExec_t graphExec = nullptr;
 	uint32_t graphSteps = 0;
 	world::StepParams params;
@@ -1204,6 +1206,12 @@ struct World
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
 		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&sideStream, cudaStreamNonBlocking));
+		for(int k = 0; k < 3; k++)
+		{
+			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&forkEv[k], cudaEventDisableTiming));
+			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&joinEv[k], cudaEventDisableTiming));
+		}
 		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || activeCount.reserve(2) || recChunks.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
 		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
 		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
@@ -1331,20 +1339,46 @@ struct World
 			threads = 32;
 		}
 		const bool big = launchLarge();
+		// block-per-scene kernels run on the side stream, concurrently with the
+		// warp-per-scene ones (separate work counters); joined before the next stage
+		auto fork = [&](int k) -> cudaError_t {
+			cudaError_t e = cudaEventRecord(forkEv[k], stream);
+			return e != cudaSuccess ? e : cudaStreamWaitEvent(sideStream, forkEv[k], 0);
+		};
+		auto join = [&](int k) -> cudaError_t {
+			cudaError_t e = cudaEventRecord(joinEv[k], sideStream);
+			return e != cudaSuccess ? e : cudaStreamWaitEvent(stream, joinEv[k], 0);
+		};
+		const cudaStream_t bigStream = plain ? stream : sideStream;
 		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
+		if(big && !plain) GBPX_CUDA_TRY(fork(0));
 		world::broadphaseKernel<<<gBp, threads, bpSmemBytes(threads / 32), stream>>>(w, params);
-		if(big) world::broadphaseBigKernel<<<plain ? 1u : gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), stream>>>(w, params);
+		if(big)
+		{
+			world::broadphaseBigKernel<<<plain ? 1u : gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), bigStream>>>(w, params);
+			if(!plain) GBPX_CUDA_TRY(join(0));
+		}
 		for(uint32_t k = 0; k < world::NB_KINDS; k++)
 		{
 			if(k == 7 && params.persistent) world::orderByPathKernel<<<plain ? std::min(gridOrder, 8u) : gridOrder, 128, 0, stream>>>(w, params);
 			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
 		}
+		if(big && !plain) GBPX_CUDA_TRY(fork(1));
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
-		if(big) world::batchBigKernel<<<plain ? 1u : gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
+		if(big)
+		{
+			world::batchBigKernel<<<plain ? 1u : gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), bigStream>>>(w, params);
+			if(!plain) GBPX_CUDA_TRY(join(1));
+		}
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
 		const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
+		if(big && !plain) GBPX_CUDA_TRY(fork(2));
 		solveKernels()[sv]<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32, sv), stream>>>(w, params);
-		if(big) world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
+		if(big)
+		{
+			world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), bigStream>>>(w, params);
+			if(!plain) GBPX_CUDA_TRY(join(2));
+		}
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
 	}
@@ -1486,6 +1520,14 @@ struct World
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
 		keys.release(); stats.release(); identity.release(); recs.release(); vel.release(); tx.release(); data.release(); pose.release(); hStage.release();
+		if(sideStream) { cudaStreamSynchronize(sideStream); cudaStreamDestroy(sideStream); }
+		sideStream = 0;
+		for(int k = 0; k < 3; k++)
+		{
+			if(forkEv[k]) cudaEventDestroy(forkEv[k]);
+			if(joinEv[k]) cudaEventDestroy(joinEv[k]);
+			forkEv[k] = joinEv[k] = nullptr;
+		}
 		if(stream) cudaStreamDestroy(stream);
 		stream = 0;
 	}
