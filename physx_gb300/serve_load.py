@@ -62,7 +62,7 @@ def run_poisson(duration=10.0, rate=20000.0, budget_bytes=150e9, nmin=16, nmax=4
     fails = 0
     while fails < 50:
         fails = 0 if admit_one() else fails + 1
-    req_scene, req_steps, lat_all, lat_scene = {}, {}, [], []
+    req_scene, req_steps, lat_all, lat_scene, lat_steps = {}, {}, [], [], []
     tag = 0
     t0 = srv.clock()
     t_next = t0
@@ -89,6 +89,7 @@ def run_poisson(duration=10.0, rate=20000.0, budget_bytes=150e9, nmin=16, nmax=4
             done_steps[sid] += n
             lat_all.append(l_)
             lat_scene.append(sizes[sid])
+            lat_steps.append(n)
             if owed[sid] == 0 and done_steps[sid] >= lifetime[sid] and len(live) > 1:
                 srv.retire(sid)
                 live.remove(sid)
@@ -100,8 +101,10 @@ def run_poisson(duration=10.0, rate=20000.0, budget_bytes=150e9, nmin=16, nmax=4
     lat = np.array(lat_all)
     sz = np.array(lat_scene)
     m512 = (sz > 256) & (sz <= 512)
+    per_step = lat / np.maximum(np.array(lat_steps), 1)   # a request of n steps: its latency per step
     pct = lambda a, q: float(np.percentile(a, q) * 1000.0) if len(a) else None  # noqa: E731
     return dict(duration_s=elapsed, rate_per_s=rate, submitted=tag, completed=len(lat), completed_per_s=len(lat) / elapsed,
                 body_steps_per_s=st["body_steps"] / elapsed, p50_ms=pct(lat, 50), p99_ms=pct(lat, 99), p50_ms_512=pct(lat[m512], 50),
-                p99_ms_512=pct(lat[m512], 99), live_scenes=st["live"], pool_slots=int(sum(slots)), retired=retired,
+                p99_ms_512=pct(lat[m512], 99), p50_ms_per_step_512=pct(per_step[m512], 50), p99_ms_per_step_512=pct(per_step[m512], 99),
+                live_scenes=st["live"], pool_slots=int(sum(slots)), retired=retired,
                 admitted_after_start=admitted, classes=list(classes), slots=[int(s) for s in slots])
