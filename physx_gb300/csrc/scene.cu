@@ -206,7 +206,8 @@ __global__ void countConstraintsKernel(const uint32_t* __restrict__ contactCount
 }
 
 __global__ void emitConstraintsKernel(const uint32_t* __restrict__ contactCount, const unsigned long long* __restrict__ keys, uint32_t n,
-                                      const uint32_t* __restrict__ blockOffsets, uint32_t* __restrict__ consPair, uint32_t* __restrict__ consBodies)
+                                      const uint32_t* __restrict__ blockOffsets, uint32_t* __restrict__ consPair, uint32_t* __restrict__ consA,
+                                      uint32_t* __restrict__ consB)
 {
 	__shared__ uint32_t warpCounts[32];
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,8 +234,8 @@ __global__ void emitConstraintsKernel(const uint32_t* __restrict__ contactCount,
 		const uint32_t r = blockOffsets[blockIdx.x] + warpCounts[warp] + __popc(ballot & laneMaskLt());
 		const unsigned long long key = keys[k];
 		consPair[r] = k;
-		consBodies[2 * r] = uint32_t(key >> 32);
-		consBodies[2 * r + 1] = uint32_t(key);
+		consA[r] = uint32_t(key >> 32);
+		consB[r] = uint32_t(key);
 	}
 }
 
@@ -399,7 +400,7 @@ struct Scene
 	DevBuf<float4> geoms, staticGeoms;
 	DevBuf<float> frictionCoef, staticPose, bounds;
 	DevBuf<unsigned long long> keysPrev, totalContacts;
-	DevBuf<uint32_t> queue, kindCount, prevSlot, contactCount, blockCounts, consPair, consBodies, order, partEnds, orderedPair;
+	DevBuf<uint32_t> queue, kindCount, prevSlot, contactCount, blockCounts, consPair, consA, consB, order, partEnds, orderedPair;
 	DevBuf<float4> contacts;
 	DevBuf<np::ManifoldRecord> manifolds[2];
 	DevBuf<tgs::FrictionState> frictionState[2];
@@ -408,7 +409,7 @@ struct Scene
 	DevBuf<tgs::BodyData> data;
 	DevBuf<Tr> pose;
 	DevBuf<tgs::ConstraintRecord> recs;
-	HostBuf<uint32_t> hConsBodies, hSmall;
+	HostBuf<uint32_t> hConsA, hConsB, hOrder, hSmall;
 	HostBuf<unsigned long long> hTotal;
 	uint32_t parity = 0, nbPairs = 0, nbPrev = 0, nbConstraints = 0, nbPartitions = 0;
 	uint64_t nbContacts = 0;
@@ -479,9 +480,9 @@ struct Scene
 			if(e) cudaEventDestroy(e);
 		bodies.release(); types.release(); staticTypes.release(); geoms.release(); staticGeoms.release(); frictionCoef.release();
 		staticPose.release(); bounds.release(); keysPrev.release(); totalContacts.release(); queue.release(); kindCount.release();
-		prevSlot.release(); contactCount.release(); blockCounts.release(); consPair.release(); consBodies.release(); order.release();
+		prevSlot.release(); contactCount.release(); blockCounts.release(); consPair.release(); consA.release(); consB.release(); order.release();
 		partEnds.release(); orderedPair.release(); contacts.release(); vel.release(); tx.release(); data.release(); pose.release();
-		recs.release(); hConsBodies.release(); hSmall.release(); hTotal.release();
+		recs.release(); hConsA.release(); hConsB.release(); hOrder.release(); hSmall.release(); hTotal.release();
 		for(int k = 0; k < 2; k++) { manifolds[k].release(); frictionState[k].release(); }
 		if(bp) gbpx_bp_release(bp);
 		bp = nullptr;
@@ -494,8 +495,9 @@ struct Scene
 		if(need <= pairCap) return GBPX_OK;
 		const size_t cap = std::max<size_t>(need + need / 4, 1024);
 		if(queue.reserve(size_t(NB_KINDS) * cap) || prevSlot.reserve(cap) || contactCount.reserve(cap) || blockCounts.reserve(cap / 256 + 2) ||
-		   consPair.reserve(cap) || consBodies.reserve(2 * cap) || order.reserve(cap) || partEnds.reserve(cap) || orderedPair.reserve(cap) ||
-		   contacts.reserve(8 * cap) || recs.reserve(cap) || hConsBodies.reserve(2 * cap))
+		   consPair.reserve(cap) || consA.reserve(cap) || consB.reserve(cap) || order.reserve(cap) || partEnds.reserve(cap) ||
+		   orderedPair.reserve(cap) || contacts.reserve(8 * cap) || recs.reserve(cap) || hConsA.reserve(cap) || hConsB.reserve(cap) ||
+		   hOrder.reserve(cap))
 			return GBPX_ERR_NOMEM;
 		if(sp.persistent)
 		{
@@ -559,7 +561,7 @@ struct Scene
 			countConstraintsKernel<<<nb, 256, 0, stream>>>(contactCount.ptr, nbPairs, blockCounts.ptr, totalContacts.ptr);
 			GBPX_CUDA_TRY(cudaMemsetAsync(blockCounts.ptr + nb, 0, 4, stream));
 			rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nb + 1);
-			emitConstraintsKernel<<<nb, 256, 0, stream>>>(contactCount.ptr, keys, nbPairs, blockCounts.ptr, consPair.ptr, consBodies.ptr);
+			emitConstraintsKernel<<<nb, 256, 0, stream>>>(contactCount.ptr, keys, nbPairs, blockCounts.ptr, consPair.ptr, consA.ptr, consB.ptr);
 			GBPX_CUDA_TRY(cudaGetLastError());
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hSmall.ptr, blockCounts.ptr + nb, 4, cudaMemcpyDeviceToHost, stream));
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hTotal.ptr, totalContacts.ptr, 8, cudaMemcpyDeviceToHost, stream));
@@ -571,16 +573,12 @@ struct Scene
 		batching::Result batch;
 		if(nc)
 		{
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hConsBodies.ptr, consBodies.ptr, size_t(nc) * 8, cudaMemcpyDeviceToHost, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hConsA.ptr, consA.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hConsB.ptr, consB.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
 			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
-			std::vector<uint32_t> ba(nc), bb(nc);
-			for(uint32_t r = 0; r < nc; r++)
-			{
-				ba[r] = hConsBodies.ptr[2 * r];
-				bb[r] = hConsBodies.ptr[2 * r + 1];
-			}
-			batching::partition(ba.data(), bb.data(), nc, nbDyn, batch);
-			GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, batch.order.data(), size_t(nc) * 4, cudaMemcpyHostToDevice, stream));
+			batching::partition(hConsA.ptr, hConsB.ptr, nc, nbDyn, batch);
+			memcpy(hOrder.ptr, batch.order.data(), size_t(nc) * 4);
+			GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, hOrder.ptr, size_t(nc) * 4, cudaMemcpyHostToDevice, stream));
 			GBPX_CUDA_TRY(cudaMemcpyAsync(partEnds.ptr, batch.partitionEnds.data(), batch.partitionEnds.size() * 4, cudaMemcpyHostToDevice, stream));
 		}
 		nbPartitions = uint32_t(batch.partitionEnds.size());
