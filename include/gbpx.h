@@ -214,10 +214,11 @@ int gbpx_world_set_large_bodies(void* world, uint32_t largeBodies);
  * chosen threshold's ms per step on the sample (0 when cached). */
 int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, uint32_t* outSolveVariant,
                         float* outMs);
-/* Staging slot of the warp-per-scene solve: 0 = rows used in place, 1 = 256
- * bytes per lane, 2 = 512 bytes per lane (default; a smaller slot leaves room
- * for more warps per SM).  Results do not depend on it.  The autotuner sets it
- * after the threshold. */
+/* Workspace of the warp-per-scene solve: variants 0-2 keep the body
+ * velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
+ * (2 is the default), variants 3-5 the same with the velocities left in HBM (a
+ * smaller workspace leaves room for more warps per SM).  Results do not depend
+ * on it.  The autotuner sets it after the threshold. */
 int gbpx_world_set_solve_variant(void* world, uint32_t variant);
 /* Pairs of each pair kind in the last step, in the kind order of the
  * narrowphase launches (sphere-sphere ... box-box): 9 counts. */

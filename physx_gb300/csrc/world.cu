@@ -843,13 +843,13 @@ struct __align__(16) IterSmemT
 	uint8_t chunks[CAPC];
 	uint32_t bc;
 };
-// Warp-per-scene solve variants by staging slot (chunks of 16 bytes per lane):
-// a smaller slot stages fewer rows but leaves room for more warps per SM.
-template <uint32_t RB>
-using IterSmemW = IterSmemT<SOLVE_SMEM_BODIES, SOLVE_SMEM_CONSTRAINTS, RB>;
+// Warp-per-scene solve variants: staging slot (chunks of 16 bytes per lane) and
+// whether the body velocities sit in shared memory (CAPB = SOLVE_SMEM_BODIES) or
+// stay in HBM/L1 (CAPB = 1).  Smaller workspaces leave room for more warps per SM.
+template <uint32_t CAPB, uint32_t RB>
+using IterSmemW = IterSmemT<CAPB, SOLVE_SMEM_CONSTRAINTS, RB>;
 using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, 0>;
-constexpr uint32_t SOLVE_VARIANTS = 3;
-__host__ __device__ constexpr uint32_t solveStageChunks(uint32_t variant) { return variant == 0 ? 0u : (variant == 1 ? 16u : RECBUF_CHUNKS); }
+constexpr uint32_t SOLVE_VARIANTS = 6;   // (velocities on chip, 0 / 256 / 512 B staging), (velocities in HBM, 0 / 256 / 512 B)
 
 template <uint32_t G, uint32_t CAPB, uint32_t CAPC, uint32_t RB, typename Vel>
 __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
@@ -1058,11 +1058,11 @@ __device__ __forceinline__ void solveScene(const WorldDev& w, const SceneDesc& s
 }
 
 constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the warp-per-scene solve kernel
-template <uint32_t RB>
+template <uint32_t CAPB, uint32_t RB>
 __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, StepParams sp)
 {
 	extern __shared__ __align__(16) unsigned char stageSmem[];
-	IterSmemW<RB>& sm = reinterpret_cast<IterSmemW<RB>*>(stageSmem)[threadIdx.x >> 5];
+	IterSmemW<CAPB, RB>& sm = reinterpret_cast<IterSmemW<CAPB, RB>*>(stageSmem)[threadIdx.x >> 5];
 	uint32_t sid;
 	SceneDesc sc;
 	while(nextScene<1>(w, WC_SOLVE, false, sp, sid, sc, nullptr)) solveScene<1>(w, sc, sid, sp, sm);
@@ -1304,12 +1304,18 @@ struct World
 	static size_t solveSmemBytes(uint32_t warps) { return warps * sizeof(world::SolveSmem); }
 	static size_t iterSmemBytes(uint32_t warps, uint32_t variant)
 	{
-		const size_t per = variant == 0 ? sizeof(world::IterSmemW<0>) : (variant == 1 ? sizeof(world::IterSmemW<16>) : sizeof(world::IterSmemW<32>));
-		return warps * per;
+		using namespace world;
+		static const size_t per[SOLVE_VARIANTS] = {sizeof(IterSmemW<SOLVE_SMEM_BODIES, 0>), sizeof(IterSmemW<SOLVE_SMEM_BODIES, 16>),
+		                                           sizeof(IterSmemW<SOLVE_SMEM_BODIES, RECBUF_CHUNKS>), sizeof(IterSmemW<1, 0>),
+		                                           sizeof(IterSmemW<1, 16>), sizeof(IterSmemW<1, RECBUF_CHUNKS>)};
+		return warps * per[variant];
 	}
 	static const StageKernel* solveKernels()
 	{
-		static const StageKernel k[world::SOLVE_VARIANTS] = {world::solveKernel<0>, world::solveKernel<16>, world::solveKernel<world::RECBUF_CHUNKS>};
+		using namespace world;
+		static const StageKernel k[SOLVE_VARIANTS] = {solveKernel<SOLVE_SMEM_BODIES, 0>, solveKernel<SOLVE_SMEM_BODIES, 16>,
+		                                              solveKernel<SOLVE_SMEM_BODIES, RECBUF_CHUNKS>, solveKernel<1, 0>, solveKernel<1, 16>,
+		                                              solveKernel<1, RECBUF_CHUNKS>};
 		return k;
 	}
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
@@ -1559,7 +1565,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
-	sp.solveVariant = gbpx::world::SOLVE_VARIANTS - 1;
+	sp.solveVariant = 2;   // velocities on chip, 512-byte staging
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -1881,9 +1887,11 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	return rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
 }
 
-// Staging slot of the warp-per-scene solve kernel: 0 = rows used in place,
-// 1 = 256 bytes per lane, 2 = 512 bytes per lane (default).  A smaller slot
-// leaves shared memory for more warps per SM.  Results do not depend on it.
+// Workspace of the warp-per-scene solve kernel: variants 0-2 keep the body
+// velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
+// (2 is the default), variants 3-5 the same with the velocities left in HBM.
+// A smaller workspace leaves room for more warps per SM.  Results do not depend
+// on it.
 GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant)
 {
 	World* w = static_cast<World*>(wv);
@@ -2185,7 +2193,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
-	sp.solveVariant = gbpx::world::SOLVE_VARIANTS - 1;
+	sp.solveVariant = 2;   // velocities on chip, 512-byte staging
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);

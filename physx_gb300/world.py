@@ -155,7 +155,9 @@ class World:
         return t.value, ms.value
 
     def set_solve_variant(self, v):
-        """Staging slot of the warp-per-scene solve (0 none, 1 256 B, 2 512 B per lane)."""
+        """Workspace of the warp-per-scene solve: 0-2 velocities in shared memory with
+        0 / 256 / 512 B of row staging per lane (2 default), 3-5 the same with the
+        velocities in HBM.  Results do not depend on it."""
         check(self._L.gbpx_world_set_solve_variant(self._h, int(v)), "gbpx_world_set_solve_variant")
 
     def kind_counts(self):
