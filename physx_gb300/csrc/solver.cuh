@@ -43,9 +43,11 @@ struct RigidBody   // PxRigidBodyData (physx/include/PxImmediateMode.h:68), 96 b
 };
 static_assert(sizeof(RigidBody) == 96, "PxRigidBodyData layout");
 
-struct BodyVel { V3 lin, ang, dLin, dAng; float maxAngVel; int kinematic; };      // PxTGSSolverBodyVel fields
-struct BodyTx { Q dq; V3 p; M33 sqrtInvInertia; };                                 // PxTGSSolverBodyTxInertia
-struct BodyData { V3 origLin, origAng; float maxContactImpulse, penBiasClamp, invMass; };  // PxTGSSolverBodyData
+// Solver-body records, 16-byte aligned (64 / 64 / 48 bytes) so that a record spans
+// whole 32-byte sectors: every constraint reads two of each.
+struct __align__(16) BodyVel { V3 lin, ang, dLin, dAng; float maxAngVel; int kinematic; };      // PxTGSSolverBodyVel fields
+struct __align__(16) BodyTx { Q dq; V3 p; M33 sqrtInvInertia; };                                 // PxTGSSolverBodyTxInertia
+struct __align__(16) BodyData { V3 origLin, origAng; float maxContactImpulse, penBiasClamp, invMass; };  // PxTGSSolverBodyData
 
 struct Contact { V3 n; float sep; V3 p; float staticFriction, dynamicFriction, restitution; };
 
