@@ -12,7 +12,7 @@ namespace gbpx
 {
 struct V3 { float x, y, z; };
 struct Q { float x, y, z, w; };
-struct Tr { Q q; V3 p; };          // PxTransform
+struct __align__(16) Tr { Q q; V3 p; };   // PxTransform fields (32 bytes in device arrays: whole sectors)
 struct M33 { V3 c0, c1, c2; };     // column-major, as PxMat33 / Mat33V
 
 __device__ __forceinline__ V3 v3(float x, float y, float z) { V3 r = {x, y, z}; return r; }
