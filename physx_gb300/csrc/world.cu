@@ -1,28 +1,30 @@
 // Batched multi-scene rigid-body step for the GB300.
 //
-// Thousands of independent scenes advance in ONE persistent launch per step:
-// each warp takes the next scene from a work table sorted by decreasing size
-// (largest first, so the tail is short) and runs the whole immediate-mode
-// pipeline for it:
-//   1. bounds + broadphase: AABBs, warp bitonic sort by encoded min X, sweep
-//      with the reference ABP's closed-interval test (X as encodeFloat keys,
-//      Y/Z as floats), bitonic sort of the pair keys -> pairs ordered by
-//      (id0, id1), statics after the dynamic bodies;
-//   2. narrowphase: PxGenerateContacts semantics per pair (contacts.cuh);
-//   3. TGS: solver bodies, the PxBatchConstraintsTGS partition rule (lane 0),
-//      contact rows, position iterations with per-substep integration and the
-//      velocity iteration, solved partition by partition across the 32 lanes
-//      (constraints of one partition touch disjoint bodies; __syncwarp between
-//      partitions), then PxIntegrateSolverBodiesTGS and write-back.
-// All scene state stays resident in HBM; a step is capturable in a CUDA graph
-// (a memset of the work counter + one kernel).
+// Thousands of independent scenes advance together, one CUDA graph per step.
+// The scene stages pull scenes from a work table sorted by decreasing size
+// (largest first, so the tail is short); scenes of up to `largeBodies` solver
+// bodies run one warp per scene, larger ones one block of 8 warps per scene
+// (on a side stream, concurrently):
+//   1. bounds + broadphase: AABBs, bitonic sort by encoded min X, sweep with the
+//      reference ABP's closed-interval test (X as encodeFloat keys, Y/Z as
+//      floats), pairs ordered by (id0, id1), statics after the dynamic bodies,
+//      each pair queued under its pair kind;
+//   2. narrowphase: one kernel per pair kind over every scene's pairs, a thread
+//      per pair, PxGenerateContacts semantics (contacts.cuh);
+//   3. batching: solver bodies and the PxBatchConstraintsTGS partition rule;
+//   4. row preparation: a thread per constraint;
+//   5. solve: position iterations with per-substep integration and the velocity
+//      iteration, partition by partition (constraints of one partition touch
+//      disjoint bodies), then PxIntegrateSolverBodiesTGS and write-back.
+// All scene state stays resident in HBM.
 //
 // The step is the reference immediate-mode snippet's frame (physx/snippets/
-// snippetimmediatemode/SnippetImmediateMode.cpp:473 stepPhysics) with a fresh
-// PxBroadPhase, fresh PxCache and fresh friction data per frame: bounds
+// snippetimmediatemode/SnippetImmediateMode.cpp:473 stepPhysics): bounds
 // inflated by a margin, ABP pairs, PxGenerateContacts, PxConstructSolverBodiesTGS,
 // PxBatchConstraintsTGS, PxCreateContactConstraintsTGS, PxSolveConstraintsTGS,
-// PxIntegrateSolverBodiesTGS.
+// PxIntegrateSolverBodiesTGS; in persistent mode (the snippet's default) each
+// pair keeps its PCM manifold and friction patches between steps
+// (SnippetImmediateMode.cpp:657-676, 941-978), double-buffered per scene.
 #include "common.cuh"
 #include "contacts.cuh"
 #include "solver.cuh"

@@ -1,8 +1,9 @@
 """One large scene: the reference immediate-mode frame (ABP broadphase,
 PxGenerateContacts, PxBatchConstraintsTGS, TGS solve and integrate, pair caches
 and friction patches kept between frames) over one scene of any size, every
-stage spread over the whole GPU.  The batched world gives each scene one warp;
-this class is for single scenes of tens of thousands of bodies and more.
+stage spread over the whole GPU.  The batched world gives each scene one warp
+or one block and holds at most 65,535 bodies per scene; this class is for single
+scenes of tens of thousands of bodies and more.
 """
 import ctypes
 

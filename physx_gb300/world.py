@@ -1,7 +1,9 @@
-"""Batched multi-scene world: thousands of independent scenes stepped in one
-persistent launch per step (optionally replayed from a CUDA graph), all state
-resident in HBM.  Each scene's frame is the reference immediate-mode loop
-(ABP broadphase, PxGenerateContacts, TGS) with fresh per-frame caches.
+"""Batched multi-scene world: thousands of independent scenes stepped by one
+CUDA graph per step (warp-per-scene or block-per-scene stage kernels, picked by
+scene size; autotune() chooses the threshold for the scene-size histogram), all
+state resident in HBM.  Each scene's frame is the reference immediate-mode loop
+(ABP broadphase, PxGenerateContacts, TGS) with the snippet's persistent pair
+state (contact manifolds and friction patches kept between steps) by default.
 """
 import ctypes
 
