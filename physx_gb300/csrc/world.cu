@@ -1059,7 +1059,7 @@ __device__ __forceinline__ void solveScene(const WorldDev& w, const SceneDesc& s
 	if(sp.persistent && tid == 0) w.sceneParity[sid] ^= 1u;
 }
 
-constexpr uint32_t SOLVE_WARPS = 2;   // warps (scenes in flight) per block of the warp-per-scene solve kernel
+constexpr uint32_t SOLVE_WARPS = 1;   // warps (scenes in flight) per block of the warp-per-scene solve kernel
 template <uint32_t CAPB, uint32_t RB>
 __global__ void __launch_bounds__(SOLVE_WARPS * 32) solveKernel(WorldDev w, StepParams sp)
 {
