@@ -484,8 +484,8 @@ def main():
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
                             constraints_per_step=st["constraints"], contacts_per_step=st["contacts"], graph=True,
                             autotune=dict(key="scene-size histogram", large_bodies=tuned_threshold,
-                                          solve_staging_bytes_per_lane=[0, 256, 512][getattr(w, "solve_variant", 2) % 3],
-                                          solve_velocities="shared memory" if getattr(w, "solve_variant", 2) < 3 else "HBM",
+                                          solve_staging_bytes_per_lane=[0, 256, 512, 0, 256, 512, 400, 400][getattr(w, "solve_variant", 2)],
+                                          solve_velocities="shared memory" if getattr(w, "solve_variant", 2) in (0, 1, 2, 6) else "HBM",
                                           sample_ms_per_step=tuned_ms),
                             l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
                             parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),

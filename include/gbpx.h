@@ -216,8 +216,9 @@ int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint
                         float* outMs);
 /* Workspace of the warp-per-scene solve: variants 0-2 keep the body
  * velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
- * (2 is the default), variants 3-5 the same with the velocities left in HBM (a
- * smaller workspace leaves room for more warps per SM).  Results do not depend
+ * (2 is the default), variants 3-5 the same with the velocities left in HBM,
+ * 6 / 7 stage 400 bytes with the velocities on chip / in HBM (a smaller
+ * workspace leaves room for more warps per SM).  Results do not depend
  * on it.  The autotuner sets it after the threshold. */
 int gbpx_world_set_solve_variant(void* world, uint32_t variant);
 /* Pairs of each pair kind in the last step, in the kind order of the

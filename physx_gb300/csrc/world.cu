@@ -851,7 +851,11 @@ struct __align__(16) IterSmemT
 template <uint32_t CAPB, uint32_t RB>
 using IterSmemW = IterSmemT<CAPB, SOLVE_SMEM_CONSTRAINTS, RB>;
 using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, 0>;
-constexpr uint32_t SOLVE_VARIANTS = 6;   // (velocities on chip, 0 / 256 / 512 B staging), (velocities in HBM, 0 / 256 / 512 B)
+// variants: (velocities on chip, 0 / 256 / 512 B staging), (velocities in HBM, 0 / 256 / 512 B), then 400 B
+// staging with velocities on chip / in HBM (the largest slot that leaves room for 8 warps per SM with
+// the velocities on chip; one-patch four-point rows are 392 B)
+constexpr uint32_t SOLVE_VARIANTS = 8;
+constexpr uint32_t MID_CHUNKS = 25;
 
 template <uint32_t G, uint32_t CAPB, uint32_t CAPC, uint32_t RB, typename Vel>
 __device__ __forceinline__ void sceneIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
@@ -1309,7 +1313,8 @@ struct World
 		using namespace world;
 		static const size_t per[SOLVE_VARIANTS] = {sizeof(IterSmemW<SOLVE_SMEM_BODIES, 0>), sizeof(IterSmemW<SOLVE_SMEM_BODIES, 16>),
 		                                           sizeof(IterSmemW<SOLVE_SMEM_BODIES, RECBUF_CHUNKS>), sizeof(IterSmemW<1, 0>),
-		                                           sizeof(IterSmemW<1, 16>), sizeof(IterSmemW<1, RECBUF_CHUNKS>)};
+		                                           sizeof(IterSmemW<1, 16>), sizeof(IterSmemW<1, RECBUF_CHUNKS>),
+		                                           sizeof(IterSmemW<SOLVE_SMEM_BODIES, MID_CHUNKS>), sizeof(IterSmemW<1, MID_CHUNKS>)};
 		return warps * per[variant];
 	}
 	static const StageKernel* solveKernels()
@@ -1317,7 +1322,8 @@ struct World
 		using namespace world;
 		static const StageKernel k[SOLVE_VARIANTS] = {solveKernel<SOLVE_SMEM_BODIES, 0>, solveKernel<SOLVE_SMEM_BODIES, 16>,
 		                                              solveKernel<SOLVE_SMEM_BODIES, RECBUF_CHUNKS>, solveKernel<1, 0>, solveKernel<1, 16>,
-		                                              solveKernel<1, RECBUF_CHUNKS>};
+		                                              solveKernel<1, RECBUF_CHUNKS>, solveKernel<SOLVE_SMEM_BODIES, MID_CHUNKS>,
+		                                              solveKernel<1, MID_CHUNKS>};
 		return k;
 	}
 	// persistent grid: every SM filled to the kernel's occupancy at 128 threads per block
@@ -1891,7 +1897,8 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 
 // Workspace of the warp-per-scene solve kernel: variants 0-2 keep the body
 // velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
-// (2 is the default), variants 3-5 the same with the velocities left in HBM.
+// (2 is the default), variants 3-5 the same with the velocities left in HBM,
+// variants 6 / 7 stage 400 bytes per lane with the velocities on chip / in HBM.
 // A smaller workspace leaves room for more warps per SM.  Results do not depend
 // on it.
 GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant)

@@ -159,7 +159,8 @@ class World:
     def set_solve_variant(self, v):
         """Workspace of the warp-per-scene solve: 0-2 velocities in shared memory with
         0 / 256 / 512 B of row staging per lane (2 default), 3-5 the same with the
-        velocities in HBM.  Results do not depend on it."""
+        velocities in HBM, 6 / 7 400 B with velocities on chip / in HBM.  Results
+        do not depend on it."""
         check(self._L.gbpx_world_set_solve_variant(self._h, int(v)), "gbpx_world_set_solve_variant")
 
     def kind_counts(self):

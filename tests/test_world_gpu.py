@@ -225,12 +225,12 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
 
 def test_world_solve_staging_variants_equal(cuda_device):
     """The warp-per-scene solve stages rows in 512 or 256 bytes per lane or uses
-    them in place, with the body velocities in shared memory or in HBM; the six
+    them in place, with the body velocities in shared memory or in HBM; the eight
     variants give the same bytes."""
     from physx_gb300.workloads import batched_scenes
     from physx_gb300.world import World
     scenes = batched_scenes(143, 48, nmin=16, nmax=500)
-    worlds = [World(scenes) for _ in range(6)]
+    worlds = [World(scenes) for _ in range(8)]
     for v, w in enumerate(worlds):
         w.set_solve_variant(v)
     for step in range(20):
