@@ -306,6 +306,25 @@ def dist_setup(n):
     return rank, world, dist
 
 
+def rank_scenes(seed, rank, nb_scenes):
+    """The scenes of one rank: every rank steps its own independent scene set
+    (weak scaling, no data-path collective)."""
+    from physx_gb300.workloads import batched_scenes
+    return batched_scenes(seed + 1000 * rank, nb_scenes)
+
+
+def reduce_over_ranks(ms, bodies, dist):
+    """Whole-job figures: the slowest rank's time and the bodies of all ranks."""
+    if not dist:
+        return ms, bodies
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    bt = torch.tensor([bodies], dtype=torch.float64)
+    dist.all_reduce(bt)
+    return float(t.item()), int(bt.item())
+
+
 def main():
     a = parse()
     import numpy as np
@@ -346,7 +365,7 @@ def main():
     import physx_gb300
     physx_gb300.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from physx_gb300.world import World
-    scenes = batched_scenes(a.seed + 1000 * rank, a.scenes)
+    scenes = rank_scenes(a.seed, rank, a.scenes)
     w = World(scenes)
     info = w.info()
     bodies = info["bodies"]
@@ -379,16 +398,7 @@ def main():
     clocks.start()
     ms = w.time_steps(a.steps, graph=True)
     clk = clocks.stop()
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        bt = torch.tensor([bodies], dtype=torch.float64)
-        dist.all_reduce(bt)
-        total_bodies = int(bt.item())
-    else:
-        total_bodies = bodies
+    ms, total_bodies = reduce_over_ranks(ms, bodies, dist)
     status = w.status()
     st = w.stats()
     value = total_bodies * a.steps / (ms / 1000.0)
