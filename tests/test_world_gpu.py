@@ -241,3 +241,32 @@ def test_world_solve_staging_variants_equal(cuda_device):
         assert w.get_bodies().tobytes() == ref
     for w in worlds:
         w.release()
+
+
+def test_world_full_size_batched_step_matches_oracle_sample(cuda_device):
+    """The batched workload at its full size (4096 scenes, log-uniform [8,512]
+    bodies, about 0.5M bodies) after a pre-roll: one step of the whole world
+    against the oracle's step of 48 scenes sampled across the size range, from the
+    same state (fresh caches, so the oracle's stateless frame applies)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from bench import split_scenes
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes = batched_scenes(4, 4096)
+    w = _world(scenes, persistent=False)
+    w.step(40)
+    state = w.get_bodies()
+    w.step(1)
+    out = w.get_bodies()
+    assert not w.status().any()
+    counts = scenes["body_count"].astype(np.int64)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    idx = np.argsort(counts)[np.linspace(0, len(counts) - 1, 48).astype(np.int64)]
+    sample = split_scenes(dict(scenes, rigid=state), idx)
+    ref = run_scene_step("orc", sample, dict(DEFAULT_PARAMS, persistent=False), steps=1)
+    got = np.concatenate([out[starts[i]:starts[i] + counts[i]] for i in idx])
+    assert velocity_error(rigid_velocity(ref), rigid_velocity(got)) <= 1e-5
+    assert np.abs(got["p"] - ref["p"]).max() <= 1e-6
+    w.release()
