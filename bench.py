@@ -115,14 +115,24 @@ def cpu_baseline(scenes, params, nb_scenes, steps, pool, cores):
 
 
 # ---------------------------------------------------------------- clocks
+def smi_gpu_id(local_rank):
+    """This rank's GPU as nvidia-smi names it: the LOCAL_RANK-th entry of
+    CUDA_VISIBLE_DEVICES (an index or a UUID) when that is set, else LOCAL_RANK."""
+    vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    return vis[local_rank] if local_rank < len(vis) else str(local_rank)
+
+
 class ClockSampler:
-    def __init__(self):
+    """nvidia-smi samples of this rank's GPU (only) during the timed region."""
+
+    def __init__(self, gpu="0"):
         self.samples = []
         self.proc = None
+        self.gpu = gpu
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
                                           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                                           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                                           "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
@@ -297,11 +307,13 @@ def bench_large_scene(steps, cpu_frames):
 
 
 def dist_setup(n):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != n:
+        sys.exit("bench.py: --gpus %d but WORLD_SIZE is %d (launch N > 1 ranks with torch.distributed.run)" % (n, world))
     if n <= 1:
         return 0, 1, None
     import torch.distributed as dist
     rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     dist.init_process_group("gloo", init_method="env://")
     return rank, world, dist
 
@@ -394,7 +406,7 @@ def main():
     state = w.get_bodies()
     if dist:
         dist.barrier()
-    clocks = ClockSampler()
+    clocks = ClockSampler(smi_gpu_id(int(os.environ.get("LOCAL_RANK", "0"))))
     clocks.start()
     ms = w.time_steps(a.steps, graph=True)
     clk = clocks.stop()

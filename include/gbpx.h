@@ -95,6 +95,9 @@ int gbpx_generate_contacts_cached(const int* type0, const float* geom0, const in
  * Inputs and outputs are the caller's device arrays (layouts as above;
  * dOutContacts holds 4 contacts x 8 floats per pair and is 16-byte aligned),
  * the work is enqueued on `stream` (a cudaStream_t, NULL = default stream).
+ * Caches are fresh (no PxCache is read or written).  Geometry types must be
+ * 0..3: the device arrays are not checked on the host, and other values give
+ * undefined contacts.
  * Scratch is a fixed 1 MiB device array, so nbPairs <= 262144
  * (GBPX_ERR_CAPACITY above).  The scratch is shared by every call on a
  * device: calls that may overlap must be serialised by the caller.  The first

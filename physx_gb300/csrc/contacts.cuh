@@ -1,7 +1,8 @@
 // Primitive contact generation (sphere / plane / capsule / box) for the GB300
-// rigid-body step: PxGenerateContacts semantics with a fresh PxCache per call
-// (physx/source/immediatemode/src/NpImmediateMode.cpp:732-849), i.e. the
-// persistent contact manifold is regenerated in full.  Per-pair generators
+// rigid-body step: PxGenerateContacts semantics
+// (physx/source/immediatemode/src/NpImmediateMode.cpp:732-849), with a fresh
+// PxCache or with the pair's persistent contact manifold (a 288-byte record,
+// refreshed, invalidated or rebuilt as the reference does).  Per-pair generators
 // follow physx/source/geomutils/src/pcm/: GuPCMContactSphereSphere.cpp:36,
 // SpherePlane.cpp:36, SphereCapsule.cpp:56, SphereBox.cpp:37,
 // PlaneCapsule.cpp:36, PlaneBox.cpp:36, CapsuleCapsule.cpp:79, BoxBox.cpp:332
@@ -9,8 +10,9 @@
 // GuPersistentContactManifold.cpp:552-1313.  One thread runs one pair; the
 // kernels in np.cu group pairs by type so a warp runs one generator.
 //
-// Known difference from the reference: box-box edge clipping uses an exact
-// reciprocal where the reference uses rcpps (GuPCMContactBoxBox.cpp:140).
+// Box-box edge clipping divides by the reference's approximate reciprocal
+// (V3RecipFast, GuPCMContactBoxBox.cpp:140): recipFast restates the x86 RCPPS
+// result bit for bit, so the clipped points round as the reference's do.
 #pragma once
 #include "vmath.cuh"
 

@@ -10,6 +10,8 @@
 // needed and the host reads counts + records in one copy.
 #include "common.cuh"
 #include "contacts.cuh"
+#include <atomic>
+#include <mutex>
 
 namespace gbpx
 {
@@ -217,20 +219,32 @@ constexpr uint32_t NP_NOALLOC_SCRATCH_WORDS = 32 + NP_NOALLOC_MAX_PAIRS;
 static __device__ __align__(256) uint32_t gNpNoAllocScratch[NP_NOALLOC_SCRATCH_WORDS];
 constexpr int NP_NOALLOC_MAX_DEVICES = 64;
 
-// Address of the scratch array on the current device, looked up once per device.
+// Address of the scratch array on the current device, looked up once per device
+// (with that device current) by whichever host thread calls first; the other
+// threads wait for that lookup.  The address belongs to the device's primary
+// context, which the runtime API uses; a failed lookup is retried on the next
+// call.
 static int npNoAllocScratch(uint32_t** out)
 {
-	static uint32_t* cache[NP_NOALLOC_MAX_DEVICES] = {};
+	static std::atomic<uint32_t*> cache[NP_NOALLOC_MAX_DEVICES] = {};
+	static std::mutex lookup;
 	int dev = 0;
 	GBPX_CUDA_TRY(cudaGetDevice(&dev));
 	if(dev < 0 || dev >= NP_NOALLOC_MAX_DEVICES) return GBPX_ERR_INVALID;
-	if(!cache[dev])
+	uint32_t* p = cache[dev].load(std::memory_order_acquire);
+	if(!p)
 	{
-		void* p = nullptr;
-		GBPX_CUDA_TRY(cudaGetSymbolAddress(&p, gNpNoAllocScratch));
-		cache[dev] = static_cast<uint32_t*>(p);
+		std::lock_guard<std::mutex> g(lookup);
+		p = cache[dev].load(std::memory_order_relaxed);
+		if(!p)
+		{
+			void* addr = nullptr;
+			GBPX_CUDA_TRY(cudaGetSymbolAddress(&addr, gNpNoAllocScratch));
+			p = static_cast<uint32_t*>(addr);
+			cache[dev].store(p, std::memory_order_release);
+		}
 	}
-	*out = cache[dev];
+	*out = p;
 	return GBPX_OK;
 }
 } // namespace gbpx
@@ -238,11 +252,14 @@ static int npNoAllocScratch(uint32_t** out)
 // PxGenerateContacts over nbPairs pairs held in device memory (layouts as
 // gbpx_generate_contacts; contacts: 4 slots of 8 floats per pair, 16-byte
 // aligned), enqueued on `stream` (a cudaStream_t, NULL for the default
-// stream).  Allocates nothing: the bucketing scratch is a fixed 1 MiB device
-// array, so nbPairs is limited to 262144 (GBPX_ERR_CAPACITY above).  The
-// scratch is shared by all calls on a device: calls that may overlap (other
-// streams, other host threads) race and must be serialised by the caller.
-// The first call on a device looks up the scratch address.
+// stream), with fresh caches.  Geometry types must be 0..3 (sphere, plane,
+// capsule, box): the device arrays are not inspected on the host, and other
+// values give undefined contacts.  Allocates nothing: the bucketing scratch is
+// a fixed 1 MiB device array, so nbPairs is limited to 262144
+// (GBPX_ERR_CAPACITY above).  The scratch is shared by all calls on a device:
+// calls that may overlap (other streams, other host threads) race and must be
+// serialised by the caller.  The first call on a device looks up the scratch
+// address.
 GBPX_API int gbpx_generate_contacts_device_noalloc(const int* dType0, const float* dGeom0, const int* dType1, const float* dGeom1,
                                                    const float* dPose0, const float* dPose1, uint32_t nbPairs, float contactDistance,
                                                    float toleranceLength, float* dOutContacts, uint32_t* dOutCounts, void* stream)

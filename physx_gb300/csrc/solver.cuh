@@ -13,12 +13,14 @@
 //   solve: solveContact / solveDynamicContactsStep (DyTGSContactPrep.cpp:1581,1492);
 //   integration: integrateCoreStep (DyTGSDynamics.cpp:1403) and
 //     PxIntegrateSolverBodiesTGS (NpImmediateMode.cpp:1719).
-// Settings are those of immediate-mode callers: fresh friction patches, unit
-// mass scales, zero rest distance and offset slop, no torsional friction.
+// Settings are those of immediate-mode callers: friction patches fresh or
+// carried from the last frame (correlated and grown), unit mass scales, zero
+// rest distance and offset slop, no torsional friction.
 //
 // GB300 layout: a pair has at most 4 contacts, so a constraint's rows fit a
-// fixed 1 KB record (<= 4 patches, <= 4 point rows, <= 8 friction rows) that
-// the prep pass writes once and every solve iteration re-reads from L2; the
+// record of at most 896 bytes (<= 4 patches, <= 4 point rows, <= 8 friction
+// rows), packed to the rows it uses, that the prep pass writes once and every
+// solve iteration reads; the
 // partitioning (batching) rule guarantees that the constraints of one
 // partition touch disjoint dynamic bodies, so a partition is solved as one
 // parallel wave and reproduces the reference's sequential order.

@@ -1481,8 +1481,9 @@ struct World
 		return rc;
 	}
 
-	// One scene per launch sequence: no batching across scenes, no graph, no
-	// persistence (the comparison point of the batched step).
+	// One scene per launch sequence: no batching across scenes and no graph; pair
+	// state is kept or not as params.persistent says (the comparison point of the
+	// batched step).
 	int stepPlain(uint32_t first, uint32_t count)
 	{
 		for(uint32_t s = first; s < first + count && s < nbScenes; s++)

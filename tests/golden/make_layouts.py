@@ -7,9 +7,19 @@ import sys
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-PHYSX_INCLUDE = "/root/reference/physx/include"
+
+
+def physx_include():
+    """The reference's include directory: $PHYSX_REFERENCE/include, else the
+    source location the oracle/ref recipe names."""
+    root = os.environ.get("PHYSX_REFERENCE")
+    if not root:
+        root = subprocess.check_output(["make", "-s", "-C", os.path.join(HERE, "..", "..", "oracle", "ref"), "print-physx"]).decode().strip()
+    return os.path.join(root, "include")
+
 
 if __name__ == "__main__":
+    PHYSX_INCLUDE = physx_include()
     if not os.path.isdir(PHYSX_INCLUDE):
         sys.exit("reference headers not found")
     with tempfile.TemporaryDirectory() as d:

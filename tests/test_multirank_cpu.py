@@ -53,3 +53,22 @@ def test_two_rank_sharding_and_reduction():
     assert ms0 == ms1 == 11.0                 # the slowest rank's time on every rank
     assert tot0 == tot1 == b0 + b1            # bodies of the whole job
     assert np.isfinite(x0) and b0 > 0 and b1 > 0
+
+
+def test_world_size_must_match_gpus(monkeypatch):
+    """--gpus N without N launched ranks is refused, not reported as N GPUs."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    with pytest.raises(SystemExit):
+        bench.dist_setup(2)
+    assert bench.dist_setup(1) == (0, 1, None)
+
+
+def test_clock_sampler_names_this_ranks_gpu(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "3,GPU-abc")
+    assert bench.smi_gpu_id(0) == "3" and bench.smi_gpu_id(1) == "GPU-abc"
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    assert bench.smi_gpu_id(2) == "2"
