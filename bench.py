@@ -31,6 +31,13 @@ WORKLOAD = ("batched: 4096 scenes, bodies log-uniform [8,512] sphere/box/capsule
             "ABP + contacts + TGS 4/1, dt 1/60, FP32")
 
 
+SOLVE_VARIANTS = ["warp per scene, rows in place, velocities on chip", "warp per scene, 256 B staging per lane, velocities on chip",
+                  "warp per scene, 512 B staging per lane, velocities on chip", "warp per scene, rows in place, velocities in HBM",
+                  "warp per scene, 256 B staging per lane, velocities in HBM", "warp per scene, 512 B staging per lane, velocities in HBM",
+                  "warp per scene, 400 B staging per lane, velocities on chip", "warp per scene, 400 B staging per lane, velocities in HBM",
+                  "resident: rows and velocities on chip for all iterations, bulk-copied once"]
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -61,27 +68,37 @@ def parse():
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle restatement, all cores)
-def _cpu_worker(payload):
+def _cpu_proc(scenes, pv, it, preroll, warmup, steps, barrier, out):
+    """One host process of the CPU baseline: its scenes through the oracle's
+    persistent frame (contact caches and friction data kept between steps, one
+    handle for the whole run), `preroll` + `warmup` untimed steps, then `steps`
+    timed steps between barriers shared with the other processes."""
     import ctypes
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_libs import _p, oracle
-    scenes, pv, it, steps = payload
     L = oracle()
     keep = [np.ascontiguousarray(scenes[k], d) for k, d in (("body_count", np.uint32), ("static_count", np.uint32), ("types", np.int32),
                                                               ("geoms", np.float32), ("friction", np.float32), ("static_poses", np.float32),
                                                               ("static_types", np.int32), ("static_geoms", np.float32))]
     rb = np.ascontiguousarray(scenes["rigid"]).copy()
-    # the reference snippet's persistent mode (contact caches and friction data kept between steps), as the world runs
     L.orc_persistent_create.restype = ctypes.c_void_p
     h = ctypes.c_void_p(L.orc_persistent_create())
-    t = time.perf_counter()
+
+    def step():
+        L.orc_scene_step_persistent(h, ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]),
+                                    _p(keep[4]), _p(keep[5]), _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
+
+    for _ in range(preroll + warmup):
+        step()
+    barrier.wait()
+    t0 = time.monotonic()
     for _ in range(steps):
-        L.orc_scene_step_persistent(h, ctypes.c_uint32(len(keep[0])), _p(keep[0]), _p(keep[1]), _p(rb), _p(keep[2]), _p(keep[3]), _p(keep[4]),
-                                    _p(keep[5]), _p(keep[6]), _p(keep[7]), _p(pv), _p(it))
-    elapsed = time.perf_counter() - t
+        step()
+    t1 = time.monotonic()
+    barrier.wait()
     L.orc_persistent_release(h)
-    return elapsed, int(keep[0].sum())
+    out.put((t0, t1, int(keep[0].sum())))
 
 
 def split_scenes(scenes, idx):
@@ -95,23 +112,41 @@ def split_scenes(scenes, idx):
                 static_types=scenes["static_types"][idx], static_geoms=scenes["static_geoms"][idx])
 
 
-def cpu_baseline(scenes, params, nb_scenes, steps, pool, cores):
-    """Oracle restatement of the reference step on a bounded sample, scenes split across `cores` processes."""
+def cpu_sample(nb_scenes_total, nb_sample):
+    """The CPU sample: every k-th scene of the world, an even spread of scene sizes."""
     import numpy as np
+    return np.linspace(0, nb_scenes_total - 1, min(nb_sample, nb_scenes_total)).astype(np.int64)
+
+
+def cpu_baseline(scenes, params, nb_scenes, steps, cores, preroll=0, warmup=1, ctx=None):
+    """The oracle restatement of the reference frame on a bounded sample of the
+    scenes, split across `cores` host processes (spawned), persistent pair state
+    as the world runs: each process pre-rolls `preroll` steps and warms up
+    `warmup` steps, then all time `steps` consecutive steps together; the wall
+    time is from the first process's start to the last one's end."""
+    import multiprocessing as mp
     from physx_gb300.world import param_vector
     pv, it = param_vector(params)
-    # an even spread of scene sizes: every k-th scene
     S = len(scenes["body_count"])
-    idx = np.linspace(0, S - 1, min(nb_scenes, S)).astype(np.int64)
-    chunks = [idx[i::cores] for i in range(cores)]
-    payloads = [(split_scenes(scenes, c), pv, it, steps) for c in chunks if len(c)]
-    t = time.perf_counter()
-    res = list(pool.map(_cpu_worker, payloads))
-    wall = time.perf_counter() - t
-    bodies = sum(r[1] for r in res)
-    return dict(value=bodies * steps / wall, unit=UNIT, cores=cores, kind="port",
-                sample="%d of %d scenes (%d bodies) x %d steps, oracle restatement, %d processes" % (len(idx), S, bodies, steps, cores),
-                seconds=wall)
+    idx = cpu_sample(S, nb_scenes)
+    chunks = [c for c in (idx[i::cores] for i in range(cores)) if len(c)]
+    ctx = ctx or mp.get_context("spawn")
+    barrier = ctx.Barrier(len(chunks))
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_proc, args=(split_scenes(scenes, c), pv, it, preroll, warmup, steps, barrier, q)) for c in chunks]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+        if p.exitcode != 0:
+            raise RuntimeError("CPU baseline process failed (exit code %s)" % p.exitcode)
+    wall = max(r[1] for r in res) - min(r[0] for r in res)
+    bodies = sum(r[2] for r in res)
+    return dict(value=bodies * steps / wall, unit=UNIT, cores=len(chunks), kind="port",
+                sample="%d of %d scenes (%d bodies, every %d-th by index), %d pre-roll + %d warm-up + %d timed persistent steps, "
+                       "oracle restatement, %d processes" % (len(idx), S, bodies, max(1, S // max(1, len(idx))), preroll, warmup, steps, len(chunks)),
+                seconds=wall, ms_per_step=1000.0 * wall / steps)
 
 
 # ---------------------------------------------------------------- clocks
@@ -348,32 +383,21 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return
-        import multiprocessing as mp
-        ctx = mp.get_context("spawn")
+        # The reference path on the host cores: the oracle restatement of the
+        # frame (the reference build does not travel to this machine), on the same
+        # workload, pre-rolled on the CPU as the GPU arm pre-rolls on the device,
+        # then --steps consecutive persistent steps after --warmup.
         scenes = batched_scenes(a.seed, a.scenes)
-        with ctx.Pool(cores) as pool:
-            # warm-up (builds the oracle library, pages code in)
-            for _ in range(max(1, min(a.warmup, 1))):
-                cpu_baseline(scenes, DEFAULT_PARAMS, min(a.cpu_scenes, 32), 1, pool, cores)
-            per_step = []
-            for _ in range(a.steps):
-                r = cpu_baseline(scenes, DEFAULT_PARAMS, a.cpu_scenes, 1, pool, cores)
-                per_step.append(r)
-        value = sum(r["value"] for r in per_step) / len(per_step)
-        ms = 1000.0 * sum(r["seconds"] for r in per_step) / len(per_step)
-        line = dict(impl="reference", metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
-                    ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
-                    config=dict(workload=WORKLOAD, scenes=a.scenes, sample_scenes=a.cpu_scenes, l2="n/a (CPU)"),
-                    cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind="port", sample=per_step[0]["sample"]),
-                    e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        r = cpu_baseline(scenes, DEFAULT_PARAMS, a.cpu_scenes, a.steps, cores, preroll=a.preroll, warmup=a.warmup)
+        line = dict(impl="reference", metric=METRIC, value=r["value"], unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
+                    ms_per_step=r["ms_per_step"], higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
+                    config=dict(workload=WORKLOAD, scenes=a.scenes, sample_scenes=len(cpu_sample(a.scenes, a.cpu_scenes)),
+                                preroll_steps=a.preroll, persistent=True, l2="n/a (CPU)"),
+                    cpu_baseline=dict(value=r["value"], unit=UNIT, cores=r["cores"], kind="port", sample=r["sample"]),
+                    e2e=dict(value=r["value"], unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
         print(json.dumps(line))
         return
 
-    # CPU baseline pool is spawned before any CUDA call
-    pool = None
-    if rank == 0:
-        import multiprocessing as mp
-        pool = mp.get_context("spawn").Pool(cores)
     import physx_gb300
     physx_gb300.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from physx_gb300.world import World
@@ -400,8 +424,6 @@ def main():
         physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
         print(json.dumps(dict(profiled_steps=a.profile_step, kernels_per_step=w.info()["kernels_per_step"],
                               large_bodies=w.info()["large_bodies"], **w.stats())))
-        if pool:
-            pool.close()
         return
     state = w.get_bodies()
     if dist:
@@ -484,9 +506,11 @@ def main():
     step_roofline = dict(algorithmic_bytes_per_step=bytes_step, achieved=bytes_step / (ms / a.steps / 1000.0) / 1e9, unit="GB/s")
     cpu = None
     if rank == 0:
-        cpu = cpu_baseline(dict(scenes, rigid=state), DEFAULT_PARAMS, a.cpu_scenes, a.cpu_steps, pool, cores)
+        # the same sample of the world in the state the timed steps started from
+        # (spawned processes: no CUDA state is inherited)
+        cpu = cpu_baseline(dict(scenes, rigid=state), DEFAULT_PARAMS, a.cpu_scenes, a.cpu_steps, cores, preroll=0, warmup=1)
         cpu.pop("seconds", None)
-        pool.close()
+        cpu.pop("ms_per_step", None)
     if rank != 0:
         return
     w.release()
@@ -506,8 +530,7 @@ def main():
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
                             constraints_per_step=st["constraints"], contacts_per_step=st["contacts"], graph=True,
                             autotune=dict(key="scene-size histogram", large_bodies=tuned_threshold,
-                                          solve_staging_bytes_per_lane=[0, 256, 512, 0, 256, 512, 400, 400][getattr(w, "solve_variant", 2)],
-                                          solve_velocities="shared memory" if getattr(w, "solve_variant", 2) in (0, 1, 2, 6) else "HBM",
+                                          solve=SOLVE_VARIANTS[getattr(w, "solve_variant", 8)],
                                           sample_ms_per_step=tuned_ms),
                             l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
                             parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),

@@ -9,6 +9,11 @@
  *   PxCreateContactConstraintsTGS    physx/include/PxImmediateMode.h:642
  *   PxSolveConstraintsTGS            physx/include/PxImmediateMode.h:716
  *   PxIntegrateSolverBodiesTGS       physx/include/PxImmediateMode.h:729
+ *   PxGetBroadPhaseStaticFilterGroup     physx/include/PxBroadPhase.h:264
+ *   PxGetBroadPhaseDynamicFilterGroup    physx/include/PxBroadPhase.h:278
+ *   PxGetBroadPhaseKinematicFilterGroup  physx/include/PxBroadPhase.h:291
+ *   PxCreateBroadPhase                   physx/include/PxBroadPhase.h:629
+ *   PxCreateAABBManager                  physx/include/PxBroadPhase.h:796
  *
  * The reference declares these PX_C_EXPORT (extern "C"), so a program built
  * against the reference's headers links them from this library instead.  This
@@ -30,6 +35,16 @@
  * and no maximum impulse, and articulations are not supported (the functions
  * return false, or do nothing, for input outside this set).  All arithmetic
  * runs on the GPU through libgbpx.
+ *
+ * PxCreateBroadPhase accepts eABP and ePABP descriptors (the same pair sets;
+ * the GPU sweep stands in for both) and returns NULL for other types, as the
+ * reference does for descriptors it cannot serve.  Its PxBroadPhase gives the
+ * reference ABP's created and lost pairs bit for bit, each list sorted by
+ * (mID0, mID1); the update's continuation task is not used (eABP is
+ * single-threaded in the reference too); getAllocator() hands out page-locked
+ * host memory, from which bounds reach the device fastest.  PxCreateAABBManager
+ * wraps such a broadphase with the reference's object bookkeeping (one manager
+ * per broadphase).
  */
 #ifndef GBPX_IMMEDIATE_H
 #define GBPX_IMMEDIATE_H
@@ -192,6 +207,124 @@ public:
 	virtual uint8_t* reserveFrictionData(const uint32_t byteSize) = 0;
 	virtual ~PxConstraintAllocator() {}
 };
+
+// ---- low- and high-level broadphase (physx/include/PxBroadPhase.h) ----
+struct PxBounds3 { PxVec3 minimum, maximum; };
+struct PxBroadPhaseType { enum Enum { eSAP, eMBP, eABP, ePABP, eGPU, eLAST }; };
+class PxBaseTask;
+class PxCudaContextManager;
+class PxBroadPhaseRegions;   // only MBP has regions: never returned here
+
+class PxAllocatorCallback   // physx/include/foundation/PxAllocatorCallback.h
+{
+public:
+	virtual ~PxAllocatorCallback() {}
+	virtual void* allocate(size_t size, const char* typeName, const char* filename, int line) = 0;
+	virtual void deallocate(void* ptr) = 0;
+};
+
+struct PxBroadPhaseCaps { uint32_t mMaxNbRegions; };
+
+class PxBroadPhaseDesc
+{
+public:
+	PxBroadPhaseDesc(PxBroadPhaseType::Enum type = PxBroadPhaseType::eLAST)
+	    : mType(type), mContextID(0), mContextManager(nullptr), mFoundLostPairsCapacity(256 * 1024), mDiscardStaticVsKinematic(false),
+	      mDiscardKinematicVsKinematic(false)
+	{
+	}
+	PxBroadPhaseType::Enum mType;
+	uint64_t mContextID;
+	PxCudaContextManager* mContextManager;
+	uint32_t mFoundLostPairsCapacity;
+	bool mDiscardStaticVsKinematic;
+	bool mDiscardKinematicVsKinematic;
+};
+
+typedef uint32_t PxBpIndex;
+typedef uint32_t PxBpFilterGroup;
+
+class PxBroadPhaseUpdateData
+{
+public:
+	PxBroadPhaseUpdateData(const PxBpIndex* created, uint32_t nbCreated, const PxBpIndex* updated, uint32_t nbUpdated, const PxBpIndex* removed,
+	                       uint32_t nbRemoved, const PxBounds3* bounds, const PxBpFilterGroup* groups, const float* distances, uint32_t capacity)
+	    : mCreated(created), mNbCreated(nbCreated), mUpdated(updated), mNbUpdated(nbUpdated), mRemoved(removed), mNbRemoved(nbRemoved),
+	      mBounds(bounds), mGroups(groups), mDistances(distances), mCapacity(capacity)
+	{
+	}
+	const PxBpIndex* mCreated;
+	const uint32_t mNbCreated;
+	const PxBpIndex* mUpdated;
+	const uint32_t mNbUpdated;
+	const PxBpIndex* mRemoved;
+	const uint32_t mNbRemoved;
+	const PxBounds3* mBounds;
+	const PxBpFilterGroup* mGroups;
+	const float* mDistances;
+	const uint32_t mCapacity;
+};
+
+struct PxBroadPhasePair { PxBpIndex mID0, mID1; };
+
+struct PxBroadPhaseResults
+{
+	PxBroadPhaseResults() : mNbCreatedPairs(0), mCreatedPairs(nullptr), mNbDeletedPairs(0), mDeletedPairs(nullptr) {}
+	uint32_t mNbCreatedPairs;
+	const PxBroadPhasePair* mCreatedPairs;
+	uint32_t mNbDeletedPairs;
+	const PxBroadPhasePair* mDeletedPairs;
+};
+
+// Same virtual functions, in the same order, as the reference's PxBroadPhase
+// (physx/include/PxBroadPhase.h:492-618): a caller's virtual calls land in the
+// same vtable slots.
+class PxBroadPhase
+{
+protected:
+	PxBroadPhase() {}
+	virtual ~PxBroadPhase() {}
+public:
+	virtual void release() = 0;
+	virtual PxBroadPhaseType::Enum getType() const = 0;
+	virtual void getCaps(PxBroadPhaseCaps& caps) const = 0;
+	virtual PxBroadPhaseRegions* getRegions() = 0;
+	virtual PxAllocatorCallback* getAllocator() = 0;
+	virtual uint64_t getContextID() const = 0;
+	virtual void setScratchBlock(void* scratchBlock, uint32_t size) = 0;
+	virtual void update(const PxBroadPhaseUpdateData& updateData, PxBaseTask* continuation = nullptr) = 0;
+	virtual void fetchResults(PxBroadPhaseResults& results) = 0;
+	void updateAndFetchResults(PxBroadPhaseResults& results, const PxBroadPhaseUpdateData& updateData)
+	{
+		update(updateData);
+		fetchResults(results);
+	}
+};
+
+// The reference's PxAABBManager (physx/include/PxBroadPhase.h:642-796), same order.
+class PxAABBManager
+{
+protected:
+	PxAABBManager() {}
+	virtual ~PxAABBManager() {}
+public:
+	virtual void release() = 0;
+	virtual PxBroadPhase& getBroadPhase() = 0;
+	virtual const PxBounds3* getBounds() const = 0;
+	virtual const float* getDistances() const = 0;
+	virtual const PxBpFilterGroup* getGroups() const = 0;
+	virtual uint32_t getCapacity() const = 0;
+	virtual void addObject(PxBpIndex index, const PxBounds3& bounds, PxBpFilterGroup group, float distance = 0.0f) = 0;
+	virtual void removeObject(PxBpIndex index) = 0;
+	virtual void updateObject(PxBpIndex index, const PxBounds3* bounds = nullptr, const float* distance = nullptr) = 0;
+	virtual void update(PxBaseTask* continuation = nullptr) = 0;
+	virtual void fetchResults(PxBroadPhaseResults& results) = 0;
+	void updateAndFetchResults(PxBroadPhaseResults& results)
+	{
+		update();
+		fetchResults(results);
+	}
+};
 } // namespace gbpx_px
 
 extern "C" {
@@ -217,6 +350,11 @@ void PxSolveConstraintsTGS(const gbpx_px::PxConstraintBatchHeader* batchHeaders,
                            void* Z, void* deltaV);
 void PxIntegrateSolverBodiesTGS(gbpx_px::PxTGSSolverBodyVel* solverBody, const gbpx_px::PxTGSSolverBodyTxInertia* txInertia,
                                 gbpx_px::PxTransform* poses, uint32_t nbBodiesToIntegrate, float dt);
+gbpx_px::PxBpFilterGroup PxGetBroadPhaseStaticFilterGroup();
+gbpx_px::PxBpFilterGroup PxGetBroadPhaseDynamicFilterGroup(uint32_t id);
+gbpx_px::PxBpFilterGroup PxGetBroadPhaseKinematicFilterGroup(uint32_t id);
+gbpx_px::PxBroadPhase* PxCreateBroadPhase(const gbpx_px::PxBroadPhaseDesc& desc);
+gbpx_px::PxAABBManager* PxCreateAABBManager(gbpx_px::PxBroadPhase& broadphase);
 }
 
 #endif /* GBPX_IMMEDIATE_H */

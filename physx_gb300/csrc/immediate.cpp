@@ -438,3 +438,213 @@ GX void PxIntegrateSolverBodiesTGS(PxTGSSolverBodyVel* solverBody, const PxTGSSo
 	(void)dt;
 	gbpx_integrate_solver_bodies_tgs(solverBody, txInertia, &poses[0].q.x, nbBodiesToIntegrate);
 }
+
+// ------------------------------------------------------------------ broadphase
+// PxCreateBroadPhase / PxBroadPhase (physx/include/PxBroadPhase.h:492-629) and
+// PxCreateAABBManager / PxAABBManager (:642-796) over libgbpx's ABP-compatible
+// broadphase (gbpx_bp_*).
+namespace
+{
+// Page-locked host memory: user bounds, groups and distances allocated here
+// reach the device without a staging copy.
+struct PinnedAllocator : PxAllocatorCallback
+{
+	void* allocate(size_t size, const char*, const char*, int) override
+	{
+		void* p = nullptr;
+		return gbpx_host_alloc(size ? size : 1, &p) == GBPX_OK ? p : nullptr;
+	}
+	void deallocate(void* ptr) override { if(ptr) gbpx_host_free(ptr); }
+};
+PinnedAllocator gPinned;
+
+class GbpxBroadPhase : public PxBroadPhase
+{
+public:
+	GbpxBroadPhase(const PxBroadPhaseDesc& d, void* h) : desc(d), handle(h) {}
+	void release() override
+	{
+		if(manager) return;   // the reference refuses while an AABB manager is attached
+		gbpx_bp_release(handle);
+		delete this;
+	}
+	PxBroadPhaseType::Enum getType() const override { return desc.mType; }
+	void getCaps(PxBroadPhaseCaps& caps) const override { caps.mMaxNbRegions = 0; }
+	PxBroadPhaseRegions* getRegions() override { return nullptr; }
+	PxAllocatorCallback* getAllocator() override { return &gPinned; }
+	uint64_t getContextID() const override { return desc.mContextID; }
+	void setScratchBlock(void*, uint32_t) override {}
+	void update(const PxBroadPhaseUpdateData& u, PxBaseTask*) override
+	{
+		status = gbpx_bp_update(handle, u.mCreated, u.mNbCreated, u.mUpdated, u.mNbUpdated, u.mRemoved, u.mNbRemoved,
+		                        reinterpret_cast<const float*>(u.mBounds), u.mGroups, u.mDistances, u.mCapacity);
+	}
+	void fetchResults(PxBroadPhaseResults& r) override
+	{
+		const uint32_t *created = nullptr, *lost = nullptr;
+		uint32_t nc = 0, nl = 0;
+		if(status == GBPX_OK && gbpx_bp_fetch_results(handle, &created, &nc, &lost, &nl) == GBPX_OK)
+		{
+			r.mNbCreatedPairs = nc;
+			r.mCreatedPairs = reinterpret_cast<const PxBroadPhasePair*>(created);
+			r.mNbDeletedPairs = nl;
+			r.mDeletedPairs = reinterpret_cast<const PxBroadPhasePair*>(lost);
+		}
+		else
+			r = PxBroadPhaseResults();
+	}
+
+	PxBroadPhaseDesc desc;
+	void* handle;
+	int status = GBPX_OK;
+	PxAABBManager* manager = nullptr;
+
+private:
+	~GbpxBroadPhase() override {}
+};
+
+// Per-index bit set (the reference's PxBitMap use: set, reset, test, visit in
+// increasing index order).
+struct IndexBits
+{
+	std::vector<uint64_t> words;
+	void grow(uint32_t n) { if(words.size() * 64 < n) words.resize((n + 63) / 64, 0); }
+	void set(uint32_t i) { grow(i + 1); words[i >> 6] |= 1ull << (i & 63); }
+	void reset(uint32_t i) { if((i >> 6) < words.size()) words[i >> 6] &= ~(1ull << (i & 63)); }
+	bool test(uint32_t i) const { return (i >> 6) < words.size() && (words[i >> 6] >> (i & 63)) & 1; }
+	void clear() { std::fill(words.begin(), words.end(), 0ull); }
+	template <typename F> void visit(F f) const
+	{
+		for(size_t w = 0; w < words.size(); w++)
+			for(uint64_t b = words[w]; b; b &= b - 1) f(uint32_t(w * 64 + __builtin_ctzll(b)));
+	}
+};
+
+constexpr PxBpFilterGroup INVALID_GROUP = 0xffffffffu;   // PX_INVALID_BP_FILTER_GROUP
+
+// The reference's high-level broadphase (NpImmediateMode.cpp:2160-2478): it owns
+// bounds / groups / distances arrays (from the broadphase's allocator, grown to
+// powers of two, one spare bounds entry for reads past the end), tracks the
+// objects added, updated and removed since the last update, and submits them
+// in increasing index order.
+class GbpxAABBManager : public PxAABBManager
+{
+public:
+	explicit GbpxAABBManager(GbpxBroadPhase& b) : bp(b) { bp.manager = this; }
+	void release() override { delete this; }
+	PxBroadPhase& getBroadPhase() override { return bp; }
+	const PxBounds3* getBounds() const override { return bounds; }
+	const float* getDistances() const override { return distances; }
+	const PxBpFilterGroup* getGroups() const override { return groups; }
+	uint32_t getCapacity() const override { return capacity; }
+
+	void addObject(PxBpIndex index, const PxBounds3& b, PxBpFilterGroup group, float distance) override
+	{
+		if(capacity < index + 1) reserve(index + 1);
+		bounds[index] = b;
+		groups[index] = group;
+		distances[index] = distance;
+		if(removedMap.test(index)) removedMap.reset(index);   // removed and re-added before an update: still in the broadphase
+		else addedMap.set(index);
+	}
+	void removeObject(PxBpIndex index) override
+	{
+		if(index >= capacity) return;
+		if(addedMap.test(index)) addedMap.reset(index);       // added since the last update: never reached the broadphase
+		else removedMap.set(index);
+		setEmpty(bounds[index]);
+		groups[index] = INVALID_GROUP;
+		distances[index] = 0.0f;
+	}
+	void updateObject(PxBpIndex index, const PxBounds3* b, const float* distance) override
+	{
+		if(index >= capacity) return;
+		updatedMap.set(index);
+		if(b) bounds[index] = *b;
+		if(distance) distances[index] = *distance;
+	}
+	void update(PxBaseTask* continuation) override
+	{
+		added.clear();
+		updated.clear();
+		removed.clear();
+		addedMap.visit([&](uint32_t i) { added.push_back(i); });
+		updatedMap.visit([&](uint32_t i) { if(!addedMap.test(i)) updated.push_back(i); });   // a new object is not also updated
+		removedMap.visit([&](uint32_t i) { removed.push_back(i); });
+		const PxBroadPhaseUpdateData data(added.data(), uint32_t(added.size()), updated.data(), uint32_t(updated.size()), removed.data(),
+		                                  uint32_t(removed.size()), bounds, groups, distances, capacity);
+		bp.update(data, continuation);
+		addedMap.clear();
+		removedMap.clear();
+		updatedMap.clear();
+	}
+	void fetchResults(PxBroadPhaseResults& r) override { bp.fetchResults(r); }
+
+private:
+	~GbpxAABBManager() override
+	{
+		PxAllocatorCallback* a = bp.getAllocator();
+		a->deallocate(distances);
+		a->deallocate(groups);
+		a->deallocate(bounds);
+		bp.manager = nullptr;
+	}
+	static void setEmpty(PxBounds3& b)   // PxBounds3::setEmpty: inverted maximal bounds
+	{
+		const float big = 0.25f * 3.402823466e+38f;   // PX_MAX_BOUNDS_EXTENTS
+		b.minimum = PxVec3{big, big, big};
+		b.maximum = PxVec3{-big, -big, -big};
+	}
+	void reserve(uint32_t needed)
+	{
+		uint32_t n = 1;
+		while(n < needed) n <<= 1;
+		PxAllocatorCallback* a = bp.getAllocator();
+		PxBounds3* nb = static_cast<PxBounds3*>(a->allocate(sizeof(PxBounds3) * (n + 1), "bounds", __FILE__, __LINE__));
+		PxBpFilterGroup* ng = static_cast<PxBpFilterGroup*>(a->allocate(sizeof(PxBpFilterGroup) * n, "groups", __FILE__, __LINE__));
+		float* nd = static_cast<float*>(a->allocate(sizeof(float) * n, "distances", __FILE__, __LINE__));
+		if(capacity)
+		{
+			memcpy(nb, bounds, sizeof(PxBounds3) * capacity);
+			memcpy(ng, groups, sizeof(PxBpFilterGroup) * capacity);
+			memcpy(nd, distances, sizeof(float) * capacity);
+		}
+		for(uint32_t i = capacity; i <= n; i++) setEmpty(nb[i]);
+		for(uint32_t i = capacity; i < n; i++) { ng[i] = INVALID_GROUP; nd[i] = 0.0f; }
+		a->deallocate(bounds);
+		a->deallocate(groups);
+		a->deallocate(distances);
+		bounds = nb;
+		groups = ng;
+		distances = nd;
+		capacity = n;
+	}
+
+	GbpxBroadPhase& bp;
+	PxBounds3* bounds = nullptr;
+	PxBpFilterGroup* groups = nullptr;
+	float* distances = nullptr;
+	uint32_t capacity = 0;
+	IndexBits addedMap, removedMap, updatedMap;
+	std::vector<uint32_t> added, updated, removed;
+};
+} // namespace
+
+GX PxBpFilterGroup PxGetBroadPhaseStaticFilterGroup() { return gbpx_bp_static_filter_group(); }
+GX PxBpFilterGroup PxGetBroadPhaseDynamicFilterGroup(uint32_t id) { return gbpx_bp_dynamic_filter_group(id); }
+GX PxBpFilterGroup PxGetBroadPhaseKinematicFilterGroup(uint32_t id) { return gbpx_bp_kinematic_filter_group(id); }
+
+GX PxBroadPhase* PxCreateBroadPhase(const PxBroadPhaseDesc& desc)
+{
+	if(desc.mType != PxBroadPhaseType::eABP && desc.mType != PxBroadPhaseType::ePABP) return nullptr;
+	void* h = nullptr;
+	if(gbpx_bp_create(desc.mDiscardStaticVsKinematic ? 1 : 0, desc.mDiscardKinematicVsKinematic ? 1 : 0, &h) != GBPX_OK) return nullptr;
+	return new GbpxBroadPhase(desc, h);
+}
+
+GX PxAABBManager* PxCreateAABBManager(PxBroadPhase& broadphase)
+{
+	GbpxBroadPhase& bp = static_cast<GbpxBroadPhase&>(broadphase);
+	if(bp.manager) return nullptr;   // one manager per broadphase
+	return new GbpxAABBManager(bp);
+}

@@ -18,7 +18,8 @@ struct StepParams
 	uint32_t nbPos, nbVel;
 	uint32_t persistent;   // carry contact manifolds and friction patches between steps
 	uint32_t largeBodies;  // scenes of more solver bodies run one block per scene (world)
-	uint32_t solveVariant; // staging slot of the warp-per-scene solve (world): 0 none, 1 256 B, 2 512 B per lane
+	uint32_t solveVariant; // solve kernel of the world: the resident solve, or a staging variant of the warp-per-scene solve
+	uint32_t resBytes;     // shared-memory workspace of one resident-solve block (world)
 };
 
 // no slot in last step's pair list (a new pair)

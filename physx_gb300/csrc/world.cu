@@ -42,7 +42,42 @@ namespace gbpx
 namespace world
 {
 constexpr uint32_t MAX_PARTITIONS = 128;
-enum : uint32_t { ST_PAIR_OVERFLOW = 1, ST_PARTITION_OVERFLOW = 2 };
+enum : uint32_t { ST_PAIR_OVERFLOW = 1, ST_PARTITION_OVERFLOW = 2, ST_STAGE_TIMEOUT = 4 };
+
+// Resident solve (solveResidentKernel): one block of RES_WARPS warps per SM
+// with the whole opt-in shared memory as its workspace.  Each scene's packed
+// rows and body velocities are copied on chip once and stay there for all
+// iterations.  Scenes are filed by on-chip footprint into RES_LEVELS levels:
+// at level L the block works as 2^L groups of RES_WARPS >> L warps, each group
+// solving one scene at a time in 1/2^L of the workspace.
+constexpr uint32_t RES_WARPS = 8;
+constexpr uint32_t RES_LEVELS = 4;
+static_assert((RES_WARPS >> (RES_LEVELS - 1)) >= 1 && RES_WARPS <= 16, "levels down to one warp; named barriers 1..RES_WARPS-1");
+constexpr uint32_t RES_HEADER = MAX_PARTITIONS * 4;   // partition ends at the start of a group's slice
+// work counters (after the per-kind pair counts and path counts): scenes filed
+// per level, then scenes taken per level
+constexpr uint32_t WC_RES_COUNT = 8 + 9 + 4;
+constexpr uint32_t WC_RES_NEXT = WC_RES_COUNT + RES_LEVELS;
+constexpr uint32_t NB_WORK_COUNTERS = WC_RES_NEXT + RES_LEVELS;
+// StepParams::solveVariant selecting the resident solve (0-7 are staging
+// variants of the warp-per-scene solve)
+constexpr uint32_t RESIDENT_VARIANT = 8;
+
+__host__ __device__ __forceinline__ uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
+// On-chip bytes of a scene in the resident solve: partition ends, 16-bit row
+// offsets (16-byte units), lin / ang / dLin / dAng of every solver body, rows.
+__host__ __device__ __forceinline__ uint32_t residentBytes(uint32_t nc, uint32_t nTot, uint32_t rowChunks)
+{
+	return RES_HEADER + align16(2 * nc) + align16(48 * nTot) + 16 * rowChunks;
+}
+// Smallest slice (deepest level) that holds `need` bytes; level 0 also takes
+// scenes too large for any slice (their rows stay in HBM).
+__host__ __device__ __forceinline__ uint32_t residentLevel(uint32_t need, uint32_t resBytes)
+{
+	uint32_t L = 0;
+	while(L + 1 < RES_LEVELS && need <= (resBytes >> (L + 1))) L++;
+	return L;
+}
 
 struct SceneDesc
 {
@@ -105,7 +140,18 @@ struct WorldDev
 	uint32_t* sceneParity;     // per scene
 	np::ManifoldRecord* manifolds[2];
 	tgs::FrictionState* frictionState[2];
+	// Resident solve: per scene, constraints prepared and their row chunks
+	// (count << 32 | chunks); per footprint level, the scenes to solve.
+	unsigned long long* sceneAcc;
+	uint32_t* resList;         // RES_LEVELS lists of resCap scene ids
+	uint32_t resCap;
 };
+__device__ __forceinline__ void residentAppend(const WorldDev& w, uint32_t sid, uint32_t level)
+{
+	const uint32_t i = atomicAdd(&w.workCounter[WC_RES_COUNT + level], 1u);
+	w.resList[size_t(level) * w.resCap + i] = sid;
+}
+
 // A group of G warps working on one scene: G = 1 is one warp (several scenes
 // per block), G > 1 is the whole block (one scene per block, for large scenes).
 template <uint32_t G>
@@ -732,6 +778,12 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 		w.nbConstraints[sid] = nc;
 		w.nbPartitions[sid] = nbPart;
 		if(!nbPart && nc) atomicOr(&w.status[sid], ST_PARTITION_OVERFLOW);
+		if(sp.solveVariant == RESIDENT_VARIANT)
+		{
+			// the row preparation files scenes with constraints once their last row is built
+			w.sceneAcc[sid] = 0;
+			if(!nbPart) residentAppend(w, sid, residentLevel(residentBytes(0, nTot, 0), sp.resBytes));
+		}
 	}
 	if(!nbPart) return;   // nothing to solve, or overflow: the scene is left unchanged
 	uint32_t qbase = 0;
@@ -759,7 +811,7 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 
 // Contact rows of one constraint (PxCreateContactConstraintsTGS for one
 // descriptor): slot = scene pair start + position in solve order.
-__device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, const StepParams& sp)
+__device__ __forceinline__ uint32_t prepSlot(const WorldDev& w, uint32_t entry, const StepParams& sp)
 {
 	const uint32_t slot = entry & 0x7fffffffu;
 	const bool block = (entry >> 31) != 0;
@@ -805,7 +857,24 @@ __device__ __forceinline__ void prepSlot(const WorldDev& w, uint32_t entry, cons
 	else
 		tgs::prepConstraint(cs, int(cnt), int(a), int(b), vel[a], vel[b], tx[a], tx[b], data[a], data[b], pose[a], pose[b], pp, rec, prevFriction,
 		                    written);
-	w.recChunks[slot] = uint8_t((rec.bytes() + 15) / 16);
+	const uint32_t chunks = (rec.bytes() + 15) / 16;
+	w.recChunks[slot] = uint8_t(chunks);
+	return chunks;
+}
+
+// Counts a prepared constraint towards its scene; the scene's last one files
+// the scene for the resident solve at the level its footprint fits.
+__device__ __forceinline__ void residentCount(const WorldDev& w, uint32_t slot, uint32_t chunks, const StepParams& sp)
+{
+	const uint32_t sid = w.slotScene[slot];
+	const unsigned long long old = atomicAdd(&w.sceneAcc[sid], (1ull << 32) | chunks);
+	const uint32_t nc = w.nbConstraints[sid];
+	if(uint32_t(old >> 32) + 1u == nc)
+	{
+		const SceneDesc sc = w.scenes[sid];
+		const uint32_t need = residentBytes(nc, sc.nbBodies + sc.nbStatics, uint32_t(old) + chunks);
+		residentAppend(w, sid, residentLevel(need, sp.resBytes));
+	}
 }
 
 // Velocities of one scene's solver bodies during the iterations: linear and
@@ -855,6 +924,7 @@ using IterSmemBig = IterSmemT<BIG_SOLVE_BODIES, BIG_SOLVE_CONSTRAINTS, 0>;
 // staging with velocities on chip / in HBM (the largest slot that leaves room for 8 warps per SM with
 // the velocities on chip; one-patch four-point rows are 392 B)
 constexpr uint32_t SOLVE_VARIANTS = 8;
+static_assert(RESIDENT_VARIANT == SOLVE_VARIANTS, "the resident solve follows the staging variants");
 constexpr uint32_t MID_CHUNKS = 25;
 
 template <uint32_t G, uint32_t CAPB, uint32_t CAPC, uint32_t RB, typename Vel>
@@ -1041,7 +1111,12 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) batchBigKernel(WorldDev w, Ste
 __global__ void __launch_bounds__(128, 5) prepKernel(WorldDev w, StepParams sp)
 {
 	const uint32_t count = w.workCounter[WC_PREP];
-	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) prepSlot(w, w.prepQueue[q], sp);
+	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+	{
+		const uint32_t entry = w.prepQueue[q];
+		const uint32_t chunks = prepSlot(w, entry, sp);
+		if(sp.solveVariant == RESIDENT_VARIANT) residentCount(w, entry & 0x7fffffffu, chunks, sp);
+	}
 }
 
 // Iterations of one scene; afterwards the state this step wrote becomes the
@@ -1081,6 +1156,330 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) solveBigKernel(WorldDev w, Ste
 	uint32_t sid;
 	SceneDesc sc;
 	while(nextScene<BIG_WARPS>(w, WC_SOLVE_BIG, true, sp, sid, sc, &sm.bc)) solveScene<BIG_WARPS>(w, sc, sid, sp, sm);
+}
+
+// ------------------------------------------------------------------ resident solve
+// Shared-memory barrier (mbarrier) and bulk-copy primitives (PTX, sm_90+).
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbarInit(unsigned long long* bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbarArriveExpectTx(unsigned long long* bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smemAddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(unsigned long long* bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
+	             : "=r"(ok)
+	             : "r"(smemAddr(bar)), "r"(parity)
+	             : "memory");
+	return ok != 0;
+}
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// this GPU's global memory into this block's shared memory, completing on `bar`.
+__device__ __forceinline__ void bulkCopyToShared(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(smemAddr(dst)), "l"(src),
+	             "r"(bytes), "r"(smemAddr(bar))
+	             : "memory");
+}
+// Orders this thread's earlier shared-memory accesses before later bulk copies into them.
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// try_wait rounds before a bulk copy counts as lost (each round may suspend the
+// thread for a while; this is well above a second)
+constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 22;
+
+// Barrier of the nt threads of a group (barId: named barrier of the group; one
+// warp synchronises with __syncwarp).
+__device__ __forceinline__ void groupSync(uint32_t barId, uint32_t nt)
+{
+	if(nt == 32) __syncwarp();
+	else asm volatile("bar.sync %0, %1;\n" ::"r"(barId), "r"(nt) : "memory");
+}
+
+// Exclusive prefix of `sum` over a group's threads in thread order; `total`
+// gets the group's sum.  scratch: one word per warp of the group.
+__device__ __forceinline__ uint32_t groupPrefix(uint32_t sum, uint32_t* scratch, uint32_t gtid, uint32_t nt, uint32_t barId, uint32_t& total)
+{
+	const uint32_t lane = gtid & 31, gwarp = gtid >> 5;
+	uint32_t incl = sum;
+	for(int o = 1; o < 32; o <<= 1)
+	{
+		const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+		if(lane >= uint32_t(o)) incl += t;
+	}
+	if(lane == 31) scratch[gwarp] = incl;
+	groupSync(barId, nt);
+	uint32_t off = 0, tot = 0;
+	for(uint32_t q = 0; q < (nt >> 5); q++)
+	{
+		const uint32_t v = scratch[q];
+		if(q < gwarp) off += v;
+		tot += v;
+	}
+	groupSync(barId, nt);
+	total = tot;
+	return off + incl - sum;
+}
+
+// Velocities of the solver bodies of a scene during the resident solve: linear,
+// (momentum-space) angular and the accumulated position / rotation deltas, in
+// four shared-memory arrays, or in the BodyVel records in HBM for scenes whose
+// bodies do not fit the slice.
+struct ResVel
+{
+	V3 *l, *a, *dl, *da;
+	__device__ __forceinline__ V3 lin(uint32_t i) const { return l[i]; }
+	__device__ __forceinline__ V3 ang(uint32_t i) const { return a[i]; }
+	__device__ __forceinline__ V3 dLin(uint32_t i) const { return dl[i]; }
+	__device__ __forceinline__ V3 dAng(uint32_t i) const { return da[i]; }
+	__device__ __forceinline__ void set(uint32_t i, V3 lv, V3 av) const { l[i] = lv; a[i] = av; }
+	__device__ __forceinline__ void setDelta(uint32_t i, V3 dlv, V3 dav) const { dl[i] = dlv; da[i] = dav; }
+};
+struct ResHbmVel
+{
+	tgs::BodyVel* v;
+	__device__ __forceinline__ V3 lin(uint32_t i) const { return v[i].lin; }
+	__device__ __forceinline__ V3 ang(uint32_t i) const { return v[i].ang; }
+	__device__ __forceinline__ V3 dLin(uint32_t i) const { return v[i].dLin; }
+	__device__ __forceinline__ V3 dAng(uint32_t i) const { return v[i].dAng; }
+	__device__ __forceinline__ void set(uint32_t i, V3 lv, V3 av) const { v[i].lin = lv; v[i].ang = av; }
+	__device__ __forceinline__ void setDelta(uint32_t i, V3 dlv, V3 dav) const { v[i].dLin = dlv; v[i].dAng = dav; }
+};
+
+// Position iterations (each followed by integration), velocity iterations,
+// PxIntegrateSolverBodiesTGS and write-back of one scene by a group of nt
+// threads: the arithmetic of sceneIterate.  ROWS_ON_CHIP: the rows of
+// constraint r sit at rows + 16 * off[r] in shared memory (the solve's impulses
+// stay there: nothing reads them after the solve); otherwise they are used in
+// place in HBM.
+template <bool ROWS_ON_CHIP, typename Vel>
+__device__ __forceinline__ void residentIterate(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp, const uint32_t* ends,
+                                                uint32_t nbPart, const uint16_t* off, unsigned char* rows, const Vel& V, uint32_t gtid,
+                                                uint32_t nt, uint32_t barId)
+{
+	const uint32_t n = sc.nbBodies;
+	tgs::BodyTx* tx = w.tx + sc.solverStart;
+	Tr* pose = w.pose + sc.solverStart;
+	auto recAt = [&](uint32_t r) -> tgs::ConstraintRecord* {
+		if constexpr(ROWS_ON_CHIP) return reinterpret_cast<tgs::ConstraintRecord*>(rows + 16u * off[r]);
+		else return w.recs + sc.pairStart + r;
+	};
+	const float stepDt = sp.dt / float(sp.nbPos);
+	float elapsed = 0.0f;
+	for(uint32_t it = 0; it < sp.nbPos + sp.nbVel; it++)
+	{
+		const bool posIter = it < sp.nbPos;
+		const bool lastIter = it + 1 == sp.nbPos + sp.nbVel;
+		const float minPen = posIter ? -FLT_MAX : 0.0f;
+		uint32_t begin = 0;
+		for(uint32_t p = 0; p < nbPart; p++)
+		{
+			const uint32_t end = ends[p];
+			for(uint32_t r = begin + gtid; r < end; r += nt)
+			{
+				tgs::ConstraintRecord* rec = recAt(r);
+				if(rec->nbPatches == 0) continue;
+				const uint32_t a = uint32_t(rec->bodyA), b = uint32_t(rec->bodyB);
+				tgs::BodyVel b0, b1;
+				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = V.dLin(a); b0.dAng = V.dAng(a);
+				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = V.dLin(b); b1.dAng = V.dAng(b);
+				const bool dynB = b < n;
+				uint32_t broken = 0;
+				tgs::solveRecord(*rec, b0, b1, dynB, minPen, elapsed, sp.persistent && lastIter ? &broken : nullptr);
+				if(broken)
+				{
+					// a patch whose friction was clamped in the last iteration marks the
+					// friction patch it wrote broken
+					tgs::FrictionState& fs = w.frictionState[w.sceneParity[sid] ^ 1u][sc.pairStart + w.ordered[sc.pairStart + r]];
+					tgs::ConstraintRecord* group[4] = {nullptr, nullptr, nullptr, nullptr};
+					if(rec->isBlock())
+					{
+						const uint32_t r0 = begin + ((r - begin) & ~3u);
+						for(uint32_t l = 0; l < 4; l++) group[l] = recAt(r0 + l);
+					}
+					for(int pi = 0; pi < rec->nbPatches; pi++)
+						if(broken & (1u << pi))
+						{
+							const int slotIdx = rec->isBlock() ? tgs::blockBrokenSlot(group, pi) : pi;
+							if(uint32_t(slotIdx) < fs.count) fs.patches[slotIdx].broken = 1;
+						}
+				}
+				V.set(a, b0.lin, b0.ang);
+				if(dynB) V.set(b, b1.lin, b1.ang);
+			}
+			begin = end;
+			groupSync(barId, nt);
+		}
+		if(posIter)
+		{
+			for(uint32_t i = gtid; i < n; i += nt)
+			{
+				tgs::BodyVel v;
+				v.lin = V.lin(i); v.ang = V.ang(i); v.dLin = V.dLin(i); v.dAng = V.dAng(i);
+				tgs::integrateStep(v, tx[i], stepDt);
+				V.setDelta(i, v.dLin, v.dAng);
+			}
+			elapsed += stepDt;
+			groupSync(barId, nt);
+		}
+	}
+	for(uint32_t i = gtid; i < n; i += nt)
+	{
+		tgs::BodyVel v;
+		v.lin = V.lin(i); v.ang = V.ang(i); v.dLin = V.dLin(i); v.dAng = V.dAng(i);
+		Tr p = pose[i];
+		V3 wv;
+		tgs::finalizeBody(v, tx[i], p, wv);
+		tgs::RigidBody& rb = w.bodies[sc.bodyStart + i];
+		rb.linVel[0] = v.lin.x; rb.linVel[1] = v.lin.y; rb.linVel[2] = v.lin.z;
+		rb.angVel[0] = wv.x; rb.angVel[1] = wv.y; rb.angVel[2] = wv.z;
+		rb.q[0] = p.q.x; rb.q[1] = p.q.y; rb.q[2] = p.q.z; rb.q[3] = p.q.w;
+		rb.p[0] = p.p.x; rb.p[1] = p.p.y; rb.p[2] = p.p.z;
+	}
+}
+
+// Per-group state of the resident solve kept in static shared memory.
+struct ResGroupState
+{
+	unsigned long long* bar;   // the group's bulk-copy barrier
+	uint32_t* phase;           // parity of the barrier phase the group waits for next
+	uint32_t* word;            // broadcast word
+	uint32_t* scratch;         // one word per warp of the group
+};
+
+// One scene on one group's slice: partition ends, row offsets, the rows (bulk
+// copies, one per constraint, completing on the group's barrier) and the body
+// velocities go on chip, then the iterations run there.  Returns false when a
+// bulk copy did not complete within the wait limit (the scene is flagged
+// ST_STAGE_TIMEOUT and the group stops).
+__device__ __forceinline__ bool solveResidentScene(const WorldDev& w, uint32_t sid, const StepParams& sp, unsigned char* slice, uint32_t sliceBytes,
+                                   const ResGroupState& gs, uint32_t gtid, uint32_t nt, uint32_t barId)
+{
+	const SceneDesc sc = w.scenes[sid];
+	const uint32_t nbPart = w.nbPartitions[sid];
+	const uint32_t ncAll = w.nbConstraints[sid];
+	if(nbPart || !ncAll)   // batching overflowed: the scene is left unchanged
+	{
+		const uint32_t nc = nbPart ? ncAll : 0u;
+		const uint32_t nTot = sc.nbBodies + sc.nbStatics;
+		uint32_t* ends = reinterpret_cast<uint32_t*>(slice);
+		uint16_t* off = reinterpret_cast<uint16_t*>(slice + RES_HEADER);
+		const uint32_t offBytes = align16(2 * nc), velBytes = align16(48 * nTot);
+		V3* velBase = reinterpret_cast<V3*>(slice + RES_HEADER + offBytes);
+		unsigned char* rows = slice + RES_HEADER + offBytes + velBytes;
+		// this thread's run of constraints and the offset of its first row chunk
+		const uint32_t per = (nc + nt - 1) / nt;
+		const uint32_t r0 = min(gtid * per, nc), r1 = min(r0 + per, nc);
+		const uint8_t* chunks = w.recChunks + sc.pairStart;
+		uint32_t runChunks = 0;
+		for(uint32_t r = r0; r < r1; r++) runChunks += chunks[r];
+		uint32_t total = 0;
+		const uint32_t first = groupPrefix(runChunks, gs.scratch, gtid, nt, barId, total);
+		const bool velOnChip = RES_HEADER + offBytes + velBytes <= sliceBytes;
+		const bool rowsOnChip = velOnChip && RES_HEADER + offBytes + velBytes + 16u * total <= sliceBytes;
+		// the slice was last read by generic loads (previous scene): order them
+		// before the bulk copies that overwrite it
+		fenceProxyAsync();
+		for(uint32_t p = gtid; p < nbPart; p += nt) ends[p] = w.partEnds[size_t(sid) * MAX_PARTITIONS + p];
+		const bool staging = rowsOnChip && total > 0;
+		if(staging)
+		{
+			if(gtid == 0) mbarArriveExpectTx(gs.bar, 16u * total);
+			groupSync(barId, nt);
+			uint32_t o = first;
+			for(uint32_t r = r0; r < r1; r++)
+			{
+				const uint32_t c = chunks[r];
+				off[r] = uint16_t(o);
+				bulkCopyToShared(rows + 16u * o, w.recs + sc.pairStart + r, 16u * c, gs.bar);
+				o += c;
+			}
+		}
+		const ResVel rv = {velBase, velBase + nTot, velBase + 2 * nTot, velBase + 3 * nTot};
+		if(velOnChip)
+		{
+			const tgs::BodyVel* vel = w.vel + sc.solverStart;
+			for(uint32_t i = gtid; i < nTot; i += nt)
+			{
+				const tgs::BodyVel v = vel[i];
+				rv.set(i, v.lin, v.ang);
+				rv.setDelta(i, v.dLin, v.dAng);
+			}
+		}
+		if(staging)
+		{
+			const uint32_t parity = *gs.phase;
+			bool done = false;
+			for(uint32_t k = 0; k < STAGE_WAIT_LIMIT && !done; k++) done = mbarTryWait(gs.bar, parity);
+			const bool allDone = __all_sync(0xffffffffu, done);
+			if(!allDone && (gtid & 31) == 0) atomicOr(gs.word, 1u);
+			groupSync(barId, nt);
+			if(*gs.word)
+			{
+				// a copy is lost: flag the scene, give the copies in flight a last bounded
+				// wait (they write into this slice), and stop this group
+				if(gtid == 0) atomicOr(&w.status[sid], ST_STAGE_TIMEOUT);
+				for(uint32_t k = 0; k < STAGE_WAIT_LIMIT && !done; k++) done = mbarTryWait(gs.bar, parity);
+				return false;
+			}
+			groupSync(barId, nt);
+			if(gtid == 0) *gs.phase = parity ^ 1u;
+		}
+		groupSync(barId, nt);
+		if(rowsOnChip) residentIterate<true>(w, sc, sid, sp, ends, nbPart, off, rows, rv, gtid, nt, barId);
+		else if(velOnChip) residentIterate<false>(w, sc, sid, sp, ends, nbPart, off, rows, rv, gtid, nt, barId);
+		else residentIterate<false>(w, sc, sid, sp, ends, nbPart, off, rows, ResHbmVel{w.vel + sc.solverStart}, gtid, nt, barId);
+	}
+	groupSync(barId, nt);
+	if(sp.persistent && gtid == 0) w.sceneParity[sid] ^= 1u;
+	return true;
+}
+
+// The resident solve: persistent, one block per SM.  Level by level (largest
+// footprints first) the block's groups take scenes from the level's list;
+// a group that finds its level's list empty splits into the next level's
+// groups, which go on without waiting for the rest of the block.
+__global__ void __launch_bounds__(RES_WARPS * 32, 1) solveResidentKernel(WorldDev w, StepParams sp)
+{
+	extern __shared__ __align__(128) unsigned char resSmem[];
+	__shared__ __align__(8) unsigned long long bar[RES_WARPS];
+	__shared__ uint32_t phase[RES_WARPS], word[RES_WARPS], scratch[RES_WARPS];
+	const uint32_t warp = threadIdx.x >> 5;
+	if(threadIdx.x < RES_WARPS)
+	{
+		mbarInit(&bar[threadIdx.x], 1);
+		phase[threadIdx.x] = 0;
+		word[threadIdx.x] = 0;
+	}
+	asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+	__syncthreads();
+	for(uint32_t level = 0; level < RES_LEVELS; level++)
+	{
+		const uint32_t gw = RES_WARPS >> level, group = warp / gw, first = group * gw;
+		const uint32_t nt = gw * 32, gtid = threadIdx.x - first * 32;
+		// named barrier of the group: 2^level + group (1 .. 2 * RES_WARPS - 1); single warps use __syncwarp
+		const uint32_t barId = nt > 32 ? (1u << level) + group : 0u;
+		const uint32_t sliceBytes = sp.resBytes >> level;
+		unsigned char* slice = resSmem + size_t(group) * sliceBytes;
+		const ResGroupState gs = {&bar[first], &phase[first], &word[first], &scratch[first]};
+		const uint32_t count = w.workCounter[WC_RES_COUNT + level];
+		for(;;)
+		{
+			if(gtid == 0) *gs.word = atomicAdd(&w.workCounter[WC_RES_NEXT + level], 1u);
+			groupSync(barId, nt);
+			const uint32_t idx = *gs.word;
+			groupSync(barId, nt);
+			if(idx >= count) break;
+			if(gtid == 0) *gs.word = 0;   // the timeout vote of this scene
+			groupSync(barId, nt);
+			if(!solveResidentScene(w, w.resList[size_t(level) * w.resCap + idx], sp, slice, sliceBytes, gs, gtid, nt, barId)) return;
+			groupSync(barId, nt);
+		}
+	}
 }
 
 // Totals over all scenes after a step: pairs, pairs with contacts, contacts.
@@ -1131,12 +1530,14 @@ struct World
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve[world::SOLVE_VARIANTS] = {}, gridNp[world::NB_KINDS] = {};
-	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0;
+	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0, gridRes = 0;
 	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
 	uint32_t pairsPerBody = 0;
 	// scenes above this many solver bodies run one block per scene (warp per scene below)
 	static constexpr uint32_t DEFAULT_LARGE_BODIES = 512;
 	static constexpr uint32_t BIG_THREADS = world::BIG_WARPS * 32;
+	static constexpr uint32_t RES_THREADS = world::RES_WARPS * 32;
+	bool resident() const { return params.solveVariant == world::RESIDENT_VARIANT; }
 	bool launchLarge() const { return maxSolverBodies > params.largeBodies; }
 	DevBuf<world::SceneDesc> scenes;
 	DevBuf<uint32_t> typeQueueSorted;
@@ -1154,6 +1555,8 @@ struct World
 	DevBuf<uint32_t> pairsPrev, pairCountPrev, prevSlot, sceneParity;
 	DevBuf<np::ManifoldRecord> manifolds[2];
 	DevBuf<tgs::FrictionState> frictionState[2];
+	DevBuf<unsigned long long> sceneAcc;
+	DevBuf<uint32_t> resList;
 	DevBuf<tgs::BodyVel> vel;
 	DevBuf<tgs::BodyTx> tx;
 	DevBuf<tgs::BodyData> data;
@@ -1163,7 +1566,8 @@ struct World
 
 	static uint32_t pow2(uint32_t x) { uint32_t p = 1; while(p < x) p <<= 1; return p; }
 	// work counters of the broadphase and solve kernels, then the per-kind pair counts
-	static constexpr uint32_t COUNTERS = 8 + world::NB_KINDS + 4;
+	static constexpr uint32_t COUNTERS = world::NB_WORK_COUNTERS;
+	static_assert(world::WC_RES_COUNT == 8 + world::NB_KINDS + 4, "resident-solve counters follow the pair-kind and path counters");
 	// broadphase, one narrowphase kernel per pair kind, batching, row preparation, solve
 	static constexpr uint32_t KERNELS_PER_STEP = 4 + world::NB_KINDS;
 
@@ -1182,6 +1586,7 @@ struct World
 		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.recChunks = recChunks.ptr;
 		w.pairsPrev = pairsPrev.ptr; w.pairCountPrev = pairCountPrev.ptr; w.prevSlot = prevSlot.ptr; w.sceneParity = sceneParity.ptr;
 		for(int k = 0; k < 2; k++) { w.manifolds[k] = manifolds[k].ptr; w.frictionState[k] = frictionState[k].ptr; }
+		w.sceneAcc = sceneAcc.ptr; w.resList = resList.ptr; w.resCap = nbScenes;
 		return w;
 	}
 
@@ -1225,7 +1630,8 @@ struct World
 		   vel.reserve(nbSolver) || tx.reserve(nbSolver) || data.reserve(nbSolver) || pose.reserve(nbSolver) || progress.reserve(nbSolver) ||
 		   maxNormal.reserve(nbSolver) || maxStatic.reserve(nbSolver) || staticProgress.reserve(nbSolver) ||
 		   partEnds.reserve(size_t(S) * world::MAX_PARTITIONS) || status.reserve(S) || hStage.reserve(b) || stats.reserve(4) ||
-		   identity.reserve(S) || pairCountPrev.reserve(S) || sceneParity.reserve(S))
+		   identity.reserve(S) || pairCountPrev.reserve(S) || sceneParity.reserve(S) || sceneAcc.reserve(S) ||
+		   resList.reserve(size_t(world::RES_LEVELS) * S))
 			return GBPX_ERR_NOMEM;
 		if(sp.persistent &&
 		   (pairsPrev.reserve(pair) || prevSlot.reserve(pair) || manifolds[0].reserve(pair) || manifolds[1].reserve(pair) ||
@@ -1293,6 +1699,17 @@ struct World
 		GBPX_CUDA_TRY(gridFor(world::batchBigKernel, sms, gridBatchBig, sizeof(world::SolveSmemBig), int(BIG_THREADS)));
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::IterSmemBig))));
 		GBPX_CUDA_TRY(gridFor(world::solveBigKernel, sms, gridSolveBig, sizeof(world::IterSmemBig), int(BIG_THREADS)));
+		// resident solve: all the opt-in shared memory a block may have, less the
+		// kernel's static part, rounded so that every level's slice stays 16-byte
+		// aligned (bulk copies and float4 rows need it); one block per SM
+		int optin = 0;
+		GBPX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+		cudaFuncAttributes fa;
+		GBPX_CUDA_TRY(cudaFuncGetAttributes(&fa, world::solveResidentKernel));
+		const size_t unit = size_t(16) << (world::RES_LEVELS - 1);   // the deepest level's slice stays a multiple of 16 bytes
+		params.resBytes = uint32_t((size_t(optin) - fa.sharedSizeBytes) / unit * unit);
+		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::solveResidentKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(params.resBytes)));
+		GBPX_CUDA_TRY(gridFor(world::solveResidentKernel, sms, gridRes, params.resBytes, int(RES_THREADS)));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 		return GBPX_OK;
 	}
@@ -1385,13 +1802,19 @@ struct World
 			if(!plain) GBPX_CUDA_TRY(join(1));
 		}
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
-		const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
-		if(big && !plain) GBPX_CUDA_TRY(fork(2));
-		solveKernels()[sv]<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32, sv), stream>>>(w, params);
-		if(big)
+		if(resident())
+			// every scene, large or small, in one launch
+			world::solveResidentKernel<<<plain ? 1u : gridRes, RES_THREADS, params.resBytes, stream>>>(w, params);
+		else
 		{
-			world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), bigStream>>>(w, params);
-			if(!plain) GBPX_CUDA_TRY(join(2));
+			const uint32_t solveThreads = plain ? 32 : world::SOLVE_WARPS * 32;
+			if(big && !plain) GBPX_CUDA_TRY(fork(2));
+			solveKernels()[sv]<<<gSolve, solveThreads, iterSmemBytes(solveThreads / 32, sv), stream>>>(w, params);
+			if(big)
+			{
+				world::solveBigKernel<<<plain ? 1u : gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), bigStream>>>(w, params);
+				if(!plain) GBPX_CUDA_TRY(join(2));
+			}
 		}
 		GBPX_CUDA_TRY(cudaGetLastError());
 		return GBPX_OK;
@@ -1463,9 +1886,13 @@ struct World
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			world::prepKernel<<<gridPrep, 128, 0, stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
-			solveKernels()[params.solveVariant]<<<gridSolve[params.solveVariant], world::SOLVE_WARPS * 32,
-			                                      iterSmemBytes(world::SOLVE_WARPS, params.solveVariant), stream>>>(w, params);
-			if(big) world::solveBigKernel<<<gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
+			if(resident()) world::solveResidentKernel<<<gridRes, RES_THREADS, params.resBytes, stream>>>(w, params);
+			else
+			{
+				solveKernels()[params.solveVariant]<<<gridSolve[params.solveVariant], world::SOLVE_WARPS * 32,
+				                                      iterSmemBytes(world::SOLVE_WARPS, params.solveVariant), stream>>>(w, params);
+				if(big) world::solveBigKernel<<<gridSolveBig, BIG_THREADS, sizeof(world::IterSmemBig), stream>>>(w, params);
+			}
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			GBPX_CUDA_TRY(cudaGetLastError());
 			GBPX_CUDA_TRY(cudaEventSynchronize(ev[K]));
@@ -1534,7 +1961,7 @@ struct World
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
-		keys.release(); stats.release(); identity.release(); recs.release(); vel.release(); tx.release(); data.release(); pose.release(); hStage.release();
+		keys.release(); stats.release(); identity.release(); recs.release(); sceneAcc.release(); resList.release(); vel.release(); tx.release(); data.release(); pose.release(); hStage.release();
 		if(sideStream) { cudaStreamSynchronize(sideStream); cudaStreamDestroy(sideStream); }
 		sideStream = 0;
 		for(int k = 0; k < 3; k++)
@@ -1574,7 +2001,8 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
-	sp.solveVariant = 2;   // velocities on chip, 512-byte staging
+	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
+	sp.resBytes = 0;       // set at creation
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -1648,7 +2076,7 @@ GBPX_API int gbpx_world_info(void* wv, uint64_t* out8)
 	if(!w || !out8) return GBPX_ERR_INVALID;
 	out8[0] = w->nbScenes; out8[1] = w->nbBodies; out8[2] = w->nbStatics; out8[3] = w->nbPairSlots; out8[4] = w->gridBlocks;
 	out8[5] = w->deviceBytes;
-	out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? 3u : 0u) + (w->params.persistent ? 1u : 0u);
+	out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? (w->resident() ? 2u : 3u) : 0u) + (w->params.persistent ? 1u : 0u);
 	out8[7] = w->params.largeBodies;
 	return GBPX_OK;
 }
@@ -1730,6 +2158,38 @@ GBPX_API int gbpx_world_stats(void* wv, uint64_t* out4)
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(out4, w->stats.ptr, 4 * 8, cudaMemcpyDeviceToHost, w->stream));
 	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	return GBPX_OK;
+}
+
+// Per scene after the last step: constraints, partitions, bytes of packed
+// constraint rows, and the widest partition (constraints) -- the figures that
+// set the solve's on-chip footprint and critical path.  out4: 4 words per scene.
+GBPX_API int gbpx_world_solve_profile(void* wv, uint32_t* out4)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !out4) return GBPX_ERR_INVALID;
+	const uint32_t S = w->nbScenes;
+	std::vector<uint32_t> nc(S), np(S), ends(size_t(S) * gbpx::world::MAX_PARTITIONS);
+	std::vector<uint8_t> chunks(w->nbPairSlots);
+	GBPX_CUDA_TRY(cudaMemcpyAsync(nc.data(), w->nbConstraints.ptr, S * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(np.data(), w->nbPartitions.ptr, S * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ends.data(), w->partEnds.ptr, ends.size() * 4, cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(chunks.data(), w->recChunks.ptr, chunks.size(), cudaMemcpyDeviceToHost, w->stream));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	for(uint32_t s = 0; s < S; s++)
+	{
+		const uint32_t p = np[s], n = p ? nc[s] : 0;
+		uint64_t bytes = 0;
+		for(uint32_t r = 0; r < n; r++) bytes += 16u * chunks[w->hScenes[s].pairStart + r];
+		uint32_t widest = 0, begin = 0;
+		for(uint32_t k = 0; k < p; k++)
+		{
+			const uint32_t e = ends[size_t(s) * gbpx::world::MAX_PARTITIONS + k];
+			widest = std::max(widest, e - begin);
+			begin = e;
+		}
+		out4[4 * s + 0] = n; out4[4 * s + 1] = p; out4[4 * s + 2] = uint32_t(bytes); out4[4 * s + 3] = widest;
+	}
 	return GBPX_OK;
 }
 
@@ -1876,9 +2336,10 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		if(ms < bestMs) { bestMs = ms; best = c; }
 	}
 	const bool anySmall = std::any_of(sizes.begin(), sizes.end(), [&](uint32_t x) { return x <= best; });
-	for(uint32_t v = 0; v < gbpx::world::SOLVE_VARIANTS && !rc && anySmall; v++)
+	for(uint32_t v = 0; v <= gbpx::world::RESIDENT_VARIANT && !rc; v++)
 	{
-		if(v == bestVariant) continue;
+		// the staging variants only change the solve of scenes below the threshold
+		if(v == bestVariant || (v != gbpx::world::RESIDENT_VARIANT && !anySmall)) continue;
 		float ms = 0.0f;
 		rc = timeConfig(best, v, ms);
 		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
@@ -1896,16 +2357,17 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	return rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
 }
 
-// Workspace of the warp-per-scene solve kernel: variants 0-2 keep the body
-// velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
-// (2 is the default), variants 3-5 the same with the velocities left in HBM,
-// variants 6 / 7 stage 400 bytes per lane with the velocities on chip / in HBM.
-// A smaller workspace leaves room for more warps per SM.  Results do not depend
-// on it.
+// Solve kernel of the world.  8 (the default): the resident solve, every
+// scene's rows and velocities on chip for all iterations.  0-7: the
+// warp-per-scene solve, whose variants 0-2 keep the body velocities in shared
+// memory and stage rows in 0 / 256 / 512 bytes per lane, 3-5 the same with the
+// velocities left in HBM, 6 / 7 stage 400 bytes per lane with the velocities on
+// chip / in HBM (a smaller workspace leaves room for more warps per SM).
+// Results do not depend on it.
 GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant)
 {
 	World* w = static_cast<World*>(wv);
-	if(!w || variant >= gbpx::world::SOLVE_VARIANTS) return GBPX_ERR_INVALID;
+	if(!w || variant > gbpx::world::RESIDENT_VARIANT) return GBPX_ERR_INVALID;
 	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
 	w->params.solveVariant = variant;
 	if(w->graphExec)
@@ -2203,7 +2665,8 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.persistent = params[11] != 0.0f ? 1u : 0u;
 	sp.nbPos = iterations[0]; sp.nbVel = iterations[1];
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
-	sp.solveVariant = 2;   // velocities on chip, 512-byte staging
+	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
+	sp.resBytes = 0;       // set at creation
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);

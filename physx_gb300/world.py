@@ -134,6 +134,13 @@ class World:
         check(self._L.gbpx_world_stats(self._h, _p(out)), "gbpx_world_stats")
         return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]), row_bytes=int(out[3]))
 
+    def solve_profile(self):
+        """Per scene after the last step: constraints, partitions, packed row bytes and the
+        widest partition, as an (S, 4) uint32 array."""
+        out = np.zeros((self.info()["scenes"], 4), np.uint32)
+        check(self._L.gbpx_world_solve_profile(self._h, _p(out)), "gbpx_world_solve_profile")
+        return out
+
     def set_large_bodies(self, n):
         """Scenes of more than n solver bodies run one block per scene in the scene
         stages (warp per scene below); results do not depend on it."""
@@ -157,10 +164,11 @@ class World:
         return t.value, ms.value
 
     def set_solve_variant(self, v):
-        """Workspace of the warp-per-scene solve: 0-2 velocities in shared memory with
-        0 / 256 / 512 B of row staging per lane (2 default), 3-5 the same with the
-        velocities in HBM, 6 / 7 400 B with velocities on chip / in HBM.  Results
-        do not depend on it."""
+        """Solve kernel: 8 (default) the resident solve (each scene's rows and
+        velocities on chip for all iterations); 0-7 the warp-per-scene solve, whose
+        variants 0-2 keep velocities in shared memory with 0 / 256 / 512 B of row
+        staging per lane, 3-5 the same with the velocities in HBM, 6 / 7 400 B with
+        velocities on chip / in HBM.  Results do not depend on it."""
         check(self._L.gbpx_world_set_solve_variant(self._h, int(v)), "gbpx_world_set_solve_variant")
 
     def kind_counts(self):

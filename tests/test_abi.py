@@ -69,8 +69,31 @@ def test_immediate_library_exports_the_reference_entry_points(gbpx_built):
     text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gbpx_immediate.h")).read(), flags=re.S)
     block = text[text.index('extern "C"'):]
     declared = sorted(set(re.findall(r"\b(Px\w+)\s*\(", block)))
-    assert len(declared) == 7, declared
+    assert len(declared) == 12, declared
     lib = os.path.join(os.path.dirname(gbpx_built), "libgbpx_immediate.so")
     out = os.popen("nm -D --defined-only %s" % lib).read()
     exported = sorted(l.split()[-1] for l in out.splitlines() if " T " in l)
     assert exported == declared, (exported, declared)
+
+
+def test_broadphase_filter_groups_and_descriptor_checks(gbpx_built):
+    """PxGetBroadPhase{Static,Dynamic,Kinematic}FilterGroup give the reference's
+    groups (Bp::getFilterGroup_Statics / _Dynamics, BpFiltering.h:79-89: statics 0,
+    otherwise ((id + 1) << 3) | type with kinematic 1, dynamic 2), and
+    PxCreateBroadPhase returns NULL for a type it does not serve (no device work)."""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(gbpx_built), "libgbpx_immediate.so"))
+    for name in ("PxGetBroadPhaseStaticFilterGroup", "PxGetBroadPhaseDynamicFilterGroup", "PxGetBroadPhaseKinematicFilterGroup"):
+        getattr(lib, name).restype = ctypes.c_uint32
+    assert lib.PxGetBroadPhaseStaticFilterGroup() == 0
+    for i in (0, 1, 7, 123456):
+        assert lib.PxGetBroadPhaseDynamicFilterGroup(ctypes.c_uint32(i)) == ((i + 1) << 3) | 2
+        assert lib.PxGetBroadPhaseKinematicFilterGroup(ctypes.c_uint32(i)) == ((i + 1) << 3) | 1
+
+    class Desc(ctypes.Structure):   # PxBroadPhaseDesc
+        _fields_ = [("mType", ctypes.c_int), ("mContextID", ctypes.c_uint64), ("mContextManager", ctypes.c_void_p),
+                    ("mFoundLostPairsCapacity", ctypes.c_uint32), ("mDiscardStaticVsKinematic", ctypes.c_bool),
+                    ("mDiscardKinematicVsKinematic", ctypes.c_bool)]
+    lib.PxCreateBroadPhase.restype = ctypes.c_void_p
+    for t in (0, 1, 4, 5):   # eSAP, eMBP, eGPU, eLAST
+        assert lib.PxCreateBroadPhase(ctypes.byref(Desc(mType=t))) is None

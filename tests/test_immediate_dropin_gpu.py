@@ -127,3 +127,49 @@ def test_immediate_persistent_frames_match_oracle(cuda_device, tmp_path, seed):
         assert velocity_error(rigid_velocity(ref), rigid_velocity(got)) <= 1e-5, f
         assert np.abs(got["p"] - ref["p"]).max() <= 1e-6, f
     orc.release()
+
+
+def _bp_blob(mode, frames):
+    parts = [np.array([mode, len(frames)], np.uint32).tobytes()]
+    for fr in frames:
+        cap = int(fr["capacity"])
+        c, u, r = (np.ascontiguousarray(fr[k], np.uint32) for k in ("created", "updated", "removed"))
+        parts += [np.array([cap, len(c), len(u), len(r)], np.uint32).tobytes(), c.tobytes(), u.tobytes(), r.tobytes()]
+        bounds = np.zeros((cap + 1, 6), np.float32)
+        b = np.asarray(fr["bounds"], np.float32)
+        bounds[:min(len(b), cap + 1)] = b[:cap + 1]
+        parts += [bounds.tobytes(), np.ascontiguousarray(fr["groups"][:cap], np.uint32).tobytes(),
+                  np.ascontiguousarray(fr["distances"][:cap], np.float32).tobytes()]
+    return b"".join(parts)
+
+
+def _bp_results(out, nframes):
+    res, off = [], 0
+    for _ in range(nframes):
+        nc, nl = np.frombuffer(out[off:off + 8], np.uint32)
+        off += 8
+        created = np.frombuffer(out[off:off + 8 * nc], np.uint32).reshape(-1, 2)
+        off += 8 * nc
+        lost = np.frombuffer(out[off:off + 8 * nl], np.uint32).reshape(-1, 2)
+        off += 8 * nl
+        res.append((created, lost))
+    assert off == len(out)
+    return res
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["PxBroadPhase", "PxAABBManager"])
+@pytest.mark.parametrize("fixture", ["bp_dense.npz", "bp_sparse.npz"])
+def test_immediate_broadphase_matches_reference_golden(cuda_device, tmp_path, fixture, mode):
+    """tests/immediate_broadphase.cpp, written against PxBroadPhase.h, drives
+    PxCreateBroadPhase(eABP) update / fetchResults with its own arrays from the
+    broadphase's allocator (mode 0), or a PxAABBManager fed object by object
+    (mode 1): the created and lost pairs of every frame equal the reference
+    ABP's own (golden fixture), bit for bit."""
+    from scenarios import sorted_pairs
+    from test_oracle_golden import GOLDEN, load_bp_fixture
+    exe = _build(str(tmp_path), "immediate_broadphase")
+    frames = load_bp_fixture(os.path.join(GOLDEN, fixture))
+    out = subprocess.run([exe], input=_bp_blob(mode, frames), capture_output=True, check=True).stdout
+    for f, ((created, lost), fr) in enumerate(zip(_bp_results(out, len(frames)), frames)):
+        assert np.array_equal(created, sorted_pairs(fr["ref_created"])), "frame %d created" % f
+        assert np.array_equal(lost, sorted_pairs(fr["ref_lost"])), "frame %d lost" % f

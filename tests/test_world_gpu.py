@@ -224,23 +224,47 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
 
 
 def test_world_solve_staging_variants_equal(cuda_device):
-    """The warp-per-scene solve stages rows in 512 or 256 bytes per lane or uses
-    them in place, with the body velocities in shared memory or in HBM; the eight
-    variants give the same bytes."""
+    """The resident solve (variant 8: rows and velocities on chip for all
+    iterations) and the warp-per-scene solve, which stages rows in 512 or 256 bytes
+    per lane or uses them in place, with the body velocities in shared memory or
+    in HBM: the nine variants give the same bytes."""
     from physx_gb300.workloads import batched_scenes
     from physx_gb300.world import World
     scenes = batched_scenes(143, 48, nmin=16, nmax=500)
-    worlds = [World(scenes) for _ in range(8)]
+    worlds = [World(scenes) for _ in range(9)]
     for v, w in enumerate(worlds):
         w.set_solve_variant(v)
     for step in range(20):
         for w in worlds:
             w.step(1)
-    ref = worlds[2].get_bodies().tobytes()
+    ref = worlds[8].get_bodies().tobytes()
     for w in worlds:
         assert w.get_bodies().tobytes() == ref
+        assert not w.status().any()
     for w in worlds:
         w.release()
+
+
+def test_world_resident_solve_of_scenes_beyond_the_workspace(cuda_device):
+    """Scenes whose rows (and, above about 4500 solver bodies, velocities) do not fit
+    the resident solve's shared memory are solved with them in HBM: the same bytes
+    as the block-per-scene solve, persistent pair state on."""
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(147, 6, nmin=1500, nmax=6000)
+    assert scenes["body_count"].max() > 5000     # velocities of 5000+ bodies exceed the workspace
+    a, b = World(scenes), World(scenes)
+    a.set_solve_variant(8)
+    b.set_solve_variant(2)
+    for _ in range(90):
+        a.step(1)
+        b.step(1)
+    prof = a.solve_profile()
+    assert prof[:, 2].max() > 232448          # some scene's rows exceed the largest workspace
+    assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
+    assert not a.status().any() and not b.status().any()
+    a.release()
+    b.release()
 
 
 def test_world_full_size_batched_step_matches_oracle_sample(cuda_device):
