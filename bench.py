@@ -467,8 +467,9 @@ def main():
     #   batching     280 B per body (PxRigidBodyData in, solver body records out) + 12 B per constraint
     #   preparation  32 B per contact in + 2 x 184 B solver bodies per constraint + packed rows written;
     #                persistent mode adds per constraint a 16 B friction header + one 112 B patch read and written
-    #   solve        packed rows read once per iteration, plus per body 48 B velocities in, per position
-    #                iteration 176 B of integration state, 124 B write-back
+    #   solve        compulsory: packed rows read once (the resident solve keeps them on chip for all
+    #                iterations), plus per body 64 B velocities in, 64 B transform and inertia in,
+    #                28 B pose in, 52 B PxRigidBodyData fields written back
     st = w.stats()
     stage_ms = w.time_stages(max(3, a.steps // 3))
     kinds = w.kind_counts()
@@ -481,7 +482,7 @@ def main():
         "narrowphase": st["pairs"] * 108 + st["contacts"] * 32 + (st["pairs"] * 8 + cached_pairs * 576 if persistent else 0),
         "batching": bodies * 280 + st["constraints"] * 12,
         "row preparation": st["contacts"] * 32 + st["constraints"] * 368 + st["row_bytes"] + (st["constraints"] * 256 if persistent else 0),
-        "solve": (nbPos + nbVel) * st["row_bytes"] + bodies * (48 + nbPos * 176 + 124),
+        "solve": st["row_bytes"] + bodies * (64 + 64 + 28 + 52),
     }
     stage_time = {"broadphase": stage_ms["broadphase"], "narrowphase": np_ms, "batching": stage_ms["batching"],
                   "row preparation": stage_ms["row preparation"], "solve": stage_ms["solve"]}
@@ -502,8 +503,16 @@ def main():
     traffic = profiled_traffic(dominant)
     roofline = dict(bound="hbm", kernel=dominant, achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
                     traffic=traffic, peak_source=peak_kind, algorithmic_bytes_per_launch=dom_bytes, launch_ms=kernel_ms[dominant])
-    bytes_step = sum(stage_bytes.values())
-    step_roofline = dict(algorithmic_bytes_per_step=bytes_step, achieved=bytes_step / (ms / a.steps / 1000.0) / 1e9, unit="GB/s")
+    # the whole step's compulsory HBM bytes, per the scope's measurement model: broadphase
+    # 36 B per updated box + 28 B per box + 16 B per active pair; narrowphase 108 B per pair
+    # + 32 B per contact (+ 576 B per pair of a cached kind); per body 96 B in + 64 B out; per
+    # pair with contacts 208 B of friction patches read and written + 32 B per contact in.
+    # Rows are built and consumed on chip and do not count.
+    statics = info["statics"]
+    bytes_step = (36 * bodies + 28 * (bodies + statics) + 16 * st["pairs"] + st["pairs"] * 108 + st["contacts"] * 32 + cached_pairs * 576 +
+                  bodies * (96 + 64) + st["constraints"] * 208 + st["contacts"] * 32)
+    step_roofline = dict(algorithmic_bytes_per_step=bytes_step, achieved=bytes_step / (ms / a.steps / 1000.0) / 1e9, unit="GB/s",
+                         peak=peak, frac=bytes_step / (ms / a.steps / 1000.0) / 1e9 / peak)
     cpu = None
     if rank == 0:
         # the same sample of the world in the state the timed steps started from

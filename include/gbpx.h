@@ -39,6 +39,14 @@ int gbpx_set_device(int device);
  * kernels launched between these calls */
 int gbpx_profiler_start(void);
 int gbpx_profiler_stop(void);
+/* Profiler zones (the reference's PX_PROFILE_ZONE, physx/include/common/PxProfileZone.h,
+ * reported to a PxProfilerCallback, physx/include/foundation/PxProfiler.h:58-69):
+ * every stage of the library's calls is an NVTX range and, once installed here,
+ * a zoneStart / zoneEnd pair on these callbacks (zoneEnd gets zoneStart's return
+ * value).  Both null removes them; install while no library call runs. */
+typedef void* (*gbpx_zone_start_fn)(const char* name, int detached, uint64_t contextId, void* user);
+typedef void (*gbpx_zone_end_fn)(void* data, const char* name, int detached, uint64_t contextId, void* user);
+int gbpx_set_profiler_callback(gbpx_zone_start_fn zoneStart, gbpx_zone_end_fn zoneEnd, void* user);
 
 /* ---------------------------------------------------------------- broadphase
  * ABP-compatible broadphase.  Replaces:

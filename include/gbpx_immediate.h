@@ -14,6 +14,8 @@
  *   PxGetBroadPhaseKinematicFilterGroup  physx/include/PxBroadPhase.h:291
  *   PxCreateBroadPhase                   physx/include/PxBroadPhase.h:629
  *   PxCreateAABBManager                  physx/include/PxBroadPhase.h:796
+ *   PxSetProfilerCallback                physx/include/foundation/PxFoundation.h:195
+ *   PxGetProfilerCallback                physx/include/foundation/PxFoundation.h:190
  *
  * The reference declares these PX_C_EXPORT (extern "C"), so a program built
  * against the reference's headers links them from this library instead.  This
@@ -44,7 +46,9 @@
  * single-threaded in the reference too); getAllocator() hands out page-locked
  * host memory, from which bounds reach the device fastest.  PxCreateAABBManager
  * wraps such a broadphase with the reference's object bookkeeping (one manager
- * per broadphase).
+ * per broadphase).  A PxProfilerCallback installed with PxSetProfilerCallback
+ * receives a zone for every stage of the library's work (the reference reports
+ * its PX_PROFILE_ZONEs the same way).
  */
 #ifndef GBPX_IMMEDIATE_H
 #define GBPX_IMMEDIATE_H
@@ -208,6 +212,19 @@ public:
 	virtual ~PxConstraintAllocator() {}
 };
 
+// The reference's profiler callback (physx/include/foundation/PxProfiler.h:40-110),
+// same virtual functions in the same order.
+class PxProfilerCallback
+{
+public:
+	virtual ~PxProfilerCallback() {}
+	virtual void* zoneStart(const char* eventName, bool detached, uint64_t contextId) = 0;
+	virtual void zoneEnd(void* profilerData, const char* eventName, bool detached, uint64_t contextId) = 0;
+	virtual void recordData(int32_t value, const char* valueName, uint64_t contextId) { (void)value; (void)valueName; (void)contextId; }
+	virtual void recordData(float value, const char* valueName, uint64_t contextId) { (void)value; (void)valueName; (void)contextId; }
+	virtual void recordFrame(const char* name, uint64_t contextId) { (void)name; (void)contextId; }
+};
+
 // ---- low- and high-level broadphase (physx/include/PxBroadPhase.h) ----
 struct PxBounds3 { PxVec3 minimum, maximum; };
 struct PxBroadPhaseType { enum Enum { eSAP, eMBP, eABP, ePABP, eGPU, eLAST }; };
@@ -355,6 +372,8 @@ gbpx_px::PxBpFilterGroup PxGetBroadPhaseDynamicFilterGroup(uint32_t id);
 gbpx_px::PxBpFilterGroup PxGetBroadPhaseKinematicFilterGroup(uint32_t id);
 gbpx_px::PxBroadPhase* PxCreateBroadPhase(const gbpx_px::PxBroadPhaseDesc& desc);
 gbpx_px::PxAABBManager* PxCreateAABBManager(gbpx_px::PxBroadPhase& broadphase);
+void PxSetProfilerCallback(gbpx_px::PxProfilerCallback* profiler);
+gbpx_px::PxProfilerCallback* PxGetProfilerCallback();
 }
 
 #endif /* GBPX_IMMEDIATE_H */

@@ -806,6 +806,7 @@ GBPX_API int gbpx_bp_update(void* bp, const uint32_t* created, uint32_t nbCreate
                             const uint32_t* removed, uint32_t nbRemoved, const float* bounds, const uint32_t* groups,
                             const float* distances, uint32_t capacity)
 {
+	gbpx::Zone zone("gbpx::bp::update");
 	if(!bp) return GBPX_ERR_INVALID;
 	return static_cast<BroadPhase*>(bp)->update(created, nbCreated, updated, nbUpdated, removed, nbRemoved, bounds, groups, distances,
 	                                            capacity);
@@ -813,6 +814,7 @@ GBPX_API int gbpx_bp_update(void* bp, const uint32_t* created, uint32_t nbCreate
 
 GBPX_API int gbpx_bp_fetch_results(void* bp, const uint32_t** created, uint32_t* nbCreated, const uint32_t** lost, uint32_t* nbLost)
 {
+	gbpx::Zone zone("gbpx::bp::fetchResults");
 	if(!bp || !created || !nbCreated || !lost || !nbLost) return GBPX_ERR_INVALID;
 	const uint2 *c = nullptr, *l = nullptr;
 	const int rc = static_cast<BroadPhase*>(bp)->fetchResults(&c, nbCreated, &l, nbLost);

@@ -34,6 +34,39 @@ namespace gbpx
 {
 static inline uint32_t divUp(uint64_t a, uint32_t b) { return uint32_t((a + b - 1) / b); }
 
+// Profiler zones, as the reference marks its stages with PX_PROFILE_ZONE
+// (physx/include/common/PxProfileZone.h): each zone is an NVTX range (seen by
+// Nsight tools) and, when the user installed callbacks with
+// gbpx_set_profiler_callback, a zoneStart / zoneEnd pair on them.  Zones are
+// host-side: they bracket the launches and copies of a stage.
+typedef void* (*ZoneStartFn)(const char* name, int detached, uint64_t contextId, void* user);
+typedef void (*ZoneEndFn)(void* data, const char* name, int detached, uint64_t contextId, void* user);
+void zoneCallbacks(ZoneStartFn* start, ZoneEndFn* end, void** user);
+void nvtxPush(const char* name);
+void nvtxPop();
+struct Zone
+{
+	const char* name;
+	uint64_t context;
+	void* data = nullptr;
+	ZoneStartFn start = nullptr;
+	ZoneEndFn end = nullptr;
+	void* user = nullptr;
+	Zone(const char* n, uint64_t ctx = 0) : name(n), context(ctx)
+	{
+		nvtxPush(n);
+		zoneCallbacks(&start, &end, &user);
+		if(start) data = start(n, 0, ctx, user);
+	}
+	~Zone()
+	{
+		if(end) end(data, name, 0, context, user);
+		nvtxPop();
+	}
+	Zone(const Zone&) = delete;
+	Zone& operator=(const Zone&) = delete;
+};
+
 // Device buffer that only grows; contents are not preserved across growth unless asked.
 template <typename T>
 struct DevBuf

@@ -648,3 +648,28 @@ GX PxAABBManager* PxCreateAABBManager(PxBroadPhase& broadphase)
 	if(bp.manager) return nullptr;   // one manager per broadphase
 	return new GbpxAABBManager(bp);
 }
+
+// ------------------------------------------------------------------ profiler
+// PxSetProfilerCallback (physx/include/foundation/PxFoundation.h:195): the
+// library's profiler zones go to the user's PxProfilerCallback.
+namespace
+{
+PxProfilerCallback* gProfiler = nullptr;
+void* profZoneStart(const char* name, int detached, uint64_t context, void* user)
+{
+	return static_cast<PxProfilerCallback*>(user)->zoneStart(name, detached != 0, context);
+}
+void profZoneEnd(void* data, const char* name, int detached, uint64_t context, void* user)
+{
+	static_cast<PxProfilerCallback*>(user)->zoneEnd(data, name, detached != 0, context);
+}
+} // namespace
+
+GX void PxSetProfilerCallback(PxProfilerCallback* profiler)
+{
+	gProfiler = profiler;
+	if(profiler) gbpx_set_profiler_callback(profZoneStart, profZoneEnd, profiler);
+	else gbpx_set_profiler_callback(nullptr, nullptr, nullptr);
+}
+
+GX PxProfilerCallback* PxGetProfilerCallback() { return gProfiler; }

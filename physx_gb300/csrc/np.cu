@@ -189,6 +189,7 @@ GBPX_API int gbpx_generate_contacts(const int* type0, const float* geom0, const 
                                     const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
                                     float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts)
 {
+	gbpx::Zone zone("gbpx::generateContacts");
 	(void)meshContactMargin;
 	return generateContactsHost(type0, geom0, type1, geom1, pose0, pose1, nbPairs, contactDistance, toleranceLength, outContacts, maxPerPair,
 	                            outCounts, nullptr);
@@ -202,6 +203,7 @@ GBPX_API int gbpx_generate_contacts_cached(const int* type0, const float* geom0,
                                            const float* pose1, uint32_t nbPairs, float contactDistance, float meshContactMargin,
                                            float toleranceLength, float* outContacts, uint32_t maxPerPair, uint32_t* outCounts, void* manifolds)
 {
+	gbpx::Zone zone("gbpx::generateContacts");
 	(void)meshContactMargin;
 	if(nbPairs && !manifolds) return GBPX_ERR_INVALID;
 	return generateContactsHost(type0, geom0, type1, geom1, pose0, pose1, nbPairs, contactDistance, toleranceLength, outContacts, maxPerPair,
@@ -264,6 +266,7 @@ GBPX_API int gbpx_generate_contacts_device_noalloc(const int* dType0, const floa
                                                    const float* dPose0, const float* dPose1, uint32_t nbPairs, float contactDistance,
                                                    float toleranceLength, float* dOutContacts, uint32_t* dOutCounts, void* stream)
 {
+	gbpx::Zone zone("gbpx::generateContacts");
 	if(!nbPairs) return GBPX_OK;
 	if(!dType0 || !dGeom0 || !dType1 || !dGeom1 || !dPose0 || !dPose1 || !dOutContacts || !dOutCounts) return GBPX_ERR_INVALID;
 	if(!(contactDistance > 0.0f) || !(toleranceLength > 0.0f)) return GBPX_ERR_INVALID;

@@ -20,6 +20,7 @@
 //      iteration, PxIntegrateSolverBodiesTGS and write-back.
 // Arithmetic is the world's: the same device functions, the same order.
 #include "common.cuh"
+#include <optional>
 #include "contacts.cuh"
 #include "solver.cuh"
 #include "step_common.cuh"
@@ -510,13 +511,20 @@ struct Scene
 		return GBPX_OK;
 	}
 
+	// host-side profiler zone of the stage in progress (closed by the next mark)
+	std::optional<Zone> stageZone;
 	void mark(uint32_t k)
 	{
+		static const char* const names[STAGES] = {"gbpx::scene::broadphase", "gbpx::scene::narrowphase", "gbpx::scene::batching",
+		                                          "gbpx::scene::rows", "gbpx::scene::iterations", "gbpx::scene::writeBack"};
 		if(timing) cudaEventRecord(ev[k], stream);
+		stageZone.reset();
+		if(k < STAGES) stageZone.emplace(names[k]);
 	}
 
 	int step()
 	{
+		struct CloseZone { std::optional<Zone>& z; ~CloseZone() { z.reset(); } } closeZone{stageZone};
 		const SceneDev d = dev();
 		mark(0);
 		// 1. bounds + broadphase; last frame's pair list is kept for the slot lookup
@@ -691,6 +699,7 @@ GBPX_API void gbpx_scene_release(void* sv)
 // Advances the scene by nbSteps frames (returns when the last has finished).
 GBPX_API int gbpx_scene_step(void* sv, uint32_t nbSteps)
 {
+	gbpx::Zone zone("gbpx::scene::step");
 	Scene* s = static_cast<Scene*>(sv);
 	if(!s) return GBPX_ERR_INVALID;
 	for(uint32_t k = 0; k < nbSteps; k++)
@@ -746,6 +755,7 @@ GBPX_API int gbpx_scene_time_steps(void* sv, uint32_t nbSteps, float* outMs)
 // outMs = event-timed milliseconds of the whole call on the scene's stream.
 GBPX_API int gbpx_scene_step_host(void* sv, const void* rigidIn, void* rigidOut, uint32_t nbSteps, float* outMs)
 {
+	gbpx::Zone zone("gbpx::scene::stepHost");
 	Scene* s = static_cast<Scene*>(sv);
 	if(!s || !rigidIn || !rigidOut || !outMs) return GBPX_ERR_INVALID;
 	const size_t bytes = size_t(s->nbDyn) * sizeof(gbpx::tgs::RigidBody);

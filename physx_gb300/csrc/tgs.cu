@@ -348,6 +348,7 @@ GBPX_API uint32_t gbpx_batch_constraints_tgs(const uint32_t* bodyA, const uint32
 GBPX_API int gbpx_construct_solver_bodies_tgs(const void* rigid, uint32_t nb, const float* gravity, float dt, void* outVel, void* outTxI,
                                               void* outData)
 {
+	gbpx::Zone zone("gbpx::constructSolverBodiesTGS");
 	if(!nb) return GBPX_OK;
 	if(!rigid || !gravity || !outVel || !outTxI || !outData) return GBPX_ERR_INVALID;
 	TgsWorkspace* ws = tgsWorkspace();
@@ -382,6 +383,7 @@ GBPX_API int gbpx_tgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
                                  float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, float* outVel, float* outPose,
                                  uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder, uint32_t* outNbHeaders)
 {
+	gbpx::Zone zone("gbpx::tgsSolve");
 	if(!nbDyn || !rigid || !gravity || !outVel || !outPose || !outNbHeaders || !(dt > 0.0f) || !nbPos || !nbVel) return GBPX_ERR_INVALID;
 	if(nbConstraints && (!pairA || !pairB || !contactStart || !contactCount || !contacts || !material || !outHeaderStart || !outHeaderStride || !outOrder))
 		return GBPX_ERR_INVALID;
@@ -525,6 +527,7 @@ GBPX_API uint32_t gbpx_constraint_row_stride(void)
 // PxConstructStaticSolverBodyTGS for n poses (PxTransform in, reference solver-body layouts out).
 GBPX_API int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void* outVel, void* outTxI, void* outData)
 {
+	gbpx::Zone zone("gbpx::constructStaticSolverBodiesTGS");
 	if(!n) return GBPX_OK;
 	if(!poses || !outVel || !outTxI || !outData) return GBPX_ERR_INVALID;
 	TgsStageWorkspace* ws = tgsStageWorkspace();
@@ -562,6 +565,7 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
                                                  const void* frictionIn, void* frictionOut, float invDt, float invTotalDt, float bounceThreshold,
                                                  float frictionOffsetThreshold, float correlationDistance, void* outRows, uint32_t* outRowBytes)
 {
+	gbpx::Zone zone("gbpx::createContactConstraintsTGS");
 	if(!n) return GBPX_OK;
 	if(!vel0 || !vel1 || !txI0 || !txI1 || !data0 || !data1 || !frame0 || !frame1 || !contactStart || !contactCount || !outRows || !outRowBytes ||
 	   (nbPoints && !contactPoints) || !(invDt > 0.0f) || !(invTotalDt > 0.0f))
@@ -624,6 +628,7 @@ GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const
                                         void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
                                         uint32_t* outBroken)
 {
+	gbpx::Zone zone("gbpx::solveConstraintsTGS");
 	if(!bodyVel || !bodyTxI || !nbBodies || nbIntegrate > nbBodies || !nbPos || !(dt > 0.0f)) return GBPX_ERR_INVALID;
 	if(n && (!rows || !bodyA || !bodyB || !waveEnds || !nbWaves || waveEnds[nbWaves - 1] != n)) return GBPX_ERR_INVALID;
 	for(uint32_t k = 0; k < n; k++)
@@ -675,6 +680,7 @@ GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const
 // velocity records, poses (PxTransform) updated in place.
 GBPX_API int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* poses, uint32_t n)
 {
+	gbpx::Zone zone("gbpx::integrateSolverBodiesTGS");
 	if(!n) return GBPX_OK;
 	if(!bodyVel || !bodyTxI || !poses) return GBPX_ERR_INVALID;
 	TgsStageWorkspace* ws = tgsStageWorkspace();

@@ -15,7 +15,9 @@
 //   4. row preparation: a thread per constraint;
 //   5. solve: position iterations with per-substep integration and the velocity
 //      iteration, partition by partition (constraints of one partition touch
-//      disjoint bodies), then PxIntegrateSolverBodiesTGS and write-back.
+//      disjoint bodies), then PxIntegrateSolverBodiesTGS and write-back; by
+//      default the resident solve, which bulk-copies each scene's rows and
+//      velocities into shared memory once and runs every iteration there.
 // All scene state stays resident in HBM.
 //
 // The step is the reference immediate-mode snippet's frame (physx/snippets/
@@ -50,8 +52,8 @@ enum : uint32_t { ST_PAIR_OVERFLOW = 1, ST_PARTITION_OVERFLOW = 2, ST_STAGE_TIME
 // iterations.  Scenes are filed by on-chip footprint into RES_LEVELS levels:
 // at level L the block works as 2^L groups of RES_WARPS >> L warps, each group
 // solving one scene at a time in 1/2^L of the workspace.
-constexpr uint32_t RES_WARPS = 8;
-constexpr uint32_t RES_LEVELS = 4;
+constexpr uint32_t RES_WARPS = 16;
+constexpr uint32_t RES_LEVELS = 5;
 static_assert((RES_WARPS >> (RES_LEVELS - 1)) >= 1 && RES_WARPS <= 16, "levels down to one warp; named barriers 1..RES_WARPS-1");
 constexpr uint32_t RES_HEADER = MAX_PARTITIONS * 4;   // partition ends at the start of a group's slice
 // work counters (after the per-kind pair counts and path counts): scenes filed
@@ -1781,6 +1783,7 @@ struct World
 			return e != cudaSuccess ? e : cudaStreamWaitEvent(stream, joinEv[k], 0);
 		};
 		const cudaStream_t bigStream = plain ? stream : sideStream;
+		Zone zone(plain ? "gbpx::world::launchPlainStep" : "gbpx::world::launchStep");
 		GBPX_CUDA_TRY(cudaMemsetAsync(workCounter.ptr, 0, COUNTERS * 4, stream));
 		if(big && !plain) GBPX_CUDA_TRY(fork(0));
 		world::broadphaseKernel<<<gBp, threads, bpSmemBytes(threads / 32), stream>>>(w, params);
@@ -2026,6 +2029,7 @@ GBPX_API void gbpx_world_release(void* w)
 // HBM).  useGraph replays a captured CUDA graph of one step.
 GBPX_API int gbpx_world_step(void* w, uint32_t nbSteps, int useGraph)
 {
+	gbpx::Zone zone("gbpx::world::step");
 	if(!w) return GBPX_ERR_INVALID;
 	return static_cast<World*>(w)->step(nbSteps, useGraph != 0);
 }
@@ -2407,6 +2411,7 @@ GBPX_API int gbpx_world_time_stages(void* wv, uint32_t nbSteps, float* outMs)
 // around the copies and the step.
 GBPX_API int gbpx_world_step_host(void* wv, const void* rigidIn, void* rigidOut, uint32_t nbSteps, int useGraph, float* outMs)
 {
+	gbpx::Zone zone("gbpx::world::stepHost");
 	World* w = static_cast<World*>(wv);
 	if(!w || !rigidIn || !rigidOut) return GBPX_ERR_INVALID;
 	if(useGraph && (!w->graphExec || w->graphSteps != 1))

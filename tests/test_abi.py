@@ -69,7 +69,7 @@ def test_immediate_library_exports_the_reference_entry_points(gbpx_built):
     text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gbpx_immediate.h")).read(), flags=re.S)
     block = text[text.index('extern "C"'):]
     declared = sorted(set(re.findall(r"\b(Px\w+)\s*\(", block)))
-    assert len(declared) == 12, declared
+    assert len(declared) == 14, declared
     lib = os.path.join(os.path.dirname(gbpx_built), "libgbpx_immediate.so")
     out = os.popen("nm -D --defined-only %s" % lib).read()
     exported = sorted(l.split()[-1] for l in out.splitlines() if " T " in l)
@@ -97,3 +97,32 @@ def test_broadphase_filter_groups_and_descriptor_checks(gbpx_built):
     lib.PxCreateBroadPhase.restype = ctypes.c_void_p
     for t in (0, 1, 4, 5):   # eSAP, eMBP, eGPU, eLAST
         assert lib.PxCreateBroadPhase(ctypes.byref(Desc(mType=t))) is None
+
+
+def test_profiler_zone_callbacks(gbpx_built):
+    """gbpx_set_profiler_callback: every library call opens a zone, reported to the
+    user's zoneStart / zoneEnd pair (the PxProfilerCallback protocol: zoneEnd gets
+    zoneStart's return value).  An invalid call still reports its zone, so no GPU
+    is needed here."""
+    import ctypes
+    from physx_gb300 import lib
+    L = lib()
+    events = []
+    START = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p)
+    END = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p)
+
+    def start(name, detached, ctx, user):
+        events.append(("start", name.decode()))
+        return 1234
+
+    def end(data, name, detached, ctx, user):
+        events.append(("end", name.decode(), data))
+
+    s_cb, e_cb = START(start), END(end)
+    L.gbpx_set_profiler_callback.argtypes = [START, END, ctypes.c_void_p]
+    assert L.gbpx_set_profiler_callback(s_cb, e_cb, None) == 0
+    L.gbpx_bp_update.argtypes = [ctypes.c_void_p] * 11
+    assert L.gbpx_bp_update(None, None, 0, None, 0, None, 0, None, None, None, 0) == -1
+    assert L.gbpx_set_profiler_callback(START(), END(), None) == 0   # removed
+    assert L.gbpx_bp_update(None, None, 0, None, 0, None, 0, None, None, None, 0) == -1
+    assert events == [("start", "gbpx::bp::update"), ("end", "gbpx::bp::update", 1234)]

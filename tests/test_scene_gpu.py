@@ -99,3 +99,30 @@ def test_scene_100k_bodies_step_matches_oracle(cuda_device):
     assert velocity_error(rigid_velocity(ref), rigid_velocity(out)) <= 1e-5
     assert np.abs(out["p"] - ref["p"]).max() <= 1e-6
     s.release()
+
+
+def test_scene_stage_profiler_zones(cuda_device):
+    """A frame of the large-scene step reports each stage as a profiler zone, in
+    order, between the step's own zone (the reference's PX_PROFILE_ZONE protocol)."""
+    import ctypes
+    from physx_gb300 import lib
+    from physx_gb300.scene import Scene
+    L = lib()
+    names = []
+    START = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p)
+    END = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p)
+    s_cb = START(lambda n, d, c, u: names.append(n.decode()) or None)
+    e_cb = END(lambda p, n, d, c, u: None)
+    L.gbpx_set_profiler_callback.argtypes = [START, END, ctypes.c_void_p]
+    s = Scene(_pile(135, 300))
+    s.step(1)
+    assert L.gbpx_set_profiler_callback(s_cb, e_cb, None) == 0
+    try:
+        s.step(1)
+    finally:
+        L.gbpx_set_profiler_callback(START(), END(), None)
+    s.release()
+    stages = [n for n in names if n.startswith("gbpx::scene::") and n != "gbpx::scene::step"]
+    assert names[0] == "gbpx::scene::step"
+    assert stages == ["gbpx::scene::broadphase", "gbpx::scene::narrowphase", "gbpx::scene::batching", "gbpx::scene::rows",
+                      "gbpx::scene::iterations", "gbpx::scene::writeBack"], names

@@ -294,3 +294,40 @@ def test_world_full_size_batched_step_matches_oracle_sample(cuda_device):
     assert velocity_error(rigid_velocity(ref), rigid_velocity(got)) <= 1e-5
     assert np.abs(got["p"] - ref["p"]).max() <= 1e-6
     w.release()
+
+
+def test_world_full_size_persistent_steps_match_oracle_sample(cuda_device):
+    """The benchmarked configuration at full size: 4096 scenes (log-uniform [8,512]
+    bodies, about 0.5M), persistent pair state, graph-replayed steps, resident
+    solve.  A 48-scene size-stratified sample is stepped by the oracle's persistent
+    frame in lockstep (each side keeps its own contact caches and friction data;
+    the oracle's bodies are set to the world's after every step, so last-ulp sin/cos
+    differences cannot grow); after 40 steps of pre-roll, 3 consecutive steps are
+    held to the per-step bar (velocities 1e-5 relative, poses 1e-6)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from bench import split_scenes
+    from oracle_libs import PersistentScenes
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import DEFAULT_PARAMS
+    scenes = batched_scenes(4, 4096)
+    w = _world(scenes)
+    counts = scenes["body_count"].astype(np.int64)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    idx = np.argsort(counts)[np.linspace(0, len(counts) - 1, 48).astype(np.int64)]
+    sel = np.concatenate([np.arange(starts[i], starts[i] + counts[i]) for i in idx])
+    orc = PersistentScenes("orc", split_scenes(scenes, idx), DEFAULT_PARAMS)
+    for step in range(43):
+        w.step(1, graph=True)
+        out = w.get_bodies()
+        got = out[sel]
+        ref = orc.step().copy()
+        orc.rb[:] = got
+        if step >= 40:
+            assert velocity_error(rigid_velocity(ref), rigid_velocity(got)) <= 1e-5, step
+            assert np.abs(got["p"] - ref["p"]).max() <= 1e-6, step
+            assert np.abs(got["q"] - ref["q"]).max() <= 1e-6, step
+    assert not w.status().any()
+    orc.release()
+    w.release()
