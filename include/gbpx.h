@@ -232,6 +232,11 @@ int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint
  * workspace leaves room for more warps per SM).  Results do not depend
  * on it.  The autotuner sets it after the threshold. */
 int gbpx_world_set_solve_variant(void* world, uint32_t variant);
+/* Persistent blocks per SM of the row preparation and of the capsule-box and
+ * box-box narrowphase kernels (0 = as many as fit, the default): their threads
+ * keep large working sets in local memory, and fewer threads in flight keep it
+ * in L1 / L2.  Results do not depend on it. */
+int gbpx_world_set_occupancy(void* world, uint32_t prepBlocksPerSm, uint32_t narrowphaseBlocksPerSm);
 /* Pairs of each pair kind in the last step, in the kind order of the
  * narrowphase launches (sphere-sphere ... box-box): 9 counts. */
 int gbpx_world_kind_counts(void* world, uint32_t* out9);

@@ -1534,6 +1534,13 @@ struct World
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve[world::SOLVE_VARIANTS] = {}, gridNp[world::NB_KINDS] = {};
 	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0, gridRes = 0;
 	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
+	// persistent blocks per SM of the row preparation and of the capsule-box and
+	// box-box narrowphase kernels (0: as many as fit).  Their threads keep large
+	// per-thread working sets in local memory (friction correlation, GJK/EPA), and
+	// fewer threads in flight keep that memory in L1 / L2 instead of HBM.
+	uint32_t sms = 0, prepPerSm = 0, npHeavyPerSm = 0;
+	uint32_t prepGrid() const { return prepPerSm ? std::min(gridPrep, sms * prepPerSm) : gridPrep; }
+	uint32_t npGrid(uint32_t k) const { return (k == 7 || k == 8) && npHeavyPerSm ? std::min(gridNp[k], sms * npHeavyPerSm) : gridNp[k]; }
 	uint32_t pairsPerBody = 0;
 	// scenes above this many solver bodies run one block per scene (warp per scene below)
 	static constexpr uint32_t DEFAULT_LARGE_BODIES = 512;
@@ -1688,6 +1695,7 @@ struct World
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solveSmemBytes(world::STAGE_WARPS))));
 		GBPX_CUDA_TRY(gridFor(world::batchKernel, sms, gridBatch, solveSmemBytes(world::STAGE_WARPS)));
 		GBPX_CUDA_TRY(gridFor(world::prepKernel, sms, gridPrep));
+		this->sms = uint32_t(sms);
 		for(uint32_t v = 0; v < world::SOLVE_VARIANTS; v++)
 		{
 			GBPX_CUDA_TRY(cudaFuncSetAttribute(solveKernels()[v], cudaFuncAttributeMaxDynamicSharedMemorySize, int(iterSmemBytes(world::SOLVE_WARPS, v))));
@@ -1761,7 +1769,7 @@ struct World
 	{
 		world::WorldDev w = dev();
 		const uint32_t sv = params.solveVariant;
-		uint32_t gBp = gridBlocks, gBatch = gridBatch, gPrep = gridPrep, gSolve = gridSolve[sv], threads = 128;
+		uint32_t gBp = gridBlocks, gBatch = gridBatch, gPrep = prepGrid(), gSolve = gridSolve[sv], threads = 128;
 		const bool plain = plainScene < nbScenes;
 		if(plain)
 		{
@@ -1795,7 +1803,7 @@ struct World
 		for(uint32_t k = 0; k < world::NB_KINDS; k++)
 		{
 			if(k == 7 && params.persistent) world::orderByPathKernel<<<plain ? std::min(gridOrder, 8u) : gridOrder, 128, 0, stream>>>(w, params);
-			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : gridNp[k], 128, 0, stream>>>(w, params);
+			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : npGrid(k), 128, 0, stream>>>(w, params);
 		}
 		if(big && !plain) GBPX_CUDA_TRY(fork(1));
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
@@ -1881,13 +1889,13 @@ struct World
 			for(uint32_t t = 0; t < world::NB_KINDS; t++)
 			{
 				if(t == 7 && params.persistent) world::orderByPathKernel<<<gridOrder, 128, 0, stream>>>(w, params);
-				npKernels()[t]<<<gridNp[t], 128, 0, stream>>>(w, params);
+				npKernels()[t]<<<npGrid(t), 128, 0, stream>>>(w, params);
 				GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			}
 			world::batchKernel<<<gridBatch, 128, solveSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
 			if(big) world::batchBigKernel<<<gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
-			world::prepKernel<<<gridPrep, 128, 0, stream>>>(w, params);
+			world::prepKernel<<<prepGrid(), 128, 0, stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			if(resident()) world::solveResidentKernel<<<gridRes, RES_THREADS, params.resBytes, stream>>>(w, params);
 			else
@@ -2215,6 +2223,25 @@ GBPX_API int gbpx_world_set_large_bodies(void* wv, uint32_t largeBodies)
 }
 
 GBPX_API int gbpx_world_set_solve_variant(void* wv, uint32_t variant);
+
+// Persistent blocks per SM of the row preparation and of the capsule-box and
+// box-box narrowphase kernels (0: as many as fit, the default).  Their threads
+// keep large working sets in local memory; fewer in flight keeps it on chip.
+// Results do not depend on it.
+GBPX_API int gbpx_world_set_occupancy(void* wv, uint32_t prepBlocksPerSm, uint32_t narrowphaseBlocksPerSm)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	w->prepPerSm = prepBlocksPerSm;
+	w->npHeavyPerSm = narrowphaseBlocksPerSm;
+	if(w->graphExec)
+	{
+		cudaGraphExecDestroy(w->graphExec);
+		w->graphExec = nullptr;
+	}
+	return GBPX_OK;
+}
 
 // ---- Autotuner of the block-per-scene threshold and the solve staging slot ----
 // The scene stages run warp-per-scene or block-per-scene kernels by scene size

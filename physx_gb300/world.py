@@ -163,6 +163,12 @@ class World:
         self.solve_variant = v.value
         return t.value, ms.value
 
+    def set_occupancy(self, prep_blocks_per_sm=0, narrowphase_blocks_per_sm=0):
+        """Persistent blocks per SM of the row preparation and of the capsule-box and
+        box-box narrowphase kernels (0 = as many as fit); results do not depend on it."""
+        self._L.gbpx_world_set_occupancy.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]
+        check(self._L.gbpx_world_set_occupancy(self._h, int(prep_blocks_per_sm), int(narrowphase_blocks_per_sm)), "gbpx_world_set_occupancy")
+
     def set_solve_variant(self, v):
         """Solve kernel: 8 (default) the resident solve (each scene's rows and
         velocities on chip for all iterations); 0-7 the warp-per-scene solve, whose

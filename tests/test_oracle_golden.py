@@ -284,3 +284,14 @@ def sys_path_root():
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     if root not in sys.path:
         sys.path.insert(0, root)
+
+
+def test_oracle_large_scene_trace_equals_reference():
+    """The oracle's 600-step trace of the 100k-body single-scene workload
+    (tests/golden/make_large_trace.py run with the oracle) is the reference's,
+    statistic for statistic: the restatement is pinned on the large-scene frame
+    as well as on the small fixtures."""
+    ref = np.load(os.path.join(GOLDEN, "large_scene_trace.npz"))
+    orc = np.load(os.path.join(GOLDEN, "large_scene_trace_orc.npz"))
+    assert int(ref["checksum"]) == int(orc["checksum"])
+    assert np.array_equal(ref["stats"], orc["stats"])

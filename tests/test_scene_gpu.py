@@ -2,7 +2,10 @@
 over one scene with every stage spread over the GPU, the ABP broadphase of
 gbpx_bp, PxBatchConstraintsTGS on the host.  Checked against the batched world
 (the same arithmetic: identical bytes), against the CPU oracle frame by frame
-(persistent and fresh), and at the full 100k-body size against one oracle frame."""
+(persistent and fresh), at the full 100k-body size against one oracle frame, and
+over the full 600-step run on physical statistics against the reference's trace."""
+import os
+
 import numpy as np
 import pytest
 
@@ -126,3 +129,46 @@ def test_scene_stage_profiler_zones(cuda_device):
     assert names[0] == "gbpx::scene::step"
     assert stages == ["gbpx::scene::broadphase", "gbpx::scene::narrowphase", "gbpx::scene::batching", "gbpx::scene::rows",
                       "gbpx::scene::iterations", "gbpx::scene::writeBack"], names
+
+
+LARGE_TRACE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "large_scene_trace.npz")
+
+
+def test_scene_100k_bodies_600_steps_statistics_match_reference(cuda_device):
+    """The single-large-scene workload over its full 600 steps (persistent pair
+    state), against the reference's own 600-step trace (tests/golden/
+    large_scene_trace.npz, made by tests/golden/make_large_trace.py with the
+    reference build).  Bodies separate chaotically after a few hundred steps, so
+    the check is on physical statistics, with these bounds:
+
+    * kinetic energy within 1 % of the reference's at every one of the first 300
+      steps (free fall and the first impacts), time-averaged within 2 %, peak within 1 %;
+    * deepest ground penetration over the run at most 1.25 x the reference's + 1 cm;
+      settled penetration (mean of the last 50 steps) within 3 cm of the reference's;
+    * settled pile height (mean body height at the end) within 2 %;
+    * fraction of bodies at rest at the end within 0.02."""
+    from physx_gb300.scene import Scene
+    from physx_gb300.workloads import large_scene
+    from trace_stats import FIELDS, body_checksum, step_stats
+    ref = np.load(LARGE_TRACE)
+    R = ref["stats"]
+    assert list(ref["fields"]) == list(FIELDS)
+    sc = large_scene()
+    assert body_checksum(sc["rigid"]) == int(ref["checksum"]), "the workload generator changed"
+    s = Scene(sc)
+    rows = []
+    for _ in range(int(ref["steps"])):
+        s.step(1)
+        st = step_stats(s.get_bodies(), sc["types"], sc["geoms"])
+        rows.append([st[f] for f in FIELDS])
+    s.release()
+    G = np.array(rows)
+    ke_r, ke_g = R[:, 0], G[:, 0]
+    assert (np.abs(ke_g[:300] - ke_r[:300]) / ke_r[:300]).max() <= 0.01
+    assert abs(ke_g.mean() - ke_r.mean()) <= 0.02 * ke_r.mean()
+    assert abs(ke_g.max() - ke_r.max()) <= 0.01 * ke_r.max()
+    assert -G[:, 1].min() <= 1.25 * -R[:, 1].min() + 0.01
+    assert abs(G[-50:, 1].mean() - R[-50:, 1].mean()) <= 0.03
+    assert abs(G[-1, 2] - R[-1, 2]) <= 0.02 * R[-1, 2]
+    assert abs(G[-1, 4] - R[-1, 4]) <= 0.02
+    assert np.isfinite(G).all()
