@@ -314,7 +314,7 @@ def bench_large_scene(steps, cpu_frames):
         ms, st = s.time_steps(k)
         total += ms * k
         chunks += 1
-        last = (ms, st, s.stats())
+        last = (ms, st, dict(s.stats(), batching_passes=s.batch_info()[0], batched_on_device=s.batch_info()[1]))
     ms_step = total / steps
     tail_ms, tail_stages, tail_stats = last
     state = s.get_bodies()

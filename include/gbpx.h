@@ -292,6 +292,14 @@ int gbpx_scene_get_bodies(void* scene, void* outRigidBodies);
 int gbpx_scene_set_bodies(void* scene, const void* rigidBodies);
 /* out4: pairs, constraints, contacts, partitions of the last step */
 int gbpx_scene_stats(void* scene, uint64_t* out4);
+/* PxBatchConstraintsTGS's rule on the device (enable = 1, the default: an exact
+ * parallel reproduction of the sequential greedy assignment) or on the host
+ * (0).  Same order and partitions either way; a frame in which a body has more
+ * than 32 dynamic constraints is batched on the host. */
+int gbpx_scene_set_device_batching(void* scene, int enable);
+/* out2[0]: colouring passes of the last frame's device batching; out2[1]: 1
+ * when that frame was batched on the device. */
+int gbpx_scene_batch_info(void* scene, uint32_t* out2);
 /* outMs[0] = ms per frame, outMs[1..6] per stage: bounds + broadphase,
  * narrowphase, constraint list + batching, bodies + rows, iterations, write-back */
 int gbpx_scene_time_steps(void* scene, uint32_t nbSteps, float* outMs);

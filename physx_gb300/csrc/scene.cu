@@ -240,6 +240,137 @@ __global__ void emitConstraintsKernel(const uint32_t* __restrict__ contactCount,
 	}
 }
 
+// ------------------------------------------------------------------ device batching
+// PxBatchConstraintsTGS's rule (DyConstraintPartition.cpp:858, restated in
+// batching.h) reproduced exactly in parallel.  The rule colours the
+// dynamic-dynamic constraints greedily in input order: a constraint takes the
+// lowest partition bit free in both bodies' masks, which holds the bits of the
+// earlier constraints of those bodies.  So a constraint's partition depends only
+// on the earlier constraints that share a body with it, and it can be computed
+// as soon as those are done (the parallel greedy colouring of Jones and
+// Plassmann, with input order as the priority): each pass colours every
+// constraint whose predecessors in both bodies' lists finished in earlier
+// passes.  At most one constraint per body is ready in a pass (the first
+// unfinished one of its list), so body masks are never written concurrently.
+// The number of passes is the longest chain of constraints linked through
+// shared bodies in input order (tens on contact graphs).  A constraint that
+// finds all 32 bits taken would go to the rule's next round of partitions: that
+// rare case is left to the host path.  Static constraints then take partition
+// maxDynamicPartition(body) + their rank among the body's static constraints,
+// and a stable sort by partition gives the reference's placement order.
+namespace sbatch
+{
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr uint32_t NOT_DONE = 0xffffffffu;
+constexpr uint32_t DEFERRED = 0xffffu;
+
+// Two incidence entries per constraint, in constraint order: (body, c) for each
+// dynamic body of a dynamic-dynamic constraint; (nbDyn + body, c) for the
+// dynamic body of a static constraint, whose second entry sorts last.
+__global__ void incidenceKernel(const uint32_t* __restrict__ consA, const uint32_t* __restrict__ consB, uint32_t nc, uint32_t nbDyn,
+                                uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t* __restrict__ ddList, uint32_t* __restrict__ counts)
+{
+	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+	if(c >= nc) return;
+	const uint32_t a = consA[c], b = consB[c];
+	const bool dd = a < nbDyn && b < nbDyn;
+	keys[2 * c] = dd ? a : nbDyn + (a < nbDyn ? a : b);
+	keys[2 * c + 1] = dd ? b : NONE;
+	vals[2 * c] = c;
+	vals[2 * c + 1] = c;
+	if(dd) ddList[atomicAdd(&counts[0], 1u)] = c;
+}
+
+// Each constraint's predecessor in each of its bodies' lists (dynamic-dynamic
+// constraints), and where each body's list of static constraints starts.
+__global__ void linkKernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t nbDyn,
+                           const uint32_t* __restrict__ consA, uint32_t* __restrict__ prevOf, uint32_t* __restrict__ staticRunStart)
+{
+	const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= n) return;
+	const uint32_t key = keys[e];
+	if(key == NONE) return;
+	const bool runStart = e == 0 || keys[e - 1] != key;
+	if(key < nbDyn)
+	{
+		const uint32_t c = vals[e];
+		prevOf[2 * c + (key == consA[c] ? 0u : 1u)] = runStart ? NONE : vals[e - 1];
+	}
+	else if(runStart)
+		staticRunStart[key - nbDyn] = e;
+}
+
+// One pass of the colouring.  donePass[c] is the pass that coloured c.
+__global__ void colorPassKernel(const uint32_t* __restrict__ ddList, uint32_t nDD, const uint32_t* __restrict__ consA,
+                                const uint32_t* __restrict__ consB, const uint32_t* __restrict__ prevOf, uint32_t* __restrict__ donePass,
+                                uint32_t* __restrict__ part, uint32_t* __restrict__ mask, uint32_t* __restrict__ maxNormal, uint32_t pass,
+                                uint32_t* __restrict__ counts)
+{
+	uint32_t done = 0;
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nDD; i += gridDim.x * blockDim.x)
+	{
+		const uint32_t c = ddList[i];
+		if(donePass[c] != NOT_DONE) continue;
+		const uint32_t pa = prevOf[2 * c], pb = prevOf[2 * c + 1];
+		if((pa != NONE && donePass[pa] >= pass) || (pb != NONE && donePass[pb] >= pass)) continue;
+		const uint32_t a = consA[c], b = consB[c];
+		const uint32_t freeBits = ~mask[a] & ~mask[b];
+		if(freeBits)
+		{
+			const uint32_t p = uint32_t(__ffs(freeBits)) - 1u;
+			mask[a] |= 1u << p;
+			mask[b] |= 1u << p;
+			maxNormal[a] = max(maxNormal[a], p + 1u);
+			maxNormal[b] = max(maxNormal[b], p + 1u);
+			part[c] = p;
+		}
+		else
+		{
+			part[c] = DEFERRED;
+			counts[2] = 1u;   // the rule's next round: the host path takes this step
+		}
+		donePass[c] = pass;
+		done++;
+	}
+	for(int o = 16; o > 0; o >>= 1) done += __shfl_xor_sync(0xffffffffu, done, o);
+	if((threadIdx.x & 31) == 0 && done) atomicSub(&counts[1], done);
+}
+
+// Partition of the static constraints, partition counts, sort keys.
+__global__ void staticPartKernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t nbDyn,
+                                 const uint32_t* __restrict__ staticRunStart, const uint32_t* __restrict__ maxNormal, uint32_t* __restrict__ part)
+{
+	const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= n) return;
+	const uint32_t key = keys[e];
+	if(key == NONE || key < nbDyn) return;
+	const uint32_t body = key - nbDyn;
+	part[vals[e]] = maxNormal[body] + (e - staticRunStart[body]);
+}
+
+constexpr uint32_t MAX_PARTS = 4096;
+__global__ void partKeysKernel(const uint32_t* __restrict__ part, uint32_t nc, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                               uint32_t* __restrict__ perPart, uint32_t* __restrict__ counts)
+{
+	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+	if(c >= nc) return;
+	const uint32_t p = part[c];
+	keys[c] = p;
+	vals[c] = c;
+	if(p < MAX_PARTS) atomicAdd(&perPart[p], 1u);
+	atomicMax(&counts[3], p + 1u);
+}
+
+// Inclusive scan of the partition counts into end offsets (one block).
+__global__ void partEndsKernel(uint32_t* __restrict__ perPart, const uint32_t* __restrict__ counts)
+{
+	if(threadIdx.x != 0) return;
+	const uint32_t np = min(counts[3], MAX_PARTS);
+	uint32_t acc = 0;
+	for(uint32_t p = 0; p < np; p++) { acc += perPart[p]; perPart[p] = acc; }
+}
+} // namespace sbatch
+
 // Solver bodies (PxConstructSolverBodiesTGS / PxConstructStaticSolverBodyTGS).
 __global__ void bodiesKernel(SceneDev s, StepParams sp, tgs::BodyVel* __restrict__ vel, tgs::BodyTx* __restrict__ tx, tgs::BodyData* __restrict__ data,
                              Tr* __restrict__ pose)
@@ -410,6 +541,14 @@ struct Scene
 	DevBuf<tgs::BodyData> data;
 	DevBuf<Tr> pose;
 	DevBuf<tgs::ConstraintRecord> recs;
+	// device batching: incidence lists, predecessors, colouring state
+	DevBuf<uint32_t> incKeys, incVals, incKeysAlt, incValsAlt, sortHist, ddList, prevOf, donePass, partOf, bodyMask, maxNormal, staticRunStart,
+	    perPart, batchCounts;
+	HostBuf<uint32_t> hBatch;   // counts and partition ends read back
+	std::vector<uint32_t> hPartEnds;
+	uint32_t lastColorPasses = 0;
+	bool deviceBatchEnabled = true;   // false: PxBatchConstraintsTGS's rule always on the host (comparison path)
+	bool lastBatchOnDevice = false;
 	HostBuf<uint32_t> hConsA, hConsB, hOrder, hSmall;
 	HostBuf<unsigned long long> hTotal;
 	uint32_t parity = 0, nbPairs = 0, nbPrev = 0, nbConstraints = 0, nbPartitions = 0;
@@ -440,7 +579,8 @@ struct Scene
 		if(bodies.reserve(n) || types.reserve(n) || geoms.reserve(n) || frictionCoef.reserve(n) || staticTypes.reserve(m + 1) ||
 		   staticGeoms.reserve(m + 1) || staticPose.reserve(7 * size_t(m) + 1) || bounds.reserve(6 * size_t(total)) || kindCount.reserve(NB_KINDS) ||
 		   totalContacts.reserve(1) || vel.reserve(total) || tx.reserve(total) || data.reserve(total) || pose.reserve(total) ||
-		   hSmall.reserve(16) || hTotal.reserve(1))
+		   hSmall.reserve(16) || hTotal.reserve(1) || bodyMask.reserve(n + 1) || maxNormal.reserve(n + 1) || staticRunStart.reserve(n + 1) ||
+		   perPart.reserve(sbatch::MAX_PARTS) || batchCounts.reserve(4) || hBatch.reserve(4 + sbatch::MAX_PARTS))
 			return GBPX_ERR_NOMEM;
 		GBPX_CUDA_TRY(cudaMemcpyAsync(bodies.ptr, rigid, size_t(n) * sizeof(tgs::RigidBody), cudaMemcpyHostToDevice, stream));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(types.ptr, t, size_t(n) * 4, cudaMemcpyHostToDevice, stream));
@@ -484,6 +624,9 @@ struct Scene
 		prevSlot.release(); contactCount.release(); blockCounts.release(); consPair.release(); consA.release(); consB.release(); order.release();
 		partEnds.release(); orderedPair.release(); contacts.release(); vel.release(); tx.release(); data.release(); pose.release();
 		recs.release(); hConsA.release(); hConsB.release(); hOrder.release(); hSmall.release(); hTotal.release();
+		incKeys.release(); incVals.release(); incKeysAlt.release(); incValsAlt.release(); sortHist.release(); ddList.release(); prevOf.release();
+		donePass.release(); partOf.release(); bodyMask.release(); maxNormal.release(); staticRunStart.release(); perPart.release();
+		batchCounts.release(); hBatch.release();
 		for(int k = 0; k < 2; k++) { manifolds[k].release(); frictionState[k].release(); }
 		if(bp) gbpx_bp_release(bp);
 		bp = nullptr;
@@ -498,7 +641,9 @@ struct Scene
 		if(queue.reserve(size_t(NB_KINDS) * cap) || prevSlot.reserve(cap) || contactCount.reserve(cap) || blockCounts.reserve(cap / 256 + 2) ||
 		   consPair.reserve(cap) || consA.reserve(cap) || consB.reserve(cap) || order.reserve(cap) || partEnds.reserve(cap) ||
 		   orderedPair.reserve(cap) || contacts.reserve(8 * cap) || recs.reserve(cap) || hConsA.reserve(cap) || hConsB.reserve(cap) ||
-		   hOrder.reserve(cap))
+		   hOrder.reserve(cap) || incKeys.reserve(2 * cap) || incVals.reserve(2 * cap) || incKeysAlt.reserve(2 * cap) ||
+		   incValsAlt.reserve(2 * cap) || sortHist.reserve(radixSortHistEntries(uint32_t(2 * cap))) || ddList.reserve(cap) ||
+		   prevOf.reserve(2 * cap) || donePass.reserve(cap) || partOf.reserve(cap))
 			return GBPX_ERR_NOMEM;
 		if(sp.persistent)
 		{
@@ -520,6 +665,67 @@ struct Scene
 		if(timing) cudaEventRecord(ev[k], stream);
 		stageZone.reset();
 		if(k < STAGES) stageZone.emplace(names[k]);
+	}
+
+	// PxBatchConstraintsTGS for the nc constraints (consA, consB) on the device
+	// (sbatch): fills order, partEnds and hPartEnds.  Returns false, with nothing
+	// filled, when a constraint needs the rule's second round of partitions (the
+	// caller then batches on the host).
+	int deviceBatch(uint32_t nc, bool& done)
+	{
+		done = false;
+		const cudaStream_t s = stream;
+		const uint32_t n2 = 2 * nc;
+		GBPX_CUDA_TRY(cudaMemsetAsync(batchCounts.ptr, 0, 16, s));
+		sbatch::incidenceKernel<<<divUp(nc, 256), 256, 0, s>>>(consA.ptr, consB.ptr, nc, nbDyn, incKeys.ptr, incVals.ptr, ddList.ptr,
+		                                                       batchCounts.ptr);
+		GBPX_CUDA_TRY(cudaMemsetAsync(bodyMask.ptr, 0, size_t(nbDyn) * 4, s));
+		GBPX_CUDA_TRY(cudaMemsetAsync(maxNormal.ptr, 0, size_t(nbDyn) * 4, s));
+		GBPX_CUDA_TRY(cudaMemsetAsync(donePass.ptr, 0xff, size_t(nc) * 4, s));
+		GBPX_CUDA_TRY(cudaMemsetAsync(perPart.ptr, 0, sbatch::MAX_PARTS * 4, s));
+		// stable sort of the incidence entries by list (body, then static lists): bits for 2 nbDyn list keys
+		int bits = 1;
+		while(bits < 32 && (1ull << bits) <= 2ull * nbDyn) bits++;
+		const int endBit = std::min(32, (bits + 7) / 8 * 8 + (bits % 8 ? 0 : 0));
+		const bool alt = radixSort<uint32_t, true>(incKeys.ptr, incVals.ptr, incKeysAlt.ptr, incValsAlt.ptr, n2, 0, endBit, sortHist.ptr, s);
+		const uint32_t* sk = alt ? incKeysAlt.ptr : incKeys.ptr;
+		const uint32_t* sv = alt ? incValsAlt.ptr : incVals.ptr;
+		sbatch::linkKernel<<<divUp(n2, 256), 256, 0, s>>>(sk, sv, n2, nbDyn, consA.ptr, prevOf.ptr, staticRunStart.ptr);
+		// remaining = number of dynamic-dynamic constraints
+		GBPX_CUDA_TRY(cudaMemcpyAsync(batchCounts.ptr + 1, batchCounts.ptr, 4, cudaMemcpyDeviceToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
+		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+		const uint32_t nDD = hBatch.ptr[0];
+		const uint32_t grid = std::max(1u, std::min(divUp(nDD, 256), 152u * 8u));
+		uint32_t pass = 0;
+		while(nDD)
+		{
+			// a pass always colours the first unfinished constraint, so nDD passes always suffice
+			for(int k = 0; k < 8; k++)
+				sbatch::colorPassKernel<<<grid, 256, 0, s>>>(ddList.ptr, nDD, consA.ptr, consB.ptr, prevOf.ptr, donePass.ptr, partOf.ptr, bodyMask.ptr,
+				                                              maxNormal.ptr, ++pass, batchCounts.ptr);
+			GBPX_CUDA_TRY(cudaGetLastError());
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
+			GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+			if(hBatch.ptr[1] == 0 || pass > nDD + 8) break;
+		}
+		lastColorPasses = pass;
+		if(nDD && (hBatch.ptr[1] != 0 || hBatch.ptr[2] != 0)) return GBPX_OK;   // second round needed: host path
+		sbatch::staticPartKernel<<<divUp(n2, 256), 256, 0, s>>>(sk, sv, n2, nbDyn, staticRunStart.ptr, maxNormal.ptr, partOf.ptr);
+		// stable sort by partition: the reference's placement (input order within a partition)
+		sbatch::partKeysKernel<<<divUp(nc, 256), 256, 0, s>>>(partOf.ptr, nc, incKeys.ptr, incVals.ptr, perPart.ptr, batchCounts.ptr);
+		sbatch::partEndsKernel<<<1, 32, 0, s>>>(perPart.ptr, batchCounts.ptr);
+		const bool alt2 = radixSort<uint32_t, true>(incKeys.ptr, incVals.ptr, incKeysAlt.ptr, incValsAlt.ptr, nc, 0, 16, sortHist.ptr, s);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, alt2 ? incValsAlt.ptr : incVals.ptr, size_t(nc) * 4, cudaMemcpyDeviceToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr + 4, perPart.ptr, sbatch::MAX_PARTS * 4, cudaMemcpyDeviceToHost, s));
+		GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+		const uint32_t nbParts = hBatch.ptr[3];
+		if(nbParts > sbatch::MAX_PARTS) return GBPX_OK;   // (never on contact scenes) host path
+		hPartEnds.assign(hBatch.ptr + 4, hBatch.ptr + 4 + nbParts);
+		GBPX_CUDA_TRY(cudaMemcpyAsync(partEnds.ptr, perPart.ptr, size_t(nbParts) * 4, cudaMemcpyDeviceToDevice, s));
+		done = true;
+		return GBPX_OK;
 	}
 
 	int step()
@@ -578,18 +784,35 @@ struct Scene
 			nbContacts = hTotal.ptr[0];
 		}
 		const uint32_t nc = nbConstraints;
-		batching::Result batch;
+		hPartEnds.clear();
+		lastBatchOnDevice = false;
 		if(nc)
 		{
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hConsA.ptr, consA.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hConsB.ptr, consB.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
-			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
-			batching::partition(hConsA.ptr, hConsB.ptr, nc, nbDyn, batch);
-			memcpy(hOrder.ptr, batch.order.data(), size_t(nc) * 4);
-			GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, hOrder.ptr, size_t(nc) * 4, cudaMemcpyHostToDevice, stream));
-			GBPX_CUDA_TRY(cudaMemcpyAsync(partEnds.ptr, batch.partitionEnds.data(), batch.partitionEnds.size() * 4, cudaMemcpyHostToDevice, stream));
+			bool onDevice = false;
+			if(deviceBatchEnabled)
+			{
+				rc = deviceBatch(nc, onDevice);
+				if(rc) return rc;
+			}
+			lastBatchOnDevice = onDevice;
+			if(!onDevice)
+			{
+				// the rule's second round of partitions (a body in more than 32 constraints): on the host
+				batching::Result batch;
+				GBPX_CUDA_TRY(cudaMemcpyAsync(hConsA.ptr, consA.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
+				GBPX_CUDA_TRY(cudaMemcpyAsync(hConsB.ptr, consB.ptr, size_t(nc) * 4, cudaMemcpyDeviceToHost, stream));
+				GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+				batching::partition(hConsA.ptr, hConsB.ptr, nc, nbDyn, batch);
+				memcpy(hOrder.ptr, batch.order.data(), size_t(nc) * 4);
+				GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, hOrder.ptr, size_t(nc) * 4, cudaMemcpyHostToDevice, stream));
+				GBPX_CUDA_TRY(cudaMemcpyAsync(partEnds.ptr, batch.partitionEnds.data(), batch.partitionEnds.size() * 4, cudaMemcpyHostToDevice, stream));
+				GBPX_CUDA_TRY(cudaStreamSynchronize(stream));   // the host vector goes out of scope
+				hPartEnds = batch.partitionEnds;
+				// the rule sizes its table in rounds of 32: drop the empty partitions at the end
+				while(hPartEnds.size() > 1 && hPartEnds.back() == hPartEnds[hPartEnds.size() - 2]) hPartEnds.pop_back();
+			}
 		}
-		nbPartitions = uint32_t(batch.partitionEnds.size());
+		nbPartitions = uint32_t(hPartEnds.size());
 		mark(3);
 		// 4. solver bodies and contact rows
 		bodiesKernel<<<divUp(nbDyn + nbStatic, 128), 128, 0, stream>>>(d, sp, vel.ptr, tx.ptr, data.ptr, pose.ptr);
@@ -610,7 +833,7 @@ struct Scene
 			tgs::FrictionState* broken = sp.persistent && last ? frictionState[par ^ 1u].ptr : nullptr;
 			for(uint32_t p = 0; p < nbPartitions; p++)
 			{
-				const uint32_t b = p ? batch.partitionEnds[p - 1] : 0u, e = batch.partitionEnds[p];
+				const uint32_t b = p ? hPartEnds[p - 1] : 0u, e = hPartEnds[p];
 				if(e > b)
 					solvePartitionKernel<<<divUp(e - b, 128), 128, 0, stream>>>(recs.ptr, b, e, vel.ptr, nbDyn, minPen, elapsed, orderedPair.ptr, broken);
 			}
@@ -738,9 +961,31 @@ GBPX_API int gbpx_scene_stats(void* sv, uint64_t* out4)
 	return GBPX_OK;
 }
 
+// PxBatchConstraintsTGS on the device (1, the default) or on the host (0).  The
+// two give the same order and partitions; the device form falls back to the
+// host for a frame in which a body has more than 32 dynamic constraints.
+GBPX_API int gbpx_scene_set_device_batching(void* sv, int enable)
+{
+	Scene* s = static_cast<Scene*>(sv);
+	if(!s) return GBPX_ERR_INVALID;
+	s->deviceBatchEnabled = enable != 0;
+	return GBPX_OK;
+}
+
+// Batching of the last frame: out2[0] = colouring passes of the device
+// batching, out2[1] = 1 when the frame was batched on the device.
+GBPX_API int gbpx_scene_batch_info(void* sv, uint32_t* out2)
+{
+	Scene* s = static_cast<Scene*>(sv);
+	if(!s || !out2) return GBPX_ERR_INVALID;
+	out2[0] = s->lastColorPasses;
+	out2[1] = s->lastBatchOnDevice ? 1u : 0u;
+	return GBPX_OK;
+}
+
 // Runs nbSteps frames with CUDA events on the scene's stream between the
 // stages; outMs[0] = average milliseconds per frame, outMs[1..6] = average per
-// stage: bounds + broadphase, narrowphase, constraint list + batching (host),
+// stage: bounds + broadphase, narrowphase, constraint list + batching,
 // solver bodies + rows, iterations, write-back.  Host work inside a frame
 // (the broadphase's count read-backs, the batching) is inside the times.
 GBPX_API int gbpx_scene_time_steps(void* sv, uint32_t nbSteps, float* outMs)

@@ -82,6 +82,19 @@ class Scene:
         check(self._L.gbpx_scene_stats(self._h, _p(out)), "gbpx_scene_stats")
         return dict(pairs=int(out[0]), constraints=int(out[1]), contacts=int(out[2]), partitions=int(out[3]))
 
+    def set_device_batching(self, enable=True):
+        """PxBatchConstraintsTGS's rule on the device (default) or on the host; the
+        results are the same."""
+        self._L.gbpx_scene_set_device_batching.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        check(self._L.gbpx_scene_set_device_batching(self._h, int(bool(enable))), "gbpx_scene_set_device_batching")
+
+    def batch_info(self):
+        """(colouring passes, batched on the device) of the last frame."""
+        out = np.zeros(2, np.uint32)
+        self._L.gbpx_scene_batch_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        check(self._L.gbpx_scene_batch_info(self._h, _p(out)), "gbpx_scene_batch_info")
+        return int(out[0]), bool(out[1])
+
     def time_steps(self, n):
         """Runs n frames; returns (ms per frame, {stage: ms per frame}) from CUDA events on the scene's stream."""
         out = np.zeros(1 + len(STAGES), np.float32)

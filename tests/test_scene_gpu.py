@@ -172,3 +172,28 @@ def test_scene_100k_bodies_600_steps_statistics_match_reference(cuda_device):
     assert abs(G[-1, 2] - R[-1, 2]) <= 0.02 * R[-1, 2]
     assert abs(G[-1, 4] - R[-1, 4]) <= 0.02
     assert np.isfinite(G).all()
+
+
+@pytest.mark.parametrize("maker", ["pile", "hub"])
+def test_scene_device_batching_equals_host_batching(cuda_device, maker):
+    """PxBatchConstraintsTGS's rule run on the device (the parallel greedy colouring)
+    and on the host give the same bytes frame after frame, persistent pair state
+    on: a 3000-body pile (device path), and a scene with a body in more than 32
+    constraints (the rule's second round: the device path hands the frame to the
+    host)."""
+    from physx_gb300.scene import Scene
+    from scenarios import hub_scene
+    sc = _pile(137, 3000) if maker == "pile" else hub_scene()
+    a, b = Scene(sc), Scene(sc)
+    b.set_device_batching(False)
+    on_device = []
+    for _ in range(12):
+        a.step(1)
+        b.step(1)
+        on_device.append(a.batch_info()[1])
+        assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
+        assert a.stats() == b.stats()
+    if maker == "pile":
+        assert all(on_device) and a.batch_info()[0] > 0
+    a.release()
+    b.release()
