@@ -456,7 +456,7 @@ struct BroadPhase
 	DevBuf<bp::UpdateRec> dRecs;
 	DevBuf<uint32_t> dRemoved;
 	HostBuf<bp::UpdateRec> hRecs;
-	DevBuf<uint32_t> blockCounts, keysA, valsA, keysB, valsB, hist;
+	DevBuf<uint32_t> blockCounts, keysA, valsA, keysB, valsB, hist, scanScratch;
 	DevBuf<uint2> sx;
 	DevBuf<float4> syz;
 	DevBuf<uint32_t> sgrp, supd, updPos, sleepPos;
@@ -503,7 +503,7 @@ struct BroadPhase
 		if(stream) cudaStreamSynchronize(stream);
 		bx.release(); byz.release(); groups.release(); live.release(); flags.release();
 		dRecs.release(); dRemoved.release(); hRecs.release();
-		blockCounts.release(); keysA.release(); valsA.release(); keysB.release(); valsB.release(); hist.release();
+		blockCounts.release(); scanScratch.release(); keysA.release(); valsA.release(); keysB.release(); valsB.release(); hist.release();
 		sx.release(); syz.release(); sgrp.release(); supd.release(); updPos.release(); sleepPos.release();
 		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
 		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release(); longScans.release();
@@ -554,7 +554,8 @@ struct BroadPhase
 		if(!n) { *total = 0; return GBPX_OK; }
 		GBPX_CUDA_TRY(cudaMemcpyAsync(posOut, selIn, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream));
 		GBPX_CUDA_TRY(cudaMemsetAsync(posOut + n, 0, 4, stream));
-		rs::scanKernel<<<1, 1024, 0, stream>>>(posOut, n + 1);
+		if(scanScratch.reserve(rs::scanScratchEntries(n + 1))) return GBPX_ERR_NOMEM;
+		rs::scanAny(posOut, n + 1, scanScratch.ptr, stream);
 		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, posOut + n, 4, cudaMemcpyDeviceToHost, stream));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		*total = hCounts.ptr[0];
@@ -675,7 +676,14 @@ struct BroadPhase
 		unsigned long long* F = found.ptr;
 		if(nFound > 1)
 		{
-			const bool a2 = radixSort<unsigned long long, false>(found.ptr, nullptr, foundAlt.ptr, nullptr, nFound, 0, 64, hist.ptr, stream);
+			// keys are (id0 << 32) | id1 with ids below the capacity: the digits above its bit
+			// width in each half are zero and are skipped
+			int idBits = 1;
+			while(idBits < 32 && (1ull << idBits) < capacity) idBits++;
+			uint32_t skip = 0;
+			for(int d = 0; d < 8; d++)
+				if((d * 8) % 32 >= idBits) skip |= 1u << d;
+			const bool a2 = radixSort<unsigned long long, false>(found.ptr, nullptr, foundAlt.ptr, nullptr, nFound, 0, 64, hist.ptr, stream, skip);
 			F = a2 ? foundAlt.ptr : found.ptr;
 		}
 
