@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--cpu-scenes", type=int, default=1024, help="scenes in the bounded CPU-baseline sample")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--plain-scenes", type=int, default=256, help="scenes timed one-per-launch for the plain comparison")
-    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the Poisson serving run (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="duration of the Poisson serving run (0 = skip)")
+    ap.add_argument("--serve-lanes", type=int, default=1, help="lanes per body-count class of the serving pool")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="request arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the serving pool")
     ap.add_argument("--extras", type=int, default=1, help="also measure the pyramid, 1M-AABB broadphase and 100k-body scene workloads")
@@ -526,7 +527,8 @@ def main():
     serving = None
     if a.serve_seconds > 0:
         from physx_gb300.serve_load import run_poisson
-        serving = run_poisson(duration=a.serve_seconds, rate=a.serve_rate, budget_bytes=a.serve_budget_gb * 1e9, seed=a.seed + 1)
+        serving = run_poisson(duration=a.serve_seconds, rate=a.serve_rate, budget_bytes=a.serve_budget_gb * 1e9, seed=a.seed + 1,
+                              lanes_per_class=a.serve_lanes)
         serving["workload"] = ("Poisson %.0f req/s of 'advance scene k by n~U{1..8} steps' over a pool of scenes log-uniform [16,4096] "
                                "bodies admitted against a %.0f GB budget, retired after U(500,5000) steps; %.0f s run" %
                                (a.serve_rate, a.serve_budget_gb, a.serve_seconds))

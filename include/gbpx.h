@@ -250,14 +250,15 @@ int gbpx_host_alloc(size_t bytes, void** out);
  * Request loop over a live pool of scenes resident in HBM (no reference
  * counterpart: it drives the batched step above).  Scenes are admitted into
  * fixed-capacity slots grouped by body-count class (class c: slots[c] slots of
- * capacity[c] bodies, staticsPerSlot statics); each class steps on its own
- * stream.  A request advances one scene by n steps; each pump issues, per
- * class, one step over every scene that still owes steps (continuous
- * batching), with at most two steps in flight per class, and completes
- * requests whose steps have finished.  Latency runs from the request's
- * arrival time to the host observing its last step done. */
+ * capacity[c] bodies, staticsPerSlot statics), each class split into
+ * lanesPerClass lanes; each lane steps on its own stream.  A request advances
+ * one scene by n steps; each pump issues, per lane, one step over every scene
+ * that still owes steps (continuous batching), with at most two steps in
+ * flight per lane, and completes requests whose steps have finished.  Latency
+ * runs from the request's arrival time to the host observing its last step
+ * done. */
 int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, const float* params,
-                       const uint32_t* iterations, uint32_t pairsPerBody, void** outServer);
+                       const uint32_t* iterations, uint32_t pairsPerBody, uint32_t lanesPerClass, void** outServer);
 void gbpx_server_release(void* server);
 /* device bytes of one slot (for sizing a pool against a memory budget), with or
  * without the persistent pair state; not a status code */
@@ -275,6 +276,19 @@ int gbpx_server_poll(void* server, uint64_t* outTags, double* outLatencySeconds,
 int gbpx_server_read_scene(void* server, uint32_t scene, void* outRigidBodies);
 /* out4: body-steps completed, class steps completed, live scenes, steps in flight */
 int gbpx_server_stats(void* server, uint64_t* out4);
+/* The open-loop serving load run in the library (no per-request host language
+ * round trips): Poisson arrivals at `rate` of "advance a live scene by n ~
+ * U{minSteps..maxSteps} steps" for `seconds`; the pool is filled from a library
+ * of nbLib scenes with one static shape each (scene k's bodies at libOffsets[k]
+ * .. libOffsets[k + 1], nbLib + 1 offsets), and a scene that owes nothing after
+ * its lifetime (U{lifeMin..lifeMax} steps) is retired and replaced.  out16:
+ * seconds, submitted, completed, body-steps, p50 and p99 request latency (ms),
+ * the same for 257..512-body scenes, their p50 and p99 latency per requested
+ * step, live scenes, retired, admitted after the start, lane steps, lanes, 0. */
+int gbpx_server_run_load(void* server, double seconds, double rate, uint32_t minSteps, uint32_t maxSteps, uint32_t lifeMin, uint32_t lifeMax,
+                         uint64_t seed, uint32_t nbLib, const uint32_t* libOffsets, const void* libRigid, const int* libTypes,
+                         const float* libGeoms, const float* libFriction, const float* libStaticPoses, const int* libStaticTypes,
+                         const float* libStaticGeoms, double* out16);
 void gbpx_host_free(void* p);
 
 /* ---- One large scene (no reference counterpart: the snippet's frame over one

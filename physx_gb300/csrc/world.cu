@@ -36,6 +36,7 @@
 #include <numeric>
 #include <chrono>
 #include <deque>
+#include <random>
 #include <map>
 #include <string>
 
@@ -1525,6 +1526,7 @@ struct World
 {
 	cudaStream_t stream = 0;
 	cudaStream_t sideStream = 0;   // block-per-scene kernels run beside the warp-per-scene ones
+	int streamPriority = 0;        // CUDA stream priority of the world's streams (set before create)
 	cudaEvent_t forkEv[3] = {}, joinEv[3] = {};
 	cudaGraphExec_t graphExec = nullptr;
 	uint32_t graphSteps = 0;
@@ -1625,8 +1627,8 @@ struct World
 		std::vector<uint32_t> order(S);
 		std::iota(order.begin(), order.end(), 0u);
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
-		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-		GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&sideStream, cudaStreamNonBlocking));
+		GBPX_CUDA_TRY(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, streamPriority));
+		GBPX_CUDA_TRY(cudaStreamCreateWithPriority(&sideStream, cudaStreamNonBlocking, streamPriority));
 		for(int k = 0; k < 3; k++)
 		{
 			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&forkEv[k], cudaEventDisableTiming));
@@ -2523,30 +2525,37 @@ struct Server
 	}
 
 	int create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, uint32_t pairsPerBody,
-	           const world::StepParams& sp)
+	           const world::StepParams& sp, uint32_t lanesPerClass)
 	{
 		uint32_t base = 0;
 		for(uint32_t c = 0; c < nbClasses; c++)
 		{
-			if(!slots[c]) continue;
-			Lane* L = new Lane;
-			lanes.push_back(L);
-			L->capacity = capacity[c];
-			L->slots = slots[c];
-			L->staticCap = staticsPerSlot;
-			L->base = base;
-			std::vector<uint32_t> cap(slots[c], capacity[c]), st(slots[c], staticsPerSlot);
-			int rc = L->w.create(slots[c], cap.data(), st.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, pairsPerBody, sp);
-			if(rc) return rc;
-			rc = L->w.capture(1);
-			if(rc) return rc;
-			for(uint32_t k = slots[c]; k > 0; k--) L->freeSlots.push_back(k - 1);
-			for(int i = 0; i < 2; i++)
+			// a class's slots split over lanesPerClass lanes: each lane steps its own
+			// scenes on its own stream, so a step covers fewer scenes and lanes overlap
+			const uint32_t k = std::max(1u, std::min(lanesPerClass, slots[c]));
+			for(uint32_t j = 0; j < k; j++)
 			{
-				GBPX_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&L->pinned[i]), (size_t(slots[c]) + 1) * 4, cudaHostAllocDefault));
-				GBPX_CUDA_TRY(cudaEventCreateWithFlags(&L->ev[i], cudaEventDisableTiming));
+				const uint32_t laneSlots = slots[c] / k + (j < slots[c] % k ? 1u : 0u);
+				if(!laneSlots) continue;
+				Lane* L = new Lane;
+				lanes.push_back(L);
+				L->capacity = capacity[c];
+				L->slots = laneSlots;
+				L->staticCap = staticsPerSlot;
+				L->base = base;
+				std::vector<uint32_t> cap(laneSlots, capacity[c]), st(laneSlots, staticsPerSlot);
+				int rc = L->w.create(laneSlots, cap.data(), st.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, pairsPerBody, sp);
+				if(rc) return rc;
+				rc = L->w.capture(1);
+				if(rc) return rc;
+				for(uint32_t q = laneSlots; q > 0; q--) L->freeSlots.push_back(q - 1);
+				for(int i = 0; i < 2; i++)
+				{
+					GBPX_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&L->pinned[i]), (size_t(laneSlots) + 1) * 4, cudaHostAllocDefault));
+					GBPX_CUDA_TRY(cudaEventCreateWithFlags(&L->ev[i], cudaEventDisableTiming));
+				}
+				base += laneSlots;
 			}
-			base += slots[c];
 		}
 		scenes.resize(base);
 		return lanes.empty() ? GBPX_ERR_INVALID : GBPX_OK;
@@ -2555,10 +2564,11 @@ struct Server
 	int admit(uint32_t nb, const void* rigid, const int* types, const float* geoms, const float* friction, uint32_t ns, const float* staticPoses,
 	          const int* staticTypes, const float* staticGeoms, uint32_t* outScene)
 	{
+		// the smallest class that holds the scene; among its lanes, the one with the most free slots
 		Lane* best = nullptr;
 		for(Lane* L : lanes)
 			if(L->capacity >= nb && !L->freeSlots.empty() && ns <= L->staticCap &&
-			   (!best || L->capacity < best->capacity))
+			   (!best || L->capacity < best->capacity || (L->capacity == best->capacity && L->freeSlots.size() > best->freeSlots.size())))
 				best = L;
 		if(!best) return GBPX_ERR_BUDGET;
 		const uint32_t slot = best->freeSlots.back();
@@ -2650,6 +2660,133 @@ struct Server
 		return GBPX_OK;
 	}
 
+	// Library of scenes the load admits (one static shape each): bodies and
+	// shapes of scene k at offsets[k] .. offsets[k + 1].
+	struct Library
+	{
+		uint32_t count;
+		const uint32_t* offsets;
+		const tgs::RigidBody* rigid;
+		const int* types;
+		const float* geoms;
+		const float* friction;
+		const float* staticPoses;   // 7 floats per scene
+		const int* staticTypes;
+		const float* staticGeoms;   // 4 floats per scene
+	};
+
+	// The open-loop serving load, run natively: Poisson arrivals at `rate` of
+	// "advance a live scene (uniform) by n ~ U{minSteps..maxSteps} steps"; the
+	// pool is filled from the library until admission fails 50 times in a row;
+	// a scene that owes nothing and has done at least its lifetime (U{lifeMin..
+	// lifeMax} steps) is retired and a library scene admitted in its place.
+	// Latency runs from a request's scheduled arrival to the pump observing its
+	// last step.  out (16 doubles): seconds, submitted, completed, body-steps,
+	// p50 / p99 latency (ms), the same for scenes of 257..512 bodies, their p50 /
+	// p99 latency per requested step, live scenes, retired, admitted after the
+	// start, lane steps, lanes.
+	int runLoad(double duration, double rate, uint32_t minSteps, uint32_t maxSteps, uint32_t lifeMin, uint32_t lifeMax, uint64_t seed,
+	            const Library& lib, double* out)
+	{
+		std::mt19937_64 rng(seed);
+		auto uniform = [&](uint64_t lo, uint64_t hi) { return lo + rng() % (hi - lo + 1); };
+		std::exponential_distribution<double> gap(rate);
+		std::vector<uint32_t> live;
+		std::vector<uint32_t> lifetime(scenes.size(), 0), owed(scenes.size(), 0), doneSteps(scenes.size(), 0), size(scenes.size(), 0);
+		auto admitOne = [&]() -> int {
+			const uint32_t k = uint32_t(uniform(0, lib.count - 1));
+			const uint32_t b0 = lib.offsets[k], nb = lib.offsets[k + 1] - b0;
+			uint32_t id = 0;
+			const int rc = admit(nb, lib.rigid + b0, lib.types + b0, lib.geoms + 4 * size_t(b0), lib.friction + b0, 1, lib.staticPoses + 7 * size_t(k),
+			                     lib.staticTypes + k, lib.staticGeoms + 4 * size_t(k), &id);
+			if(rc) return rc;
+			live.push_back(id);
+			lifetime[id] = uint32_t(uniform(lifeMin, lifeMax));
+			owed[id] = 0;
+			doneSteps[id] = 0;
+			size[id] = nb;
+			return GBPX_OK;
+		};
+		for(int fails = 0; fails < 50;)
+		{
+			const int rc = admitOne();
+			if(rc == GBPX_ERR_BUDGET) fails++;
+			else if(rc) return rc;
+			else fails = 0;
+		}
+		if(live.empty()) return GBPX_ERR_BUDGET;
+		for(Lane* L : lanes) GBPX_CUDA_TRY(cudaStreamSynchronize(L->w.stream));   // admissions done
+		std::vector<uint32_t> reqScene, reqSteps;
+		std::vector<double> lat, lat512, perStep512;
+		uint64_t tag = 0, retired = 0, admitted = 0;
+		const uint64_t bodySteps0 = bodySteps, steps0 = steps;
+		doneTags.clear();
+		doneLatency.clear();
+		const double t0 = now(), tEnd = t0 + duration;
+		double tNext = t0;
+		for(;;)
+		{
+			const double t = now();
+			if(t >= tEnd) break;
+			while(tNext <= t)
+			{
+				const uint32_t id = live[uniform(0, live.size() - 1)];
+				const uint32_t n = uint32_t(uniform(minSteps, maxSteps));
+				int rc = submit(id, n, tag, tNext);
+				if(rc) return rc;
+				reqScene.push_back(id);
+				reqSteps.push_back(n);
+				owed[id] += n;
+				tag++;
+				tNext += gap(rng);
+			}
+			int rc = pump(nullptr);
+			if(rc) return rc;
+			for(size_t i = 0; i < doneTags.size(); i++)
+			{
+				const uint64_t tg = doneTags[i];
+				const uint32_t id = reqScene[tg], n = reqSteps[tg];
+				const double l = doneLatency[i];
+				lat.push_back(l);
+				if(size[id] > 256 && size[id] <= 512)
+				{
+					lat512.push_back(l);
+					perStep512.push_back(l / n);
+				}
+				owed[id] -= n;
+				doneSteps[id] += n;
+				if(owed[id] == 0 && doneSteps[id] >= lifetime[id] && live.size() > 1)
+				{
+					rc = retire(id);
+					if(rc) return rc;
+					live.erase(std::find(live.begin(), live.end(), id));
+					retired++;
+					rc = admitOne();
+					if(rc == GBPX_OK) admitted++;
+					else if(rc != GBPX_ERR_BUDGET) return rc;
+				}
+			}
+			doneTags.clear();
+			doneLatency.clear();
+		}
+		const double elapsed = now() - t0;
+		auto pct = [](std::vector<double> v, double q) -> double {
+			if(v.empty()) return -1.0;
+			std::sort(v.begin(), v.end());
+			const double pos = q * double(v.size() - 1);
+			const size_t i = size_t(pos);
+			const double f = pos - double(i);
+			return 1000.0 * (i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i]);
+		};
+		uint64_t liveNow = 0;
+		for(const auto& sc : scenes) liveNow += sc.live ? 1 : 0;
+		const double vals[16] = {elapsed, double(tag), double(lat.size()), double(bodySteps - bodySteps0), pct(lat, 0.5), pct(lat, 0.99),
+		                         pct(lat512, 0.5), pct(lat512, 0.99), pct(perStep512, 0.5), pct(perStep512, 0.99), double(liveNow), double(retired),
+		                         double(admitted), double(steps - steps0), double(lanes.size()), 0.0};
+		for(int i = 0; i < 16; i++) out[i] = vals[i];
+		return GBPX_OK;
+	}
+
 	int readScene(uint32_t id, void* out)
 	{
 		if(id >= scenes.size() || !scenes[id].live) return GBPX_ERR_INVALID;
@@ -2684,9 +2821,10 @@ using gbpx::Server;
 // slots[c] slots of capacity[c] bodies and staticsPerSlot statics each.
 // params/iterations as gbpx_world_create.
 GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, const uint32_t* slots, uint32_t staticsPerSlot, const float* params,
-                                const uint32_t* iterations, uint32_t pairsPerBody, void** outServer)
+                                const uint32_t* iterations, uint32_t pairsPerBody, uint32_t lanesPerClass, void** outServer)
 {
-	if(!outServer || !nbClasses || !capacity || !slots || !params || !iterations || !iterations[0] || !iterations[1] || !pairsPerBody)
+	if(!outServer || !nbClasses || !capacity || !slots || !params || !iterations || !iterations[0] || !iterations[1] || !pairsPerBody ||
+	   !lanesPerClass)
 		return GBPX_ERR_INVALID;
 	for(uint32_t c = 0; c < nbClasses; c++)
 		if(!capacity[c] || capacity[c] + staticsPerSlot > 65535u) return GBPX_ERR_INVALID;
@@ -2701,7 +2839,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.resBytes = 0;       // set at creation
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
-	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp);
+	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp, lanesPerClass);
 	if(rc) { s->release(); delete s; return rc; }
 	*outServer = s;
 	return GBPX_OK;
@@ -2798,4 +2936,25 @@ GBPX_API int gbpx_server_stats(void* sv, uint64_t* out4)
 	for(const auto* L : s->lanes) inflight += L->nbInflight;
 	out4[0] = s->bodySteps; out4[1] = s->steps; out4[2] = live; out4[3] = inflight;
 	return GBPX_OK;
+}
+
+// The open-loop Poisson serving load run natively on the pool (Server::runLoad):
+// the library holds nbLib scenes of one static shape each (scene k's bodies at
+// libOffsets[k] .. libOffsets[k + 1]); out receives 16 figures (see runLoad).
+GBPX_API int gbpx_server_run_load(void* sv, double seconds, double rate, uint32_t minSteps, uint32_t maxSteps, uint32_t lifeMin, uint32_t lifeMax,
+                                  uint64_t seed, uint32_t nbLib, const uint32_t* libOffsets, const void* libRigid, const int* libTypes,
+                                  const float* libGeoms, const float* libFriction, const float* libStaticPoses, const int* libStaticTypes,
+                                  const float* libStaticGeoms, double* out16)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s || !(seconds > 0.0) || !(rate > 0.0) || !minSteps || maxSteps < minSteps || lifeMax < lifeMin || !nbLib || !libOffsets || !libRigid ||
+	   !libTypes || !libGeoms || !libFriction || !libStaticPoses || !libStaticTypes || !libStaticGeoms || !out16)
+		return GBPX_ERR_INVALID;
+	for(uint32_t k = 0; k < nbLib; k++)
+		if(libOffsets[k + 1] <= libOffsets[k]) return GBPX_ERR_INVALID;
+	for(uint32_t i = 0; i < libOffsets[nbLib]; i++)
+		if(uint32_t(libTypes[i]) > 3u || libTypes[i] == 1) return GBPX_ERR_INVALID;
+	const Server::Library lib = {nbLib, libOffsets, static_cast<const gbpx::tgs::RigidBody*>(libRigid), libTypes, libGeoms, libFriction,
+	                             libStaticPoses, libStaticTypes, libStaticGeoms};
+	return s->runLoad(seconds, rate, minSteps, maxSteps, lifeMin, lifeMax, seed, lib, out16);
 }

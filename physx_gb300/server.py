@@ -14,7 +14,9 @@ def _setup():
     L = lib()
     if not getattr(L, "_server_ready", False):
         L.gbpx_server_create.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
-                                         ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+        L.gbpx_server_run_load.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_void_p] * 9
         L.gbpx_server_release.argtypes = [ctypes.c_void_p]
         L.gbpx_server_slot_bytes.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
         L.gbpx_server_slot_bytes.restype = ctypes.c_uint64
@@ -48,7 +50,7 @@ def slots_for_budget(capacities, budget_bytes, weights=None, statics=1, pairs_pe
 class Server:
     _h = None
 
-    def __init__(self, capacities, slots, statics=1, pairs_per_body=8, **params):
+    def __init__(self, capacities, slots, statics=1, pairs_per_body=8, lanes_per_class=1, **params):
         L = _setup()
         p = dict(DEFAULT_PARAMS)
         p.update(params)
@@ -56,7 +58,8 @@ class Server:
         cap = np.ascontiguousarray(capacities, np.uint32)
         sl = np.ascontiguousarray(slots, np.uint32)
         h = ctypes.c_void_p()
-        check(L.gbpx_server_create(len(cap), _p(cap), _p(sl), statics, _p(pv), _p(it), pairs_per_body, ctypes.byref(h)), "gbpx_server_create")
+        check(L.gbpx_server_create(len(cap), _p(cap), _p(sl), statics, _p(pv), _p(it), pairs_per_body, lanes_per_class, ctypes.byref(h)),
+              "gbpx_server_create")
         self._h, self._L = h, L
         self._sizes = {}
         self._dtype = None
@@ -131,3 +134,20 @@ class Server:
                 lats.append(l_)
                 break
         return np.concatenate(tags), np.concatenate(lats)
+
+    def run_load(self, library, seconds, rate, steps=(1, 8), life=(500, 5000), seed=5):
+        """The open-loop Poisson load run in the library (gbpx_server_run_load) over a
+        library of scenes (dicts with one static shape each); returns its figures."""
+        off = np.zeros(len(library) + 1, np.uint32)
+        off[1:] = np.cumsum([len(sc["rigid"]) for sc in library])
+        cat = lambda k, dt: np.ascontiguousarray(np.concatenate([np.asarray(sc[k]).reshape(len(sc[k]), -1) for sc in library]), dt)  # noqa: E731
+        rigid = np.ascontiguousarray(np.concatenate([sc["rigid"] for sc in library]))
+        types, geoms, fr = cat("types", np.int32), cat("geoms", np.float32), cat("friction", np.float32)
+        spose, stype, sgeom = cat("static_poses", np.float32), cat("static_types", np.int32), cat("static_geoms", np.float32)
+        out = np.zeros(16, np.float64)
+        check(self._L.gbpx_server_run_load(self._h, float(seconds), float(rate), int(steps[0]), int(steps[1]), int(life[0]), int(life[1]),
+                                           int(seed), len(library), _p(off), _p(rigid), _p(types), _p(geoms), _p(fr), _p(spose), _p(stype),
+                                           _p(sgeom), _p(out)), "gbpx_server_run_load")
+        keys = ("seconds", "submitted", "completed", "body_steps", "p50_ms", "p99_ms", "p50_ms_512", "p99_ms_512", "p50_ms_per_step_512",
+                "p99_ms_per_step_512", "live_scenes", "retired", "admitted_after_start", "lane_steps", "lanes")
+        return {k: float(v) for k, v in zip(keys, out)}

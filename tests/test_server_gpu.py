@@ -77,3 +77,47 @@ def test_admission_budget_and_retirement(cuda_device):
     s.admit(parts[3])          # the slot is free again
     assert s.stats()["live"] == 2
     s.release()
+
+
+def test_scene_result_same_with_lanes_and_classes(cuda_device):
+    """Scenes of several body-count classes, each class split into two lanes, served
+    in a mix of requests: every scene's bodies equal the batched world's after the
+    same number of steps."""
+    from physx_gb300.server import Server
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(83, 6, nmin=20, nmax=200)
+    parts = [one_scene(scenes, k) for k in range(6)]
+    s = Server([32, 64, 128, 256], [2, 2, 2, 2], lanes_per_class=2)
+    ids = [s.admit(p) for p in parts]
+    rng = np.random.default_rng(1)
+    owed = [0] * len(ids)
+    tag = 0
+    for _ in range(4):
+        for k, sid in enumerate(ids):
+            n = int(rng.integers(1, 4))
+            s.submit(sid, n, tag)
+            owed[k] += n
+            tag += 1
+        s.pump()
+    tags, _ = s.drain()
+    assert sorted(tags) == list(range(tag))
+    for k, sid in enumerate(ids):
+        got = s.read_scene(sid)
+        w = World(parts[k])
+        w.step(owed[k])
+        assert np.array_equal(got.view(np.uint8), w.get_bodies().view(np.uint8)), k
+        w.release()
+    s.release()
+
+
+def test_native_poisson_load_retires_and_readmits(cuda_device):
+    """The open-loop load run in the library (gbpx_server_run_load): requests
+    complete, scenes that reach their lifetime are retired and replaced, and the
+    figures are consistent."""
+    from physx_gb300.serve_load import run_poisson
+    r = run_poisson(duration=2.0, rate=3000.0, budget_bytes=2e9, nmin=16, nmax=256, life=(5, 30), seed=9, per_class=3, lanes_per_class=2)
+    assert r["completed"] > 1000 and r["completed"] <= r["submitted"]
+    assert r["retired"] > 0 and r["admitted_after_start"] > 0
+    assert r["body_steps_per_s"] > 0 and r["p50_ms"] > 0 and r["p99_ms"] >= r["p50_ms"]
+    assert r["lanes"] == 2 * len(r["classes"])
