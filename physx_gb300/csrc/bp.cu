@@ -246,13 +246,15 @@ __global__ void sweepUpdatedKernel(const uint32_t* __restrict__ updPos, uint32_t
 // later in sorted order (pairs whose first box in sorted order did not move).
 // A box whose X range covers more than SLEEP_SCAN_MAX updated boxes (a static
 // ground plane covers all of them) is handed to sweepLongKernel as (box, first,
-// end) so that no thread runs a long serial scan.
+// end, first chunk) so that no thread runs a long serial scan: its candidates
+// are cut into chunks of LONG_CHUNK that any block may take.
 constexpr uint32_t SLEEP_SCAN_MAX = 256;
+constexpr uint32_t LONG_CHUNK = 1024;
 __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint32_t nbSleep, const uint32_t* __restrict__ updPos,
                                     uint32_t nbUpd, const uint2* __restrict__ sx, const float4* __restrict__ syz,
                                     const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds, uint32_t lutLo,
                                     uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter,
-                                    uint3* __restrict__ longScans, uint32_t* __restrict__ longCount)
+                                    uint4* __restrict__ longScans, unsigned long long* __restrict__ longCount)
 {
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31;
@@ -285,7 +287,11 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
 		}
 		if(a - lo > SLEEP_SCAN_MAX)
 		{
-			longScans[atomicAdd(longCount, 1u)] = make_uint3(p, lo, a);
+			// one atomic counts the item (high word) and its chunks (low word), so the
+			// items are numbered in increasing order of their first chunk
+			const unsigned long long chunks = (a - lo + LONG_CHUNK - 1) / LONG_CHUNK;
+			const unsigned long long old = atomicAdd(longCount, (1ull << 32) | chunks);
+			longScans[uint32_t(old >> 32)] = make_uint4(p, lo, a, uint32_t(old));
 			lo = nbUpd;
 		}
 	}
@@ -325,28 +331,37 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
 	}
 }
 
-// The long scans of pass 2: a block per (box, first, end) item, its threads
-// striding over the candidates.
-__global__ void __launch_bounds__(256) sweepLongKernel(const uint3* __restrict__ longScans, const uint32_t* __restrict__ longCount,
+// The long scans of pass 2: blocks take chunks of LONG_CHUNK candidates of any
+// item (its box against updated boxes [first, end)), threads striding over a chunk.
+__global__ void __launch_bounds__(256) sweepLongKernel(const uint4* __restrict__ longScans, const unsigned long long* __restrict__ longCount,
                                                        const uint32_t* __restrict__ updPos, const uint2* __restrict__ sx,
                                                        const float4* __restrict__ syz, const uint32_t* __restrict__ sgrp,
                                                        const uint32_t* __restrict__ sortedIds, uint32_t lutLo, uint32_t lutHi,
                                                        unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
 {
-	const uint32_t count = *longCount;
-	for(uint32_t item = blockIdx.x; item < count; item += gridDim.x)
+	const unsigned long long lc = *longCount;
+	const uint32_t items = uint32_t(lc >> 32), chunks = uint32_t(lc);
+	for(uint32_t g = blockIdx.x; g < chunks; g += gridDim.x)
 	{
-		const uint3 ls = longScans[item];
+		// the item holding chunk g: the last whose first chunk is <= g
+		uint32_t a = 0, b = items;
+		while(b - a > 1)
+		{
+			const uint32_t m = (a + b) >> 1;
+			if(longScans[m].w <= g) a = m; else b = m;
+		}
+		const uint4 ls = longScans[a];
 		const uint32_t p = ls.x;
 		const float4 yz0 = syz[p];
 		const uint32_t g0 = sgrp[p];
 		const uint32_t id0 = sortedIds[p];
-		for(uint32_t u0 = ls.y; u0 < ls.z; u0 += blockDim.x)
+		const uint32_t first = ls.y + (g - ls.w) * LONG_CHUNK, end = min(ls.z, first + LONG_CHUNK);
+		for(uint32_t u0 = first; u0 < end; u0 += blockDim.x)
 		{
 			const uint32_t u = u0 + threadIdx.x;
 			bool hit = false;
 			uint32_t idq = 0;
-			if(u < ls.z)
+			if(u < end)
 			{
 				const uint32_t q = updPos[u];
 				idq = sortedIds[q];
@@ -462,7 +477,7 @@ struct BroadPhase
 	DevBuf<uint32_t> sgrp, supd, updPos, sleepPos;
 	DevBuf<unsigned long long> found, foundAlt, prev, next, created, lost;
 	DevBuf<uint32_t> counter, cls, sel, pos;
-	DevBuf<uint3> longScans;
+	DevBuf<uint4> longScans;
 	DevBuf<uint2> createdPairs, lostPairs;
 	HostBuf<uint32_t> hCounts;
 	HostBuf<uint2> hCreated, hLost;
@@ -646,7 +661,7 @@ struct BroadPhase
 		if(found.reserve(1024) || foundAlt.reserve(1024) || longScans.reserve(size_t(nbSleep) + 1)) return GBPX_ERR_NOMEM;
 		for(int attempt = 0; attempt < 3; attempt++)
 		{
-			GBPX_CUDA_TRY(cudaMemsetAsync(counter.ptr, 0, 8, stream));
+			GBPX_CUDA_TRY(cudaMemsetAsync(counter.ptr, 0, 16, stream));
 			const uint32_t capF = uint32_t(std::min<size_t>(found.cap, 0xffffffffu));
 			if(nbUpd)
 			{
@@ -658,9 +673,11 @@ struct BroadPhase
 				{
 					bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
 					                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
-					                                                                 counter.ptr, longScans.ptr, counter.ptr + 1);
-					bp::sweepLongKernel<<<std::min<uint32_t>(nbSleep, 152u * 4u), 256, 0, stream>>>(
-					    longScans.ptr, counter.ptr + 1, updPos.ptr, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF, counter.ptr);
+					                                                                 counter.ptr, longScans.ptr,
+					                                                                 reinterpret_cast<unsigned long long*>(counter.ptr + 2));
+					bp::sweepLongKernel<<<152u * 4u, 256, 0, stream>>>(longScans.ptr, reinterpret_cast<const unsigned long long*>(counter.ptr + 2),
+					                                                    updPos.ptr, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr,
+					                                                    capF, counter.ptr);
 				}
 			}
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, counter.ptr, 4, cudaMemcpyDeviceToHost, stream));
