@@ -263,7 +263,7 @@ def bench_broadphase(frames, cpu_frames):
         return 36 * len(fr["updated"]) + 28 * n_total + 16 * active + 8 * (created + lost)
 
     bp = BroadPhase()
-    times, pairs, byts = [], [], []
+    times, pairs, byts, dev_ms, host_ms = [], [], [], [], []
     for f, fr in enumerate(aabb_stress_frames(frames=frames + 1)):
         t = time.perf_counter()
         bp.update(fr["created"], fr["updated"], fr["removed"], fr["bounds"], fr["groups"], fr["distances"], fr["capacity"])
@@ -272,6 +272,9 @@ def bench_broadphase(frames, cpu_frames):
         st = bp.stats()
         if f == 0:
             continue   # the first frame creates every box
+        hm, dm = bp.timing()
+        host_ms.append(hm)
+        dev_ms.append(dm)
         times.append(dt)
         pairs.append(st["active"] + len(c) + len(l))
         byts.append(algorithmic(fr, st["live"], st["active"], len(c), len(l)))
@@ -289,6 +292,7 @@ def bench_broadphase(frames, cpu_frames):
     cpu_ms = 1000.0 * float(np.median(ct))
     return dict(workload="1M AABBs U(0,1000)^3, half-extents lognormal(ln 0.5, 0.5), all dynamic, distance 0; 10% moved N(0, 0.2 m) per frame",
                 frames=frames, ms_per_frame=ms, value=pairs[k] / (ms / 1000.0), unit="pairs/s (active + created + lost)",
+                device_ms_per_frame=float(np.median(dev_ms)), host_staging_ms_per_frame=float(np.median(host_ms)),
                 e2e_note="host arrays in, created/lost pairs out (PxBroadPhase::update + fetchResults)",
                 algorithmic_gbs=byts[k] / (ms / 1000.0) / 1e9,
                 cpu_baseline=dict(value=pairs[k] / (cpu_ms / 1000.0), ms_per_frame=cpu_ms, unit="pairs/s", cores=1, kind="port",

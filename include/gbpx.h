@@ -68,6 +68,13 @@ int gbpx_bp_fetch_results(void* broadPhase, const uint32_t** createdPairs, uint3
                           uint32_t* nbLost);
 /* live boxes, updated boxes, found pairs, active pairs of the last update */
 int gbpx_bp_stats(void* broadPhase, uint64_t* out4);
+/* sweep kernels of the following updates: 1 = shared-memory tiled (default),
+ * 0 = one warp per updated box / one thread per other box; both find the same pairs */
+int gbpx_bp_set_sweep(void* broadPhase, int tiled);
+/* timing of the last update + fetchResults: out2[0] host milliseconds staging the
+ * user's arrays, out2[1] device milliseconds from the first upload to the results
+ * in host memory (CUDA events) */
+int gbpx_bp_timing(void* broadPhase, float* out2);
 /* PxGetBroadPhaseStaticFilterGroup / DynamicFilterGroup / KinematicFilterGroup
  * (physx/include/PxBroadPhase.h:264-291) */
 uint32_t gbpx_bp_static_filter_group(void);

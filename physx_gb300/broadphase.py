@@ -89,6 +89,19 @@ class BroadPhase:
         lost = np.ctypeslib.as_array(lp, shape=(nl.value * 2,)).reshape(-1, 2).copy() if nl.value else np.zeros((0, 2), np.uint32)
         return created, lost
 
+    def set_sweep(self, tiled):
+        """Sweep kernels for the following updates: True = shared-memory tiled (default),
+        False = one warp per updated box / one thread per other box (same pairs)."""
+        self._L.gbpx_bp_set_sweep.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        check(self._L.gbpx_bp_set_sweep(self._h, 1 if tiled else 0), "gbpx_bp_set_sweep")
+
+    def timing(self):
+        """(host ms staging the user's arrays, device ms) of the last update + fetch."""
+        out = np.zeros(2, np.float32)
+        self._L.gbpx_bp_timing.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        check(self._L.gbpx_bp_timing(self._h, _ptr(out)), "gbpx_bp_timing")
+        return float(out[0]), float(out[1])
+
     def stats(self):
         out = np.zeros(4, np.uint64)
         check(self._L.gbpx_bp_stats(self._h, _ptr(out)), "gbpx_bp_stats")

@@ -22,6 +22,7 @@
 // keys (id0 << 32 | id1, id0 < id1), so created/lost lists come out sorted and
 // deterministic.
 #include "common.cuh"
+#include <chrono>
 #include "bp_internal.h"
 #include "radix_sort.cuh"
 #include <vector>
@@ -48,6 +49,22 @@ static_assert(sizeof(UpdateRec) == 40, "UpdateRec layout");
 __device__ __forceinline__ bool lutAllows(uint32_t t0, uint32_t t1, uint32_t lutBits)
 {
 	return (lutBits >> (t0 * 7 + t1)) & 1u;
+}
+
+// The group filter's table row for a box of group g0: bit t1 set when a box of
+// type t1 < 7 may pair with it (bit 7 stays clear, type 7 never pairs); zero for
+// a box of type 7.  groupRowAllows(g0, groupRow(g0), g1) == groupFilter(g0, g1).
+__device__ __forceinline__ uint32_t groupRow(uint32_t g0, uint32_t lutLo, uint32_t lutHi)
+{
+	const uint32_t t0 = g0 & 7u;
+	if(t0 >= 7u) return 0u;
+	const unsigned long long bits = (static_cast<unsigned long long>(lutHi) << 32) | lutLo;
+	return uint32_t(bits >> (t0 * 7u)) & 0x7fu;
+}
+
+__device__ __forceinline__ bool groupRowAllows(uint32_t g0, uint32_t row, uint32_t g1)
+{
+	return (g0 != g1) & (((row >> (g1 & 7u)) & 1u) != 0u);
 }
 
 __device__ __forceinline__ bool groupFilter(uint32_t g0, uint32_t g1, uint32_t lutLo, uint32_t lutHi)
@@ -331,8 +348,10 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
 	}
 }
 
-// The long scans of pass 2: blocks take chunks of LONG_CHUNK candidates of any
-// item (its box against updated boxes [first, end)), threads striding over a chunk.
+// The long scans of pass 2: warps take chunks of LONG_CHUNK candidates of any
+// item (its box against updated boxes [first, end)), lanes striding over a chunk.
+// The item holding chunk g (the last whose first chunk is <= g) is found by a
+// 32-way search: each step the lanes probe 32 evenly spaced items.
 __global__ void __launch_bounds__(256) sweepLongKernel(const uint4* __restrict__ longScans, const unsigned long long* __restrict__ longCount,
                                                        const uint32_t* __restrict__ updPos, const uint2* __restrict__ sx,
                                                        const float4* __restrict__ syz, const uint32_t* __restrict__ sgrp,
@@ -341,33 +360,260 @@ __global__ void __launch_bounds__(256) sweepLongKernel(const uint4* __restrict__
 {
 	const unsigned long long lc = *longCount;
 	const uint32_t items = uint32_t(lc >> 32), chunks = uint32_t(lc);
-	for(uint32_t g = blockIdx.x; g < chunks; g += gridDim.x)
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nWarps = (gridDim.x * blockDim.x) >> 5;
+	for(uint32_t g = warpId; g < chunks; g += nWarps)
 	{
-		// the item holding chunk g: the last whose first chunk is <= g
+		// invariant: longScans[a].w <= g, and b == items or longScans[b].w > g
 		uint32_t a = 0, b = items;
-		while(b - a > 1)
+		while(b - a > 32)
 		{
-			const uint32_t m = (a + b) >> 1;
-			if(longScans[m].w <= g) a = m; else b = m;
+			const uint32_t step = (b - a + 31) / 32;
+			const uint32_t idx = a + lane * step;
+			const bool le = idx < b && longScans[idx].w <= g;
+			const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, le));   // a prefix of the lanes
+			a += (cnt - 1) * step;
+			b = min(b, a + step);
 		}
+		const bool le = a + lane < b && longScans[a + lane].w <= g;
+		a += __popc(__ballot_sync(0xffffffffu, le)) - 1;
 		const uint4 ls = longScans[a];
 		const uint32_t p = ls.x;
 		const float4 yz0 = syz[p];
-		const uint32_t g0 = sgrp[p];
+		const uint32_t g0 = sgrp[p], row = groupRow(g0, lutLo, lutHi);
 		const uint32_t id0 = sortedIds[p];
 		const uint32_t first = ls.y + (g - ls.w) * LONG_CHUNK, end = min(ls.z, first + LONG_CHUNK);
-		for(uint32_t u0 = first; u0 < end; u0 += blockDim.x)
+		for(uint32_t u0 = first; u0 < end; u0 += 32)
 		{
-			const uint32_t u = u0 + threadIdx.x;
+			const uint32_t u = u0 + lane;
 			bool hit = false;
 			uint32_t idq = 0;
 			if(u < end)
 			{
 				const uint32_t q = updPos[u];
-				idq = sortedIds[q];
-				hit = overlapYZ(yz0, syz[q]) && groupFilter(g0, sgrp[q], lutLo, lutHi);
+				hit = overlapYZ(yz0, syz[q]) && groupRowAllows(g0, row, sgrp[q]);
+				if(hit) idq = sortedIds[q];
 			}
 			emitPairs(__ballot_sync(0xffffffffu, hit), id0, idq, out, cap, counter);
+		}
+	}
+}
+
+// Pass 1, tiled: a block takes UPD_PER_BLOCK consecutive updated boxes (in
+// sorted order, so their candidate ranges overlap) and streams the union of the
+// ranges through shared memory in tiles of SWEEP_TILE sorted positions; each
+// warp tests its UPD_PER_WARP boxes against each tile, lanes striding over the
+// positions.  The end of a box's range within the tile (the first later position
+// whose min X is past its max X) is found first by a 32-way search of the
+// tile's min X keys, which ascend.  The candidates are read from memory about
+// once per block instead of once per box, and tiles that no unfinished box
+// reaches are skipped.  Finds the same pairs as sweepUpdatedKernel.
+constexpr uint32_t UPD_PER_WARP = 8;
+constexpr uint32_t UPD_PER_BLOCK = 8 * UPD_PER_WARP;   // 8 warps
+constexpr uint32_t SWEEP_TILE = 1024;
+__global__ void __launch_bounds__(256) sweepUpdatedTiledKernel(const uint32_t* __restrict__ updPos, uint32_t nbUpd, uint32_t n,
+                                                               const uint2* __restrict__ sx, const float4* __restrict__ syz,
+                                                               const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds,
+                                                               uint32_t lutLo, uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap,
+                                                               uint32_t* __restrict__ counter)
+{
+	__shared__ uint32_t tMinX[SWEEP_TILE], tGrp[SWEEP_TILE], tId[SWEEP_TILE];
+	__shared__ float4 tYZ[SWEEP_TILE];
+	__shared__ uint32_t warpNext[8];
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for(uint32_t blk = blockIdx.x; blk * UPD_PER_BLOCK < nbUpd; blk += gridDim.x)
+	{
+		const uint32_t k0 = blk * UPD_PER_BLOCK;
+		// lane j < UPD_PER_WARP holds box k0 + warp * UPD_PER_WARP + j
+		const uint32_t kb = k0 + warp * UPD_PER_WARP + lane;
+		bool pending = lane < UPD_PER_WARP && kb < nbUpd;
+		uint32_t bp = 0, bMaxX = 0, bGrp = 0, bRow = 0, bId = 0;
+		float4 bYZ = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		if(pending)
+		{
+			bp = updPos[kb];
+			bMaxX = sx[bp].y;
+			bYZ = syz[bp];
+			bGrp = sgrp[bp];
+			bRow = groupRow(bGrp, lutLo, lutHi);
+			bId = sortedIds[bp];
+			pending = bp + 1 < n;
+		}
+		uint32_t tileStart = updPos[k0] + 1;   // updPos ascends: the block's first box comes first
+		while(tileStart < n)
+		{
+			const uint32_t tileEnd = min(n, tileStart + SWEEP_TILE);
+			__syncthreads();
+			for(uint32_t i = threadIdx.x; tileStart + i < tileEnd; i += blockDim.x)
+			{
+				const uint32_t q = tileStart + i;
+				tMinX[i] = sx[q].x;
+				tYZ[i] = syz[q];
+				tGrp[i] = sgrp[q];
+				tId[i] = sortedIds[q];
+			}
+			__syncthreads();
+			for(uint32_t j = 0; j < UPD_PER_WARP; j++)
+			{
+				if(!__shfl_sync(0xffffffffu, pending ? 1u : 0u, j)) continue;
+				const uint32_t p = __shfl_sync(0xffffffffu, bp, j);
+				const uint32_t first = max(p + 1, tileStart);
+				if(first >= tileEnd) continue;
+				const uint32_t maxX = __shfl_sync(0xffffffffu, bMaxX, j);
+				// end of the range in this tile: positions in [a, end) are in range, [end, b) are not
+				uint32_t a = first, b = tileEnd;
+				while(b - a > 32)
+				{
+					const uint32_t step = (b - a + 31) >> 5;
+					const uint32_t idx = a + lane * step;
+					const bool le = idx < b && tMinX[idx - tileStart] <= maxX;
+					const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, le));   // a prefix of the lanes
+					if(cnt == 0) { b = a; break; }
+					const uint32_t hiB = a + cnt * step;
+					a += (cnt - 1) * step + 1;
+					b = min(b, hiB);
+				}
+				const uint32_t end = a + __popc(__ballot_sync(0xffffffffu, a + lane < b && tMinX[min(a + lane, tileEnd - 1) - tileStart] <= maxX));
+				if(end < tileEnd && lane == j) pending = false;   // the range ends inside this tile
+				if(end <= first) continue;
+				const uint32_t g0 = __shfl_sync(0xffffffffu, bGrp, j), row = __shfl_sync(0xffffffffu, bRow, j);
+				const uint32_t id0 = __shfl_sync(0xffffffffu, bId, j);
+				const float4 yz0 = make_float4(__shfl_sync(0xffffffffu, bYZ.x, j), __shfl_sync(0xffffffffu, bYZ.y, j),
+				                               __shfl_sync(0xffffffffu, bYZ.z, j), __shfl_sync(0xffffffffu, bYZ.w, j));
+				for(uint32_t q0 = first; q0 < end; q0 += 32)
+				{
+					const uint32_t q = q0 + lane;
+					bool hit = false;
+					uint32_t idq = 0;
+					if(q < end)
+					{
+						const uint32_t i = q - tileStart;
+						hit = overlapYZ(yz0, tYZ[i]) && groupRowAllows(g0, row, tGrp[i]);
+						if(hit) idq = tId[i];
+					}
+					const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+					if(hm) emitPairs(hm, id0, idq, out, cap, counter);
+				}
+			}
+			// next tile: the smallest position an unfinished box still has to scan
+			uint32_t next = pending ? max(bp + 1, tileEnd) : 0xffffffffu;
+			next = __reduce_min_sync(0xffffffffu, next);
+			if(lane == 0) warpNext[warp] = next;
+			__syncthreads();
+			next = warpNext[0];
+			for(uint32_t w = 1; w < 8; w++) next = min(next, warpNext[w]);
+			tileStart = next;   // all ones when every box is done
+		}
+	}
+}
+
+// Pass 2, tiled: a block takes SLEEP_PER_BLOCK consecutive non-updated boxes (in
+// sorted order), one per thread.  Each finds its candidates (updated boxes later
+// in sorted order whose min X is within its X range) as sweepSleepingKernel does,
+// handing a range longer than SLEEP_SCAN_MAX to the long-scan list.  The updated
+// boxes of the union of the block's ranges are gathered into shared memory a tile
+// at a time; each warp then takes its 32 boxes one after another, lanes striding
+// over the box's candidates in the tile.  Finds the same pairs as
+// sweepSleepingKernel.
+constexpr uint32_t SLEEP_PER_BLOCK = 256;
+constexpr uint32_t SLEEP_TILE = 1024;
+struct SleepBox
+{
+	float4 yz;
+	uint32_t lo, hi, grp, id;
+};
+__global__ void __launch_bounds__(256) sweepSleepingTiledKernel(const uint32_t* __restrict__ sleepPos, uint32_t nbSleep,
+                                                                const uint32_t* __restrict__ updPos, uint32_t nbUpd,
+                                                                const uint2* __restrict__ sx, const float4* __restrict__ syz,
+                                                                const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds,
+                                                                uint32_t lutLo, uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap,
+                                                                uint32_t* __restrict__ counter, uint4* __restrict__ longScans,
+                                                                unsigned long long* __restrict__ longCount)
+{
+	__shared__ uint32_t tGrp[SLEEP_TILE], tId[SLEEP_TILE];
+	__shared__ float4 tYZ[SLEEP_TILE];
+	__shared__ SleepBox boxes[SLEEP_PER_BLOCK];
+	__shared__ uint32_t sLo, sHi;
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for(uint32_t blk = blockIdx.x; blk * SLEEP_PER_BLOCK < nbSleep; blk += gridDim.x)
+	{
+		const uint32_t k = blk * SLEEP_PER_BLOCK + threadIdx.x;
+		__syncthreads();   // the previous box set is done with the shared state
+		if(threadIdx.x == 0) { sLo = 0xffffffffu; sHi = 0; }
+		__syncthreads();
+		SleepBox box{make_float4(0.0f, 0.0f, 0.0f, 0.0f), 0u, 0u, 0u, 0u};
+		if(k < nbSleep)
+		{
+			const uint32_t p = sleepPos[k];
+			const uint2 x0 = sx[p];
+			box.yz = syz[p];
+			box.grp = sgrp[p];
+			box.id = sortedIds[p];
+			// sleepPos and updPos partition the sorted positions, both ascending: the
+			// updated boxes before position p number p - k
+			const uint32_t lo = p - k;
+			// end of the candidates (their min X ascends with the position), searched
+			// within SLEEP_SCAN_MAX + 1 of lo unless the range is a long one
+			uint32_t a = lo, b = min(nbUpd, lo + SLEEP_SCAN_MAX + 1);
+			if(b == lo + SLEEP_SCAN_MAX + 1 && sx[updPos[b - 1]].x <= x0.y) { a = b; b = nbUpd; }
+			while(a < b)
+			{
+				const uint32_t m = (a + b) >> 1;
+				if(sx[updPos[m]].x <= x0.y) a = m + 1; else b = m;
+			}
+			uint32_t hi = a;
+			if(hi - lo > SLEEP_SCAN_MAX)
+			{
+				const unsigned long long chunks = (hi - lo + LONG_CHUNK - 1) / LONG_CHUNK;
+				const unsigned long long old = atomicAdd(longCount, (1ull << 32) | chunks);
+				longScans[uint32_t(old >> 32)] = make_uint4(p, lo, hi, uint32_t(old));
+				hi = lo;
+			}
+			box.lo = lo;
+			box.hi = hi;
+			if(hi > lo)
+			{
+				atomicMin(&sLo, lo);
+				atomicMax(&sHi, hi);
+			}
+		}
+		boxes[threadIdx.x] = box;
+		__syncthreads();
+		const uint32_t uLo = sLo, uHi = sHi;
+		for(uint32_t t0 = uLo; t0 < uHi; t0 += SLEEP_TILE)
+		{
+			const uint32_t t1 = min(uHi, t0 + SLEEP_TILE);
+			for(uint32_t i = threadIdx.x; t0 + i < t1; i += blockDim.x)
+			{
+				const uint32_t q = updPos[t0 + i];
+				tYZ[i] = syz[q];
+				tGrp[i] = sgrp[q];
+				tId[i] = sortedIds[q];
+			}
+			__syncthreads();
+			for(uint32_t j = 0; j < 32; j++)
+			{
+				const SleepBox& bx = boxes[warp * 32 + j];
+				const uint32_t a = max(bx.lo, t0), b = min(bx.hi, t1);
+				if(a >= b) continue;
+				const float4 yz0 = bx.yz;
+				const uint32_t g0 = bx.grp, id0 = bx.id, row = groupRow(g0, lutLo, lutHi);
+				for(uint32_t u0 = a; u0 < b; u0 += 32)
+				{
+					const uint32_t u = u0 + lane;
+					bool hit = false;
+					uint32_t idq = 0;
+					if(u < b)
+					{
+						const uint32_t i = u - t0;
+						hit = overlapYZ(yz0, tYZ[i]) && groupRowAllows(g0, row, tGrp[i]);
+						if(hit) idq = tId[i];
+					}
+					const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+					if(hm) emitPairs(hm, id0, idq, out, cap, counter);
+				}
+			}
+			__syncthreads();
 		}
 	}
 }
@@ -485,6 +731,11 @@ struct BroadPhase
 	uint32_t nbCreatedOut = 0, nbLostOut = 0;
 	bool pending = false;
 	uint64_t stats[4] = {0, 0, 0, 0};  // live boxes, updated boxes, found pairs, active pairs (last update)
+	// timing of the last update: host staging of the user's arrays (ms), and the
+	// device work from the first upload to the results in host memory (CUDA events)
+	float lastHostMs = 0.0f, lastDeviceMs = 0.0f;
+	int sweepTiled = 1;   // 1: shared-memory tiled sweeps, 0: one warp / thread per box
+	cudaEvent_t evBegin = nullptr, evEnd = nullptr;
 
 	int init(bool discardStaticKinematic, bool discardKinematicKinematic)
 	{
@@ -523,6 +774,9 @@ struct BroadPhase
 		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
 		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release(); longScans.release();
 		hCounts.release(); hCreated.release(); hLost.release();
+		if(evBegin) cudaEventDestroy(evBegin);
+		if(evEnd) cudaEventDestroy(evEnd);
+		evBegin = evEnd = nullptr;
 		if(stream) cudaStreamDestroy(stream);
 		stream = 0;
 	}
@@ -595,18 +849,29 @@ struct BroadPhase
 		const uint32_t nbRec = nbCreated + nbUpdated;
 		if(hRecs.reserve(nbRec ? nbRec : 1) || dRecs.reserve(nbRec ? nbRec : 1) || dRemoved.reserve(nbRemoved ? nbRemoved : 1))
 			return GBPX_ERR_NOMEM;
-		for(uint32_t i = 0; i < nbRec; i++)
-		{
-			const bool isC = i < nbCreated;
-			const uint32_t id = isC ? createdIds[i] : updatedIds[i - nbCreated];
-			bp::UpdateRec& r = hRecs.ptr[i];
-			r.id = id;
-			r.group = isC ? groupsIn[id] : 0u;
-			r.dist = distances[id];
-			memcpy(r.mn, bounds + 6 * size_t(id), 12);
-			memcpy(r.mx, bounds + 6 * size_t(id) + 3, 12);
-			r.isCreate = isC ? 1u : 0u;
-		}
+		const auto hostBegin = std::chrono::steady_clock::now();
+		auto gather = [&](uint32_t begin, uint32_t end) {
+			for(uint32_t i = begin; i < end; i++)
+			{
+				const bool isC = i < nbCreated;
+				const uint32_t id = isC ? createdIds[i] : updatedIds[i - nbCreated];
+				bp::UpdateRec& r = hRecs.ptr[i];
+				r.id = id;
+				r.group = isC ? groupsIn[id] : 0u;
+				r.dist = distances[id];
+				memcpy(r.mn, bounds + 6 * size_t(id), 12);
+				memcpy(r.mx, bounds + 6 * size_t(id) + 3, 12);
+				r.isCreate = isC ? 1u : 0u;
+			}
+		};
+		// the gather reads the user's arrays at random handles: large batches are
+		// split over the host worker pool
+		if(nbRec >= (1u << 15)) hostParallelFor(nbRec, 4096, gather);
+		else gather(0, nbRec);
+		lastHostMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hostBegin).count();
+		if(!evBegin) GBPX_CUDA_TRY(cudaEventCreate(&evBegin));
+		if(!evEnd) GBPX_CUDA_TRY(cudaEventCreate(&evEnd));
+		GBPX_CUDA_TRY(cudaEventRecord(evBegin, stream));
 		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
 		if(nbRemoved)
 		{
@@ -665,17 +930,27 @@ struct BroadPhase
 			const uint32_t capF = uint32_t(std::min<size_t>(found.cap, 0xffffffffu));
 			if(nbUpd)
 			{
-				const uint32_t warps = nbUpd;
-				const uint32_t blocks = std::min<uint32_t>(divUp(uint64_t(warps) * 32, 256), 152u * 64u);
-				bp::sweepUpdatedKernel<<<blocks, 256, 0, stream>>>(updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
-				                                                  found.ptr, capF, counter.ptr);
+				unsigned long long* longCount = reinterpret_cast<unsigned long long*>(counter.ptr + 2);
+				if(sweepTiled)
+					bp::sweepUpdatedTiledKernel<<<std::min<uint32_t>(divUp(nbUpd, bp::UPD_PER_BLOCK), 152u * 64u), 256, 0, stream>>>(
+					    updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF, counter.ptr);
+				else
+				{
+					const uint32_t blocks = std::min<uint32_t>(divUp(uint64_t(nbUpd) * 32, 256), 152u * 64u);
+					bp::sweepUpdatedKernel<<<blocks, 256, 0, stream>>>(updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
+					                                                  found.ptr, capF, counter.ptr);
+				}
 				if(nbSleep)
 				{
-					bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
-					                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
-					                                                                 counter.ptr, longScans.ptr,
-					                                                                 reinterpret_cast<unsigned long long*>(counter.ptr + 2));
-					bp::sweepLongKernel<<<152u * 4u, 256, 0, stream>>>(longScans.ptr, reinterpret_cast<const unsigned long long*>(counter.ptr + 2),
+					if(sweepTiled)
+						bp::sweepSleepingTiledKernel<<<std::min<uint32_t>(divUp(nbSleep, bp::SLEEP_PER_BLOCK), 152u * 64u), 256, 0, stream>>>(
+						    sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
+						    counter.ptr, longScans.ptr, longCount);
+					else
+						bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
+						                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
+						                                                                 counter.ptr, longScans.ptr, longCount);
+					bp::sweepLongKernel<<<152u * 8u, 256, 0, stream>>>(longScans.ptr, reinterpret_cast<const unsigned long long*>(counter.ptr + 2),
 					                                                    updPos.ptr, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr,
 					                                                    capF, counter.ptr);
 				}
@@ -751,6 +1026,7 @@ struct BroadPhase
 			bp::keysToPairsKernel<<<divUp(nLost, 256), 256, 0, stream>>>(lost.ptr, nLost, lostPairs.ptr);
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hLost.ptr, lostPairs.ptr, size_t(nLost) * 8, cudaMemcpyDeviceToHost, stream));
 		}
+		if(evEnd) GBPX_CUDA_TRY(cudaEventRecord(evEnd, stream));
 		nbCreatedOut = nCreated;
 		nbLostOut = nLost;
 		stats[0] = n; stats[1] = nbUpd; stats[2] = nFound; stats[3] = nPrev;
@@ -780,6 +1056,7 @@ struct BroadPhase
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		GBPX_CUDA_TRY(cudaGetLastError());
 		pending = false;
+		if(evBegin && evEnd && cudaEventElapsedTime(&lastDeviceMs, evBegin, evEnd) != cudaSuccess) lastDeviceMs = -1.0f;
 		*outCreated = hCreated.ptr;
 		*nbCreated = nbCreatedOut;
 		*outLost = hLost.ptr;
@@ -852,5 +1129,25 @@ GBPX_API int gbpx_bp_stats(void* bp, uint64_t* out4)
 {
 	if(!bp || !out4) return GBPX_ERR_INVALID;
 	memcpy(out4, static_cast<BroadPhase*>(bp)->stats, sizeof(uint64_t) * 4);
+	return GBPX_OK;
+}
+
+// Sweep kernels of the following updates: 1 = shared-memory tiled (default),
+// 0 = one warp per updated box and one thread per other box.  Same pairs.
+GBPX_API int gbpx_bp_set_sweep(void* bp, int tiled)
+{
+	if(!bp || (tiled != 0 && tiled != 1)) return GBPX_ERR_INVALID;
+	static_cast<BroadPhase*>(bp)->sweepTiled = tiled;
+	return GBPX_OK;
+}
+
+// Timing of the last update + fetchResults: out2[0] = host milliseconds staging
+// the user's arrays (the gather of the created and updated boxes), out2[1] =
+// device milliseconds from the first upload to the results in host memory.
+GBPX_API int gbpx_bp_timing(void* bp, float* out2)
+{
+	if(!bp || !out2) return GBPX_ERR_INVALID;
+	out2[0] = static_cast<BroadPhase*>(bp)->lastHostMs;
+	out2[1] = static_cast<BroadPhase*>(bp)->lastDeviceMs;
 	return GBPX_OK;
 }

@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
+#include <functional>
 
 #define GBPX_API extern "C" __attribute__((visibility("default")))
 
@@ -66,6 +67,14 @@ struct Zone
 	Zone(const Zone&) = delete;
 	Zone& operator=(const Zone&) = delete;
 };
+
+// Host-side parallel loop over [0, n) in chunks of `chunk` items, run by a
+// process-wide pool of worker threads (created on first use, at most 7 workers
+// plus the caller) so that large host gathers do not pay a thread start each
+// call.  fn(begin, end) must be safe to run concurrently on disjoint ranges.
+// Calls from several threads are serialised.  Falls back to the caller alone
+// when n <= chunk.
+void hostParallelFor(uint32_t n, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn);
 
 // Device buffer that only grows; contents are not preserved across growth unless asked.
 template <typename T>

@@ -3,6 +3,11 @@
 #include <cuda_profiler_api.h>
 #include <nvtx3/nvToolsExt.h>
 #include <atomic>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
+#include <vector>
+#include <unistd.h>
 
 GBPX_API int gbpx_device_count(int* out)
 {
@@ -76,6 +81,102 @@ void zoneCallbacks(ZoneStartFn* start, ZoneEndFn* end, void** user)
 
 void nvtxPush(const char* name) { nvtxRangePushA(name); }
 void nvtxPop() { nvtxRangePop(); }
+
+// ---- host worker pool ----
+namespace
+{
+// Workers sleep on a condition variable; a job hands out chunks through an
+// atomic counter that the caller drains too.  The pool is never destroyed (its
+// threads end with the process); a child process made by fork() gets a new one.
+struct HostPool
+{
+	std::mutex lock;     // guards the job fields below
+	std::mutex runLock;  // one job at a time
+	std::condition_variable wake, idle;
+	std::vector<std::thread> workers;
+	const std::function<void(uint32_t, uint32_t)>* job = nullptr;
+	std::atomic<uint32_t> next{0};
+	uint32_t total = 0, chunk = 0, busy = 0;
+	uint64_t generation = 0;
+
+	explicit HostPool(uint32_t nbWorkers)
+	{
+		for(uint32_t t = 0; t < nbWorkers; t++) workers.emplace_back([this] { loop(); });
+	}
+	void drain(const std::function<void(uint32_t, uint32_t)>& fn, uint32_t n, uint32_t c)
+	{
+		for(;;)
+		{
+			const uint32_t b = next.fetch_add(c);
+			if(b >= n) return;
+			fn(b, n - b < c ? n : b + c);
+		}
+	}
+	void loop()
+	{
+		uint64_t seen = 0;
+		for(;;)
+		{
+			const std::function<void(uint32_t, uint32_t)>* fn;
+			uint32_t n, c;
+			{
+				std::unique_lock<std::mutex> l(lock);
+				wake.wait(l, [&] { return generation != seen; });
+				seen = generation;
+				fn = job;
+				n = total;
+				c = chunk;
+			}
+			drain(*fn, n, c);
+			std::lock_guard<std::mutex> g(lock);
+			if(--busy == 0) idle.notify_one();
+		}
+	}
+	void run(uint32_t n, uint32_t c, const std::function<void(uint32_t, uint32_t)>& fn)
+	{
+		std::lock_guard<std::mutex> serial(runLock);
+		{
+			std::lock_guard<std::mutex> g(lock);
+			job = &fn;
+			total = n;
+			chunk = c;
+			next.store(0);
+			busy = uint32_t(workers.size());
+			generation++;
+		}
+		wake.notify_all();
+		drain(fn, n, c);
+		std::unique_lock<std::mutex> l(lock);
+		idle.wait(l, [&] { return busy == 0; });
+	}
+};
+std::mutex gPoolLock;
+HostPool* gPool = nullptr;
+pid_t gPoolPid = 0;
+} // namespace
+
+void hostParallelFor(uint32_t n, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn)
+{
+	if(chunk == 0) chunk = 1;
+	if(n <= chunk)
+	{
+		if(n) fn(0, n);
+		return;
+	}
+	HostPool* pool;
+	{
+		std::lock_guard<std::mutex> g(gPoolLock);
+		if(!gPool || gPoolPid != getpid())
+		{
+			const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+			gPool = new HostPool(std::min(7u, hw - 1));   // a pool left by the parent process is abandoned
+			gPoolPid = getpid();
+		}
+		pool = gPool;
+	}
+	if(pool->workers.empty()) fn(0, n);
+	else pool->run(n, chunk, fn);
+}
 } // namespace gbpx
 
 // Installs (or, with null functions, removes) the callbacks every profiler

@@ -21,8 +21,10 @@ def _run(bp, fr):
 
 
 @pytest.mark.parametrize("path", BP_FIXTURES, ids=[p.rsplit("/", 1)[-1] for p in BP_FIXTURES])
-def test_bp_matches_reference_golden(cuda_device, path):
+@pytest.mark.parametrize("tiled", [True, False], ids=["tiled", "per-box"])
+def test_bp_matches_reference_golden(cuda_device, path, tiled):
     bp = _gpu_bp()
+    bp.set_sweep(tiled)
     for f, fr in enumerate(load_bp_fixture(path)):
         created, lost = _run(bp, fr)
         # bit-exact sets; the GB300 lists also come out already sorted
@@ -31,10 +33,15 @@ def test_bp_matches_reference_golden(cuda_device, path):
     bp.release()
 
 
+@pytest.mark.parametrize("tiled", [True, False], ids=["tiled", "per-box"])
 @pytest.mark.parametrize("seed,n,frames,extent,move", [(31, 20000, 4, 60.0, 0.1), (32, 100000, 3, 300.0, 0.1),
-                                                         (33, 5000, 6, 8.0, 0.5)])
-def test_bp_matches_oracle(cuda_device, seed, n, frames, extent, move):
+                                                         (33, 5000, 6, 8.0, 0.5),
+                                                         # X ranges over ~1600 sorted positions (several shared-memory
+                                                         # tiles), with updated boxes sparse and then nearly all
+                                                         (34, 30000, 3, 20.0, 0.01), (35, 30000, 3, 20.0, 0.9)])
+def test_bp_matches_oracle(cuda_device, seed, n, frames, extent, move, tiled):
     bp, orc = _gpu_bp(), CpuBroadPhase("orc")
+    bp.set_sweep(tiled)
     for f, fr in enumerate(bp_frames(seed, n, frames, extent=extent, move_frac=move)):
         gc, gl = _run(bp, fr)
         oc, ol = orc.update(fr)
