@@ -22,6 +22,7 @@
 // per-pair path.  The results equal the reference's bit for bit (tests).
 #include "pxmath.h"
 #include "tgs_frame.h"
+#include "tgs_bodies.h"
 #include <string.h>
 #include <vector>
 #include <algorithm>
@@ -32,33 +33,6 @@ using namespace orc;
 
 namespace
 {
-struct RigidBodyData   // PxRigidBodyData, 96 bytes
-{
-	float linVel[3]; float invMass;
-	float angVel[3]; float maxDepenetrationVelocity;
-	float invInertia[3]; float maxContactImpulse;
-	float q[4]; float p[3];
-	float linearDamping, angularDamping, maxLinearVelocitySq, maxAngularVelocitySq;
-	uint32_t pad;
-};
-static_assert(sizeof(RigidBodyData) == 96, "PxRigidBodyData layout");
-
-struct BodyVel      // PxTGSSolverBodyVel fields used by the solver
-{
-	V3 lin, ang, dLin, dAng;
-	float maxAngVel;
-	bool kinematic;
-};
-struct BodyTx       // PxTGSSolverBodyTxInertia
-{
-	Q dq; V3 p; M33 sqrtInvInertia;
-};
-struct BodyData     // PxTGSSolverBodyData
-{
-	V3 origLin, origAng;
-	float maxContactImpulse, penBiasClamp, invMass;
-};
-
 struct PointRow { V3 raXnI, rbXnI; float velMultiplier, separation, biasCoefficient, targetVelocity, recipResponse, maxImpulse, force; };
 struct FrictionRow { V3 normal; float error; V3 raXnI; float targetVel; V3 rbXnI; float velMultiplier; float appliedForce, frictionScale, biasScale; };
 struct PatchRows
@@ -139,12 +113,6 @@ void copyToSolverBody(V3 lv, V3 av, float invMass, V3 invInertia, const Tr& pose
 }
 
 // ------------------------------------------------------------ batching
-struct BatchOut
-{
-	std::vector<int> order;              // ordered constraint indices
-	std::vector<uint32_t> headerStart, headerStride;
-};
-
 void batchConstraints(const uint32_t* bodyA, const uint32_t* bodyB, int n, int nbDyn, BatchOut& out)
 {
 	const uint32_t MAXP = 32;
@@ -1107,32 +1075,11 @@ uint32_t orc::tgsFrame(const void* rigid, uint32_t nbDyn, const float* staticPos
                   float correlationDistance, float* outVel, float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outOrder,
                   std::vector<std::vector<FrictionPatch>>* friction)
 {
-	const uint32_t nbTotal = nbDyn + nbStatic;
-	std::vector<BodyVel> vels(nbTotal);
-	std::vector<BodyTx> txs(nbTotal);
-	std::vector<BodyData> datas(nbTotal);
-	std::vector<Tr> poses(nbTotal);
-	const RigidBodyData* rb = static_cast<const RigidBodyData*>(rigid);
-	const V3 g = v3(gravity[0], gravity[1], gravity[2]);
-	for(uint32_t a = 0; a < nbDyn; a++)
-	{
-		const RigidBodyData& r = rb[a];
-		V3 lv = v3(r.linVel[0], r.linVel[1], r.linVel[2]);
-		V3 av = v3(r.angVel[0], r.angVel[1], r.angVel[2]);
-		unconstrainedVelocity(g, dt, r.linearDamping, r.angularDamping, r.maxLinearVelocitySq, r.maxAngularVelocitySq, lv, av);
-		Tr pose;
-		pose.q.x = r.q[0]; pose.q.y = r.q[1]; pose.q.z = r.q[2]; pose.q.w = r.q[3];
-		pose.p = v3(r.p[0], r.p[1], r.p[2]);
-		poses[a] = pose;
-		copyToSolverBody(lv, av, r.invMass, v3(r.invInertia[0], r.invInertia[1], r.invInertia[2]), pose, -r.maxDepenetrationVelocity,
-		                 r.maxContactImpulse, r.maxAngularVelocitySq, false, vels[a], txs[a], datas[a]);
-	}
-	for(uint32_t s = 0; s < nbStatic; s++)
-	{
-		poses[nbDyn + s] = loadTr(staticPose + 7 * s);
-		copyToSolverBody(zero3(), zero3(), 0.0f, zero3(), poses[nbDyn + s], -FLT_MAX, FLT_MAX, FLT_MAX, true, vels[nbDyn + s], txs[nbDyn + s],
-		                 datas[nbDyn + s]);
-	}
+	std::vector<BodyVel> vels;
+	std::vector<BodyTx> txs;
+	std::vector<BodyData> datas;
+	std::vector<Tr> poses;
+	buildSolverBodies(rigid, nbDyn, staticPose, nbStatic, gravity, dt, vels, txs, datas, poses);
 	BatchOut batch;
 	batchConstraints(pairA, pairB, int(nbConstraints), int(nbDyn), batch);
 	for(size_t h = 0; h < batch.headerStart.size(); h++)
@@ -1255,20 +1202,7 @@ uint32_t orc::tgsFrame(const void* rigid, uint32_t nbDyn, const float* staticPos
 			}
 			(*friction)[ci] = cr.written;
 		}
-	// PxIntegrateSolverBodiesTGS
-	for(uint32_t a = 0; a < nbDyn; a++)
-	{
-		const V3 w = m33MulVS(txs[a].sqrtInvInertia, vels[a].ang);
-		Q q = qMulS(txs[a].dq, poses[a].q);
-		const float m = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-		const float inv = 1.0f / m;
-		q.x *= inv; q.y *= inv; q.z *= inv; q.w *= inv;
-		outVel[6 * a + 0] = vels[a].lin.x; outVel[6 * a + 1] = vels[a].lin.y; outVel[6 * a + 2] = vels[a].lin.z;
-		outVel[6 * a + 3] = w.x; outVel[6 * a + 4] = w.y; outVel[6 * a + 5] = w.z;
-		float* o = outPose + 7 * a;
-		o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w;
-		o[4] = txs[a].p.x; o[5] = txs[a].p.y; o[6] = txs[a].p.z;
-	}
+	finishSolverBodies(vels, txs, poses, nbDyn, outVel, outPose);
 	return uint32_t(batch.headerStart.size());
 }
 
@@ -1284,4 +1218,60 @@ OX uint32_t orc_tgs_solve(const void* rigid, uint32_t nbDyn, const float* static
 	return tgsFrame(rigid, nbDyn, staticPose, nbStatic, pairA, pairB, nbConstraints, contactStart, contactCount, contacts, material, gravity, dt,
 	                nbPos, nbVel, bounceThreshold, frictionOffsetThreshold, correlationDistance, outVel, outPose, outHeaderStart, outHeaderStride,
 	                outOrder, nullptr);
+}
+
+void orc::buildSolverBodies(const void* rigid, uint32_t nbDyn, const float* staticPose, uint32_t nbStatic, const float* gravity, float dt,
+                            std::vector<BodyVel>& vels, std::vector<BodyTx>& txs, std::vector<BodyData>& datas, std::vector<Tr>& poses)
+{
+	const uint32_t nbTotal = nbDyn + nbStatic;
+	vels.assign(nbTotal, BodyVel());
+	txs.assign(nbTotal, BodyTx());
+	datas.assign(nbTotal, BodyData());
+	poses.assign(nbTotal, Tr());
+	const RigidBodyData* rb = static_cast<const RigidBodyData*>(rigid);
+	const V3 g = v3(gravity[0], gravity[1], gravity[2]);
+	for(uint32_t a = 0; a < nbDyn; a++)
+	{
+		const RigidBodyData& r = rb[a];
+		V3 lv = v3(r.linVel[0], r.linVel[1], r.linVel[2]);
+		V3 av = v3(r.angVel[0], r.angVel[1], r.angVel[2]);
+		unconstrainedVelocity(g, dt, r.linearDamping, r.angularDamping, r.maxLinearVelocitySq, r.maxAngularVelocitySq, lv, av);
+		Tr pose;
+		pose.q.x = r.q[0]; pose.q.y = r.q[1]; pose.q.z = r.q[2]; pose.q.w = r.q[3];
+		pose.p = v3(r.p[0], r.p[1], r.p[2]);
+		poses[a] = pose;
+		copyToSolverBody(lv, av, r.invMass, v3(r.invInertia[0], r.invInertia[1], r.invInertia[2]), pose, -r.maxDepenetrationVelocity,
+		                 r.maxContactImpulse, r.maxAngularVelocitySq, false, vels[a], txs[a], datas[a]);
+	}
+	for(uint32_t s = 0; s < nbStatic; s++)
+	{
+		poses[nbDyn + s] = loadTr(staticPose + 7 * s);
+		copyToSolverBody(zero3(), zero3(), 0.0f, zero3(), poses[nbDyn + s], -FLT_MAX, FLT_MAX, FLT_MAX, true, vels[nbDyn + s], txs[nbDyn + s],
+		                 datas[nbDyn + s]);
+	}
+}
+
+void orc::batchSolverConstraints(const uint32_t* bodyA, const uint32_t* bodyB, int n, int nbDyn, BatchOut& out)
+{
+	batchConstraints(bodyA, bodyB, n, nbDyn, out);
+}
+
+void orc::integrateSolverBody(BodyVel& v, BodyTx& t, float dt) { integrateStep(v, t, dt); }
+
+void orc::finishSolverBodies(const std::vector<BodyVel>& vels, const std::vector<BodyTx>& txs, const std::vector<Tr>& poses, uint32_t nbDyn,
+                             float* outVel, float* outPose)
+{
+	for(uint32_t a = 0; a < nbDyn; a++)
+	{
+		const V3 w = m33MulVS(txs[a].sqrtInvInertia, vels[a].ang);
+		Q q = qMulS(txs[a].dq, poses[a].q);
+		const float m = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+		const float inv = 1.0f / m;
+		q.x *= inv; q.y *= inv; q.z *= inv; q.w *= inv;
+		outVel[6 * a + 0] = vels[a].lin.x; outVel[6 * a + 1] = vels[a].lin.y; outVel[6 * a + 2] = vels[a].lin.z;
+		outVel[6 * a + 3] = w.x; outVel[6 * a + 4] = w.y; outVel[6 * a + 5] = w.z;
+		float* o = outPose + 7 * a;
+		o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w;
+		o[4] = txs[a].p.x; o[5] = txs[a].p.y; o[6] = txs[a].p.z;
+	}
 }

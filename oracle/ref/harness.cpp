@@ -193,6 +193,8 @@ HX int pxref_sizeof(int which)
 	case 9: return int(sizeof(PxBounds3));
 	case 10: return int(sizeof(PxBroadPhasePair));
 	case 11: return int(sizeof(PxTransform));
+	case 12: return int(sizeof(Px1DConstraint));
+	case 13: return int(sizeof(PxTGSSolverConstraintPrepDesc));
 	default: return -1;
 	}
 }
@@ -534,6 +536,178 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 	return tgsFrameRef(rigid, nbDyn, staticPose, nbStatic, pairA, pairB, nbConstraints, contactStart, contactCount, contacts, material, gravity, dt,
 		nbPos, nbVel, bounceThreshold, frictionOffsetThreshold, correlationDistance, outVel, outPose, outHeaderStart, outHeaderStride, outOrder,
 		outBodyVelRaw, outTxIRaw, alloc, NULL, NULL);
+}
+
+//////////////////////////////////////////////////////////////////////////////
+// One TGS frame of joints, built as the immediate-mode snippet builds its
+// joints (SnippetImmediateMode.cpp:838-1061) but with the caller's 1D rows in
+// place of a joint shader: construct bodies, PxBatchConstraintsTGS over the
+// joints, PxCreateJointConstraintsTGS per header, PxSolveConstraintsTGS,
+// PxIntegrateSolverBodiesTGS.
+//
+// jointA/B          body indices (>= nbDyn: static nbDyn+s)
+// rowStart/rowCount per joint into rows (Px1DConstraint, 80 B each; copied,
+//                   the prep rewrites them)
+// params            per joint 20 floats: invMassScales (linear0, angular0,
+//                   linear1, angular1), cA2w, cB2w, body0WorldOffset,
+//                   linBreakForce, angBreakForce, minResponseThreshold, flags
+//                   (float holding 1 disablePreprocessing | 2 improvedSlerp |
+//                   4 driveLimitsAreForces), 3 unused
+// out*              velocities and poses as pxref_tgs_solve; headers with their
+//                   constraint type (DY_SC_TYPE_*); per joint the write-back's
+//                   linear and angular impulse (6 floats) and broken flag
+// batchJoints       0: one header of stride 1 per joint in input order (the
+//                   snippet without BATCH_CONTACTS), else PxBatchConstraintsTGS
+namespace
+{
+struct JointWriteback   // Dy::ConstraintWriteback (DyConstraintWriteBack.h:42)
+{
+	PxVec3 linearImpulse;
+	PxU32 broken;
+	PxVec3 angularImpulse;
+	PxReal residual;
+};
+}
+
+HX PxU32 pxref_joint_frame(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
+	const PxU32* jointA, const PxU32* jointB, PxU32 nbJoints, const PxU32* rowStart, const PxU32* rowCount, const void* rows,
+	const float* params, const float* gravity, float dt, PxU32 nbPos, PxU32 nbVel, PxU32 batchJoints,
+	float* outVel, float* outPose, PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outHeaderType, PxU32* outOrder,
+	float* outForce, PxU32* outBroken)
+{
+	ensureFoundation();
+	const PxU32 nbTotal = nbDyn + nbStatic;
+	std::vector<PxTGSSolverBodyVel> bodies(nbTotal);
+	std::vector<PxTGSSolverBodyTxInertia> txI(nbTotal);
+	std::vector<PxTGSSolverBodyData> bodyData(nbTotal);
+	std::vector<PxTransform> poses(nbTotal);
+	const PxRigidBodyData* rb = static_cast<const PxRigidBodyData*>(rigid);
+	const PxVec3 g(gravity[0], gravity[1], gravity[2]);
+	for(PxU32 a = 0; a < nbDyn; a++)
+	{
+		PxConstructSolverBodiesTGS(&rb[a], &bodies[a], &txI[a], &bodyData[a], 1, g, dt, false);
+		poses[a] = rb[a].body2World;
+	}
+	for(PxU32 s = 0; s < nbStatic; s++)
+	{
+		poses[nbDyn + s] = loadPose(staticPose + 7 * s);
+		PxConstructStaticSolverBodyTGS(poses[nbDyn + s], bodies[nbDyn + s], txI[nbDyn + s], bodyData[nbDyn + s]);
+	}
+	PxU32 nbRowsTotal = 0;
+	for(PxU32 j = 0; j < nbJoints; j++) nbRowsTotal = PxMax(nbRowsTotal, rowStart[j] + rowCount[j]);
+	std::vector<Px1DConstraint> rowCopy(nbRowsTotal ? nbRowsTotal : 1);
+	if(nbRowsTotal) memcpy(rowCopy.data(), rows, sizeof(Px1DConstraint) * nbRowsTotal);
+	std::vector<JointWriteback> writeback(nbJoints ? nbJoints : 1);
+	memset(writeback.data(), 0, sizeof(JointWriteback) * writeback.size());
+
+	std::vector<PxSolverConstraintDesc> descs(nbJoints), ordered(nbJoints);
+	std::vector<PxU32> ids(nbJoints);
+	for(PxU32 i = 0; i < nbJoints; i++)
+	{
+		PxSolverConstraintDesc& d = descs[i];
+		memset(&d, 0, sizeof(d));
+		d.tgsBodyA = &bodies[jointA[i]];
+		d.tgsBodyB = &bodies[jointB[i]];
+		d.bodyADataIndex = jointA[i];
+		d.bodyBDataIndex = jointB[i];
+		d.linkIndexA = PxSolverConstraintDesc::RIGID_BODY;
+		d.linkIndexB = PxSolverConstraintDesc::RIGID_BODY;
+		ids[i] = i;
+		d.constraint = reinterpret_cast<PxU8*>(&ids[i]);
+		d.constraintType = PxSolverConstraintDesc::eJOINT_CONSTRAINT;
+	}
+	std::vector<PxConstraintBatchHeader> headers(nbJoints ? nbJoints : 1);
+	PxU32 nbHeaders = nbJoints;
+	if(batchJoints)
+		nbHeaders = PxBatchConstraintsTGS(descs.data(), nbJoints, bodies.data(), nbDyn, headers.data(), ordered.data());
+	else
+	{
+		// the snippet's unbatched path: one header of stride 1 per joint, in input order
+		for(PxU32 i = 0; i < nbJoints; i++)
+		{
+			headers[i].startIndex = i;
+			headers[i].stride = 1;
+			headers[i].constraintType = PxSolverConstraintDesc::eJOINT_CONSTRAINT;
+			ordered[i] = descs[i];
+		}
+	}
+	for(PxU32 i = 0; i < nbJoints; i++)
+		outOrder[i] = *reinterpret_cast<const PxU32*>(ordered[i].constraint);
+
+	const PxReal invDt = 1.0f / dt;
+	const PxReal stepDt = dt / PxReal(nbPos);
+	const PxReal invStepDt = invDt * PxReal(nbPos);
+	FrameConstraintAllocator alloc;
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		PxConstraintBatchHeader& header = headers[h];
+		PxTGSSolverConstraintPrepDesc jd[4];
+		for(PxU32 a = 0; a < header.stride; a++)
+		{
+			PxSolverConstraintDesc& desc = ordered[header.startIndex + a];
+			const PxU32 ji = *reinterpret_cast<const PxU32*>(desc.constraint);
+			const float* pr = params + 20 * ji;
+			PxTGSSolverConstraintPrepDesc& c = jd[a];
+			memset(&c, 0, sizeof(c));
+			c.body0 = desc.tgsBodyA;
+			c.body1 = desc.tgsBodyB;
+			c.bodyData0 = &bodyData[desc.bodyADataIndex];
+			c.bodyData1 = &bodyData[desc.bodyBDataIndex];
+			c.body0TxI = &txI[desc.bodyADataIndex];
+			c.body1TxI = &txI[desc.bodyBDataIndex];
+			c.bodyFrame0 = poses[desc.bodyADataIndex];
+			c.bodyFrame1 = poses[desc.bodyBDataIndex];
+			c.bodyState0 = desc.bodyADataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
+			c.bodyState1 = desc.bodyBDataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
+			c.desc = &desc;
+			c.writeback = &writeback[ji];
+			c.invMassScales = PxConstraintInvMassScale(pr[0], pr[1], pr[2], pr[3]);
+			c.cA2w = PxVec3(pr[4], pr[5], pr[6]);
+			c.cB2w = PxVec3(pr[7], pr[8], pr[9]);
+			c.body0WorldOffset = PxVec3(pr[10], pr[11], pr[12]);
+			c.linBreakForce = pr[13];
+			c.angBreakForce = pr[14];
+			c.minResponseThreshold = pr[15];
+			const PxU32 fl = PxU32(pr[16]);
+			c.disablePreprocessing = (fl & 1u) != 0;
+			c.improvedSlerp = (fl & 2u) != 0;
+			c.driveLimitsAreForces = (fl & 4u) != 0;
+			c.rows = rowCopy.data() + rowStart[ji];
+			c.numRows = rowCount[ji];
+		}
+		PxCreateJointConstraintsTGS(&header, 1, jd, alloc, stepDt, dt, invStepDt, invDt, 1.0f);
+	}
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		outHeaderStart[h] = headers[h].startIndex;
+		outHeaderStride[h] = headers[h].stride;
+		outHeaderType[h] = headers[h].constraintType;
+	}
+
+	PxSolveConstraintsTGS(headers.data(), nbHeaders, ordered.data(), bodies.data(), txI.data(), nbDyn, nbPos, nbVel, stepDt, invStepDt);
+	PxIntegrateSolverBodiesTGS(bodies.data(), txI.data(), poses.data(), nbDyn, dt);
+	for(PxU32 a = 0; a < nbDyn; a++)
+	{
+		outVel[6 * a + 0] = bodies[a].linearVelocity.x;
+		outVel[6 * a + 1] = bodies[a].linearVelocity.y;
+		outVel[6 * a + 2] = bodies[a].linearVelocity.z;
+		outVel[6 * a + 3] = bodies[a].angularVelocity.x;
+		outVel[6 * a + 4] = bodies[a].angularVelocity.y;
+		outVel[6 * a + 5] = bodies[a].angularVelocity.z;
+		storePose(outPose + 7 * a, poses[a]);
+	}
+	for(PxU32 j = 0; j < nbJoints; j++)
+	{
+		const JointWriteback& w = writeback[j];
+		outForce[6 * j + 0] = w.linearImpulse.x;
+		outForce[6 * j + 1] = w.linearImpulse.y;
+		outForce[6 * j + 2] = w.linearImpulse.z;
+		outForce[6 * j + 3] = w.angularImpulse.x;
+		outForce[6 * j + 4] = w.angularImpulse.y;
+		outForce[6 * j + 5] = w.angularImpulse.z;
+		outBroken[j] = (w.broken & 0x80000000u) ? 1u : 0u;
+	}
+	return nbHeaders;
 }
 
 //////////////////////////////////////////////////////////////////////////////

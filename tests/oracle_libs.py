@@ -252,3 +252,48 @@ class PersistentScenes:
         if self.h:
             (self.L.orc_persistent_release if self.which == "orc" else self.L.pxref_persistent_release)(self.h)
             self.h = None
+
+
+def run_joints(which, frame, dt=1.0 / 60.0, nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0), batch=True):
+    """One TGS frame of joints (construct, batch, PxCreateJointConstraintsTGS,
+    solve, integrate) through the oracle ("orc") or the reference ("pxref").
+    frame: dict of nb_dyn, static_poses, joint_a, joint_b, rigid (PxRigidBodyData),
+    rows (Px1DConstraint), row_start, row_count, params (see joint_scenes.joint_frame).
+    Returns velocities (n,6), poses (n,7), headers (start, stride, type), the
+    joint order, per-joint impulses (J,6) and broken flags.  batch=False: one
+    header of stride 1 per joint in input order."""
+    A = np.ascontiguousarray(frame["joint_a"], np.uint32)
+    B = np.ascontiguousarray(frame["joint_b"], np.uint32)
+    n = int(frame["nb_dyn"])
+    m = len(frame["static_poses"])
+    nj = len(A)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nj, 1), np.uint32)
+    hst = np.zeros(max(nj, 1), np.uint32)
+    ht = np.zeros(max(nj, 1), np.uint32)
+    order = np.zeros(max(nj, 1), np.uint32)
+    force = np.zeros((max(nj, 1), 6), np.float32)
+    broken = np.zeros(max(nj, 1), np.uint32)
+    g = np.array(gravity, np.float32)
+    L = oracle() if which == "orc" else reference()
+    fn = L.orc_joint_frame if which == "orc" else L.pxref_joint_frame
+    fn.restype = ctypes.c_uint32
+    rb = np.ascontiguousarray(frame["rigid"])
+    nh = fn(_p(rb), ctypes.c_uint32(n), _p(np.ascontiguousarray(frame["static_poses"], np.float32)), ctypes.c_uint32(m), _p(A), _p(B),
+            ctypes.c_uint32(nj), _p(np.ascontiguousarray(frame["row_start"], np.uint32)), _p(np.ascontiguousarray(frame["row_count"], np.uint32)),
+            _p(np.ascontiguousarray(frame["rows"])), _p(np.ascontiguousarray(frame["params"], np.float32)), _p(g), ctypes.c_float(dt),
+            ctypes.c_uint32(nb_pos), ctypes.c_uint32(nb_vel), ctypes.c_uint32(1 if batch else 0), _p(vel), _p(pose), _p(hs), _p(hst), _p(ht),
+            _p(order), _p(force), _p(broken))
+    return dict(vel=vel, pose=pose, header_start=hs[:nh].copy(), header_stride=hst[:nh].copy(), header_type=ht[:nh].copy(),
+                order=order[:nj].copy(), force=force[:nj].copy(), broken=broken[:nj].copy())
+
+
+def advance_rigid(rigid, vel, pose):
+    """PxRigidBodyData for the next frame from a frame's velocities and poses."""
+    out = rigid.copy()
+    out["linVel"] = vel[:, :3]
+    out["angVel"] = vel[:, 3:]
+    out["q"] = pose[:, :4]
+    out["p"] = pose[:, 4:]
+    return out

@@ -295,3 +295,42 @@ def test_oracle_large_scene_trace_equals_reference():
     orc = np.load(os.path.join(GOLDEN, "large_scene_trace_orc.npz"))
     assert int(ref["checksum"]) == int(orc["checksum"])
     assert np.array_equal(ref["stats"], orc["stats"])
+
+
+JOINT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "joints_*.npz")))
+JOINT_KEYS = ("vel", "pose", "header_start", "header_stride", "header_type", "order", "force", "broken")
+
+
+def test_joint_fixtures_present():
+    assert len(JOINT_FIXTURES) >= 2
+
+
+@pytest.mark.parametrize("path", JOINT_FIXTURES, ids=[os.path.basename(p) for p in JOINT_FIXTURES])
+def test_oracle_joints_match_reference_golden(path):
+    """PxCreateJointConstraintsTGS + PxSolveConstraintsTGS on the reference's
+    joint frames: headers (with their per-pair / 4-wide types), order,
+    velocities, poses, write-back impulses and broken flags, bit for bit."""
+    from joint_scenes import load_joint_fixture
+    from oracle_libs import run_joints
+    for fr in load_joint_fixture(path):
+        got = run_joints("orc", fr)
+        for k in JOINT_KEYS:
+            assert np.array_equal(got[k], fr["ref_" + k]), "frame %d %s" % (fr["frame"], k)
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed,batch", [(31, True), (32, False), (33, True)])
+def test_oracle_joints_match_reference_live(seed, batch):
+    """30 consecutive frames of a seeded joint scene (each frame's rows written
+    from the poses the previous one left), the oracle against the reference."""
+    from joint_scenes import joint_frame, make_joint_scene
+    from oracle_libs import advance_rigid, run_joints
+    sc = make_joint_scene(seed, nb_chains=8, links=(2, 7))
+    rigid = sc["rigid"]
+    for f in range(30):
+        fr = joint_frame(sc, rigid)
+        ref = run_joints("pxref", fr, batch=batch)
+        got = run_joints("orc", fr, batch=batch)
+        for k in JOINT_KEYS:
+            assert np.array_equal(got[k], ref[k]), "frame %d %s" % (f, k)
+        rigid = advance_rigid(rigid, ref["vel"], ref["pose"])
