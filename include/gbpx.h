@@ -186,6 +186,61 @@ int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t
                                void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
                                uint32_t* outBroken);
 int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI, float* poses, uint32_t n);
+/* PxBatchConstraintsTGS over a list mixing contacts and joints: kind[i] = the
+ * constraint's PxSolverConstraintDesc type (0 contact, 1 joint); a header only
+ * joins consecutive constraints of one type (createHeaders,
+ * physx/source/immediatemode/src/NpImmediateMode.cpp:159). */
+uint32_t gbpx_batch_typed_constraints_tgs(const uint32_t* bodyA, const uint32_t* bodyB, const uint8_t* kind, uint32_t nbConstraints,
+                                          uint32_t nbDynamic, uint32_t nbStatic, uint32_t* outHeaderStart, uint32_t* outHeaderStride,
+                                          uint32_t* outOrder);
+
+/* -------------------------------------------------------- joints (1D constraints)
+ * Replace, on the rigid-body path:
+ *   PxCreateJointConstraintsTGS      physx/include/PxImmediateMode.h:659
+ *     (NpImmediateMode.cpp:1480: per-pair setupSolverConstraintStep, or the
+ *     4-wide setupSolverConstraintStep4 for a header of stride 4 whose joints
+ *     all have rows)
+ *   the joint half of PxSolveConstraintsTGS (solve1DStep / solve1DStep4,
+ *     conclude, write-back)
+ * Rows are the caller's Px1DConstraint (80 bytes, <= 12 per joint).  Per joint
+ * 20 parameter floats: PxConstraintInvMassScale (linear0, angular0, linear1,
+ * angular1), cA2w, cB2w, body0WorldOffset, linBreakForce, angBreakForce,
+ * minResponseThreshold, flags (a float holding 1 disablePreprocessing |
+ * 4 driveLimitsAreForces; 2 improvedSlerp is refused with GBPX_ERR_INVALID),
+ * 3 unused.  Joint records are this build's own format,
+ * gbpx_joint_record_bytes() each. */
+uint32_t gbpx_joint_record_bytes(void);
+/* One joint per entry: the bodies' records in the reference's layouts, frames
+ * (PxTransform), rows[rowStart[k] .. +rowCount[k]], params + 20 k, block[k] = 1
+ * for a lane of a 4-wide header.  Times as the immediate-mode snippet passes
+ * them to PxCreateJointConstraintsTGS: stepDt, simDt, 1/stepDt, 1/simDt, lengthScale. */
+int gbpx_create_joint_constraints_tgs(uint32_t n, const void* vel0, const void* vel1, const void* txI0, const void* txI1, const void* data0,
+                                      const void* data1, const float* frame0, const float* frame1, const uint32_t* rowStart, const uint32_t* rowCount,
+                                      const void* rows, uint32_t nbRows, const float* params, const uint8_t* block, float stepDt, float simDt,
+                                      float recipStepDt, float recipSimDt, float lengthScale, void* outRecords);
+/* PxSolveConstraintsTGS over contacts and joints: wave w solves contacts
+ * [waveEnds[w-1], waveEnds[w]) and joints [jointWaveEnds[w-1], jointWaveEnds[w])
+ * (distinct dynamic bodies); otherwise as gbpx_solve_constraints_tgs.
+ * outJointForce / outJointBroken (null: not wanted): per joint the write-back
+ * impulse (linear, angular: 6 floats) and broken flag. */
+int gbpx_solve_constraints_joints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds,
+                                      void* jointRecords, const uint32_t* jointA, const uint32_t* jointB, uint32_t nbJoints,
+                                      const uint32_t* jointWaveEnds, uint32_t nbWaves, void* bodyVel, void* bodyTxI, uint32_t nbBodies,
+                                      uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt, uint32_t* outBroken, float* outJointForce,
+                                      uint32_t* outJointBroken);
+/* One immediate-mode TGS frame of joints, the snippet's joint sequence
+ * (SnippetImmediateMode.cpp:838-1061) with the caller's rows: construct
+ * bodies, PxBatchConstraintsTGS over the joints (batchJoints = 0: one header of
+ * stride 1 per joint in input order), PxCreateJointConstraintsTGS per header,
+ * nbPos + nbVel iterations, PxIntegrateSolverBodiesTGS.  Outputs: velocity
+ * (linear, world angular) and pose per dynamic body, headers (start, stride,
+ * DY_SC_TYPE_RB_1D = 2 or DY_SC_TYPE_BLOCK_1D = 8), joint order, per joint the
+ * write-back impulse (6 floats) and broken flag. */
+int gbpx_joint_frame(const void* rigidBodies, uint32_t nbDynamic, const float* staticPoses, uint32_t nbStatic, const uint32_t* jointA,
+                     const uint32_t* jointB, uint32_t nbJoints, const uint32_t* rowStart, const uint32_t* rowCount, const void* rows,
+                     const float* params, const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel, uint32_t batchJoints, float* outVelocity,
+                     float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outHeaderType, uint32_t* outOrder,
+                     float* outForce, uint32_t* outBroken, uint32_t* outNbHeaders);
 
 /* -------------------------------------------------------- batched world
  * Many independent scenes advanced together: one persistent launch per step

@@ -204,6 +204,51 @@ struct PxTGSSolverContactDesc
 	float offsetSlop;
 };
 
+// Px1DConstraint (physx/include/PxConstraintDesc.h:194): one joint row
+struct alignas(16) Px1DConstraint
+{
+	PxVec3 linear0; float geometricError;
+	PxVec3 angular0; float velocityTarget;
+	PxVec3 linear1; float minImpulse;
+	PxVec3 angular1; float maxImpulse;
+	float mods[2];     // spring stiffness / damping, or restitution / bounce velocity threshold
+	uint16_t flags;    // Px1DConstraintFlag
+	uint16_t solveHint;
+	uint32_t pad;
+};
+
+struct PxVec3p { PxVec3 v; uint32_t padding; };   // PxVec3Padded
+
+// PxTGSSolverConstraintPrepDesc (physx/include/solver/PxSolverDefs.h:615-668)
+struct PxTGSSolverConstraintPrepDesc
+{
+	PxConstraintInvMassScale invMassScales;
+	PxSolverConstraintDesc* desc;
+	const PxTGSSolverBodyVel* body0;
+	const PxTGSSolverBodyVel* body1;
+	const PxTGSSolverBodyTxInertia* body0TxI;
+	const PxTGSSolverBodyTxInertia* body1TxI;
+	const PxTGSSolverBodyData* bodyData0;
+	const PxTGSSolverBodyData* bodyData1;
+	PxTransform bodyFrame0;
+	PxTransform bodyFrame1;
+	int bodyState0;
+	int bodyState1;
+	void* writeback;   // Dy::ConstraintWriteback (linearImpulse, broken bit 31, angularImpulse, residual) or null
+	Px1DConstraint* rows;
+	uint32_t numRows;
+	float linBreakForce, angBreakForce;
+	float minResponseThreshold;
+	bool disablePreprocessing;
+	bool improvedSlerp;
+	bool driveLimitsAreForces;
+	bool extendedLimits;
+	bool disableConstraint;
+	PxVec3p body0WorldOffset;
+	PxVec3p cA2w;
+	PxVec3p cB2w;
+};
+
 class PxConstraintAllocator
 {
 public:
@@ -360,6 +405,8 @@ uint32_t PxBatchConstraintsTGS(const gbpx_px::PxSolverConstraintDesc* solverCons
 bool PxCreateContactConstraintsTGS(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, gbpx_px::PxTGSSolverContactDesc* contactDescs,
                                    gbpx_px::PxConstraintAllocator& allocator, float invDt, float invTotalDt, float bounceThreshold,
                                    float frictionOffsetThreshold, float correlationDistance);
+bool PxCreateJointConstraintsTGS(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, gbpx_px::PxTGSSolverConstraintPrepDesc* jointDescs,
+                                 gbpx_px::PxConstraintAllocator& allocator, float dt, float totalDt, float invDt, float invTotalDt, float lengthScale);
 void PxSolveConstraintsTGS(const gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders,
                            const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, gbpx_px::PxTGSSolverBodyVel* solverBodies,
                            gbpx_px::PxTGSSolverBodyTxInertia* txInertias, uint32_t nbSolverBodies, uint32_t nbPositionIterations,

@@ -29,7 +29,10 @@ struct Result
 	std::vector<uint32_t> headerStart, headerStride;
 };
 
-inline void partition(const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, uint32_t nbDyn, Result& out)
+// kind (may be null: one kind): per constraint its PxSolverConstraintDesc
+// constraint type; a header only joins consecutive constraints of one kind
+// (createHeaders, physx/source/immediatemode/src/NpImmediateMode.cpp:159).
+inline void partition(const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, uint32_t nbDyn, Result& out, const uint8_t* kind = nullptr)
 {
 	const uint32_t MAXP = 32;
 	std::vector<uint32_t> progress(nbDyn, 0), maxNormal(nbDyn, 0), maxStatic(nbDyn, 0);
@@ -138,7 +141,16 @@ inline void partition(const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, 
 		if(loopMax > 0)
 		{
 			j = 1;
-			if(cur < maxPartition) j = loopMax;   // all contact constraints share one type
+			if(cur < maxPartition)
+			{
+				if(!kind) j = loopMax;
+				else
+				{
+					// (a constraint between two non-dynamic bodies is not placed: its slot stays unset)
+					const uint32_t first = out.order[a];
+					while(j < loopMax && first < n && out.order[a + j] < n && kind[out.order[a + j]] == kind[first]) j++;
+				}
+			}
 		}
 		out.headerStride.push_back(j);
 		if(maxJ == a + j && maxJ != n)

@@ -45,6 +45,15 @@ bool packShape(const PxGeometry& g, int& type, float* out)
 	}
 }
 
+// PxConstraintBatchHeader::constraintType after constraint creation
+// (lowleveldynamics/src/DySolverConstraintTypes.h:38, SolverConstraintType)
+enum : uint16_t
+{
+	DY_SC_TYPE_RB_CONTACT = 1, DY_SC_TYPE_RB_1D = 2, DY_SC_TYPE_EXT_1D = 4, DY_SC_TYPE_STATIC_CONTACT = 5, DY_SC_TYPE_BLOCK_RB_CONTACT = 6,
+	DY_SC_TYPE_BLOCK_STATIC_RB_CONTACT = 7, DY_SC_TYPE_BLOCK_1D = 8
+};
+bool isJointHeader(uint16_t type) { return type == DY_SC_TYPE_RB_1D || type == DY_SC_TYPE_EXT_1D || type == DY_SC_TYPE_BLOCK_1D; }
+
 uint32_t stridesTotal(const PxConstraintBatchHeader* headers, uint32_t nbHeaders)
 {
 	uint32_t n = 0;
@@ -199,7 +208,11 @@ GX uint32_t PxBatchConstraintsTGS(const PxSolverConstraintDesc* descs, uint32_t 
 		a[i] = index(descs[i].tgsBodyA);
 		b[i] = index(descs[i].tgsBodyB);
 	}
-	const uint32_t nbHeaders = gbpx_batch_constraints_tgs(a.data(), b.data(), nbConstraints, nbBodies, 1, hs.data(), hst.data(), order.data());
+	// a header only joins constraints of one PxSolverConstraintDesc type (contact / joint)
+	std::vector<uint8_t> kind(nbConstraints);
+	for(uint32_t i = 0; i < nbConstraints; i++) kind[i] = uint8_t(descs[i].constraintLengthOver16);
+	const uint32_t nbHeaders =
+	    gbpx_batch_typed_constraints_tgs(a.data(), b.data(), kind.data(), nbConstraints, nbBodies, 1, hs.data(), hst.data(), order.data());
 	for(uint32_t i = 0; i < nbConstraints; i++) outOrdered[i] = descs[order[i]];
 	for(uint32_t h = 0; h < nbHeaders; h++)
 	{
@@ -282,6 +295,24 @@ GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uin
 	                                       frictionOut.data(), invDt, invTotalDt, bounceThreshold, frictionOffsetThreshold, correlationDistance,
 	                                       rows.data(), bytes.data()) != GBPX_OK)
 		return false;
+	// header types as the reference leaves them (NpImmediateMode.cpp:1444-1472):
+	// the 4-wide path's DY_SC_TYPE_BLOCK_RB_CONTACT / _BLOCK_STATIC_RB_CONTACT,
+	// else the first constraint's DY_SC_TYPE_RB_CONTACT / _STATIC_CONTACT (a
+	// static-typed header with a dynamic constraint becomes RB_CONTACT)
+	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
+	{
+		PxConstraintBatchHeader& hd = batchHeaders[h];
+		if(laneFlags[k] & 1u) { hd.constraintType = uint16_t((laneFlags[k] & 2u) ? DY_SC_TYPE_BLOCK_RB_CONTACT : DY_SC_TYPE_BLOCK_STATIC_RB_CONTACT); continue; }
+		auto typeOf = [&](uint32_t j) {
+			const int st = contactDescs[j].bodyState1;
+			return uint16_t((st == eSTATIC_BODY || st == eKINEMATIC_BODY) ? DY_SC_TYPE_STATIC_CONTACT : DY_SC_TYPE_RB_CONTACT);
+		};
+		uint16_t type = typeOf(k);
+		if(type == DY_SC_TYPE_STATIC_CONTACT)
+			for(uint32_t l = 1; l < hd.stride; l++)
+				if(typeOf(k + l) == DY_SC_TYPE_RB_CONTACT) { type = DY_SC_TYPE_RB_CONTACT; break; }
+		hd.constraintType = type;
+	}
 	// header of every constraint (position of its header's first lane)
 	std::vector<uint32_t> headerFirst(n, 0);
 	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
@@ -340,8 +371,113 @@ GX bool PxCreateContactConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uin
 	return true;
 }
 
+// Joint records in constraint memory: the record header (up to its rows) and
+// the rows in use, this library's format (gbpx_joint_record_bytes() at most).
+constexpr uint32_t JOINT_HEADER_BYTES = 192, JOINT_ROW_BYTES = 96, JOINT_COUNT_OFFSET = 8;
+uint32_t jointRecordUsedBytes(const uint8_t* rec)
+{
+	uint32_t count;
+	memcpy(&count, rec + JOINT_COUNT_OFFSET, 4);
+	return JOINT_HEADER_BYTES + std::min<uint32_t>(count, 12) * JOINT_ROW_BYTES;
+}
+
+// Dy::ConstraintWriteback (lowleveldynamics/include/DyConstraintWriteBack.h:42)
+struct JointWriteback
+{
+	PxVec3 linearImpulse;
+	uint32_t brokenAndResidual;   // broken in bit 31 (setCombined), position residual (0) below
+	PxVec3 angularImpulse;
+	float residual;
+};
+
+// PxCreateJointConstraintsTGS: one record per joint into the allocator's
+// constraint memory; a header of stride 4 whose joints all have rows takes the
+// reference's 4-wide path (NpImmediateMode.cpp:1495-1517) and is typed
+// DY_SC_TYPE_BLOCK_1D, every other DY_SC_TYPE_RB_1D.  A joint without rows gets
+// no constraint (desc->constraint = null).  The caller's rows are read, not
+// rewritten.  Joints between articulation links and eIMPROVED_SLERP drives are
+// not supported (false).
+GX bool PxCreateJointConstraintsTGS(PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, PxTGSSolverConstraintPrepDesc* jointDescs,
+                                    PxConstraintAllocator& allocator, float dt, float totalDt, float invDt, float invTotalDt, float lengthScale)
+{
+	const uint32_t n = stridesTotal(batchHeaders, nbHeaders);
+	if(!n) return true;
+	if(!(dt > 0.0f) || !(totalDt > 0.0f)) return false;
+	static const PxTGSSolverBodyVel zeroVel = [] { PxTGSSolverBodyVel v; memset(&v, 0, sizeof(v)); v.isKinematic = true; return v; }();
+	static const PxTGSSolverBodyTxInertia zeroTx = [] { PxTGSSolverBodyTxInertia t; memset(&t, 0, sizeof(t)); t.deltaBody2WorldQ.w = 1.0f; return t; }();
+	static const PxTGSSolverBodyData zeroData = [] { PxTGSSolverBodyData d; memset(&d, 0, sizeof(d)); d.maxContactImpulse = 3.4e38f; return d; }();
+	std::vector<PxTGSSolverBodyVel> v0(n), v1(n);
+	std::vector<PxTGSSolverBodyTxInertia> x0(n), x1(n);
+	std::vector<PxTGSSolverBodyData> d0(n), d1(n);
+	std::vector<PxTransform> f0(n), f1(n);
+	std::vector<uint32_t> rs(n), rc(n);
+	std::vector<Px1DConstraint> rows;
+	std::vector<float> params(size_t(n) * 20, 0.0f);
+	std::vector<uint8_t> block(n, 0);
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxTGSSolverConstraintPrepDesc& d = jointDescs[k];
+		if(!d.desc || d.numRows > 12 || (d.numRows && !d.rows) || d.improvedSlerp || (d.bodyState0 & eARTICULATION) || (d.bodyState1 & eARTICULATION))
+			return false;
+		v0[k] = d.body0 ? *d.body0 : zeroVel;
+		v1[k] = d.body1 ? *d.body1 : zeroVel;
+		x0[k] = d.body0TxI ? *d.body0TxI : zeroTx;
+		x1[k] = d.body1TxI ? *d.body1TxI : zeroTx;
+		d0[k] = d.bodyData0 ? *d.bodyData0 : zeroData;
+		d1[k] = d.bodyData1 ? *d.bodyData1 : zeroData;
+		f0[k] = d.bodyFrame0;
+		f1[k] = d.bodyFrame1;
+		rs[k] = uint32_t(rows.size());
+		rc[k] = d.numRows;
+		rows.insert(rows.end(), d.rows, d.rows + d.numRows);
+		float* p = &params[size_t(k) * 20];
+		p[0] = d.invMassScales.linear0; p[1] = d.invMassScales.angular0; p[2] = d.invMassScales.linear1; p[3] = d.invMassScales.angular1;
+		p[4] = d.cA2w.v.x; p[5] = d.cA2w.v.y; p[6] = d.cA2w.v.z;
+		p[7] = d.cB2w.v.x; p[8] = d.cB2w.v.y; p[9] = d.cB2w.v.z;
+		p[10] = d.body0WorldOffset.v.x; p[11] = d.body0WorldOffset.v.y; p[12] = d.body0WorldOffset.v.z;
+		p[13] = d.linBreakForce; p[14] = d.angBreakForce; p[15] = d.minResponseThreshold;
+		p[16] = float((d.disablePreprocessing ? 1u : 0u) | (d.driveLimitsAreForces ? 4u : 0u));
+	}
+	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
+	{
+		PxConstraintBatchHeader& hd = batchHeaders[h];
+		bool b = hd.stride == 4;
+		for(uint32_t l = 0; l < hd.stride && b; l++) b = jointDescs[k + l].numRows > 0;
+		hd.constraintType = b ? DY_SC_TYPE_BLOCK_1D : DY_SC_TYPE_RB_1D;
+		for(uint32_t l = 0; l < hd.stride; l++) block[k + l] = b ? 1 : 0;
+	}
+	const uint32_t recBytes = gbpx_joint_record_bytes();
+	std::vector<uint8_t> recs(size_t(n) * recBytes);
+	if(gbpx_create_joint_constraints_tgs(n, v0.data(), v1.data(), x0.data(), x1.data(), d0.data(), d1.data(), &f0[0].q.x, &f1[0].q.x, rs.data(),
+	                                     rc.data(), rows.data(), uint32_t(rows.size()), params.data(), block.data(), dt, totalDt, invDt, invTotalDt,
+	                                     lengthScale, recs.data()) != GBPX_OK)
+		return false;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		PxSolverConstraintDesc& sd = *jointDescs[k].desc;
+		if(jointDescs[k].numRows == 0)
+		{
+			sd.constraint = nullptr;
+			sd.writeBack = nullptr;
+			sd.constraintLengthOver16 = 0;
+			continue;
+		}
+		const uint8_t* rec = &recs[size_t(k) * recBytes];
+		const uint32_t size = jointRecordUsedBytes(rec);
+		uint8_t* mem = allocator.reserveConstraintData(size);
+		if(!mem) return false;
+		memcpy(mem, rec, size);
+		sd.constraint = mem;
+		sd.constraintLengthOver16 = uint16_t(size / 16);
+		sd.writeBack = jointDescs[k].writeback;
+	}
+	return true;
+}
+
 // PxSolveConstraintsTGS: headers are solved in order; consecutive headers whose
-// constraints touch distinct dynamic bodies run as one parallel wave.
+// constraints touch distinct dynamic bodies run as one parallel wave.  Joint
+// headers (DY_SC_TYPE_RB_1D / _BLOCK_1D) hold joint records, every other
+// header contact rows.
 GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders, const PxSolverConstraintDesc* descs,
                               PxTGSSolverBodyVel* solverBodies, PxTGSSolverBodyTxInertia* txInertias, uint32_t nbSolverBodies, uint32_t nbPositionIterations,
                               uint32_t nbVelocityIterations, float dt, float invDt, uint32_t nbSolverArticulations, void** solverArticulations, void* Z,
@@ -352,7 +488,6 @@ GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint3
 	(void)Z;
 	(void)deltaV;
 	if(nbSolverArticulations || !nbSolverBodies) return;
-	const uint32_t n = stridesTotal(batchHeaders, nbBatchHeaders);
 	// bodies: the caller's solver bodies, then every other (static / kinematic) body the constraints reference
 	std::vector<PxTGSSolverBodyVel> vel(solverBodies, solverBodies + nbSolverBodies);
 	std::vector<PxTGSSolverBodyTxInertia> tx(txInertias, txInertias + nbSolverBodies);
@@ -371,15 +506,17 @@ GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint3
 		return id;
 	};
 	const uint32_t stride = gbpx_constraint_row_stride();
-	std::vector<uint8_t> rows(size_t(n) * stride, 0);
-	std::vector<uint32_t> a(n), b(n), waveEnds;
-	std::vector<uint32_t> lastWave;   // per dynamic body: wave that last used it (+1)
-	lastWave.assign(nbSolverBodies, 0);
+	const uint32_t jointBytes = gbpx_joint_record_bytes();
+	std::vector<uint8_t> rows, joints;
+	std::vector<uint32_t> a, b, ja, jb, waveEnds, jointWaveEnds;
+	std::vector<const PxSolverConstraintDesc*> contactDesc, jointDesc;
+	std::vector<uint32_t> lastWave(nbSolverBodies, 0);   // per dynamic body: wave that last used it (+1)
 	uint32_t wave = 1;
 	bool waveOpen = false;
-	for(uint32_t h = 0, k = 0; h < nbBatchHeaders; h++)
+	for(uint32_t h = 0; h < nbBatchHeaders; h++)
 	{
 		const PxConstraintBatchHeader& hd = batchHeaders[h];
+		const bool isJoint = isJointHeader(hd.constraintType);
 		bool clash = false;
 		for(uint32_t j = 0; j < hd.stride; j++)
 		{
@@ -389,47 +526,86 @@ GX void PxSolveConstraintsTGS(const PxConstraintBatchHeader* batchHeaders, uint3
 		}
 		if(clash && waveOpen)
 		{
-			waveEnds.push_back(k);
+			waveEnds.push_back(uint32_t(a.size()));
+			jointWaveEnds.push_back(uint32_t(ja.size()));
 			wave++;
 		}
-		for(uint32_t j = 0; j < hd.stride; j++, k++)
+		for(uint32_t j = 0; j < hd.stride; j++)
 		{
 			const PxSolverConstraintDesc& d = descs[hd.startIndex + j];
-			a[k] = index(d.tgsBodyA);
-			b[k] = index(d.tgsBodyB);
-			if(a[k] < nbSolverBodies) lastWave[a[k]] = wave;
-			if(b[k] < nbSolverBodies) lastWave[b[k]] = wave;
-			if(d.constraint) memcpy(&rows[size_t(k) * stride], d.constraint, std::min<size_t>(size_t(d.constraintLengthOver16) * 16, stride));
+			const uint32_t ia = index(d.tgsBodyA), ib = index(d.tgsBodyB);
+			if(ia < nbSolverBodies) lastWave[ia] = wave;
+			if(ib < nbSolverBodies) lastWave[ib] = wave;
+			if(isJoint)
+			{
+				if(!d.constraint) continue;   // a joint without rows
+				ja.push_back(ia);
+				jb.push_back(ib);
+				jointDesc.push_back(&d);
+				joints.resize(joints.size() + jointBytes, 0);
+				memcpy(&joints[joints.size() - jointBytes], d.constraint, std::min<size_t>(size_t(d.constraintLengthOver16) * 16, jointBytes));
+			}
+			else
+			{
+				a.push_back(ia);
+				b.push_back(ib);
+				contactDesc.push_back(&d);
+				rows.resize(rows.size() + stride, 0);
+				if(d.constraint) memcpy(&rows[rows.size() - stride], d.constraint, std::min<size_t>(size_t(d.constraintLengthOver16) * 16, stride));
+			}
 		}
 		waveOpen = true;
 	}
-	if(n) waveEnds.push_back(n);
-	std::vector<uint32_t> broken(n ? n : 1, 0);
-	if(gbpx_solve_constraints_tgs(n ? rows.data() : nullptr, a.data(), b.data(), n, waveEnds.data(), uint32_t(waveEnds.size()), vel.data(), tx.data(),
-	                              uint32_t(vel.size()), nbSolverBodies, nbPositionIterations, nbVelocityIterations, dt, broken.data()) != GBPX_OK)
+	const uint32_t n = uint32_t(a.size()), nj = uint32_t(ja.size());
+	if(waveOpen)
+	{
+		waveEnds.push_back(n);
+		jointWaveEnds.push_back(nj);
+	}
+	std::vector<uint32_t> broken(n ? n : 1, 0), jointBroken(nj ? nj : 1, 0);
+	std::vector<float> jointForce(size_t(nj ? nj : 1) * 6, 0.0f);
+	if(gbpx_solve_constraints_joints_tgs(n ? rows.data() : nullptr, a.data(), b.data(), n, waveEnds.data(), nj ? joints.data() : nullptr, ja.data(),
+	                                     jb.data(), nj, jointWaveEnds.data(), uint32_t(waveEnds.size()), vel.data(), tx.data(), uint32_t(vel.size()),
+	                                     nbSolverBodies, nbPositionIterations, nbVelocityIterations, dt, broken.data(), jointForce.data(),
+	                                     jointBroken.data()) != GBPX_OK)
 		return;
 	memcpy(solverBodies, vel.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyVel));
 	memcpy(txInertias, tx.data(), size_t(nbSolverBodies) * sizeof(PxTGSSolverBodyTxInertia));
-	for(uint32_t h = 0, k = 0; h < nbBatchHeaders; h++)
-		for(uint32_t j = 0; j < batchHeaders[h].stride; j++, k++)
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxSolverConstraintDesc& d = *contactDesc[k];
+		if(!d.constraint) continue;
+		const size_t size = size_t(d.constraintLengthOver16) * 16;
+		memcpy(d.constraint, &rows[size_t(k) * stride], std::min<size_t>(size, stride));
+		// write-back of the last iteration: clamped friction marks its patch broken
+		if(broken[k])
 		{
-			const PxSolverConstraintDesc& d = descs[batchHeaders[h].startIndex + j];
-			if(!d.constraint) continue;
-			const size_t size = size_t(d.constraintLengthOver16) * 16;
-			memcpy(d.constraint, &rows[size_t(k) * stride], std::min<size_t>(size, stride));
-			// write-back of the last iteration: clamped friction marks its patch broken
-			if(broken[k])
-			{
-				RowTrailer tr;
-				memcpy(&tr, d.constraint + size, sizeof(tr));
-				for(uint32_t p = 0; p < MAX_PATCHES; p++)
-					if((broken[k] & (1u << p)) && tr.friction && tr.slots[p] < tr.count)
-					{
-						const uint32_t one = 1;
-						memcpy(tr.friction + size_t(tr.slots[p]) * PATCH_BYTES + PATCH_BROKEN_OFFSET, &one, 4);
-					}
-			}
+			RowTrailer tr;
+			memcpy(&tr, d.constraint + size, sizeof(tr));
+			for(uint32_t p = 0; p < MAX_PATCHES; p++)
+				if((broken[k] & (1u << p)) && tr.friction && tr.slots[p] < tr.count)
+				{
+					const uint32_t one = 1;
+					memcpy(tr.friction + size_t(tr.slots[p]) * PATCH_BYTES + PATCH_BROKEN_OFFSET, &one, 4);
+				}
 		}
+	}
+	// joints: records back into constraint memory, impulses and broken flags to the write-back
+	for(uint32_t k = 0; k < nj; k++)
+	{
+		const PxSolverConstraintDesc& d = *jointDesc[k];
+		memcpy(d.constraint, &joints[size_t(k) * jointBytes], std::min<size_t>(size_t(d.constraintLengthOver16) * 16, jointBytes));
+		if(d.writeBack)
+		{
+			JointWriteback w;
+			const float* f = &jointForce[size_t(k) * 6];
+			w.linearImpulse = PxVec3{f[0], f[1], f[2]};
+			w.angularImpulse = PxVec3{f[3], f[4], f[5]};
+			w.brokenAndResidual = jointBroken[k] ? 0x80000000u : 0u;
+			w.residual = 0.0f;
+			memcpy(d.writeBack, &w, sizeof(w));
+		}
+	}
 }
 
 GX void PxIntegrateSolverBodiesTGS(PxTGSSolverBodyVel* solverBody, const PxTGSSolverBodyTxInertia* txInertia, PxTransform* poses, uint32_t nbBodiesToIntegrate,

@@ -10,6 +10,7 @@
 // in world.cu and reuses the same device functions.
 #include "common.cuh"
 #include "solver.cuh"
+#include "joint.cuh"
 #include "batching.h"
 #include <vector>
 
@@ -260,6 +261,32 @@ __global__ void solveWaveRefKernel(ConstraintRecord* __restrict__ recs, const ui
 	vb[0] = b1.lin.x; vb[1] = b1.lin.y; vb[2] = b1.lin.z; vb[4] = b1.ang.x; vb[5] = b1.ang.y; vb[6] = b1.ang.z;
 }
 
+// One wave of joints on solver bodies in the reference's layouts: joint k
+// joins bodyA[k], bodyB[k]; conclude after the last position iteration's solve.
+__global__ void solveJointWaveRefKernel(joint::JointRecord* __restrict__ recs, const uint32_t* __restrict__ bodyA, const uint32_t* __restrict__ bodyB,
+                                        uint32_t begin, uint32_t end, float* __restrict__ vel, const float* __restrict__ tx, float elapsed, int conclude)
+{
+	const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= end) return;
+	joint::JointRecord& j = recs[k];
+	if(j.count)
+	{
+		float* va = vel + 16 * size_t(bodyA[k]);
+		float* vb = vel + 16 * size_t(bodyB[k]);
+		BodyVel b0 = loadVelRef(va), b1 = loadVelRef(vb);
+		joint::solveJoint(j, b0, b1, loadTxRef(tx + 16 * size_t(bodyA[k])), loadTxRef(tx + 16 * size_t(bodyB[k])), elapsed);
+		va[0] = b0.lin.x; va[1] = b0.lin.y; va[2] = b0.lin.z; va[4] = b0.ang.x; va[5] = b0.ang.y; va[6] = b0.ang.z;
+		vb[0] = b1.lin.x; vb[1] = b1.lin.y; vb[2] = b1.lin.z; vb[4] = b1.ang.x; vb[5] = b1.ang.y; vb[6] = b1.ang.z;
+	}
+	if(conclude) joint::concludeJoint(j);
+}
+
+__global__ void jointWriteBackKernel(const joint::JointRecord* __restrict__ recs, uint32_t n, float* __restrict__ force, uint32_t* __restrict__ broken)
+{
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k < n) joint::writeBackJoint(recs[k], force + 6 * size_t(k), broken + k);
+}
+
 // integrateCoreStep on records in the reference's layouts.
 __global__ void integrateRefKernel(float* __restrict__ vel, float* __restrict__ tx, uint32_t n, float dt)
 {
@@ -334,6 +361,28 @@ GBPX_API uint32_t gbpx_batch_constraints_tgs(const uint32_t* bodyA, const uint32
 	if(!bodyA || !bodyB || !outHeaderStart || !outHeaderStride || !outOrder) return 0;
 	batching::Result r;
 	batching::partition(bodyA, bodyB, nbConstraints, nbDyn, r);
+	for(size_t h = 0; h < r.headerStart.size(); h++)
+	{
+		outHeaderStart[h] = r.headerStart[h];
+		outHeaderStride[h] = r.headerStride[h];
+	}
+	for(uint32_t i = 0; i < nbConstraints; i++) outOrder[i] = r.order[i];
+	return uint32_t(r.headerStart.size());
+}
+
+// PxBatchConstraintsTGS over a list mixing constraint types: kind[i] is
+// constraint i's PxSolverConstraintDesc type (0 contact, 1 joint); a header
+// only joins consecutive constraints of one type.  Otherwise as
+// gbpx_batch_constraints_tgs.
+GBPX_API uint32_t gbpx_batch_typed_constraints_tgs(const uint32_t* bodyA, const uint32_t* bodyB, const uint8_t* kind, uint32_t nbConstraints,
+                                                   uint32_t nbDyn, uint32_t nbStatic, uint32_t* outHeaderStart, uint32_t* outHeaderStride,
+                                                   uint32_t* outOrder)
+{
+	(void)nbStatic;
+	if(!nbConstraints) return 0;
+	if(!bodyA || !bodyB || !kind || !outHeaderStart || !outHeaderStride || !outOrder) return 0;
+	batching::Result r;
+	batching::partition(bodyA, bodyB, nbConstraints, nbDyn, r, kind);
 	for(size_t h = 0; h < r.headerStart.size(); h++)
 	{
 		outHeaderStart[h] = r.headerStart[h];
@@ -504,6 +553,9 @@ struct TgsStageWorkspace
 	DevBuf<uint8_t> laneFlags;
 	DevBuf<tgs::FrictionState> frictionIn, frictionOut;
 	DevBuf<tgs::ConstraintRecord> recs;
+	DevBuf<joint::JointRecord> jointRecs;
+	DevBuf<uint32_t> jointA, jointB, jointBroken;
+	DevBuf<float> jointForce;
 	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
 };
 static TgsStageWorkspace* tgsStageWorkspace()
@@ -615,32 +667,48 @@ GBPX_API int gbpx_create_contact_constraints_tgs(uint32_t n, const void* vel0, c
 	return GBPX_OK;
 }
 
-// PxSolveConstraintsTGS: rows (n blocks of gbpx_constraint_row_stride() bytes,
-// in solve order, updated in place with the accumulated impulses), constraint
-// k joining bodies bodyA[k], bodyB[k] of the body arrays; the constraints
-// [waveEnds[w-1], waveEnds[w]) touch distinct bodies.  bodyVel/bodyTxI:
-// nbBodies records in the reference's layouts, updated in place; the first
-// nbIntegrate bodies are integrated after every position iteration.
-// dt = time step / nbPositionIterations.  outBroken (may be null): per
-// constraint, bit p set when patch p's friction was clamped in the last
-// iteration (the broken flag its friction patch gets).
-GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
-                                        void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
-                                        uint32_t* outBroken)
+// PxSolveConstraintsTGS over contacts and joints: contact rows (n blocks of
+// gbpx_constraint_row_stride() bytes, in solve order, updated in place with
+// the accumulated impulses), contact k joining bodies bodyA[k], bodyB[k]; joint
+// records (nbJoints of gbpx_joint_record_bytes(), from
+// gbpx_create_joint_constraints_tgs, in solve order, updated in place), joint
+// k joining jointA[k], jointB[k].  Wave w solves contacts [waveEnds[w-1],
+// waveEnds[w]) and joints [jointWaveEnds[w-1], jointWaveEnds[w]), which touch
+// distinct dynamic bodies.  bodyVel/bodyTxI: nbBodies records in the
+// reference's layouts, updated in place; the first nbIntegrate bodies are
+// integrated after every position iteration.  dt = time step /
+// nbPositionIterations.  outBroken (may be null): per contact, bit p set when
+// patch p's friction was clamped in the last iteration.  outJointForce /
+// outJointBroken (may be null): per joint the write-back impulse (linear,
+// angular) and broken flag.
+GBPX_API int gbpx_solve_constraints_joints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds,
+                                               void* jointRecords, const uint32_t* jointA, const uint32_t* jointB, uint32_t nbJoints,
+                                               const uint32_t* jointWaveEnds, uint32_t nbWaves, void* bodyVel, void* bodyTxI, uint32_t nbBodies,
+                                               uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt, uint32_t* outBroken, float* outJointForce,
+                                               uint32_t* outJointBroken)
 {
 	gbpx::Zone zone("gbpx::solveConstraintsTGS");
 	if(!bodyVel || !bodyTxI || !nbBodies || nbIntegrate > nbBodies || !nbPos || !(dt > 0.0f)) return GBPX_ERR_INVALID;
 	if(n && (!rows || !bodyA || !bodyB || !waveEnds || !nbWaves || waveEnds[nbWaves - 1] != n)) return GBPX_ERR_INVALID;
+	if(nbJoints && (!jointRecords || !jointA || !jointB || !jointWaveEnds || !nbWaves || jointWaveEnds[nbWaves - 1] != nbJoints))
+		return GBPX_ERR_INVALID;
 	for(uint32_t k = 0; k < n; k++)
 		if(bodyA[k] >= nbBodies || bodyB[k] >= nbBodies) return GBPX_ERR_INVALID;
+	for(uint32_t k = 0; k < nbJoints; k++)
+		if(jointA[k] >= nbBodies || jointB[k] >= nbBodies) return GBPX_ERR_INVALID;
+	for(uint32_t w = 0; w < nbWaves; w++)
+		if((n && (waveEnds[w] > n || (w && waveEnds[w] < waveEnds[w - 1]))) ||
+		   (nbJoints && (jointWaveEnds[w] > nbJoints || (w && jointWaveEnds[w] < jointWaveEnds[w - 1]))))
+			return GBPX_ERR_INVALID;
 	TgsStageWorkspace* ws = tgsStageWorkspace();
 	if(!ws) return GBPX_ERR_CUDA;
-	const size_t m = n ? n : 1;
+	const size_t m = n ? n : 1, mj = nbJoints ? nbJoints : 1;
 	if(ws->vel.reserve(16 * size_t(nbBodies)) || ws->tx.reserve(16 * size_t(nbBodies)) || ws->bodyA.reserve(m) || ws->bodyB.reserve(m) ||
-	   ws->recs.reserve(m) || (outBroken && ws->broken.reserve(m)))
+	   ws->recs.reserve(m) || (outBroken && ws->broken.reserve(m)) || ws->jointRecs.reserve(mj) || ws->jointA.reserve(mj) ||
+	   ws->jointB.reserve(mj) || ws->jointForce.reserve(6 * mj) || ws->jointBroken.reserve(mj))
 		return GBPX_ERR_NOMEM;
-	if(outBroken && n) GBPX_CUDA_TRY(cudaMemsetAsync(ws->broken.ptr, 0, size_t(n) * 4, ws->stream));
 	cudaStream_t s = ws->stream;
+	if(outBroken && n) GBPX_CUDA_TRY(cudaMemsetAsync(ws->broken.ptr, 0, size_t(n) * 4, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->vel.ptr, bodyVel, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->tx.ptr, bodyTxI, size_t(nbBodies) * 64, cudaMemcpyHostToDevice, s));
 	if(n)
@@ -649,31 +717,65 @@ GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const
 		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodyB.ptr, bodyB, size_t(n) * 4, cudaMemcpyHostToDevice, s));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->recs.ptr, rows, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyHostToDevice, s));
 	}
+	if(nbJoints)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->jointA.ptr, jointA, size_t(nbJoints) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->jointB.ptr, jointB, size_t(nbJoints) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->jointRecs.ptr, jointRecords, size_t(nbJoints) * sizeof(joint::JointRecord), cudaMemcpyHostToDevice, s));
+	}
 	float elapsed = 0.0f;
-	auto sweep = [&](float minPen, bool last) {
+	auto sweep = [&](float minPen, bool last, bool conclude) {
 		for(uint32_t w = 0; w < nbWaves; w++)
 		{
-			const uint32_t b = w ? waveEnds[w - 1] : 0u, e = waveEnds[w];
-			if(e > b)
-				tgs::solveWaveRefKernel<<<divUp(e - b, 128), 128, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, minPen, elapsed,
-				                                                         last && outBroken ? ws->broken.ptr : nullptr);
+			if(n)
+			{
+				const uint32_t b = w ? waveEnds[w - 1] : 0u, e = waveEnds[w];
+				if(e > b)
+					tgs::solveWaveRefKernel<<<divUp(e - b, 128), 128, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, minPen,
+					                                                         elapsed, last && outBroken ? ws->broken.ptr : nullptr);
+			}
+			if(nbJoints)
+			{
+				const uint32_t b = w ? jointWaveEnds[w - 1] : 0u, e = jointWaveEnds[w];
+				if(e > b)
+					tgs::solveJointWaveRefKernel<<<divUp(e - b, 64), 64, 0, s>>>(ws->jointRecs.ptr, ws->jointA.ptr, ws->jointB.ptr, b, e, ws->vel.ptr,
+					                                                            ws->tx.ptr, elapsed, conclude ? 1 : 0);
+			}
 		}
 	};
+	const bool any = n || nbJoints;
 	for(uint32_t it = 0; it < nbPos; it++)
 	{
-		if(n) sweep(-FLT_MAX, !nbVel && it + 1 == nbPos);
+		if(any) sweep(-FLT_MAX, !nbVel && it + 1 == nbPos, it + 1 == nbPos);
 		if(nbIntegrate) tgs::integrateRefKernel<<<divUp(nbIntegrate, 128), 128, 0, s>>>(ws->vel.ptr, ws->tx.ptr, nbIntegrate, dt);
 		elapsed += dt;
 	}
 	for(uint32_t it = 0; it < nbVel; it++)
-		if(n) sweep(0.0f, it + 1 == nbVel);
+		if(any) sweep(0.0f, it + 1 == nbVel, false);
+	if(nbJoints) tgs::jointWriteBackKernel<<<divUp(nbJoints, 128), 128, 0, s>>>(ws->jointRecs.ptr, nbJoints, ws->jointForce.ptr, ws->jointBroken.ptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyVel, ws->vel.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(bodyTxI, ws->tx.ptr, size_t(nbBodies) * 64, cudaMemcpyDeviceToHost, s));
 	if(n) GBPX_CUDA_TRY(cudaMemcpyAsync(rows, ws->recs.ptr, size_t(n) * sizeof(tgs::ConstraintRecord), cudaMemcpyDeviceToHost, s));
 	if(n && outBroken) GBPX_CUDA_TRY(cudaMemcpyAsync(outBroken, ws->broken.ptr, size_t(n) * 4, cudaMemcpyDeviceToHost, s));
+	if(nbJoints)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(jointRecords, ws->jointRecs.ptr, size_t(nbJoints) * sizeof(joint::JointRecord), cudaMemcpyDeviceToHost, s));
+		if(outJointForce) GBPX_CUDA_TRY(cudaMemcpyAsync(outJointForce, ws->jointForce.ptr, size_t(nbJoints) * 24, cudaMemcpyDeviceToHost, s));
+		if(outJointBroken) GBPX_CUDA_TRY(cudaMemcpyAsync(outJointBroken, ws->jointBroken.ptr, size_t(nbJoints) * 4, cudaMemcpyDeviceToHost, s));
+	}
 	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 	return GBPX_OK;
+}
+
+// PxSolveConstraintsTGS over contacts only: as gbpx_solve_constraints_joints_tgs
+// without joints.
+GBPX_API int gbpx_solve_constraints_tgs(void* rows, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds, uint32_t nbWaves,
+                                        void* bodyVel, void* bodyTxI, uint32_t nbBodies, uint32_t nbIntegrate, uint32_t nbPos, uint32_t nbVel, float dt,
+                                        uint32_t* outBroken)
+{
+	return gbpx_solve_constraints_joints_tgs(rows, bodyA, bodyB, n, waveEnds, nullptr, nullptr, nullptr, 0, nullptr, nbWaves, bodyVel, bodyTxI,
+	                                         nbBodies, nbIntegrate, nbPos, nbVel, dt, outBroken, nullptr, nullptr);
 }
 
 // PxIntegrateSolverBodiesTGS: world angular velocity written back into the

@@ -79,3 +79,41 @@ def tgs_step(rigid, static_poses, body_a, body_b, contact_start, contact_count, 
                            dt, nb_pos, nb_vel, bounce, friction_offset, correlation, _p(vel), _p(pose), _p(hs), _p(hst),
                            _p(order), ctypes.byref(nh)), "TGS step")
     return vel, pose, hs[:nh.value].copy(), hst[:nh.value].copy(), order[:nc].copy()
+
+
+def joint_frame(frame, dt=1.0 / 60.0, nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0), batch=True):
+    """One TGS frame of joints on the GB300 (gbpx_joint_frame: construct bodies,
+    PxBatchConstraintsTGS over the joints, PxCreateJointConstraintsTGS, solve,
+    write-back, PxIntegrateSolverBodiesTGS).  frame: dict of nb_dyn,
+    static_poses, joint_a, joint_b, rigid (PxRigidBodyData), rows
+    (Px1DConstraint records, 80 bytes), row_start, row_count, params (20 floats
+    per joint).  Returns velocities (n,6), poses (n,7), headers (start,
+    stride, type), the joint order, per-joint impulses (J,6) and broken flags."""
+    L = _setup()
+    A = np.ascontiguousarray(frame["joint_a"], np.uint32)
+    B = np.ascontiguousarray(frame["joint_b"], np.uint32)
+    n = int(frame["nb_dyn"])
+    statics = np.ascontiguousarray(frame["static_poses"], np.float32)
+    nj = len(A)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nj, 1), np.uint32)
+    hst = np.zeros(max(nj, 1), np.uint32)
+    ht = np.zeros(max(nj, 1), np.uint32)
+    order = np.zeros(max(nj, 1), np.uint32)
+    force = np.zeros((max(nj, 1), 6), np.float32)
+    broken = np.zeros(max(nj, 1), np.uint32)
+    nh = np.zeros(1, np.uint32)
+    g = np.asarray(gravity, np.float32)
+    keep = [np.ascontiguousarray(frame["rigid"]), np.ascontiguousarray(frame["row_start"], np.uint32),
+            np.ascontiguousarray(frame["row_count"], np.uint32), np.ascontiguousarray(frame["rows"]),
+            np.ascontiguousarray(frame["params"], np.float32)]
+    L.gbpx_joint_frame.argtypes = ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_uint32] + [ctypes.c_void_p] * 5 +
+                                   [ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32] + [ctypes.c_void_p] * 9)
+    check(L.gbpx_joint_frame(_p(keep[0]), n, _p(statics), len(statics), _p(A), _p(B), nj, _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4]),
+                             _p(g), dt, nb_pos, nb_vel, 1 if batch else 0, _p(vel), _p(pose), _p(hs), _p(hst), _p(ht), _p(order), _p(force),
+                             _p(broken), _p(nh)), "gbpx_joint_frame")
+    k = int(nh[0])
+    return dict(vel=vel, pose=pose, header_start=hs[:k].copy(), header_stride=hst[:k].copy(), header_type=ht[:k].copy(),
+                order=order[:nj].copy(), force=force[:nj].copy(), broken=broken[:nj].copy())

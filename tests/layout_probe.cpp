@@ -50,6 +50,19 @@ int main(){
  O(PxTGSSolverContactDesc, numFrictionPatches); O(PxTGSSolverContactDesc, startContactPatchIndex); O(PxTGSSolverContactDesc, numContactPatches);
  O(PxTGSSolverContactDesc, axisConstraintCount); O(PxTGSSolverContactDesc, maxImpulse); O(PxTGSSolverContactDesc, torsionalPatchRadius);
  O(PxTGSSolverContactDesc, minTorsionalPatchRadius); O(PxTGSSolverContactDesc, offsetSlop);
+ S(Px1DConstraint); O(Px1DConstraint, geometricError); O(Px1DConstraint, angular0); O(Px1DConstraint, velocityTarget); O(Px1DConstraint, linear1);
+ O(Px1DConstraint, minImpulse); O(Px1DConstraint, angular1); O(Px1DConstraint, maxImpulse); O(Px1DConstraint, mods); O(Px1DConstraint, flags);
+ O(Px1DConstraint, solveHint);
+ S(PxTGSSolverConstraintPrepDesc); O(PxTGSSolverConstraintPrepDesc, invMassScales); O(PxTGSSolverConstraintPrepDesc, desc);
+ O(PxTGSSolverConstraintPrepDesc, body0); O(PxTGSSolverConstraintPrepDesc, body1); O(PxTGSSolverConstraintPrepDesc, body0TxI);
+ O(PxTGSSolverConstraintPrepDesc, body1TxI); O(PxTGSSolverConstraintPrepDesc, bodyData0); O(PxTGSSolverConstraintPrepDesc, bodyData1);
+ O(PxTGSSolverConstraintPrepDesc, bodyFrame0); O(PxTGSSolverConstraintPrepDesc, bodyFrame1); O(PxTGSSolverConstraintPrepDesc, bodyState0);
+ O(PxTGSSolverConstraintPrepDesc, bodyState1); O(PxTGSSolverConstraintPrepDesc, writeback); O(PxTGSSolverConstraintPrepDesc, rows);
+ O(PxTGSSolverConstraintPrepDesc, numRows); O(PxTGSSolverConstraintPrepDesc, linBreakForce); O(PxTGSSolverConstraintPrepDesc, angBreakForce);
+ O(PxTGSSolverConstraintPrepDesc, minResponseThreshold); O(PxTGSSolverConstraintPrepDesc, disablePreprocessing);
+ O(PxTGSSolverConstraintPrepDesc, improvedSlerp); O(PxTGSSolverConstraintPrepDesc, driveLimitsAreForces); O(PxTGSSolverConstraintPrepDesc, extendedLimits);
+ O(PxTGSSolverConstraintPrepDesc, disableConstraint); O(PxTGSSolverConstraintPrepDesc, body0WorldOffset); O(PxTGSSolverConstraintPrepDesc, cA2w);
+ O(PxTGSSolverConstraintPrepDesc, cB2w);
  printf("\"end\": 0\n}\n");
  return 0;
 }
