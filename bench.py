@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--large-cpu-frames", type=int, default=1)
     ap.add_argument("--large-bodies", type=int, default=0,
                     help="block-per-scene threshold of the world's scene stages (0 = autotuned for the scene-size histogram)")
+    ap.add_argument("--joint-frames", type=int, default=20)
+    ap.add_argument("--profile-extra", default="", choices=["", "broadphase", "large-scene", "joints"],
+                    help="only run one frame of this side workload inside a profiler range and exit")
     ap.add_argument("--profile-step", type=int, default=0,
                     help="only build the state (pre-roll, autotune, warm-up), then run this many un-captured steps inside a "
                          "profiler range (for ncu --profile-from-start off) and exit")
@@ -346,6 +349,91 @@ def bench_large_scene(steps, cpu_frames):
                                   sample="%d persistent frame(s) of the final state, oracle restatement, one thread" % cpu_frames))
 
 
+def joint_workload(chains=1500):
+    """The joint bench frame: `chains` chains of 2-9 boxes hung from static
+    anchors by spherical / revolute / fixed / prismatic / sprung joints (rows
+    written from the poses, as a joint shader would), the frame after one
+    settling frame."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from joint_scenes import joint_frame, make_joint_scene
+    from oracle_libs import advance_rigid, run_joints
+    sc = make_joint_scene(77, nb_chains=chains, links=(2, 9))
+    fr = joint_frame(sc, sc["rigid"])
+    r = run_joints("orc", fr)
+    return joint_frame(sc, advance_rigid(sc["rigid"], r["vel"], r["pose"]))
+
+
+def bench_joints(frames, cpu_frames):
+    """Joints (PxCreateJointConstraintsTGS + PxSolveConstraintsTGS, 4 position +
+    1 velocity iterations) through gbpx_joint_frame with host arrays in and out,
+    against the oracle's frame on one host thread."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import run_joints
+    from physx_gb300.solver import joint_frame as gpu_joint_frame
+    fr = joint_workload()
+    nj, nrows = len(fr["joint_a"]), len(fr["rows"])
+    for _ in range(3):
+        gpu_joint_frame(fr)
+    times = []
+    for _ in range(frames):
+        t = time.perf_counter()
+        out = gpu_joint_frame(fr)
+        times.append(time.perf_counter() - t)
+    ms = 1000.0 * float(np.median(times))
+    t = time.perf_counter()
+    for _ in range(cpu_frames):
+        run_joints("orc", fr)
+    cpu_ms = 1000.0 * (time.perf_counter() - t) / cpu_frames
+    types = np.bincount(out["header_type"], minlength=9)
+    return dict(workload="%d joints (%d rows) in 1500 chains of 2-9 boxes hung from static anchors: spherical / revolute / fixed / "
+                         "prismatic / sprung joints with limits, drives, restitution, break forces" % (nj, nrows),
+                joints=nj, rows=nrows, bodies=int(fr["nb_dyn"]), headers_per_pair_path=int(types[2]), headers_4_wide=int(types[8]),
+                frames=frames, ms_per_frame=ms, value=nj / (ms / 1000.0), unit="joints/s (one TGS frame each)",
+                e2e_note="host arrays in (bodies, rows, parameters), velocities, poses and impulses out, every frame",
+                cpu_baseline=dict(value=nj / (cpu_ms / 1000.0), ms_per_frame=cpu_ms, unit="joints/s", cores=1, kind="port",
+                                  sample="%d frame(s) of the same state, oracle restatement, one thread" % cpu_frames))
+
+
+def profile_extra(which):
+    """One frame of a side workload inside a profiler range (for ncu
+    --profile-from-start off), after untimed warm-up frames."""
+    import physx_gb300
+    L = physx_gb300.lib()
+    if which == "broadphase":
+        from physx_gb300.broadphase import BroadPhase
+        from physx_gb300.workloads import aabb_stress_frames
+        bp = BroadPhase()
+        for f, fr in enumerate(aabb_stress_frames(frames=4)):
+            if f == 3:
+                physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+            bp.update(fr["created"], fr["updated"], fr["removed"], fr["bounds"], fr["groups"], fr["distances"], fr["capacity"])
+            bp.fetch_results()
+            if f == 3:
+                physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        out = bp.stats()
+        bp.release()
+    elif which == "large-scene":
+        from physx_gb300.scene import Scene
+        from physx_gb300.workloads import large_scene
+        s = Scene(large_scene())
+        s.step(300)
+        physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+        s.step(1)
+        physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        out = s.stats()
+        s.release()
+    else:
+        from physx_gb300.solver import joint_frame as gpu_joint_frame
+        fr = joint_workload()
+        gpu_joint_frame(fr)
+        physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+        r = gpu_joint_frame(fr)
+        physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        out = dict(joints=len(fr["joint_a"]), headers=len(r["header_start"]))
+    print(json.dumps(dict(profiled=which, **{k: (int(v) if hasattr(v, "__int__") else v) for k, v in out.items()})))
+
+
 def dist_setup(n):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world != n:
@@ -380,6 +468,9 @@ def reduce_over_ranks(ms, bodies, dist):
 def main():
     a = parse()
     import numpy as np
+    if a.profile_extra:
+        profile_extra(a.profile_extra)
+        return
     rank, world, dist = dist_setup(a.gpus)
     from physx_gb300.workloads import batched_scenes
     from physx_gb300.world import DEFAULT_PARAMS
@@ -539,7 +630,7 @@ def main():
     extras = None
     if a.extras:
         extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames),
-                      large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames))
+                      large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames), joints=bench_joints(a.joint_frames, 5))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
