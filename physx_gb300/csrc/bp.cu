@@ -78,6 +78,8 @@ __device__ __forceinline__ bool groupFilter(uint32_t g0, uint32_t g1, uint32_t l
 
 __global__ void applyRemovedKernel(const uint32_t* __restrict__ ids, uint32_t n, uint8_t* __restrict__ live, uint8_t* __restrict__ flags)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n) return;
 	const uint32_t id = ids[i];
@@ -88,6 +90,8 @@ __global__ void applyRemovedKernel(const uint32_t* __restrict__ ids, uint32_t n,
 __global__ void applyUpdatesKernel(const UpdateRec* __restrict__ recs, uint32_t n, uint2* __restrict__ bx, float4* __restrict__ byz,
                                    uint32_t* __restrict__ groups, uint8_t* __restrict__ live, uint8_t* __restrict__ flags)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n) return;
 	const UpdateRec r = recs[i];
@@ -107,6 +111,8 @@ __global__ void applyUpdatesKernel(const UpdateRec* __restrict__ recs, uint32_t 
 __global__ void applyDeviceBoundsKernel(const float* __restrict__ bounds, uint32_t n, uint2* __restrict__ bx, float4* __restrict__ byz,
                                         uint8_t* __restrict__ flags)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n) return;
 	const float* r = bounds + 6 * size_t(i);
@@ -118,6 +124,8 @@ __global__ void applyDeviceBoundsKernel(const float* __restrict__ bounds, uint32
 // Stable compaction of live handles into (key = encoded min X, value = handle).
 __global__ void countLiveKernel(const uint8_t* __restrict__ live, uint32_t cap, uint32_t* __restrict__ blockCounts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool v = i < cap && live[i];
 	const uint32_t b = __syncthreads_count(v);
@@ -127,6 +135,8 @@ __global__ void countLiveKernel(const uint8_t* __restrict__ live, uint32_t cap, 
 __global__ void emitLiveKernel(const uint8_t* __restrict__ live, const uint2* __restrict__ bx, uint32_t cap,
                                const uint32_t* __restrict__ blockOffsets, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpCounts[32];
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool v = i < cap && live[i];
@@ -160,6 +170,8 @@ __global__ void gatherSortedKernel(const uint32_t* __restrict__ sortedIds, uint3
                                    const float4* __restrict__ byz, const uint32_t* __restrict__ groups, const uint8_t* __restrict__ flags,
                                    uint2* __restrict__ sx, float4* __restrict__ syz, uint32_t* __restrict__ sgrp, uint32_t* __restrict__ supd)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= n) return;
 	const uint32_t id = sortedIds[p];
@@ -172,6 +184,8 @@ __global__ void gatherSortedKernel(const uint32_t* __restrict__ sortedIds, uint3
 // Stable compaction of sorted positions that were / were not updated.
 __global__ void countFlagKernel(const uint32_t* __restrict__ flag, uint32_t n, uint32_t want, uint32_t* __restrict__ blockCounts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool v = i < n && flag[i] == want;
 	const uint32_t b = __syncthreads_count(v);
@@ -181,6 +195,8 @@ __global__ void countFlagKernel(const uint32_t* __restrict__ flag, uint32_t n, u
 __global__ void emitFlagKernel(const uint32_t* __restrict__ flag, uint32_t n, uint32_t want, const uint32_t* __restrict__ blockOffsets,
                                uint32_t* __restrict__ out)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpCounts[32];
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool v = i < n && flag[i] == want;
@@ -233,6 +249,8 @@ __global__ void sweepUpdatedKernel(const uint32_t* __restrict__ updPos, uint32_t
                                    const float4* __restrict__ syz, const uint32_t* __restrict__ sgrp, const uint32_t* __restrict__ sortedIds,
                                    uint32_t lutLo, uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
@@ -273,6 +291,8 @@ __global__ void sweepSleepingKernel(const uint32_t* __restrict__ sleepPos, uint3
                                     uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter,
                                     uint4* __restrict__ longScans, unsigned long long* __restrict__ longCount)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31;
 	uint32_t p = 0, lo = nbUpd;
@@ -358,6 +378,8 @@ __global__ void __launch_bounds__(256) sweepLongKernel(const uint4* __restrict__
                                                        const uint32_t* __restrict__ sortedIds, uint32_t lutLo, uint32_t lutHi,
                                                        unsigned long long* __restrict__ out, uint32_t cap, uint32_t* __restrict__ counter)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const unsigned long long lc = *longCount;
 	const uint32_t items = uint32_t(lc >> 32), chunks = uint32_t(lc);
 	const uint32_t lane = threadIdx.x & 31;
@@ -417,6 +439,8 @@ __global__ void __launch_bounds__(256) sweepUpdatedTiledKernel(const uint32_t* _
                                                                uint32_t lutLo, uint32_t lutHi, unsigned long long* __restrict__ out, uint32_t cap,
                                                                uint32_t* __restrict__ counter)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t tMinX[SWEEP_TILE], tGrp[SWEEP_TILE], tId[SWEEP_TILE];
 	__shared__ float4 tYZ[SWEEP_TILE];
 	__shared__ uint32_t warpNext[8];
@@ -530,6 +554,8 @@ __global__ void __launch_bounds__(256) sweepSleepingTiledKernel(const uint32_t* 
                                                                 uint32_t* __restrict__ counter, uint4* __restrict__ longScans,
                                                                 unsigned long long* __restrict__ longCount)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t tGrp[SLEEP_TILE], tId[SLEEP_TILE];
 	__shared__ float4 tYZ[SLEEP_TILE];
 	__shared__ SleepBox boxes[SLEEP_PER_BLOCK];
@@ -644,6 +670,8 @@ __device__ __forceinline__ uint32_t lowerBound(const unsigned long long* __restr
 __global__ void classifyFoundKernel(const unsigned long long* __restrict__ found, uint32_t nFound, const unsigned long long* __restrict__ prev,
                                     uint32_t nPrev, uint32_t* __restrict__ isCreated)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= nFound) return;
 	isCreated[i] = containsKey(prev, nPrev, found[i]) ? 0u : 1u;
@@ -654,6 +682,8 @@ __global__ void classifyFoundKernel(const unsigned long long* __restrict__ found
 __global__ void classifyPrevKernel(const unsigned long long* __restrict__ prev, uint32_t nPrev, const unsigned long long* __restrict__ found,
                                    uint32_t nFound, const uint8_t* __restrict__ flags, uint32_t* __restrict__ cls)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= nPrev) return;
 	const unsigned long long k = prev[i];
@@ -669,6 +699,8 @@ __global__ void classifyPrevKernel(const unsigned long long* __restrict__ prev, 
 
 __global__ void flagEqualsKernel(const uint32_t* __restrict__ cls, uint32_t n, uint32_t want, uint32_t* __restrict__ out)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n) out[i] = cls[i] == want ? 1u : 0u;
 }
@@ -676,6 +708,8 @@ __global__ void flagEqualsKernel(const uint32_t* __restrict__ cls, uint32_t n, u
 __global__ void scatterSelectedKernel(const unsigned long long* __restrict__ src, const uint32_t* __restrict__ sel,
                                       const uint32_t* __restrict__ pos, uint32_t n, unsigned long long* __restrict__ dst)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n && sel[i]) dst[pos[i]] = src[i];
 }
@@ -684,6 +718,8 @@ __global__ void scatterSelectedKernel(const unsigned long long* __restrict__ src
 __global__ void mergeKernel(const unsigned long long* __restrict__ a, uint32_t na, const unsigned long long* __restrict__ b, uint32_t nb,
                             unsigned long long* __restrict__ out)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < na) out[i + lowerBound(b, nb, a[i])] = a[i];
 	else if(i < na + nb)
@@ -695,6 +731,8 @@ __global__ void mergeKernel(const unsigned long long* __restrict__ a, uint32_t n
 
 __global__ void keysToPairsKernel(const unsigned long long* __restrict__ keys, uint32_t n, uint2* __restrict__ out)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n) out[i] = make_uint2(uint32_t(keys[i] >> 32), uint32_t(keys[i]));
 }
@@ -810,10 +848,10 @@ struct BroadPhase
 	{
 		const uint32_t nb = divUp(n, 256);
 		if(blockCounts.reserve(nb + 1)) return GBPX_ERR_NOMEM;
-		bp::countFlagKernel<<<nb, 256, 0, stream>>>(flag, n, want, blockCounts.ptr);
+		(void)launchDependent(bp::countFlagKernel, nb, 256, stream, flag, n, want, blockCounts.ptr);
 		if(cudaMemsetAsync(blockCounts.ptr + nb, 0, 4, stream) != cudaSuccess) return GBPX_ERR_CUDA;
-		rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nb + 1);
-		bp::emitFlagKernel<<<nb, 256, 0, stream>>>(flag, n, want, blockCounts.ptr, out);
+		(void)launchDependent(rs::scanKernel, 1, 1024, stream, blockCounts.ptr, nb + 1);
+		(void)launchDependent(bp::emitFlagKernel, nb, 256, stream, flag, n, want, blockCounts.ptr, out);
 		return GBPX_OK;
 	}
 
@@ -876,12 +914,12 @@ struct BroadPhase
 		if(nbRemoved)
 		{
 			GBPX_CUDA_TRY(cudaMemcpyAsync(dRemoved.ptr, removedIds, size_t(nbRemoved) * 4, cudaMemcpyHostToDevice, stream));
-			bp::applyRemovedKernel<<<divUp(nbRemoved, 256), 256, 0, stream>>>(dRemoved.ptr, nbRemoved, live.ptr, flags.ptr);
+			(void)launchDependent(bp::applyRemovedKernel, divUp(nbRemoved, 256), 256, stream, dRemoved.ptr, nbRemoved, live.ptr, flags.ptr);
 		}
 		if(nbRec)
 		{
 			GBPX_CUDA_TRY(cudaMemcpyAsync(dRecs.ptr, hRecs.ptr, size_t(nbRec) * sizeof(bp::UpdateRec), cudaMemcpyHostToDevice, stream));
-			bp::applyUpdatesKernel<<<divUp(nbRec, 256), 256, 0, stream>>>(dRecs.ptr, nbRec, bx.ptr, byz.ptr, groups.ptr, live.ptr, flags.ptr);
+			(void)launchDependent(bp::applyUpdatesKernel, divUp(nbRec, 256), 256, stream, dRecs.ptr, nbRec, bx.ptr, byz.ptr, groups.ptr, live.ptr, flags.ptr);
 		}
 		return runFrame(nbRec + nbRemoved);
 	}
@@ -892,9 +930,9 @@ struct BroadPhase
 		// 2. Live boxes sorted by encoded min X.
 		const uint32_t nbBlk = divUp(capacity, 256);
 		if(blockCounts.reserve(nbBlk + 1)) return GBPX_ERR_NOMEM;
-		bp::countLiveKernel<<<nbBlk, 256, 0, stream>>>(live.ptr, capacity, blockCounts.ptr);
+		(void)launchDependent(bp::countLiveKernel, nbBlk, 256, stream, live.ptr, capacity, blockCounts.ptr);
 		GBPX_CUDA_TRY(cudaMemsetAsync(blockCounts.ptr + nbBlk, 0, 4, stream));
-		rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nbBlk + 1);
+		(void)launchDependent(rs::scanKernel, 1, 1024, stream, blockCounts.ptr, nbBlk + 1);
 		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + nbBlk, 4, cudaMemcpyDeviceToHost, stream));
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		const uint32_t n = hCounts.ptr[0];
@@ -902,11 +940,11 @@ struct BroadPhase
 		   hist.reserve(radixSortHistEntries(n) + 1) || sx.reserve(n + 1) || syz.reserve(n + 1) || sgrp.reserve(n + 1) ||
 		   supd.reserve(n + 1) || updPos.reserve(n + 1) || sleepPos.reserve(n + 1))
 			return GBPX_ERR_NOMEM;
-		bp::emitLiveKernel<<<nbBlk, 256, 0, stream>>>(live.ptr, bx.ptr, capacity, blockCounts.ptr, keysA.ptr, valsA.ptr);
+		(void)launchDependent(bp::emitLiveKernel, nbBlk, 256, stream, live.ptr, bx.ptr, capacity, blockCounts.ptr, keysA.ptr, valsA.ptr);
 		const bool alt = radixSort<uint32_t, true>(keysA.ptr, valsA.ptr, keysB.ptr, valsB.ptr, n, 0, 32, hist.ptr, stream);
 		const uint32_t* sortedIds = alt ? valsB.ptr : valsA.ptr;
 		if(n)
-			bp::gatherSortedKernel<<<divUp(n, 256), 256, 0, stream>>>(sortedIds, n, bx.ptr, byz.ptr, groups.ptr, flags.ptr, sx.ptr, syz.ptr,
+			(void)launchDependent(bp::gatherSortedKernel, divUp(n, 256), 256, stream, sortedIds, n, bx.ptr, byz.ptr, groups.ptr, flags.ptr, sx.ptr, syz.ptr,
 			                                                        sgrp.ptr, supd.ptr);
 
 		// 3. Split sorted positions into updated / sleeping lists.
@@ -932,25 +970,25 @@ struct BroadPhase
 			{
 				unsigned long long* longCount = reinterpret_cast<unsigned long long*>(counter.ptr + 2);
 				if(sweepTiled)
-					bp::sweepUpdatedTiledKernel<<<std::min<uint32_t>(divUp(nbUpd, bp::UPD_PER_BLOCK), 152u * 64u), 256, 0, stream>>>(
+					(void)launchDependent(bp::sweepUpdatedTiledKernel, std::min<uint32_t>(divUp(nbUpd, bp::UPD_PER_BLOCK), 152u * 64u), 256, stream, 
 					    updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF, counter.ptr);
 				else
 				{
 					const uint32_t blocks = std::min<uint32_t>(divUp(uint64_t(nbUpd) * 32, 256), 152u * 64u);
-					bp::sweepUpdatedKernel<<<blocks, 256, 0, stream>>>(updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
+					(void)launchDependent(bp::sweepUpdatedKernel, blocks, 256, stream, updPos.ptr, nbUpd, n, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi,
 					                                                  found.ptr, capF, counter.ptr);
 				}
 				if(nbSleep)
 				{
 					if(sweepTiled)
-						bp::sweepSleepingTiledKernel<<<std::min<uint32_t>(divUp(nbSleep, bp::SLEEP_PER_BLOCK), 152u * 64u), 256, 0, stream>>>(
+						(void)launchDependent(bp::sweepSleepingTiledKernel, std::min<uint32_t>(divUp(nbSleep, bp::SLEEP_PER_BLOCK), 152u * 64u), 256, stream, 
 						    sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
 						    counter.ptr, longScans.ptr, longCount);
 					else
-						bp::sweepSleepingKernel<<<divUp(nbSleep, 256), 256, 0, stream>>>(sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
+						(void)launchDependent(bp::sweepSleepingKernel, divUp(nbSleep, 256), 256, stream, sleepPos.ptr, nbSleep, updPos.ptr, nbUpd, sx.ptr, syz.ptr,
 						                                                                 sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr, capF,
 						                                                                 counter.ptr, longScans.ptr, longCount);
-					bp::sweepLongKernel<<<152u * 8u, 256, 0, stream>>>(longScans.ptr, reinterpret_cast<const unsigned long long*>(counter.ptr + 2),
+					(void)launchDependent(bp::sweepLongKernel, 152u * 8u, 256, stream, longScans.ptr, reinterpret_cast<const unsigned long long*>(counter.ptr + 2),
 					                                                    updPos.ptr, sx.ptr, syz.ptr, sgrp.ptr, sortedIds, lutLo, lutHi, found.ptr,
 					                                                    capF, counter.ptr);
 				}
@@ -987,10 +1025,10 @@ struct BroadPhase
 		uint32_t nCreated = 0, nLost = 0, nKeep = 0;
 		if(nFound)
 		{
-			bp::classifyFoundKernel<<<divUp(nFound, 256), 256, 0, stream>>>(F, nFound, prev.ptr, nPrev, sel.ptr);
+			(void)launchDependent(bp::classifyFoundKernel, divUp(nFound, 256), 256, stream, F, nFound, prev.ptr, nPrev, sel.ptr);
 			int r2 = scanSelect(sel.ptr, nFound, pos.ptr, &nCreated);
 			if(r2) return r2;
-			bp::scatterSelectedKernel<<<divUp(nFound, 256), 256, 0, stream>>>(F, sel.ptr, pos.ptr, nFound, created.ptr);
+			(void)launchDependent(bp::scatterSelectedKernel, divUp(nFound, 256), 256, stream, F, sel.ptr, pos.ptr, nFound, created.ptr);
 		}
 		unsigned long long* keep = lost.ptr + 0;  // placeholder, reassigned below
 		DevBuf<unsigned long long>& keepBuf = foundAlt.ptr == F ? found : foundAlt;  // the sort buffer not holding F
@@ -998,19 +1036,19 @@ struct BroadPhase
 		keep = keepBuf.ptr;
 		if(nPrev)
 		{
-			bp::classifyPrevKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, nPrev, F, nFound, flags.ptr, cls.ptr);
-			bp::flagEqualsKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(cls.ptr, nPrev, 2u, sel.ptr);
+			(void)launchDependent(bp::classifyPrevKernel, divUp(nPrev, 256), 256, stream, prev.ptr, nPrev, F, nFound, flags.ptr, cls.ptr);
+			(void)launchDependent(bp::flagEqualsKernel, divUp(nPrev, 256), 256, stream, cls.ptr, nPrev, 2u, sel.ptr);
 			int r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nLost);
 			if(r2) return r2;
-			bp::scatterSelectedKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, sel.ptr, pos.ptr, nPrev, lost.ptr);
-			bp::flagEqualsKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(cls.ptr, nPrev, 1u, sel.ptr);
+			(void)launchDependent(bp::scatterSelectedKernel, divUp(nPrev, 256), 256, stream, prev.ptr, sel.ptr, pos.ptr, nPrev, lost.ptr);
+			(void)launchDependent(bp::flagEqualsKernel, divUp(nPrev, 256), 256, stream, cls.ptr, nPrev, 1u, sel.ptr);
 			r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nKeep);
 			if(r2) return r2;
-			bp::scatterSelectedKernel<<<divUp(nPrev, 256), 256, 0, stream>>>(prev.ptr, sel.ptr, pos.ptr, nPrev, keep);
+			(void)launchDependent(bp::scatterSelectedKernel, divUp(nPrev, 256), 256, stream, prev.ptr, sel.ptr, pos.ptr, nPrev, keep);
 		}
 		const uint32_t nNext = nKeep + nFound;
 		if(nNext)
-			bp::mergeKernel<<<divUp(nNext, 256), 256, 0, stream>>>(keep, nKeep, F, nFound, next.ptr);
+			(void)launchDependent(bp::mergeKernel, divUp(nNext, 256), 256, stream, keep, nKeep, F, nFound, next.ptr);
 		std::swap(prev, next);
 		nPrev = nNext;
 
@@ -1018,12 +1056,12 @@ struct BroadPhase
 		if(hCreated.reserve(nCreated + 1) || hLost.reserve(nLost + 1)) return GBPX_ERR_NOMEM;
 		if(nCreated)
 		{
-			bp::keysToPairsKernel<<<divUp(nCreated, 256), 256, 0, stream>>>(created.ptr, nCreated, createdPairs.ptr);
+			(void)launchDependent(bp::keysToPairsKernel, divUp(nCreated, 256), 256, stream, created.ptr, nCreated, createdPairs.ptr);
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hCreated.ptr, createdPairs.ptr, size_t(nCreated) * 8, cudaMemcpyDeviceToHost, stream));
 		}
 		if(nLost)
 		{
-			bp::keysToPairsKernel<<<divUp(nLost, 256), 256, 0, stream>>>(lost.ptr, nLost, lostPairs.ptr);
+			(void)launchDependent(bp::keysToPairsKernel, divUp(nLost, 256), 256, stream, lost.ptr, nLost, lostPairs.ptr);
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hLost.ptr, lostPairs.ptr, size_t(nLost) * 8, cudaMemcpyDeviceToHost, stream));
 		}
 		if(evEnd) GBPX_CUDA_TRY(cudaEventRecord(evEnd, stream));
@@ -1042,7 +1080,7 @@ struct BroadPhase
 	{
 		if(pending || n > capacity) return GBPX_ERR_STATE;
 		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
-		if(n) bp::applyDeviceBoundsKernel<<<divUp(n, 256), 256, 0, stream>>>(dBounds, n, bx.ptr, byz.ptr, flags.ptr);
+		if(n) (void)launchDependent(bp::applyDeviceBoundsKernel, divUp(n, 256), 256, stream, dBounds, n, bx.ptr, byz.ptr, flags.ptr);
 		const int rc = runFrame(n);
 		if(rc) return rc;
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));

@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <functional>
+#include <utility>
 
 #define GBPX_API extern "C" __attribute__((visibility("default")))
 
@@ -134,6 +135,29 @@ __device__ __forceinline__ uint32_t laneMaskLt()
 	uint32_t m;
 	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
 	return m;
+}
+
+// Programmatic dependent launch: a kernel launched with launchDependent() may
+// start while the previous kernel in the stream is finishing; it must call
+// gridDependencyWait() before touching anything that kernel writes (the wait
+// returns once the previous grid has completed and its writes are visible),
+// and may call gridLaunchDependents() to let the next such launch begin.
+__device__ __forceinline__ void gridDependencyWait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void gridLaunchDependents() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
+template <typename... Params, typename... Args>
+inline cudaError_t launchDependent(void (*kernel)(Params...), uint32_t grid, uint32_t block, cudaStream_t stream, Args&&... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(block);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = stream;
+	cudaLaunchAttribute attr;
+	attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr.val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = &attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // Asynchronous 16-byte global -> shared copy (cp.async; complete in the issuing

@@ -23,6 +23,8 @@ template <typename K>
 __global__ void __launch_bounds__(THREADS) histogramKernel(const K* __restrict__ keys, uint32_t n, int shift, uint32_t numTiles,
                                                            uint32_t* __restrict__ hist)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t h[256];
 	h[threadIdx.x] = 0;
 	__syncthreads();
@@ -96,6 +98,8 @@ constexpr uint32_t SCAN_CHUNK = 1024 * 4;
 // Exclusive scan of `count` u32 values in place by one block of 1024 threads.
 static __global__ void __launch_bounds__(1024) scanKernel(uint32_t* __restrict__ data, uint32_t count)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpSums[33];
 	uint32_t carry = 0;
 	for(uint32_t start = 0; start < count; start += SCAN_CHUNK) carry = scanChunk(data, count, start, carry, warpSums);
@@ -104,6 +108,8 @@ static __global__ void __launch_bounds__(1024) scanKernel(uint32_t* __restrict__
 // Sum of each SCAN_CHUNK-entry chunk of data: chunk b -> sums[b].
 static __global__ void __launch_bounds__(1024) chunkSumKernel(const uint32_t* __restrict__ data, uint32_t count, uint32_t* __restrict__ sums)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpSums[32];
 	const uint32_t b = blockIdx.x * SCAN_CHUNK + threadIdx.x * 4;
 	uint32_t local = 0;
@@ -123,6 +129,8 @@ static __global__ void __launch_bounds__(1024) chunkSumKernel(const uint32_t* __
 // Exclusive scan of chunk b of data, offset by offsets[b] (the exclusive scan of the chunk sums).
 static __global__ void __launch_bounds__(1024) chunkScanKernel(uint32_t* __restrict__ data, uint32_t count, const uint32_t* __restrict__ offsets)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpSums[33];
 	scanChunk(data, count, blockIdx.x * SCAN_CHUNK, offsets[blockIdx.x], warpSums);
 }
@@ -136,13 +144,13 @@ static inline void scanAny(uint32_t* data, uint32_t count, uint32_t* scratch, cu
 {
 	if(count <= 4 * SCAN_CHUNK)
 	{
-		scanKernel<<<1, 1024, 0, s>>>(data, count);
+		(void)launchDependent(scanKernel, 1, 1024, s, data, count);
 		return;
 	}
 	const uint32_t chunks = (count + SCAN_CHUNK - 1) / SCAN_CHUNK;
-	chunkSumKernel<<<chunks, 1024, 0, s>>>(data, count, scratch);
-	scanKernel<<<1, 1024, 0, s>>>(scratch, chunks);
-	chunkScanKernel<<<chunks, 1024, 0, s>>>(data, count, scratch);
+	(void)launchDependent(chunkSumKernel, chunks, 1024, s, data, count, scratch);
+	(void)launchDependent(scanKernel, 1, 1024, s, scratch, chunks);
+	(void)launchDependent(chunkScanKernel, chunks, 1024, s, data, count, scratch);
 }
 
 template <typename K, bool HAS_VAL>
@@ -150,6 +158,8 @@ __global__ void __launch_bounds__(THREADS) scatterKernel(const K* __restrict__ k
                                                          K* __restrict__ keysOut, uint32_t* __restrict__ valsOut, uint32_t n,
                                                          int shift, uint32_t numTiles, const uint32_t* __restrict__ offsets)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t cnt[WARPS][256];
 	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	for(int d = threadIdx.x; d < WARPS * 256; d += THREADS) (&cnt[0][0])[d] = 0;
@@ -231,9 +241,9 @@ static bool radixSort(K* keys, uint32_t* vals, K* keysAlt, uint32_t* valsAlt, ui
 		const uint32_t* vin = inAlt ? valsAlt : vals;
 		K* kout = inAlt ? keys : keysAlt;
 		uint32_t* vout = inAlt ? vals : valsAlt;
-		rs::histogramKernel<K><<<numTiles, rs::THREADS, 0, s>>>(kin, n, shift, numTiles, hist);
+		(void)launchDependent(rs::histogramKernel<K>, numTiles, rs::THREADS, s, kin, n, shift, numTiles, hist);
 		rs::scanAny(hist, 256u * numTiles, hist + 256u * numTiles, s);
-		rs::scatterKernel<K, HAS_VAL><<<numTiles, rs::THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, numTiles, hist);
+		(void)launchDependent(rs::scatterKernel<K, HAS_VAL>, numTiles, rs::THREADS, s, kin, vin, kout, vout, n, shift, numTiles, hist);
 		inAlt = !inAlt;
 	}
 	return inAlt;

@@ -306,6 +306,8 @@ __global__ void colorPassKernel(const uint32_t* __restrict__ ddList, uint32_t nD
                                 uint32_t* __restrict__ part, uint32_t* __restrict__ mask, uint32_t* __restrict__ maxNormal, uint32_t pass,
                                 uint32_t* __restrict__ counts)
 {
+	gridDependencyWait();   // launched dependent on the previous pass (launchDependent)
+	gridLaunchDependents();
 	uint32_t done = 0;
 	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nDD; i += gridDim.x * blockDim.x)
 	{
@@ -456,6 +458,9 @@ __global__ void solvePartitionKernel(tgs::ConstraintRecord* __restrict__ recs, u
                                      uint32_t nbDyn, float minPen, float elapsed, const uint32_t* __restrict__ orderedPair,
                                      tgs::FrictionState* __restrict__ frictionOut)
 {
+	// launched dependent on the previous partition / integration (launchDependent)
+	gridDependencyWait();
+	gridLaunchDependents();
 	const uint32_t r = begin + blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= end) return;
 	tgs::ConstraintRecord& rec = recs[r];
@@ -493,6 +498,8 @@ __global__ void solvePartitionKernel(tgs::ConstraintRecord* __restrict__ recs, u
 
 __global__ void integrateKernel(tgs::BodyVel* __restrict__ vel, tgs::BodyTx* __restrict__ tx, uint32_t nbDyn, float stepDt)
 {
+	gridDependencyWait();   // launched dependent on the last partition (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= nbDyn) return;
 	tgs::BodyVel v = vel[i];
@@ -702,8 +709,8 @@ struct Scene
 		{
 			// a pass always colours the first unfinished constraint, so nDD passes always suffice
 			for(int k = 0; k < 8; k++)
-				sbatch::colorPassKernel<<<grid, 256, 0, s>>>(ddList.ptr, nDD, consA.ptr, consB.ptr, prevOf.ptr, donePass.ptr, partOf.ptr, bodyMask.ptr,
-				                                              maxNormal.ptr, ++pass, batchCounts.ptr);
+				GBPX_CUDA_TRY(launchDependent(sbatch::colorPassKernel, grid, 256, s, ddList.ptr, nDD, consA.ptr, consB.ptr, prevOf.ptr, donePass.ptr,
+				                              partOf.ptr, bodyMask.ptr, maxNormal.ptr, ++pass, batchCounts.ptr));
 			GBPX_CUDA_TRY(cudaGetLastError());
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
 			GBPX_CUDA_TRY(cudaStreamSynchronize(s));
@@ -834,12 +841,15 @@ struct Scene
 			for(uint32_t p = 0; p < nbPartitions; p++)
 			{
 				const uint32_t b = p ? hPartEnds[p - 1] : 0u, e = hPartEnds[p];
+				// each launch overlaps the previous kernel's tail and waits on the device
+				// for its completion (programmatic dependent launch)
 				if(e > b)
-					solvePartitionKernel<<<divUp(e - b, 128), 128, 0, stream>>>(recs.ptr, b, e, vel.ptr, nbDyn, minPen, elapsed, orderedPair.ptr, broken);
+					GBPX_CUDA_TRY(launchDependent(solvePartitionKernel, divUp(e - b, 128), 128, stream, recs.ptr, b, e, vel.ptr, nbDyn, minPen, elapsed,
+					                              orderedPair.ptr, broken));
 			}
 			if(posIter)
 			{
-				integrateKernel<<<divUp(nbDyn, 128), 128, 0, stream>>>(vel.ptr, tx.ptr, nbDyn, stepDt);
+				GBPX_CUDA_TRY(launchDependent(integrateKernel, divUp(nbDyn, 128), 128, stream, vel.ptr, tx.ptr, nbDyn, stepDt));
 				elapsed += stepDt;
 			}
 		}
