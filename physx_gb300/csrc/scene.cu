@@ -83,6 +83,8 @@ __device__ __forceinline__ void shapeOf(const SceneDev& s, uint32_t id, int& typ
 // unbounded.
 __global__ void boundsKernel(SceneDev s, uint32_t count, float margin, float* __restrict__ out)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= count) return;
 	int type;
@@ -101,6 +103,8 @@ __global__ void boundsKernel(SceneDev s, uint32_t count, float margin, float* __
 __global__ void kindKernel(SceneDev s, const unsigned long long* __restrict__ keys, uint32_t nbPairs, uint32_t* __restrict__ queue,
                            uint32_t queueCap, uint32_t* __restrict__ kindCount)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	const uint32_t lane = threadIdx.x & 31;
 	uint32_t kind = NB_KINDS;
@@ -134,6 +138,8 @@ __global__ void __launch_bounds__(128) narrowphaseKernel(SceneDev s, StepParams 
                                                          np::ManifoldRecord* __restrict__ manifoldsOut, tgs::FrictionState* __restrict__ frictionOut,
                                                          float4* __restrict__ contacts, uint32_t* __restrict__ contactCount)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	constexpr uint32_t KIND = TA == 0 ? uint32_t(TB) : (TA == 1 ? uint32_t(TB + 2) : (TA == 2 ? uint32_t(TB + 4) : 8u));
 	constexpr bool CACHED = world::cachedPairKind(KIND);
 	const uint32_t count = kindCount[KIND];
@@ -198,6 +204,8 @@ static const NpKernel* npKernels()
 __global__ void countConstraintsKernel(const uint32_t* __restrict__ contactCount, uint32_t n, uint32_t* __restrict__ blockCounts,
                                        unsigned long long* __restrict__ totalContacts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	uint32_t cnt = k < n ? contactCount[k] : 0u;
 	const uint32_t c = __syncthreads_count(cnt > 0);
@@ -210,6 +218,8 @@ __global__ void emitConstraintsKernel(const uint32_t* __restrict__ contactCount,
                                       const uint32_t* __restrict__ blockOffsets, uint32_t* __restrict__ consPair, uint32_t* __restrict__ consA,
                                       uint32_t* __restrict__ consB)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	__shared__ uint32_t warpCounts[32];
 	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool v = k < n && contactCount[k] > 0;
@@ -270,6 +280,8 @@ constexpr uint32_t DEFERRED = 0xffffu;
 __global__ void incidenceKernel(const uint32_t* __restrict__ consA, const uint32_t* __restrict__ consB, uint32_t nc, uint32_t nbDyn,
                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t* __restrict__ ddList, uint32_t* __restrict__ counts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
 	if(c >= nc) return;
 	const uint32_t a = consA[c], b = consB[c];
@@ -286,6 +298,8 @@ __global__ void incidenceKernel(const uint32_t* __restrict__ consA, const uint32
 __global__ void linkKernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t nbDyn,
                            const uint32_t* __restrict__ consA, uint32_t* __restrict__ prevOf, uint32_t* __restrict__ staticRunStart)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= n) return;
 	const uint32_t key = keys[e];
@@ -342,6 +356,8 @@ __global__ void colorPassKernel(const uint32_t* __restrict__ ddList, uint32_t nD
 __global__ void staticPartKernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, uint32_t nbDyn,
                                  const uint32_t* __restrict__ staticRunStart, const uint32_t* __restrict__ maxNormal, uint32_t* __restrict__ part)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= n) return;
 	const uint32_t key = keys[e];
@@ -354,6 +370,8 @@ constexpr uint32_t MAX_PARTS = 4096;
 __global__ void partKeysKernel(const uint32_t* __restrict__ part, uint32_t nc, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                uint32_t* __restrict__ perPart, uint32_t* __restrict__ counts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
 	if(c >= nc) return;
 	const uint32_t p = part[c];
@@ -366,6 +384,8 @@ __global__ void partKeysKernel(const uint32_t* __restrict__ part, uint32_t nc, u
 // Inclusive scan of the partition counts into end offsets (one block).
 __global__ void partEndsKernel(uint32_t* __restrict__ perPart, const uint32_t* __restrict__ counts)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	if(threadIdx.x != 0) return;
 	const uint32_t np = min(counts[3], MAX_PARTS);
 	uint32_t acc = 0;
@@ -377,6 +397,8 @@ __global__ void partEndsKernel(uint32_t* __restrict__ perPart, const uint32_t* _
 __global__ void bodiesKernel(SceneDev s, StepParams sp, tgs::BodyVel* __restrict__ vel, tgs::BodyTx* __restrict__ tx, tgs::BodyData* __restrict__ data,
                              Tr* __restrict__ pose)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < s.nbDyn)
 	{
@@ -402,6 +424,8 @@ __global__ void prepKernel(SceneDev s, StepParams sp, uint32_t nc, const uint32_
                            const uint32_t* __restrict__ prevSlot, const tgs::FrictionState* __restrict__ frictionIn,
                            tgs::FrictionState* __restrict__ frictionOut, uint32_t* __restrict__ orderedPair, tgs::ConstraintRecord* __restrict__ recs)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= nc) return;
 	uint32_t lo = 0, hi = nbPart - 1;   // partition of r: first end above r
@@ -511,6 +535,8 @@ __global__ void integrateKernel(tgs::BodyVel* __restrict__ vel, tgs::BodyTx* __r
 // PxIntegrateSolverBodiesTGS and write-back into the PxRigidBodyData records.
 __global__ void finalizeKernel(SceneDev s, const tgs::BodyVel* __restrict__ vel, const tgs::BodyTx* __restrict__ tx, const Tr* __restrict__ pose)
 {
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= s.nbDyn) return;
 	tgs::BodyVel v = vel[i];
@@ -602,7 +628,7 @@ struct Scene
 		for(uint32_t k = 0; k <= STAGES; k++) GBPX_CUDA_TRY(cudaEventCreate(&ev[k]));
 		// every shape enters the broadphase once: dynamic bodies in their own filter
 		// groups, statics in the static group (PxBpFilterGroup encodings)
-		boundsKernel<<<divUp(total, 128), 128, 0, stream>>>(dev(), total, sp.boundsMargin, bounds.ptr);
+		(void)launchDependent(boundsKernel, divUp(total, 128), 128, stream, dev(), total, sp.boundsMargin, bounds.ptr);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		std::vector<float> hb(6 * size_t(total));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(hb.data(), bounds.ptr, hb.size() * 4, cudaMemcpyDeviceToHost, stream));
@@ -684,7 +710,7 @@ struct Scene
 		const cudaStream_t s = stream;
 		const uint32_t n2 = 2 * nc;
 		GBPX_CUDA_TRY(cudaMemsetAsync(batchCounts.ptr, 0, 16, s));
-		sbatch::incidenceKernel<<<divUp(nc, 256), 256, 0, s>>>(consA.ptr, consB.ptr, nc, nbDyn, incKeys.ptr, incVals.ptr, ddList.ptr,
+		(void)launchDependent(sbatch::incidenceKernel, divUp(nc, 256), 256, s, consA.ptr, consB.ptr, nc, nbDyn, incKeys.ptr, incVals.ptr, ddList.ptr,
 		                                                       batchCounts.ptr);
 		GBPX_CUDA_TRY(cudaMemsetAsync(bodyMask.ptr, 0, size_t(nbDyn) * 4, s));
 		GBPX_CUDA_TRY(cudaMemsetAsync(maxNormal.ptr, 0, size_t(nbDyn) * 4, s));
@@ -697,7 +723,7 @@ struct Scene
 		const bool alt = radixSort<uint32_t, true>(incKeys.ptr, incVals.ptr, incKeysAlt.ptr, incValsAlt.ptr, n2, 0, endBit, sortHist.ptr, s);
 		const uint32_t* sk = alt ? incKeysAlt.ptr : incKeys.ptr;
 		const uint32_t* sv = alt ? incValsAlt.ptr : incVals.ptr;
-		sbatch::linkKernel<<<divUp(n2, 256), 256, 0, s>>>(sk, sv, n2, nbDyn, consA.ptr, prevOf.ptr, staticRunStart.ptr);
+		(void)launchDependent(sbatch::linkKernel, divUp(n2, 256), 256, s, sk, sv, n2, nbDyn, consA.ptr, prevOf.ptr, staticRunStart.ptr);
 		// remaining = number of dynamic-dynamic constraints
 		GBPX_CUDA_TRY(cudaMemcpyAsync(batchCounts.ptr + 1, batchCounts.ptr, 4, cudaMemcpyDeviceToDevice, s));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
@@ -718,10 +744,10 @@ struct Scene
 		}
 		lastColorPasses = pass;
 		if(nDD && (hBatch.ptr[1] != 0 || hBatch.ptr[2] != 0)) return GBPX_OK;   // second round needed: host path
-		sbatch::staticPartKernel<<<divUp(n2, 256), 256, 0, s>>>(sk, sv, n2, nbDyn, staticRunStart.ptr, maxNormal.ptr, partOf.ptr);
+		(void)launchDependent(sbatch::staticPartKernel, divUp(n2, 256), 256, s, sk, sv, n2, nbDyn, staticRunStart.ptr, maxNormal.ptr, partOf.ptr);
 		// stable sort by partition: the reference's placement (input order within a partition)
-		sbatch::partKeysKernel<<<divUp(nc, 256), 256, 0, s>>>(partOf.ptr, nc, incKeys.ptr, incVals.ptr, perPart.ptr, batchCounts.ptr);
-		sbatch::partEndsKernel<<<1, 32, 0, s>>>(perPart.ptr, batchCounts.ptr);
+		(void)launchDependent(sbatch::partKeysKernel, divUp(nc, 256), 256, s, partOf.ptr, nc, incKeys.ptr, incVals.ptr, perPart.ptr, batchCounts.ptr);
+		(void)launchDependent(sbatch::partEndsKernel, 1, 32, s, perPart.ptr, batchCounts.ptr);
 		const bool alt2 = radixSort<uint32_t, true>(incKeys.ptr, incVals.ptr, incKeysAlt.ptr, incValsAlt.ptr, nc, 0, 16, sortHist.ptr, s);
 		GBPX_CUDA_TRY(cudaMemcpyAsync(order.ptr, alt2 ? incValsAlt.ptr : incVals.ptr, size_t(nc) * 4, cudaMemcpyDeviceToDevice, s));
 		GBPX_CUDA_TRY(cudaMemcpyAsync(hBatch.ptr, batchCounts.ptr, 16, cudaMemcpyDeviceToHost, s));
@@ -751,7 +777,7 @@ struct Scene
 		}
 		else
 			nbPrev = 0;
-		boundsKernel<<<divUp(nbDyn, 128), 128, 0, stream>>>(d, nbDyn, sp.boundsMargin, bounds.ptr);
+		(void)launchDependent(boundsKernel, divUp(nbDyn, 128), 128, stream, d, nbDyn, sp.boundsMargin, bounds.ptr);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		int rc = bpi::updateFromDevice(bp, bounds.ptr, nbDyn);
 		if(rc) return rc;
@@ -765,10 +791,10 @@ struct Scene
 		GBPX_CUDA_TRY(cudaMemsetAsync(totalContacts.ptr, 0, 8, stream));
 		if(nbPairs)
 		{
-			kindKernel<<<divUp(nbPairs, 128), 128, 0, stream>>>(d, keys, nbPairs, queue.ptr, uint32_t(pairCap), kindCount.ptr);
+			(void)launchDependent(kindKernel, divUp(nbPairs, 128), 128, stream, d, keys, nbPairs, queue.ptr, uint32_t(pairCap), kindCount.ptr);
 			const uint32_t grid = std::min<uint32_t>(divUp(nbPairs, 128), 152u * 16u);
 			for(uint32_t k = 0; k < NB_KINDS; k++)
-				npKernels()[k]<<<grid, 128, 0, stream>>>(d, sp, keys, keysPrev.ptr, nbPrev, queue.ptr + size_t(k) * pairCap, kindCount.ptr, prevSlot.ptr,
+				(void)launchDependent(npKernels()[k], grid, 128, stream, d, sp, keys, keysPrev.ptr, nbPrev, queue.ptr + size_t(k) * pairCap, kindCount.ptr, prevSlot.ptr,
 				                                         manifolds[par].ptr, manifolds[par ^ 1u].ptr, frictionState[par ^ 1u].ptr, contacts.ptr,
 				                                         contactCount.ptr);
 			GBPX_CUDA_TRY(cudaGetLastError());
@@ -779,10 +805,10 @@ struct Scene
 		if(nbPairs)
 		{
 			const uint32_t nb = divUp(nbPairs, 256);
-			countConstraintsKernel<<<nb, 256, 0, stream>>>(contactCount.ptr, nbPairs, blockCounts.ptr, totalContacts.ptr);
+			(void)launchDependent(countConstraintsKernel, nb, 256, stream, contactCount.ptr, nbPairs, blockCounts.ptr, totalContacts.ptr);
 			GBPX_CUDA_TRY(cudaMemsetAsync(blockCounts.ptr + nb, 0, 4, stream));
-			rs::scanKernel<<<1, 1024, 0, stream>>>(blockCounts.ptr, nb + 1);
-			emitConstraintsKernel<<<nb, 256, 0, stream>>>(contactCount.ptr, keys, nbPairs, blockCounts.ptr, consPair.ptr, consA.ptr, consB.ptr);
+			(void)launchDependent(rs::scanKernel, 1, 1024, stream, blockCounts.ptr, nb + 1);
+			(void)launchDependent(emitConstraintsKernel, nb, 256, stream, contactCount.ptr, keys, nbPairs, blockCounts.ptr, consPair.ptr, consA.ptr, consB.ptr);
 			GBPX_CUDA_TRY(cudaGetLastError());
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hSmall.ptr, blockCounts.ptr + nb, 4, cudaMemcpyDeviceToHost, stream));
 			GBPX_CUDA_TRY(cudaMemcpyAsync(hTotal.ptr, totalContacts.ptr, 8, cudaMemcpyDeviceToHost, stream));
@@ -822,9 +848,9 @@ struct Scene
 		nbPartitions = uint32_t(hPartEnds.size());
 		mark(3);
 		// 4. solver bodies and contact rows
-		bodiesKernel<<<divUp(nbDyn + nbStatic, 128), 128, 0, stream>>>(d, sp, vel.ptr, tx.ptr, data.ptr, pose.ptr);
+		(void)launchDependent(bodiesKernel, divUp(nbDyn + nbStatic, 128), 128, stream, d, sp, vel.ptr, tx.ptr, data.ptr, pose.ptr);
 		if(nc)
-			prepKernel<<<divUp(nc, 128), 128, 0, stream>>>(d, sp, nc, order.ptr, consPair.ptr, partEnds.ptr, nbPartitions, keys, contacts.ptr,
+			(void)launchDependent(prepKernel, divUp(nc, 128), 128, stream, d, sp, nc, order.ptr, consPair.ptr, partEnds.ptr, nbPartitions, keys, contacts.ptr,
 			                                               contactCount.ptr, vel.ptr, tx.ptr, data.ptr, pose.ptr, prevSlot.ptr, frictionState[par].ptr,
 			                                               frictionState[par ^ 1u].ptr, orderedPair.ptr, recs.ptr);
 		GBPX_CUDA_TRY(cudaGetLastError());
@@ -856,7 +882,7 @@ struct Scene
 		GBPX_CUDA_TRY(cudaGetLastError());
 		mark(5);
 		// 6. PxIntegrateSolverBodiesTGS + write-back
-		finalizeKernel<<<divUp(nbDyn, 128), 128, 0, stream>>>(d, vel.ptr, tx.ptr, pose.ptr);
+		(void)launchDependent(finalizeKernel, divUp(nbDyn, 128), 128, stream, d, vel.ptr, tx.ptr, pose.ptr);
 		GBPX_CUDA_TRY(cudaGetLastError());
 		mark(6);
 		if(sp.persistent) parity ^= 1u;
