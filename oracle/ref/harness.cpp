@@ -201,6 +201,15 @@ HX int pxref_sizeof(int which)
 
 //////////////////////////////////////////////////////////////////////////////
 // Broadphase: PxCreateBroadPhase(eABP) + update/fetchResults.
+HX void* pxref_bp_create_typed(int type, int discardStaticVsKinematic, int discardKinematicVsKinematic)
+{
+	ensureFoundation();
+	PxBroadPhaseDesc desc(type == 1 ? PxBroadPhaseType::ePABP : PxBroadPhaseType::eABP);
+	desc.mDiscardStaticVsKinematic = discardStaticVsKinematic != 0;
+	desc.mDiscardKinematicVsKinematic = discardKinematicVsKinematic != 0;
+	return PxCreateBroadPhase(desc);
+}
+
 HX void* pxref_bp_create(int discardStaticVsKinematic, int discardKinematicVsKinematic)
 {
 	ensureFoundation();

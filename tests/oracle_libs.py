@@ -43,10 +43,16 @@ def reference():
 class CpuBroadPhase:
     """Same call pattern for the oracle ("orc") and the reference ("pxref")."""
 
-    def __init__(self, which="orc", discard_sk=0, discard_kk=0):
+    def __init__(self, which="orc", discard_sk=0, discard_kk=0, pabp=False):
+        """pabp: the reference's ePABP broadphase instead of eABP (reference only)."""
         self.L = oracle() if which == "orc" else reference()
         self.pre = which
-        self.h = ctypes.c_void_p(getattr(self.L, self.pre + "_bp_create")(discard_sk, discard_kk))
+        if pabp:
+            assert which == "pxref"
+            self.L.pxref_bp_create_typed.restype = ctypes.c_void_p
+            self.h = ctypes.c_void_p(self.L.pxref_bp_create_typed(1, discard_sk, discard_kk))
+        else:
+            self.h = ctypes.c_void_p(getattr(self.L, self.pre + "_bp_create")(discard_sk, discard_kk))
 
     def update(self, fr):
         cap = int(fr["capacity"])

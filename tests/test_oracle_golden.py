@@ -334,3 +334,17 @@ def test_oracle_joints_match_reference_live(seed, batch):
         for k in JOINT_KEYS:
             assert np.array_equal(got[k], ref[k]), "frame %d %s" % (f, k)
         rigid = advance_rigid(rigid, ref["vel"], ref["pose"])
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed,n,frames,extent", [(51, 3000, 6, 40.0), (52, 400, 8, 6.0)])
+def test_reference_pabp_pairs_equal_abp(seed, n, frames, extent):
+    """PxCreateBroadPhase(ePABP) gives the same created / lost pair sets as eABP
+    frame by frame (the reference's own two broadphases), so serving ePABP
+    descriptors with the ABP-exact device broadphase keeps ePABP's results."""
+    abp, pabp = CpuBroadPhase("pxref"), CpuBroadPhase("pxref", pabp=True)
+    for f, fr in enumerate(bp_frames(seed, n, frames, extent=extent)):
+        ac, al = abp.update(fr)
+        pc, pl = pabp.update(fr)
+        assert np.array_equal(sorted_pairs(ac), sorted_pairs(pc)), "frame %d created" % f
+        assert np.array_equal(sorted_pairs(al), sorted_pairs(pl)), "frame %d lost" % f
