@@ -511,6 +511,7 @@ def main():
         tuned_threshold, tuned_ms = a.large_bodies, 0.0
     else:
         tuned_threshold, tuned_ms = w.autotune(steps=3)
+    tuning = w.tuning()
     w.step(a.warmup, graph=True)
     w.synchronize()
     if a.profile_step:
@@ -637,6 +638,8 @@ def main():
                             constraints_per_step=st["constraints"], contacts_per_step=st["contacts"], graph=True,
                             autotune=dict(key="scene-size histogram", large_bodies=tuned_threshold,
                                           solve=SOLVE_VARIANTS[getattr(w, "solve_variant", 8)],
+                                          prep_blocks_per_sm=tuning["prep_blocks_per_sm"],
+                                          narrowphase_blocks_per_sm=tuning["narrowphase_blocks_per_sm"],
                                           sample_ms_per_step=tuned_ms),
                             l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
                             parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),

@@ -279,14 +279,18 @@ int gbpx_world_stats(void* world, uint64_t* out4);
  * one warp per scene; default 512.  Results do not depend on it. */
 int gbpx_world_set_large_bodies(void* world, uint32_t largeBodies);
 /* Autotuner keyed on the scene-size histogram: times candidate thresholds of
- * gbpx_world_set_large_bodies, then the solve staging slots, on a
+ * gbpx_world_set_large_bodies, then the solve kernel, then the preparation
+ * and heavy narrowphase blocks per SM (gbpx_world_set_occupancy), on a
  * size-stratified sample of sampleScenes
  * scenes (a temporary world in the current state, `steps` graph steps each),
  * sets the fastest and caches it per histogram.  The sample must load the GPU
  * like the whole world (pass the scene count to copy every scene).  outMs: the
- * chosen threshold's ms per step on the sample (0 when cached). */
+ * chosen configuration's ms per step on the sample (0 when cached). */
 int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, uint32_t* outSolveVariant,
                         float* outMs);
+/* The world's tuning: out4 = block-per-scene threshold, solve kernel,
+ * preparation and heavy narrowphase blocks per SM (0 = as many as fit). */
+int gbpx_world_tuning(void* world, uint32_t* out4);
 /* Workspace of the warp-per-scene solve: variants 0-2 keep the body
  * velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane
  * (2 is the default), variants 3-5 the same with the velocities left in HBM,

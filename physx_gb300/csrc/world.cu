@@ -2272,9 +2272,16 @@ std::string histogramKey(const std::vector<gbpx::world::SceneDesc>& sc)
 	}
 	return key;
 }
-std::map<std::string, std::pair<uint32_t, uint32_t>>& tunedThresholds()
+// a tuned configuration: block-per-scene threshold, solve kernel, and the
+// blocks per SM of the preparation and heavy narrowphase kernels (0 = as many
+// as fit)
+struct Tuning
 {
-	static std::map<std::string, std::pair<uint32_t, uint32_t>> m;
+	uint32_t largeBodies, solveVariant, prepPerSm, npHeavyPerSm;
+};
+std::map<std::string, Tuning>& tunedConfigs()
+{
+	static std::map<std::string, Tuning> m;
 	return m;
 }
 } // namespace
@@ -2285,15 +2292,17 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	World* w = static_cast<World*>(wv);
 	if(!w || !sampleScenes || !steps || !outLargeBodies || !outSolveVariant) return GBPX_ERR_INVALID;
 	const std::string key = histogramKey(w->hScenes);
-	auto& cache = tunedThresholds();
+	auto& cache = tunedConfigs();
 	auto hit = cache.find(key);
 	if(hit != cache.end())
 	{
-		*outLargeBodies = hit->second.first;
-		*outSolveVariant = hit->second.second;
+		const Tuning& c = hit->second;
+		*outLargeBodies = c.largeBodies;
+		*outSolveVariant = c.solveVariant;
 		if(outMs) *outMs = 0.0f;
-		const int rc = gbpx_world_set_large_bodies(wv, hit->second.first);
-		return rc ? rc : gbpx_world_set_solve_variant(wv, hit->second.second);
+		int rc = gbpx_world_set_large_bodies(wv, c.largeBodies);
+		rc = rc ? rc : gbpx_world_set_solve_variant(wv, c.solveVariant);
+		return rc ? rc : gbpx_world_set_occupancy(wv, c.prepPerSm, c.npHeavyPerSm);
 	}
 	// size-stratified sample: every k-th scene in order of size
 	std::vector<uint32_t> order(w->nbScenes);
@@ -2377,17 +2386,51 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		rc = timeConfig(best, v, ms);
 		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
 	}
+	// then the blocks per SM of the row preparation (rows per CTA wave) and of the
+	// two heavy narrowphase kinds (pairs per CTA wave), one after the other
+	uint32_t bestPrep = t->prepPerSm, bestNp = t->npHeavyPerSm;
+	for(uint32_t c : {2u, 3u, 4u})
+	{
+		if(rc) break;
+		t->prepPerSm = c;
+		float ms = 0.0f;
+		rc = timeConfig(best, bestVariant, ms);
+		if(!rc && ms < bestMs) { bestMs = ms; bestPrep = c; }
+	}
+	t->prepPerSm = bestPrep;
+	for(uint32_t c : {1u, 2u, 3u})
+	{
+		if(rc) break;
+		t->npHeavyPerSm = c;
+		float ms = 0.0f;
+		rc = timeConfig(best, bestVariant, ms);
+		if(!rc && ms < bestMs) { bestMs = ms; bestNp = c; }
+	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	t->release();
 	delete t;
 	if(rc) return rc;
-	cache[key] = std::make_pair(best, bestVariant);
+	cache[key] = Tuning{best, bestVariant, bestPrep, bestNp};
 	*outLargeBodies = best;
 	*outSolveVariant = bestVariant;
 	if(outMs) *outMs = bestMs / float(steps);
 	rc = gbpx_world_set_large_bodies(wv, best);
-	return rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
+	rc = rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
+	return rc ? rc : gbpx_world_set_occupancy(wv, bestPrep, bestNp);
+}
+
+// The world's current tuning: out4 = block-per-scene threshold, solve kernel,
+// preparation blocks per SM, heavy narrowphase blocks per SM (0 = as many as fit).
+GBPX_API int gbpx_world_tuning(void* wv, uint32_t* out4)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || !out4) return GBPX_ERR_INVALID;
+	out4[0] = w->params.largeBodies;
+	out4[1] = w->params.solveVariant;
+	out4[2] = w->prepPerSm;
+	out4[3] = w->npHeavyPerSm;
+	return GBPX_OK;
 }
 
 // Solve kernel of the world.  8 (the default): the resident solve, every

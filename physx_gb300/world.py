@@ -149,9 +149,10 @@ class World:
     def autotune(self, sample_scenes=None, steps=3):
         """Picks the block-per-scene threshold for this world's scene-size histogram
         (timed on a temporary copy of a size-stratified sample of the scenes, all of
-        them by default; cached per histogram), then the solve staging slot; returns
-        (threshold, ms per step of the sample with them, 0 if cached) and keeps the
-        slot in self.solve_variant.  The sample should load the GPU like the whole
+        them by default; cached per histogram), then the solve kernel and the
+        preparation / heavy narrowphase blocks per SM; returns (threshold, ms per step
+        of the sample with them, 0 if cached) and keeps the solve kernel in
+        self.solve_variant (tuning() has the whole choice).  The sample should load the GPU like the whole
         world: warp-per-scene kernels need many scenes to fill it."""
         if sample_scenes is None:
             sample_scenes = len(self._keep[0])
@@ -162,6 +163,14 @@ class World:
               "gbpx_world_autotune")
         self.solve_variant = v.value
         return t.value, ms.value
+
+    def tuning(self):
+        """{large_bodies, solve_variant, prep_blocks_per_sm, narrowphase_blocks_per_sm} in force
+        (the autotuner's choice, or what was set by hand; 0 blocks per SM = as many as fit)."""
+        out = np.zeros(4, np.uint32)
+        check(self._L.gbpx_world_tuning(self._h, _p(out)), "gbpx_world_tuning")
+        return dict(large_bodies=int(out[0]), solve_variant=int(out[1]), prep_blocks_per_sm=int(out[2]),
+                    narrowphase_blocks_per_sm=int(out[3]))
 
     def set_occupancy(self, prep_blocks_per_sm=0, narrowphase_blocks_per_sm=0):
         """Persistent blocks per SM of the row preparation and of the capsule-box and

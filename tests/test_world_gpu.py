@@ -215,12 +215,37 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
     assert a.info()["large_bodies"] == thr
     thr2, ms2 = b.autotune(sample_scenes=32, steps=2)
     assert thr2 == thr and ms2 == 0.0
+    assert b.tuning() == a.tuning()   # the cached choice includes the occupancies
+    t = a.tuning()
+    assert t["prep_blocks_per_sm"] in (0, 2, 3, 4) and t["narrowphase_blocks_per_sm"] in (0, 1, 2, 3)
     b.set_large_bodies(512)
+    b.set_occupancy(0, 0)
     a.step(10)
     b.step(10)
     assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
     a.release()
     b.release()
+
+
+def test_world_occupancy_keeps_results(cuda_device):
+    """The blocks per SM of the row preparation and the heavy narrowphase kernels
+    (what the autotuner chooses after the threshold and the solve) do not change
+    any result."""
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(144, 96, nmin=16, nmax=512)
+    worlds = [World(scenes) for _ in range(3)]
+    worlds[1].set_occupancy(2, 1)
+    worlds[2].set_occupancy(4, 3)
+    for _ in range(15):
+        for w in worlds:
+            w.step(1)
+    ref = worlds[0].get_bodies().tobytes()
+    for w in worlds:
+        assert w.get_bodies().tobytes() == ref
+        assert not w.status().any()
+    for w in worlds:
+        w.release()
 
 
 def test_world_solve_staging_variants_equal(cuda_device):
