@@ -166,6 +166,97 @@ __global__ void emitLiveKernel(const uint8_t* __restrict__ live, const uint2* __
 }
 
 // Gathers the sorted SoA arrays and marks which sorted positions were updated.
+// ---- sorted order, incremental (ABP's updated-only sort, BpBroadPhaseABP.cpp:1344,1484-1596):
+// last frame's order without the removed and updated boxes is still sorted
+// (their keys did not change); only the created / updated boxes are sorted, then
+// the two lists are merged.  Equal keys put the kept box first; the order among
+// equal keys changes no pair (a pair with an updated box is found once from
+// whichever box comes first) and the found pairs are sorted afterwards.
+__device__ __forceinline__ uint32_t lowerBound32(const uint32_t* __restrict__ arr, uint32_t n, uint32_t key)
+{
+	uint32_t a = 0, b = n;
+	while(a < b)
+	{
+		const uint32_t m = (a + b) >> 1;
+		if(arr[m] < key) a = m + 1; else b = m;
+	}
+	return a;
+}
+__device__ __forceinline__ uint32_t upperBound32(const uint32_t* __restrict__ arr, uint32_t n, uint32_t key)
+{
+	uint32_t a = 0, b = n;
+	while(a < b)
+	{
+		const uint32_t m = (a + b) >> 1;
+		if(arr[m] <= key) a = m + 1; else b = m;
+	}
+	return a;
+}
+
+// keep[i] = 1 for the boxes of last frame's order that are live and were not updated
+__global__ void keepFlagKernel(const uint32_t* __restrict__ prevOrder, uint32_t n, const uint8_t* __restrict__ live,
+                               const uint8_t* __restrict__ flags, uint32_t* __restrict__ keep)
+{
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const uint32_t id = prevOrder[i];
+	keep[i] = (live[id] && !(flags[id] & F_UPDATED)) ? 1u : 0u;
+}
+
+// (key, handle) of the created / updated boxes: the update records' handles, or
+// handles [0, n) (recs null: the device-bounds path)
+__global__ void updatedKeysKernel(const UpdateRec* __restrict__ recs, uint32_t n, const uint2* __restrict__ bx, uint32_t* __restrict__ keys,
+                                  uint32_t* __restrict__ vals)
+{
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const uint32_t id = recs ? recs[i].id : i;
+	keys[i] = bx[id].x;
+	vals[i] = id;
+}
+
+// kept handles and their keys, in last frame's order
+__global__ void gatherKeptKernel(const uint32_t* __restrict__ prevOrder, const uint32_t* __restrict__ keptPos, uint32_t n,
+                                 const uint2* __restrict__ bx, uint32_t* __restrict__ ids, uint32_t* __restrict__ keys)
+{
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
+	const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+	if(j >= n) return;
+	const uint32_t id = prevOrder[keptPos[j]];
+	ids[j] = id;
+	keys[j] = bx[id].x;
+}
+
+// Merge by co-ranking: the updated boxes after kept boxes of equal key.  Writes
+// the merged order and the sorted positions of the updated (updPos) and kept
+// (sleepPos) boxes, both ascending.
+__global__ void mergeOrderKernel(const uint32_t* __restrict__ uKeys, const uint32_t* __restrict__ uIds, uint32_t nU,
+                                 const uint32_t* __restrict__ sKeys, const uint32_t* __restrict__ sIds, uint32_t nS, uint32_t* __restrict__ order,
+                                 uint32_t* __restrict__ updPos, uint32_t* __restrict__ sleepPos)
+{
+	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
+	gridLaunchDependents();
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < nU)
+	{
+		const uint32_t pos = i + upperBound32(sKeys, nS, uKeys[i]);
+		order[pos] = uIds[i];
+		updPos[i] = pos;
+	}
+	else if(i < nU + nS)
+	{
+		const uint32_t j = i - nU;
+		const uint32_t pos = j + lowerBound32(uKeys, nU, sKeys[j]);
+		order[pos] = sIds[j];
+		sleepPos[j] = pos;
+	}
+}
+
 __global__ void gatherSortedKernel(const uint32_t* __restrict__ sortedIds, uint32_t n, const uint2* __restrict__ bx,
                                    const float4* __restrict__ byz, const uint32_t* __restrict__ groups, const uint8_t* __restrict__ flags,
                                    uint2* __restrict__ sx, float4* __restrict__ syz, uint32_t* __restrict__ sgrp, uint32_t* __restrict__ supd)
@@ -759,6 +850,9 @@ struct BroadPhase
 	DevBuf<uint2> sx;
 	DevBuf<float4> syz;
 	DevBuf<uint32_t> sgrp, supd, updPos, sleepPos;
+	// the sorted order of the live boxes, kept from frame to frame (two sides)
+	DevBuf<uint32_t> order[2], keepFlag, keptPos, keptIds, keptKeys;
+	uint32_t orderSide = 0, nOrder = 0;
 	DevBuf<unsigned long long> found, foundAlt, prev, next, created, lost;
 	DevBuf<uint32_t> counter, cls, sel, pos;
 	DevBuf<uint4> longScans;
@@ -809,6 +903,7 @@ struct BroadPhase
 		dRecs.release(); dRemoved.release(); hRecs.release();
 		blockCounts.release(); scanScratch.release(); keysA.release(); valsA.release(); keysB.release(); valsB.release(); hist.release();
 		sx.release(); syz.release(); sgrp.release(); supd.release(); updPos.release(); sleepPos.release();
+		order[0].release(); order[1].release(); keepFlag.release(); keptPos.release(); keptIds.release(); keptKeys.release();
 		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
 		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release(); longScans.release();
 		hCounts.release(); hCreated.release(); hLost.release();
@@ -921,43 +1016,56 @@ struct BroadPhase
 			GBPX_CUDA_TRY(cudaMemcpyAsync(dRecs.ptr, hRecs.ptr, size_t(nbRec) * sizeof(bp::UpdateRec), cudaMemcpyHostToDevice, stream));
 			(void)launchDependent(bp::applyUpdatesKernel, divUp(nbRec, 256), 256, stream, dRecs.ptr, nbRec, bx.ptr, byz.ptr, groups.ptr, live.ptr, flags.ptr);
 		}
-		return runFrame(nbRec + nbRemoved);
+		return runFrame(nbRec + nbRemoved, dRecs.ptr, nbRec);
 	}
 
 	// Everything after the object state is current on the device.
-	int runFrame(uint32_t nbTouched)
+	// updatedRecs: the update records of the created / updated boxes (null: handles
+	// [0, nbUpdatedBoxes) were updated from device bounds)
+	int runFrame(uint32_t nbTouched, const bp::UpdateRec* updatedRecs, uint32_t nbUpdatedBoxes)
 	{
-		// 2. Live boxes sorted by encoded min X.
-		const uint32_t nbBlk = divUp(capacity, 256);
-		if(blockCounts.reserve(nbBlk + 1)) return GBPX_ERR_NOMEM;
-		(void)launchDependent(bp::countLiveKernel, nbBlk, 256, stream, live.ptr, capacity, blockCounts.ptr);
-		GBPX_CUDA_TRY(cudaMemsetAsync(blockCounts.ptr + nbBlk, 0, 4, stream));
-		(void)launchDependent(rs::scanKernel, 1, 1024, stream, blockCounts.ptr, nbBlk + 1);
-		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + nbBlk, 4, cudaMemcpyDeviceToHost, stream));
-		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
-		const uint32_t n = hCounts.ptr[0];
-		if(keysA.reserve(n + 1) || valsA.reserve(n + 1) || keysB.reserve(n + 1) || valsB.reserve(n + 1) ||
-		   hist.reserve(radixSortHistEntries(n) + 1) || sx.reserve(n + 1) || syz.reserve(n + 1) || sgrp.reserve(n + 1) ||
-		   supd.reserve(n + 1) || updPos.reserve(n + 1) || sleepPos.reserve(n + 1))
+		// 2. Live boxes sorted by encoded min X: last frame's order without the
+		// removed and updated boxes, merged with the created / updated ones sorted.
+		const uint32_t nPrevOrder = nOrder;
+		const uint32_t* prevOrder = order[orderSide].ptr;
+		uint32_t nbS = 0;
+		if(nPrevOrder)
+		{
+			if(keepFlag.reserve(nPrevOrder + 1) || keptPos.reserve(nPrevOrder + 1)) return GBPX_ERR_NOMEM;
+			(void)launchDependent(bp::keepFlagKernel, divUp(nPrevOrder, 256), 256, stream, prevOrder, nPrevOrder, live.ptr, flags.ptr, keepFlag.ptr);
+			if(compactFlag(keepFlag.ptr, nPrevOrder, 1u, keptPos.ptr)) return GBPX_ERR_NOMEM;
+			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + divUp(nPrevOrder, 256), 4, cudaMemcpyDeviceToHost, stream));
+			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+			nbS = hCounts.ptr[0];
+		}
+		const uint32_t nbU = nbUpdatedBoxes;
+		const uint32_t n = nbS + nbU;
+		if(keysA.reserve(nbU + 1) || valsA.reserve(nbU + 1) || keysB.reserve(nbU + 1) || valsB.reserve(nbU + 1) ||
+		   hist.reserve(radixSortHistEntries(nbU) + 1) || keptIds.reserve(nbS + 1) || keptKeys.reserve(nbS + 1) ||
+		   order[orderSide ^ 1u].reserve(n + 1) || sx.reserve(n + 1) || syz.reserve(n + 1) || sgrp.reserve(n + 1) || supd.reserve(n + 1) ||
+		   updPos.reserve(nbU + 1) || sleepPos.reserve(nbS + 1))
 			return GBPX_ERR_NOMEM;
-		(void)launchDependent(bp::emitLiveKernel, nbBlk, 256, stream, live.ptr, bx.ptr, capacity, blockCounts.ptr, keysA.ptr, valsA.ptr);
-		const bool alt = radixSort<uint32_t, true>(keysA.ptr, valsA.ptr, keysB.ptr, valsB.ptr, n, 0, 32, hist.ptr, stream);
-		const uint32_t* sortedIds = alt ? valsB.ptr : valsA.ptr;
-		if(n)
-			(void)launchDependent(bp::gatherSortedKernel, divUp(n, 256), 256, stream, sortedIds, n, bx.ptr, byz.ptr, groups.ptr, flags.ptr, sx.ptr, syz.ptr,
-			                                                        sgrp.ptr, supd.ptr);
-
-		// 3. Split sorted positions into updated / sleeping lists.
-		uint32_t nbUpd = 0;
+		if(nbU) (void)launchDependent(bp::updatedKeysKernel, divUp(nbU, 256), 256, stream, updatedRecs, nbU, bx.ptr, keysA.ptr, valsA.ptr);
+		const bool alt = radixSort<uint32_t, true>(keysA.ptr, valsA.ptr, keysB.ptr, valsB.ptr, nbU, 0, 32, hist.ptr, stream);
+		const uint32_t* uKeys = alt ? keysB.ptr : keysA.ptr;
+		const uint32_t* uIds = alt ? valsB.ptr : valsA.ptr;
+		if(nbS)
+			(void)launchDependent(bp::gatherKeptKernel, divUp(nbS, 256), 256, stream, prevOrder, keptPos.ptr, nbS, bx.ptr, keptIds.ptr, keptKeys.ptr);
+		uint32_t* sortedIds = order[orderSide ^ 1u].ptr;
 		if(n)
 		{
-			if(compactFlag(supd.ptr, n, 1u, updPos.ptr)) return GBPX_ERR_NOMEM;
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, blockCounts.ptr + divUp(n, 256), 4, cudaMemcpyDeviceToHost, stream));
-			GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
-			nbUpd = hCounts.ptr[0];
-			if(compactFlag(supd.ptr, n, 0u, sleepPos.ptr)) return GBPX_ERR_NOMEM;
+			(void)launchDependent(bp::mergeOrderKernel, divUp(n, 256), 256, stream, uKeys, uIds, nbU, keptKeys.ptr, keptIds.ptr, nbS, sortedIds,
+			                      updPos.ptr, sleepPos.ptr);
+			(void)launchDependent(bp::gatherSortedKernel, divUp(n, 256), 256, stream, sortedIds, n, bx.ptr, byz.ptr, groups.ptr, flags.ptr, sx.ptr,
+			                      syz.ptr, sgrp.ptr, supd.ptr);
 		}
-		const uint32_t nbSleep = n - nbUpd;
+		orderSide ^= 1u;
+		nOrder = n;
+
+		// 3. The sweep's lists: sorted positions of the updated boxes (updPos) and of
+		// the others (sleepPos), both written by the merge.
+		const uint32_t nbUpd = nbU;
+		const uint32_t nbSleep = nbS;
 
 		// 4. Sweep.  The found buffer grows and the sweep reruns if it overflowed.
 		uint32_t nFound = 0;
@@ -1081,7 +1189,7 @@ struct BroadPhase
 		if(pending || n > capacity) return GBPX_ERR_STATE;
 		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
 		if(n) (void)launchDependent(bp::applyDeviceBoundsKernel, divUp(n, 256), 256, stream, dBounds, n, bx.ptr, byz.ptr, flags.ptr);
-		const int rc = runFrame(n);
+		const int rc = runFrame(n, nullptr, n);
 		if(rc) return rc;
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		pending = false;
