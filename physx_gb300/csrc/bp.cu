@@ -805,27 +805,37 @@ __global__ void scatterSelectedKernel(const unsigned long long* __restrict__ src
 	if(i < n && sel[i]) dst[pos[i]] = src[i];
 }
 
-// Merge of two sorted, disjoint key arrays by co-ranking.
-__global__ void mergeKernel(const unsigned long long* __restrict__ a, uint32_t na, const unsigned long long* __restrict__ b, uint32_t nb,
-                            unsigned long long* __restrict__ out)
+// Merge of two sorted, disjoint key arrays by co-ranking, the first one's length
+// read from device memory: threads [0, keepCap) place its keys (those below
+// *nKeep), threads [keepCap, keepCap + nb) the second's; thread 0 also writes the
+// merged count to *nOut.
+__global__ void mergeCountedKernel(const unsigned long long* __restrict__ a, const uint32_t* __restrict__ nKeep, uint32_t keepCap,
+                                   const unsigned long long* __restrict__ b, uint32_t nb, unsigned long long* __restrict__ out, uint32_t* __restrict__ nOut)
 {
 	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
 	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i < na) out[i + lowerBound(b, nb, a[i])] = a[i];
-	else if(i < na + nb)
+	const uint32_t na = *nKeep;
+	if(i == 0) *nOut = na + nb;
+	if(i < keepCap)
 	{
-		const uint32_t j = i - na;
+		if(i < na) out[i + lowerBound(b, nb, a[i])] = a[i];
+	}
+	else if(i < keepCap + nb)
+	{
+		const uint32_t j = i - keepCap;
 		out[j + lowerBound(a, na, b[j])] = b[j];
 	}
 }
 
-__global__ void keysToPairsKernel(const unsigned long long* __restrict__ keys, uint32_t n, uint2* __restrict__ out)
+// Pair keys (id0 << 32 | id1) to (id0, id1) for the first *n keys; the grid is
+// sized by an upper bound of *n.
+__global__ void keysToPairsCountedKernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ n, uint2* __restrict__ out)
 {
 	gridDependencyWait();   // may be launched dependent on the previous kernel (launchDependent)
 	gridLaunchDependents();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i < n) out[i] = make_uint2(uint32_t(keys[i] >> 32), uint32_t(keys[i]));
+	if(i < *n) out[i] = make_uint2(uint32_t(keys[i] >> 32), uint32_t(keys[i]));
 }
 
 } // namespace bp
@@ -856,11 +866,15 @@ struct BroadPhase
 	DevBuf<unsigned long long> found, foundAlt, prev, next, created, lost;
 	DevBuf<uint32_t> counter, cls, sel, pos;
 	DevBuf<uint4> longScans;
-	DevBuf<uint2> createdPairs, lostPairs;
 	HostBuf<uint32_t> hCounts;
 	HostBuf<uint2> hCreated, hLost;
 	uint32_t nPrev = 0;
 	uint32_t nbCreatedOut = 0, nbLostOut = 0;
+	// created, lost, kept and next-active counts of the frame in flight, on the device
+	// and (after the frame's one synchronisation) in pinned host memory
+	DevBuf<uint32_t> frameCounts;
+	HostBuf<uint32_t> hFrameCounts;
+	uint32_t nFoundLast = 0;
 	bool pending = false;
 	uint64_t stats[4] = {0, 0, 0, 0};  // live boxes, updated boxes, found pairs, active pairs (last update)
 	// timing of the last update: host staging of the user's arrays (ms), and the
@@ -905,8 +919,8 @@ struct BroadPhase
 		sx.release(); syz.release(); sgrp.release(); supd.release(); updPos.release(); sleepPos.release();
 		order[0].release(); order[1].release(); keepFlag.release(); keptPos.release(); keptIds.release(); keptKeys.release();
 		found.release(); foundAlt.release(); prev.release(); next.release(); created.release(); lost.release();
-		counter.release(); cls.release(); sel.release(); pos.release(); createdPairs.release(); lostPairs.release(); longScans.release();
-		hCounts.release(); hCreated.release(); hLost.release();
+		counter.release(); cls.release(); sel.release(); pos.release(); frameCounts.release(); longScans.release();
+		hCounts.release(); hCreated.release(); hLost.release(); hFrameCounts.release();
 		if(evBegin) cudaEventDestroy(evBegin);
 		if(evEnd) cudaEventDestroy(evEnd);
 		evBegin = evEnd = nullptr;
@@ -950,18 +964,25 @@ struct BroadPhase
 		return GBPX_OK;
 	}
 
-	// Exclusive scan of sel[0..n) into pos; total read back to *total (synchronous).
-	int scanSelect(const uint32_t* selIn, uint32_t n, uint32_t* posOut, uint32_t* total)
+	// Exclusive scan of sel[0..n) into pos (total at pos[n]), copied to *countOut on
+	// the device; nothing waits for it.
+	int scanToDevice(const uint32_t* selIn, uint32_t n, uint32_t* posOut, uint32_t* countOut)
 	{
-		if(!n) { *total = 0; return GBPX_OK; }
 		GBPX_CUDA_TRY(cudaMemcpyAsync(posOut, selIn, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream));
 		GBPX_CUDA_TRY(cudaMemsetAsync(posOut + n, 0, 4, stream));
 		if(scanScratch.reserve(rs::scanScratchEntries(n + 1))) return GBPX_ERR_NOMEM;
 		rs::scanAny(posOut, n + 1, scanScratch.ptr, stream);
-		GBPX_CUDA_TRY(cudaMemcpyAsync(hCounts.ptr, posOut + n, 4, cudaMemcpyDeviceToHost, stream));
-		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
-		*total = hCounts.ptr[0];
+		GBPX_CUDA_TRY(cudaMemcpyAsync(countOut, posOut + n, 4, cudaMemcpyDeviceToDevice, stream));
 		return GBPX_OK;
+	}
+
+	// The host side of the frame once its stream has drained: counts in force.
+	void finishFrame()
+	{
+		nbCreatedOut = hFrameCounts.ptr[0];
+		nbLostOut = hFrameCounts.ptr[1];
+		nPrev = hFrameCounts.ptr[3];
+		stats[3] = nPrev;
 	}
 
 	int update(const uint32_t* createdIds, uint32_t nbCreated, const uint32_t* updatedIds, uint32_t nbUpdated,
@@ -1016,13 +1037,13 @@ struct BroadPhase
 			GBPX_CUDA_TRY(cudaMemcpyAsync(dRecs.ptr, hRecs.ptr, size_t(nbRec) * sizeof(bp::UpdateRec), cudaMemcpyHostToDevice, stream));
 			(void)launchDependent(bp::applyUpdatesKernel, divUp(nbRec, 256), 256, stream, dRecs.ptr, nbRec, bx.ptr, byz.ptr, groups.ptr, live.ptr, flags.ptr);
 		}
-		return runFrame(nbRec + nbRemoved, dRecs.ptr, nbRec);
+		return runFrame(nbRec + nbRemoved, dRecs.ptr, nbRec, true);
 	}
 
 	// Everything after the object state is current on the device.
 	// updatedRecs: the update records of the created / updated boxes (null: handles
 	// [0, nbUpdatedBoxes) were updated from device bounds)
-	int runFrame(uint32_t nbTouched, const bp::UpdateRec* updatedRecs, uint32_t nbUpdatedBoxes)
+	int runFrame(uint32_t nbTouched, const bp::UpdateRec* updatedRecs, uint32_t nbUpdatedBoxes, bool hostResults)
 	{
 		// 2. Live boxes sorted by encoded min X: last frame's order without the
 		// removed and updated boxes, merged with the created / updated ones sorted.
@@ -1125,57 +1146,62 @@ struct BroadPhase
 			F = a2 ? foundAlt.ptr : found.ptr;
 		}
 
-		// 6. Created / lost / next active set.
+		// 6. Created / lost / next active set; the counts stay on the device until the
+		// frame's one synchronisation (fetchResults / updateFromDevice).
 		const uint32_t m = std::max(nFound, nPrev) + 1;
 		if(cls.reserve(m) || sel.reserve(m) || pos.reserve(m + 1) || created.reserve(m) || lost.reserve(m) || next.reserve(size_t(nFound) + nPrev + 1) ||
-		   prev.reserve(1) || createdPairs.reserve(m) || lostPairs.reserve(m))
+		   prev.reserve(1) || frameCounts.reserve(4) || hFrameCounts.reserve(4) ||
+		   (hostResults && (hCreated.reserve(size_t(nFound) + 1) || hLost.reserve(size_t(nPrev) + 1))))
 			return GBPX_ERR_NOMEM;
-		uint32_t nCreated = 0, nLost = 0, nKeep = 0;
+		GBPX_CUDA_TRY(cudaMemsetAsync(frameCounts.ptr, 0, 16, stream));
+		uint32_t* dCreated = frameCounts.ptr + 0;
+		uint32_t* dLost = frameCounts.ptr + 1;
+		uint32_t* dKeep = frameCounts.ptr + 2;
+		uint32_t* dNext = frameCounts.ptr + 3;
 		if(nFound)
 		{
 			(void)launchDependent(bp::classifyFoundKernel, divUp(nFound, 256), 256, stream, F, nFound, prev.ptr, nPrev, sel.ptr);
-			int r2 = scanSelect(sel.ptr, nFound, pos.ptr, &nCreated);
+			int r2 = scanToDevice(sel.ptr, nFound, pos.ptr, dCreated);
 			if(r2) return r2;
 			(void)launchDependent(bp::scatterSelectedKernel, divUp(nFound, 256), 256, stream, F, sel.ptr, pos.ptr, nFound, created.ptr);
 		}
-		unsigned long long* keep = lost.ptr + 0;  // placeholder, reassigned below
 		DevBuf<unsigned long long>& keepBuf = foundAlt.ptr == F ? found : foundAlt;  // the sort buffer not holding F
 		if(keepBuf.reserve(size_t(nPrev) + 1)) return GBPX_ERR_NOMEM;
-		keep = keepBuf.ptr;
+		unsigned long long* keep = keepBuf.ptr;
 		if(nPrev)
 		{
 			(void)launchDependent(bp::classifyPrevKernel, divUp(nPrev, 256), 256, stream, prev.ptr, nPrev, F, nFound, flags.ptr, cls.ptr);
 			(void)launchDependent(bp::flagEqualsKernel, divUp(nPrev, 256), 256, stream, cls.ptr, nPrev, 2u, sel.ptr);
-			int r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nLost);
+			int r2 = scanToDevice(sel.ptr, nPrev, pos.ptr, dLost);
 			if(r2) return r2;
 			(void)launchDependent(bp::scatterSelectedKernel, divUp(nPrev, 256), 256, stream, prev.ptr, sel.ptr, pos.ptr, nPrev, lost.ptr);
 			(void)launchDependent(bp::flagEqualsKernel, divUp(nPrev, 256), 256, stream, cls.ptr, nPrev, 1u, sel.ptr);
-			r2 = scanSelect(sel.ptr, nPrev, pos.ptr, &nKeep);
+			r2 = scanToDevice(sel.ptr, nPrev, pos.ptr, dKeep);
 			if(r2) return r2;
 			(void)launchDependent(bp::scatterSelectedKernel, divUp(nPrev, 256), 256, stream, prev.ptr, sel.ptr, pos.ptr, nPrev, keep);
 		}
-		const uint32_t nNext = nKeep + nFound;
-		if(nNext)
-			(void)launchDependent(bp::mergeKernel, divUp(nNext, 256), 256, stream, keep, nKeep, F, nFound, next.ptr);
+		// the next active set: kept pairs merged with the found ones (sizes bounded by nPrev, nFound)
+		if(nPrev + nFound)
+			(void)launchDependent(bp::mergeCountedKernel, divUp(nPrev + nFound, 256), 256, stream, keep, dKeep, nPrev, F, nFound, next.ptr, dNext);
 		std::swap(prev, next);
-		nPrev = nNext;
 
-		// 7. Results to the host (owned by the broadphase until the next update).
-		if(hCreated.reserve(nCreated + 1) || hLost.reserve(nLost + 1)) return GBPX_ERR_NOMEM;
-		if(nCreated)
+		// 7. Results to the host (owned by the broadphase until the next update): the
+		// pair lists are written straight into pinned host memory, only as many pairs
+		// as the device counts hold (created <= found, lost <= previous active).
+		if(hostResults)
 		{
-			(void)launchDependent(bp::keysToPairsKernel, divUp(nCreated, 256), 256, stream, created.ptr, nCreated, createdPairs.ptr);
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hCreated.ptr, createdPairs.ptr, size_t(nCreated) * 8, cudaMemcpyDeviceToHost, stream));
+			uint2* dHostCreated = nullptr;
+			uint2* dHostLost = nullptr;
+			GBPX_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&dHostCreated), hCreated.ptr, 0));
+			GBPX_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&dHostLost), hLost.ptr, 0));
+			if(nFound)
+				(void)launchDependent(bp::keysToPairsCountedKernel, divUp(nFound, 256), 256, stream, created.ptr, dCreated, dHostCreated);
+			if(nPrev)
+				(void)launchDependent(bp::keysToPairsCountedKernel, divUp(nPrev, 256), 256, stream, lost.ptr, dLost, dHostLost);
 		}
-		if(nLost)
-		{
-			(void)launchDependent(bp::keysToPairsKernel, divUp(nLost, 256), 256, stream, lost.ptr, nLost, lostPairs.ptr);
-			GBPX_CUDA_TRY(cudaMemcpyAsync(hLost.ptr, lostPairs.ptr, size_t(nLost) * 8, cudaMemcpyDeviceToHost, stream));
-		}
+		GBPX_CUDA_TRY(cudaMemcpyAsync(hFrameCounts.ptr, frameCounts.ptr, 16, cudaMemcpyDeviceToHost, stream));
 		if(evEnd) GBPX_CUDA_TRY(cudaEventRecord(evEnd, stream));
-		nbCreatedOut = nCreated;
-		nbLostOut = nLost;
-		stats[0] = n; stats[1] = nbUpd; stats[2] = nFound; stats[3] = nPrev;
+		stats[0] = n; stats[1] = nbUpd; stats[2] = nFound;
 		(void)nbTouched;
 		pending = true;
 		return GBPX_OK;
@@ -1189,9 +1215,10 @@ struct BroadPhase
 		if(pending || n > capacity) return GBPX_ERR_STATE;
 		GBPX_CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, capacity, stream));
 		if(n) (void)launchDependent(bp::applyDeviceBoundsKernel, divUp(n, 256), 256, stream, dBounds, n, bx.ptr, byz.ptr, flags.ptr);
-		const int rc = runFrame(n, nullptr, n);
+		const int rc = runFrame(n, nullptr, n, false);
 		if(rc) return rc;
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		finishFrame();
 		pending = false;
 		return GBPX_OK;
 	}
@@ -1201,6 +1228,7 @@ struct BroadPhase
 		if(!pending) return GBPX_ERR_STATE;
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		GBPX_CUDA_TRY(cudaGetLastError());
+		finishFrame();
 		pending = false;
 		if(evBegin && evEnd && cudaEventElapsedTime(&lastDeviceMs, evBegin, evEnd) != cudaSuccess) lastDeviceMs = -1.0f;
 		*outCreated = hCreated.ptr;
