@@ -83,9 +83,17 @@ uint32_t gbpx_bp_kinematic_filter_group(uint32_t id);
 
 /* -------------------------------------------------------------- narrowphase
  * immediate::PxGenerateContacts (physx/include/PxImmediateMode.h:267) for
- * sphere / plane / capsule / box pairs with a fresh PxCache per pair.
- * type: PxGeometryType (0 sphere, 1 plane, 2 capsule, 3 box); geom: 4 floats
- * (sphere r | capsule r, halfHeight | box hx, hy, hz); pose: PxTransform.
+ * sphere / plane / capsule / box / convex-core pairs with a fresh PxCache per
+ * pair.  type: PxGeometryType (0 sphere, 1 plane, 2 capsule, 3 box, 4 convex
+ * core) in the low byte; for a convex core (PxConvexCoreGeometry,
+ * physx/include/geometry/PxConvexCoreGeometry.h) bits 8..15 hold its
+ * PxConvexCore::Type (0 point, 1 segment, 2 box, 3 ellipsoid, 4 cylinder,
+ * 5 cone), so type = 4 | coreType << 8.  geom: 4 floats (sphere r | capsule r,
+ * halfHeight | box hx, hy, hz | convex core: the core's floats — segment
+ * length; box extents xyz; ellipsoid radii xyz; cylinder or cone height,
+ * radius — then the margin in geom[3]); pose: PxTransform.  Convex-core pairs
+ * give at most 4 contacts (GuConvexSupport.h MAX_CONVEX_CONTACTS) and keep no
+ * cache.
  * outContacts: nbPairs x maxPerPair x 8 floats (normal xyz, separation,
  * point xyz, 0); outCounts: contacts per pair.  The normal points along the
  * direction shape0 must move, as PxContactPoint (geomutils/PxContactPoint.h:39). */
@@ -111,8 +119,8 @@ int gbpx_generate_contacts_cached(const int* type0, const float* geom0, const in
  * dOutContacts holds 4 contacts x 8 floats per pair and is 16-byte aligned),
  * the work is enqueued on `stream` (a cudaStream_t, NULL = default stream).
  * Caches are fresh (no PxCache is read or written).  Geometry types must be
- * 0..3: the device arrays are not checked on the host, and other values give
- * undefined contacts.
+ * the ones above: the device arrays are not checked on the host, and other
+ * values give undefined contacts.
  * Scratch is a fixed 1 MiB device array, so nbPairs <= 262144
  * (GBPX_ERR_CAPACITY above).  The scratch is shared by every call on a
  * device: calls that may overlap must be serialised by the caller.  The first

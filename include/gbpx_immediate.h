@@ -69,6 +69,10 @@ struct PxSphereGeometry : PxGeometry { float radius; };
 struct PxCapsuleGeometry : PxGeometry { float radius, halfHeight; };
 struct PxBoxGeometry : PxGeometry { PxVec3 halfExtents; };
 struct PxPlaneGeometry : PxGeometry {};
+// PxConvexCoreGeometry (geometry/PxConvexCoreGeometry.h:227): PxConvexCore::Type,
+// the core's data (MAX_CORE_SIZE = 6 floats: segment length; box extents;
+// ellipsoid radii; cylinder / cone height, radius) and the margin
+struct PxConvexCoreGeometry : PxGeometry { int mCoreType; uint8_t mCore[24]; float mMargin; };
 
 struct alignas(16) PxContactPoint
 {

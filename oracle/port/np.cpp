@@ -21,6 +21,8 @@
 #include <string.h>
 #include <algorithm>
 
+#include "convex_core.h"
+
 #define OX extern "C" __attribute__((visibility("default")))
 
 using namespace orc;
@@ -1526,6 +1528,28 @@ Tr loadTr(const float* p)
 }
 } // namespace
 
+// A pair with a convex core (type low byte 4, core type in bits 8..15): the
+// reference's table order (shape types ascending, normals negated when
+// swapped), contactPlaneConvexCore or contactConvexCoreConvex.  Returns the count.
+static int convexCorePair(int ta, const float* ga, int tb, const float* gb, Tr pa, Tr pb, float contactDistance, float* out, uint32_t maxPerPair)
+{
+	const bool swap = (ta & 0xff) > (tb & 0xff);
+	if(swap) { std::swap(ta, tb); std::swap(ga, gb); std::swap(pa, pb); }
+	V3 normal = v3(0, 0, 0), points[cc::MAX_CONTACTS];
+	float dists[cc::MAX_CONTACTS];
+	const uint32_t n = cc::generatePair(ta, ga, tb, gb, pa, pb, contactDistance, normal, points, dists);
+	if(swap) normal = neg(normal);
+	for(uint32_t c = 0; c < n && c < maxPerPair; c++)
+	{
+		float* o = out + size_t(c) * 8;
+		o[0] = normal.x; o[1] = normal.y; o[2] = normal.z; o[3] = dists[c];
+		o[4] = points[c].x; o[5] = points[c].y; o[6] = points[c].z; o[7] = 0.0f;
+	}
+	return int(n);
+}
+
+static bool isConvexCorePair(int ta, int tb) { return (ta & 0xff) == 4 || (tb & 0xff) == 4; }
+
 // PxGenerateContacts over nbPairs pairs with fresh caches.  Layout as the
 // reference harness (pose 7 floats, geom 4 floats, contact 8 floats).
 OX int orc_np_run(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0, const float* pose1,
@@ -1540,6 +1564,13 @@ OX int orc_np_run(const int* type0, const float* geom0, const int* type1, const 
 		const float* ga = geom0 + 4 * i;
 		const float* gb = geom1 + 4 * i;
 		Tr pa = loadTr(pose0 + 7 * i), pb = loadTr(pose1 + 7 * i);
+		if(isConvexCorePair(ta, tb))
+		{
+			const int n = convexCorePair(ta, ga, tb, gb, pa, pb, contactDistance, outContacts + size_t(i) * maxPerPair * 8, maxPerPair);
+			outCounts[i] = uint32_t(n);
+			if(uint32_t(n) > maxPerPair) overflow = 1;
+			continue;
+		}
 		const bool swap = ta > tb;
 		if(swap) { std::swap(ta, tb); std::swap(ga, gb); std::swap(pa, pb); }
 		Buffer buf;
@@ -1630,6 +1661,13 @@ OX int orc_np_run_cached(const int* type0, const float* geom0, const int* type1,
 		const float* ga = geom0 + 4 * i;
 		const float* gb = geom1 + 4 * i;
 		Tr pa = loadTr(pose0 + 7 * i), pb = loadTr(pose1 + 7 * i);
+		if(isConvexCorePair(ta, tb))
+		{
+			const int n = convexCorePair(ta, ga, tb, gb, pa, pb, contactDistance, outContacts + size_t(i) * maxPerPair * 8, maxPerPair);
+			outCounts[i] = uint32_t(n);
+			if(uint32_t(n) > maxPerPair) overflow = 1;
+			continue;   // no manifold is kept for these pairs: the record is left as it was
+		}
 		const bool swap = ta > tb;
 		if(swap) { std::swap(ta, tb); std::swap(ga, gb); std::swap(pa, pb); }
 		Buffer buf;

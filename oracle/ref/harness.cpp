@@ -8,8 +8,10 @@
 //
 // Layout conventions shared with the rest of the repository:
 //   pose    = 7 floats  (qx, qy, qz, qw, px, py, pz)          -- PxTransform
-//   geom    = type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box) +
-//             4 floats (sphere: r; capsule: r, halfHeight; box: hx, hy, hz)
+//   geom    = type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box, 4 convex core
+//             with its PxConvexCore::Type in bits 8..15) +
+//             4 floats (sphere: r; capsule: r, halfHeight; box: hx, hy, hz;
+//             convex core: its core floats, margin in the fourth)
 //   contact = 8 floats  (nx, ny, nz, separation, px, py, pz, 0)
 #include "PxImmediateMode.h"
 #include "PxBroadPhase.h"
@@ -21,6 +23,7 @@
 #include "geometry/PxPlaneGeometry.h"
 #include "geometry/PxCapsuleGeometry.h"
 #include "geometry/PxBoxGeometry.h"
+#include "geometry/PxConvexCoreGeometry.h"
 #include "geomutils/PxContactPoint.h"
 #include "collision/PxCollisionDefs.h"
 #include "solver/PxSolverDefs.h"
@@ -130,14 +133,26 @@ struct GeomHolder
 	PxPlaneGeometry plane;
 	PxCapsuleGeometry capsule;
 	PxBoxGeometry box;
+	PxConvexCoreGeometry convex;
 	const PxGeometry* set(int type, const float* p)
 	{
-		switch(type)
+		switch(type & 0xff)
 		{
 		case 0: sphere = PxSphereGeometry(p[0]); return &sphere;
 		case 1: plane = PxPlaneGeometry(); return &plane;
 		case 2: capsule = PxCapsuleGeometry(p[0], p[1]); return &capsule;
 		case 3: box = PxBoxGeometry(p[0], p[1], p[2]); return &box;
+		case 4:   // convex core: PxConvexCore::Type in bits 8..15, core floats, margin in p[3]
+			switch((type >> 8) & 0xff)
+			{
+			case 0: convex = PxConvexCoreGeometry(PxConvexCore::Point(), p[3]); return &convex;
+			case 1: convex = PxConvexCoreGeometry(PxConvexCore::Segment(p[0]), p[3]); return &convex;
+			case 2: convex = PxConvexCoreGeometry(PxConvexCore::Box(p[0], p[1], p[2]), p[3]); return &convex;
+			case 3: convex = PxConvexCoreGeometry(PxConvexCore::Ellipsoid(p[0], p[1], p[2]), p[3]); return &convex;
+			case 4: convex = PxConvexCoreGeometry(PxConvexCore::Cylinder(p[0], p[1]), p[3]); return &convex;
+			case 5: convex = PxConvexCoreGeometry(PxConvexCore::Cone(p[0], p[1]), p[3]); return &convex;
+			default: return nullptr;
+			}
 		default: return nullptr;
 		}
 	}

@@ -1,9 +1,12 @@
 """immediate::PxGenerateContacts mirror over the GB300 narrowphase.
 
 Mirrors physx/include/PxImmediateMode.h:267 for sphere / plane / capsule / box
-geometries with a fresh PxCache per pair.  Pairs are given as arrays:
-type0/type1 (PxGeometryType), geom0/geom1 (4 floats), pose0/pose1 (7 floats
-qx qy qz qw px py pz).  Contacts come back as (counts, contacts[n, max, 8]).
+and convex-core (PxConvexCoreGeometry) geometries with a fresh PxCache per
+pair.  Pairs are given as arrays: type0/type1 (PxGeometryType; a convex core is
+4 | its PxConvexCore::Type << 8, see workloads.convex_core_type), geom0/geom1
+(4 floats; a convex core's core floats and its margin last), pose0/pose1
+(7 floats qx qy qz qw px py pz).  Contacts come back as
+(counts, contacts[n, max, 8]).
 """
 import ctypes
 

@@ -41,6 +41,16 @@ bool packShape(const PxGeometry& g, int& type, float* out)
 		out[0] = h.x; out[1] = h.y; out[2] = h.z;
 		return true;
 	}
+	case 4:
+	{
+		// convex core: its type in bits 8..15, the first 3 core floats, the margin
+		const PxConvexCoreGeometry& c = static_cast<const PxConvexCoreGeometry&>(g);
+		if(c.mCoreType < 0 || c.mCoreType > 5) return false;
+		type = 4 | (c.mCoreType << 8);
+		memcpy(out, c.mCore, 3 * sizeof(float));
+		out[3] = c.mMargin;
+		return true;
+	}
 	default: return false;
 	}
 }

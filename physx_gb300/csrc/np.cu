@@ -1,15 +1,20 @@
 // Narrowphase for the GB300 rigid-body step: immediate::PxGenerateContacts
 // (physx/include/PxImmediateMode.h:267, physx/source/immediatemode/src/NpImmediateMode.cpp:732)
-// over a batch of sphere / plane / capsule / box pairs, with fresh caches or
-// with each pair's persistent contact manifold carried between calls.
+// over a batch of sphere / plane / capsule / box / convex-core pairs, with
+// fresh caches or with each pair's persistent contact manifold carried between
+// calls (convex-core pairs keep none).
 //
-// GB300 layout: the batch is bucketed by (type0, type1) with a 16-bin counting
-// pass so every warp runs a single generator (no divergence between pair
-// types); each lane runs one pair and writes its <= 4 contacts as float4 pairs
+// GB300 layout: the batch is bucketed by (type0, type1) with a counting pass
+// (16 bins for the sphere/plane/capsule/box kinds, then 5 for the pairs with a
+// convex core, which come last) so every warp runs a single generator (no
+// divergence between pair types); the convex-core pairs run in their own
+// kernel, whose GJK/EPA working set does not weigh on the others' registers.
+// Each lane runs one pair and writes its <= 4 contacts as float4 pairs
 // (normal|separation, point|0) into a fixed 4-slot record, so no compaction is
 // needed and the host reads counts + records in one copy.
 #include "common.cuh"
 #include "contacts.cuh"
+#include "convex_core.cuh"
 #include <atomic>
 #include <mutex>
 
@@ -30,21 +35,29 @@ __device__ __forceinline__ Tr loadPose7(const float* p)
 	return t;
 }
 
+constexpr uint32_t NP_BINS = 32;   // 16 primitive kinds, 5 convex-core kinds, unused
+
+// a shape type's PxGeometryType (the low byte; a convex core carries its core type above it)
+__device__ __forceinline__ int geomType(int t) { return t & 0xff; }
+__device__ __forceinline__ bool convexCorePair(int t0, int t1) { return geomType(t0) == 4 || geomType(t1) == 4; }
+
 __device__ __forceinline__ uint32_t pairKey(int t0, int t1)
 {
-	const int a = t0 < t1 ? t0 : t1, b = t0 < t1 ? t1 : t0;
+	const int g0 = geomType(t0), g1 = geomType(t1);
+	const int a = g0 < g1 ? g0 : g1, b = g0 < g1 ? g1 : g0;
+	if(b == 4) return 16u + uint32_t(a & 7);
 	return uint32_t(((a & 3) << 2) | (b & 3));
 }
 
 __global__ void bucketCountKernel(PairRef pr, uint32_t n, uint32_t* __restrict__ hist)
 {
-	__shared__ uint32_t h[16];
-	if(threadIdx.x < 16) h[threadIdx.x] = 0;
+	__shared__ uint32_t h[NP_BINS];
+	if(threadIdx.x < NP_BINS) h[threadIdx.x] = 0;
 	__syncthreads();
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n) atomicAdd(&h[pairKey(pr.type0[i], pr.type1[i])], 1u);
 	__syncthreads();
-	if(threadIdx.x < 16 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+	if(threadIdx.x < NP_BINS && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
 __global__ void bucketOffsetsKernel(uint32_t* __restrict__ hist)
@@ -52,7 +65,7 @@ __global__ void bucketOffsetsKernel(uint32_t* __restrict__ hist)
 	if(threadIdx.x == 0)
 	{
 		uint32_t run = 0;
-		for(int k = 0; k < 16; k++) { const uint32_t c = hist[k]; hist[k] = run; hist[16 + k] = run; run += c; }
+		for(uint32_t k = 0; k < NP_BINS; k++) { const uint32_t c = hist[k]; hist[k] = run; hist[NP_BINS + k] = run; run += c; }
 	}
 }
 
@@ -64,7 +77,8 @@ __global__ void bucketScatterKernel(PairRef pr, uint32_t n, uint32_t* __restrict
 	perm[slot] = i;
 }
 
-// One lane per pair (in bucket order).  out: n x 4 contacts x 2 float4.
+// One lane per pair (in bucket order) of slots [0, n) of perm; convex-core pairs
+// are left to generateConvexCoreKernel.  out: n x 4 contacts x 2 float4.
 // manifolds: per pair, the persistent manifold read and updated (null: fresh caches).
 __global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t* __restrict__ perm, uint32_t n, float contactDistance,
                                                       float toleranceLength, float4* __restrict__ out, uint32_t* __restrict__ counts,
@@ -74,6 +88,7 @@ __global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t
 	if(k >= n) return;
 	const uint32_t i = perm[k];
 	int ta = pr.type0[i], tb = pr.type1[i];
+	if(convexCorePair(ta, tb)) return;
 	float ga[4], gb[4];
 #pragma unroll
 	for(int c = 0; c < 4; c++) { ga[c] = pr.geom0[4 * size_t(i) + c]; gb[c] = pr.geom1[4 * size_t(i) + c]; }
@@ -99,6 +114,39 @@ __global__ void __launch_bounds__(128) generateKernel(PairRef pr, const uint32_t
 		if(swap) nn = neg(nn);
 		o[2 * c] = make_float4(nn.x, nn.y, nn.z, buf.c[c].sep);
 		o[2 * c + 1] = make_float4(buf.c[c].p.x, buf.c[c].p.y, buf.c[c].p.z, 0.0f);
+	}
+}
+// One lane per convex-core pair among slots [begin, end) of perm (the other
+// kinds are skipped): contactPlaneConvexCore / contactConvexCoreConvex with the
+// shapes in the reference's table order and the normals negated when swapped.
+__global__ void __launch_bounds__(128) generateConvexCoreKernel(PairRef pr, const uint32_t* __restrict__ perm, uint32_t begin, uint32_t end,
+                                                                float contactDistance, float4* __restrict__ out, uint32_t* __restrict__ counts)
+{
+	const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= end) return;
+	const uint32_t i = perm[k];
+	int ta = pr.type0[i], tb = pr.type1[i];
+	if(!convexCorePair(ta, tb)) return;
+	const float* ga = pr.geom0 + 4 * size_t(i);
+	const float* gb = pr.geom1 + 4 * size_t(i);
+	Tr pa = loadPose7(pr.pose0 + 7 * size_t(i)), pb = loadPose7(pr.pose1 + 7 * size_t(i));
+	const bool swap = geomType(ta) > geomType(tb);
+	if(swap)
+	{
+		const int t = ta; ta = tb; tb = t;
+		const float* g = ga; ga = gb; gb = g;
+		const Tr t2 = pa; pa = pb; pb = t2;
+	}
+	V3 normal = v3(0.0f, 0.0f, 0.0f), points[cc::MAX_CONTACTS];
+	float dists[cc::MAX_CONTACTS];
+	const uint32_t c = cc::generatePair(ta, ga, tb, gb, pa, pb, contactDistance, normal, points, dists);
+	counts[i] = c;
+	if(swap) normal = neg(normal);
+	float4* o = out + size_t(i) * 8;
+	for(uint32_t j = 0; j < c; j++)
+	{
+		o[2 * j] = make_float4(normal.x, normal.y, normal.z, dists[j]);
+		o[2 * j + 1] = make_float4(points[j].x, points[j].y, points[j].z, 0.0f);
 	}
 }
 } // namespace np
@@ -131,9 +179,18 @@ static NpWorkspace* npWorkspace()
 
 using namespace gbpx;
 
+// a shape type this narrowphase generates for: PxGeometryType 0..3, or 4 (convex
+// core) with a PxConvexCore::Type 0..5 in bits 8..15
+static bool validShapeType(int t)
+{
+	const uint32_t u = uint32_t(t);
+	if(u <= 3u) return true;
+	return (u & 0xffu) == 4u && (u >> 8) < uint32_t(cc::CORE_COUNT);
+}
+
 // PxGenerateContacts over nbPairs pairs (host arrays, fresh caches).  Layout:
-// geometry type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box) and 4
-// floats per shape, poses 7 floats, contacts 8 floats (normal, separation,
+// geometry type (PxGeometryType: 0 sphere, 1 plane, 2 capsule, 3 box, 4 convex
+// core with its core type in bits 8..15) and 4 floats per shape, poses 7 floats, contacts 8 floats (normal, separation,
 // point, 0) with maxPerPair slots per pair.  Returns GBPX_ERR_CAPACITY if a
 // pair produced more than maxPerPair contacts (counts are still exact).
 static int generateContactsHost(const int* type0, const float* geom0, const int* type1, const float* geom1, const float* pose0, const float* pose1,
@@ -143,13 +200,17 @@ static int generateContactsHost(const int* type0, const float* geom0, const int*
 	if(!nbPairs) return GBPX_OK;
 	if(!type0 || !geom0 || !type1 || !geom1 || !pose0 || !pose1 || !outContacts || !outCounts || !maxPerPair) return GBPX_ERR_INVALID;
 	if(!(contactDistance > 0.0f) || !(toleranceLength > 0.0f)) return GBPX_ERR_INVALID;
+	uint32_t nbConvexCore = 0;
 	for(uint32_t i = 0; i < nbPairs; i++)
-		if(uint32_t(type0[i]) > 3u || uint32_t(type1[i]) > 3u) return GBPX_ERR_INVALID;
+	{
+		if(!validShapeType(type0[i]) || !validShapeType(type1[i])) return GBPX_ERR_INVALID;
+		if((type0[i] & 0xff) == 4 || (type1[i] & 0xff) == 4) nbConvexCore++;
+	}
 	NpWorkspace* ws = npWorkspace();
 	if(!ws) return GBPX_ERR_CUDA;
 	const size_t n = nbPairs;
 	if(ws->t0.reserve(n) || ws->t1.reserve(n) || ws->g0.reserve(4 * n) || ws->g1.reserve(4 * n) || ws->p0.reserve(7 * n) ||
-	   ws->p1.reserve(7 * n) || ws->hist.reserve(32) || ws->perm.reserve(n) || ws->counts.reserve(n) || ws->out.reserve(8 * n) ||
+	   ws->p1.reserve(7 * n) || ws->hist.reserve(2 * np::NP_BINS) || ws->perm.reserve(n) || ws->counts.reserve(n) || ws->out.reserve(8 * n) ||
 	   ws->hOut.reserve(8 * n) || ws->hCounts.reserve(n) || (manifolds && ws->manifolds.reserve(n)))
 		return GBPX_ERR_NOMEM;
 	cudaStream_t s = ws->stream;
@@ -159,15 +220,21 @@ static int generateContactsHost(const int* type0, const float* geom0, const int*
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->g1.ptr, geom1, n * 16, cudaMemcpyHostToDevice, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->p0.ptr, pose0, n * 28, cudaMemcpyHostToDevice, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->p1.ptr, pose1, n * 28, cudaMemcpyHostToDevice, s));
-	GBPX_CUDA_TRY(cudaMemsetAsync(ws->hist.ptr, 0, 32 * 4, s));
+	GBPX_CUDA_TRY(cudaMemsetAsync(ws->hist.ptr, 0, 2 * np::NP_BINS * 4, s));
 	np::PairRef pr = {ws->t0.ptr, ws->g0.ptr, ws->t1.ptr, ws->g1.ptr, ws->p0.ptr, ws->p1.ptr};
 	const uint32_t blocks = divUp(n, 256);
 	np::bucketCountKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr);
 	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(ws->hist.ptr);
-	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr + 16, ws->perm.ptr);
+	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, ws->hist.ptr + np::NP_BINS, ws->perm.ptr);
 	if(manifolds) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->manifolds.ptr, manifolds, n * sizeof(np::ManifoldRecord), cudaMemcpyHostToDevice, s));
-	np::generateKernel<<<divUp(n, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPairs, contactDistance, toleranceLength, ws->out.ptr, ws->counts.ptr,
-	                                                 manifolds ? ws->manifolds.ptr : nullptr);
+	// the convex-core pairs occupy the last nbConvexCore slots of the bucket order
+	const uint32_t nbPrimitive = nbPairs - nbConvexCore;
+	if(nbPrimitive)
+		np::generateKernel<<<divUp(nbPrimitive, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPrimitive, contactDistance, toleranceLength, ws->out.ptr,
+		                                                           ws->counts.ptr, manifolds ? ws->manifolds.ptr : nullptr);
+	if(nbConvexCore)
+		np::generateConvexCoreKernel<<<divUp(nbConvexCore, 128), 128, 0, s>>>(pr, ws->perm.ptr, nbPrimitive, nbPairs, contactDistance, ws->out.ptr,
+		                                                                       ws->counts.ptr);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	if(manifolds) GBPX_CUDA_TRY(cudaMemcpyAsync(manifolds, ws->manifolds.ptr, n * sizeof(np::ManifoldRecord), cudaMemcpyDeviceToHost, s));
 	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->hCounts.ptr, ws->counts.ptr, n * 4, cudaMemcpyDeviceToHost, s));
@@ -212,12 +279,12 @@ GBPX_API int gbpx_generate_contacts_cached(const int* type0, const float* geom0,
 
 // ------------------------------------------------------------------ no-allocation variant
 // The same narrowphase over caller-owned device arrays, with its bucketing
-// scratch (16 bin counters, 16 bin cursors and the pair permutation) in a
+// scratch (the bin counters, the bin cursors and the pair permutation) in a
 // fixed file-scope device array instead of per-call allocations.
 namespace gbpx
 {
 constexpr uint32_t NP_NOALLOC_MAX_PAIRS = 262144;                  // 1 MiB of permutation
-constexpr uint32_t NP_NOALLOC_SCRATCH_WORDS = 32 + NP_NOALLOC_MAX_PAIRS;
+constexpr uint32_t NP_NOALLOC_SCRATCH_WORDS = 2 * np::NP_BINS + NP_NOALLOC_MAX_PAIRS;
 static __device__ __align__(256) uint32_t gNpNoAllocScratch[NP_NOALLOC_SCRATCH_WORDS];
 constexpr int NP_NOALLOC_MAX_DEVICES = 64;
 
@@ -254,9 +321,9 @@ static int npNoAllocScratch(uint32_t** out)
 // PxGenerateContacts over nbPairs pairs held in device memory (layouts as
 // gbpx_generate_contacts; contacts: 4 slots of 8 floats per pair, 16-byte
 // aligned), enqueued on `stream` (a cudaStream_t, NULL for the default
-// stream), with fresh caches.  Geometry types must be 0..3 (sphere, plane,
-// capsule, box): the device arrays are not inspected on the host, and other
-// values give undefined contacts.  Allocates nothing: the bucketing scratch is
+// stream), with fresh caches.  Geometry types must be those of
+// gbpx_generate_contacts (sphere, plane, capsule, box, convex core): the device
+// arrays are not inspected on the host, and other values give undefined contacts.  Allocates nothing: the bucketing scratch is
 // a fixed 1 MiB device array, so nbPairs is limited to 262144
 // (GBPX_ERR_CAPACITY above).  The scratch is shared by all calls on a device:
 // calls that may overlap (other streams, other host threads) race and must be
@@ -277,14 +344,19 @@ GBPX_API int gbpx_generate_contacts_device_noalloc(const int* dType0, const floa
 	if(rc) return rc;
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	// the bin counters start at zero; the cursors and the permutation are fully rewritten
-	GBPX_CUDA_TRY(cudaMemsetAsync(scratch, 0, 32 * 4, s));
+	GBPX_CUDA_TRY(cudaMemsetAsync(scratch, 0, 2 * np::NP_BINS * 4, s));
 	np::PairRef pr = {dType0, dGeom0, dType1, dGeom1, dPose0, dPose1};
 	const uint32_t blocks = divUp(nbPairs, 256);
+	uint32_t* perm = scratch + 2 * np::NP_BINS;
 	np::bucketCountKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch);
 	np::bucketOffsetsKernel<<<1, 32, 0, s>>>(scratch);
-	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch + 16, scratch + 32);
-	np::generateKernel<<<divUp(nbPairs, 128), 128, 0, s>>>(pr, scratch + 32, nbPairs, contactDistance, toleranceLength,
+	np::bucketScatterKernel<<<blocks, 256, 0, s>>>(pr, nbPairs, scratch + np::NP_BINS, perm);
+	// the split between the kinds is not known on the host: both generators cover
+	// every slot and skip the other's pairs
+	np::generateKernel<<<divUp(nbPairs, 128), 128, 0, s>>>(pr, perm, nbPairs, contactDistance, toleranceLength,
 	                                                        reinterpret_cast<float4*>(dOutContacts), dOutCounts, nullptr);
+	np::generateConvexCoreKernel<<<divUp(nbPairs, 128), 128, 0, s>>>(pr, perm, 0, nbPairs, contactDistance,
+	                                                                  reinterpret_cast<float4*>(dOutContacts), dOutCounts);
 	GBPX_CUDA_TRY(cudaGetLastError());
 	return GBPX_OK;
 }

@@ -219,3 +219,137 @@ def aabb_stress_frames(seed=3, n=1_000_000, frames=10, extent=1000.0, move_frac=
         bounds[moved, :3] += d
         bounds[moved, 3:] += d
         yield dict(created=empty, updated=np.sort(moved), removed=empty, bounds=bounds, groups=groups, distances=dist, capacity=n)
+
+
+CONVEX_CORE = 4   # PxGeometryType::eCONVEXCORE
+CORE_NAMES = ("point", "segment", "box", "ellipsoid", "cylinder", "cone")   # PxConvexCore::Type
+
+
+def convex_core_type(core):
+    """The shape type of a PxConvexCoreGeometry in the narrowphase's encoding:
+    PxGeometryType 4 in the low byte, the PxConvexCore::Type in bits 8..15."""
+    return CONVEX_CORE | (int(core) << 8)
+
+
+def convex_core_params(rng, core):
+    """Core floats and margin (4 floats) of a random convex core of the given type,
+    with flat / degenerate variants (zero-margin boxes, disk and needle
+    ellipsoids, flat cylinders) in the mix."""
+    g = np.zeros(4, np.float32)
+    if core == 0:
+        g[3] = rng.uniform(0.15, 0.6)
+    elif core == 1:
+        g[0] = rng.uniform(0.2, 1.5)
+        g[3] = rng.uniform(0.05, 0.3)
+    elif core == 2:
+        g[:3] = rng.uniform(0.2, 1.5, size=3)
+        if rng.random() < 0.1:
+            g[rng.integers(3)] = 0.0          # a flat box (a rectangle grown by the margin)
+        g[3] = 0.0 if rng.random() < 0.4 else rng.uniform(0.01, 0.1)
+    elif core == 3:
+        g[:3] = rng.uniform(0.1, 0.8, size=3)
+        u = rng.random()
+        if u < 0.15:
+            g[rng.integers(3)] = 0.0          # a disk
+        elif u < 0.25:
+            keep = rng.integers(3)
+            g[[k for k in range(3) if k != keep]] = 0.0   # a needle
+        g[3] = 0.0 if rng.random() < 0.5 else rng.uniform(0.01, 0.05)
+    else:
+        g[0] = rng.uniform(0.2, 1.5) if rng.random() > 0.1 else 0.0
+        g[1] = rng.uniform(0.1, 0.6)
+        g[3] = 0.0 if rng.random() < 0.5 else rng.uniform(0.01, 0.05)
+    return g
+
+
+def convex_core_radius(core, g):
+    """Radius of a sphere about the shape's origin that holds the convex core."""
+    if core == 0:
+        r = 0.0
+    elif core == 1:
+        r = 0.5 * g[0]
+    elif core == 2:
+        r = 0.5 * float(np.linalg.norm(g[:3]))
+    elif core == 3:
+        r = float(g[:3].max())
+    else:
+        r = float(np.hypot(0.5 * g[0], g[1]))
+    return r + float(g[3])
+
+
+def _axis_aligned_quat(rng, jitter):
+    """One of the 24 rotations that map axes to axes, turned by up to `jitter` radians."""
+    base = [np.array([0, 0, 0, 1.0]), np.array([1.0, 0, 0, 0]), np.array([0, 1.0, 0, 0]), np.array([0, 0, 1.0, 0])]
+    h = np.sqrt(0.5)
+    base += [np.array(v) for v in ([h, 0, 0, h], [0, h, 0, h], [0, 0, h, h], [-h, 0, 0, h], [0, -h, 0, h], [0, 0, -h, h])]
+    q = base[rng.integers(len(base))]
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    a = rng.uniform(-jitter, jitter)
+    d = np.concatenate([ax * np.sin(a / 2), [np.cos(a / 2)]])
+    # quaternion product d * q, (x, y, z, w)
+    x1, y1, z1, w1 = d
+    x2, y2, z2, w2 = q
+    r = np.array([w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2, w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2,
+                  w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2, w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2])
+    return (r / np.linalg.norm(r)).astype(np.float32)
+
+
+def convex_core_pairs(seed, n, aligned_frac=0.4):
+    """Near-contact pairs with at least one convex core (PxConvexCoreGeometry of
+    every core type) against spheres, planes, capsules, boxes and other convex
+    cores, in both argument orders.  `aligned_frac` of the pairs have axis-aligned
+    orientations (within 0.02 rad) and are offset along an axis, so that the
+    contact faces of the cores (and the face clipping) are exercised.  Returns
+    the narrowphase's pair arrays (type0, geom0, type1, geom1, pose0, pose1)."""
+    rng = np.random.default_rng(seed)
+    t0 = np.zeros(n, np.int32)
+    t1 = np.zeros(n, np.int32)
+    g0 = np.zeros((n, 4), np.float32)
+    g1 = np.zeros((n, 4), np.float32)
+    p0 = np.zeros((n, 7), np.float32)
+    p1 = np.zeros((n, 7), np.float32)
+    prim = {0: lambda: np.array([rng.uniform(0.25, 1.0), 0, 0, 0], np.float32),
+            2: lambda: np.array([rng.uniform(0.2, 0.5), rng.uniform(0.25, 1.0), 0, 0], np.float32),
+            3: lambda: np.concatenate([rng.uniform(0.25, 1.0, size=3), [0]]).astype(np.float32)}
+    prim_radius = {0: lambda g: g[0], 2: lambda g: g[0] + g[1], 3: lambda g: float(np.linalg.norm(g[:3]))}
+    for i in range(n):
+        core = int(rng.integers(6))
+        tc, gc, rc = convex_core_type(core), convex_core_params(rng, core), 0.0
+        rc = convex_core_radius(core, gc)
+        other = int(rng.integers(5))   # 0 sphere, 1 plane, 2 capsule, 3 box, 4 another convex core
+        if other == 4:
+            core2 = int(rng.integers(6))
+            to, go = convex_core_type(core2), convex_core_params(rng, core2)
+            ro = convex_core_radius(core2, go)
+        elif other == 1:
+            to, go, ro = 1, np.zeros(4, np.float32), 0.0
+        else:
+            to = other
+            go = prim[other]()
+            ro = prim_radius[other](go)
+        aligned = rng.random() < aligned_frac
+        qc = _axis_aligned_quat(rng, 0.02) if aligned else random_quat(rng, 1)[0]
+        qo = _axis_aligned_quat(rng, 0.02) if aligned else random_quat(rng, 1)[0]
+        c0 = rng.uniform(-5, 5, size=3).astype(np.float32)
+        if other == 1:
+            po = plane_pose_y_up()
+            po[4:] = [rng.uniform(-3, 3), 0.0, rng.uniform(-3, 3)]
+            pc = np.concatenate([qc, [po[4] + rng.uniform(-1, 1), rng.uniform(-0.3, 1.0) * rc, po[6] + rng.uniform(-1, 1)]])
+        else:
+            if aligned:
+                d = np.zeros(3)
+                d[rng.integers(3)] = rng.choice([-1.0, 1.0])
+                d += rng.normal(size=3) * 0.05
+            else:
+                d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            dist = (rc + ro) * rng.uniform(0.4, 1.05)
+            pc = np.concatenate([qc, c0])
+            po = np.concatenate([qo, c0 + (d * dist).astype(np.float32)])
+        first_core = rng.random() < 0.5
+        if first_core:
+            t0[i], g0[i], p0[i], t1[i], g1[i], p1[i] = tc, gc, pc, to, go, po
+        else:
+            t0[i], g0[i], p0[i], t1[i], g1[i], p1[i] = to, go, po, tc, gc, pc
+    return dict(type0=t0, geom0=g0, type1=t1, geom1=g1, pose0=p0.astype(np.float32), pose1=p1.astype(np.float32))

@@ -1,8 +1,9 @@
 """Pair-by-pair comparison of contact sets against the reference's
 PxGenerateContacts (fresh caches), with the tolerance the GB300 build claims:
-for every pair kind (sphere, plane, capsule, box in all combinations, including
-the GJK/EPA paths of capsule-box and edge-edge box-box) the same contact count
-and every value (normal, separation, point) within 1e-5.  The oracle and the
+for every pair kind (sphere, plane, capsule, box and convex cores in all
+combinations, including the GJK/EPA paths of capsule-box, edge-edge box-box
+and the convex cores) the same contact count and every value (normal,
+separation, point) within 1e-5.  The oracle and the
 device code reproduce the reference's evaluation order, including its
 approximate reciprocal in box-box edge clipping, so the observed difference is
 0; the 1e-5 bound is the claim.
@@ -10,12 +11,20 @@ approximate reciprocal in box-box edge clipping, so the observed difference is
 import numpy as np
 
 NAMES = {0: "sphere", 1: "plane", 2: "capsule", 3: "box"}
+CORES = ("point", "segment", "box", "ellipsoid", "cylinder", "cone")   # PxConvexCore::Type
 CONTACT_TOL = 1e-5
 
 
+def shape_name(t):
+    t = int(t)
+    if t & 0xff == 4:   # convex core: PxConvexCore::Type in bits 8..15
+        return "convex_" + CORES[t >> 8]
+    return NAMES[t]
+
+
 def kind(t0, t1):
-    a, b = sorted((int(t0), int(t1)))
-    return NAMES[a] + "-" + NAMES[b]
+    a, b = sorted((int(t0), int(t1)), key=lambda t: (t & 0xff, t >> 8))
+    return shape_name(a) + "-" + shape_name(b)
 
 
 def unpack(counts, packed):

@@ -20,6 +20,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from oracle_libs import CachedContacts, CpuBroadPhase, PersistentScenes, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
 from scenarios import bp_frames, moving_pairs, np_pairs, pile_scenes, random_scene  # noqa: E402
+from physx_gb300.workloads import convex_core_pairs  # noqa: E402
 
 BP_CASES = [
     # name, seed, boxes, frames, extent
@@ -46,14 +47,17 @@ def make_bp():
 
 
 NP_CASES = [
-    # name, seed, pairs: near-contact pairs of every sphere/plane/capsule/box combination
-    ("np_mixed", 17, 3000),
+    # name, seed, pairs, generator
+    # near-contact pairs of every sphere/plane/capsule/box combination
+    ("np_mixed", 17, 3000, np_pairs),
+    # pairs with a convex core (PxConvexCoreGeometry, every core type) against every shape type
+    ("np_convex_core", 19, 3000, lambda seed, n: convex_core_pairs(seed, n, aligned_frac=0.6)),
 ]
 
 
 def make_np():
-    for name, seed, n in NP_CASES:
-        pairs = np_pairs(seed, n)
+    for name, seed, n, gen in NP_CASES:
+        pairs = gen(seed, n)
         cnt, out = run_contacts("pxref", pairs, max_per_pair=8)
         packed = np.concatenate([out[i, :cnt[i]] for i in range(n) if cnt[i]]) if cnt.sum() else np.zeros((0, 8), np.float32)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), counts=cnt, contacts=packed.astype(np.float32),

@@ -3,8 +3,8 @@
 // way the reference's immediate-mode snippet keeps its pair caches
 // (SnippetImmediateMode.cpp:657-676).  Used by tests/test_immediate_dropin_gpu.py.
 //
-// stdin (binary): nbPairs, nbFrames (u32); per pair type0, type1 (i32) and
-// geometry (4 + 4 floats); per frame the poses of both shapes (7 + 7 floats per
+// stdin (binary): nbPairs, nbFrames (u32); per pair type0, type1 (i32; a
+// convex core is 4 | its PxConvexCore::Type << 8) and geometry (4 + 4 floats); per frame the poses of both shapes (7 + 7 floats per
 // pair, PxTransform).
 // stdout (binary): per frame per pair the contact count (u32) and per contact
 // normal xyz, separation, point xyz, 0 (8 floats).
@@ -27,14 +27,21 @@ template <typename T> void readAll(T* p, size_t n)
 
 struct Shape
 {
-	union { PxGeometry any; PxSphereGeometry sphere; PxCapsuleGeometry capsule; PxBoxGeometry box; PxPlaneGeometry plane; };
+	union { PxGeometry any; PxSphereGeometry sphere; PxCapsuleGeometry capsule; PxBoxGeometry box; PxPlaneGeometry plane; PxConvexCoreGeometry convex; };
 	Shape() { memset(this, 0, sizeof(*this)); }
 	void set(int type, const float* g)
 	{
-		any.mType = type;
+		any.mType = type & 0xff;
 		if(type == 0) sphere.radius = g[0];
 		if(type == 2) { capsule.radius = g[0]; capsule.halfHeight = g[1]; }
 		if(type == 3) box.halfExtents = PxVec3{g[0], g[1], g[2]};
+		if((type & 0xff) == 4)
+		{
+			// PxConvexCoreGeometry: core type in bits 8..15 of the input type, core floats, margin
+			convex.mCoreType = type >> 8;
+			memcpy(convex.mCore, g, 3 * sizeof(float));
+			convex.mMargin = g[3];
+		}
 	}
 };
 

@@ -8,6 +8,7 @@
 #include "geometry/PxCapsuleGeometry.h"
 #include "geometry/PxBoxGeometry.h"
 #include "geometry/PxPlaneGeometry.h"
+#include "geometry/PxConvexCoreGeometry.h"
 #include "geomutils/PxContactPoint.h"
 #include "collision/PxCollisionDefs.h"
 #include "solver/PxSolverDefs.h"
@@ -19,12 +20,33 @@ using namespace gbpx_px;
 #endif
 #include <cstdio>
 #include <cstddef>
+#include <cstring>
 #define S(T) printf("\"%s\": %zu,\n", #T, sizeof(T))
 #define O(T, f) printf("\"%s.%s\": %zu,\n", #T, #f, offsetof(T, f))
 int main(){
  printf("{\n");
  S(PxTransform); S(PxGeometry); S(PxSphereGeometry); S(PxCapsuleGeometry); S(PxBoxGeometry); S(PxPlaneGeometry);
  O(PxSphereGeometry, radius); O(PxCapsuleGeometry, radius); O(PxCapsuleGeometry, halfHeight); O(PxBoxGeometry, halfExtents);
+ S(PxConvexCoreGeometry);
+#ifdef PROBE_REFERENCE
+ {
+	// the members are private: locate them in a geometry with known values
+	const PxConvexCoreGeometry g(PxConvexCore::Cylinder(1.5f, 0.25f), 0.125f);
+	const char* b = reinterpret_cast<const char*>(&g);
+	const size_t core = static_cast<const char*>(g.getCoreData()) - b;
+	size_t type = 0, margin = 0;
+	for(size_t o = 8; o + 4 <= sizeof(g); o += 4)
+	{
+		float f; int i;
+		memcpy(&f, b + o, 4); memcpy(&i, b + o, 4);
+		if(o < core && i == int(PxConvexCore::eCYLINDER)) type = o;
+		if(o >= core + PxConvexCoreGeometry::MAX_CORE_SIZE && f == 0.125f) margin = o;
+	}
+	printf("\"PxConvexCoreGeometry.mCoreType\": %zu,\n\"PxConvexCoreGeometry.mCore\": %zu,\n\"PxConvexCoreGeometry.mMargin\": %zu,\n", type, core, margin);
+ }
+#else
+ O(PxConvexCoreGeometry, mCoreType); O(PxConvexCoreGeometry, mCore); O(PxConvexCoreGeometry, mMargin);
+#endif
  S(PxContactPoint); O(PxContactPoint, normal); O(PxContactPoint, separation); O(PxContactPoint, point); O(PxContactPoint, maxImpulse);
  O(PxContactPoint, targetVel); O(PxContactPoint, staticFriction); O(PxContactPoint, materialFlags); O(PxContactPoint, internalFaceIndex1);
  O(PxContactPoint, dynamicFriction); O(PxContactPoint, restitution); O(PxContactPoint, damping);

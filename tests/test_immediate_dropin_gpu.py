@@ -7,7 +7,8 @@ PxIntegrateSolverBodiesTGS) are linked against this library:
 * tests/immediate_dropin.cpp, one frame with fresh caches, matches the CPU
   oracle's frame on the same scene;
 * tests/immediate_contacts.cpp, PxGenerateContacts with PxCache memory kept
-  between frames, matches the reference's own outputs (pcm_cached.npz);
+  between frames, matches the reference's own outputs (pcm_cached.npz), and
+  with PxConvexCoreGeometry shapes (np_convex_core.npz);
 * tests/immediate_dropin_frames.cpp, frames of one scene in the snippet's
   persistent mode (pair caches and friction data carried from frame to frame),
   matches the oracle's persistent frames step by step."""
@@ -85,6 +86,35 @@ def test_immediate_cached_contacts_match_reference_golden(cuda_device, tmp_path)
             k += 8 * c
             if c:
                 assert np.abs(got[:, :7] - ref[i][:, :7]).max() <= CONTACT_TOL, (f, i)
+    assert k == len(words)
+
+
+def test_immediate_convex_core_contacts_match_reference_golden(cuda_device, tmp_path):
+    """PxGenerateContacts of libgbpx_immediate.so with PxConvexCoreGeometry shapes
+    (every core type against every shape type, np_convex_core.npz: the
+    reference's own outputs): same counts, every value within the contact
+    tolerance, and no cache memory kept for these pairs."""
+    from contact_compare import CONTACT_TOL, unpack
+    from test_oracle_golden import GOLDEN, load_np_fixture
+    exe = _build(str(tmp_path), "immediate_contacts")
+    pairs, rc, rpacked, _, _ = load_np_fixture(os.path.join(GOLDEN, "np_convex_core.npz"))
+    n = len(pairs["type0"])
+    geom = np.concatenate([np.asarray(pairs["geom0"], np.float32), np.asarray(pairs["geom1"], np.float32)], 1)
+    blob = [np.array([n, 1], np.uint32).tobytes(), np.asarray(pairs["type0"], np.int32).tobytes(),
+            np.asarray(pairs["type1"], np.int32).tobytes(), np.ascontiguousarray(geom).tobytes(),
+            np.ascontiguousarray(pairs["pose0"], np.float32).tobytes(), np.ascontiguousarray(pairs["pose1"], np.float32).tobytes()]
+    out = subprocess.run([exe], input=b"".join(blob), capture_output=True, check=True).stdout
+    words = np.frombuffer(out, np.uint32)
+    ref = unpack(rc, rpacked)
+    k = 0
+    for i in range(n):
+        c = int(words[k])
+        k += 1
+        assert c == rc[i], i
+        got = words[k:k + 8 * c].view(np.float32).reshape(c, 8)
+        k += 8 * c
+        if c:
+            assert np.abs(got[:, :7] - ref[i][:, :7]).max() <= CONTACT_TOL, i
     assert k == len(words)
 
 

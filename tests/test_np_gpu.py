@@ -7,6 +7,7 @@ from contact_compare import assert_report, compare, unpack
 from oracle_libs import run_contacts
 from scenarios import np_pairs
 from test_oracle_golden import NP_FIXTURES, load_np_fixture
+from physx_gb300.workloads import convex_core_pairs, convex_core_type
 
 pytestmark = pytest.mark.gpu
 
@@ -29,6 +30,72 @@ def test_contacts_match_oracle(cuda_device, seed, n):
     assert np.array_equal(gc, oc)
     for i in np.flatnonzero(oc):
         assert np.abs(go[i, :oc[i], :7] - oo[i, :oc[i], :7]).max() <= 1e-6, i
+
+
+def _exact(gc, go, oc, oo):
+    assert np.array_equal(gc, oc)
+    for i in np.flatnonzero(oc):
+        assert np.array_equal(go[i, :oc[i], :7], oo[i, :oc[i], :7]), i
+
+
+@pytest.mark.parametrize("seed,n", [(103, 20000), (104, 3000)])
+def test_convex_core_contacts_match_oracle(cuda_device, seed, n):
+    """Convex cores of every type against every shape type, both argument orders:
+    the same counts and bit-identical normals, separations and points."""
+    from physx_gb300.contacts import generate_contacts
+    pairs = convex_core_pairs(seed, n, aligned_frac=0.6)
+    gc, go = generate_contacts(pairs, max_per_pair=4)
+    oc, oo = run_contacts("orc", pairs, max_per_pair=4)
+    assert (oc > 1).sum() > n // 20   # face contacts (2-4 points) are in the mix
+    _exact(gc, go, oc, oo)
+
+
+def test_mixed_primitive_and_convex_core_batch(cuda_device):
+    """One batch with primitive and convex-core pairs interleaved: each pair's
+    contacts come from its own generator (the buckets split the batch)."""
+    from physx_gb300.contacts import generate_contacts
+    a, b = np_pairs(105, 4000), convex_core_pairs(106, 4000)
+    order = np.random.default_rng(107).permutation(8000)
+    pairs = {k: np.concatenate([a[k], b[k]])[order] for k in a}
+    gc, go = generate_contacts(pairs, max_per_pair=4)
+    oc, oo = run_contacts("orc", pairs, max_per_pair=4)
+    _exact(gc, go, oc, oo)
+
+
+def test_convex_core_edge_cases(cuda_device):
+    from physx_gb300 import GbpxError
+    from physx_gb300.contacts import generate_contacts
+    ident = np.array([0, 0, 0, 1, 0, 0, 0], np.float32)
+    up = np.array([0, 0, 0, 1, 0, 0.95, 0], np.float32)
+    s = np.float32(np.sqrt(0.5))
+    plane = np.array([0, 0, s, s, 0, 0, 0], np.float32)
+    cases = [
+        # coincident point cores (spheres): EPA on a degenerate polytope
+        (convex_core_type(0), [0, 0, 0, 0.5], ident, convex_core_type(0), [0, 0, 0, 0.5], ident),
+        # a zero-size box core with no margin against a plane, touching
+        (convex_core_type(2), [0, 0, 0, 0], ident, 1, [0, 0, 0, 0], plane),
+        # a flat box (a rectangle) resting on a box core: face contact
+        (convex_core_type(2), [1, 0, 1, 0.05], up, convex_core_type(2), [2, 1.8, 2, 0], ident),
+        # a cylinder on its cap, a cone on its base against a plane
+        (1, [0, 0, 0, 0], plane, convex_core_type(4), [1.0, 0.5, 0, 0], np.array([0, 0, s, s, 0, 0.49, 0], np.float32)),
+        (1, [0, 0, 0, 0], plane, convex_core_type(5), [1.0, 0.5, 0, 0], np.array([0, 0, s, s, 0, 0.51, 0], np.float32)),
+        # far apart: no contact
+        (convex_core_type(3), [0.5, 0.2, 0.3, 0], ident, 3, [0.5, 0.5, 0.5, 0], np.array([0, 0, 0, 1, 9, 0, 0], np.float32)),
+    ]
+    pairs = dict(type0=np.array([c[0] for c in cases], np.int32), geom0=np.array([c[1] for c in cases], np.float32),
+                 type1=np.array([c[3] for c in cases], np.int32), geom1=np.array([c[4] for c in cases], np.float32),
+                 pose0=np.stack([c[2] for c in cases]), pose1=np.stack([c[5] for c in cases]))
+    gc, go = generate_contacts(pairs, max_per_pair=4)
+    oc, oo = run_contacts("orc", pairs, max_per_pair=4)
+    _exact(gc, go, oc, oo)
+    assert gc[-1] == 0 and gc[2] >= 2 and gc[3] == 4
+    # an unknown core type and a core type on a primitive are rejected
+    for bad in (convex_core_type(6), 3 | (2 << 8)):
+        b = dict(pairs)
+        b["type0"] = pairs["type0"].copy()
+        b["type0"][0] = bad
+        with pytest.raises(GbpxError):
+            generate_contacts(b)
 
 
 def test_contacts_edge_cases(cuda_device):

@@ -73,8 +73,15 @@ def test_oracle_contacts_match_reference_golden(path):
     rep = compare(pairs, rc, unpack(rc, rpacked), oc, [oo[i, :oc[i]] for i in range(len(oc))])
     assert_report(rep)
     # every pair kind, including the GJK/EPA paths, is reproduced bit for bit
-    for k in ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule",
-              "capsule-box", "box-box"):
+    if "convex" in os.path.basename(path):
+        kinds = [k for k in rep if "convex_" in k]
+        for core in ("point", "segment", "box", "ellipsoid", "cylinder", "cone"):
+            for other in ("sphere", "plane", "capsule", "box", "convex_point"):
+                assert any(k in ("%s-convex_%s" % (other, core), "convex_%s-%s" % (core, other)) for k in kinds), (core, other)
+    else:
+        kinds = ("sphere-sphere", "sphere-plane", "sphere-capsule", "sphere-box", "plane-capsule", "plane-box", "capsule-capsule",
+                 "capsule-box", "box-box")
+    for k in kinds:
         assert rep[k]["maxdiff"] == 0.0, (k, rep[k])
 
 

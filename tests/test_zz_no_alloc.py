@@ -78,6 +78,18 @@ def test_noalloc_matches_allocating_entry_point_and_oracle_twice(cuda_device):
         _same(cnt, out, orc_cnt, orc_out)
 
 
+def test_noalloc_convex_core_pairs(cuda_device):
+    """Primitive and convex-core pairs in one device batch: the host does not know
+    the split, both generators cover the batch and skip each other's pairs."""
+    from physx_gb300.workloads import convex_core_pairs
+    a, b = np_pairs(93, 2000), convex_core_pairs(94, 2000)
+    order = np.random.default_rng(95).permutation(4000)
+    pairs = {k: np.concatenate([a[k], b[k]])[order] for k in a}
+    orc_cnt, orc_out = run_contacts("orc", pairs, max_per_pair=4)
+    cnt, out = _run_device(pairs)
+    _same(cnt, out, orc_cnt, orc_out)
+
+
 def test_noalloc_on_a_caller_stream(cuda_device):
     import torch
     pairs = np_pairs(93, 4000)
