@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--large-bodies", type=int, default=0,
                     help="block-per-scene threshold of the world's scene stages (0 = autotuned for the scene-size histogram)")
     ap.add_argument("--joint-frames", type=int, default=20)
-    ap.add_argument("--profile-extra", default="", choices=["", "broadphase", "large-scene", "joints"],
+    ap.add_argument("--profile-extra", default="", choices=["", "broadphase", "large-scene", "joints", "convex-core"],
                     help="only run one frame of this side workload inside a profiler range and exit")
     ap.add_argument("--profile-step", type=int, default=0,
                     help="only build the state (pre-roll, autotune, warm-up), then run this many un-captured steps inside a "
@@ -395,6 +395,81 @@ def bench_joints(frames, cpu_frames):
                                   sample="%d frame(s) of the same state, oracle restatement, one thread" % cpu_frames))
 
 
+def convex_core_workload(reps=8, unique=32768):
+    """Convex-core contact pairs (every core type against every shape type, 60 %
+    axis-aligned for face contacts): `unique` seeded pairs repeated `reps` times
+    (262,144 pairs, the no-allocation entry point's limit)."""
+    import numpy as np
+    from physx_gb300.workloads import convex_core_pairs
+    base = convex_core_pairs(7, unique, aligned_frac=0.6)
+    return {k: np.ascontiguousarray(np.concatenate([v] * reps)) for k, v in base.items()}
+
+
+def bench_convex_core(iters, cpu_pairs):
+    """Convex-core contact generation (PxGenerateContacts for PxConvexCoreGeometry
+    pairs): device-resident through gbpx_generate_contacts_device_noalloc on the
+    caller's device arrays (CUDA events on the launching stream, L2 flushed
+    before every timed call), end to end through gbpx_generate_contacts with host
+    arrays in and contacts out, and the oracle on one host thread."""
+    import ctypes
+    import numpy as np
+    import torch
+    import physx_gb300
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import run_contacts
+    from physx_gb300.contacts import generate_contacts
+    pairs = convex_core_workload()
+    n = len(pairs["type0"])
+    L = physx_gb300.lib()
+    f = L.gbpx_generate_contacts_device_noalloc
+    f.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    dev = torch.device("cuda:0")
+    keys = ("type0", "geom0", "type1", "geom1", "pose0", "pose1")
+    ins = [torch.from_numpy(pairs[k]).to(dev) for k in keys]
+    out = torch.zeros((n, 4, 8), dtype=torch.float32, device=dev)
+    cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)   # 256 MB, twice the L2
+
+    def launch():
+        physx_gb300.check(f(*[t.data_ptr() for t in ins], n, 0.04, 1.0, out.data_ptr(), cnt.data_ptr(), ctypes.c_void_p(stream.cuda_stream)),
+                          "gbpx_generate_contacts_device_noalloc")
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            launch()
+        times = []
+        for _ in range(iters):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            stream.synchronize()
+            times.append(e0.elapsed_time(e1))
+    dev_ms = float(np.median(times))
+    counts = cnt.cpu().numpy()
+    generate_contacts(pairs, max_per_pair=4)
+    e2e = []
+    for _ in range(iters):
+        t = time.perf_counter()
+        generate_contacts(pairs, max_per_pair=4)
+        e2e.append(time.perf_counter() - t)
+    e2e_ms = 1000.0 * float(np.median(e2e))
+    sample = {k: v[:cpu_pairs] for k, v in pairs.items()}
+    t = time.perf_counter()
+    run_contacts("orc", sample, max_per_pair=4)
+    cpu_s = time.perf_counter() - t
+    return dict(workload="%d convex-core pairs (point / segment / box / ellipsoid / cylinder / cone cores with margins against spheres, "
+                         "planes, capsules, boxes and convex cores; 32768 seeded pairs repeated 8 times)" % n,
+                pairs=n, contacts=int(counts.sum()), pairs_with_contacts=int((counts > 0).sum()), face_pairs=int((counts > 1).sum()),
+                device_ms=dev_ms, value=n / (dev_ms / 1000.0), unit="pairs/s",
+                note="device-resident, 5 kernels per call (bucket count / offsets / scatter, two generators); L2 flushed before each call",
+                e2e=dict(value=n / (e2e_ms / 1000.0), ms=e2e_ms, unit="pairs/s", h2d_bytes=int(n * 96), d2h_bytes=int(n * (4 + 128))),
+                cpu_baseline=dict(value=cpu_pairs / cpu_s, unit="pairs/s", cores=1, kind="port",
+                                  sample="first %d pairs, oracle restatement, one thread" % cpu_pairs))
+
+
 def profile_extra(which):
     """One frame of a side workload inside a profiler range (for ncu
     --profile-from-start off), after untimed warm-up frames."""
@@ -423,6 +498,14 @@ def profile_extra(which):
         physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
         out = s.stats()
         s.release()
+    elif which == "convex-core":
+        from physx_gb300.contacts import generate_contacts
+        pairs = convex_core_workload()
+        generate_contacts(pairs, max_per_pair=4)
+        physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+        cnt, _ = generate_contacts(pairs, max_per_pair=4)
+        physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        out = dict(pairs=len(cnt), contacts=int(cnt.sum()))
     else:
         from physx_gb300.solver import joint_frame as gpu_joint_frame
         fr = joint_workload()
@@ -631,7 +714,8 @@ def main():
     extras = None
     if a.extras:
         extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames),
-                      large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames), joints=bench_joints(a.joint_frames, 5))
+                      large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames), joints=bench_joints(a.joint_frames, 5),
+                      convex_core=bench_convex_core(20, 20000))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],

@@ -5,8 +5,8 @@
 // calls (convex-core pairs keep none).
 //
 // GB300 layout: the batch is bucketed by (type0, type1) with a counting pass
-// (16 bins for the sphere/plane/capsule/box kinds, then 5 for the pairs with a
-// convex core, which come last) so every warp runs a single generator (no
+// (16 bins for the sphere/plane/capsule/box kinds, then the pairs with a convex
+// core by shape and core types, which come last) so every warp runs a single generator (no
 // divergence between pair types); the convex-core pairs run in their own
 // kernel, whose GJK/EPA working set does not weigh on the others' registers.
 // Each lane runs one pair and writes its <= 4 contacts as float4 pairs
@@ -35,17 +35,29 @@ __device__ __forceinline__ Tr loadPose7(const float* p)
 	return t;
 }
 
-constexpr uint32_t NP_BINS = 32;   // 16 primitive kinds, 5 convex-core kinds, unused
+// 16 bins for the primitive kinds, then the convex-core pairs: 24 bins for a
+// primitive (sphere / plane / capsule / box) against each of the 6 core types,
+// 36 for the ordered pairs of core types
+constexpr uint32_t NP_BINS = 16 + 24 + 36;
 
 // a shape type's PxGeometryType (the low byte; a convex core carries its core type above it)
 __device__ __forceinline__ int geomType(int t) { return t & 0xff; }
+__device__ __forceinline__ uint32_t coreType(int t) { const uint32_t c = uint32_t(t) >> 8; return c < 6u ? c : 5u; }
 __device__ __forceinline__ bool convexCorePair(int t0, int t1) { return geomType(t0) == 4 || geomType(t1) == 4; }
 
+// the pair's bucket: the convex-core pairs come after the primitive kinds, split
+// by core types, so that a warp runs one core type's support and face code
 __device__ __forceinline__ uint32_t pairKey(int t0, int t1)
 {
 	const int g0 = geomType(t0), g1 = geomType(t1);
+	if(g0 == 4 && g1 == 4)
+	{
+		const uint32_t c0 = coreType(t0), c1 = coreType(t1);
+		return 40u + (c0 < c1 ? c0 * 6u + c1 : c1 * 6u + c0);
+	}
+	if(g0 == 4) return 16u + uint32_t(g1 & 3) * 6u + coreType(t0);
+	if(g1 == 4) return 16u + uint32_t(g0 & 3) * 6u + coreType(t1);
 	const int a = g0 < g1 ? g0 : g1, b = g0 < g1 ? g1 : g0;
-	if(b == 4) return 16u + uint32_t(a & 7);
 	return uint32_t(((a & 3) << 2) | (b & 3));
 }
 

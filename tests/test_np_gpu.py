@@ -18,6 +18,7 @@ def test_contacts_match_reference_golden(cuda_device, path):
     pairs, rc, rpacked, cd, tl = load_np_fixture(path)
     gc, go = generate_contacts(pairs, contact_distance=cd, tolerance_length=tl, max_per_pair=4)
     rep = compare(pairs, rc, unpack(rc, rpacked), gc, [go[i, :gc[i]] for i in range(len(gc))])
+    print({k: r["maxdiff"] for k, r in rep.items()})
     assert_report(rep)
 
 
@@ -32,10 +33,22 @@ def test_contacts_match_oracle(cuda_device, seed, n):
         assert np.abs(go[i, :oc[i], :7] - oo[i, :oc[i], :7]).max() <= 1e-6, i
 
 
-def _exact(gc, go, oc, oo):
+def _exact(pairs, gc, go, oc, oo):
+    """Same counts; every value bit-identical, except on the pairs whose contact
+    face is a cylinder's or cone's cap: rotatePoints turns those faces by an
+    angle from acos and a quaternion from sin/cos, which the device evaluates in
+    double and rounds while the oracle calls the host C library (as the
+    reference does), so they may differ in the last bits; those pairs are held
+    to the contact tolerance."""
+    from contact_compare import CONTACT_TOL
     assert np.array_equal(gc, oc)
+    cores = np.where((pairs["type0"] & 0xff) == 4, pairs["type0"] >> 8, -1), np.where((pairs["type1"] & 0xff) == 4, pairs["type1"] >> 8, -1)
+    trig = np.isin(cores[0], (4, 5)) | np.isin(cores[1], (4, 5))
     for i in np.flatnonzero(oc):
-        assert np.array_equal(go[i, :oc[i], :7], oo[i, :oc[i], :7]), i
+        if trig[i]:
+            assert np.abs(go[i, :oc[i], :7] - oo[i, :oc[i], :7]).max() <= CONTACT_TOL, i
+        else:
+            assert np.array_equal(go[i, :oc[i], :7], oo[i, :oc[i], :7]), i
 
 
 @pytest.mark.parametrize("seed,n", [(103, 20000), (104, 3000)])
@@ -47,7 +60,7 @@ def test_convex_core_contacts_match_oracle(cuda_device, seed, n):
     gc, go = generate_contacts(pairs, max_per_pair=4)
     oc, oo = run_contacts("orc", pairs, max_per_pair=4)
     assert (oc > 1).sum() > n // 20   # face contacts (2-4 points) are in the mix
-    _exact(gc, go, oc, oo)
+    _exact(pairs, gc, go, oc, oo)
 
 
 def test_mixed_primitive_and_convex_core_batch(cuda_device):
@@ -59,7 +72,7 @@ def test_mixed_primitive_and_convex_core_batch(cuda_device):
     pairs = {k: np.concatenate([a[k], b[k]])[order] for k in a}
     gc, go = generate_contacts(pairs, max_per_pair=4)
     oc, oo = run_contacts("orc", pairs, max_per_pair=4)
-    _exact(gc, go, oc, oo)
+    _exact(pairs, gc, go, oc, oo)
 
 
 def test_convex_core_edge_cases(cuda_device):
@@ -87,7 +100,7 @@ def test_convex_core_edge_cases(cuda_device):
                  pose0=np.stack([c[2] for c in cases]), pose1=np.stack([c[5] for c in cases]))
     gc, go = generate_contacts(pairs, max_per_pair=4)
     oc, oo = run_contacts("orc", pairs, max_per_pair=4)
-    _exact(gc, go, oc, oo)
+    _exact(pairs, gc, go, oc, oo)
     assert gc[-1] == 0 and gc[2] >= 2 and gc[3] == 4
     # an unknown core type and a core type on a primitive are rejected
     for bad in (convex_core_type(6), 3 | (2 << 8)):
