@@ -1275,3 +1275,5 @@ void orc::finishSolverBodies(const std::vector<BodyVel>& vels, const std::vector
 		o[4] = txs[a].p.x; o[5] = txs[a].p.y; o[6] = txs[a].p.z;
 	}
 }
+
+#include "pgs.inl"

@@ -563,6 +563,151 @@ HX PxU32 pxref_tgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose
 }
 
 //////////////////////////////////////////////////////////////////////////////
+// One PGS solve from given contacts, as the immediate-mode snippet's PGS branch
+// runs it (SnippetImmediateMode.cpp:749,761,961,1080-1099): PxConstructSolverBodies /
+// PxConstructStaticSolverBody, PxBatchConstraints (batch != 0; else one header
+// per constraint, typed as PxCreateContactConstraints types them), PxCreateContactConstraints
+// per header, the solver bodies zeroed, PxSolveConstraints,
+// PxIntegrateSolverBodies.  Inputs as pxref_tgs_solve.
+// out*        velocities and poses of the dynamic bodies after integration
+//             (PxSolverBodyData linear / angular velocity, body2World);
+//             headers (start, stride, constraintType) and the constraint order;
+//             outForces: per contact the normal impulse the last velocity
+//             iteration wrote back (PxSolverContactDesc::contactForces).
+HX PxU32 pxref_pgs_solve(const void* rigid, PxU32 nbDyn, const float* staticPose, PxU32 nbStatic,
+	const PxU32* pairA, const PxU32* pairB, PxU32 nbConstraints, const PxU32* contactStart, const PxU32* contactCount,
+	const float* contacts, const float* material, const float* gravity, float dt, PxU32 nbPos, PxU32 nbVel,
+	float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, int batch,
+	float* outVel, float* outPose, PxU32* outHeaderStart, PxU32* outHeaderStride, PxU32* outHeaderType, PxU32* outOrder, float* outForces)
+{
+	ensureFoundation();
+	FrameConstraintAllocator alloc;
+	const PxU32 nbTotal = nbDyn + nbStatic;
+	std::vector<PxSolverBody> bodies(nbTotal);
+	std::vector<PxSolverBodyData> bodyData(nbTotal);
+	const PxRigidBodyData* rb = static_cast<const PxRigidBodyData*>(rigid);
+	const PxVec3 g(gravity[0], gravity[1], gravity[2]);
+	for(PxU32 a = 0; a < nbDyn; a++)
+		PxConstructSolverBodies(&rb[a], &bodyData[a], 1, g, dt, false);
+	for(PxU32 s = 0; s < nbStatic; s++)
+		PxConstructStaticSolverBody(loadPose(staticPose + 7 * s), bodyData[nbDyn + s]);
+
+	PxU32 nbContactsTotal = 0;
+	for(PxU32 i = 0; i < nbConstraints; i++)
+		nbContactsTotal = PxMax(nbContactsTotal, contactStart[i] + contactCount[i]);
+	std::vector<PxContactPoint> points(nbContactsTotal ? nbContactsTotal : 1);
+	for(PxU32 i = 0; i < nbConstraints; i++)
+	{
+		for(PxU32 c = 0; c < contactCount[i]; c++)
+		{
+			const float* s = contacts + 8 * (contactStart[i] + c);
+			PxContactPoint& p = points[contactStart[i] + c];
+			memset(&p, 0, sizeof(p));
+			p.normal = PxVec3(s[0], s[1], s[2]);
+			p.separation = s[3];
+			p.point = PxVec3(s[4], s[5], s[6]);
+			p.maxImpulse = PX_MAX_F32;
+			p.targetVel = PxVec3(0.0f);
+			p.staticFriction = material[3 * i + 0];
+			p.dynamicFriction = material[3 * i + 1];
+			p.restitution = material[3 * i + 2];
+			p.damping = 0.0f;
+			p.materialFlags = 0;
+		}
+	}
+	std::vector<PxReal> forces(nbContactsTotal ? nbContactsTotal : 1, 0.0f);
+
+	std::vector<PxSolverConstraintDesc> descs(nbConstraints), ordered(nbConstraints);
+	std::vector<PxU32> ids(nbConstraints);
+	for(PxU32 i = 0; i < nbConstraints; i++)
+	{
+		PxSolverConstraintDesc& d = descs[i];
+		memset(&d, 0, sizeof(d));
+		d.bodyA = &bodies[pairA[i]];
+		d.bodyB = &bodies[pairB[i]];
+		d.bodyADataIndex = pairA[i];
+		d.bodyBDataIndex = pairB[i];
+		d.linkIndexA = PxSolverConstraintDesc::RIGID_BODY;
+		d.linkIndexB = PxSolverConstraintDesc::RIGID_BODY;
+		ids[i] = i;
+		d.constraint = reinterpret_cast<PxU8*>(&ids[i]);
+		d.constraintType = PxSolverConstraintDesc::eCONTACT_CONSTRAINT;
+	}
+	std::vector<PxConstraintBatchHeader> headers(nbConstraints ? nbConstraints : 1);
+	PxU32 nbHeaders = 0;
+	if(batch)
+		nbHeaders = PxBatchConstraints(descs.data(), nbConstraints, bodies.data(), nbDyn, headers.data(), ordered.data());
+	else
+	{
+		for(PxU32 i = 0; i < nbConstraints; i++)
+		{
+			headers[i].startIndex = i;
+			headers[i].stride = 1;
+			headers[i].constraintType = PxSolverConstraintDesc::eCONTACT_CONSTRAINT;
+			ordered[i] = descs[i];
+		}
+		nbHeaders = nbConstraints;
+	}
+	for(PxU32 i = 0; i < nbConstraints; i++)
+		outOrder[i] = *reinterpret_cast<const PxU32*>(ordered[i].constraint);
+
+	const PxReal invDt = 1.0f / dt;
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		PxConstraintBatchHeader& header = headers[h];
+		PxSolverContactDesc cd[4];
+		for(PxU32 a = 0; a < header.stride; a++)
+		{
+			PxSolverConstraintDesc& desc = ordered[header.startIndex + a];
+			const PxU32 ci = *reinterpret_cast<const PxU32*>(desc.constraint);
+			PxSolverContactDesc& c = cd[a];
+			memset(&c, 0, sizeof(c));
+			c.body0 = desc.bodyA;
+			c.body1 = desc.bodyB;
+			c.data0 = &bodyData[desc.bodyADataIndex];
+			c.data1 = &bodyData[desc.bodyBDataIndex];
+			c.bodyFrame0 = c.data0->body2World;
+			c.bodyFrame1 = c.data1->body2World;
+			c.contactForces = &forces[contactStart[ci]];
+			c.contacts = &points[contactStart[ci]];
+			c.numContacts = contactCount[ci];
+			c.frictionPtr = NULL;
+			c.frictionCount = 0;
+			c.shapeInteraction = NULL;
+			c.maxCCDSeparation = PX_MAX_F32;
+			c.bodyState0 = PxSolverConstraintPrepDescBase::eDYNAMIC_BODY;
+			c.bodyState1 = desc.bodyBDataIndex < nbDyn ? PxSolverConstraintPrepDescBase::eDYNAMIC_BODY : PxSolverConstraintPrepDescBase::eSTATIC_BODY;
+			c.desc = &desc;
+			c.invMassScales.angular0 = c.invMassScales.angular1 = c.invMassScales.linear0 = c.invMassScales.linear1 = 1.0f;
+		}
+		PxCreateContactConstraints(&header, 1, cd, alloc, invDt, bounceThreshold, frictionOffsetThreshold, correlationDistance);
+	}
+	for(PxU32 h = 0; h < nbHeaders; h++)
+	{
+		outHeaderStart[h] = headers[h].startIndex;
+		outHeaderStride[h] = headers[h].stride;
+		outHeaderType[h] = headers[h].constraintType;
+	}
+	std::vector<PxVec3> motionLin(nbDyn ? nbDyn : 1), motionAng(nbDyn ? nbDyn : 1);
+	PxMemZero(bodies.data(), bodies.size() * sizeof(PxSolverBody));
+	PxSolveConstraints(headers.data(), nbHeaders, ordered.data(), bodies.data(), motionLin.data(), motionAng.data(), nbDyn, nbPos, nbVel);
+	PxIntegrateSolverBodies(bodyData.data(), bodies.data(), motionLin.data(), motionAng.data(), nbDyn, dt);
+	for(PxU32 a = 0; a < nbDyn; a++)
+	{
+		const PxSolverBodyData& d = bodyData[a];
+		outVel[6 * a + 0] = d.linearVelocity.x;
+		outVel[6 * a + 1] = d.linearVelocity.y;
+		outVel[6 * a + 2] = d.linearVelocity.z;
+		outVel[6 * a + 3] = d.angularVelocity.x;
+		outVel[6 * a + 4] = d.angularVelocity.y;
+		outVel[6 * a + 5] = d.angularVelocity.z;
+		storePose(outPose + 7 * a, d.body2World);
+	}
+	if(outForces) memcpy(outForces, forces.data(), sizeof(float) * nbContactsTotal);
+	return nbHeaders;
+}
+
+//////////////////////////////////////////////////////////////////////////////
 // One TGS frame of joints, built as the immediate-mode snippet builds its
 // joints (SnippetImmediateMode.cpp:838-1061) but with the caller's 1D rows in
 // place of a joint shader: construct bodies, PxBatchConstraintsTGS over the

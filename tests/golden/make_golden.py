@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_libs import CachedContacts, CpuBroadPhase, PersistentScenes, reference, run_contacts, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
+from oracle_libs import CachedContacts, CpuBroadPhase, PersistentScenes, reference, run_contacts, run_pgs, run_scene_step, run_tgs, scene_contacts, scene_pairs  # noqa: E402
 from scenarios import bp_frames, moving_pairs, np_pairs, pile_scenes, random_scene  # noqa: E402
 from physx_gb300.workloads import convex_core_pairs  # noqa: E402
 
@@ -115,6 +115,32 @@ def make_tgs():
         print("wrote", name)
 
 
+PGS_CASES = [
+    # name, seed, bodies, restitution: one PGS frame (PxConstructSolverBodies, PxBatchConstraints,
+    # PxCreateContactConstraints with the 4-wide block path and the per-pair path, PxSolveConstraints,
+    # PxIntegrateSolverBodies) with the batching and with one header per constraint
+    ("pgs_pile", 51, 160, 0.0),
+    ("pgs_pile_bouncy", 52, 80, 0.4),
+]
+
+
+def make_pgs():
+    out_keys = ("vel", "pose", "header_start", "header_stride", "header_type", "order", "forces")
+    for name, seed, n, rest in PGS_CASES:
+        sc = random_scene(seed, n)
+        A, B = scene_pairs(sc)
+        a, b, s_, c, ct, mat = scene_contacts("pxref", sc, A, B)
+        mat[:, 2] = rest
+        out = dict(rigid=sc["rigid"].view(np.uint8).reshape(n, 96), static_poses=sc["static_poses"], body_a=a, body_b=b,
+                   contact_start=s_, contact_count=c, contacts=ct, material=mat)
+        for tag, batch in (("batched", True), ("single", False)):
+            r = run_pgs("pxref", sc, a, b, s_, c, ct, mat, batch=batch)
+            for k in out_keys:
+                out["ref_%s_%s" % (tag, k)] = r[k]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name)
+
+
 SCENE_CASES = [
     # name, seed, scenes, bodies per scene, shapes: one full frame (bounds, ABP, contacts, TGS) per scene
     ("scene_spheres_capsules", 41, 4, 48, (0, 2)),
@@ -201,7 +227,7 @@ def make_pyramid():
 if __name__ == "__main__":
     if reference() is None:
         sys.exit("oracle/_ref/libpxref.so is missing: build it with make -C oracle/ref")
-    which = sys.argv[1:] or ["bp", "np", "np_cached", "tgs", "scene", "persistent", "recip", "pyramid"]
+    which = sys.argv[1:] or ["bp", "np", "np_cached", "tgs", "pgs", "scene", "persistent", "recip", "pyramid"]
     if "bp" in which:
         make_bp()
     if "np" in which:
@@ -210,6 +236,8 @@ if __name__ == "__main__":
         make_np_cached()
     if "tgs" in which:
         make_tgs()
+    if "pgs" in which:
+        make_pgs()
     if "scene" in which:
         make_scene()
     if "persistent" in which:

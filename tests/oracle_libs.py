@@ -170,6 +170,35 @@ def run_tgs(which, scene, A, B, start, count, contacts, mat, dt=1.0 / 60.0, nb_p
     return vel, pose, hs[:nh].copy(), hst[:nh].copy(), order[:nc].copy()
 
 
+def run_pgs(which, scene, A, B, start, count, contacts, mat, dt=1.0 / 60.0, nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0),
+            bounce=-2.0, friction_offset=0.04, correlation=0.025, batch=True):
+    """One PGS solve (PxConstructSolverBodies, PxBatchConstraints or one header per
+    constraint, PxCreateContactConstraints, PxSolveConstraints,
+    PxIntegrateSolverBodies): returns velocities (n,6), poses (n,7), headers
+    (start, stride, type), the constraint order and the written-back normal
+    impulse per contact."""
+    n = len(scene["types"])
+    m = len(scene["static_poses"])
+    nc = len(A)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nc, 1) * 2, np.uint32)
+    hst = np.zeros(max(nc, 1) * 2, np.uint32)
+    hty = np.zeros(max(nc, 1) * 2, np.uint32)
+    order = np.zeros(max(nc, 1), np.uint32)
+    forces = np.zeros(max(len(contacts), 1), np.float32)
+    g = np.array(gravity, np.float32)
+    L = oracle() if which == "orc" else reference()
+    fn = L.orc_pgs_solve if which == "orc" else L.pxref_pgs_solve
+    fn.restype = ctypes.c_uint32
+    nh = fn(_p(scene["rigid"]), ctypes.c_uint32(n), _p(np.ascontiguousarray(scene["static_poses"], np.float32)), ctypes.c_uint32(m),
+            _p(A), _p(B), ctypes.c_uint32(nc), _p(start), _p(count), _p(contacts), _p(mat), _p(g), ctypes.c_float(dt),
+            ctypes.c_uint32(nb_pos), ctypes.c_uint32(nb_vel), ctypes.c_float(bounce), ctypes.c_float(friction_offset),
+            ctypes.c_float(correlation), ctypes.c_int(1 if batch else 0), _p(vel), _p(pose), _p(hs), _p(hst), _p(hty), _p(order), _p(forces))
+    return dict(vel=vel, pose=pose, header_start=hs[:nh].copy(), header_stride=hst[:nh].copy(), header_type=hty[:nh].copy(),
+                order=order[:nc].copy(), forces=forces[:len(contacts)].copy())
+
+
 def run_scene_step(which, scenes, params, steps=1):
     """Steps every scene `steps` times through the oracle ("orc") or the reference
     ("pxref"); returns the updated PxRigidBodyData array."""

@@ -193,6 +193,50 @@ def test_oracle_tgs_matches_reference_golden(path):
     assert np.array_equal(vel, z["ref_velocity"]) and np.array_equal(pose, z["ref_pose"])
 
 
+PGS_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "pgs_*.npz")))
+PGS_KEYS = ("vel", "pose", "header_start", "header_stride", "header_type", "order", "forces")
+
+
+def pgs_fixture_args(path):
+    rb, z = load_tgs_fixture(path)
+    sc = dict(types=np.zeros(len(rb), np.int32), rigid=rb, static_poses=z["static_poses"])
+    return sc, z, (z["body_a"], z["body_b"], z["contact_start"], z["contact_count"], z["contacts"], z["material"])
+
+
+@pytest.mark.parametrize("batch", [True, False], ids=["batched", "one header per constraint"])
+@pytest.mark.parametrize("path", PGS_FIXTURES, ids=[os.path.basename(p) for p in PGS_FIXTURES])
+def test_oracle_pgs_matches_reference_golden(path, batch):
+    """One PGS frame (PxConstructSolverBodies, PxBatchConstraints,
+    PxCreateContactConstraints, PxSolveConstraints, PxIntegrateSolverBodies):
+    velocities, poses, headers with their types, the order and the
+    written-back normal impulses equal the reference's bit for bit, with the
+    4-wide block path (batched) and the per-pair path."""
+    from oracle_libs import run_pgs
+    sc, z, args = pgs_fixture_args(path)
+    got = run_pgs("orc", sc, *args, batch=batch)
+    tag = "batched" if batch else "single"
+    for k in PGS_KEYS:
+        assert np.array_equal(got[k], z["ref_%s_%s" % (tag, k)]), k
+    if batch:
+        assert {6, 7} & set(got["header_type"].tolist())   # block headers are in the fixture
+
+
+@pytest.mark.skipif(reference() is None, reason="reference build (oracle/_ref) not present on this machine")
+@pytest.mark.parametrize("seed,n,restitution,iters", [(61, 40, 0.0, (4, 1)), (62, 200, 0.3, (4, 1)), (63, 120, 0.0, (8, 2)), (64, 60, 0.5, (1, 1))])
+def test_oracle_pgs_matches_reference_live(seed, n, restitution, iters):
+    from oracle_libs import run_pgs, scene_contacts, scene_pairs
+    from scenarios import random_scene
+    sc = random_scene(seed, n)
+    A, B = scene_pairs(sc)
+    a, b, s, c, ct, mat = scene_contacts("pxref", sc, A, B)
+    mat[:, 2] = restitution
+    for batch in (True, False):
+        r = run_pgs("pxref", sc, a, b, s, c, ct, mat, batch=batch, nb_pos=iters[0], nb_vel=iters[1])
+        o = run_pgs("orc", sc, a, b, s, c, ct, mat, batch=batch, nb_pos=iters[0], nb_vel=iters[1])
+        for k in PGS_KEYS:
+            assert np.array_equal(r[k], o[k]), (batch, k)
+
+
 SCENE_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "scene_*.npz")))
 
 
