@@ -202,6 +202,29 @@ uint32_t gbpx_batch_typed_constraints_tgs(const uint32_t* bodyA, const uint32_t*
                                           uint32_t nbDynamic, uint32_t nbStatic, uint32_t* outHeaderStart, uint32_t* outHeaderStride,
                                           uint32_t* outOrder);
 
+/* ---------------------------------------------------------------------- PGS
+ * One immediate-mode PGS frame (PxConstructSolverBodies,
+ * PxConstructStaticSolverBody, PxBatchConstraints, PxCreateContactConstraints,
+ * PxSolveConstraints, PxIntegrateSolverBodies: physx/include/PxImmediateMode.h;
+ * physx/source/immediatemode/src/NpImmediateMode.cpp:55-78,269,292,552) from
+ * given contacts.  Inputs as gbpx_tgs_solve (body A of every constraint
+ * dynamic, 1..4 contacts per constraint); batch != 0 batches with
+ * PxBatchConstraints's rule, else one header per constraint in the caller's
+ * order.  Headers of stride 4 with at most 64 contacts take the reference's
+ * 4-wide block path.  Outputs: per dynamic body the linear and angular
+ * velocity (6 floats) and pose (7 floats) after integration; headers (start,
+ * stride, constraintType: DY_SC_TYPE_RB_CONTACT 1, _STATIC_CONTACT 5,
+ * _BLOCK_RB_CONTACT 6, _BLOCK_STATIC_RB_CONTACT 7) and the constraint order
+ * (arrays of at least nbConstraints); outForces (may be NULL): per contact the
+ * normal impulse the last velocity iteration writes back, in the
+ * constraint's row order (as PxSolverContactDesc::contactForces receives it). */
+int gbpx_pgs_solve(const void* rigid, uint32_t nbDyn, const float* staticPose, uint32_t nbStatic, const uint32_t* pairA,
+                   const uint32_t* pairB, uint32_t nbConstraints, const uint32_t* contactStart, const uint32_t* contactCount,
+                   const float* contacts, const float* material, const float* gravity, float dt, uint32_t nbPos, uint32_t nbVel,
+                   float bounceThreshold, float frictionOffsetThreshold, float correlationDistance, int batch, float* outVel,
+                   float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outHeaderType, uint32_t* outOrder,
+                   float* outForces, uint32_t* outNbHeaders);
+
 /* -------------------------------------------------------- joints (1D constraints)
  * Replace, on the rigid-body path:
  *   PxCreateJointConstraintsTGS      physx/include/PxImmediateMode.h:659

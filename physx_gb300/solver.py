@@ -1,8 +1,11 @@
-"""Immediate-mode TGS mirror over the GB300 solver kernels.
+"""Immediate-mode TGS and PGS mirror over the GB300 solver kernels.
 
 Mirrors physx/include/PxImmediateMode.h:592-729: PxConstructSolverBodiesTGS,
 PxBatchConstraintsTGS and one full TGS step (PxCreateContactConstraintsTGS +
-PxSolveConstraintsTGS + PxIntegrateSolverBodiesTGS) from given contacts.
+PxSolveConstraintsTGS + PxIntegrateSolverBodiesTGS) from given contacts; one
+PGS frame (PxConstructSolverBodies, PxBatchConstraints,
+PxCreateContactConstraints, PxSolveConstraints, PxIntegrateSolverBodies); joint
+frames.
 Rigid bodies are PxRigidBodyData records (numpy structured array, 96 bytes).
 """
 import ctypes
@@ -79,6 +82,45 @@ def tgs_step(rigid, static_poses, body_a, body_b, contact_start, contact_count, 
                            dt, nb_pos, nb_vel, bounce, friction_offset, correlation, _p(vel), _p(pose), _p(hs), _p(hst),
                            _p(order), ctypes.byref(nh)), "TGS step")
     return vel, pose, hs[:nh.value].copy(), hst[:nh.value].copy(), order[:nc].copy()
+
+
+def pgs_step(rigid, static_poses, body_a, body_b, contact_start, contact_count, contacts, material, dt=1.0 / 60.0,
+             nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0), bounce=-2.0, friction_offset=0.04, correlation=0.025, batch=True):
+    """One PGS frame (PxConstructSolverBodies, PxBatchConstraints or one header per
+    constraint, PxCreateContactConstraints, PxSolveConstraints,
+    PxIntegrateSolverBodies): returns dict(vel (n,6), pose (n,7), header_start,
+    header_stride, header_type, order, forces (per contact))."""
+    L = lib()
+    if not getattr(L, "_pgs_ready", False):
+        L.gbpx_pgs_solve.argtypes = ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 5 +
+                                     [ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_int] + [ctypes.c_void_p] * 8)
+        L._pgs_ready = True
+    rigid = np.ascontiguousarray(rigid)
+    n = len(rigid)
+    sp = np.ascontiguousarray(static_poses, np.float32)
+    a = np.ascontiguousarray(body_a, np.uint32)
+    b = np.ascontiguousarray(body_b, np.uint32)
+    ct = np.ascontiguousarray(contacts, np.float32)
+    nc = len(a)
+    vel = np.zeros((n, 6), np.float32)
+    pose = np.zeros((n, 7), np.float32)
+    hs = np.zeros(max(nc, 1), np.uint32)
+    hst = np.zeros(max(nc, 1), np.uint32)
+    hty = np.zeros(max(nc, 1), np.uint32)
+    order = np.zeros(max(nc, 1), np.uint32)
+    forces = np.zeros(max(len(ct), 1), np.float32)
+    nh = ctypes.c_uint32(0)
+    g = np.asarray(gravity, np.float32)
+    check(L.gbpx_pgs_solve(_p(rigid), n, _p(sp), len(sp), _p(a), _p(b), nc,
+                           _p(np.ascontiguousarray(contact_start, np.uint32)), _p(np.ascontiguousarray(contact_count, np.uint32)),
+                           _p(ct), _p(np.ascontiguousarray(material, np.float32)), _p(g), dt, nb_pos, nb_vel, bounce, friction_offset,
+                           correlation, 1 if batch else 0, _p(vel), _p(pose), _p(hs), _p(hst), _p(hty), _p(order), _p(forces),
+                           ctypes.byref(nh)), "PGS step")
+    k = nh.value
+    return dict(vel=vel, pose=pose, header_start=hs[:k].copy(), header_stride=hst[:k].copy(), header_type=hty[:k].copy(),
+                order=order[:nc].copy(), forces=forces[:len(ct)].copy())
 
 
 def joint_frame(frame, dt=1.0 / 60.0, nb_pos=4, nb_vel=1, gravity=(0.0, -9.81, 0.0), batch=True):
