@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--large-bodies", type=int, default=0,
                     help="block-per-scene threshold of the world's scene stages (0 = autotuned for the scene-size histogram)")
     ap.add_argument("--joint-frames", type=int, default=20)
-    ap.add_argument("--profile-extra", default="", choices=["", "broadphase", "large-scene", "joints", "convex-core"],
+    ap.add_argument("--profile-extra", default="", choices=["", "broadphase", "large-scene", "joints", "convex-core", "pgs"],
                     help="only run one frame of this side workload inside a profiler range and exit")
     ap.add_argument("--profile-step", type=int, default=0,
                     help="only build the state (pre-roll, autotune, warm-up), then run this many un-captured steps inside a "
@@ -395,6 +395,85 @@ def bench_joints(frames, cpu_frames):
                                   sample="%d frame(s) of the same state, oracle restatement, one thread" % cpu_frames))
 
 
+def pgs_workload(copies=48, spacing=3.0, friction=0.5):
+    """The immediate-mode snippet's 210-box pyramid repeated `copies` times side
+    by side (z offsets of `spacing` m) in one PGS frame: contacts from the
+    GB300 narrowphase for every box pair whose bounds (inflated by the contact
+    distance) overlap and for every box against the plane."""
+    import numpy as np
+    from physx_gb300.contacts import generate_contacts
+    from physx_gb300.workloads import pyramid_scene
+    base = pyramid_scene()
+    n0 = len(base["rigid"])
+    rigid = np.concatenate([base["rigid"]] * copies)
+    for k in range(copies):
+        rigid["p"][k * n0:(k + 1) * n0, 2] += np.float32(spacing * k)
+    n = len(rigid)
+    half = float(base["geoms"][0, 0])
+    r = half * 1.05 + 0.04
+    A, B = [], []
+    for k in range(copies):
+        p = rigid["p"][k * n0:(k + 1) * n0].astype(np.float64)
+        close = np.all(np.abs(p[:, None, :] - p[None, :, :]) <= 2 * r, axis=2)
+        i, j = np.nonzero(np.triu(close, 1))
+        A.append(i + k * n0)
+        B.append(j + k * n0)
+    A.append(np.arange(n))
+    B.append(np.full(n, n))   # the plane, static body n
+    A = np.concatenate(A).astype(np.uint32)
+    B = np.concatenate(B).astype(np.uint32)
+    box = np.array([half, half, half, 0], np.float32)
+    plane_pose = base["static_poses"][0]
+    pose = lambda idx: np.where((idx < n)[:, None], np.concatenate([rigid["q"], rigid["p"]], 1)[np.minimum(idx, n - 1)], plane_pose)  # noqa: E731
+    pairs = dict(type0=np.full(len(A), 3, np.int32), geom0=np.tile(box, (len(A), 1)), type1=np.where(B < n, 3, 1).astype(np.int32),
+                 geom1=np.where((B < n)[:, None], box, 0).astype(np.float32), pose0=pose(A).astype(np.float32), pose1=pose(B).astype(np.float32))
+    cnt, out = generate_contacts(pairs, max_per_pair=4)
+    keep = np.flatnonzero(cnt > 0)
+    count = cnt[keep].astype(np.uint32)
+    start = np.zeros(len(keep), np.uint32)
+    start[1:] = np.cumsum(count)[:-1]
+    contacts = np.ascontiguousarray(np.concatenate([out[k, :cnt[k]] for k in keep]), np.float32)
+    mat = np.zeros((len(keep), 3), np.float32)
+    mat[:, 0] = mat[:, 1] = friction
+    return dict(rigid=rigid, static_poses=base["static_poses"], body_a=A[keep], body_b=B[keep], contact_start=start, contact_count=count,
+                contacts=contacts, material=mat)
+
+
+def bench_pgs(frames, cpu_frames):
+    """One immediate-mode PGS frame (PxConstructSolverBodies, PxBatchConstraints,
+    PxCreateContactConstraints, PxSolveConstraints 4/1, PxIntegrateSolverBodies)
+    through gbpx_pgs_solve with host arrays in and out, per frame; the oracle's
+    frame on one host thread."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_libs import run_pgs
+    from physx_gb300.solver import pgs_step
+    w = pgs_workload()
+    args = (w["rigid"], w["static_poses"], w["body_a"], w["body_b"], w["contact_start"], w["contact_count"], w["contacts"], w["material"])
+    for _ in range(3):
+        out = pgs_step(*args)
+    times = []
+    for _ in range(frames):
+        t = time.perf_counter()
+        out = pgs_step(*args)
+        times.append(time.perf_counter() - t)
+    ms = 1000.0 * float(np.median(times))
+    sc = dict(types=np.zeros(len(w["rigid"]), np.int32), rigid=w["rigid"], static_poses=w["static_poses"])
+    t = time.perf_counter()
+    for _ in range(cpu_frames):
+        run_pgs("orc", sc, *args[2:])
+    cpu_ms = 1000.0 * (time.perf_counter() - t) / cpu_frames
+    n, nc = len(w["rigid"]), len(w["body_a"])
+    types = np.bincount(out["header_type"], minlength=8)
+    return dict(workload="48 copies of the snippet's 210-box pyramid side by side (%d boxes, %d contact constraints, %d contacts), "
+                         "plane, PGS 4 position / 1 velocity iterations, dt 1/60" % (n, nc, len(w["contacts"])),
+                bodies=n, constraints=nc, headers_block=int(types[6] + types[7]), headers_per_pair=int(types[1] + types[5]),
+                frames=frames, ms_per_frame=ms, value=n / (ms / 1000.0), unit="body-steps/s (one PGS frame each)",
+                e2e_note="host arrays in (bodies, contacts, materials), velocities, poses and impulses out, every frame",
+                cpu_baseline=dict(value=n / (cpu_ms / 1000.0), ms_per_frame=cpu_ms, unit="body-steps/s", cores=1, kind="port",
+                                  sample="%d frame(s) of the same state, oracle restatement, one thread" % cpu_frames))
+
+
 def convex_core_workload(reps=8, unique=32768):
     """Convex-core contact pairs (every core type against every shape type, 60 %
     axis-aligned for face contacts): `unique` seeded pairs repeated `reps` times
@@ -498,6 +577,15 @@ def profile_extra(which):
         physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
         out = s.stats()
         s.release()
+    elif which == "pgs":
+        from physx_gb300.solver import pgs_step
+        w = pgs_workload()
+        args = (w["rigid"], w["static_poses"], w["body_a"], w["body_b"], w["contact_start"], w["contact_count"], w["contacts"], w["material"])
+        pgs_step(*args)
+        physx_gb300.check(L.gbpx_profiler_start(), "gbpx_profiler_start")
+        r = pgs_step(*args)
+        physx_gb300.check(L.gbpx_profiler_stop(), "gbpx_profiler_stop")
+        out = dict(bodies=len(w["rigid"]), constraints=len(w["body_a"]), headers=len(r["header_start"]))
     elif which == "convex-core":
         from physx_gb300.contacts import generate_contacts
         pairs = convex_core_workload()
@@ -715,7 +803,7 @@ def main():
     if a.extras:
         extras = dict(pyramid=bench_pyramid(a.pyramid_steps), broadphase_1m=bench_broadphase(a.bp_frames, a.bp_cpu_frames),
                       large_scene_100k=bench_large_scene(a.large_steps, a.large_cpu_frames), joints=bench_joints(a.joint_frames, 5),
-                      convex_core=bench_convex_core(20, 20000))
+                      convex_core=bench_convex_core(20, 20000), pgs=bench_pgs(20, 3))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup, ms_per_step=ms / a.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
                 config=dict(workload=WORKLOAD, scenes=a.scenes, bodies_per_gpu=bodies, preroll_steps=a.preroll, pairs_per_step=st["pairs"],
