@@ -225,6 +225,35 @@ int gbpx_pgs_solve(const void* rigid, uint32_t nbDyn, const float* staticPose, u
                    float* outPose, uint32_t* outHeaderStart, uint32_t* outHeaderStride, uint32_t* outHeaderType, uint32_t* outOrder,
                    float* outForces, uint32_t* outNbHeaders);
 
+/* The PGS stages on solver bodies in the reference's layouts (PxSolverBodyData
+ * 112 B, PxSolverBody 32 B), for the physx::immediate drop-in: records of
+ * gbpx_pgs_record_bytes() each. */
+uint32_t gbpx_pgs_record_bytes(void);
+/* PxConstructSolverBodies (rigid: nb PxRigidBodyData) or, with rigid NULL,
+ * PxConstructStaticSolverBody (poses: nb PxTransform) into nb PxSolverBodyData. */
+int gbpx_construct_solver_bodies_pgs(const void* rigid, const float* poses, uint32_t nb, const float* gravity, float dt, void* outData);
+/* PxCreateContactConstraints, one contact descriptor per constraint: both
+ * bodies' PxSolverBodyData, the body frames, contactPoints[contactStart[k] ..
+ * +contactCount[k]] (PxContactPoint, 80 B, 1..4 per constraint).  laneFlags[k]:
+ * bit 0 a lane of a stride-4 header on the 4-wide block path, bit 1 that header
+ * has a dynamic body B, bit 2 the block solve stores body B (bodyBDataIndex != 0),
+ * bit 3 the per-pair solve treats body B as dynamic (DY_SC_TYPE_RB_CONTACT). */
+int gbpx_create_contact_constraints_pgs(uint32_t n, const void* data0, const void* data1, const float* frame0, const float* frame1,
+                                        const uint32_t* contactStart, const uint32_t* contactCount, const void* contactPoints,
+                                        uint32_t nbPoints, const uint8_t* laneFlags, float invDt, float bounceThreshold,
+                                        float frictionOffsetThreshold, void* outRecords);
+/* PxSolveConstraints over n records in solve order (updated in place), record k
+ * joining bodies bodyA[k], bodyB[k] (>= nbBodies: a zero body outside the
+ * caller's array); wave w = records [waveEnds[w-1], waveEnds[w]) touching
+ * distinct bodies.  bodies: nbBodies PxSolverBody (zeroed), updated in place;
+ * outMotionLin / outMotionAng: the velocities after the position iterations. */
+int gbpx_solve_constraints_pgs(void* records, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds,
+                               uint32_t nbWaves, void* bodies, uint32_t nbBodies, uint32_t nbPos, uint32_t nbVel, float* outMotionLin,
+                               float* outMotionAng);
+/* PxIntegrateSolverBodies (integrateCore): data (PxSolverBodyData) updated in
+ * place, the motion velocities replaced by those integrated with. */
+int gbpx_integrate_solver_bodies_pgs(void* data, const void* bodies, float* motionLin, float* motionAng, uint32_t n, float dt);
+
 /* -------------------------------------------------------- joints (1D constraints)
  * Replace, on the rigid-body path:
  *   PxCreateJointConstraintsTGS      physx/include/PxImmediateMode.h:659

@@ -9,6 +9,12 @@
  *   PxCreateContactConstraintsTGS    physx/include/PxImmediateMode.h:642
  *   PxSolveConstraintsTGS            physx/include/PxImmediateMode.h:716
  *   PxIntegrateSolverBodiesTGS       physx/include/PxImmediateMode.h:729
+ *   PxConstructSolverBodies          physx/include/PxImmediateMode.h:111
+ *   PxConstructStaticSolverBody      physx/include/PxImmediateMode.h:118
+ *   PxBatchConstraints               physx/include/PxImmediateMode.h:137
+ *   PxCreateContactConstraints       physx/include/PxImmediateMode.h:159
+ *   PxSolveConstraints               physx/include/PxImmediateMode.h:231
+ *   PxIntegrateSolverBodies          physx/include/PxImmediateMode.h:245
  *   PxGetBroadPhaseStaticFilterGroup     physx/include/PxBroadPhase.h:264
  *   PxGetBroadPhaseDynamicFilterGroup    physx/include/PxBroadPhase.h:278
  *   PxGetBroadPhaseKinematicFilterGroup  physx/include/PxBroadPhase.h:291
@@ -33,10 +39,12 @@
  * PxSolveConstraintsTGS); fresh caches and null friction pointers start over.
  * The bytes behind both are this library's own layout, opaque to the caller as
  * the reference's are.  The supported pair set is sphere / plane / capsule /
- * box; contact descriptors must use unit inverse-mass scales, restDistance 0
- * and no maximum impulse, and articulations are not supported (the functions
- * return false, or do nothing, for input outside this set).  All arithmetic
- * runs on the GPU through libgbpx.
+ * box, and convex cores; contact descriptors must use unit inverse-mass
+ * scales, restDistance 0 and no maximum impulse, and articulations are not
+ * supported (the functions return false, or do nothing, for input outside this
+ * set).  The PGS functions start every frame from fresh friction data:
+ * PxCreateContactConstraints hands back no friction patches (frictionPtr NULL,
+ * frictionCount 0).  All arithmetic runs on the GPU through libgbpx.
  *
  * PxCreateBroadPhase accepts eABP and ePABP descriptors (the same pair sets;
  * the GPU sweep stands in for both) and returns NULL for other types, as the
@@ -152,12 +160,38 @@ struct alignas(16) PxTGSSolverBodyData
 	uint32_t pad;
 };
 
+// PxSolverBody (physx/include/solver/PxSolverDefs.h:54): the PGS solver's
+// delta linear velocity and angular state
+struct alignas(16) PxSolverBody
+{
+	alignas(16) PxVec3 linearVelocity;
+	uint16_t maxSolverNormalProgress;
+	uint16_t maxSolverFrictionProgress;
+	PxVec3 angularState;
+	uint32_t solverProgress;
+};
+
+// PxSolverBodyData (PxSolverDefs.h:74)
+struct alignas(16) PxSolverBodyData
+{
+	alignas(16) PxVec3 linearVelocity;
+	float invMass;
+	PxVec3 angularVelocity;
+	float reportThreshold;
+	PxMat33 sqrtInvInertia;
+	float penBiasClamp;
+	uint32_t nodeIndex;
+	float maxContactImpulse;
+	PxTransform body2World;
+	uint16_t pad;
+};
+
 struct PxConstraintBatchHeader { uint32_t startIndex; uint16_t stride; uint16_t constraintType; };
 
 struct alignas(16) PxSolverConstraintDesc
 {
-	PxTGSSolverBodyVel* tgsBodyA;
-	PxTGSSolverBodyVel* tgsBodyB;
+	union { PxSolverBody* bodyA; PxTGSSolverBodyVel* tgsBodyA; void* articulationA; };
+	union { PxSolverBody* bodyB; PxTGSSolverBodyVel* tgsBodyB; void* articulationB; };
 	uint32_t bodyADataIndex, bodyBDataIndex;
 	uint32_t linkIndexA, linkIndexB;
 	uint8_t* constraint;
@@ -205,6 +239,38 @@ struct PxTGSSolverContactDesc
 	float maxImpulse;
 	float torsionalPatchRadius;
 	float minTorsionalPatchRadius;
+	float offsetSlop;
+};
+
+// PxSolverContactDesc (PxSolverDefs.h:157,221): the PGS contact descriptor
+struct PxSolverContactDesc
+{
+	PxConstraintInvMassScale invMassScales;
+	PxSolverConstraintDesc* desc;
+	const PxSolverBody* body0;
+	const PxSolverBody* body1;
+	const PxSolverBodyData* data0;
+	const PxSolverBodyData* data1;
+	PxTransform bodyFrame0;
+	PxTransform bodyFrame1;
+	int bodyState0;
+	int bodyState1;
+	void* shapeInteraction;
+	uint8_t* frictionPtr;
+	const PxContactPoint* contacts;
+	uint32_t numContacts;
+	uint8_t frictionCount;
+	bool hasMaxImpulse;
+	bool disableStrongFriction;
+	bool hasForceThresholds;
+	float restDistance;
+	float maxCCDSeparation;
+	float* contactForces;
+	uint32_t startFrictionPatchIndex;
+	uint32_t numFrictionPatches;
+	uint32_t startContactPatchIndex;
+	uint16_t numContactPatches;
+	uint16_t axisConstraintCount;
 	float offsetSlop;
 };
 
@@ -418,6 +484,22 @@ void PxSolveConstraintsTGS(const gbpx_px::PxConstraintBatchHeader* batchHeaders,
                            void* Z, void* deltaV);
 void PxIntegrateSolverBodiesTGS(gbpx_px::PxTGSSolverBodyVel* solverBody, const gbpx_px::PxTGSSolverBodyTxInertia* txInertia,
                                 gbpx_px::PxTransform* poses, uint32_t nbBodiesToIntegrate, float dt);
+void PxConstructSolverBodies(const gbpx_px::PxRigidBodyData* inRigidData, gbpx_px::PxSolverBodyData* outSolverBodyData, uint32_t nbBodies,
+                             const gbpx_px::PxVec3& gravity, float dt, bool gyroscopicForces);
+void PxConstructStaticSolverBody(const gbpx_px::PxTransform& globalPose, gbpx_px::PxSolverBodyData& solverBodyData);
+uint32_t PxBatchConstraints(const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, uint32_t nbConstraints, gbpx_px::PxSolverBody* solverBodies,
+                            uint32_t nbBodies, gbpx_px::PxConstraintBatchHeader* outBatchHeaders,
+                            gbpx_px::PxSolverConstraintDesc* outOrderedConstraintDescs, void** articulations, uint32_t nbArticulations);
+bool PxCreateContactConstraints(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, gbpx_px::PxSolverContactDesc* contactDescs,
+                                gbpx_px::PxConstraintAllocator& allocator, float invDt, float bounceThreshold, float frictionOffsetThreshold,
+                                float correlationDistance, void* ZV);
+void PxSolveConstraints(const gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders,
+                        const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, const gbpx_px::PxSolverBody* solverBodies,
+                        gbpx_px::PxVec3* linearMotionVelocity, gbpx_px::PxVec3* angularMotionVelocity, uint32_t nbSolverBodies,
+                        uint32_t nbPositionIterations, uint32_t nbVelocityIterations, float dt, float invDt, uint32_t nbSolverArticulations,
+                        void** solverArticulations, void* Z, void* deltaV);
+void PxIntegrateSolverBodies(gbpx_px::PxSolverBodyData* solverBodyData, gbpx_px::PxSolverBody* solverBody, gbpx_px::PxVec3* linearMotionVelocity,
+                             gbpx_px::PxVec3* angularMotionState, uint32_t nbBodiesToIntegrate, float dt);
 gbpx_px::PxBpFilterGroup PxGetBroadPhaseStaticFilterGroup();
 gbpx_px::PxBpFilterGroup PxGetBroadPhaseDynamicFilterGroup(uint32_t id);
 gbpx_px::PxBpFilterGroup PxGetBroadPhaseKinematicFilterGroup(uint32_t id);

@@ -625,6 +625,237 @@ GX void PxIntegrateSolverBodiesTGS(PxTGSSolverBodyVel* solverBody, const PxTGSSo
 	gbpx_integrate_solver_bodies_tgs(solverBody, txInertia, &poses[0].q.x, nbBodiesToIntegrate);
 }
 
+// ------------------------------------------------------------------ PGS
+// PxConstructSolverBodies / PxConstructStaticSolverBody / PxBatchConstraints /
+// PxCreateContactConstraints / PxSolveConstraints / PxIntegrateSolverBodies
+// (physx/include/PxImmediateMode.h:111-245) over libgbpx's PGS stages.  The
+// constraint memory of a contact descriptor holds libgbpx's PGS record; body
+// indices are resolved at the solve from the descriptors' PxSolverBody pointers.
+GX void PxConstructSolverBodies(const PxRigidBodyData* inRigidData, PxSolverBodyData* outSolverBodyData, uint32_t nbBodies, const PxVec3& gravity,
+                                float dt, bool gyroscopicForces)
+{
+	(void)gyroscopicForces;   // gyroscopic integration is not on this path
+	gbpx_construct_solver_bodies_pgs(inRigidData, nullptr, nbBodies, &gravity.x, dt, outSolverBodyData);
+}
+
+GX void PxConstructStaticSolverBody(const PxTransform& globalPose, PxSolverBodyData& solverBodyData)
+{
+	gbpx_construct_solver_bodies_pgs(nullptr, &globalPose.q.x, 1, nullptr, 0.0f, &solverBodyData);
+}
+
+// PxBatchConstraints: bodies inside [solverBodies, solverBodies + nbBodies)
+// are dynamic, every other body static or kinematic (as the reference).
+GX uint32_t PxBatchConstraints(const PxSolverConstraintDesc* descs, uint32_t nbConstraints, PxSolverBody* solverBodies, uint32_t nbBodies,
+                               PxConstraintBatchHeader* outBatchHeaders, PxSolverConstraintDesc* outOrdered, void** articulations,
+                               uint32_t nbArticulations)
+{
+	(void)articulations;
+	if(!nbConstraints || nbArticulations) return 0;
+	std::vector<uint32_t> a(nbConstraints), b(nbConstraints), hs(nbConstraints), hst(nbConstraints), order(nbConstraints);
+	auto index = [&](const PxSolverBody* p) { return (p >= solverBodies && p < solverBodies + nbBodies) ? uint32_t(p - solverBodies) : nbBodies; };
+	for(uint32_t i = 0; i < nbConstraints; i++)
+	{
+		a[i] = index(descs[i].bodyA);
+		b[i] = index(descs[i].bodyB);
+	}
+	std::vector<uint8_t> kind(nbConstraints);
+	for(uint32_t i = 0; i < nbConstraints; i++) kind[i] = uint8_t(descs[i].constraintLengthOver16);
+	const uint32_t nbHeaders =
+	    gbpx_batch_typed_constraints_tgs(a.data(), b.data(), kind.data(), nbConstraints, nbBodies, 1, hs.data(), hst.data(), order.data());
+	for(uint32_t i = 0; i < nbConstraints; i++) outOrdered[i] = descs[order[i]];
+	for(uint32_t h = 0; h < nbHeaders; h++)
+	{
+		outBatchHeaders[h].startIndex = hs[h];
+		outBatchHeaders[h].stride = uint16_t(hst[h]);
+		outBatchHeaders[h].constraintType = outOrdered[hs[h]].constraintLengthOver16;
+	}
+	return nbHeaders;
+}
+
+// PxCreateContactConstraints: a record per descriptor into the allocator's
+// constraint memory; the header types as the reference leaves them
+// (NpImmediateMode.cpp:292-367).  Friction data is not kept between frames.
+GX bool PxCreateContactConstraints(PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, PxSolverContactDesc* contactDescs,
+                                   PxConstraintAllocator& allocator, float invDt, float bounceThreshold, float frictionOffsetThreshold,
+                                   float correlationDistance, void* ZV)
+{
+	(void)correlationDistance;
+	(void)ZV;
+	const uint32_t n = stridesTotal(batchHeaders, nbHeaders);
+	if(!n) return true;
+	static const PxSolverBodyData zeroData = [] {
+		PxSolverBodyData d;
+		memset(&d, 0, sizeof(d));
+		d.maxContactImpulse = 3.4e38f;
+		d.penBiasClamp = -3.4e38f;
+		d.body2World.q.w = 1.0f;
+		return d;
+	}();
+	std::vector<PxSolverBodyData> d0(n), d1(n);
+	std::vector<PxTransform> f0(n), f1(n);
+	std::vector<uint32_t> cs(n), cc(n);
+	std::vector<PxContactPoint> points;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxSolverContactDesc& d = contactDescs[k];
+		if(!d.desc || !d.numContacts || d.numContacts > 4 || d.restDistance != 0.0f || d.hasMaxImpulse || d.invMassScales.linear0 != 1.0f ||
+		   d.invMassScales.angular0 != 1.0f || d.invMassScales.linear1 != 1.0f || d.invMassScales.angular1 != 1.0f || d.bodyState0 != eDYNAMIC_BODY ||
+		   (d.bodyState1 & eARTICULATION))
+			return false;
+		d0[k] = d.data0 ? *d.data0 : zeroData;
+		d1[k] = d.data1 ? *d.data1 : zeroData;
+		f0[k] = d.bodyFrame0;
+		f1[k] = d.bodyFrame1;
+		cs[k] = uint32_t(points.size());
+		cc[k] = d.numContacts;
+		points.insert(points.end(), d.contacts, d.contacts + d.numContacts);
+	}
+	// a header of stride 4 with at most 64 contacts takes the reference's 4-wide
+	// block path (NpImmediateMode.cpp:312-330); otherwise the first constraint's
+	// type, a static one turning dynamic when another constraint of the header is
+	std::vector<uint8_t> laneFlags(n, 0);
+	for(uint32_t h = 0, k = 0; h < nbHeaders; k += batchHeaders[h].stride, h++)
+	{
+		PxConstraintBatchHeader& hd = batchHeaders[h];
+		uint32_t total = 0;
+		bool dyn = false;
+		for(uint32_t l = 0; l < hd.stride; l++)
+		{
+			total += contactDescs[k + l].numContacts;
+			dyn = dyn || contactDescs[k + l].bodyState1 == eDYNAMIC_BODY;
+		}
+		if(hd.stride == 4 && total <= 64)
+		{
+			hd.constraintType = uint16_t(dyn ? DY_SC_TYPE_BLOCK_RB_CONTACT : DY_SC_TYPE_BLOCK_STATIC_RB_CONTACT);
+			for(uint32_t l = 0; l < 4; l++)
+				laneFlags[k + l] = uint8_t(1u | (dyn ? 2u : 0u) | (contactDescs[k + l].desc->bodyBDataIndex != 0 ? 4u : 0u));
+			continue;
+		}
+		auto typeOf = [&](uint32_t j) {
+			const int st = contactDescs[j].bodyState1;
+			return uint16_t((st == eSTATIC_BODY || st == eKINEMATIC_BODY) ? DY_SC_TYPE_STATIC_CONTACT : DY_SC_TYPE_RB_CONTACT);
+		};
+		uint16_t type = typeOf(k);
+		if(type == DY_SC_TYPE_STATIC_CONTACT)
+			for(uint32_t l = 1; l < hd.stride; l++)
+				if(typeOf(k + l) == DY_SC_TYPE_RB_CONTACT) { type = DY_SC_TYPE_RB_CONTACT; break; }
+		hd.constraintType = type;
+		for(uint32_t l = 0; l < hd.stride; l++) laneFlags[k + l] = type == DY_SC_TYPE_RB_CONTACT ? 8u : 0u;
+	}
+	const uint32_t recBytes = gbpx_pgs_record_bytes();
+	std::vector<uint8_t> recs(size_t(n) * recBytes);
+	if(gbpx_create_contact_constraints_pgs(n, d0.data(), d1.data(), &f0[0].q.x, &f1[0].q.x, cs.data(), cc.data(), points.data(),
+	                                       uint32_t(points.size()), laneFlags.data(), invDt, bounceThreshold, frictionOffsetThreshold,
+	                                       recs.data()) != GBPX_OK)
+		return false;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		PxSolverContactDesc& d = contactDescs[k];
+		uint8_t* mem = allocator.reserveConstraintData(recBytes);
+		if(!mem) return false;
+		memcpy(mem, &recs[size_t(k) * recBytes], recBytes);
+		d.desc->constraint = mem;
+		d.desc->constraintLengthOver16 = uint16_t(recBytes / 16);
+		d.desc->writeBack = d.contactForces;
+		d.frictionPtr = nullptr;
+		d.frictionCount = 0;
+	}
+	return true;
+}
+
+// PxSolveConstraints: headers are solved in order; consecutive headers whose
+// constraints touch distinct dynamic bodies run as one parallel wave.  The
+// normal impulses of the last velocity iteration go to each descriptor's
+// write-back (its PxSolverContactDesc::contactForces), in row order.
+GX void PxSolveConstraints(const PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders, const PxSolverConstraintDesc* descs,
+                           const PxSolverBody* solverBodies, PxVec3* linearMotionVelocity, PxVec3* angularMotionVelocity, uint32_t nbSolverBodies,
+                           uint32_t nbPositionIterations, uint32_t nbVelocityIterations, float dt, float invDt, uint32_t nbSolverArticulations,
+                           void** solverArticulations, void* Z, void* deltaV)
+{
+	(void)dt;
+	(void)invDt;
+	(void)solverArticulations;
+	(void)Z;
+	(void)deltaV;
+	if(nbSolverArticulations || !nbSolverBodies || !nbPositionIterations || !nbVelocityIterations) return;
+	auto index = [&](const PxSolverBody* p) {
+		return (p >= solverBodies && p < solverBodies + nbSolverBodies) ? uint32_t(p - solverBodies) : nbSolverBodies;
+	};
+	const uint32_t recBytes = gbpx_pgs_record_bytes();
+	std::vector<uint8_t> recs;
+	std::vector<uint32_t> a, b, waveEnds;
+	std::vector<const PxSolverConstraintDesc*> used;
+	std::vector<uint32_t> lastWave(nbSolverBodies, 0);
+	uint32_t wave = 1;
+	bool waveOpen = false;
+	for(uint32_t h = 0; h < nbBatchHeaders; h++)
+	{
+		const PxConstraintBatchHeader& hd = batchHeaders[h];
+		if(isJointHeader(hd.constraintType)) return;   // PGS joints are not on this path
+		bool clash = false;
+		for(uint32_t j = 0; j < hd.stride; j++)
+		{
+			const PxSolverConstraintDesc& d = descs[hd.startIndex + j];
+			const uint32_t ia = index(d.bodyA), ib = index(d.bodyB);
+			clash = clash || (ia < nbSolverBodies && lastWave[ia] == wave) || (ib < nbSolverBodies && lastWave[ib] == wave);
+		}
+		if(clash && waveOpen)
+		{
+			waveEnds.push_back(uint32_t(a.size()));
+			wave++;
+		}
+		for(uint32_t j = 0; j < hd.stride; j++)
+		{
+			const PxSolverConstraintDesc& d = descs[hd.startIndex + j];
+			const uint32_t ia = index(d.bodyA), ib = index(d.bodyB);
+			if(ia < nbSolverBodies) lastWave[ia] = wave;
+			if(ib < nbSolverBodies) lastWave[ib] = wave;
+			if(!d.constraint) continue;
+			a.push_back(ia);
+			b.push_back(ib);
+			used.push_back(&d);
+			recs.resize(recs.size() + recBytes);
+			memcpy(&recs[recs.size() - recBytes], d.constraint, recBytes);
+		}
+		waveOpen = true;
+	}
+	const uint32_t n = uint32_t(a.size());
+	if(waveOpen) waveEnds.push_back(n);
+	std::vector<PxSolverBody> bodies(solverBodies, solverBodies + nbSolverBodies);
+	if(gbpx_solve_constraints_pgs(n ? recs.data() : nullptr, a.data(), b.data(), n, waveEnds.data(), uint32_t(waveEnds.size()), bodies.data(),
+	                              nbSolverBodies, nbPositionIterations, nbVelocityIterations, &linearMotionVelocity[0].x,
+	                              &angularMotionVelocity[0].x) != GBPX_OK)
+		return;
+	// PxSolveConstraints leaves the velocities in the caller's solver bodies
+	memcpy(const_cast<PxSolverBody*>(solverBodies), bodies.data(), size_t(nbSolverBodies) * sizeof(PxSolverBody));
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const PxSolverConstraintDesc& d = *used[k];
+		const uint8_t* rec = &recs[size_t(k) * recBytes];
+		memcpy(d.constraint, rec, recBytes);
+		if(!d.writeBack) continue;
+		// record: bodyA, bodyB, nbPatches, flags, 4 patches of 48 bytes (nbPoints at +36),
+		// then the point rows (48 bytes, the impulse at +40)
+		uint32_t nbPatches;
+		memcpy(&nbPatches, rec + 8, 4);
+		uint32_t points = 0;
+		for(uint32_t p = 0; p < std::min<uint32_t>(nbPatches, 4); p++)
+		{
+			uint32_t np;
+			memcpy(&np, rec + 16 + 48 * p + 36, 4);
+			points += np;
+		}
+		float* out = static_cast<float*>(d.writeBack);
+		for(uint32_t i = 0; i < std::min<uint32_t>(points, 4); i++) memcpy(&out[i], rec + 16 + 4 * 48 + 48 * i + 40, 4);
+	}
+}
+
+GX void PxIntegrateSolverBodies(PxSolverBodyData* solverBodyData, PxSolverBody* solverBody, PxVec3* linearMotionVelocity, PxVec3* angularMotionState,
+                                uint32_t nbBodiesToIntegrate, float dt)
+{
+	gbpx_integrate_solver_bodies_pgs(solverBodyData, solverBody, &linearMotionVelocity[0].x, &angularMotionState[0].x, nbBodiesToIntegrate, dt);
+}
+
 // ------------------------------------------------------------------ broadphase
 // PxCreateBroadPhase / PxBroadPhase (physx/include/PxBroadPhase.h:492-629) and
 // PxCreateAABBManager / PxAABBManager (:642-796) over libgbpx's ABP-compatible

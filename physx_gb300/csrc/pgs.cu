@@ -332,3 +332,367 @@ GBPX_API int gbpx_pgs_solve(const void* rigid, uint32_t nbDyn, const float* stat
 	*outNbHeaders = uint32_t(nbHeaders);
 	return GBPX_OK;
 }
+
+// ---------------------------------------------------------------- split-phase PGS on reference layouts
+// The stages of the reference's immediate-mode PGS as separate calls, on solver
+// bodies in the reference's layouts (PxSolverBodyData 112 B: linearVelocity,
+// invMass, angularVelocity, reportThreshold, sqrtInvInertia, penBiasClamp,
+// nodeIndex, maxContactImpulse, body2World; PxSolverBody 32 B: linearVelocity,
+// progress counters, angularState, solverProgress), for callers that drive the
+// stages themselves (the physx::immediate drop-in).
+namespace gbpx
+{
+namespace pgs
+{
+__device__ __forceinline__ BodyData loadDataRef(const float* r)
+{
+	BodyData d;
+	d.lin = v3(r[0], r[1], r[2]); d.invMass = r[3];
+	d.ang = v3(r[4], r[5], r[6]);
+	d.sqrtInvInertia.c0 = v3(r[8], r[9], r[10]);
+	d.sqrtInvInertia.c1 = v3(r[11], r[12], r[13]);
+	d.sqrtInvInertia.c2 = v3(r[14], r[15], r[16]);
+	d.penBiasClamp = r[17];
+	d.maxContactImpulse = r[19];
+	d.pose.q.x = r[20]; d.pose.q.y = r[21]; d.pose.q.z = r[22]; d.pose.q.w = r[23];
+	d.pose.p = v3(r[24], r[25], r[26]);
+	return d;
+}
+// reportThreshold = PX_MAX_F32, nodeIndex = PX_INVALID_NODE, as the immediate-mode
+// constructors pass them (NpImmediateMode.cpp:64,75)
+__device__ __forceinline__ void storeDataRef(const BodyData& d, float* r)
+{
+	r[0] = d.lin.x; r[1] = d.lin.y; r[2] = d.lin.z; r[3] = d.invMass;
+	r[4] = d.ang.x; r[5] = d.ang.y; r[6] = d.ang.z; r[7] = FLT_MAX;
+	r[8] = d.sqrtInvInertia.c0.x; r[9] = d.sqrtInvInertia.c0.y; r[10] = d.sqrtInvInertia.c0.z;
+	r[11] = d.sqrtInvInertia.c1.x; r[12] = d.sqrtInvInertia.c1.y; r[13] = d.sqrtInvInertia.c1.z;
+	r[14] = d.sqrtInvInertia.c2.x; r[15] = d.sqrtInvInertia.c2.y; r[16] = d.sqrtInvInertia.c2.z;
+	r[17] = d.penBiasClamp;
+	r[18] = __uint_as_float(0xffffffffu);
+	r[19] = d.maxContactImpulse;
+	r[20] = d.pose.q.x; r[21] = d.pose.q.y; r[22] = d.pose.q.z; r[23] = d.pose.q.w;
+	r[24] = d.pose.p.x; r[25] = d.pose.p.y; r[26] = d.pose.p.z;
+	r[27] = 0.0f;
+}
+
+__global__ void constructRefKernel(const RigidBody* __restrict__ rigid, const float* __restrict__ poses, uint32_t n, float gx, float gy, float gz,
+                                   float dt, float* __restrict__ out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	BodyData d;
+	if(rigid)
+		constructDynamicBody(rigid[i], v3(gx, gy, gz), dt, d);
+	else
+	{
+		const float* s = poses + 7 * size_t(i);
+		Tr p;
+		p.q.x = s[0]; p.q.y = s[1]; p.q.z = s[2]; p.q.w = s[3];
+		p.p = v3(s[4], s[5], s[6]);
+		constructStaticBody(p, d);
+	}
+	storeDataRef(d, out + 28 * size_t(i));
+}
+
+// rows of constraint k from its bodies' PxSolverBodyData, its frames (the
+// PxSolverContactDesc's bodyFrame0/1) and its PxContactPoints (80 B each:
+// friction and restitution read from the points)
+__global__ void prepRefKernel(uint32_t n, const float* __restrict__ data0, const float* __restrict__ data1, const float* __restrict__ frame0,
+                              const float* __restrict__ frame1, const uint32_t* __restrict__ cStart, const uint32_t* __restrict__ cCount,
+                              const float* __restrict__ points, const uint8_t* __restrict__ laneFlags, PrepParams pp, Record* __restrict__ recs)
+{
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= n) return;
+	Contact cs[MAX_CONTACTS];
+	const uint32_t cnt = cCount[k] < uint32_t(MAX_CONTACTS) ? cCount[k] : uint32_t(MAX_CONTACTS);
+	for(uint32_t c = 0; c < cnt; c++)
+	{
+		const float* s = points + 20 * size_t(cStart[k] + c);
+		cs[c].n = v3(s[0], s[1], s[2]);
+		cs[c].sep = s[3];
+		cs[c].p = v3(s[4], s[5], s[6]);
+		cs[c].staticFriction = s[11];
+		cs[c].dynamicFriction = s[14];
+		cs[c].restitution = s[15];
+	}
+	BodyData d0 = loadDataRef(data0 + 28 * size_t(k)), d1 = loadDataRef(data1 + 28 * size_t(k));
+	const float* a = frame0 + 7 * size_t(k);
+	const float* b = frame1 + 7 * size_t(k);
+	d0.pose.q.x = a[0]; d0.pose.q.y = a[1]; d0.pose.q.z = a[2]; d0.pose.q.w = a[3]; d0.pose.p = v3(a[4], a[5], a[6]);
+	d1.pose.q.x = b[0]; d1.pose.q.y = b[1]; d1.pose.q.z = b[2]; d1.pose.q.w = b[3]; d1.pose.p = v3(b[4], b[5], b[6]);
+	const uint8_t f = laneFlags[k];
+	if(f & LANE_BLOCK)
+		prepBlockLane(cs, int(cnt), 0, 1, d0, d1, pp, (f & LANE_BLOCK_DYNAMIC) != 0, (f & LANE_STORE_B) != 0, recs[k]);
+	else
+		prepPair(cs, int(cnt), 0, 1, d0, d1, pp, (f & LANE_DYNAMIC_B) != 0, recs[k]);
+}
+
+// PxSolverBody (32 B) <-> BodyVel: linearVelocity at 0, angularState at 16
+__global__ void loadVelKernel(const float* __restrict__ ref, uint32_t n, BodyVel* __restrict__ vel)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	const float* r = ref + 8 * size_t(i);
+	BodyVel v;
+	v.lin = v3(r[0], r[1], r[2]); v.pad0 = 0.0f;
+	v.ang = v3(r[4], r[5], r[6]); v.pad1 = 0.0f;
+	vel[i] = v;
+}
+__global__ void storeVelKernel(const BodyVel* __restrict__ vel, uint32_t n, float* __restrict__ ref, float* __restrict__ motionLin,
+                               float* __restrict__ motionAng, const BodyVel* __restrict__ motion)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	float* r = ref + 8 * size_t(i);
+	r[0] = vel[i].lin.x; r[1] = vel[i].lin.y; r[2] = vel[i].lin.z;
+	r[4] = vel[i].ang.x; r[5] = vel[i].ang.y; r[6] = vel[i].ang.z;
+	float* ml = motionLin + 3 * size_t(i);
+	float* ma = motionAng + 3 * size_t(i);
+	ml[0] = motion[i].lin.x; ml[1] = motion[i].lin.y; ml[2] = motion[i].lin.z;
+	ma[0] = motion[i].ang.x; ma[1] = motion[i].ang.y; ma[2] = motion[i].ang.z;
+}
+
+// one wave of records whose bodies are bodyA[k], bodyB[k] (indices into vel;
+// >= nbBodies: a body outside the caller's solver-body array, read as zero and
+// never written)
+__global__ void solveWaveRefKernel(Record* __restrict__ recs, const uint32_t* __restrict__ bodyA, const uint32_t* __restrict__ bodyB, uint32_t begin,
+                                   uint32_t end, BodyVel* __restrict__ vel, uint32_t nbBodies, int doFriction, int conclude)
+{
+	const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= end) return;
+	Record& r = recs[k];
+	if(r.nbPatches == 0) return;
+	const uint32_t a = bodyA[k], b = bodyB[k];
+	BodyVel zero;
+	zero.lin = zero3(); zero.ang = zero3(); zero.pad0 = zero.pad1 = 0.0f;
+	BodyVel b0 = a < nbBodies ? vel[a] : zero;
+	BodyVel b1 = b < nbBodies ? vel[b] : zero;
+	bool writeB;
+	if(r.flags & REC_BLOCK)
+	{
+		solveBlockLane(r, b0, b1, doFriction != 0, conclude != 0);
+		writeB = (r.flags & REC_BLOCK_DYNAMIC) && (r.flags & REC_STORE_B);
+	}
+	else
+	{
+		solvePair(r, b0, b1, doFriction != 0, conclude != 0);
+		writeB = (r.flags & REC_DYNAMIC_B) != 0;
+	}
+	if(a < nbBodies) vel[a] = b0;
+	if(writeB && b < nbBodies) vel[b] = b1;
+}
+
+__global__ void integrateRefKernel(float* __restrict__ data, const float* __restrict__ bodies, float* __restrict__ motionLin,
+                                   float* __restrict__ motionAng, uint32_t n, float dt)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	float* r = data + 28 * size_t(i);
+	BodyData d = loadDataRef(r);
+	const float* sb = bodies + 8 * size_t(i);
+	BodyVel v;
+	v.lin = v3(sb[0], sb[1], sb[2]);
+	v.ang = v3(sb[4], sb[5], sb[6]);
+	float* ml = motionLin + 3 * size_t(i);
+	float* ma = motionAng + 3 * size_t(i);
+	const V3 mLin = v3(ml[0], ml[1], ml[2]), mAng = v3(ma[0], ma[1], ma[2]);
+	// integrateCore also returns the motion velocities it integrated with
+	const V3 linearMotionVel = add(d.lin, mLin);
+	const V3 angularMotionVelIn = add(d.ang, m33MulVS(d.sqrtInvInertia, mAng));
+	integrateBody(mLin, mAng, v, d, dt);
+	V3 angularMotionVel = angularMotionVelIn;
+	const float w = sqrtf(lenSqS(angularMotionVel));
+	if(w > 1e+7f) angularMotionVel = scale(normalizeS(angularMotionVel), 1e+7f);
+	ml[0] = linearMotionVel.x; ml[1] = linearMotionVel.y; ml[2] = linearMotionVel.z;
+	ma[0] = angularMotionVel.x; ma[1] = angularMotionVel.y; ma[2] = angularMotionVel.z;
+	const float keep7 = r[7], keep18 = r[18];   // reportThreshold, nodeIndex as the caller left them
+	storeDataRef(d, r);
+	r[7] = keep7;
+	r[18] = keep18;
+}
+} // namespace pgs
+
+struct PgsStageWorkspace
+{
+	cudaStream_t stream = 0;
+	DevBuf<pgs::RigidBody> rigid;
+	DevBuf<float> poses, data, data0, data1, frame0, frame1, points, bodies, motionLin, motionAng;
+	DevBuf<uint32_t> cStart, cCount, bodyA, bodyB;
+	DevBuf<uint8_t> laneFlags;
+	DevBuf<pgs::BodyVel> vel, motion;
+	DevBuf<pgs::Record> recs;
+	int init() { GBPX_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); return GBPX_OK; }
+};
+
+static PgsStageWorkspace* pgsStageWorkspace()
+{
+	static PgsStageWorkspace* ws = nullptr;
+	if(!ws)
+	{
+		ws = new PgsStageWorkspace;
+		if(ws->init()) { delete ws; ws = nullptr; }
+	}
+	return ws;
+}
+} // namespace gbpx
+
+// Bytes of one PGS constraint record (gbpx_create_contact_constraints_pgs).
+GBPX_API uint32_t gbpx_pgs_record_bytes(void) { return uint32_t(sizeof(pgs::Record)); }
+
+// PxConstructSolverBodies (rigid != NULL: nb PxRigidBodyData) or
+// PxConstructStaticSolverBody (rigid == NULL: nb poses, 7 floats each) into nb
+// PxSolverBodyData records (112 B).
+GBPX_API int gbpx_construct_solver_bodies_pgs(const void* rigid, const float* poses, uint32_t nb, const float* gravity, float dt, void* outData)
+{
+	gbpx::Zone zone("gbpx::constructSolverBodies");
+	if(!nb) return GBPX_OK;
+	if((!rigid && !poses) || !outData || (rigid && !gravity)) return GBPX_ERR_INVALID;
+	PgsStageWorkspace* ws = pgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	if(ws->rigid.reserve(nb) || ws->poses.reserve(7 * size_t(nb)) || ws->data.reserve(28 * size_t(nb))) return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	if(rigid) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->rigid.ptr, rigid, size_t(nb) * sizeof(pgs::RigidBody), cudaMemcpyHostToDevice, s));
+	else GBPX_CUDA_TRY(cudaMemcpyAsync(ws->poses.ptr, poses, size_t(nb) * 28, cudaMemcpyHostToDevice, s));
+	const float g0 = rigid ? gravity[0] : 0.0f, g1 = rigid ? gravity[1] : 0.0f, g2 = rigid ? gravity[2] : 0.0f;
+	pgs::constructRefKernel<<<divUp(nb, 128), 128, 0, s>>>(rigid ? ws->rigid.ptr : nullptr, ws->poses.ptr, nb, g0, g1, g2, dt, ws->data.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outData, ws->data.ptr, size_t(nb) * 112, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxCreateContactConstraints, one contact descriptor per constraint: the two
+// bodies' PxSolverBodyData (data0/data1, 112 B each), the body frames
+// (PxTransform), contactPoints[contactStart[k] .. +contactCount[k]]
+// (PxContactPoint, 80 B, 1..4 per constraint).  laneFlags[k]: bit 0 one of the
+// four constraints of a header of stride 4 on the reference's 4-wide block
+// path, bit 1 that header has a dynamic body B, bit 2 the block solve stores
+// body B (its bodyBDataIndex is not 0), bit 3 the per-pair solve treats body B
+// as dynamic (the header is DY_SC_TYPE_RB_CONTACT).  Records (gbpx_pgs_record_bytes()
+// each) go to outRecords.
+GBPX_API int gbpx_create_contact_constraints_pgs(uint32_t n, const void* data0, const void* data1, const float* frame0, const float* frame1,
+                                                 const uint32_t* contactStart, const uint32_t* contactCount, const void* contactPoints,
+                                                 uint32_t nbPoints, const uint8_t* laneFlags, float invDt, float bounceThreshold,
+                                                 float frictionOffsetThreshold, void* outRecords)
+{
+	gbpx::Zone zone("gbpx::createContactConstraints");
+	if(!n) return GBPX_OK;
+	if(!data0 || !data1 || !frame0 || !frame1 || !contactStart || !contactCount || !laneFlags || !outRecords || (nbPoints && !contactPoints) ||
+	   !(invDt > 0.0f))
+		return GBPX_ERR_INVALID;
+	for(uint32_t k = 0; k < n; k++)
+		if(!contactCount[k] || contactCount[k] > uint32_t(pgs::MAX_CONTACTS) || contactStart[k] + contactCount[k] > nbPoints) return GBPX_ERR_INVALID;
+	PgsStageWorkspace* ws = pgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	const size_t m = n;
+	if(ws->data0.reserve(28 * m) || ws->data1.reserve(28 * m) || ws->frame0.reserve(7 * m) || ws->frame1.reserve(7 * m) || ws->cStart.reserve(m) ||
+	   ws->cCount.reserve(m) || ws->points.reserve(20 * size_t(nbPoints) + 20) || ws->laneFlags.reserve(m) || ws->recs.reserve(m))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->data0.ptr, data0, m * 112, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->data1.ptr, data1, m * 112, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->frame0.ptr, frame0, m * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->frame1.ptr, frame1, m * 28, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cStart.ptr, contactStart, m * 4, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->cCount.ptr, contactCount, m * 4, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->laneFlags.ptr, laneFlags, m, cudaMemcpyHostToDevice, s));
+	if(nbPoints) GBPX_CUDA_TRY(cudaMemcpyAsync(ws->points.ptr, contactPoints, size_t(nbPoints) * 80, cudaMemcpyHostToDevice, s));
+	pgs::PrepParams pp;
+	pp.invDt = invDt;
+	pp.bounceThreshold = bounceThreshold;
+	pp.frictionOffsetThreshold = frictionOffsetThreshold;
+	pgs::prepRefKernel<<<divUp(n, 128), 128, 0, s>>>(n, ws->data0.ptr, ws->data1.ptr, ws->frame0.ptr, ws->frame1.ptr, ws->cStart.ptr, ws->cCount.ptr,
+	                                                 ws->points.ptr, ws->laneFlags.ptr, pp, ws->recs.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(outRecords, ws->recs.ptr, m * sizeof(pgs::Record), cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxSolveConstraints: records (n of gbpx_pgs_record_bytes(), in solve order,
+// updated in place with the impulses), record k joining bodies bodyA[k],
+// bodyB[k] (indices into bodies; >= nbBodies: read as a zero solver body, not
+// written).  Wave w solves records [waveEnds[w-1], waveEnds[w]), which touch
+// distinct bodies below nbBodies.  bodies: nbBodies PxSolverBody records (32 B,
+// zeroed by the caller), updated in place; outMotionLin / outMotionAng
+// (nbBodies x 3 floats): the velocities after the position iterations.
+GBPX_API int gbpx_solve_constraints_pgs(void* records, const uint32_t* bodyA, const uint32_t* bodyB, uint32_t n, const uint32_t* waveEnds,
+                                        uint32_t nbWaves, void* bodies, uint32_t nbBodies, uint32_t nbPos, uint32_t nbVel, float* outMotionLin,
+                                        float* outMotionAng)
+{
+	gbpx::Zone zone("gbpx::solveConstraints");
+	if(!nbPos || !nbVel || (nbBodies && (!bodies || !outMotionLin || !outMotionAng))) return GBPX_ERR_INVALID;
+	if(n && (!records || !bodyA || !bodyB || !waveEnds || !nbWaves || waveEnds[nbWaves - 1] != n)) return GBPX_ERR_INVALID;
+	for(uint32_t w = 0; w < nbWaves; w++)
+		if(waveEnds[w] > n || (w && waveEnds[w] < waveEnds[w - 1])) return GBPX_ERR_INVALID;
+	PgsStageWorkspace* ws = pgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	const size_t m = n ? n : 1, nb = nbBodies ? nbBodies : 1;
+	if(ws->recs.reserve(m) || ws->bodyA.reserve(m) || ws->bodyB.reserve(m) || ws->bodies.reserve(8 * nb) || ws->vel.reserve(nb) ||
+	   ws->motion.reserve(nb) || ws->motionLin.reserve(3 * nb) || ws->motionAng.reserve(3 * nb))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	if(n)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->recs.ptr, records, size_t(n) * sizeof(pgs::Record), cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodyA.ptr, bodyA, size_t(n) * 4, cudaMemcpyHostToDevice, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodyB.ptr, bodyB, size_t(n) * 4, cudaMemcpyHostToDevice, s));
+	}
+	if(nbBodies)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodies.ptr, bodies, size_t(nbBodies) * 32, cudaMemcpyHostToDevice, s));
+		pgs::loadVelKernel<<<divUp(nbBodies, 128), 128, 0, s>>>(ws->bodies.ptr, nbBodies, ws->vel.ptr);
+	}
+	auto iterate = [&](int doFriction, int conclude) {
+		for(uint32_t w = 0; w < nbWaves; w++)
+		{
+			const uint32_t b = w ? waveEnds[w - 1] : 0u, e = waveEnds[w];
+			if(e > b)
+				pgs::solveWaveRefKernel<<<divUp(e - b, 64), 64, 0, s>>>(ws->recs.ptr, ws->bodyA.ptr, ws->bodyB.ptr, b, e, ws->vel.ptr, nbBodies, doFriction,
+				                                                         conclude);
+		}
+	};
+	for(uint32_t i = nbPos; i > 1; --i) iterate(i <= 3 ? 1 : 0, 0);
+	iterate(1, 1);
+	if(nbBodies) pgs::saveMotionKernel<<<divUp(nbBodies, 128), 128, 0, s>>>(ws->vel.ptr, nbBodies, ws->motion.ptr);
+	for(uint32_t i = nbVel; i > 0; --i) iterate(1, 0);
+	if(nbBodies)
+		pgs::storeVelKernel<<<divUp(nbBodies, 128), 128, 0, s>>>(ws->vel.ptr, nbBodies, ws->bodies.ptr, ws->motionLin.ptr, ws->motionAng.ptr,
+		                                                          ws->motion.ptr);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	if(n) GBPX_CUDA_TRY(cudaMemcpyAsync(records, ws->recs.ptr, size_t(n) * sizeof(pgs::Record), cudaMemcpyDeviceToHost, s));
+	if(nbBodies)
+	{
+		GBPX_CUDA_TRY(cudaMemcpyAsync(bodies, ws->bodies.ptr, size_t(nbBodies) * 32, cudaMemcpyDeviceToHost, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(outMotionLin, ws->motionLin.ptr, size_t(nbBodies) * 12, cudaMemcpyDeviceToHost, s));
+		GBPX_CUDA_TRY(cudaMemcpyAsync(outMotionAng, ws->motionAng.ptr, size_t(nbBodies) * 12, cudaMemcpyDeviceToHost, s));
+	}
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}
+
+// PxIntegrateSolverBodies: n PxSolverBodyData records (updated in place: pose,
+// velocities), PxSolverBody records and the motion velocities of
+// gbpx_solve_constraints_pgs (replaced by the velocities integrated with).
+GBPX_API int gbpx_integrate_solver_bodies_pgs(void* data, const void* bodies, float* motionLin, float* motionAng, uint32_t n, float dt)
+{
+	gbpx::Zone zone("gbpx::integrateSolverBodies");
+	if(!n) return GBPX_OK;
+	if(!data || !bodies || !motionLin || !motionAng) return GBPX_ERR_INVALID;
+	PgsStageWorkspace* ws = pgsStageWorkspace();
+	if(!ws) return GBPX_ERR_CUDA;
+	if(ws->data.reserve(28 * size_t(n)) || ws->bodies.reserve(8 * size_t(n)) || ws->motionLin.reserve(3 * size_t(n)) || ws->motionAng.reserve(3 * size_t(n)))
+		return GBPX_ERR_NOMEM;
+	cudaStream_t s = ws->stream;
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->data.ptr, data, size_t(n) * 112, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->bodies.ptr, bodies, size_t(n) * 32, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->motionLin.ptr, motionLin, size_t(n) * 12, cudaMemcpyHostToDevice, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(ws->motionAng.ptr, motionAng, size_t(n) * 12, cudaMemcpyHostToDevice, s));
+	pgs::integrateRefKernel<<<divUp(n, 128), 128, 0, s>>>(ws->data.ptr, ws->bodies.ptr, ws->motionLin.ptr, ws->motionAng.ptr, n, dt);
+	GBPX_CUDA_TRY(cudaGetLastError());
+	GBPX_CUDA_TRY(cudaMemcpyAsync(data, ws->data.ptr, size_t(n) * 112, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(motionLin, ws->motionLin.ptr, size_t(n) * 12, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaMemcpyAsync(motionAng, ws->motionAng.ptr, size_t(n) * 12, cudaMemcpyDeviceToHost, s));
+	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
+	return GBPX_OK;
+}

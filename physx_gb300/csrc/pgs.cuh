@@ -75,6 +75,11 @@ struct __align__(16) Record
 	FrictionRow friction[MAX_FRICTION];
 };
 
+// the drop-in reads the point count and the impulses out of a record's bytes
+static_assert(sizeof(PatchRow) == 48 && offsetof(PatchRow, nbPoints) == 36, "PatchRow layout");
+static_assert(sizeof(PointRow) == 48 && offsetof(PointRow, force) == 40, "PointRow layout");
+static_assert(offsetof(Record, patch) == 16 && offsetof(Record, point) == 16 + MAX_CONTACTS * sizeof(PatchRow), "Record layout");
+
 // copyToSolverBodyData (DyRigidBodyToSolverBody.cpp:38) after
 // bodyCoreComputeUnconstrainedVelocity (DyBodyCoreIntegrator.h:38)
 __device__ __forceinline__ void copyToSolverBody(V3 lv, V3 av, float invMass, V3 invInertia, const Tr& pose, float maxDepen, float maxImpulse,

@@ -58,6 +58,16 @@ int main(){
  S(PxTGSSolverBodyData); O(PxTGSSolverBodyData, maxContactImpulse); O(PxTGSSolverBodyData, originalAngularVelocity); O(PxTGSSolverBodyData, penBiasClamp);
  O(PxTGSSolverBodyData, invMass); O(PxTGSSolverBodyData, nodeIndex); O(PxTGSSolverBodyData, reportThreshold);
  S(PxConstraintBatchHeader); O(PxConstraintBatchHeader, stride); O(PxConstraintBatchHeader, constraintType);
+ S(PxSolverBody); O(PxSolverBody, maxSolverNormalProgress); O(PxSolverBody, angularState); O(PxSolverBody, solverProgress);
+ S(PxSolverBodyData); O(PxSolverBodyData, invMass); O(PxSolverBodyData, angularVelocity); O(PxSolverBodyData, reportThreshold);
+ O(PxSolverBodyData, sqrtInvInertia); O(PxSolverBodyData, penBiasClamp); O(PxSolverBodyData, nodeIndex); O(PxSolverBodyData, maxContactImpulse);
+ O(PxSolverBodyData, body2World);
+ S(PxSolverContactDesc); O(PxSolverContactDesc, desc); O(PxSolverContactDesc, body0); O(PxSolverContactDesc, data0); O(PxSolverContactDesc, data1);
+ O(PxSolverContactDesc, bodyFrame0); O(PxSolverContactDesc, bodyFrame1); O(PxSolverContactDesc, bodyState0); O(PxSolverContactDesc, bodyState1);
+ O(PxSolverContactDesc, shapeInteraction); O(PxSolverContactDesc, frictionPtr); O(PxSolverContactDesc, contacts); O(PxSolverContactDesc, numContacts);
+ O(PxSolverContactDesc, frictionCount); O(PxSolverContactDesc, hasMaxImpulse); O(PxSolverContactDesc, restDistance);
+ O(PxSolverContactDesc, maxCCDSeparation); O(PxSolverContactDesc, contactForces); O(PxSolverContactDesc, numContactPatches);
+ O(PxSolverContactDesc, axisConstraintCount); O(PxSolverContactDesc, offsetSlop); O(PxSolverConstraintDesc, bodyA); O(PxSolverConstraintDesc, bodyB);
  S(PxSolverConstraintDesc); O(PxSolverConstraintDesc, tgsBodyA); O(PxSolverConstraintDesc, tgsBodyB); O(PxSolverConstraintDesc, bodyADataIndex);
  O(PxSolverConstraintDesc, bodyBDataIndex); O(PxSolverConstraintDesc, linkIndexA); O(PxSolverConstraintDesc, linkIndexB); O(PxSolverConstraintDesc, constraint);
  O(PxSolverConstraintDesc, writeBack); O(PxSolverConstraintDesc, writeBackFriction); O(PxSolverConstraintDesc, progressA); O(PxSolverConstraintDesc, progressB);

@@ -118,6 +118,42 @@ def test_immediate_convex_core_contacts_match_reference_golden(cuda_device, tmp_
     assert k == len(words)
 
 
+@pytest.mark.parametrize("batch", [True, False], ids=["batched", "one header per constraint"])
+def test_immediate_pgs_frames_match_reference_golden(cuda_device, tmp_path, batch):
+    """A program written against the reference's PGS interface (PxConstructSolverBodies,
+    PxConstructStaticSolverBody, PxBatchConstraints, PxCreateContactConstraints,
+    PxSolveConstraints, PxIntegrateSolverBodies; tests/immediate_pgs.cpp) linked
+    against libgbpx_immediate.so reproduces the reference's PGS frames
+    (pgs_*.npz): headers, types and order exactly, velocities, poses and the
+    written-back normal impulses within the PGS bar of tests/test_pgs_gpu.py."""
+    import glob
+    import struct
+    from test_oracle_golden import GOLDEN, load_tgs_fixture
+    from test_pgs_gpu import assert_pgs_close
+    exe = _build(str(tmp_path), "immediate_pgs")
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "pgs_*.npz"))):
+        rb, z = load_tgs_fixture(path)
+        n, m, nc, ncts = len(rb), len(z["static_poses"]), len(z["body_a"]), len(z["contacts"])
+        blob = struct.pack("<5I", n, m, nc, ncts, 1 if batch else 0) + rb.tobytes() + np.ascontiguousarray(z["static_poses"], np.float32).tobytes()
+        for k in ("body_a", "body_b", "contact_start", "contact_count"):
+            blob += np.ascontiguousarray(z[k], np.uint32).tobytes()
+        blob += np.ascontiguousarray(z["contacts"], np.float32).tobytes() + np.ascontiguousarray(z["material"], np.float32).tobytes()
+        blob += struct.pack("<4f2I", 1.0 / 60.0, 0.0, -9.81, 0.0, 4, 1)
+        out = subprocess.run([exe], input=blob, capture_output=True, check=True).stdout
+        body = np.frombuffer(out[: n * 52], np.float32).reshape(n, 13)
+        nh = struct.unpack_from("<I", out, n * 52)[0]
+        off = n * 52 + 4
+        hdr = np.frombuffer(out[off: off + nh * 12], np.uint32).reshape(nh, 3)
+        off += nh * 12
+        order = np.frombuffer(out[off: off + nc * 4], np.uint32)
+        forces = np.frombuffer(out[off + nc * 4:], np.float32)
+        got = dict(vel=body[:, :6].copy(), pose=body[:, 6:].copy(), header_start=hdr[:, 0].copy(), header_stride=hdr[:, 1].copy(),
+                   header_type=hdr[:, 2].copy(), order=order.copy(), forces=forces.copy())
+        tag = "batched" if batch else "single"
+        ref = {k: z["ref_%s_%s" % (tag, k)] for k in ("vel", "pose", "header_start", "header_stride", "header_type", "order", "forces")}
+        assert_pgs_close(ref, got, path)
+
+
 @pytest.mark.parametrize("seed", [121, 122])
 def test_immediate_persistent_frames_match_oracle(cuda_device, tmp_path, seed):
     """Ten frames of a pile through the drop-in the way the snippet runs its
