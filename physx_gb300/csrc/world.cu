@@ -1527,7 +1527,7 @@ struct World
 	cudaStream_t stream = 0;
 	cudaStream_t sideStream = 0;   // block-per-scene kernels run beside the warp-per-scene ones
 	int streamPriority = 0;        // CUDA stream priority of the world's streams (set before create)
-	cudaEvent_t forkEv[3] = {}, joinEv[3] = {};
+	cudaEvent_t forkEv[4] = {}, joinEv[4] = {};
 	cudaGraphExec_t graphExec = nullptr;
 	uint32_t graphSteps = 0;
 	world::StepParams params;
@@ -1629,7 +1629,7 @@ struct World
 		std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return hScenes[x].nbBodies > hScenes[y].nbBodies; });
 		GBPX_CUDA_TRY(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, streamPriority));
 		GBPX_CUDA_TRY(cudaStreamCreateWithPriority(&sideStream, cudaStreamNonBlocking, streamPriority));
-		for(int k = 0; k < 3; k++)
+		for(int k = 0; k < 4; k++)
 		{
 			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&forkEv[k], cudaEventDisableTiming));
 			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&joinEv[k], cudaEventDisableTiming));
@@ -1802,11 +1802,17 @@ struct World
 			world::broadphaseBigKernel<<<plain ? 1u : gridBpBig, BIG_THREADS, sizeof(world::BpSmemBig), bigStream>>>(w, params);
 			if(!plain) GBPX_CUDA_TRY(join(0));
 		}
-		for(uint32_t k = 0; k < world::NB_KINDS; k++)
+		// the pair kinds write disjoint slots: capsule-box and box-box (the long
+		// kernels) run on the side stream beside the seven other kinds
+		if(!plain) GBPX_CUDA_TRY(fork(3));
+		const cudaStream_t heavyStream = plain ? stream : sideStream;
+		for(uint32_t k = 7; k < world::NB_KINDS; k++)
 		{
-			if(k == 7 && params.persistent) world::orderByPathKernel<<<plain ? std::min(gridOrder, 8u) : gridOrder, 128, 0, stream>>>(w, params);
-			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : npGrid(k), 128, 0, stream>>>(w, params);
+			if(k == 7 && params.persistent) world::orderByPathKernel<<<plain ? std::min(gridOrder, 8u) : gridOrder, 128, 0, heavyStream>>>(w, params);
+			npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : npGrid(k), 128, 0, heavyStream>>>(w, params);
 		}
+		for(uint32_t k = 0; k < 7; k++) npKernels()[k]<<<plain ? std::min(gridNp[k], 8u) : npGrid(k), 128, 0, stream>>>(w, params);
+		if(!plain) GBPX_CUDA_TRY(join(3));
 		if(big && !plain) GBPX_CUDA_TRY(fork(1));
 		world::batchKernel<<<gBatch, threads, solveSmemBytes(threads / 32), stream>>>(w, params);
 		if(big)
@@ -1977,7 +1983,7 @@ struct World
 		keys.release(); stats.release(); identity.release(); recs.release(); sceneAcc.release(); resList.release(); vel.release(); tx.release(); data.release(); pose.release(); hStage.release();
 		if(sideStream) { cudaStreamSynchronize(sideStream); cudaStreamDestroy(sideStream); }
 		sideStream = 0;
-		for(int k = 0; k < 3; k++)
+		for(int k = 0; k < 4; k++)
 		{
 			if(forkEv[k]) cudaEventDestroy(forkEv[k]);
 			if(joinEv[k]) cudaEventDestroy(joinEv[k]);
