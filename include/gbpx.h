@@ -167,6 +167,11 @@ int gbpx_tgs_solve(const void* rigidBodies, uint32_t nbDynamic, const float* sta
  * Constraint rows are this build's own format, gbpx_constraint_row_stride()
  * bytes per constraint at most. */
 uint32_t gbpx_constraint_row_stride(void);
+/* The integrator's sine and cosine of the half angle (no reference
+ * counterpart; numerics check): for each of n angles (host array) out gets 4
+ * floats: the sine and cosine the solver uses, and double-precision sin / cos
+ * rounded to float. */
+int gbpx_eval_sincos_angle(const float* x, uint32_t n, float* out);
 int gbpx_construct_static_solver_bodies_tgs(const float* poses, uint32_t n, void* outVel, void* outTxI, void* outData);
 /* one descriptor per constraint: both bodies' records (64/64/48 B), frames
  * (PxTransform) and PxContactPoints (80 B); laneFlags[k] (null: all per-pair):

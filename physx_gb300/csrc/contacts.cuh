@@ -490,10 +490,10 @@ static __device__ bool invalidateBoxConvex(const Manifold& m, const Tr& cur, Q q
 	const float thresholdQ = kInvalidateQuatThresholds(m.num);
 	const float dqA = quatDot(quatA, m.quatA), dqB = quatDot(quatB, m.quatB);
 	if(deltaP > thresholdP || thresholdQ > dqA || thresholdQ > dqB) return true;
-	// acos evaluated in double and rounded: the host C library's acosf is nearer to the
-	// correctly rounded value than the single-precision device acosf
-	const float aRadian = dqA < 1.0f ? float(acos(double(dqA))) : 0.0f;
-	const float bRadian = dqB < 1.0f ? float(acos(double(dqB))) : 0.0f;
+	// the angles only meet a threshold: the device acosf (within 2 ulp of the host
+	// C library's) decides the same except within a few ulp of the threshold
+	const float aRadian = dqA < 1.0f ? acosf(dqA) : 0.0f;
+	const float bRadian = dqB < 1.0f ? acosf(dqB) : 0.0f;
 	return aRadian * radiusA > thresholdP || bRadian * radiusB > thresholdP;
 }
 

@@ -600,10 +600,8 @@ __device__ __forceinline__ void integrateBody(V3 motionLin, V3 motionAng, const 
 			w = maxW;
 		}
 		const float v = dt * w * 0.5f;
-		double ds, dc;
-		sincos(double(v), &ds, &dc);
-		float s = float(ds);
-		const float q = float(dc);
+		float s, q;
+		sinCosAngle(v, s, q);   // correctly rounded (the host C library's sinf / cosf match it far more often than the device ones)
 		s = s / w;
 		const V3 pqr = scale(angularMotionVel, s);
 		const Q quatVel = {pqr.x, pqr.y, pqr.z, 0.0f};

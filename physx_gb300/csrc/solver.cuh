@@ -1008,12 +1008,10 @@ __device__ __forceinline__ void integrateStep(BodyVel& v, BodyTx& t, float dt)
 	{
 		const float w = sqrtf(w2);
 		const float vv = dt * w * 0.5f;
-		// sin/cos evaluated in double and rounded: the host C library's sinf/cosf are
-		// nearer to the correctly rounded value than the single-precision device ones
-		double ds, dc;
-		sincos(double(vv), &ds, &dc);
-		float s = float(ds);
-		const float q = float(dc);
+		// sin/cos correctly rounded, which the host C library's sinf/cosf match far
+		// more often than the single-precision device functions do
+		float s, q;
+		sinCosAngle(vv, s, q);
 		s /= w;
 		const V3 pqr = scale(angMotion, s);
 		const Q qv_ = {pqr.x, pqr.y, pqr.z, 0.0f};

@@ -799,3 +799,45 @@ GBPX_API int gbpx_integrate_solver_bodies_tgs(void* bodyVel, const void* bodyTxI
 	GBPX_CUDA_TRY(cudaStreamSynchronize(s));
 	return GBPX_OK;
 }
+
+namespace gbpx
+{
+namespace tgs
+{
+__global__ void sinCosAngleKernel(const float* __restrict__ x, uint32_t n, float* __restrict__ out)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n) return;
+	float s, c;
+	sinCosAngle(x[i], s, c);
+	double ds, dc;
+	sincos(double(x[i]), &ds, &dc);
+	out[4 * size_t(i) + 0] = s;
+	out[4 * size_t(i) + 1] = c;
+	out[4 * size_t(i) + 2] = float(ds);
+	out[4 * size_t(i) + 3] = float(dc);
+}
+} // namespace tgs
+} // namespace gbpx
+
+// The integrator's sine and cosine of n angles (host arrays): per angle the
+// values the solver uses and the double-precision values rounded to float
+// (out: 4 floats per angle).
+GBPX_API int gbpx_eval_sincos_angle(const float* x, uint32_t n, float* out)
+{
+	if(!n) return GBPX_OK;
+	if(!x || !out) return GBPX_ERR_INVALID;
+	float *dx = nullptr, *dout = nullptr;
+	cudaError_t e = cudaMalloc(&dx, size_t(n) * 4);
+	if(e == cudaSuccess) e = cudaMalloc(&dout, size_t(n) * 16);
+	if(e == cudaSuccess) e = cudaMemcpy(dx, x, size_t(n) * 4, cudaMemcpyHostToDevice);
+	if(e == cudaSuccess)
+	{
+		gbpx::tgs::sinCosAngleKernel<<<(n + 255) / 256, 256>>>(dx, n, dout);
+		e = cudaGetLastError();
+	}
+	if(e == cudaSuccess) e = cudaMemcpy(out, dout, size_t(n) * 16, cudaMemcpyDeviceToHost);
+	cudaFree(dx);
+	cudaFree(dout);
+	return e == cudaSuccess ? GBPX_OK : GBPX_ERR_CUDA;
+}

@@ -65,6 +65,42 @@ __device__ __forceinline__ float recipFast(float x)
 	}
 	return __uint_as_float(r);
 }
+// sin x and cos x of the integrator's half angles without double precision
+// for |x| <= 0.125: each result is one rounding of a two-float value -- the
+// leading Taylor terms (x - x^3/6, 1 - x^2/2) carried exactly by error-free
+// transformations (the exact square and cube from FMA residuals, Dekker's
+// fast two-sum) plus the rest of the Taylor series in single precision
+// (truncated below 2^-54 relative).  The result is the correctly rounded
+// sine / cosine unless that lies within about 2^-43 (relative) of a rounding
+// boundary, the same values as evaluating in double and rounding.  Larger
+// angles are evaluated in double.
+__device__ __forceinline__ void sinCosAngle(float x, float& s, float& c)
+{
+	if(!(fabsf(x) <= 0.125f))
+	{
+		double ds, dc;
+		sincos(double(x), &ds, &dc);
+		s = float(ds);
+		c = float(dc);
+		return;
+	}
+	const float SIXTH_HI = 0.1666666716337204f, SIXTH_LO = -4.967053879312289e-09f;   // 1/6 = HI + LO to 2^-52
+	const float x2 = x * x;
+	const float x2e = fmaf(x, x, -x2);                  // x^2 = x2 + x2e exactly
+	const float x3 = x2 * x;
+	const float x3e = fmaf(x2, x, -x3) + x2e * x;       // x^3 = x3 + x3e
+	const float t = x3 * SIXTH_HI;
+	const float te = fmaf(x3, SIXTH_HI, -t) + (x3 * SIXTH_LO + x3e * SIXTH_HI);   // x^3/6 = t + te
+	const float hs = x3 * x2 * (1.0f / 120.0f - x2 * (1.0f / 5040.0f - x2 * (1.0f / 362880.0f)));
+	const float sh = x - t;
+	const float se = (x - sh) - t;                      // x - t = sh + se exactly (|x| >= |t|)
+	s = sh + ((se - te) + hs);
+	const float a = 0.5f * x2, ae = 0.5f * x2e;         // x^2/2 = a + ae exactly
+	const float hc = x2 * x2 * (1.0f / 24.0f - x2 * (1.0f / 720.0f - x2 * (1.0f / 40320.0f - x2 * (1.0f / 3628800.0f))));
+	const float ch = 1.0f - a;
+	const float ce = (1.0f - ch) - a;                   // 1 - a = ch + ce exactly
+	c = ch + ((ce - ae) + hc);
+}
 __device__ __forceinline__ V3 unitX() { return v3(1, 0, 0); }
 __device__ __forceinline__ V3 zero3() { return v3(0, 0, 0); }
 __device__ __forceinline__ float getc(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
