@@ -812,6 +812,7 @@ def main():
                                           solve=SOLVE_VARIANTS[getattr(w, "solve_variant", 8)],
                                           prep_blocks_per_sm=tuning["prep_blocks_per_sm"],
                                           narrowphase_blocks_per_sm=tuning["narrowphase_blocks_per_sm"],
+                                          resident_stream_levels=tuning["resident_stream"],
                                           sample_ms_per_step=tuned_ms),
                             l2="inputs larger than L2: resident scene state %.0f MB per GPU" % (info["device_bytes"] / 1e6),
                             parallelism="scene-sharded replicas" if a.gpus > 1 else "single GPU"),

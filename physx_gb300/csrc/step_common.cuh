@@ -20,6 +20,7 @@ struct StepParams
 	uint32_t largeBodies;  // scenes of more solver bodies run one block per scene (world)
 	uint32_t solveVariant; // solve kernel of the world: the resident solve, or a staging variant of the warp-per-scene solve
 	uint32_t resBytes;     // shared-memory workspace of one resident-solve block (world)
+	uint32_t resStream;    // resident solve: levels a scene may go deeper with its rows streamed through a two-slot ring
 };
 
 // no slot in last step's pair list (a new pair)

@@ -73,6 +73,21 @@ __host__ __device__ __forceinline__ uint32_t residentBytes(uint32_t nc, uint32_t
 {
 	return RES_HEADER + align16(2 * nc) + align16(48 * nTot) + 16 * rowChunks;
 }
+// Streamed rows (a scene whose rows do not fit its slice): each iteration's
+// rows arrive chunk by chunk (consecutive constraints of one partition, at
+// most a ring slot) in a two-slot ring, the next chunk's bulk copies running
+// while the current one is solved; the solve writes each constraint's
+// impulses back to its record in HBM, where the next iteration's copy reads
+// them.  Footprint: partition ends, row offsets, velocities, the chunk table
+// and two slots of at least RES_MIN_SLOT bytes.
+constexpr uint32_t RES_MAX_CHUNKS = 256;   // chunks of one iteration
+constexpr uint32_t RES_TABLE = (RES_MAX_CHUNKS + 1 + MAX_PARTITIONS + 1 + 2) * 4;   // chunk starts, first chunk per partition, total
+constexpr uint32_t RES_MIN_SLOT = 16384;
+constexpr uint32_t RES_RECORD_UNITS = 56;  // 16-byte units of the largest constraint record
+__host__ __device__ __forceinline__ uint32_t residentStreamBytes(uint32_t nc, uint32_t nTot)
+{
+	return RES_HEADER + align16(2 * nc) + align16(48 * nTot) + align16(RES_TABLE) + 2 * RES_MIN_SLOT;
+}
 // Smallest slice (deepest level) that holds `need` bytes; level 0 also takes
 // scenes too large for any slice (their rows stay in HBM).
 __host__ __device__ __forceinline__ uint32_t residentLevel(uint32_t need, uint32_t resBytes)
@@ -875,8 +890,13 @@ __device__ __forceinline__ void residentCount(const WorldDev& w, uint32_t slot, 
 	if(uint32_t(old >> 32) + 1u == nc)
 	{
 		const SceneDesc sc = w.scenes[sid];
-		const uint32_t need = residentBytes(nc, sc.nbBodies + sc.nbStatics, uint32_t(old) + chunks);
-		residentAppend(w, sid, residentLevel(need, sp.resBytes));
+		const uint32_t nTot = sc.nbBodies + sc.nbStatics;
+		uint32_t level = residentLevel(residentBytes(nc, nTot, uint32_t(old) + chunks), sp.resBytes);
+		// streamed rows: up to resStream levels deeper (groups of two warps at least),
+		// so more scenes are in flight per SM
+		for(uint32_t d = 0; d < sp.resStream && level + 2 < RES_LEVELS && residentStreamBytes(nc, nTot) <= (sp.resBytes >> (level + 1)); d++)
+			level++;
+		residentAppend(w, sid, level);
 	}
 }
 
@@ -1191,6 +1211,8 @@ __device__ __forceinline__ void bulkCopyToShared(void* dst, const void* src, uin
 }
 // Orders this thread's earlier shared-memory accesses before later bulk copies into them.
 __device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// Orders this thread's earlier global writes before later bulk copies that read them.
+__device__ __forceinline__ void fenceProxyAsyncGlobal() { asm volatile("fence.proxy.async.global;\n" ::: "memory"); }
 // try_wait rounds before a bulk copy counts as lost (each round may suspend the
 // thread for a while; this is well above a second)
 constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 22;
@@ -1345,6 +1367,154 @@ __device__ __forceinline__ void residentIterate(const WorldDev& w, const SceneDe
 	}
 }
 
+// The iterations of residentIterate for a scene with streamed rows.  table:
+// chunkFirst[0..nChunks] (first constraint of each chunk, then nc) followed by
+// the first chunk of each partition; off: each constraint's row offset (16-byte
+// units) from the scene's first row, total: all rows; slots: the two ring slots
+// of slotBytes; bars / phase: the two slot barriers and the parity each waits
+// for next.  Returns false when a bulk copy did not complete within the wait
+// limit (after a bounded wait for the copies in flight).
+template <typename Vel>
+__device__ __forceinline__ bool residentIterateStreamed(const WorldDev& w, const SceneDesc& sc, uint32_t sid, const StepParams& sp,
+                                                        const uint32_t* ends, uint32_t nbPart, const uint16_t* off, uint32_t total,
+                                                        const uint32_t* chunkFirst, uint32_t nChunks, unsigned char* slot0, uint32_t slotBytes,
+                                                        const Vel& V, uint32_t gtid, uint32_t nt, uint32_t barId, unsigned long long* bars,
+                                                        uint32_t* phase, uint32_t* word)
+{
+	const uint32_t n = sc.nbBodies, nc = ends[nbPart - 1];
+	tgs::BodyTx* tx = w.tx + sc.solverStart;
+	Tr* pose = w.pose + sc.solverStart;
+	tgs::ConstraintRecord* recs = w.recs + sc.pairStart;
+	const uint32_t nIter = sp.nbPos + sp.nbVel, nSeq = nIter * nChunks;
+	const uint32_t ph0 = phase[0], ph1 = phase[1];
+	auto unitEnd = [&](uint32_t r) -> uint32_t { return r < nc ? uint32_t(off[r]) : total; };
+	// bulk copies of chunk g of the sequence (iteration g / nChunks) into slot g & 1
+	auto issue = [&](uint32_t g) {
+		const uint32_t j = g % nChunks, sl = g & 1u;
+		const uint32_t c0 = chunkFirst[j], c1 = chunkFirst[j + 1];
+		const uint32_t u0 = off[c0];
+		unsigned char* dst = slot0 + size_t(sl) * slotBytes;
+		if(gtid == 0) mbarArriveExpectTx(&bars[sl], 16u * (unitEnd(c1) - u0));
+		for(uint32_t r = c0 + gtid; r < c1; r += nt)
+			bulkCopyToShared(dst + 16u * (off[r] - u0), recs + r, 16u * (unitEnd(r + 1) - off[r]), &bars[sl]);
+	};
+	// bounded wait for chunk g, voted over the group
+	auto ready = [&](uint32_t g) -> bool {
+		const uint32_t sl = g & 1u, parity = (sl ? ph1 : ph0) ^ ((g >> 1) & 1u);
+		bool done = false;
+		for(uint32_t k = 0; k < STAGE_WAIT_LIMIT && !done; k++) done = mbarTryWait(&bars[sl], parity);
+		if(!__all_sync(0xffffffffu, done) && (gtid & 31) == 0) atomicOr(word, 1u);
+		groupSync(barId, nt);
+		return *word == 0;
+	};
+	auto fail = [&](uint32_t g) {
+		// a copy is lost: flag the scene and give the copies in flight a last bounded wait
+		if(gtid == 0) atomicOr(&w.status[sid], ST_STAGE_TIMEOUT);
+		for(uint32_t h = g; h < g + 2 && h < nSeq; h++)
+		{
+			const uint32_t sl = h & 1u, parity = (sl ? ph1 : ph0) ^ ((h >> 1) & 1u);
+			bool done = false;
+			for(uint32_t k = 0; k < STAGE_WAIT_LIMIT && !done; k++) done = mbarTryWait(&bars[sl], parity);
+		}
+	};
+	const float stepDt = sp.dt / float(sp.nbPos);
+	float elapsed = 0.0f;
+	uint32_t g = 0;
+	issue(0);
+	for(uint32_t it = 0; it < nIter; it++)
+	{
+		const bool posIter = it < sp.nbPos;
+		const bool lastIter = it + 1 == nIter;
+		const float minPen = posIter ? -FLT_MAX : 0.0f;
+		for(uint32_t j = 0; j < nChunks; j++, g++)
+		{
+			if(!ready(g)) { fail(g); return false; }
+			// slot (g + 1) & 1 held chunk g - 1, solved before the last barrier
+			if(g + 1 < nSeq) issue(g + 1);
+			unsigned char* base = slot0 + size_t(g & 1u) * slotBytes;
+			const uint32_t c0 = chunkFirst[j], c1 = chunkFirst[j + 1], u0 = off[c0];
+			for(uint32_t r = c0 + gtid; r < c1; r += nt)
+			{
+				tgs::ConstraintRecord* rec = reinterpret_cast<tgs::ConstraintRecord*>(base + 16u * (off[r] - u0));
+				if(rec->nbPatches == 0) continue;
+				const uint32_t a = uint32_t(rec->bodyA), b = uint32_t(rec->bodyB);
+				tgs::BodyVel b0, b1;
+				b0.lin = V.lin(a); b0.ang = V.ang(a); b0.dLin = V.dLin(a); b0.dAng = V.dAng(a);
+				b1.lin = V.lin(b); b1.ang = V.ang(b); b1.dLin = V.dLin(b); b1.dAng = V.dAng(b);
+				const bool dynB = b < n;
+				uint32_t broken = 0;
+				tgs::solveRecord(*rec, b0, b1, dynB, minPen, elapsed, sp.persistent && lastIter ? &broken : nullptr);
+				// the impulses go back to the record in HBM for the next iteration's copy
+				const float* src = rec->force();
+				float* dst = reinterpret_cast<float*>(reinterpret_cast<char*>(recs + r) + (reinterpret_cast<const char*>(src) - reinterpret_cast<const char*>(rec)));
+				const int nImp = rec->nbPoints() + rec->nbFriction();
+				for(int i = 0; i < nImp; i++) dst[i] = src[i];
+				if(broken)
+				{
+					tgs::FrictionState& fs = w.frictionState[w.sceneParity[sid] ^ 1u][sc.pairStart + w.ordered[sc.pairStart + r]];
+					tgs::ConstraintRecord* group[4] = {nullptr, nullptr, nullptr, nullptr};
+					if(rec->isBlock())
+					{
+						// the header's lanes (consecutive constraints of the partition) read in HBM:
+						// only their patch and friction counts are used
+						uint32_t pb = 0;
+						while(ends[pb] <= r) pb++;
+						const uint32_t begin = pb ? ends[pb - 1] : 0u;
+						const uint32_t r0 = begin + ((r - begin) & ~3u);
+						for(uint32_t l = 0; l < 4; l++) group[l] = recs + r0 + l;
+					}
+					for(int pi = 0; pi < rec->nbPatches; pi++)
+						if(broken & (1u << pi))
+						{
+							const int slotIdx = rec->isBlock() ? tgs::blockBrokenSlot(group, pi) : pi;
+							if(uint32_t(slotIdx) < fs.count) fs.patches[slotIdx].broken = 1;
+						}
+				}
+				V.set(a, b0.lin, b0.ang);
+				if(dynB) V.set(b, b1.lin, b1.ang);
+			}
+			// this chunk's slot is overwritten by a later bulk copy; its records' impulses
+			// are read by one
+			fenceProxyAsync();
+			fenceProxyAsyncGlobal();
+			groupSync(barId, nt);
+		}
+		if(posIter)
+		{
+			for(uint32_t i = gtid; i < n; i += nt)
+			{
+				tgs::BodyVel v;
+				v.lin = V.lin(i); v.ang = V.ang(i); v.dLin = V.dLin(i); v.dAng = V.dAng(i);
+				tgs::integrateStep(v, tx[i], stepDt);
+				V.setDelta(i, v.dLin, v.dAng);
+			}
+			elapsed += stepDt;
+			groupSync(barId, nt);
+		}
+	}
+	for(uint32_t i = gtid; i < n; i += nt)
+	{
+		tgs::BodyVel v;
+		v.lin = V.lin(i); v.ang = V.ang(i); v.dLin = V.dLin(i); v.dAng = V.dAng(i);
+		Tr p = pose[i];
+		V3 wv;
+		tgs::finalizeBody(v, tx[i], p, wv);
+		tgs::RigidBody& rb = w.bodies[sc.bodyStart + i];
+		rb.linVel[0] = v.lin.x; rb.linVel[1] = v.lin.y; rb.linVel[2] = v.lin.z;
+		rb.angVel[0] = wv.x; rb.angVel[1] = wv.y; rb.angVel[2] = wv.z;
+		rb.q[0] = p.q.x; rb.q[1] = p.q.y; rb.q[2] = p.q.z; rb.q[3] = p.q.w;
+		rb.p[0] = p.p.x; rb.p[1] = p.p.y; rb.p[2] = p.p.z;
+	}
+	// parities after this scene's fills (slot 0: ceil(nSeq / 2), slot 1: floor)
+	groupSync(barId, nt);
+	if(gtid == 0)
+	{
+		phase[0] = ph0 ^ (((nSeq + 1) >> 1) & 1u);
+		phase[1] = ph1 ^ ((nSeq >> 1) & 1u);
+	}
+	return true;
+}
+
 // Per-group state of the resident solve kept in static shared memory.
 struct ResGroupState
 {
@@ -1384,6 +1554,11 @@ __device__ __forceinline__ bool solveResidentScene(const WorldDev& w, uint32_t s
 		const uint32_t first = groupPrefix(runChunks, gs.scratch, gtid, nt, barId, total);
 		const bool velOnChip = RES_HEADER + offBytes + velBytes <= sliceBytes;
 		const bool rowsOnChip = velOnChip && RES_HEADER + offBytes + velBytes + 16u * total <= sliceBytes;
+		// streamed rows: a two-slot ring after the chunk table
+		const uint32_t tableOff = RES_HEADER + offBytes + velBytes, ringOff = tableOff + align16(RES_TABLE);
+		const uint32_t slotBytes = ringOff < sliceBytes ? ((sliceBytes - ringOff) / 2u) & ~15u : 0u;
+		bool stream = sp.resStream && velOnChip && !rowsOnChip && nt >= 64 && nbPart > 0 && total > 0 && total <= 65535u &&
+		              slotBytes >= RES_MIN_SLOT;
 		// the slice was last read by generic loads (previous scene): order them
 		// before the bulk copies that overwrite it
 		fenceProxyAsync();
@@ -1401,6 +1576,66 @@ __device__ __forceinline__ bool solveResidentScene(const WorldDev& w, uint32_t s
 				bulkCopyToShared(rows + 16u * o, w.recs + sc.pairStart + r, 16u * c, gs.bar);
 				o += c;
 			}
+		}
+		uint32_t* chunkFirst = reinterpret_cast<uint32_t*>(slice + tableOff);
+		uint32_t* partChunk = chunkFirst + RES_MAX_CHUNKS + 1;
+		uint32_t nChunks = 0;
+		if(stream)
+		{
+			uint32_t o = first;
+			for(uint32_t r = r0; r < r1; r++)
+			{
+				off[r] = uint16_t(o);
+				o += chunks[r];
+			}
+			groupSync(barId, nt);
+			// chunk k of partition p: its constraints whose rows start in
+			// [k, k + 1) * capU units after the partition's first row (at most a slot)
+			const uint32_t capU = slotBytes / 16u - RES_RECORD_UNITS;
+			if(gtid < 32)
+			{
+				uint32_t carry = 0;
+				for(uint32_t p0 = 0; p0 < nbPart; p0 += 32)
+				{
+					const uint32_t p = p0 + gtid;
+					uint32_t cnt = 0;
+					if(p < nbPart)
+					{
+						const uint32_t b = p ? ends[p - 1] : 0u, e = ends[p];
+						if(e > b) cnt = uint32_t(off[e - 1] - off[b]) / capU + 1u;
+					}
+					uint32_t incl = cnt;
+					for(int d = 1; d < 32; d <<= 1)
+					{
+						const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+						if(gtid >= uint32_t(d)) incl += t;
+					}
+					if(p < nbPart) partChunk[p] = carry + incl - cnt;
+					carry += __shfl_sync(0xffffffffu, incl, 31);
+				}
+				if(gtid == 0) partChunk[nbPart] = carry;
+			}
+			groupSync(barId, nt);
+			nChunks = partChunk[nbPart];
+			stream = nChunks <= RES_MAX_CHUNKS;
+			if(stream)
+			{
+				for(uint32_t r = gtid; r < nc; r += nt)
+				{
+					uint32_t lo = 0, hi = nbPart - 1;   // partition of r: first p with ends[p] > r
+					while(lo < hi)
+					{
+						const uint32_t mid = (lo + hi) >> 1;
+						if(ends[mid] > r) hi = mid;
+						else lo = mid + 1;
+					}
+					const uint32_t b = lo ? ends[lo - 1] : 0u;
+					const uint32_t k = uint32_t(off[r] - off[b]) / capU;
+					if(r == b || k != uint32_t(off[r - 1] - off[b]) / capU) chunkFirst[partChunk[lo] + k] = r;
+				}
+				if(gtid == 0) chunkFirst[nChunks] = nc;
+			}
+			groupSync(barId, nt);
 		}
 		const ResVel rv = {velBase, velBase + nTot, velBase + 2 * nTot, velBase + 3 * nTot};
 		if(velOnChip)
@@ -1434,6 +1669,12 @@ __device__ __forceinline__ bool solveResidentScene(const WorldDev& w, uint32_t s
 		}
 		groupSync(barId, nt);
 		if(rowsOnChip) residentIterate<true>(w, sc, sid, sp, ends, nbPart, off, rows, rv, gtid, nt, barId);
+		else if(stream)
+		{
+			if(!residentIterateStreamed(w, sc, sid, sp, ends, nbPart, off, total, chunkFirst, nChunks, slice + ringOff, slotBytes, rv, gtid, nt,
+			                            barId, gs.bar, gs.phase, gs.word))
+				return false;
+		}
 		else if(velOnChip) residentIterate<false>(w, sc, sid, sp, ends, nbPart, off, rows, rv, gtid, nt, barId);
 		else residentIterate<false>(w, sc, sid, sp, ends, nbPart, off, rows, ResHbmVel{w.vel + sc.solverStart}, gtid, nt, barId);
 	}
@@ -2022,6 +2263,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
 	sp.resBytes = 0;       // set at creation
+	sp.resStream = 0;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -2283,7 +2525,7 @@ std::string histogramKey(const std::vector<gbpx::world::SceneDesc>& sc)
 // as fit)
 struct Tuning
 {
-	uint32_t largeBodies, solveVariant, prepPerSm, npHeavyPerSm;
+	uint32_t largeBodies, solveVariant, prepPerSm, npHeavyPerSm, resStream;
 };
 std::map<std::string, Tuning>& tunedConfigs()
 {
@@ -2292,6 +2534,7 @@ std::map<std::string, Tuning>& tunedConfigs()
 }
 } // namespace
 
+GBPX_API int gbpx_world_set_resident_stream(void* wv, uint32_t levels);
 GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps, uint32_t* outLargeBodies, uint32_t* outSolveVariant,
                                  float* outMs)
 {
@@ -2308,6 +2551,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		if(outMs) *outMs = 0.0f;
 		int rc = gbpx_world_set_large_bodies(wv, c.largeBodies);
 		rc = rc ? rc : gbpx_world_set_solve_variant(wv, c.solveVariant);
+		rc = rc ? rc : gbpx_world_set_resident_stream(wv, c.resStream);
 		return rc ? rc : gbpx_world_set_occupancy(wv, c.prepPerSm, c.npHeavyPerSm);
 	}
 	// size-stratified sample: every k-th scene in order of size
@@ -2348,6 +2592,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	                   sp7.empty() ? nullptr : sp7.data(), sty.empty() ? nullptr : sty.data(),
 	                   sge.empty() ? nullptr : reinterpret_cast<const float*>(sge.data()), w->pairsPerBody, w->params);
 	if(rc) { t->release(); delete t; return rc; }
+	t->params.resStream = 0;
 	// candidates that classify the sample differently
 	const uint32_t cands[] = {64u, 128u, 256u, 512u, 1024u, 2048u, 0xffffffffu};
 	std::vector<uint32_t> sizes;
@@ -2392,6 +2637,17 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		rc = timeConfig(best, v, ms);
 		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
 	}
+	// the resident solve's streamed-row levels
+	uint32_t bestStream = 0;
+	if(bestVariant == gbpx::world::RESIDENT_VARIANT)
+		for(uint32_t d = 1; d <= 2 && !rc; d++)
+		{
+			t->params.resStream = d;
+			float ms = 0.0f;
+			rc = timeConfig(best, bestVariant, ms);
+			if(!rc && ms < bestMs) { bestMs = ms; bestStream = d; }
+		}
+	t->params.resStream = bestStream;
 	// then the blocks per SM of the row preparation (rows per CTA wave) and of the
 	// two heavy narrowphase kinds (pairs per CTA wave), one after the other
 	uint32_t bestPrep = t->prepPerSm, bestNp = t->npHeavyPerSm;
@@ -2417,25 +2673,46 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	t->release();
 	delete t;
 	if(rc) return rc;
-	cache[key] = Tuning{best, bestVariant, bestPrep, bestNp};
+	cache[key] = Tuning{best, bestVariant, bestPrep, bestNp, bestStream};
 	*outLargeBodies = best;
 	*outSolveVariant = bestVariant;
 	if(outMs) *outMs = bestMs / float(steps);
 	rc = gbpx_world_set_large_bodies(wv, best);
 	rc = rc ? rc : gbpx_world_set_solve_variant(wv, bestVariant);
+	rc = rc ? rc : gbpx_world_set_resident_stream(wv, bestStream);
 	return rc ? rc : gbpx_world_set_occupancy(wv, bestPrep, bestNp);
 }
 
 // The world's current tuning: out4 = block-per-scene threshold, solve kernel,
 // preparation blocks per SM, heavy narrowphase blocks per SM (0 = as many as fit).
-GBPX_API int gbpx_world_tuning(void* wv, uint32_t* out4)
+GBPX_API int gbpx_world_tuning(void* wv, uint32_t* out5)
 {
 	World* w = static_cast<World*>(wv);
-	if(!w || !out4) return GBPX_ERR_INVALID;
-	out4[0] = w->params.largeBodies;
-	out4[1] = w->params.solveVariant;
-	out4[2] = w->prepPerSm;
-	out4[3] = w->npHeavyPerSm;
+	if(!w || !out5) return GBPX_ERR_INVALID;
+	out5[0] = w->params.largeBodies;
+	out5[1] = w->params.solveVariant;
+	out5[2] = w->prepPerSm;
+	out5[3] = w->npHeavyPerSm;
+	out5[4] = w->params.resStream;
+	return GBPX_OK;
+}
+
+// Streamed rows in the resident solve (0, the default, .. 3): a scene may be
+// solved up to `levels` levels deeper than its rows and velocities allow (by a
+// group of at least two warps) with its rows streamed chunk by chunk through a
+// two-slot ring in its slice, so more scenes are in flight per SM; scenes too
+// large for any slice stream their rows too.  Results do not depend on it.
+GBPX_API int gbpx_world_set_resident_stream(void* wv, uint32_t levels)
+{
+	World* w = static_cast<World*>(wv);
+	if(!w || levels + 1 >= gbpx::world::RES_LEVELS) return GBPX_ERR_INVALID;
+	GBPX_CUDA_TRY(cudaStreamSynchronize(w->stream));
+	w->params.resStream = levels;
+	if(w->graphExec)
+	{
+		cudaGraphExecDestroy(w->graphExec);
+		w->graphExec = nullptr;
+	}
 	return GBPX_OK;
 }
 
@@ -2886,6 +3163,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
 	sp.resBytes = 0;       // set at creation
+	sp.resStream = 0;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp, lanesPerClass);

@@ -165,12 +165,20 @@ class World:
         return t.value, ms.value
 
     def tuning(self):
-        """{large_bodies, solve_variant, prep_blocks_per_sm, narrowphase_blocks_per_sm} in force
-        (the autotuner's choice, or what was set by hand; 0 blocks per SM = as many as fit)."""
-        out = np.zeros(4, np.uint32)
+        """{large_bodies, solve_variant, prep_blocks_per_sm, narrowphase_blocks_per_sm,
+        resident_stream} in force (the autotuner's choice, or what was set by hand; 0
+        blocks per SM = as many as fit)."""
+        out = np.zeros(5, np.uint32)
         check(self._L.gbpx_world_tuning(self._h, _p(out)), "gbpx_world_tuning")
         return dict(large_bodies=int(out[0]), solve_variant=int(out[1]), prep_blocks_per_sm=int(out[2]),
-                    narrowphase_blocks_per_sm=int(out[3]))
+                    narrowphase_blocks_per_sm=int(out[3]), resident_stream=int(out[4]))
+
+    def set_resident_stream(self, levels):
+        """Streamed rows in the resident solve (0-3): scenes may go up to `levels`
+        levels deeper, their rows streamed through a two-slot ring; results do not
+        depend on it."""
+        self._L.gbpx_world_set_resident_stream.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        check(self._L.gbpx_world_set_resident_stream(self._h, int(levels)), "gbpx_world_set_resident_stream")
 
     def set_occupancy(self, prep_blocks_per_sm=0, narrowphase_blocks_per_sm=0):
         """Persistent blocks per SM of the row preparation and of the capsule-box and

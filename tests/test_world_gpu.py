@@ -218,8 +218,10 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
     assert b.tuning() == a.tuning()   # the cached choice includes the occupancies
     t = a.tuning()
     assert t["prep_blocks_per_sm"] in (0, 2, 3, 4) and t["narrowphase_blocks_per_sm"] in (0, 1, 2, 3)
+    assert t["resident_stream"] in (0, 1, 2)
     b.set_large_bodies(512)
     b.set_occupancy(0, 0)
+    b.set_resident_stream(0)
     a.step(10)
     b.step(10)
     assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
@@ -229,14 +231,16 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
 
 def test_world_occupancy_keeps_results(cuda_device):
     """The blocks per SM of the row preparation and the heavy narrowphase kernels
-    (what the autotuner chooses after the threshold and the solve) do not change
-    any result."""
+    and the streamed-row levels of the resident solve (what the autotuner
+    chooses after the threshold and the solve) do not change any result."""
     from physx_gb300.workloads import batched_scenes
     from physx_gb300.world import World
-    scenes = batched_scenes(144, 96, nmin=16, nmax=512)
-    worlds = [World(scenes) for _ in range(3)]
+    scenes = batched_scenes(144, 96, nmin=16, nmax=1024)
+    worlds = [World(scenes) for _ in range(6)]
     worlds[1].set_occupancy(2, 1)
     worlds[2].set_occupancy(4, 3)
+    for w, d in zip(worlds[3:], (1, 2, 3)):
+        w.set_resident_stream(d)
     for _ in range(15):
         for w in worlds:
             w.step(1)
