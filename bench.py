@@ -35,7 +35,7 @@ SOLVE_VARIANTS = ["warp per scene, rows in place, velocities on chip", "warp per
                   "warp per scene, 512 B staging per lane, velocities on chip", "warp per scene, rows in place, velocities in HBM",
                   "warp per scene, 256 B staging per lane, velocities in HBM", "warp per scene, 512 B staging per lane, velocities in HBM",
                   "warp per scene, 400 B staging per lane, velocities on chip", "warp per scene, 400 B staging per lane, velocities in HBM",
-                  "resident: rows and velocities on chip for all iterations, bulk-copied once"]
+                  "resident: velocities on chip; rows bulk-copied on chip once, or streamed through a two-slot ring"]
 
 
 def parse():

@@ -357,13 +357,13 @@ int gbpx_world_autotune(void* world, uint32_t sampleScenes, uint32_t steps, uint
  * preparation and heavy narrowphase blocks per SM (0 = as many as fit),
  * streamed-row levels of the resident solve. */
 int gbpx_world_tuning(void* world, uint32_t* out5);
-/* Streamed rows in the resident solve (0 = default .. 3): a scene may be
- * solved up to `levels` levels deeper than its on-chip footprint allows (by a
- * group of at least two warps), its rows streamed chunk by chunk (consecutive
- * constraints of one partition) through a two-slot ring of bulk copies while
- * the previous chunk is solved, so more scenes are in flight per SM; scenes
- * too large for any slice stream their rows too.  The autotuner sets it after
- * the solve kernel.  Results do not depend on it. */
+/* Streamed rows in the resident solve (0 .. 3, default 1): a scene whose
+ * on-chip footprint needs a level above `levels` is solved one level deeper
+ * (by a group of at least two warps), its rows streamed chunk by chunk
+ * (consecutive constraints of one partition) through a two-slot ring of bulk
+ * copies while the previous chunk is solved, so more scenes are in flight per
+ * SM; scenes too large for any slice stream their rows too (levels > 0).  The
+ * autotuner sets it after the solve kernel.  Results do not depend on it. */
 int gbpx_world_set_resident_stream(void* world, uint32_t levels);
 /* Workspace of the warp-per-scene solve: variants 0-2 keep the body
  * velocities in shared memory and stage rows in 0 / 256 / 512 bytes per lane

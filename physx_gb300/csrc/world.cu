@@ -892,10 +892,9 @@ __device__ __forceinline__ void residentCount(const WorldDev& w, uint32_t slot, 
 		const SceneDesc sc = w.scenes[sid];
 		const uint32_t nTot = sc.nbBodies + sc.nbStatics;
 		uint32_t level = residentLevel(residentBytes(nc, nTot, uint32_t(old) + chunks), sp.resBytes);
-		// streamed rows: up to resStream levels deeper (groups of two warps at least),
-		// so more scenes are in flight per SM
-		for(uint32_t d = 0; d < sp.resStream && level + 2 < RES_LEVELS && residentStreamBytes(nc, nTot) <= (sp.resBytes >> (level + 1)); d++)
-			level++;
+		// streamed rows: a scene filed above level resStream goes one level deeper
+		// (groups of two warps at least), so more scenes are in flight per SM
+		if(level < sp.resStream && level + 2 < RES_LEVELS && residentStreamBytes(nc, nTot) <= (sp.resBytes >> (level + 1))) level++;
 		residentAppend(w, sid, level);
 	}
 }
@@ -1787,6 +1786,7 @@ struct World
 	uint32_t pairsPerBody = 0;
 	// scenes above this many solver bodies run one block per scene (warp per scene below)
 	static constexpr uint32_t DEFAULT_LARGE_BODIES = 512;
+	static constexpr uint32_t DEFAULT_RES_STREAM = 1;   // streamed-row levels of the resident solve
 	static constexpr uint32_t BIG_THREADS = world::BIG_WARPS * 32;
 	static constexpr uint32_t RES_THREADS = world::RES_WARPS * 32;
 	bool resident() const { return params.solveVariant == world::RESIDENT_VARIANT; }
@@ -2263,7 +2263,7 @@ GBPX_API int gbpx_world_create(uint32_t nbScenes, const uint32_t* sceneBodyCount
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
 	sp.resBytes = 0;       // set at creation
-	sp.resStream = 0;
+	sp.resStream = World::DEFAULT_RES_STREAM;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	for(uint32_t s = 0, b = 0; s < nbScenes; s++)
 		for(uint32_t i = 0; i < sceneBodyCount[s]; i++, b++)
@@ -2592,7 +2592,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 	                   sp7.empty() ? nullptr : sp7.data(), sty.empty() ? nullptr : sty.data(),
 	                   sge.empty() ? nullptr : reinterpret_cast<const float*>(sge.data()), w->pairsPerBody, w->params);
 	if(rc) { t->release(); delete t; return rc; }
-	t->params.resStream = 0;
+	t->params.resStream = World::DEFAULT_RES_STREAM;
 	// candidates that classify the sample differently
 	const uint32_t cands[] = {64u, 128u, 256u, 512u, 1024u, 2048u, 0xffffffffu};
 	std::vector<uint32_t> sizes;
@@ -2638,10 +2638,11 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
 	}
 	// the resident solve's streamed-row levels
-	uint32_t bestStream = 0;
+	uint32_t bestStream = World::DEFAULT_RES_STREAM;
 	if(bestVariant == gbpx::world::RESIDENT_VARIANT)
-		for(uint32_t d = 1; d <= 2 && !rc; d++)
+		for(uint32_t d = 0; d <= 2 && !rc; d++)
 		{
+			if(d == World::DEFAULT_RES_STREAM) continue;
 			t->params.resStream = d;
 			float ms = 0.0f;
 			rc = timeConfig(best, bestVariant, ms);
@@ -2697,11 +2698,12 @@ GBPX_API int gbpx_world_tuning(void* wv, uint32_t* out5)
 	return GBPX_OK;
 }
 
-// Streamed rows in the resident solve (0, the default, .. 3): a scene may be
-// solved up to `levels` levels deeper than its rows and velocities allow (by a
+// Streamed rows in the resident solve (0 .. 3, default 1): a scene whose rows
+// and velocities need a level above `levels` is solved one level deeper (by a
 // group of at least two warps) with its rows streamed chunk by chunk through a
 // two-slot ring in its slice, so more scenes are in flight per SM; scenes too
-// large for any slice stream their rows too.  Results do not depend on it.
+// large for any slice stream their rows too (levels > 0).  Results do not
+// depend on it.
 GBPX_API int gbpx_world_set_resident_stream(void* wv, uint32_t levels)
 {
 	World* w = static_cast<World*>(wv);
@@ -3163,7 +3165,7 @@ GBPX_API int gbpx_server_create(uint32_t nbClasses, const uint32_t* capacity, co
 	sp.largeBodies = World::DEFAULT_LARGE_BODIES;
 	sp.solveVariant = gbpx::world::RESIDENT_VARIANT;
 	sp.resBytes = 0;       // set at creation
-	sp.resStream = 0;
+	sp.resStream = World::DEFAULT_RES_STREAM;
 	if(!(sp.dt > 0.0f) || !(sp.contactDistance > 0.0f)) return GBPX_ERR_INVALID;
 	Server* s = new Server;
 	const int rc = s->create(nbClasses, capacity, slots, staticsPerSlot, pairsPerBody, sp, lanesPerClass);

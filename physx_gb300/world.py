@@ -174,9 +174,9 @@ class World:
                     narrowphase_blocks_per_sm=int(out[3]), resident_stream=int(out[4]))
 
     def set_resident_stream(self, levels):
-        """Streamed rows in the resident solve (0-3): scenes may go up to `levels`
-        levels deeper, their rows streamed through a two-slot ring; results do not
-        depend on it."""
+        """Streamed rows in the resident solve (0-3, default 1): scenes filed above
+        level `levels` go one level deeper, their rows streamed through a two-slot
+        ring; results do not depend on it."""
         self._L.gbpx_world_set_resident_stream.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         check(self._L.gbpx_world_set_resident_stream(self._h, int(levels)), "gbpx_world_set_resident_stream")
 

@@ -221,7 +221,7 @@ def test_world_autotune_picks_a_threshold_and_keeps_results(cuda_device):
     assert t["resident_stream"] in (0, 1, 2)
     b.set_large_bodies(512)
     b.set_occupancy(0, 0)
-    b.set_resident_stream(0)
+    b.set_resident_stream(1)
     a.step(10)
     b.step(10)
     assert a.get_bodies().tobytes() == b.get_bodies().tobytes()
@@ -239,7 +239,7 @@ def test_world_occupancy_keeps_results(cuda_device):
     worlds = [World(scenes) for _ in range(6)]
     worlds[1].set_occupancy(2, 1)
     worlds[2].set_occupancy(4, 3)
-    for w, d in zip(worlds[3:], (1, 2, 3)):
+    for w, d in zip(worlds[3:], (0, 2, 3)):
         w.set_resident_stream(d)
     for _ in range(15):
         for w in worlds:
