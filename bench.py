@@ -681,7 +681,7 @@ def main():
         w.set_large_bodies(a.large_bodies)
         tuned_threshold, tuned_ms = a.large_bodies, 0.0
     else:
-        tuned_threshold, tuned_ms = w.autotune(steps=3)
+        tuned_threshold, tuned_ms = w.autotune(steps=6)
     tuning = w.tuning()
     w.step(a.warmup, graph=True)
     w.synchronize()

@@ -2614,6 +2614,9 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		GBPX_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
 		return GBPX_OK;
 	};
+	// a later candidate replaces the incumbent only when it is at least 1 % faster
+	// (a few steps' timing varies by about that much)
+	const float TUNE_MARGIN = 0.99f;
 	// the threshold first (default staging), then the staging slot at that threshold
 	uint32_t best = w->params.largeBodies, bestVariant = w->params.solveVariant;
 	float bestMs = 3.4e38f;
@@ -2635,7 +2638,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		if(v == bestVariant || (v != gbpx::world::RESIDENT_VARIANT && !anySmall)) continue;
 		float ms = 0.0f;
 		rc = timeConfig(best, v, ms);
-		if(!rc && ms < bestMs) { bestMs = ms; bestVariant = v; }
+		if(!rc && ms < bestMs * TUNE_MARGIN) { bestMs = ms; bestVariant = v; }
 	}
 	// the resident solve's streamed-row levels
 	uint32_t bestStream = World::DEFAULT_RES_STREAM;
@@ -2646,7 +2649,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 			t->params.resStream = d;
 			float ms = 0.0f;
 			rc = timeConfig(best, bestVariant, ms);
-			if(!rc && ms < bestMs) { bestMs = ms; bestStream = d; }
+			if(!rc && ms < bestMs * TUNE_MARGIN) { bestMs = ms; bestStream = d; }
 		}
 	t->params.resStream = bestStream;
 	// then the blocks per SM of the row preparation (rows per CTA wave) and of the
@@ -2658,7 +2661,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		t->prepPerSm = c;
 		float ms = 0.0f;
 		rc = timeConfig(best, bestVariant, ms);
-		if(!rc && ms < bestMs) { bestMs = ms; bestPrep = c; }
+		if(!rc && ms < bestMs * TUNE_MARGIN) { bestMs = ms; bestPrep = c; }
 	}
 	t->prepPerSm = bestPrep;
 	for(uint32_t c : {1u, 2u, 3u})
@@ -2667,7 +2670,7 @@ GBPX_API int gbpx_world_autotune(void* wv, uint32_t sampleScenes, uint32_t steps
 		t->npHeavyPerSm = c;
 		float ms = 0.0f;
 		rc = timeConfig(best, bestVariant, ms);
-		if(!rc && ms < bestMs) { bestMs = ms; bestNp = c; }
+		if(!rc && ms < bestMs * TUNE_MARGIN) { bestMs = ms; bestNp = c; }
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
