@@ -57,11 +57,19 @@ constexpr uint32_t RES_WARPS = 16;
 constexpr uint32_t RES_LEVELS = 5;
 static_assert((RES_WARPS >> (RES_LEVELS - 1)) >= 1 && RES_WARPS <= 16, "levels down to one warp; named barriers 1..RES_WARPS-1");
 constexpr uint32_t RES_HEADER = MAX_PARTITIONS * 4;   // partition ends at the start of a group's slice
+// work counters of the persistent stage kernels (scenes or entries taken)
+enum : uint32_t { WC_BP = 0, WC_BATCH = 1, WC_SOLVE = 2, WC_PREP = 3, WC_BP_BIG = 4, WC_BATCH_BIG = 5, WC_SOLVE_BIG = 6 };
 // work counters (after the per-kind pair counts and path counts): scenes filed
 // per level, then scenes taken per level
 constexpr uint32_t WC_RES_COUNT = 8 + 9 + 4;
 constexpr uint32_t WC_RES_NEXT = WC_RES_COUNT + RES_LEVELS;
-constexpr uint32_t NB_WORK_COUNTERS = WC_RES_NEXT + RES_LEVELS;
+// the row preparation's queue classes (constraints with the same path, contact
+// count and count of last step's friction patches): entries per class, then
+// entries placed per class
+constexpr uint32_t PREP_CLASSES = 32;
+constexpr uint32_t WC_PREP_CLASS = WC_RES_NEXT + RES_LEVELS;
+constexpr uint32_t WC_PREP_PLACED = WC_PREP_CLASS + PREP_CLASSES;
+constexpr uint32_t NB_WORK_COUNTERS = WC_PREP_PLACED + PREP_CLASSES;
 // StepParams::solveVariant selecting the resident solve (0-7 are staging
 // variants of the warp-per-scene solve)
 constexpr uint32_t RESIDENT_VARIANT = 8;
@@ -148,6 +156,8 @@ struct WorldDev
 	uint32_t* nbConstraints;   // per scene: constraints (pairs with contacts) of this step
 	uint32_t* nbPartitions;    // per scene: partitions, 0 when batching overflowed
 	uint32_t* prepQueue;       // constraint slots of all scenes, for the row-preparation kernel
+	uint8_t* prepClass;        // class of each prepQueue entry
+	uint32_t* prepQueueSorted; // prepQueue grouped by class (what prepKernel reads)
 	uint8_t* recChunks;        // per constraint slot: 16-byte chunks its packed rows occupy
 	// Persistent pair state (the reference snippet's persistent mode): per pair
 	// slot a contact manifold and the friction patches its constraint left, in
@@ -824,6 +834,53 @@ __device__ __forceinline__ void sceneBatchStage(const WorldDev& w, const SceneDe
 		const uint32_t start = lo ? sm.perPart[lo - 1] : 0u, size = sm.perPart[lo] - start;
 		const bool block = (r - start) < (size & ~3u);
 		w.prepQueue[qbase + r] = (sc.pairStart + r) | (block ? 0x80000000u : 0u);
+		// class: the path, the contact count and last step's friction patches, so that
+		// a warp of the preparation runs one code path
+		const uint32_t k = w.ordered[sc.pairStart + r];
+		const uint32_t cnt = w.contactCount[sc.pairStart + k];
+		uint32_t prevPatches = 0;
+		if(sp.persistent)
+		{
+			const uint32_t prev = w.prevSlot[sc.pairStart + k];
+			if(prev != NO_PREV) prevPatches = w.frictionState[w.sceneParity[sid]][sc.pairStart + prev].count;
+		}
+		const uint32_t cls = (block ? 16u : 0u) | (((cnt - 1u) & 3u) << 2) | (prevPatches < 3u ? prevPatches : 3u);
+		w.prepClass[qbase + r] = uint8_t(cls);
+		const uint32_t peers = __match_any_sync(__activemask(), cls);
+		if((threadIdx.x & 31) == uint32_t(__ffs(peers) - 1)) atomicAdd(&w.workCounter[WC_PREP_CLASS + cls], uint32_t(__popc(peers)));
+	}
+}
+
+// The preparation queue grouped by class (a stable order is not needed: every
+// constraint's rows go to its own slot).
+__global__ void __launch_bounds__(128) prepOrderKernel(WorldDev w, StepParams sp)
+{
+	__shared__ uint32_t first[PREP_CLASSES];
+	if(threadIdx.x < 32)
+	{
+		const uint32_t c = w.workCounter[WC_PREP_CLASS + threadIdx.x];
+		uint32_t incl = c;
+		for(int d = 1; d < 32; d <<= 1)
+		{
+			const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+			if(threadIdx.x >= uint32_t(d)) incl += t;
+		}
+		first[threadIdx.x] = incl - c;
+	}
+	__syncthreads();
+	const uint32_t count = w.workCounter[WC_PREP];
+	const uint32_t lane = threadIdx.x & 31;
+	for(uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x)
+	{
+		const uint32_t q = base + threadIdx.x;
+		const bool valid = q < count;
+		const uint32_t cls = valid ? uint32_t(w.prepClass[q]) : 0xffu;
+		const uint32_t peers = __match_any_sync(0xffffffffu, cls);
+		const uint32_t leader = __ffs(peers) - 1;
+		uint32_t b = 0;
+		if(valid && lane == leader) b = atomicAdd(&w.workCounter[WC_PREP_PLACED + cls], uint32_t(__popc(peers)));
+		b = __shfl_sync(0xffffffffu, b, leader);
+		if(valid) w.prepQueueSorted[first[cls] + b + __popc(peers & laneMaskLt())] = w.prepQueue[q];
 	}
 }
 
@@ -1091,7 +1148,6 @@ __device__ __forceinline__ bool nextScene(const WorldDev& w, uint32_t counter, b
 	}
 }
 
-enum : uint32_t { WC_BP = 0, WC_BATCH = 1, WC_SOLVE = 2, WC_PREP = 3, WC_BP_BIG = 4, WC_BATCH_BIG = 5, WC_SOLVE_BIG = 6 };
 
 __global__ void __launch_bounds__(128) broadphaseKernel(WorldDev w, StepParams sp)
 {
@@ -1135,7 +1191,7 @@ __global__ void __launch_bounds__(128, 5) prepKernel(WorldDev w, StepParams sp)
 	const uint32_t count = w.workCounter[WC_PREP];
 	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
 	{
-		const uint32_t entry = w.prepQueue[q];
+		const uint32_t entry = w.prepQueueSorted[q];
 		const uint32_t chunks = prepSlot(w, entry, sp);
 		if(sp.solveVariant == RESIDENT_VARIANT) residentCount(w, entry & 0x7fffffffu, chunks, sp);
 	}
@@ -1774,7 +1830,7 @@ struct World
 	std::vector<world::SceneDesc> hScenes;
 	uint32_t nbScenes = 0, nbBodies = 0, nbStatics = 0, nbSolver = 0, nbKeys = 0, nbPairSlots = 0;
 	uint32_t gridBlocks = 0, gridBatch = 0, gridPrep = 0, gridSolve[world::SOLVE_VARIANTS] = {}, gridNp[world::NB_KINDS] = {};
-	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0, gridRes = 0;
+	uint32_t gridBpBig = 0, gridBatchBig = 0, gridSolveBig = 0, gridOrder = 0, gridPrepOrder = 0, gridRes = 0;
 	uint32_t maxSolverBodies = 0;   // largest scene (bodies + statics) a slot can hold
 	// persistent blocks per SM of the row preparation and of the capsule-box and
 	// box-box narrowphase kernels (0: as many as fit).  Their threads keep large
@@ -1794,6 +1850,8 @@ struct World
 	DevBuf<world::SceneDesc> scenes;
 	DevBuf<uint32_t> typeQueueSorted;
 	DevBuf<uint32_t> typeQueue, slotScene, nbConstraints, nbPartitions, prepQueue, activeCount;
+	DevBuf<uint32_t> prepQueueSorted;
+	DevBuf<uint8_t> prepClass;
 	DevBuf<uint8_t> recChunks;
 	DevBuf<uint32_t> workOrder, workCounter, pairs, pairCount, contactCount, ordered, consList, tag, progress, maxNormal, maxStatic,
 	    staticProgress, partEnds, status;
@@ -1835,7 +1893,7 @@ struct World
 		w.maxStatic = maxStatic.ptr; w.staticProgress = staticProgress.ptr; w.partEnds = partEnds.ptr; w.status = status.ptr;
 		w.typeCount = workCounter.ptr + 8; w.pathCount = workCounter.ptr + 8 + world::NB_KINDS; w.typeQueueSorted = typeQueueSorted.ptr;
 		w.typeQueue = typeQueue.ptr; w.queueCap = nbPairSlots; w.slotScene = slotScene.ptr;
-		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.recChunks = recChunks.ptr;
+		w.nbConstraints = nbConstraints.ptr; w.nbPartitions = nbPartitions.ptr; w.prepQueue = prepQueue.ptr; w.prepQueueSorted = prepQueueSorted.ptr; w.prepClass = prepClass.ptr; w.recChunks = recChunks.ptr;
 		w.pairsPrev = pairsPrev.ptr; w.pairCountPrev = pairCountPrev.ptr; w.prevSlot = prevSlot.ptr; w.sceneParity = sceneParity.ptr;
 		for(int k = 0; k < 2; k++) { w.manifolds[k] = manifolds[k].ptr; w.frictionState[k] = frictionState[k].ptr; }
 		w.sceneAcc = sceneAcc.ptr; w.resList = resList.ptr; w.resCap = nbScenes;
@@ -1875,7 +1933,7 @@ struct World
 			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&forkEv[k], cudaEventDisableTiming));
 			GBPX_CUDA_TRY(cudaEventCreateWithFlags(&joinEv[k], cudaEventDisableTiming));
 		}
-		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || activeCount.reserve(2) || recChunks.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
+		if(scenes.reserve(S) || workOrder.reserve(S) || workCounter.reserve(COUNTERS) || typeQueue.reserve(size_t(world::NB_KINDS) * pair) || slotScene.reserve(pair) || activeCount.reserve(2) || recChunks.reserve(pair) || nbConstraints.reserve(S) || nbPartitions.reserve(S) || prepQueue.reserve(pair) || prepQueueSorted.reserve(pair) || prepClass.reserve(pair) || bodies.reserve(b) || types.reserve(b) || geoms.reserve(b) ||
 		   friction.reserve(b) || staticPose.reserve(7 * size_t(st) + 1) || staticTypes.reserve(st + 1) || staticGeoms.reserve(st + 1) ||
 		   aabb.reserve(6 * size_t(b)) || keys.reserve(key) || pairs.reserve(pair) || pairCount.reserve(S) || contacts.reserve(8 * size_t(pair)) ||
 		   contactCount.reserve(pair) || ordered.reserve(pair) || consList.reserve(pair) || tag.reserve(pair) || recs.reserve(pair) ||
@@ -1946,6 +2004,7 @@ struct World
 		}
 		for(uint32_t k = 0; k < world::NB_KINDS; k++) GBPX_CUDA_TRY(gridFor(npKernels()[k], sms, gridNp[k]));
 		GBPX_CUDA_TRY(gridFor(world::orderByPathKernel, sms, gridOrder));
+		GBPX_CUDA_TRY(gridFor(world::prepOrderKernel, sms, gridPrepOrder));
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::broadphaseBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::BpSmemBig))));
 		GBPX_CUDA_TRY(gridFor(world::broadphaseBigKernel, sms, gridBpBig, sizeof(world::BpSmemBig), int(BIG_THREADS)));
 		GBPX_CUDA_TRY(cudaFuncSetAttribute(world::batchBigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(world::SolveSmemBig))));
@@ -2061,6 +2120,7 @@ struct World
 			world::batchBigKernel<<<plain ? 1u : gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), bigStream>>>(w, params);
 			if(!plain) GBPX_CUDA_TRY(join(1));
 		}
+		world::prepOrderKernel<<<plain ? std::min(gridPrepOrder, 8u) : gridPrepOrder, 128, 0, stream>>>(w, params);
 		world::prepKernel<<<gPrep, 128, 0, stream>>>(w, params);
 		if(resident())
 			// every scene, large or small, in one launch
@@ -2144,6 +2204,7 @@ struct World
 			world::batchKernel<<<gridBatch, 128, solveSmemBytes(world::STAGE_WARPS), stream>>>(w, params);
 			if(big) world::batchBigKernel<<<gridBatchBig, BIG_THREADS, sizeof(world::SolveSmemBig), stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
+			world::prepOrderKernel<<<gridPrepOrder, 128, 0, stream>>>(w, params);
 			world::prepKernel<<<prepGrid(), 128, 0, stream>>>(w, params);
 			GBPX_CUDA_TRY(cudaEventRecord(ev[k++], stream));
 			if(resident()) world::solveResidentKernel<<<gridRes, RES_THREADS, params.resBytes, stream>>>(w, params);
@@ -2217,7 +2278,7 @@ struct World
 		pairsPrev.release(); pairCountPrev.release(); prevSlot.release(); sceneParity.release();
 		for(int k = 0; k < 2; k++) { manifolds[k].release(); frictionState[k].release(); }
 		typeQueueSorted.release();
-		scenes.release(); typeQueue.release(); slotScene.release(); activeCount.release(); recChunks.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
+		scenes.release(); typeQueue.release(); slotScene.release(); activeCount.release(); recChunks.release(); nbConstraints.release(); nbPartitions.release(); prepQueue.release(); prepQueueSorted.release(); prepClass.release(); workOrder.release(); workCounter.release(); pairs.release(); pairCount.release(); contactCount.release();
 		ordered.release(); consList.release(); tag.release(); progress.release(); maxNormal.release(); maxStatic.release();
 		staticProgress.release(); partEnds.release(); status.release(); bodies.release(); types.release(); staticTypes.release();
 		geoms.release(); staticGeoms.release(); contacts.release(); friction.release(); staticPose.release(); aabb.release();
@@ -2338,7 +2399,7 @@ GBPX_API int gbpx_world_info(void* wv, uint64_t* out8)
 	if(!w || !out8) return GBPX_ERR_INVALID;
 	out8[0] = w->nbScenes; out8[1] = w->nbBodies; out8[2] = w->nbStatics; out8[3] = w->nbPairSlots; out8[4] = w->gridBlocks;
 	out8[5] = w->deviceBytes;
-	out8[6] = World::KERNELS_PER_STEP + (w->launchLarge() ? (w->resident() ? 2u : 3u) : 0u) + (w->params.persistent ? 1u : 0u);
+	out8[6] = World::KERNELS_PER_STEP + 1u + (w->launchLarge() ? (w->resident() ? 2u : 3u) : 0u) + (w->params.persistent ? 1u : 0u);
 	out8[7] = w->params.largeBodies;
 	return GBPX_OK;
 }
