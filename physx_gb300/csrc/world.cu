@@ -69,7 +69,9 @@ constexpr uint32_t WC_RES_NEXT = WC_RES_COUNT + RES_LEVELS;
 constexpr uint32_t PREP_CLASSES = 32;
 constexpr uint32_t WC_PREP_CLASS = WC_RES_NEXT + RES_LEVELS;
 constexpr uint32_t WC_PREP_PLACED = WC_PREP_CLASS + PREP_CLASSES;
-constexpr uint32_t NB_WORK_COUNTERS = WC_PREP_PLACED + PREP_CLASSES;
+// pairs taken per pair kind by the narrowphase kernels' warps
+constexpr uint32_t WC_NP_TAKEN = WC_PREP_PLACED + PREP_CLASSES;
+constexpr uint32_t NB_WORK_COUNTERS = WC_NP_TAKEN + 9;
 // StepParams::solveVariant selecting the resident solve (0-7 are staging
 // variants of the warp-per-scene solve)
 constexpr uint32_t RESIDENT_VARIANT = 8;
@@ -519,10 +521,19 @@ __global__ void __launch_bounds__(128, (TA == 3 && TB == 3) ? 4 : 5) narrowphase
 {
 	constexpr uint32_t KIND = TA == 0 ? uint32_t(TB) : (TA == 1 ? uint32_t(TB + 2) : (TA == 2 ? uint32_t(TB + 4) : 8u));
 	const uint32_t count = w.typeCount[KIND];
-	const uint32_t* queue = (KIND == 7 || KIND == 8) && sp.persistent ? w.typeQueueSorted + size_t(KIND - 7) * w.queueCap
-	                                                                   : w.typeQueue + size_t(KIND) * w.queueCap;
-	for(uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+	const bool sorted = (KIND == 7 || KIND == 8) && sp.persistent;
+	const uint32_t* queue = sorted ? w.typeQueueSorted + size_t(KIND - 7) * w.queueCap : w.typeQueue + size_t(KIND) * w.queueCap;
+	// each warp takes 32 queued pairs at a time; the sorted queues (refresh path
+	// first, full path last) are taken from the back, so the long pairs start first
+	const uint32_t lane = threadIdx.x & 31;
+	for(;;)
 	{
+		uint32_t base = 0;
+		if(lane == 0) base = atomicAdd(&w.workCounter[WC_NP_TAKEN + KIND], 32u);
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if(base >= count) break;
+		if(base + lane >= count) continue;
+		const uint32_t q = sorted ? count - 1u - (base + lane) : base + lane;
 		const uint32_t slot = queue[q];
 		const uint32_t sid = w.slotScene[slot];
 		const SceneDesc sc = w.scenes[sid];
