@@ -7,6 +7,9 @@
  *   PxConstructStaticSolverBodyTGS   physx/include/PxImmediateMode.h:601
  *   PxBatchConstraintsTGS            physx/include/PxImmediateMode.h:620
  *   PxCreateContactConstraintsTGS    physx/include/PxImmediateMode.h:642
+ *   PxCreateJointConstraintsTGS      physx/include/PxImmediateMode.h:659
+ *   PxCreateJointConstraintsWithImmediateShadersTGS
+ *                                    physx/include/PxImmediateMode.h:696
  *   PxSolveConstraintsTGS            physx/include/PxImmediateMode.h:716
  *   PxIntegrateSolverBodiesTGS       physx/include/PxImmediateMode.h:729
  *   PxConstructSolverBodies          physx/include/PxImmediateMode.h:111
@@ -319,6 +322,18 @@ struct PxTGSSolverConstraintPrepDesc
 	PxVec3p cB2w;
 };
 
+// PxConstraintSolverPrep (PxConstraintDesc.h:278): a joint shader filling up to
+// maxConstraints rows; returns the rows it wrote.
+typedef uint32_t (*PxConstraintSolverPrep)(Px1DConstraint* constraints, PxVec3p& bodyAWorldOffset, uint32_t maxConstraints,
+                                           PxConstraintInvMassScale& invMassScale, const void* constantBlock, const PxTransform& bodyAToWorld,
+                                           const PxTransform& bodyBToWorld, bool useExtendedLimits, PxVec3p& cAtW, PxVec3p& cBtW);
+// PxImmediateConstraint (PxImmediateMode.h:192)
+struct PxImmediateConstraint
+{
+	PxConstraintSolverPrep prep;
+	const void* constantBlock;
+};
+
 class PxConstraintAllocator
 {
 public:
@@ -477,6 +492,10 @@ bool PxCreateContactConstraintsTGS(gbpx_px::PxConstraintBatchHeader* batchHeader
                                    float frictionOffsetThreshold, float correlationDistance);
 bool PxCreateJointConstraintsTGS(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, gbpx_px::PxTGSSolverConstraintPrepDesc* jointDescs,
                                  gbpx_px::PxConstraintAllocator& allocator, float dt, float totalDt, float invDt, float invTotalDt, float lengthScale);
+bool PxCreateJointConstraintsWithImmediateShadersTGS(gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders,
+                                                     gbpx_px::PxImmediateConstraint* constraints,
+                                                     gbpx_px::PxTGSSolverConstraintPrepDesc* jointDescs, gbpx_px::PxConstraintAllocator& allocator,
+                                                     float dt, float totalDt, float invDt, float invTotalDt, float lengthScale);
 void PxSolveConstraintsTGS(const gbpx_px::PxConstraintBatchHeader* batchHeaders, uint32_t nbBatchHeaders,
                            const gbpx_px::PxSolverConstraintDesc* solverConstraintDescs, gbpx_px::PxTGSSolverBodyVel* solverBodies,
                            gbpx_px::PxTGSSolverBodyTxInertia* txInertias, uint32_t nbSolverBodies, uint32_t nbPositionIterations,

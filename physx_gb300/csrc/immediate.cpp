@@ -672,6 +672,47 @@ GX uint32_t PxBatchConstraints(const PxSolverConstraintDesc* descs, uint32_t nbC
 	return nbHeaders;
 }
 
+// PxCreateJointConstraintsWithImmediateShadersTGS (NpImmediateMode.cpp:1543-1628):
+// each descriptor's shader fills its rows on the host (unit mass scales and a
+// zero body-0 offset first, up to 20 rows set to zero with unbounded impulse
+// limits, as setupConstraintRows, DyConstraintPrep.h:115), then the rows of
+// every header are prepared on the device in one PxCreateJointConstraintsTGS
+// call.  The reference prepares header by header into one reused row buffer;
+// each shader sees the same fresh rows here.
+GX bool PxCreateJointConstraintsWithImmediateShadersTGS(PxConstraintBatchHeader* batchHeaders, uint32_t nbHeaders, PxImmediateConstraint* constraints,
+                                                        PxTGSSolverConstraintPrepDesc* jointDescs, PxConstraintAllocator& allocator, float dt,
+                                                        float totalDt, float invDt, float invTotalDt, float lengthScale)
+{
+	constexpr uint32_t MAX_ROWS = 20;   // Dy::MAX_CONSTRAINT_ROWS
+	const uint32_t n = stridesTotal(batchHeaders, nbHeaders);
+	if(!n) return true;
+	if(!constraints || !jointDescs) return false;
+	std::vector<Px1DConstraint> rows(size_t(n) * MAX_ROWS);
+	uint32_t d = 0;
+	for(uint32_t h = 0; h < nbHeaders; h++)
+		for(uint32_t a = 0; a < batchHeaders[h].stride; a++, d++)
+		{
+			PxTGSSolverConstraintPrepDesc& desc = jointDescs[d];
+			const PxImmediateConstraint& ic = constraints[d];
+			if(!ic.prep) return false;
+			Px1DConstraint* r = rows.data() + size_t(d) * MAX_ROWS;
+			memset(r, 0, sizeof(Px1DConstraint) * MAX_ROWS);
+			for(uint32_t i = 0; i < MAX_ROWS; i++)
+			{
+				r[i].minImpulse = -3.402823466e+38f;
+				r[i].maxImpulse = 3.402823466e+38f;
+			}
+			desc.invMassScales = PxConstraintInvMassScale{1.0f, 1.0f, 1.0f, 1.0f};
+			desc.body0WorldOffset.v = PxVec3{0.0f, 0.0f, 0.0f};
+			const uint32_t count = ic.prep(r, desc.body0WorldOffset, MAX_ROWS, desc.invMassScales, ic.constantBlock, desc.bodyFrame0, desc.bodyFrame1,
+			                               false, desc.cA2w, desc.cB2w);
+			if(count > MAX_ROWS) return false;
+			desc.rows = r;
+			desc.numRows = count;
+		}
+	return PxCreateJointConstraintsTGS(batchHeaders, nbHeaders, jointDescs, allocator, dt, totalDt, invDt, invTotalDt, lengthScale);
+}
+
 // PxCreateContactConstraints: a record per descriptor into the allocator's
 // constraint memory; the header types as the reference leaves them
 // (NpImmediateMode.cpp:292-367).  Friction data is not kept between frames.

@@ -3,8 +3,9 @@
 // PxBatchConstraintsTGS, PxCreateJointConstraintsTGS, PxSolveConstraintsTGS,
 // PxIntegrateSolverBodiesTGS) the way the reference's immediate-mode snippet
 // builds its joints (SnippetImmediateMode.cpp:838-1061), with the joint rows
-// given instead of a joint shader; linked against libgbpx_immediate.so.  Used
-// by tests/test_joints_gpu.py.
+// given instead of a joint shader, or (argument "shader") returned by an
+// immediate joint shader through PxCreateJointConstraintsWithImmediateShadersTGS;
+// linked against libgbpx_immediate.so.  Used by tests/test_joints_gpu.py.
 //
 // stdin (binary): nbDyn, nbStatic, nbJoints, nbRows, batch (u32);
 // PxRigidBodyData[nbDyn]; static poses (PxTransform); jointA, jointB,
@@ -45,6 +46,26 @@ struct Arena : PxConstraintAllocator
 	uint8_t* reserveFrictionData(const uint32_t size) override { return reserveConstraintData(size); }
 };
 
+// constant block of the immediate joint shader: the joint's rows and parameters
+struct JointBlock
+{
+	const Px1DConstraint* rows;
+	uint32_t count;
+	const float* p;
+};
+uint32_t copyRowsShader(Px1DConstraint* rows, PxVec3p& body0WorldOffset, uint32_t maxRows, PxConstraintInvMassScale& invMassScale,
+                        const void* constantBlock, const PxTransform&, const PxTransform&, bool, PxVec3p& cA2w, PxVec3p& cB2w)
+{
+	const JointBlock& b = *static_cast<const JointBlock*>(constantBlock);
+	const uint32_t n = b.count < maxRows ? b.count : maxRows;
+	memcpy(rows, b.rows, sizeof(Px1DConstraint) * n);
+	invMassScale = PxConstraintInvMassScale{b.p[0], b.p[1], b.p[2], b.p[3]};
+	cA2w.v = PxVec3{b.p[4], b.p[5], b.p[6]};
+	cB2w.v = PxVec3{b.p[7], b.p[8], b.p[9]};
+	body0WorldOffset.v = PxVec3{b.p[10], b.p[11], b.p[12]};
+	return n;
+}
+
 // Dy::ConstraintWriteback
 struct Writeback
 {
@@ -55,8 +76,9 @@ struct Writeback
 };
 } // namespace
 
-int main()
+int main(int argc, char** argv)
 {
+	const bool shader = argc > 1 && strcmp(argv[1], "shader") == 0;
 	uint32_t head[5];
 	readAll(head, 5);
 	const uint32_t nbDyn = head[0], nbStatic = head[1], nbJoints = head[2], nbRows = head[3], batch = head[4];
@@ -135,6 +157,10 @@ int main()
 	std::vector<Writeback> writeback(nbJoints ? nbJoints : 1);
 	memset(writeback.data(), 0, sizeof(Writeback) * writeback.size());
 	std::vector<Px1DConstraint> rowCopy(rows);
+	// shader mode: every header's descriptors, in header order, and their shaders
+	std::vector<PxTGSSolverConstraintPrepDesc> jdAll(nbJoints ? nbJoints : 1);
+	std::vector<JointBlock> blocks(nbJoints ? nbJoints : 1);
+	std::vector<PxImmediateConstraint> shaders(nbJoints ? nbJoints : 1);
 	for(uint32_t h = 0; h < nbHeaders; h++)
 	{
 		PxConstraintBatchHeader& header = headers[h];
@@ -144,7 +170,7 @@ int main()
 			PxSolverConstraintDesc& desc = ordered[header.startIndex + a];
 			const uint32_t j = order[header.startIndex + a];
 			const float* p = &params[size_t(j) * 20];
-			PxTGSSolverConstraintPrepDesc& c = jd[a];
+			PxTGSSolverConstraintPrepDesc& c = shader ? jdAll[header.startIndex + a] : jd[a];
 			memset(&c, 0, sizeof(c));
 			c.body0 = desc.tgsBodyA;
 			c.body1 = desc.tgsBodyB;
@@ -170,8 +196,26 @@ int main()
 			c.driveLimitsAreForces = (fl & 4u) != 0;
 			c.rows = rowCopy.data() + rs[j];
 			c.numRows = rc[j];
+			if(shader)
+			{
+				// the shader sets the rows, mass scales, frames and offset itself
+				c.rows = nullptr;
+				c.numRows = 0;
+				blocks[header.startIndex + a] = JointBlock{rowCopy.data() + rs[j], rc[j], p};
+				shaders[header.startIndex + a] = PxImmediateConstraint{copyRowsShader, &blocks[header.startIndex + a]};
+			}
 		}
-		if(!PxCreateJointConstraintsTGS(&header, 1, jd, arena, stepDt, dt, invStepDt, invDt, 1.0f)) { fprintf(stderr, "joint prep failed\n"); return 3; }
+		if(!shader && !PxCreateJointConstraintsTGS(&header, 1, jd, arena, stepDt, dt, invStepDt, invDt, 1.0f))
+		{
+			fprintf(stderr, "joint prep failed\n");
+			return 3;
+		}
+	}
+	if(shader && !PxCreateJointConstraintsWithImmediateShadersTGS(headers.data(), nbHeaders, shaders.data(), jdAll.data(), arena, stepDt, dt,
+	                                                             invStepDt, invDt, 1.0f))
+	{
+		fprintf(stderr, "joint prep failed\n");
+		return 3;
 	}
 	PxSolveConstraintsTGS(headers.data(), nbHeaders, ordered.data(), bodies.data(), txI.data(), nbDyn, nbPos, nbVel, stepDt, invStepDt, 0, nullptr,
 	                      nullptr, nullptr);

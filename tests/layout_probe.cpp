@@ -73,6 +73,7 @@ int main(){
  O(PxSolverConstraintDesc, writeBack); O(PxSolverConstraintDesc, writeBackFriction); O(PxSolverConstraintDesc, progressA); O(PxSolverConstraintDesc, progressB);
  O(PxSolverConstraintDesc, constraintLengthOver16);
  S(PxConstraintInvMassScale);
+ S(PxImmediateConstraint); O(PxImmediateConstraint, prep); O(PxImmediateConstraint, constantBlock);
  S(PxTGSSolverContactDesc); O(PxTGSSolverContactDesc, invMassScales); O(PxTGSSolverContactDesc, desc); O(PxTGSSolverContactDesc, body0); O(PxTGSSolverContactDesc, body1);
  O(PxTGSSolverContactDesc, body0TxI); O(PxTGSSolverContactDesc, body1TxI); O(PxTGSSolverContactDesc, bodyData0); O(PxTGSSolverContactDesc, bodyData1);
  O(PxTGSSolverContactDesc, bodyFrame0); O(PxTGSSolverContactDesc, bodyFrame1); O(PxTGSSolverContactDesc, bodyState0); O(PxTGSSolverContactDesc, bodyState1);

@@ -69,7 +69,7 @@ def test_immediate_library_exports_the_reference_entry_points(gbpx_built):
     text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gbpx_immediate.h")).read(), flags=re.S)
     block = text[text.index('extern "C"'):]
     declared = sorted(set(re.findall(r"\b(Px\w+)\s*\(", block)))
-    assert len(declared) == 21, declared
+    assert len(declared) == 22, declared
     lib = os.path.join(os.path.dirname(gbpx_built), "libgbpx_immediate.so")
     out = os.popen("nm -D --defined-only %s" % lib).read()
     exported = sorted(l.split()[-1] for l in out.splitlines() if " T " in l)

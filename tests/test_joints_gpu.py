@@ -73,7 +73,7 @@ def _build(tmp):
     return exe
 
 
-def _run_dropin(exe, fr, batch, dt=1.0 / 60.0, gravity=(0.0, -9.81, 0.0), nb_pos=4, nb_vel=1):
+def _run_dropin(exe, fr, batch, dt=1.0 / 60.0, gravity=(0.0, -9.81, 0.0), nb_pos=4, nb_vel=1, shader=False):
     n, nj = int(fr["nb_dyn"]), len(fr["joint_a"])
     rows = np.ascontiguousarray(fr["rows"])
     blob = struct.pack("<5I", n, len(fr["static_poses"]), nj, len(rows), 1 if batch else 0)
@@ -82,7 +82,7 @@ def _run_dropin(exe, fr, batch, dt=1.0 / 60.0, gravity=(0.0, -9.81, 0.0), nb_pos
         blob += np.ascontiguousarray(fr[k], np.uint32).tobytes()
     blob += rows.tobytes() + np.ascontiguousarray(fr["params"], np.float32).tobytes()
     blob += struct.pack("<4f2I", dt, *gravity, nb_pos, nb_vel)
-    out = subprocess.run([exe], input=blob, capture_output=True, check=True).stdout
+    out = subprocess.run([exe] + (["shader"] if shader else []), input=blob, capture_output=True, check=True).stdout
     body = np.frombuffer(out[: n * 52], np.float32).reshape(n, 13)
     nh = struct.unpack_from("<I", out, n * 52)[0]
     hdr = np.frombuffer(out[n * 52 + 4: n * 52 + 4 + nh * 12], np.uint32).reshape(nh, 3)
@@ -108,6 +108,22 @@ def test_immediate_joints_match_reference_golden(cuda_device, tmp_path, batch):
         else:
             ref = run_joints("orc", fr, batch=False)
         got = _run_dropin(exe, fr, batch)
+        for k in ("header_start", "header_stride", "header_type", "broken"):
+            assert np.array_equal(got[k], ref[k]), "frame %d %s" % (fr["frame"], k)
+        assert velocity_error(ref["vel"], got["vel"]) <= 1e-5
+        assert np.abs(ref["pose"] - got["pose"]).max() <= 2e-6
+        assert impulse_error(ref["force"], got["force"]) <= 1e-5
+
+
+def test_immediate_joint_shaders_match_reference_golden(cuda_device, tmp_path):
+    """The same program with its rows returned by an immediate joint shader
+    (PxImmediateConstraint; PxCreateJointConstraintsWithImmediateShadersTGS,
+    PxImmediateMode.h:696): the shader also sets the mass scales, the constraint
+    frames and body 0's offset, and the frames equal the reference's."""
+    exe = _build(str(tmp_path))
+    for fr in load_joint_fixture(os.path.join(GOLDEN, "joints_chains.npz")):
+        ref = {k: fr["ref_" + k] for k in ("vel", "pose", "header_start", "header_stride", "header_type", "force", "broken")}
+        got = _run_dropin(exe, fr, True, shader=True)
         for k in ("header_start", "header_stride", "header_type", "broken"):
             assert np.array_equal(got[k], ref[k]), "frame %d %s" % (fr["frame"], k)
         assert velocity_error(ref["vel"], got["vel"]) <= 1e-5
