@@ -360,3 +360,26 @@ def test_world_full_size_persistent_steps_match_oracle_sample(cuda_device):
     assert not w.status().any()
     orc.release()
     w.release()
+
+
+def test_world_step_host_equals_device_steps(cuda_device):
+    """The end-to-end call (gbpx_world_step_host: bodies uploaded from pinned host
+    memory, one graph-replayed step, bodies downloaded) gives the bytes of a
+    device-resident step from the same state, step after step."""
+    from physx_gb300.workloads import batched_scenes
+    from physx_gb300.world import World
+    scenes = batched_scenes(151, 64, nmin=8, nmax=256)
+    a, b = World(scenes), World(scenes)
+    a.step(20)
+    b.step(20)
+    host_in, host_out = b.pinned_bodies(), b.pinned_bodies()
+    host_out[:] = b.get_bodies()
+    for _ in range(5):
+        a.step(1)
+        host_in[:] = host_out
+        ms = b.step_host(host_in, host_out, 1)
+        assert ms > 0
+        assert host_out.tobytes() == a.get_bodies().tobytes()
+    assert not a.status().any() and not b.status().any()
+    a.release()
+    b.release()
