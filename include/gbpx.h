@@ -414,6 +414,16 @@ int gbpx_server_pump(void* server, uint32_t* outIssued);
 int gbpx_server_clock(void* server, double* outSeconds);
 int gbpx_server_poll(void* server, uint64_t* outTags, double* outLatencySeconds, uint32_t capacity, uint32_t* outCount);
 int gbpx_server_read_scene(void* server, uint32_t scene, void* outRigidBodies);
+/* Eviction and re-admission (checkpoint / resume of served state): the snapshot
+ * of a scene that owes no steps -- bodies, shapes, statics and, with persistent
+ * pair state, its sorted pair list with each pair's contact manifold and
+ * friction patches -- in this library's layout; *outBytes gets its size and out
+ * (capacity bytes, GBPX_ERR_CAPACITY if short) the snapshot unless null.
+ * Restoring admits it as a new scene (the smallest class that holds its bodies,
+ * statics and pairs) whose following steps give the results the scene would
+ * have had. */
+int gbpx_server_snapshot_scene(void* server, uint32_t scene, void* out, uint64_t capacity, uint64_t* outBytes);
+int gbpx_server_restore_scene(void* server, const void* snapshot, uint64_t bytes, uint32_t* outScene);
 /* out4: body-steps completed, class steps completed, live scenes, steps in flight */
 int gbpx_server_stats(void* server, uint64_t* out4);
 /* The open-loop serving load run in the library (no per-request host language

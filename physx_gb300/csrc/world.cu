@@ -2281,6 +2281,96 @@ struct World
 		return GBPX_OK;
 	}
 
+	// Snapshot of a scene between steps (this library's byte layout): a header
+	// (magic, version, bodies, statics, pairs, whether pair state follows), the
+	// bodies (PxRigidBodyData), shapes, statics and, in persistent mode, the
+	// sorted pair list with each pair's contact manifold and friction patches as
+	// the last step left them (the buffer sceneParity names).  Restoring it into
+	// a slot of enough capacity continues the scene with the same results.
+	struct SnapshotHeader { uint32_t magic, version, nbBodies, nbStatics, nbPairs, pairState, pad[2]; };
+	static constexpr uint32_t SNAPSHOT_MAGIC = 0x53535847u;   // "GXSS"
+	static size_t snapshotBytes(uint32_t nb, uint32_t ns, uint32_t np, bool pairState)
+	{
+		return sizeof(SnapshotHeader) + size_t(nb) * (sizeof(tgs::RigidBody) + 4 + 16 + 4) + size_t(ns) * (28 + 4 + 16) +
+		       (pairState ? size_t(np) * (4 + sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0);
+	}
+	int snapshot(uint32_t slot, std::vector<uint8_t>& out)
+	{
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		const world::SceneDesc& d = hScenes[slot];
+		const bool ps = params.persistent != 0;
+		uint32_t np = 0, par = 0;
+		if(ps)
+		{
+			GBPX_CUDA_TRY(cudaMemcpy(&np, pairCount.ptr + slot, 4, cudaMemcpyDeviceToHost));
+			GBPX_CUDA_TRY(cudaMemcpy(&par, sceneParity.ptr + slot, 4, cudaMemcpyDeviceToHost));
+			if(np > d.pairCap || par > 1u) return GBPX_ERR_STATE;
+		}
+		out.resize(snapshotBytes(d.nbBodies, d.nbStatics, np, ps));
+		SnapshotHeader h = {SNAPSHOT_MAGIC, 1u, d.nbBodies, d.nbStatics, np, ps ? 1u : 0u, {0u, 0u}};
+		uint8_t* o = out.data();
+		memcpy(o, &h, sizeof(h));
+		o += sizeof(h);
+		auto get = [&](const void* src, size_t bytes) -> cudaError_t {
+			const cudaError_t e = bytes ? cudaMemcpy(o, src, bytes, cudaMemcpyDeviceToHost) : cudaSuccess;
+			o += bytes;
+			return e;
+		};
+		const uint32_t b = d.bodyStart, st = d.staticStart, nb = d.nbBodies, ns = d.nbStatics;
+		GBPX_CUDA_TRY(get(bodies.ptr + b, size_t(nb) * sizeof(tgs::RigidBody)));
+		GBPX_CUDA_TRY(get(types.ptr + b, size_t(nb) * 4));
+		GBPX_CUDA_TRY(get(geoms.ptr + b, size_t(nb) * 16));
+		GBPX_CUDA_TRY(get(friction.ptr + b, size_t(nb) * 4));
+		GBPX_CUDA_TRY(get(staticPose.ptr + 7 * size_t(st), size_t(ns) * 28));
+		GBPX_CUDA_TRY(get(staticTypes.ptr + st, size_t(ns) * 4));
+		GBPX_CUDA_TRY(get(staticGeoms.ptr + st, size_t(ns) * 16));
+		if(ps)
+		{
+			GBPX_CUDA_TRY(get(pairs.ptr + d.pairStart, size_t(np) * 4));
+			GBPX_CUDA_TRY(get(manifolds[par].ptr + d.pairStart, size_t(np) * sizeof(np::ManifoldRecord)));
+			GBPX_CUDA_TRY(get(frictionState[par].ptr + d.pairStart, size_t(np) * sizeof(tgs::FrictionState)));
+		}
+		return GBPX_OK;
+	}
+	// The scene of a snapshot into slot `slot` (capacity checked by the caller).
+	int restore(uint32_t slot, const uint8_t* in, size_t bytes)
+	{
+		SnapshotHeader h;
+		if(bytes < sizeof(h)) return GBPX_ERR_INVALID;
+		memcpy(&h, in, sizeof(h));
+		const bool ps = h.pairState != 0;
+		if(h.magic != SNAPSHOT_MAGIC || h.version != 1u || bytes != snapshotBytes(h.nbBodies, h.nbStatics, h.nbPairs, ps) ||
+		   ps != (params.persistent != 0))
+			return GBPX_ERR_INVALID;
+		const world::SceneDesc& d = hScenes[slot];
+		if(ps && h.nbPairs > d.pairCap) return GBPX_ERR_CAPACITY;
+		const uint8_t* p = in + sizeof(h);
+		const uint32_t nb = h.nbBodies, ns = h.nbStatics;
+		const uint8_t* rigid = p;
+		const int* ty = reinterpret_cast<const int*>(rigid + size_t(nb) * sizeof(tgs::RigidBody));
+		const float* ge = reinterpret_cast<const float*>(reinterpret_cast<const uint8_t*>(ty) + size_t(nb) * 4);
+		const float* fr = ge + size_t(nb) * 4;
+		const float* sp7 = fr + nb;
+		const int* sty = reinterpret_cast<const int*>(sp7 + size_t(ns) * 7);
+		const float* sge = reinterpret_cast<const float*>(sty + ns);
+		const uint8_t* pairState = reinterpret_cast<const uint8_t*>(sge + size_t(ns) * 4);
+		int rc = admit(slot, nb, rigid, ty, ge, fr, ns, sp7, sty, sge);
+		if(rc || !ps) return rc;
+		// the pair list and its state into the buffer the slot reads next
+		uint32_t par = 0;
+		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
+		GBPX_CUDA_TRY(cudaMemcpy(&par, sceneParity.ptr + slot, 4, cudaMemcpyDeviceToHost));
+		if(par > 1u) return GBPX_ERR_STATE;
+		const size_t np = h.nbPairs;
+		GBPX_CUDA_TRY(cudaMemcpy(pairs.ptr + d.pairStart, pairState, np * 4, cudaMemcpyHostToDevice));
+		GBPX_CUDA_TRY(cudaMemcpy(manifolds[par].ptr + d.pairStart, pairState + np * 4, np * sizeof(np::ManifoldRecord), cudaMemcpyHostToDevice));
+		GBPX_CUDA_TRY(cudaMemcpy(frictionState[par].ptr + d.pairStart, pairState + np * (4 + sizeof(np::ManifoldRecord)),
+		                         np * sizeof(tgs::FrictionState), cudaMemcpyHostToDevice));
+		const uint32_t np32 = uint32_t(np);
+		GBPX_CUDA_TRY(cudaMemcpy(pairCount.ptr + slot, &np32, 4, cudaMemcpyHostToDevice));
+		return GBPX_OK;
+	}
+
 	void release()
 	{
 		if(stream) cudaStreamSynchronize(stream);
@@ -2994,6 +3084,54 @@ struct Server
 		return GBPX_OK;
 	}
 
+	// Snapshot of a scene that owes no steps (World::snapshot's layout);
+	// *outBytes is its size, and out (capacity bytes) receives it unless null.
+	int snapshotScene(uint32_t id, void* out, uint64_t capacity, uint64_t* outBytes)
+	{
+		if(id >= scenes.size() || !scenes[id].live || !outBytes) return GBPX_ERR_INVALID;
+		const Scene& s = scenes[id];
+		if(s.done != s.requested) return GBPX_ERR_STATE;   // owes steps
+		std::vector<uint8_t> blob;
+		const int rc = lanes[s.lane]->w.snapshot(s.slot, blob);
+		if(rc) return rc;
+		*outBytes = blob.size();
+		if(!out) return GBPX_OK;
+		if(capacity < blob.size()) return GBPX_ERR_CAPACITY;
+		memcpy(out, blob.data(), blob.size());
+		return GBPX_OK;
+	}
+
+	// A snapshot admitted as a new scene (the smallest class that holds its
+	// bodies, statics and pairs), continuing where the snapshot was taken.
+	int restoreScene(const void* snap, uint64_t bytes, uint32_t* outScene)
+	{
+		World::SnapshotHeader h;
+		if(!snap || !outScene || bytes < sizeof(h)) return GBPX_ERR_INVALID;
+		memcpy(&h, snap, sizeof(h));
+		Lane* best = nullptr;
+		for(Lane* L : lanes)
+		{
+			const uint32_t pairCap = L->w.hScenes.empty() ? 0u : L->w.hScenes[0].pairCap;   // every slot of a lane alike
+			if(L->capacity >= h.nbBodies && !L->freeSlots.empty() && h.nbStatics <= L->staticCap && h.nbPairs <= pairCap &&
+			   (!best || L->capacity < best->capacity || (L->capacity == best->capacity && L->freeSlots.size() > best->freeSlots.size())))
+				best = L;
+		}
+		if(!best) return GBPX_ERR_BUDGET;
+		const uint32_t slot = best->freeSlots.back();
+		const int rc = best->w.restore(slot, static_cast<const uint8_t*>(snap), bytes);
+		if(rc) return rc;
+		best->freeSlots.pop_back();
+		const uint32_t id = best->base + slot;
+		Scene& s = scenes[id];
+		s = Scene();
+		s.lane = uint32_t(std::find(lanes.begin(), lanes.end(), best) - lanes.begin());
+		s.slot = slot;
+		s.nbBodies = h.nbBodies;
+		s.live = true;
+		*outScene = id;
+		return GBPX_OK;
+	}
+
 	int retire(uint32_t id)
 	{
 		if(id >= scenes.size() || !scenes[id].live) return GBPX_ERR_INVALID;
@@ -3333,6 +3471,26 @@ GBPX_API int gbpx_server_read_scene(void* sv, uint32_t scene, void* outRigidBodi
 	Server* s = static_cast<Server*>(sv);
 	if(!s || !outRigidBodies) return GBPX_ERR_INVALID;
 	return s->readScene(scene, outRigidBodies);
+}
+
+// Snapshot of a scene that owes no steps: bodies, shapes, statics and (persistent
+// mode) its pair list with each pair's contact manifold and friction patches, in
+// this library's layout.  *outBytes gets the size; out (capacity bytes) the
+// snapshot unless null.
+GBPX_API int gbpx_server_snapshot_scene(void* sv, uint32_t scene, void* out, uint64_t capacity, uint64_t* outBytes)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s) return GBPX_ERR_INVALID;
+	return s->snapshotScene(scene, out, capacity, outBytes);
+}
+
+// A snapshot admitted as a new scene (*outScene), continuing with the results the
+// scene would have had.
+GBPX_API int gbpx_server_restore_scene(void* sv, const void* snapshot, uint64_t bytes, uint32_t* outScene)
+{
+	Server* s = static_cast<Server*>(sv);
+	if(!s) return GBPX_ERR_INVALID;
+	return s->restoreScene(snapshot, bytes, outScene);
 }
 
 // out4: body-steps completed, lane steps completed, live scenes, steps in flight

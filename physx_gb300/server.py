@@ -28,6 +28,9 @@ def _setup():
         L.gbpx_server_clock.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
         L.gbpx_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         L.gbpx_server_read_scene.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
+        L.gbpx_server_snapshot_scene.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                                                 ctypes.POINTER(ctypes.c_uint64)]
+        L.gbpx_server_restore_scene.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32)]
         L.gbpx_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L._server_ready = True
     return L
@@ -111,6 +114,23 @@ class Server:
         out = np.zeros(self._sizes[scene], self._dtype)
         check(self._L.gbpx_server_read_scene(self._h, scene, _p(out)), "gbpx_server_read_scene")
         return out
+
+    def snapshot(self, scene):
+        """The scene's state between steps (bytes): bodies, shapes, statics and its
+        pair list with contact manifolds and friction patches."""
+        n = ctypes.c_uint64(0)
+        check(self._L.gbpx_server_snapshot_scene(self._h, scene, None, 0, ctypes.byref(n)), "gbpx_server_snapshot_scene")
+        out = np.zeros(n.value, np.uint8)
+        check(self._L.gbpx_server_snapshot_scene(self._h, scene, _p(out), n.value, ctypes.byref(n)), "gbpx_server_snapshot_scene")
+        return out
+
+    def restore(self, snap):
+        """Admits a snapshot as a new scene; returns its id."""
+        snap = np.ascontiguousarray(snap, np.uint8)
+        sid = ctypes.c_uint32(0)
+        check(self._L.gbpx_server_restore_scene(self._h, _p(snap), len(snap), ctypes.byref(sid)), "gbpx_server_restore_scene")
+        self._sizes[sid.value] = int(np.frombuffer(snap[8:12].tobytes(), np.uint32)[0])
+        return sid.value
 
     def stats(self):
         out = np.zeros(4, np.uint64)

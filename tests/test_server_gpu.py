@@ -121,3 +121,33 @@ def test_native_poisson_load_retires_and_readmits(cuda_device):
     assert r["retired"] > 0 and r["admitted_after_start"] > 0
     assert r["body_steps_per_s"] > 0 and r["p50_ms"] > 0 and r["p99_ms"] >= r["p50_ms"]
     assert r["lanes"] == 2 * len(r["classes"])
+
+
+def test_snapshot_and_restore_continue_the_scene(cuda_device):
+    """Eviction and re-admission: a scene snapshotted after 12 steps, retired and
+    restored into another slot, then stepped 10 more times, ends with the bytes of
+    the same scene stepped 22 times without interruption; the snapshot carries its
+    pair list with the contact manifolds and friction patches."""
+    from physx_gb300.server import Server
+    scenes = pile_scenes(83, 3, 40, shapes=(0, 2, 3))
+    part = one_scene(scenes, 0)
+    s = Server([64], [4])
+    ref = s.admit(part)
+    a = s.admit(part)
+    s.submit(ref, 22, 1)
+    s.submit(a, 12, 2)
+    s.drain()
+    snap = s.snapshot(a)
+    nb, ns, npairs, pair_state = np.frombuffer(snap[8:24].tobytes(), np.uint32)
+    assert nb == len(part["rigid"]) and ns == 1 and npairs > 0 and pair_state == 1
+    s.retire(a)
+    s.admit(one_scene(scenes, 1))   # takes the freed slot
+    b = s.restore(snap)
+    assert b != a
+    s.submit(b, 10, 3)
+    s.drain()
+    assert s.read_scene(b).tobytes() == s.read_scene(ref).tobytes()
+    from physx_gb300 import GbpxError
+    with pytest.raises(GbpxError):
+        s.restore(snap[:-4])   # a truncated snapshot is refused
+    s.release()
