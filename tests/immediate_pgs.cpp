@@ -4,7 +4,9 @@
 // PxIntegrateSolverBodies) the way the reference's immediate-mode snippet runs
 // its PGS branch (SnippetImmediateMode.cpp:495-503,749,761,886-961,1080-1099),
 // from given contacts; linked against libgbpx_immediate.so.  Used by
-// tests/test_immediate_dropin_gpu.py.
+// tests/test_immediate_dropin_gpu.py.  With the argument "nullalloc" the
+// constraint allocator returns null: PxCreateContactConstraints must return
+// false (exit code 3) without touching the memory.
 //
 // stdin (binary): nbDyn, nbStatic, nbConstraints, nbContacts, batch (u32);
 // PxRigidBodyData[nbDyn]; static poses (PxTransform); pairA, pairB,
@@ -35,8 +37,10 @@ template <typename T> void writeAll(const T* p, size_t n) { if(n) fwrite(p, size
 struct Arena : PxConstraintAllocator
 {
 	std::vector<std::vector<uint8_t>> blocks;
+	bool null = false;
 	uint8_t* reserveConstraintData(const uint32_t size) override
 	{
+		if(null) return nullptr;
 		blocks.emplace_back(size + 16);
 		uint8_t* p = blocks.back().data();
 		return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
@@ -45,8 +49,9 @@ struct Arena : PxConstraintAllocator
 };
 } // namespace
 
-int main()
+int main(int argc, char** argv)
 {
+	const bool nullAlloc = argc > 1 && strcmp(argv[1], "nullalloc") == 0;
 	uint32_t head[5];
 	readAll(head, 5);
 	const uint32_t nbDyn = head[0], nbStatic = head[1], nbCons = head[2], nbContacts = head[3], batch = head[4];
@@ -129,6 +134,7 @@ int main()
 
 	const float invDt = 1.0f / dt;
 	Arena arena;
+	arena.null = nullAlloc;
 	for(uint32_t h = 0; h < nbHeaders; h++)
 	{
 		PxConstraintBatchHeader& header = headers[h];

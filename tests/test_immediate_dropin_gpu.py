@@ -154,6 +154,25 @@ def test_immediate_pgs_frames_match_reference_golden(cuda_device, tmp_path, batc
         assert_pgs_close(ref, got, path)
 
 
+def test_immediate_pgs_null_allocator_fails_cleanly(cuda_device, tmp_path):
+    """A PxConstraintAllocator that returns null: PxCreateContactConstraints returns
+    false (the program reports it and exits 3) instead of writing through it."""
+    import glob
+    import struct
+    from test_oracle_golden import GOLDEN, load_tgs_fixture
+    exe = _build(str(tmp_path), "immediate_pgs")
+    path = sorted(glob.glob(os.path.join(GOLDEN, "pgs_*.npz")))[0]
+    rb, z = load_tgs_fixture(path)
+    n, m, nc, ncts = len(rb), len(z["static_poses"]), len(z["body_a"]), len(z["contacts"])
+    blob = struct.pack("<5I", n, m, nc, ncts, 1) + rb.tobytes() + np.ascontiguousarray(z["static_poses"], np.float32).tobytes()
+    for k in ("body_a", "body_b", "contact_start", "contact_count"):
+        blob += np.ascontiguousarray(z[k], np.uint32).tobytes()
+    blob += np.ascontiguousarray(z["contacts"], np.float32).tobytes() + np.ascontiguousarray(z["material"], np.float32).tobytes()
+    blob += struct.pack("<4f2I", 1.0 / 60.0, 0.0, -9.81, 0.0, 4, 1)
+    r = subprocess.run([exe, "nullalloc"], input=blob, capture_output=True)
+    assert r.returncode == 3 and b"contact prep failed" in r.stderr
+
+
 @pytest.mark.parametrize("seed", [121, 122])
 def test_immediate_persistent_frames_match_oracle(cuda_device, tmp_path, seed):
     """Ten frames of a pile through the drop-in the way the snippet runs its
