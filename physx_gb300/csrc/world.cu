@@ -2289,25 +2289,25 @@ struct World
 	// a slot of enough capacity continues the scene with the same results.
 	struct SnapshotHeader { uint32_t magic, version, nbBodies, nbStatics, nbPairs, pairState, pad[2]; };
 	static constexpr uint32_t SNAPSHOT_MAGIC = 0x53535847u;   // "GXSS"
-	static size_t snapshotBytes(uint32_t nb, uint32_t ns, uint32_t np, bool pairState)
+	static size_t snapshotBytes(uint32_t nb, uint32_t ns, uint32_t nbPairs, bool pairState)
 	{
 		return sizeof(SnapshotHeader) + size_t(nb) * (sizeof(tgs::RigidBody) + 4 + 16 + 4) + size_t(ns) * (28 + 4 + 16) +
-		       (pairState ? size_t(np) * (4 + sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0);
+		       (pairState ? size_t(nbPairs) * (4 + sizeof(np::ManifoldRecord) + sizeof(tgs::FrictionState)) : 0);
 	}
 	int snapshot(uint32_t slot, std::vector<uint8_t>& out)
 	{
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		const world::SceneDesc& d = hScenes[slot];
 		const bool ps = params.persistent != 0;
-		uint32_t np = 0, par = 0;
+		uint32_t nbPairs = 0, par = 0;
 		if(ps)
 		{
-			GBPX_CUDA_TRY(cudaMemcpy(&np, pairCount.ptr + slot, 4, cudaMemcpyDeviceToHost));
+			GBPX_CUDA_TRY(cudaMemcpy(&nbPairs, pairCount.ptr + slot, 4, cudaMemcpyDeviceToHost));
 			GBPX_CUDA_TRY(cudaMemcpy(&par, sceneParity.ptr + slot, 4, cudaMemcpyDeviceToHost));
-			if(np > d.pairCap || par > 1u) return GBPX_ERR_STATE;
+			if(nbPairs > d.pairCap || par > 1u) return GBPX_ERR_STATE;
 		}
-		out.resize(snapshotBytes(d.nbBodies, d.nbStatics, np, ps));
-		SnapshotHeader h = {SNAPSHOT_MAGIC, 1u, d.nbBodies, d.nbStatics, np, ps ? 1u : 0u, {0u, 0u}};
+		out.resize(snapshotBytes(d.nbBodies, d.nbStatics, nbPairs, ps));
+		SnapshotHeader h = {SNAPSHOT_MAGIC, 1u, d.nbBodies, d.nbStatics, nbPairs, ps ? 1u : 0u, {0u, 0u}};
 		uint8_t* o = out.data();
 		memcpy(o, &h, sizeof(h));
 		o += sizeof(h);
@@ -2326,9 +2326,9 @@ struct World
 		GBPX_CUDA_TRY(get(staticGeoms.ptr + st, size_t(ns) * 16));
 		if(ps)
 		{
-			GBPX_CUDA_TRY(get(pairs.ptr + d.pairStart, size_t(np) * 4));
-			GBPX_CUDA_TRY(get(manifolds[par].ptr + d.pairStart, size_t(np) * sizeof(np::ManifoldRecord)));
-			GBPX_CUDA_TRY(get(frictionState[par].ptr + d.pairStart, size_t(np) * sizeof(tgs::FrictionState)));
+			GBPX_CUDA_TRY(get(pairs.ptr + d.pairStart, size_t(nbPairs) * 4));
+			GBPX_CUDA_TRY(get(manifolds[par].ptr + d.pairStart, size_t(nbPairs) * sizeof(np::ManifoldRecord)));
+			GBPX_CUDA_TRY(get(frictionState[par].ptr + d.pairStart, size_t(nbPairs) * sizeof(tgs::FrictionState)));
 		}
 		return GBPX_OK;
 	}
@@ -2361,12 +2361,12 @@ struct World
 		GBPX_CUDA_TRY(cudaStreamSynchronize(stream));
 		GBPX_CUDA_TRY(cudaMemcpy(&par, sceneParity.ptr + slot, 4, cudaMemcpyDeviceToHost));
 		if(par > 1u) return GBPX_ERR_STATE;
-		const size_t np = h.nbPairs;
-		GBPX_CUDA_TRY(cudaMemcpy(pairs.ptr + d.pairStart, pairState, np * 4, cudaMemcpyHostToDevice));
-		GBPX_CUDA_TRY(cudaMemcpy(manifolds[par].ptr + d.pairStart, pairState + np * 4, np * sizeof(np::ManifoldRecord), cudaMemcpyHostToDevice));
-		GBPX_CUDA_TRY(cudaMemcpy(frictionState[par].ptr + d.pairStart, pairState + np * (4 + sizeof(np::ManifoldRecord)),
-		                         np * sizeof(tgs::FrictionState), cudaMemcpyHostToDevice));
-		const uint32_t np32 = uint32_t(np);
+		const size_t pairsIn = h.nbPairs;
+		GBPX_CUDA_TRY(cudaMemcpy(pairs.ptr + d.pairStart, pairState, pairsIn * 4, cudaMemcpyHostToDevice));
+		GBPX_CUDA_TRY(cudaMemcpy(manifolds[par].ptr + d.pairStart, pairState + pairsIn * 4, pairsIn * sizeof(np::ManifoldRecord), cudaMemcpyHostToDevice));
+		GBPX_CUDA_TRY(cudaMemcpy(frictionState[par].ptr + d.pairStart, pairState + pairsIn * (4 + sizeof(np::ManifoldRecord)),
+		                         pairsIn * sizeof(tgs::FrictionState), cudaMemcpyHostToDevice));
+		const uint32_t np32 = uint32_t(pairsIn);
 		GBPX_CUDA_TRY(cudaMemcpy(pairCount.ptr + slot, &np32, 4, cudaMemcpyHostToDevice));
 		return GBPX_OK;
 	}
