@@ -78,8 +78,33 @@ class World:
         check(L.gbpx_world_create(len(k[0]), _p(k[0]), _p(k[1]), _p(k[2]), _p(k[3]), _p(k[4]), _p(k[5]), _p(k[6]), _p(k[7]), _p(k[8]),
                                   _p(pv), _p(it), pairs_per_body, ctypes.byref(h)), "gbpx_world_create")
         self._h, self._L = h, L
+        self.pairs_per_body = pairs_per_body
         self.nb_bodies = len(k[2])
         self.rigid_dtype = k[2].dtype
+
+    def step_checked(self, n=1, max_pairs_per_body=128):
+        """n steps, one at a time; a step after which a scene reports that its pair
+        slots overflowed (status bit 1) is taken again, from the bodies before it, in
+        a world with twice the pair slots per body (pair history restarts there),
+        until it fits or max_pairs_per_body is reached (then GbpxError).  Returns the
+        pair slots per body in use."""
+        from . import GbpxError
+        for _ in range(n):
+            before = self.get_bodies()
+            self.step(1, graph=False)
+            while (self.status() & 1).any():
+                if self.pairs_per_body * 2 > max_pairs_per_body:
+                    raise GbpxError(-3, "World.step_checked: pair slots")
+                k = self._keep
+                h = ctypes.c_void_p()
+                check(self._L.gbpx_world_create(len(k[0]), _p(k[0]), _p(k[1]), _p(before), _p(k[3]), _p(k[4]), _p(k[5]), _p(k[6]),
+                                                _p(k[7]), _p(k[8]), _p(k[9]), _p(k[10]), self.pairs_per_body * 2, ctypes.byref(h)),
+                      "gbpx_world_create")
+                self._L.gbpx_world_release(self._h)
+                self._h = h
+                self.pairs_per_body *= 2
+                self.step(1, graph=False)
+        return self.pairs_per_body
 
     def release(self):
         if self._h:

@@ -78,6 +78,21 @@ def test_world_reports_pair_overflow(cuda_device):
     w.release()
 
 
+def test_world_step_checked_retries_with_more_pair_slots(cuda_device):
+    """Host retry with a larger arena: a step that overflows the pair slots is taken
+    again from the bodies before it in a world with twice the slots per body until
+    it fits; the result equals a world created with those slots."""
+    scenes = pile_scenes(73, 2, 60, shapes=(0,), spread=1.0)
+    w = _world(scenes, pairs_per_body=1)
+    ppb = w.step_checked(2)
+    assert ppb >= 16 and not w.status().any()
+    ref = _world(scenes, pairs_per_body=ppb)
+    ref.step(2, graph=False)
+    assert w.get_bodies().tobytes() == ref.get_bodies().tobytes()
+    w.release()
+    ref.release()
+
+
 def test_world_rejects_bad_input(cuda_device):
     from physx_gb300 import GbpxError
     scenes = pile_scenes(74, 1, 8, shapes=(0,))
