@@ -532,6 +532,7 @@ __global__ void __launch_bounds__(128, (TA == 3 && TB == 3) ? 4 : 5) narrowphase
 		if(lane == 0) base = atomicAdd(&w.workCounter[WC_NP_TAKEN + KIND], 32u);
 		base = __shfl_sync(0xffffffffu, base, 0);
 		if(base >= count) break;
+		// lanes past the end wait at the next iteration's shuffle for the others
 		if(base + lane >= count) continue;
 		const uint32_t q = sorted ? count - 1u - (base + lane) : base + lane;
 		const uint32_t slot = queue[q];
